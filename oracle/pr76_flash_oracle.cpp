@@ -1,0 +1,1752 @@
+// PR76 two-phase PT flash -- CPU oracle (test infrastructure, not product code).
+//
+// This file restates, in plain sequential C++20, the reference algorithm of
+// MPMC_HNU's PR76 PT flash and its implicit sensitivity so that the GPU kernels
+// can be checked against it on the GPU host, where the reference sources are
+// not available.  It is only ever called by the tests, by the smoke check and
+// by the CPU-baseline leg of the benchmark; the shipped library never links it.
+//
+// Parity is pinned: tests/golden holds fixtures produced by compiling the
+// reference headers themselves (oracle/ref_harness.cpp, built into oracle/_ref
+// by oracle/Makefile) together with the reference's own published golden
+// vectors, and tests/test_oracle_golden.py checks this restatement against both.
+//
+// Every numbered step cites the reference file and line it restates
+// (paths relative to the MPMC_HNU project root).  Exceptions of the reference
+// are replaced by status codes with the same meaning.  Floating-point
+// operations keep the reference's evaluation order; build with
+// -ffp-contract=off so x86-64 and aarch64 hosts round identically.
+
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstddef>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <thread>
+#include <vector>
+
+namespace oracle {
+
+constexpr double kEps = std::numeric_limits<double>::epsilon();
+constexpr double kR = 8.31446261815324;  // modules/thermodynamics/.../pr76_pure.hpp:115-117
+constexpr double kNaN = std::numeric_limits<double>::quiet_NaN();
+
+// ---------------------------------------------------------------------------
+// Error codes standing in for the reference exception/issue classes.
+// modules/flash/include/mpmc/flash/pt_stability.hpp:23-26
+enum Issue {
+    kOk = 0,
+    kRootTopology = 1,        // near_multiple
+    kRootIterationLimit = 2,  // iteration_limit
+    kRootRange = 3,           // unrepresentable root / range_error
+    kIllConditionedRoot = 4,
+    kNoAdmissibleBranch = 5,
+    kNonfinite = 6,
+    kDomain = 7,              // std::domain_error (not caught by the flash)
+};
+
+// Kahan step, pt_stability.hpp:99-104
+inline void kahan_add(double term, double& sum, double& c) {
+    const double inc = term - c;
+    const double next = sum + inc;
+    c = (next - sum) - inc;
+    sum = next;
+}
+inline double kahan_sum(const double* x, int n) {
+    double s = 0, c = 0;
+    for (int i = 0; i < n; ++i) kahan_add(x[i], s, c);
+    return s;
+}
+inline double midpoint(double a, double b) { return (a + b) / 2; }
+
+// ---------------------------------------------------------------------------
+// Forward-mode number with one tangent direction; used only on the
+// sensitivity path (the reference uses Dual<double,4> blocks,
+// modules/ad/include/mpmc/ad/dual.hpp:80; one direction per pass gives the
+// same first-order derivatives).
+struct D1 {
+    double v = 0, d = 0;
+    D1() = default;
+    explicit D1(double value, double tangent = 0) : v(value), d(tangent) {}
+};
+inline D1 operator+(D1 a, D1 b) { return D1(a.v + b.v, a.d + b.d); }
+inline D1 operator-(D1 a, D1 b) { return D1(a.v - b.v, a.d - b.d); }
+inline D1 operator*(D1 a, D1 b) { return D1(a.v * b.v, a.d * b.v + a.v * b.d); }
+inline D1 operator/(D1 a, D1 b) {
+    const double q = a.v / b.v;
+    return D1(q, (a.d - q * b.d) / b.v);
+}
+inline D1 operator+(D1 a, double b) { return D1(a.v + b, a.d); }
+inline D1 operator+(double a, D1 b) { return D1(a + b.v, b.d); }
+inline D1 operator-(D1 a, double b) { return D1(a.v - b, a.d); }
+inline D1 operator-(double a, D1 b) { return D1(a - b.v, -b.d); }
+inline D1 operator*(D1 a, double b) { return D1(a.v * b, a.d * b); }
+inline D1 operator*(double a, D1 b) { return D1(a * b.v, a * b.d); }
+inline D1 operator/(D1 a, double b) { return D1(a.v / b, a.d / b); }
+inline D1 operator/(double a, D1 b) {
+    const double q = a / b.v;
+    return D1(q, -q * b.d / b.v);
+}
+inline D1 sqrt(D1 a) {
+    const double s = std::sqrt(a.v);
+    return D1(s, a.d / (2 * s));
+}
+inline D1 log(D1 a) { return D1(std::log(a.v), a.d / a.v); }
+inline D1 log1p(D1 a) { return D1(std::log1p(a.v), a.d / (1 + a.v)); }
+inline double val(double a) { return a; }
+inline double val(const D1& a) { return a.v; }
+inline bool finite(double a) { return std::isfinite(a); }
+inline bool finite(const D1& a) { return std::isfinite(a.v) && std::isfinite(a.d); }
+using std::log;
+using std::log1p;
+using std::sqrt;
+
+// ---------------------------------------------------------------------------
+// Prepared mixture: pr76_pure.hpp:181-199 and pr76_mixture.hpp:229-251.
+struct Model {
+    int n = 0;
+    std::vector<double> tc, sqrt_tc, kappa, ac, b, factor;  // factor = 1 - kij (row-major)
+};
+
+inline Model make_model(int n, const double* tc, const double* pc, const double* omega,
+                        const double* kij) {
+    Model m;
+    m.n = n;
+    m.tc.assign(tc, tc + n);
+    m.sqrt_tc.resize(n);
+    m.kappa.resize(n);
+    m.ac.resize(n);
+    m.b.resize(n);
+    for (int i = 0; i < n; ++i) {
+        m.sqrt_tc[i] = std::sqrt(tc[i]);
+        // pr76_pure.hpp:189-190, Horner order
+        m.kappa[i] = 0.37464 + omega[i] * (1.54226 - 0.26992 * omega[i]);
+        const double rtc = kR * tc[i];
+        m.ac[i] = (0.45724 * rtc) * (rtc / pc[i]);  // :193
+        m.b[i] = (0.07780 * rtc) / pc[i];           // :194
+    }
+    m.factor.resize(static_cast<size_t>(n) * n);
+    for (int k = 0; k < n * n; ++k) m.factor[k] = 1.0 - kij[k];
+    return m;
+}
+
+// Per-temperature constants.  pr76_mixture.hpp:172-204 recomputes these on
+// every call; they depend on T only, so computing them once per cell gives
+// bit-identical values.
+struct TempCache {
+    std::vector<double> a, root, aij;  // a_i(T), sqrt(a_i), (root_i*f_ij)*root_j
+};
+inline bool make_temp_cache(const Model& m, double t, TempCache& c) {
+    const int n = m.n;
+    c.a.resize(n);
+    c.root.resize(n);
+    c.aij.assign(static_cast<size_t>(n) * n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        // pr76_pure.hpp:153-163
+        const double reduced_root = std::sqrt(t) / m.sqrt_tc[i];
+        const double bracket = 1.0 + m.kappa[i] * (1.0 - reduced_root);
+        const double attraction = (bracket * m.ac[i]) * bracket;
+        if (!std::isfinite(attraction) || (attraction == 0 && bracket != 0)) return false;
+        c.a[i] = attraction;
+        if (n > 1) {
+            if (!(attraction > 0)) return false;  // pr76_mixture.hpp:180-182
+            c.root[i] = std::sqrt(attraction);
+        }
+    }
+    for (int i = 0; i < n; ++i)
+        for (int j = i + 1; j < n; ++j)
+            c.aij[i * n + j] = (c.root[i] * m.factor[i * n + j]) * c.root[j];  // :198-199
+    return true;
+}
+
+// Mixing with row sums, pr76_mixture.hpp:170-218 (WithSums=true order).
+inline bool mix(const Model& m, const TempCache& c, const double* x, double& amix, double& bmix,
+                double* sums) {
+    const int n = m.n;
+    double attraction = 0, covolume = 0;
+    for (int i = 0; i < n; ++i) {
+        attraction += (x[i] * c.a[i]) * x[i];
+        covolume += x[i] * m.b[i];
+        sums[i] = x[i] * c.a[i];
+    }
+    for (int i = 0; i < n; ++i) {
+        for (int j = i + 1; j < n; ++j) {
+            const double cross = ((x[i] * c.root[i]) * (x[j] * c.root[j])) * m.factor[i * n + j];
+            attraction += cross;
+            attraction += cross;
+            const double aij = c.aij[i * n + j];
+            sums[i] += x[j] * aij;
+            sums[j] += x[i] * aij;
+        }
+    }
+    amix = attraction;
+    bmix = covolume;
+    if (!std::isfinite(attraction) || !std::isfinite(covolume) || !(covolume > 0)) return false;
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(sums[i])) return false;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Cubic roots, modules/thermodynamics/include/mpmc/thermodynamics/pr76_roots.hpp
+enum RootStatus { kRootSuccess, kRootNearMultiple, kRootIterLimit, kRootUnrepresentable };
+struct Root {
+    double z, free_volume, slope_ratio;
+    bool derivative_valid;
+    int slope_sign;
+};
+struct RootSet {
+    Root roots[3];
+    int count = 0;
+    double scale = 1;
+    RootStatus status = kRootUnrepresentable;
+    int iterations = 0;  // total bisection steps (work counter)
+};
+struct Cubic {
+    double c2, c1, c0;
+};
+inline Cubic cubic_coefficients(double a, double b, double scale) {  // :50-58
+    const double bs = b / scale;
+    const double inv = 1.0 / scale;
+    return {4.0 * bs - inv, (a / scale) / scale + 2.0 * bs * bs - 4.0 * bs * inv,
+            ((-2.0 * bs) * bs) * inv};
+}
+inline double poly(double y, const Cubic& c) {  // :60-63
+    return std::fma(std::fma(y + c.c2, y, c.c1), y, c.c0);
+}
+inline double poly_scale(double y, const Cubic& c) {  // :64-68
+    return ((std::abs(y) + std::abs(c.c2)) * std::abs(y) + std::abs(c.c1)) * std::abs(y) +
+           std::abs(c.c0);
+}
+
+inline RootSet solve_roots(double a, double b) {  // :77-173
+    RootSet r;
+    if (!std::isfinite(a) || !std::isfinite(b) || !(b > 0)) return r;
+    r.scale = std::max({1.0, b, std::sqrt(std::abs(a))});
+    const Cubic c = cubic_coefficients(a, b, r.scale);
+    if (!std::isfinite(c.c2) || !std::isfinite(c.c1) || !std::isfinite(c.c0) || !(c.c0 < 0))
+        return r;
+    const double upper = 1.0 + std::max({std::abs(c.c2), std::abs(c.c1), std::abs(c.c0)});
+    double endpoints[4] = {0, 0, 0, 0};
+    int endpoint_count = 1;
+    const double disc = std::fma(c.c2, c.c2, -3.0 * c.c1);
+    if (disc > 0) {  // :95-112
+        const double q = -c.c2 - std::copysign(std::sqrt(disc), c.c2);
+        double st[2] = {q / 3.0, c.c1 / q};
+        if (st[1] < st[0]) std::swap(st[0], st[1]);
+        for (double point : st) {
+            if (point > 0 && point < upper) {
+                const double value = poly(point, c);
+                const double magnitude = poly_scale(point, c);
+                if (!std::isfinite(value) || !(magnitude > 0)) return r;
+                if (std::abs(value) <= 64.0 * kEps * magnitude) {
+                    r.status = kRootNearMultiple;
+                    return r;
+                }
+                endpoints[endpoint_count++] = point;
+            }
+        }
+    }
+    endpoints[endpoint_count++] = upper;
+    for (int interval = 1; interval < endpoint_count; ++interval) {  // :114-170
+        double left = endpoints[interval - 1], right = endpoints[interval];
+        double fl = poly(left, c);
+        const double fr = poly(right, c);
+        if (!std::isfinite(fl) || !std::isfinite(fr)) return r;
+        if (std::signbit(fl) == std::signbit(fr)) continue;
+        double y = 0;
+        bool converged = false;
+        int it = 0;
+        for (; it < 2048; ++it) {
+            y = midpoint(left, right);
+            const double fy = poly(y, c);
+            if (fy == 0 || y == left || y == right ||
+                right - left <= 4.0 * kEps * std::max(y, std::numeric_limits<double>::min())) {
+                converged = true;
+                break;
+            }
+            if (std::signbit(fy) == std::signbit(fl)) {
+                left = y;
+                fl = fy;
+            } else {
+                right = y;
+            }
+        }
+        r.iterations += it + 1;
+        if (!converged) {
+            r.count = 0;
+            r.status = kRootIterLimit;
+            return r;
+        }
+        const double xv = y * r.scale;
+        const double z = xv + b;
+        const double magnitude = poly_scale(y, c);
+        const double residual = std::abs(poly(y, c)) / magnitude;
+        const double dh = std::fma(3.0 * y + 2.0 * c.c2, y, c.c1);
+        const double dh_scale = 3.0 * y * y + 2.0 * std::abs(c.c2) * y + std::abs(c.c1);
+        const double slope_ratio = dh_scale > 0 ? std::abs(dh) / dh_scale : 0.0;
+        const double bz = b / z;
+        const double repulsion = 1.0 / xv;
+        const double attraction = ((a / z) / z) / (1.0 + 2.0 * bz - bz * bz);
+        const double pressure_residual = std::abs(repulsion - attraction - 1.0) /
+                                         (1.0 + std::abs(repulsion) + std::abs(attraction));
+        if (!std::isfinite(z) || !(z > b) || !std::isfinite(residual) ||
+            !std::isfinite(pressure_residual) || residual > 128.0 * kEps ||
+            pressure_residual > 512.0 * kEps || r.count == 3) {
+            r.count = 0;
+            r.status = kRootUnrepresentable;
+            return r;
+        }
+        if (r.count != 0 && !(z > r.roots[r.count - 1].z)) {
+            r.count = 0;
+            r.status = kRootNearMultiple;
+            return r;
+        }
+        r.roots[r.count++] = {z, xv, slope_ratio, slope_ratio > 8.0 * std::sqrt(kEps),
+                              dh > 0 ? 1 : (dh < 0 ? -1 : 0)};
+    }
+    r.status = r.count > 0 ? kRootSuccess : kRootUnrepresentable;
+    return r;
+}
+
+inline Issue root_issue(RootStatus s) {  // pr76_stability.hpp:42-53
+    switch (s) {
+    case kRootSuccess: return kOk;
+    case kRootNearMultiple: return kRootTopology;
+    case kRootIterLimit: return kRootIterationLimit;
+    default: return kRootRange;
+    }
+}
+
+// log1p(u)/u with the series branch, pr76_phase.hpp:67-79
+template <class Num>
+inline Num log1p_over_x(const Num& u) {
+    if (std::abs(val(u)) <= 1.0 / 8.0) {
+        constexpr int degree = std::numeric_limits<double>::digits / 3 + 2;
+        Num value{(degree % 2 == 0 ? 1.0 : -1.0) / static_cast<double>(degree + 1)};
+        for (int k = degree - 1; k >= 0; --k)
+            value = (k % 2 == 0 ? 1.0 : -1.0) / static_cast<double>(k + 1) + u * value;
+        return value;
+    }
+    return log1p(u) / u;
+}
+
+// Reduced coefficients A, B, pr76_phase.hpp:175-191
+inline bool coefficients(double p, double t, double amix, double bmix, double& A, double& B) {
+    const double rt = kR * t;
+    if (!std::isfinite(rt) || !(rt > 0)) return false;
+    const double prt = p / rt;
+    A = (amix / rt) * prt;
+    B = bmix * prt;
+    if (!std::isfinite(A) || !std::isfinite(B) || !(B > 0) || (A == 0 && amix != 0)) return false;
+    return true;
+}
+
+// ln(phi) of a resolved root, pr76_phase.hpp:223-253 (plain double path).
+inline bool ln_phi_of_root(const Model& m, double p, double t, double amix, double bmix,
+                           const double* sums, double A, double B, const Root& root,
+                           double* ln_phi) {
+    const double free_volume = root.free_volume;
+    const double z = free_volume + B;
+    const double sqrt2 = std::sqrt(2.0);
+    const double denominator = free_volume + (2.0 - sqrt2) * B;
+    const double u = (2.0 * sqrt2) * (B / denominator);
+    const double log_factor = log1p_over_x(u) / denominator;
+    double z_minus_one = z - 1.0;
+    double log_free = std::log(free_volume);
+    if (std::abs(z_minus_one) < 0.25 && B < 0.125) {
+        const double bz = B / z;
+        z_minus_one = B / free_volume - (A / z) / (1.0 + 2.0 * bz - bz * bz);
+        log_free = std::log1p(z_minus_one - B);
+    }
+    const double rt = kR * t;
+    const double prt = p / rt;
+    for (int i = 0; i < m.n; ++i) {
+        const double ratio = m.b[i] / bmix;
+        const double coefficient = ((2.0 * sums[i] - amix * ratio) / rt) * prt;
+        ln_phi[i] = ratio * z_minus_one - log_free - coefficient * log_factor;
+        if (!std::isfinite(ln_phi[i])) return false;
+    }
+    return std::isfinite(z);
+}
+
+// ---------------------------------------------------------------------------
+// Scratch for one cell.
+struct Work {
+    int n = 0;
+    TempCache tc;
+    std::vector<double> sums;
+    std::vector<double> lnphi_tmp[3];
+    long long evaluations = 0;     // provider calls
+    long long root_bisections = 0; // cubic bisection steps
+    long long rr_iterations = 0;
+    void init(int nn) {
+        n = nn;
+        sums.resize(n);
+        for (auto& v : lnphi_tmp) v.resize(n);
+    }
+};
+
+struct StabilityPhase {
+    std::vector<double> ln_phi;
+    int branch = 0;
+    bool smooth = true;
+    double z = kNaN;  // Z of the selected branch (diagnostic output)
+};
+
+// Stability provider, modules/flash/include/mpmc/flash/pr76_stability.hpp:36-119
+inline Issue stability_provider(const Model& m, Work& w, double p, double t, const double* x,
+                                StabilityPhase& out) {
+    const int n = m.n;
+    ++w.evaluations;
+    double amix, bmix, A, B;
+    if (!mix(m, w.tc, x, amix, bmix, w.sums.data())) return kRootRange;
+    if (!coefficients(p, t, amix, bmix, A, B)) return kRootRange;
+    const RootSet roots = solve_roots(A, B);
+    w.root_bisections += roots.iterations;
+    if (roots.status != kRootSuccess) return root_issue(roots.status);
+    int cand[3], ncand = 0;
+    for (int k = 0; k < roots.count; ++k) {
+        if (roots.roots[k].slope_sign <= 0) continue;  // :58
+        if (!ln_phi_of_root(m, p, t, amix, bmix, w.sums.data(), A, B, roots.roots[k],
+                            w.lnphi_tmp[ncand].data()))
+            return kRootRange;
+        cand[ncand++] = k;
+    }
+    if (ncand == 0) return kNoAdmissibleBranch;
+    auto difference = [&](int a, int b, double& value) {  // :67-78
+        double v = 0, c = 0;
+        for (int i = 0; i < n; ++i)
+            kahan_add(x[i] * (w.lnphi_tmp[a][i] - w.lnphi_tmp[b][i]), v, c);
+        value = v;
+        return std::isfinite(v);
+    };
+    int best = 0;
+    for (int k = 1; k < ncand; ++k) {
+        double d;
+        if (!difference(k, best, d)) return kNonfinite;
+        if (d < 0) best = k;
+    }
+    if (!roots.roots[cand[best]].derivative_valid) return kIllConditionedRoot;
+    bool smooth = true;
+    for (int k = 0; k < ncand; ++k) {  // :89-104
+        if (k == best) continue;
+        double magnitude = 1;
+        for (int i = 0; i < n; ++i)
+            magnitude += x[i] * (std::abs(w.lnphi_tmp[k][i]) + std::abs(w.lnphi_tmp[best][i]));
+        if (!std::isfinite(magnitude)) return kNonfinite;
+        double d;
+        if (!difference(k, best, d)) return kNonfinite;
+        if (std::abs(d) <= 256.0 * kEps * magnitude) smooth = false;
+    }
+    out.ln_phi.assign(w.lnphi_tmp[best].begin(), w.lnphi_tmp[best].end());
+    out.branch = cand[best];
+    out.smooth = smooth;
+    out.z = roots.roots[cand[best]].z;
+    return kOk;
+}
+
+struct SplitPhase {
+    std::vector<double> ln_phi;
+    int branch = 0;
+    double z = 0;
+};
+
+// Role provider, modules/flash/include/mpmc/flash/pr76_split.hpp:38-84 plus
+// split_check_phase, pt_split.hpp:197-203.
+inline Issue role_provider(const Model& m, Work& w, double p, double t, const double* x,
+                           bool vapor, SplitPhase& out) {
+    ++w.evaluations;
+    double amix, bmix, A, B;
+    if (!mix(m, w.tc, x, amix, bmix, w.sums.data())) return kRootRange;
+    if (!coefficients(p, t, amix, bmix, A, B)) return kRootRange;
+    const RootSet roots = solve_roots(A, B);
+    w.root_bisections += roots.iterations;
+    if (roots.status != kRootSuccess) return root_issue(roots.status);
+    int selected = -1;
+    for (int k = 0; k < roots.count; ++k) {
+        if (roots.roots[k].slope_sign <= 0) continue;
+        selected = k;
+        if (!vapor) break;
+    }
+    if (selected < 0) return kNoAdmissibleBranch;
+    if (!roots.roots[selected].derivative_valid) return kIllConditionedRoot;
+    out.ln_phi.resize(m.n);
+    if (!ln_phi_of_root(m, p, t, amix, bmix, w.sums.data(), A, B, roots.roots[selected],
+                        out.ln_phi.data()))
+        return kRootRange;
+    out.branch = selected;
+    out.z = roots.roots[selected].z;
+    if (!std::isfinite(out.z) || out.z <= 0) return kIllConditionedRoot;
+    return kOk;
+}
+
+// ---------------------------------------------------------------------------
+// TPD stability, modules/flash/include/mpmc/flash/pt_stability.hpp
+struct StabilityOptions {  // :44-56
+    double tpd_tolerance = 1e-10;
+    double stationarity_tolerance = 1e-8;
+    double armijo = 1e-4;
+    double log_step_limit = 4.0;
+    int max_iterations = 512;
+    int max_backtracks = 32;
+    long long max_evaluations = 100000;
+};
+enum TrialStatus {
+    kNegativeTpd, kStationary, kIterationLimit, kEvaluationLimit, kLineSearchFailed,
+    kPropertyFailure, kNonsmooth, kUnrepresentableComposition
+};
+struct TpdPoint {
+    std::vector<double> w, residual;
+    double value = 0, guard = 0, stationarity = 0;
+    bool smooth = true;
+};
+struct Trial {
+    std::vector<double> initial;
+    TpdPoint point;
+    bool has_point = false;
+    TrialStatus status = kEvaluationLimit;
+    int iterations = 0;
+};
+enum StabilityStatus { kUnstable, kNoInstabilityFound, kStabilityIndeterminate };
+struct StabilityResult {
+    StabilityStatus status = kStabilityIndeterminate;
+    std::vector<double> feed;
+    StabilityPhase reference;
+    bool has_reference = false;
+    std::vector<Trial> trials;
+    long long evaluations = 0;
+    int trial_iterations = 0;
+};
+
+// Composition check, pt_stability.hpp:110-122
+inline bool check_composition(const double* x, int n, double& sum) {
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(x[i]) || x[i] < 0 || x[i] > 1) return false;
+    sum = kahan_sum(x, n);
+    return std::abs(sum - 1.0) <= 64.0 * kEps;
+}
+
+inline bool stability_negative(const TpdPoint& p, const StabilityOptions& o) {  // :150-152
+    return p.value < -o.tpd_tolerance - p.guard;
+}
+inline bool stability_accept(const TpdPoint& point, const TpdPoint& next, double predicted,
+                             double armijo, double relative_step) {  // :157-171
+    const double guard = point.guard + next.guard;
+    if (predicted <= guard)
+        return next.value <= point.value + guard && relative_step > 0 &&
+               next.stationarity < point.stationarity;
+    return next.value <= point.value - armijo * predicted;
+}
+
+// tangent_plane_distance, pt_stability.hpp:178-220
+inline Issue tpd(const double* w, const std::vector<double>& z, const std::vector<double>& lnphi_w,
+                 const std::vector<double>& lnphi_ref, int n, TpdPoint& out) {
+    double sum;
+    if (!check_composition(w, n, sum)) return kDomain;
+    out.w.assign(w, w + n);
+    out.residual.assign(n, 0.0);
+    out.value = 0;
+    out.stationarity = 0;
+    double correction = 0, magnitude = 1, mc = 0;
+    bool boundary = false;
+    for (int i = 0; i < n; ++i) {
+        if (z[i] == 0) {
+            if (w[i] != 0) return kDomain;
+            continue;
+        }
+        if (w[i] == 0) {
+            boundary = true;
+            continue;
+        }
+        const double lw = std::log(w[i]), lz = std::log(z[i]);
+        const double log_ratio =
+            std::abs(w[i] - z[i]) < 0.5 * z[i] ? std::log1p((w[i] - z[i]) / z[i]) : lw - lz;
+        const double q = log_ratio + (lnphi_w[i] - lnphi_ref[i]);
+        out.residual[i] = q;
+        kahan_add(w[i] * q, out.value, correction);
+        kahan_add(w[i] * (std::abs(lw) + std::abs(lz) + std::abs(lnphi_w[i]) +
+                          std::abs(lnphi_ref[i])),
+                  magnitude, mc);
+    }
+    const double mean = out.value / sum;
+    for (int i = 0; i < n; ++i) {
+        if (z[i] == 0) continue;
+        out.residual[i] = w[i] == 0 ? -std::numeric_limits<double>::infinity() : out.residual[i] - mean;
+        out.stationarity = std::max(out.stationarity, std::abs(out.residual[i]));
+    }
+    out.guard = 256.0 * kEps * magnitude;
+    if (!std::isfinite(out.value) || !std::isfinite(out.guard) ||
+        (!boundary && !std::isfinite(out.stationarity)))
+        return kNonfinite;
+    return kOk;
+}
+
+// test_pt_stability_impl, pt_stability.hpp:228-461.  `imposed` empty selects
+// the feed-phase reference; otherwise it is the common log activity.
+inline bool stability_test(const Model& m, Work& wk, double p, double t, const std::vector<double>& feed_in,
+                           const StabilityOptions& o, const std::vector<std::vector<double>>& extra,
+                           const std::vector<double>& imposed, StabilityResult& res) {
+    const int n = m.n;
+    double input_sum;
+    if (!check_composition(feed_in.data(), n, input_sum)) return false;
+    int active = 0;
+    for (double v : feed_in) active += v > 0;
+    for (const auto& s : extra) {  // :263-272, a domain_error in the reference
+        double ssum;
+        if (static_cast<int>(s.size()) != n || !check_composition(s.data(), n, ssum)) return false;
+        for (int i = 0; i < n; ++i)
+            if ((feed_in[i] == 0 && s[i] != 0) || (feed_in[i] > 0 && s[i] == 0)) return false;
+    }
+    res = StabilityResult();
+    res.feed.resize(n);
+    for (int i = 0; i < n; ++i) res.feed[i] = feed_in[i] / input_sum;
+    for (int i = 0; i < n; ++i)
+        if (feed_in[i] > 0 && res.feed[i] == 0) return true;  // indeterminate, :280-285
+    auto add_start = [&](std::vector<double> s) {
+        const double sum = kahan_sum(s.data(), n);
+        for (double& v : s) v /= sum;
+        Trial tr;
+        tr.initial = std::move(s);
+        res.trials.push_back(std::move(tr));
+    };
+    add_start(res.feed);  // :294-310
+    if (active > 1) {
+        std::vector<double> uniform(n, 0.0);
+        for (int i = 0; i < n; ++i)
+            if (res.feed[i] > 0) uniform[i] = 1.0 / static_cast<double>(active);
+        add_start(uniform);
+        for (int i = 0; i < n; ++i) {
+            if (res.feed[i] == 0) continue;
+            std::vector<double> s = res.feed;
+            for (double& v : s) v *= 0.1;
+            s[i] += 0.9;
+            add_start(s);
+        }
+    }
+    for (const auto& s : extra) add_start(s);
+    StabilityPhase imposed_phase;
+    const long long eval0 = wk.evaluations;
+    if (imposed.empty()) {  // :313-335
+        Issue is = stability_provider(m, wk, p, t, res.feed.data(), res.reference);
+        if (is == kDomain) return false;
+        if (is != kOk) {
+            for (auto& tr : res.trials) tr.status = kPropertyFailure;
+            res.evaluations = wk.evaluations - eval0;
+            return true;
+        }
+        res.has_reference = true;
+    } else {
+        imposed_phase.ln_phi.resize(n);
+        for (int i = 0; i < n; ++i)
+            imposed_phase.ln_phi[i] = res.feed[i] > 0 ? imposed[i] - std::log(res.feed[i]) : 0.0;
+        for (double v : imposed_phase.ln_phi)
+            if (!std::isfinite(v)) {
+                for (auto& tr : res.trials) tr.status = kPropertyFailure;
+                return true;
+            }
+    }
+    const std::vector<double>& ref = imposed.empty() ? res.reference.ln_phi : imposed_phase.ln_phi;
+    bool negative_found = false, all_stationary = true;
+    StabilityPhase phase;
+    std::vector<double> direction(n), candidate(n);
+    for (auto& tr : res.trials) {  // :343-457
+        auto evaluate = [&](const double* w, TpdPoint& out) -> Issue {
+            Issue is = stability_provider(m, wk, p, t, w, phase);
+            if (is != kOk) return is;
+            for (double v : phase.ln_phi)
+                if (!std::isfinite(v)) return kNonfinite;
+            is = tpd(w, res.feed, phase.ln_phi, ref, n, out);
+            out.smooth = phase.smooth;
+            return is;
+        };
+        bool support_lost = false;
+        for (int i = 0; i < n; ++i) support_lost = support_lost || (res.feed[i] > 0 && tr.initial[i] == 0);
+        if (support_lost) {
+            tr.status = kUnrepresentableComposition;
+            all_stationary = false;
+            continue;
+        }
+        if (wk.evaluations - eval0 >= o.max_evaluations) {
+            tr.status = kEvaluationLimit;
+            all_stationary = false;
+            continue;
+        }
+        {
+            Issue is = evaluate(tr.initial.data(), tr.point);
+            if (is == kDomain) return false;
+            if (is != kOk) {
+                tr.status = kPropertyFailure;
+                all_stationary = false;
+                continue;
+            }
+            tr.has_point = true;
+        }
+        TpdPoint next;
+        for (;;) {
+            const TpdPoint& point = tr.point;
+            if (stability_negative(point, o)) {
+                tr.status = kNegativeTpd;
+                negative_found = true;
+                break;
+            }
+            if (!point.smooth) {
+                tr.status = kNonsmooth;
+                break;
+            }
+            if (point.stationarity <= o.stationarity_tolerance) {
+                tr.status = kStationary;
+                break;
+            }
+            if (tr.iterations >= o.max_iterations) {
+                tr.status = kIterationLimit;
+                break;
+            }
+            const double scale = std::max(1.0, point.stationarity / o.log_step_limit);
+            double slope = 0, correction = 0;
+            for (int i = 0; i < n; ++i) {
+                direction[i] = 0;
+                if (res.feed[i] == 0) continue;
+                direction[i] = -point.residual[i] / scale;
+                kahan_add((point.w[i] * point.residual[i]) * direction[i], slope, correction);
+            }
+            if (!std::isfinite(slope) || !(slope < 0)) {
+                tr.status = kLineSearchFailed;
+                break;
+            }
+            bool accepted = false;
+            double alpha = 1;
+            tr.status = kLineSearchFailed;
+            for (int bt = 0; bt < o.max_backtracks; ++bt, alpha *= 0.5) {
+                double largest = -std::numeric_limits<double>::infinity();
+                for (int i = 0; i < n; ++i) {
+                    if (res.feed[i] > 0) {
+                        candidate[i] = std::log(point.w[i]) + alpha * direction[i];
+                        largest = std::max(largest, candidate[i]);
+                    }
+                }
+                for (int i = 0; i < n; ++i)
+                    candidate[i] = res.feed[i] > 0 ? std::exp(candidate[i] - largest) : 0.0;
+                const double sum = kahan_sum(candidate.data(), n);
+                bool positive = std::isfinite(sum) && sum > 0;
+                for (int i = 0; i < n; ++i) {
+                    candidate[i] /= sum;
+                    positive = positive && (res.feed[i] == 0 || candidate[i] > 0);
+                }
+                if (!positive) continue;
+                if (wk.evaluations - eval0 >= o.max_evaluations) {
+                    tr.status = kEvaluationLimit;
+                    break;
+                }
+                Issue is = evaluate(candidate.data(), next);
+                if (is == kDomain) return false;
+                if (is != kOk) continue;  // rejected property evaluation
+                if (stability_negative(next, o) ||
+                    stability_accept(point, next, -alpha * slope, o.armijo, alpha / scale)) {
+                    std::swap(tr.point, next);
+                    accepted = true;
+                    break;
+                }
+            }
+            if (!accepted) break;
+            ++tr.iterations;
+        }
+        res.trial_iterations += tr.iterations;
+        all_stationary = all_stationary && tr.status == kStationary;
+    }
+    res.status = negative_found ? kUnstable : (all_stationary ? kNoInstabilityFound : kStabilityIndeterminate);
+    res.evaluations = wk.evaluations - eval0;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Rachford-Rice, modules/flash/include/mpmc/flash/rachford_rice.hpp
+enum RrStatus { kRrInterior, kRrNoInterior, kRrDegenerate, kRrIterLimit, kRrUnrepresentable };
+struct RrResult {
+    RrStatus status = kRrUnrepresentable;
+    double beta = kNaN;
+    std::vector<double> x, y;
+    double mass_absolute = 0, mass_relative = 0;
+};
+inline double rr_log_sum(const std::vector<double>& z, const std::vector<double>& lk, double sign) {
+    const int n = static_cast<int>(z.size());  // :42-52
+    double largest = -std::numeric_limits<double>::infinity();
+    for (int i = 0; i < n; ++i)
+        if (z[i] > 0) largest = std::max(largest, std::log(z[i]) + sign * lk[i]);
+    double sum = 0, c = 0;
+    for (int i = 0; i < n; ++i)
+        if (z[i] > 0) kahan_add(std::exp(std::log(z[i]) + sign * lk[i] - largest), sum, c);
+    return largest + std::log(sum);
+}
+inline RrResult solve_rr(const std::vector<double>& z, const std::vector<double>& lk, Work& wk) {
+    const int n = static_cast<int>(z.size());  // :70-147
+    RrResult r;
+    double contrast = 0;
+    for (int i = 0; i < n; ++i)
+        if (z[i] > 0) contrast = std::max(contrast, std::abs(lk[i]));
+    if (contrast == 0) {
+        r.status = kRrDegenerate;
+        return r;
+    }
+    const double ls = rr_log_sum(z, lk, 1), rs = rr_log_sum(z, lk, -1);
+    if (!std::isfinite(ls) || !std::isfinite(rs)) return r;
+    if (ls <= 64 * kEps || rs <= 64 * kEps) {
+        r.status = kRrNoInterior;
+        return r;
+    }
+    // exp(-|lnK|) and the expm1 numerators do not depend on beta; they are
+    // formed once here instead of once per bisection step (same values).
+    std::vector<double> e(n), num(n);
+    for (int i = 0; i < n; ++i) {
+        if (z[i] == 0) continue;
+        e[i] = std::exp(-std::abs(lk[i]));
+        num[i] = lk[i] >= 0 ? -std::expm1(-lk[i]) : std::expm1(lk[i]);
+    }
+    double left = 0, right = 1, beta = 0.5, value = 0;
+    bool resolved = false;
+    for (int it = 0; it < 192; ++it) {
+        ++wk.rr_iterations;
+        beta = midpoint(left, right);
+        if (!(beta > 0 && beta < 1)) break;
+        double v = 0, c = 0;  // rr_value, :53-63
+        for (int i = 0; i < n; ++i) {
+            if (z[i] == 0) continue;
+            const double den = lk[i] >= 0 ? beta + (1 - beta) * e[i] : (1 - beta) + beta * e[i];
+            kahan_add((z[i] / den) * num[i], v, c);
+        }
+        value = v;
+        if (!std::isfinite(value)) return r;
+        if (value == 0 || beta == left || beta == right ||
+            right - left <= 8 * kEps * std::min(beta, 1 - beta)) {
+            resolved = true;
+            break;
+        }
+        if (value > 0) left = beta; else right = beta;
+    }
+    if (!resolved) {
+        r.status = kRrIterLimit;
+        return r;
+    }
+    r.beta = beta;
+    if (std::abs(value) > 64 * kEps) return r;
+    r.x.assign(n, 0.0);
+    r.y.assign(n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        if (z[i] == 0) continue;
+        const double den = lk[i] >= 0 ? beta + (1 - beta) * e[i] : (1 - beta) + beta * e[i];
+        const double larger = z[i] / den;
+        r.x[i] = lk[i] >= 0 ? larger * e[i] : larger;
+        r.y[i] = lk[i] >= 0 ? larger : larger * e[i];
+        if (!std::isfinite(larger) || !(r.x[i] > 0 && r.y[i] > 0)) return r;
+    }
+    const double sx = kahan_sum(r.x.data(), n), sy = kahan_sum(r.y.data(), n);
+    if (std::abs(sx - 1) > 64 * kEps || std::abs(sy - 1) > 64 * kEps) return r;
+    for (int i = 0; i < n; ++i) {
+        r.x[i] /= sx;
+        r.y[i] /= sy;
+        const double recovered = std::fma(beta, r.y[i], (1 - beta) * r.x[i]);
+        const double err = std::abs(recovered - z[i]);
+        r.mass_absolute = std::max(r.mass_absolute, err);
+        if (z[i] > 0) {
+            if (!(r.x[i] > 0 && r.y[i] > 0)) return r;
+            r.mass_relative = std::max(r.mass_relative, err / z[i]);
+        } else if (recovered != 0) {
+            return r;
+        }
+    }
+    r.status = kRrInterior;
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// Split iteration, modules/flash/include/mpmc/flash/pt_split.hpp:275-408
+enum AttemptStatus {
+    kConverged, kNoInteriorRr, kRrFailure, kIndistinguishable, kPhaseDisappearance,
+    kAttemptPropertyFailure, kAttemptIterationLimit, kAttemptEvaluationLimit,
+    kAttemptLineSearchFailed, kUnrepresentableSeed, kBalanceFailure
+};
+struct SplitOptions {  // :30-44
+    double fugacity_tolerance = 1e-11;
+    double mass_absolute_tolerance = 1e-12;
+    double mass_relative_tolerance = 1e-10;
+    double minimum_phase_fraction = 1e-10;
+    double log_k_separation = 1e-7;
+    double relative_z_separation = 1e-8;
+    double max_log_step = 2;
+    double residual_decrease = 1e-4;
+    int max_iterations = 512;
+    int max_backtracks = 24;
+    long long max_evaluations = 20000;
+    double gibbs_armijo = 1e-4;
+};
+struct SplitState {
+    RrResult rr;
+    SplitPhase liquid, vapor;
+    std::vector<double> log_k, residual, common;
+    double fug_norm = 0, gibbs = 0, guard = 0;
+};
+struct Attempt {
+    AttemptStatus status = kUnrepresentableSeed;
+    SplitState point;
+    bool has_point = false;
+    int iterations = 0;
+    long long evaluations = 0;
+};
+
+// Split evaluation, pt_split.hpp:300-341.  Returns false with `st` set to the
+// failure class (SplitStepError or property failure).
+inline bool split_evaluate(const Model& m, Work& wk, double p, double t, const std::vector<double>& z,
+                           const std::vector<double>& lk, const SplitOptions& o, long long& evals,
+                           long long budget, SplitState& s, AttemptStatus& st) {
+    const int n = m.n;
+    s.rr = solve_rr(z, lk, wk);
+    if (s.rr.status != kRrInterior) {
+        st = s.rr.status == kRrDegenerate ? kIndistinguishable
+             : (s.rr.status == kRrNoInterior ? kNoInteriorRr : kRrFailure);
+        return false;
+    }
+    for (int role = 0; role < 2; ++role) {
+        if (evals >= budget) {
+            st = kAttemptEvaluationLimit;
+            return false;
+        }
+        ++evals;
+        SplitPhase& ph = role == 0 ? s.liquid : s.vapor;
+        Issue is = role_provider(m, wk, p, t, role == 0 ? s.rr.x.data() : s.rr.y.data(), role == 1, ph);
+        if (is != kOk) {
+            st = kAttemptPropertyFailure;
+            return false;
+        }
+    }
+    s.log_k.assign(n, 0.0);
+    s.residual.assign(n, 0.0);
+    s.common.assign(n, 0.0);
+    s.fug_norm = 0;
+    s.gibbs = 0;
+    double correction = 0, magnitude = 1, mc = 0;
+    const double beta = s.rr.beta;
+    for (int i = 0; i < n; ++i) {
+        if (z[i] == 0) continue;
+        const double lx = std::log(s.rr.x[i]);
+        const double ly = std::log(s.rr.y[i]);
+        const double mu_l = lx + s.liquid.ln_phi[i];
+        const double mu_v = ly + s.vapor.ln_phi[i];
+        s.log_k[i] = ly - lx;
+        s.residual[i] = (lx - ly) + (s.liquid.ln_phi[i] - s.vapor.ln_phi[i]);
+        s.common[i] = midpoint(mu_l, mu_v);
+        s.fug_norm = std::max(s.fug_norm, std::abs(s.residual[i]));
+        kahan_add((1 - beta) * s.rr.x[i] * mu_l + beta * s.rr.y[i] * mu_v, s.gibbs, correction);
+        kahan_add((1 - beta) * s.rr.x[i] * (std::abs(lx) + std::abs(s.liquid.ln_phi[i])) +
+                      beta * s.rr.y[i] * (std::abs(ly) + std::abs(s.vapor.ln_phi[i])),
+                  magnitude, mc);
+        if (!std::isfinite(s.residual[i]) || !std::isfinite(s.common[i])) {
+            st = kAttemptPropertyFailure;
+            return false;
+        }
+    }
+    s.guard = 256 * kEps * magnitude;
+    if (!std::isfinite(s.gibbs) || !std::isfinite(s.guard)) {
+        st = kAttemptPropertyFailure;
+        return false;
+    }
+    return true;
+}
+
+inline double gibbs_slope(const SplitState& s, const std::vector<double>& z, double scale) {
+    double h = 0, hc = 0, first = 0, fc = 0, second = 0, sc = 0;  // pt_split.hpp:213-231
+    for (size_t i = 0; i < z.size(); ++i) {
+        if (z[i] == 0) continue;
+        const double x = s.rr.x[i], y = s.rr.y[i];
+        const double c = (x / z[i]) * y;
+        const double d = y - x;
+        const double r = s.residual[i];
+        kahan_add(d * (d / z[i]), h, hc);
+        kahan_add(c * r, first, fc);
+        kahan_add((c * r) * r, second, sc);
+    }
+    if (!(h > 0) || !std::isfinite(h) || !std::isfinite(first) || !std::isfinite(second) ||
+        !std::isfinite(scale) || !(scale >= 1))
+        return kNaN;
+    const double beta = s.rr.beta;
+    return -(beta * (1 - beta) * second + (first / h) * first) / scale;
+}
+
+inline bool split_accept(const SplitState& point, const SplitState& next, double predicted,
+                         double relative_step, const SplitOptions& o) {  // :232-244
+    const double guard = point.guard + next.guard;
+    if (predicted > guard) return next.gibbs <= point.gibbs - o.gibbs_armijo * predicted;
+    return next.gibbs <= point.gibbs + guard &&
+           (next.fug_norm <= o.fugacity_tolerance ||
+            point.fug_norm - next.fug_norm > o.residual_decrease * relative_step * point.fug_norm);
+}
+
+inline bool split_seed(const std::vector<double>& z, const std::vector<double>& w, bool as_vapor,
+                       std::vector<double>& lk) {  // :245-267
+    const int n = static_cast<int>(z.size());
+    double amount = 0.1;
+    for (int i = 0; i < n; ++i)
+        if (z[i] > 0) amount = std::min(amount, 0.5 * (z[i] / w[i]));
+    if (!(amount > 0 && amount < 1)) return false;
+    std::vector<double> other(n, 0.0);
+    lk.assign(n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        if (z[i] == 0) continue;
+        other[i] = std::fma(-amount, w[i], z[i]) / (1 - amount);
+        if (!(other[i] > 0)) return false;
+    }
+    const double sum = kahan_sum(other.data(), n);
+    if (!std::isfinite(sum) || std::abs(sum - 1) > 64 * kEps) return false;
+    for (int i = 0; i < n; ++i) {
+        if (z[i] == 0) continue;
+        other[i] /= sum;
+        lk[i] = (as_vapor ? 1.0 : -1.0) * (std::log(w[i]) - std::log(other[i]));
+        if (!std::isfinite(lk[i])) return false;
+    }
+    return true;
+}
+
+inline Attempt iterate_split(const Model& m, Work& wk, double p, double t, const std::vector<double>& z,
+                             const std::vector<double>& lk0, const SplitOptions& o, long long budget) {
+    Attempt a;
+    AttemptStatus st;
+    if (!split_evaluate(m, wk, p, t, z, lk0, o, a.evaluations, budget, a.point, st)) {
+        a.status = st;
+        return a;
+    }
+    a.has_point = true;
+    const int n = m.n;
+    SplitState next;
+    std::vector<double> next_lk(n);
+    for (;;) {
+        const SplitState& point = a.point;
+        if (point.fug_norm <= o.fugacity_tolerance) {  // :351-363
+            const double beta = point.rr.beta;
+            double contrast = 0;
+            for (double v : point.log_k) contrast = std::max(contrast, std::abs(v));
+            if (!(point.rr.mass_absolute <= o.mass_absolute_tolerance &&
+                  point.rr.mass_relative <= o.mass_relative_tolerance))
+                a.status = kBalanceFailure;
+            else if (beta <= o.minimum_phase_fraction || 1 - beta <= o.minimum_phase_fraction)
+                a.status = kPhaseDisappearance;
+            else if (contrast <= o.log_k_separation ||
+                     point.vapor.z - point.liquid.z <=
+                         o.relative_z_separation * std::max(point.vapor.z, point.liquid.z))
+                a.status = kIndistinguishable;
+            else
+                a.status = kConverged;
+            return a;
+        }
+        if (a.iterations >= o.max_iterations) {
+            a.status = kAttemptIterationLimit;
+            return a;
+        }
+        const double scale = std::max(1.0, point.fug_norm / o.max_log_step);
+        const double slope = gibbs_slope(point, z, scale);
+        if (!std::isfinite(slope) || !(slope < 0)) {
+            a.status = kAttemptLineSearchFailed;
+            return a;
+        }
+        bool accepted = false;
+        double alpha = 1;
+        a.status = kAttemptLineSearchFailed;
+        for (int bt = 0; bt < o.max_backtracks; ++bt, alpha *= 0.5) {
+            for (int i = 0; i < n; ++i) next_lk[i] = point.log_k[i] + (alpha / scale) * point.residual[i];
+            if (split_evaluate(m, wk, p, t, z, next_lk, o, a.evaluations, budget, next, st)) {
+                if (split_accept(point, next, -alpha * slope, alpha / scale, o)) {
+                    std::swap(a.point, next);
+                    accepted = true;
+                    break;
+                }
+            } else if (st == kAttemptEvaluationLimit) {
+                a.status = st;
+                return a;
+            }
+        }
+        if (!accepted) return a;
+        ++a.iterations;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Full VLE, modules/flash/include/mpmc/flash/pt_split.hpp:415-525
+enum FlashStatus { kSinglePhase = 0, kTwoPhase = 1, kPhaseSetUnstable = 2, kIndeterminate = 3, kInvalid = -1 };
+struct FlashResult {
+    FlashStatus status = kIndeterminate;
+    StabilityResult initial, final_review;
+    bool has_candidate = false;
+    SplitState candidate;
+    int attempts = 0;
+    int split_iterations = 0;
+    long long split_evaluations = 0;
+};
+
+inline FlashResult solve_vle(const Model& m, Work& wk, double p, double t, const std::vector<double>& feed) {
+    FlashResult res;
+    const int n = m.n;
+    double sum;
+    if (!std::isfinite(p) || p <= 0 || !std::isfinite(t) || t <= 0 ||
+        !check_composition(feed.data(), n, sum)) {
+        res.status = kInvalid;
+        return res;
+    }
+    StabilityOptions so;
+    SplitOptions sp;
+    if (!stability_test(m, wk, p, t, feed, so, {}, {}, res.initial)) {
+        res.status = kInvalid;
+        return res;
+    }
+    if (res.initial.status == kNoInstabilityFound) {
+        res.status = kSinglePhase;
+        return res;
+    }
+    if (res.initial.status != kUnstable) {
+        res.status = kIndeterminate;
+        return res;
+    }
+    const std::vector<double>& z = res.initial.feed;
+    int selected = -1;
+    bool limit = false;
+    for (size_t k = 0; k < res.initial.trials.size() && !limit; ++k) {  // :459-486
+        const Trial& wit = res.initial.trials[k];
+        if (wit.status != kNegativeTpd || !wit.has_point || !stability_negative(wit.point, so)) continue;
+        for (bool as_vapor : {true, false}) {
+            if (res.attempts >= 16 || res.split_evaluations >= sp.max_evaluations) {
+                limit = true;
+                break;
+            }
+            std::vector<double> seed;
+            Attempt a;
+            if (split_seed(z, wit.point.w, as_vapor, seed))
+                a = iterate_split(m, wk, p, t, z, seed, sp, sp.max_evaluations - res.split_evaluations);
+            res.split_evaluations += a.evaluations;
+            res.split_iterations += a.iterations;
+            ++res.attempts;
+            if (a.status == kConverged && (selected < 0 || a.point.gibbs < res.candidate.gibbs)) {
+                selected = res.attempts - 1;
+                res.candidate = a.point;
+                res.has_candidate = true;
+            }
+        }
+    }
+    if (selected < 0) {
+        res.status = kIndeterminate;
+        return res;
+    }
+    const SplitState& cand = res.candidate;
+    double feed_g = 0, correction = 0, magnitude = 1;  // :491-500
+    for (int i = 0; i < n; ++i) {
+        if (z[i] == 0) continue;
+        const double lz = std::log(z[i]);
+        const double phi = res.initial.reference.ln_phi[i];
+        kahan_add(z[i] * (lz + phi), feed_g, correction);
+        magnitude += z[i] * (std::abs(lz) + std::abs(phi));
+    }
+    const double gibbs_change = cand.gibbs - feed_g;
+    const double gibbs_guard = cand.guard + 256 * kEps * magnitude;
+    StabilityOptions fo = so;
+    fo.tpd_tolerance += 0.5 * cand.fug_norm;
+    if (!std::isfinite(gibbs_change) || !std::isfinite(gibbs_guard) || !std::isfinite(fo.tpd_tolerance)) {
+        res.status = kIndeterminate;
+        return res;
+    }
+    std::vector<std::vector<double>> starts{cand.rr.x, cand.rr.y};
+    if (!stability_test(m, wk, p, t, z, fo, starts, cand.common, res.final_review)) {
+        res.status = kInvalid;
+        return res;
+    }
+    if (res.final_review.status == kUnstable)
+        res.status = kPhaseSetUnstable;
+    else if (gibbs_change > gibbs_guard)
+        res.status = kIndeterminate;
+    else if (res.final_review.status == kNoInstabilityFound)
+        res.status = kTwoPhase;
+    else
+        res.status = kIndeterminate;
+    return res;
+}
+
+// ---------------------------------------------------------------------------
+// Forward-mode phase evaluation (generic Number), pr76_mixture.hpp:125-219 and
+// pr76_phase.hpp:193-258.  x holds all n fractions already in Number form.
+template <class Num>
+inline bool phase_eval_ad(const Model& m, const Num& p, const Num& t, const std::vector<Num>& x,
+                          int root_index, Num& z_out, std::vector<Num>& ln_phi) {
+    const int n = m.n;
+    std::vector<Num> a(n), root(n), sums(n);
+    Num attraction(0.0), covolume(0.0);
+    for (int i = 0; i < n; ++i) {
+        const Num reduced_root = sqrt(t) / m.sqrt_tc[i];
+        const Num bracket = 1.0 + m.kappa[i] * (1.0 - reduced_root);
+        a[i] = (bracket * m.ac[i]) * bracket;
+        attraction = attraction + (x[i] * a[i]) * x[i];
+        covolume = covolume + x[i] * m.b[i];
+        sums[i] = x[i] * a[i];
+        if (n > 1) root[i] = sqrt(a[i]);
+    }
+    for (int i = 0; i < n; ++i)
+        for (int j = i + 1; j < n; ++j) {
+            const Num cross = ((x[i] * root[i]) * (x[j] * root[j])) * m.factor[i * n + j];
+            attraction = attraction + cross;
+            attraction = attraction + cross;
+            const Num aij = (root[i] * m.factor[i * n + j]) * root[j];
+            sums[i] = sums[i] + x[j] * aij;
+            sums[j] = sums[j] + x[i] * aij;
+        }
+    const Num rt = kR * t;
+    const Num prt = p / rt;
+    const Num A = (attraction / rt) * prt;
+    const Num B = covolume * prt;
+    const RootSet roots = solve_roots(val(A), val(B));
+    if (roots.status != kRootSuccess || root_index >= roots.count) return false;
+    const Root& rootv = roots.roots[root_index];
+    Num free_volume(rootv.free_volume);
+    {
+        // First-order implicit function theorem on the scaled cubic,
+        // pr76_phase.hpp:208-222.
+        if (!rootv.derivative_valid) return false;
+        const double y0 = rootv.free_volume / roots.scale;
+        const double scale = roots.scale;
+        const Num bs = B / scale;
+        const double inv = 1.0 / scale;
+        const Num c2 = 4.0 * bs - inv;
+        const Num c1 = (A / scale) / scale + 2.0 * bs * bs - 4.0 * bs * inv;
+        const Num c0 = ((-2.0 * bs) * bs) * inv;
+        const Num residual = ((Num(y0) + c2) * y0 + c1) * y0 + c0;
+        const double dh = (3.0 * y0 + 2.0 * val(c2)) * y0 + val(c1);
+        free_volume = free_volume - ((residual - Num(val(residual))) / dh) * scale;
+    }
+    const Num z = free_volume + B;
+    const double sqrt2 = std::sqrt(2.0);
+    const Num denominator = free_volume + (2.0 - sqrt2) * B;
+    const Num u = (2.0 * sqrt2) * (B / denominator);
+    const Num log_factor = log1p_over_x(u) / denominator;
+    Num z_minus_one = z - 1.0;
+    Num log_free = log(free_volume);
+    if (std::abs(val(z_minus_one)) < 0.25 && val(B) < 0.125) {
+        const Num bz = B / z;
+        z_minus_one = B / free_volume - (A / z) / (1.0 + 2.0 * bz - bz * bz);
+        log_free = log1p(z_minus_one - B);
+    }
+    ln_phi.resize(n);
+    for (int i = 0; i < n; ++i) {
+        const Num ratio = Num(m.b[i]) / covolume;
+        const Num coefficient = ((2.0 * sums[i] - attraction * ratio) / rt) * prt;
+        ln_phi[i] = ratio * z_minus_one - log_free - coefficient * log_factor;
+        if (!finite(ln_phi[i])) return false;
+    }
+    z_out = z;
+    return finite(z);
+}
+
+// Sensitivity outputs (reduced chart q = p, T, z_0..z_{n-2}).
+struct Sensitivity {
+    int status = 6;  // PtSensitivityStatus; 0 = success
+    std::vector<double> dlnk, dx, dy;  // n x (n+1), row-major
+    std::vector<double> dbeta;         // n+1
+    std::vector<double> dzl, dzv, drhol, drhov;  // n+1 (closure linearisation)
+    std::vector<double> jl, jv;        // (n+1) x (n+2): d[Z, ln phi]/d[p, T, x_full]
+};
+
+// LU with partial pivoting + rcond, pt_sensitivity_detail.hpp:364-471
+struct Lu {
+    int n = 0;
+    std::vector<double> v;
+    std::vector<int> piv;
+    double norm_inf = 0;
+};
+inline bool lu_factor(const std::vector<double>& a, int n, Lu& f) {
+    f.n = n;
+    f.v = a;
+    f.piv.assign(n, 0);
+    f.norm_inf = 0;
+    for (int r = 0; r < n; ++r) {
+        double s = 0;
+        for (int c = 0; c < n; ++c) s += std::abs(a[r * n + c]);
+        f.norm_inf = std::max(f.norm_inf, s);
+    }
+    if (!(f.norm_inf > 0) || !std::isfinite(f.norm_inf)) return false;
+    const double guard = 64.0 * kEps * n * f.norm_inf;
+    for (int c = 0; c < n; ++c) {
+        int piv = c;
+        double mag = std::abs(f.v[c * n + c]);
+        for (int r = c + 1; r < n; ++r) {
+            const double cand = std::abs(f.v[r * n + c]);
+            if (cand > mag) {
+                mag = cand;
+                piv = r;
+            }
+        }
+        if (!std::isfinite(mag) || !(mag > guard)) return false;
+        f.piv[c] = piv;
+        if (piv != c)
+            for (int j = 0; j < n; ++j) std::swap(f.v[c * n + j], f.v[piv * n + j]);
+        const double diag = f.v[c * n + c];
+        for (int r = c + 1; r < n; ++r) {
+            const double mult = f.v[r * n + c] / diag;
+            f.v[r * n + c] = mult;
+            for (int j = c + 1; j < n; ++j) f.v[r * n + j] -= mult * f.v[c * n + j];
+        }
+    }
+    return true;
+}
+inline bool lu_solve(const Lu& f, std::vector<double>& rhs) {
+    const int n = f.n;
+    for (int c = 0; c < n; ++c)
+        if (f.piv[c] != c) std::swap(rhs[c], rhs[f.piv[c]]);
+    for (int r = 0; r < n; ++r)
+        for (int c = 0; c < r; ++c) rhs[r] -= f.v[r * n + c] * rhs[c];
+    for (int r = n - 1; r >= 0; --r) {
+        for (int c = r + 1; c < n; ++c) rhs[r] -= f.v[r * n + c] * rhs[c];
+        rhs[r] /= f.v[r * n + r];
+        if (!std::isfinite(rhs[r])) return false;
+    }
+    return true;
+}
+inline double lu_rcond(const Lu& f) {
+    const int n = f.n;
+    std::vector<double> rows(n, 0.0);
+    for (int c = 0; c < n; ++c) {
+        std::vector<double> e(n, 0.0);
+        e[c] = 1;
+        if (!lu_solve(f, e)) return 0;
+        for (int r = 0; r < n; ++r) rows[r] += std::abs(e[r]);
+    }
+    const double inv = *std::max_element(rows.begin(), rows.end());
+    const double prod = f.norm_inf * inv;
+    if (!(prod > 0) || !std::isfinite(prod)) return 0;
+    return 1 / prod;
+}
+
+// differentiate_pr76_pt_vle, modules/flash/include/mpmc/flash/pr76_sensitivity.hpp:51-390,
+// with the local system of detail/pr76_sensitivity_local.hpp:29-109 and the RR
+// linearisation of detail/pt_sensitivity_detail.hpp:46-143; closure dZ/drho of
+// modules/physics/include/mpmc/physics/pr76_thermodynamic_closure.hpp:279-337;
+// per-phase full-chart Jacobians of pr76_phase_ad.hpp:57-122.
+inline void differentiate(const Model& m, const FlashResult& fr, double p, double t, Sensitivity& s) {
+    const int n = m.n;
+    const int q = n + 1;
+    s = Sensitivity();
+    if (fr.status != kTwoPhase || !fr.has_candidate) {
+        s.status = 1;  // solution_not_accepted
+        return;
+    }
+    const std::vector<double>& feed = fr.initial.feed;
+    for (double v : feed)
+        if (!(v > 0)) {
+            s.status = 3;  // unsupported_feed_support
+            return;
+        }
+    const SplitState& c = fr.candidate;
+    double contrast = 0;
+    for (double v : c.log_k) contrast = std::max(contrast, std::abs(v));
+    if (!(contrast > 1e-7) || !(c.vapor.z - c.liquid.z > 1e-8 * std::max(c.vapor.z, c.liquid.z))) {
+        s.status = 2;  // phase_boundary
+        return;
+    }
+    const double beta = c.rr.beta;
+    const double guard = std::max(1.490116119384765625e-8, 1e-10);
+    if (!(beta > guard) || !(1 - beta > guard)) {
+        s.status = 2;
+        return;
+    }
+    if (!(c.fug_norm <= 1e-11)) {
+        s.status = 1;
+        return;
+    }
+    // Base RR point, pt_sensitivity_detail.hpp:269-300
+    std::vector<double> xb(n), yb(n);
+    double xs = 0, ys = 0;
+    for (int i = 0; i + 1 < n; ++i) {
+        xb[i] = c.rr.x[i];
+        yb[i] = c.rr.y[i];
+        xs += xb[i];
+        ys += yb[i];
+    }
+    xb[n - 1] = 1.0 - xs;
+    yb[n - 1] = 1.0 - ys;
+    for (int i = 0; i < n; ++i)
+        if (!(xb[i] > 0) || !(yb[i] > 0)) {
+            s.status = 2;
+            return;
+        }
+    double h = 0;
+    for (int i = 0; i < n; ++i) {
+        const double d = yb[i] - xb[i];
+        h += d * d / feed[i];
+    }
+    if (!std::isfinite(h) || !(h > 0)) {
+        s.status = 5;
+        return;
+    }
+    // Local system Jacobian: variables [lnK(n), p, T, z_0..z_{n-2}],
+    // outputs [F(n), beta, x(n), y(n)].  One tangent direction per pass.
+    const int nv = 2 * n + 1, no = 3 * n + 1;
+    std::vector<double> J(static_cast<size_t>(no) * nv), F(no);
+    for (int v = 0; v < nv; ++v) {
+        std::vector<D1> lk(n), zf(n);
+        for (int i = 0; i < n; ++i) lk[i] = D1(c.log_k[i], v == i ? 1.0 : 0.0);
+        D1 pd(p, v == n ? 1.0 : 0.0), td(t, v == n + 1 ? 1.0 : 0.0);
+        D1 fsum(0.0);
+        for (int i = 0; i + 1 < n; ++i) {
+            zf[i] = D1(feed[i], v == n + 2 + i ? 1.0 : 0.0);
+            fsum = fsum + zf[i];
+        }
+        zf[n - 1] = 1.0 - fsum;
+        double num = 0;
+        for (int i = 0; i < n; ++i) {
+            const double zi = zf[i].v;
+            num += (xb[i] * yb[i] / zi) * lk[i].d + ((yb[i] - xb[i]) / zi) * zf[i].d;
+        }
+        const double dbeta = num / h;
+        std::vector<D1> xl(n), yv(n);
+        D1 lsum(0.0), vsum(0.0);
+        for (int i = 0; i + 1 < n; ++i) {
+            const double zi = zf[i].v;
+            const double dlx = zf[i].d / zi - ((yb[i] - xb[i]) / zi) * dbeta - beta * (yb[i] / zi) * lk[i].d;
+            xl[i] = D1(xb[i], xb[i] * dlx);
+            yv[i] = D1(yb[i], yb[i] * (dlx + lk[i].d));
+            lsum = lsum + xl[i];
+            vsum = vsum + yv[i];
+        }
+        xl[n - 1] = 1.0 - lsum;
+        yv[n - 1] = 1.0 - vsum;
+        D1 zl, zv;
+        std::vector<D1> pl, pv;
+        if (!phase_eval_ad(m, pd, td, xl, c.liquid.branch, zl, pl) ||
+            !phase_eval_ad(m, pd, td, yv, c.vapor.branch, zv, pv)) {
+            s.status = 4;  // property_failure
+            return;
+        }
+        for (int i = 0; i < n; ++i) {
+            const D1 fi = log(xl[i]) - log(yv[i]) + pl[i] - pv[i];
+            J[i * nv + v] = fi.d;
+            F[i] = fi.v;
+        }
+        J[n * nv + v] = dbeta;
+        F[n] = beta;
+        for (int i = 0; i < n; ++i) {
+            J[(n + 1 + i) * nv + v] = xl[i].d;
+            J[(2 * n + 1 + i) * nv + v] = yv[i].d;
+            F[n + 1 + i] = xl[i].v;
+            F[2 * n + 1 + i] = yv[i].v;
+        }
+    }
+    const double arithmetic_scale = 8192.0 * kEps * n;  // pr76_sensitivity.hpp:219-229
+    double res_norm = 0;
+    for (int i = 0; i < n; ++i) res_norm = std::max(res_norm, std::abs(F[i]));
+    if (res_norm > 1e-11 + arithmetic_scale) {
+        s.status = 1;
+        return;
+    }
+    std::vector<double> A(n * n), Bm(n * q);
+    for (int r = 0; r < n; ++r) {
+        for (int cc = 0; cc < n; ++cc) A[r * n + cc] = J[r * nv + cc];
+        for (int cc = 0; cc < q; ++cc) Bm[r * q + cc] = J[r * nv + n + cc];
+    }
+    Lu f;
+    if (!lu_factor(A, n, f)) {
+        s.status = 5;
+        return;
+    }
+    const double rc = lu_rcond(f);
+    if (!std::isfinite(rc) || !(rc > 256.0 * kEps * n)) {
+        s.status = 5;
+        return;
+    }
+    s.dlnk.assign(n * q, 0.0);
+    for (int cc = 0; cc < q; ++cc) {
+        std::vector<double> rhs(n);
+        for (int r = 0; r < n; ++r) rhs[r] = -Bm[r * q + cc];
+        if (!lu_solve(f, rhs)) {
+            s.status = 5;
+            return;
+        }
+        for (int r = 0; r < n; ++r) s.dlnk[r * q + cc] = rhs[r];
+    }
+    double backward = 0;
+    for (int cc = 0; cc < q; ++cc)
+        for (int r = 0; r < n; ++r) {
+            double res = Bm[r * q + cc], sc = std::abs(res);
+            for (int j = 0; j < n; ++j) {
+                const double term = A[r * n + j] * s.dlnk[j * q + cc];
+                res += term;
+                sc += std::abs(term);
+            }
+            backward = std::max(backward, std::abs(res) / std::max(1.0, sc));
+        }
+    if (!std::isfinite(backward) || backward > arithmetic_scale) {
+        s.status = 6;
+        return;
+    }
+    auto total = [&](int out, int col) {
+        double v = J[out * nv + n + col];
+        for (int j = 0; j < n; ++j) v += J[out * nv + j] * s.dlnk[j * q + col];
+        return v;
+    };
+    s.dbeta.assign(q, 0.0);
+    s.dx.assign(n * q, 0.0);
+    s.dy.assign(n * q, 0.0);
+    for (int cc = 0; cc < q; ++cc) {
+        s.dbeta[cc] = total(n, cc);
+        for (int i = 0; i < n; ++i) {
+            s.dx[i * q + cc] = total(n + 1 + i, cc);
+            s.dy[i * q + cc] = total(2 * n + 1 + i, cc);
+        }
+    }
+    for (double v : s.dbeta) if (!std::isfinite(v)) { s.status = 6; return; }
+    for (double v : s.dx) if (!std::isfinite(v)) { s.status = 6; return; }
+    for (double v : s.dy) if (!std::isfinite(v)) { s.status = 6; return; }
+    for (int cc = 0; cc < q; ++cc) {  // :346-385
+        double ls = 0, vs = 0;
+        for (int i = 0; i < n; ++i) {
+            ls += s.dx[i * q + cc];
+            vs += s.dy[i * q + cc];
+        }
+        if (std::abs(ls) > arithmetic_scale || std::abs(vs) > arithmetic_scale) {
+            s.status = 6;
+            return;
+        }
+        for (int i = 0; i < n; ++i) {
+            const double dz = cc < 2 ? 0.0 : (i == cc - 2 ? 1.0 : (i + 1 == n ? -1.0 : 0.0));
+            const double xv = F[n + 1 + i], yv = F[2 * n + 1 + i];
+            const double der = (1 - beta) * s.dx[i * q + cc] + beta * s.dy[i * q + cc] +
+                               (yv - xv) * s.dbeta[cc] - dz;
+            const double sc = std::max(1.0, std::abs(s.dx[i * q + cc]) + std::abs(s.dy[i * q + cc]) +
+                                                std::abs(s.dbeta[cc]) + std::abs(dz));
+            if (std::abs(der) > arithmetic_scale * sc) {
+                s.status = 6;
+                return;
+            }
+        }
+    }
+    s.status = 0;
+    // Per-phase full-chart Jacobians d[Z, ln phi]/d[p, T, x_0..x_{n-1}].
+    for (int ph = 0; ph < 2; ++ph) {
+        const std::vector<double>& comp = ph == 0 ? c.rr.x : c.rr.y;
+        const int branch = ph == 0 ? c.liquid.branch : c.vapor.branch;
+        std::vector<double>& jac = ph == 0 ? s.jl : s.jv;
+        jac.assign((n + 1) * (n + 2), 0.0);
+        for (int v = 0; v < n + 2; ++v) {
+            D1 pd(p, v == 0 ? 1.0 : 0.0), td(t, v == 1 ? 1.0 : 0.0);
+            std::vector<D1> xs2(n);
+            for (int i = 0; i < n; ++i) xs2[i] = D1(comp[i], v == 2 + i ? 1.0 : 0.0);
+            D1 zz;
+            std::vector<D1> lp;
+            if (!phase_eval_ad(m, pd, td, xs2, branch, zz, lp)) {
+                s.status = 4;
+                return;
+            }
+            jac[0 * (n + 2) + v] = zz.d;
+            for (int i = 0; i < n; ++i) jac[(1 + i) * (n + 2) + v] = lp[i].d;
+        }
+    }
+    // Closure dZ and d(rho), pr76_thermodynamic_closure.hpp:81-118, 309-337.
+    s.dzl.assign(q, 0.0);
+    s.dzv.assign(q, 0.0);
+    s.drhol.assign(q, 0.0);
+    s.drhov.assign(q, 0.0);
+    for (int ph = 0; ph < 2; ++ph) {
+        const std::vector<double>& comp = ph == 0 ? c.rr.x : c.rr.y;
+        const int branch = ph == 0 ? c.liquid.branch : c.vapor.branch;
+        std::vector<double> grad(q);
+        for (int v = 0; v < q; ++v) {
+            D1 pd(p, v == 0 ? 1.0 : 0.0), td(t, v == 1 ? 1.0 : 0.0);
+            std::vector<D1> xs2(n);
+            D1 ssum(0.0);
+            for (int i = 0; i + 1 < n; ++i) {
+                xs2[i] = D1(comp[i], v == 2 + i ? 1.0 : 0.0);
+                ssum = ssum + xs2[i];
+            }
+            xs2[n - 1] = 1.0 - ssum;
+            D1 zz;
+            std::vector<D1> lp;
+            if (!phase_eval_ad(m, pd, td, xs2, branch, zz, lp)) {
+                s.status = 4;
+                return;
+            }
+            grad[v] = zz.d;
+        }
+        const double zph = ph == 0 ? c.liquid.z : c.vapor.z;
+        const double rho = p / (zph * kR * t);
+        const std::vector<double>& dcomp = ph == 0 ? s.dx : s.dy;
+        for (int cc = 0; cc < q; ++cc) {
+            double dz = cc == 0 ? grad[0] : (cc == 1 ? grad[1] : 0.0);
+            for (int k = 0; k + 1 < n; ++k) dz += grad[2 + k] * dcomp[k * q + cc];
+            const double dp = cc == 0 ? 1.0 / p : 0.0;
+            const double dt = cc == 1 ? 1.0 / t : 0.0;
+            (ph == 0 ? s.dzl : s.dzv)[cc] = dz;
+            (ph == 0 ? s.drhol : s.drhov)[cc] = rho * (dp - dz / zph - dt);
+        }
+    }
+}
+
+}  // namespace oracle
+
+// ===========================================================================
+// C interface (ctypes).  Layout: every per-component or per-entry array is
+// entry-major with the cell index fastest: a[k * ncell + c].
+extern "C" {
+
+struct OracleOutputs {
+    int32_t* status;        // [ncell]
+    double* beta;           // [ncell]
+    double* x;              // [n*ncell]
+    double* y;              // [n*ncell]
+    double* ln_k;           // [n*ncell]
+    double* ln_phi_l;       // [n*ncell]
+    double* ln_phi_v;       // [n*ncell]
+    double* z_l;            // [ncell]
+    double* z_v;            // [ncell]
+    int64_t* counters;      // [8*ncell]: init evals, split evals, final evals, split iters,
+                            //  rr iters, root bisection steps, attempts, trial iterations
+    int32_t* sens_status;   // [ncell]
+    double* dlnk;           // [n*(n+1)*ncell]
+    double* dbeta;          // [(n+1)*ncell]
+    double* dx;             // [n*(n+1)*ncell]
+    double* dy;             // [n*(n+1)*ncell]
+    double* dzl;            // [(n+1)*ncell]
+    double* dzv;            // [(n+1)*ncell]
+    double* drhol;          // [(n+1)*ncell]
+    double* drhov;          // [(n+1)*ncell]
+    double* jl;             // [(n+1)*(n+2)*ncell]
+    double* jv;             // [(n+1)*(n+2)*ncell]
+};
+
+static void oracle_cell(const oracle::Model& m, int64_t ncell, int64_t c, const double* p, const double* t,
+                        const double* z, int want_sens, const OracleOutputs* o) {
+    using namespace oracle;
+    const int n = m.n;
+    const double nan = kNaN;
+    Work wk;
+    wk.init(n);
+    std::vector<double> feed(n);
+    for (int i = 0; i < n; ++i) feed[i] = z[i * ncell + c];
+    FlashResult fr;
+    if (!std::isfinite(t[c]) || !(t[c] > 0) || !make_temp_cache(m, t[c], wk.tc)) {
+        fr.status = kInvalid;
+    } else {
+        fr = solve_vle(m, wk, p[c], t[c], feed);
+    }
+    auto put = [&](double* arr, int k, double v) {
+        if (arr) arr[k * ncell + c] = v;
+    };
+    if (o->status) o->status[c] = fr.status;
+    const bool pair = fr.has_candidate && fr.status != kSinglePhase && fr.status != kInvalid;
+    put(o->beta, 0, pair ? fr.candidate.rr.beta : nan);
+    for (int i = 0; i < n; ++i) {
+        if (pair) {
+            put(o->x, i, fr.candidate.rr.x[i]);
+            put(o->y, i, fr.candidate.rr.y[i]);
+            put(o->ln_k, i, fr.candidate.log_k[i]);
+            put(o->ln_phi_l, i, fr.candidate.liquid.ln_phi[i]);
+            put(o->ln_phi_v, i, fr.candidate.vapor.ln_phi[i]);
+        } else if (fr.status == kSinglePhase) {
+            put(o->x, i, fr.initial.feed[i]);
+            put(o->y, i, nan);
+            put(o->ln_k, i, nan);
+            put(o->ln_phi_l, i, fr.initial.reference.ln_phi[i]);
+            put(o->ln_phi_v, i, nan);
+        } else {
+            put(o->x, i, nan);
+            put(o->y, i, nan);
+            put(o->ln_k, i, nan);
+            put(o->ln_phi_l, i, nan);
+            put(o->ln_phi_v, i, nan);
+        }
+    }
+    put(o->z_l, 0, pair ? fr.candidate.liquid.z : (fr.status == kSinglePhase ? fr.initial.reference.z : nan));
+    put(o->z_v, 0, pair ? fr.candidate.vapor.z : nan);
+    if (o->counters) {
+        const int64_t cnt[8] = {fr.initial.evaluations, fr.split_evaluations, fr.final_review.evaluations,
+                                fr.split_iterations, wk.rr_iterations, wk.root_bisections, fr.attempts,
+                                fr.initial.trial_iterations + fr.final_review.trial_iterations};
+        for (int k = 0; k < 8; ++k) o->counters[k * ncell + c] = cnt[k];
+    }
+    if (!want_sens) return;
+    Sensitivity s;
+    if (fr.status == kTwoPhase) differentiate(m, fr, p[c], t[c], s);
+    else s.status = 1;
+    if (o->sens_status) o->sens_status[c] = s.status;
+    const int q = n + 1;
+    const bool ok = s.status == 0;
+    for (int k = 0; k < n * q; ++k) {
+        put(o->dlnk, k, ok ? s.dlnk[k] : nan);
+        put(o->dx, k, ok ? s.dx[k] : nan);
+        put(o->dy, k, ok ? s.dy[k] : nan);
+    }
+    for (int k = 0; k < q; ++k) {
+        put(o->dbeta, k, ok ? s.dbeta[k] : nan);
+        put(o->dzl, k, ok ? s.dzl[k] : nan);
+        put(o->dzv, k, ok ? s.dzv[k] : nan);
+        put(o->drhol, k, ok ? s.drhol[k] : nan);
+        put(o->drhov, k, ok ? s.drhov[k] : nan);
+    }
+    for (int k = 0; k < (n + 1) * (n + 2); ++k) {
+        put(o->jl, k, ok ? s.jl[k] : nan);
+        put(o->jv, k, ok ? s.jv[k] : nan);
+    }
+}
+
+// Flash `ncell` cells of one mixture with `threads` host threads (static
+// partition, one scratch workspace per thread).  Returns 0, or -1 on invalid
+// arguments.
+int oracle_flash_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                       int64_t ncell, const double* p, const double* t, const double* z, int threads,
+                       int want_sensitivity, const OracleOutputs* out) {
+    if (n < 1 || n > 256 || ncell < 0 || !tc || !pc || !omega || !kij || !p || !t || !z || !out) return -1;
+    const oracle::Model m = oracle::make_model(n, tc, pc, omega, kij);
+    if (threads < 1) threads = 1;
+    if (threads > ncell) threads = static_cast<int>(std::max<int64_t>(ncell, 1));
+    auto run = [&](int64_t lo, int64_t hi) {
+        for (int64_t c = lo; c < hi; ++c) oracle_cell(m, ncell, c, p, t, z, want_sensitivity, out);
+    };
+    if (threads == 1) {
+        run(0, ncell);
+        return 0;
+    }
+    std::vector<std::thread> pool;
+    const int64_t chunk = (ncell + threads - 1) / threads;
+    for (int k = 0; k < threads; ++k) {
+        const int64_t lo = k * chunk, hi = std::min<int64_t>(ncell, lo + chunk);
+        if (lo < hi) pool.emplace_back(run, lo, hi);
+    }
+    for (auto& th : pool) th.join();
+    return 0;
+}
+
+// One phase property evaluation at a fixed composition (stability provider:
+// minimum-Gibbs admissible branch).  Returns the issue code (0 = ok).
+int oracle_stability_phase(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                           double p, double t, const double* x, double* ln_phi, double* z_out, int* branch,
+                           int* smooth) {
+    const oracle::Model m = oracle::make_model(n, tc, pc, omega, kij);
+    oracle::Work wk;
+    wk.init(n);
+    if (!oracle::make_temp_cache(m, t, wk.tc)) return oracle::kRootRange;
+    oracle::StabilityPhase ph;
+    const oracle::Issue is = oracle::stability_provider(m, wk, p, t, x, ph);
+    if (is != oracle::kOk) return is;
+    for (int i = 0; i < n; ++i) ln_phi[i] = ph.ln_phi[i];
+    *z_out = ph.z;
+    *branch = ph.branch;
+    *smooth = ph.smooth ? 1 : 0;
+    return 0;
+}
+
+// Rachford-Rice at fixed ln K.  Returns the RR status code.
+int oracle_rachford_rice(int n, const double* z, const double* ln_k, double* beta, double* x, double* y) {
+    std::vector<double> zz(z, z + n), lk(ln_k, ln_k + n);
+    oracle::Work wk;
+    const oracle::RrResult r = oracle::solve_rr(zz, lk, wk);
+    *beta = r.beta;
+    if (r.status == oracle::kRrInterior)
+        for (int i = 0; i < n; ++i) {
+            x[i] = r.x[i];
+            y[i] = r.y[i];
+        }
+    return r.status;
+}
+
+}  // extern "C"

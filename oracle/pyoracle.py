@@ -1,0 +1,128 @@
+"""ctypes loader for the CPU oracle (test infrastructure).
+
+Only tests, the smoke check and the benchmark's CPU-baseline leg use this
+module.  `flash()` runs oracle/_build/libpr76_oracle.so (the C++ restatement of
+the reference algorithm); `reference_flash()` runs oracle/_ref/libpr76_ref.so
+(the reference headers themselves), which exists only where the reference
+sources were available at build time.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libpr76_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libpr76_ref.so")
+
+FIELDS = [
+    ("status", ctypes.c_void_p), ("beta", ctypes.c_void_p), ("x", ctypes.c_void_p),
+    ("y", ctypes.c_void_p), ("ln_k", ctypes.c_void_p), ("ln_phi_l", ctypes.c_void_p),
+    ("ln_phi_v", ctypes.c_void_p), ("z_l", ctypes.c_void_p), ("z_v", ctypes.c_void_p),
+    ("counters", ctypes.c_void_p), ("sens_status", ctypes.c_void_p), ("dlnk", ctypes.c_void_p),
+    ("dbeta", ctypes.c_void_p), ("dx", ctypes.c_void_p), ("dy", ctypes.c_void_p),
+    ("dzl", ctypes.c_void_p), ("dzv", ctypes.c_void_p), ("drhol", ctypes.c_void_p),
+    ("drhov", ctypes.c_void_p), ("jl", ctypes.c_void_p), ("jv", ctypes.c_void_p),
+]
+
+COUNTER_NAMES = ["init_evals", "split_evals", "final_evals", "split_iters", "rr_iters",
+                 "root_bisections", "attempts", "trial_iters"]
+
+
+class _Out(ctypes.Structure):
+    _fields_ = FIELDS
+
+
+def build(force: bool = False) -> None:
+    """Compile the oracle (always) and the reference harness (if sources exist)."""
+    if force or not os.path.exists(ORACLE_SO):
+        subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+    if os.path.isdir("/root/reference/modules") and (force or not os.path.exists(REF_SO)):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref"])
+
+
+_libs: dict[str, ctypes.CDLL] = {}
+
+
+def _lib(path: str) -> ctypes.CDLL:
+    if path not in _libs:
+        _libs[path] = ctypes.CDLL(path)
+    return _libs[path]
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_SO)
+
+
+def _alloc(n: int, ncell: int, sens: bool):
+    q = n + 1
+    out = {
+        "status": np.full(ncell, -9, np.int32), "beta": np.empty(ncell),
+        "x": np.empty((n, ncell)), "y": np.empty((n, ncell)), "ln_k": np.empty((n, ncell)),
+        "ln_phi_l": np.empty((n, ncell)), "ln_phi_v": np.empty((n, ncell)),
+        "z_l": np.empty(ncell), "z_v": np.empty(ncell), "counters": np.zeros((8, ncell), np.int64),
+    }
+    if sens:
+        out.update({
+            "sens_status": np.full(ncell, -9, np.int32), "dlnk": np.empty((n * q, ncell)),
+            "dbeta": np.empty((q, ncell)), "dx": np.empty((n * q, ncell)), "dy": np.empty((n * q, ncell)),
+            "dzl": np.empty((q, ncell)), "dzv": np.empty((q, ncell)), "drhol": np.empty((q, ncell)),
+            "drhov": np.empty((q, ncell)), "jl": np.empty(((n + 1) * (n + 2), ncell)),
+            "jv": np.empty(((n + 1) * (n + 2), ncell)),
+        })
+    s = _Out()
+    for name, _ in FIELDS:
+        setattr(s, name, out[name].ctypes.data if name in out else None)
+    return out, s
+
+
+def _run(fn_name: str, so: str, mix, p, t, z, threads: int, sens: bool):
+    tc, pc, omega, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    z = np.ascontiguousarray(z, dtype=np.float64)
+    n, ncell = z.shape
+    out, s = _alloc(n, ncell, sens)
+    fn = getattr(_lib(so), fn_name)
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 4 + [ctypes.c_int64] + [ctypes.c_void_p] * 3 + \
+        [ctypes.c_int, ctypes.c_int, ctypes.POINTER(_Out)]
+    rc = fn(n, tc.ctypes.data, pc.ctypes.data, omega.ctypes.data, kij.ctypes.data, ncell,
+            p.ctypes.data, t.ctypes.data, z.ctypes.data, threads, int(sens), ctypes.byref(s))
+    if rc != 0:
+        raise RuntimeError(f"{fn_name} returned {rc}")
+    return out
+
+
+def flash(mix, p, t, z, threads: int = 1, sens: bool = False):
+    """CPU restatement of the reference flash; see oracle/pr76_flash_oracle.cpp."""
+    build()
+    return _run("oracle_flash_batch", ORACLE_SO, mix, p, t, z, threads, sens)
+
+
+def reference_flash(mix, p, t, z, threads: int = 1, sens: bool = False):
+    """The reference headers themselves (only where they were compiled)."""
+    if not reference_available():
+        raise FileNotFoundError(REF_SO)
+    return _run("ref_flash_batch", REF_SO, mix, p, t, z, threads, sens)
+
+
+def reference_backend(mix, p, t, z, threads: int = 1):
+    """Pr76PtFlashBackend::solve per cell: (PtPhaseSetStatus, accepted phase count)."""
+    tc, pc, omega, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
+    z = np.ascontiguousarray(z, dtype=np.float64)
+    n, ncell = z.shape
+    status = np.empty(ncell, np.int32)
+    count = np.empty(ncell, np.int32)
+    fn = _lib(REF_SO).ref_backend_batch
+    fn.restype = ctypes.c_int
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    fn(ctypes.c_int(n), *(ctypes.c_void_p(a.ctypes.data) for a in (tc, pc, omega, kij)), ctypes.c_int64(ncell),
+       *(ctypes.c_void_p(a.ctypes.data) for a in (p, t, z)), ctypes.c_int(threads),
+       ctypes.c_void_p(status.ctypes.data), ctypes.c_void_p(count.ctypes.data))
+    return status, count

@@ -1,0 +1,275 @@
+// Harness around the UNMODIFIED MPMC_HNU reference headers (test
+// infrastructure).  oracle/Makefile compiles this file against the reference
+// include directories where they lie and writes oracle/_ref/libpr76_ref.so.
+// It exposes the same C interface as oracle/pr76_flash_oracle.cpp
+// (ref_flash_batch <-> oracle_flash_batch) so that tests can compare the CPU
+// restatement with the reference on identical inputs, and so that
+// tests/golden/make_golden.py can record reference outputs as fixtures.
+//
+// Reference entry points used:
+//   mpmc::flash::solve_pr76_pt_vle                 modules/flash/include/mpmc/flash/pr76_split.hpp:99
+//   mpmc::flash::differentiate_pr76_pt_vle         modules/flash/include/mpmc/flash/pr76_sensitivity.hpp:51
+//   mpmc::physics::build_pr76_pt_vle_closure       modules/physics/include/mpmc/physics/pr76_thermodynamic_closure.hpp:148
+//   mpmc::thermodynamics::Pr76PhaseAdWorkspace     modules/thermodynamics/include/mpmc/thermodynamics/pr76_phase_ad.hpp:43
+//   mpmc::flash::Pr76PtFlashBackend::solve         modules/flash/include/mpmc/flash/pr76_pt_flash_backend.hpp:190
+
+#include <mpmc/flash/pr76_pt_flash_backend.hpp>
+#include <mpmc/flash/pr76_sensitivity.hpp>
+#include <mpmc/physics/pr76_thermodynamic_closure.hpp>
+#include <mpmc/thermodynamics/pr76_phase_ad.hpp>
+
+#include <cmath>
+#include <cstdint>
+#include <limits>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace {
+namespace fl = mpmc::flash;
+namespace th = mpmc::thermodynamics;
+namespace ph = mpmc::physics;
+
+th::Provenance synthetic_source() {
+    th::Provenance p;
+    p.kind = th::SourceKind::synthetic_test;
+    p.reference = "mpmc-gb300-synthetic";
+    p.revision = "v1";
+    p.locator = "seeded generator";
+    p.note = "synthetic mixture for GPU parity tests";
+    p.acquisition = "generated";
+    p.usage_terms = "test data";
+    return p;
+}
+
+th::PrParameterSet make_parameters(int n, const double* tc, const double* pc, const double* omega,
+                                   const double* kij, std::vector<std::string>& order) {
+    const auto src = synthetic_source();
+    std::vector<th::Component> catalog;
+    th::PrParameterInput input;
+    input.model_id = std::string(th::pr76_profile);
+    input.dataset_id = "synthetic";
+    input.revision = "v1";
+    input.applicability = {std::nullopt, std::nullopt, src};
+    order.clear();
+    for (int i = 0; i < n; ++i) {
+        const std::string id = "c" + std::to_string(i);
+        order.push_back(id);
+        catalog.push_back({id, id, th::ComponentKind::pure, src, {}});
+        input.pure.push_back({id, th::SourcedScalar{tc[i], th::Unit::kelvin, src, "K", "identity"},
+                              th::SourcedScalar{pc[i], th::Unit::pascal, src, "Pa", "identity"},
+                              th::SourcedScalar{omega[i], th::Unit::dimensionless, src, "1", "identity"}});
+    }
+    for (int i = 0; i < n; ++i)
+        for (int j = i + 1; j < n; ++j)
+            input.binary.push_back({order[i], order[j],
+                                    th::SourcedScalar{kij[i * n + j], th::Unit::dimensionless, src, "1",
+                                                      "identity"}});
+    return th::PrParameterSet::create(catalog, order, input, th::DataPolicy::allow_synthetic_tests);
+}
+
+int status_code(fl::PtSplitStatus s) {
+    switch (s) {
+    case fl::PtSplitStatus::single_phase_no_instability_found: return 0;
+    case fl::PtSplitStatus::two_phase_no_instability_found: return 1;
+    case fl::PtSplitStatus::phase_set_unstable: return 2;
+    case fl::PtSplitStatus::indeterminate: return 3;
+    }
+    return 3;
+}
+}  // namespace
+
+extern "C" {
+
+struct OracleOutputs {
+    int32_t* status;
+    double* beta;
+    double* x;
+    double* y;
+    double* ln_k;
+    double* ln_phi_l;
+    double* ln_phi_v;
+    double* z_l;
+    double* z_v;
+    int64_t* counters;
+    int32_t* sens_status;
+    double* dlnk;
+    double* dbeta;
+    double* dx;
+    double* dy;
+    double* dzl;
+    double* dzv;
+    double* drhol;
+    double* drhov;
+    double* jl;
+    double* jv;
+};
+
+int ref_flash_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                    int64_t ncell, const double* p, const double* t, const double* z, int threads,
+                    int want_sensitivity, const OracleOutputs* o) {
+    std::vector<std::string> order;
+    const th::PrParameterSet params = make_parameters(n, tc, pc, omega, kij, order);
+    const auto model = th::Pr76Phase<double>::from_parameters(params);
+    const double nan = std::numeric_limits<double>::quiet_NaN();
+    auto run = [&](int64_t lo, int64_t hi) {
+        fl::Pr76VleEvaluator evaluator(model);
+        for (int64_t c = lo; c < hi; ++c) {
+            auto put = [&](double* arr, int k, double v) {
+                if (arr) arr[k * ncell + c] = v;
+            };
+            std::vector<double> feed(n);
+            for (int i = 0; i < n; ++i) feed[i] = z[i * ncell + c];
+            fl::Pr76PtSplitResult split;
+            bool invalid = false;
+            try {
+                split = fl::solve_pr76_pt_vle(p[c], t[c], feed, evaluator);
+            } catch (const std::exception&) {
+                invalid = true;
+            }
+            const int st = invalid ? -1 : status_code(split.solution.status);
+            if (o->status) o->status[c] = st;
+            const fl::PtSplitState* cand = invalid ? nullptr : split.solution.candidate();
+            const bool pair = cand != nullptr && st != 0;
+            put(o->beta, 0, pair ? cand->fractions.vapor_fraction : nan);
+            double zl = nan;
+            if (!invalid && st == 0) {
+                // Z of the minimum-Gibbs feed branch (the reference's generic
+                // stability phase carries only its branch index).
+                th::Pr76PhaseWorkspace<double> ws;
+                const auto& ref = *split.solution.initial_stability.reference;
+                zl = model.evaluate_full(p[c], t[c], std::span<const double>{split.solution.initial_stability.feed},
+                                         ref.branch, ws)
+                         .z;
+            }
+            for (int i = 0; i < n; ++i) {
+                if (pair) {
+                    put(o->x, i, cand->fractions.liquid[i]);
+                    put(o->y, i, cand->fractions.vapor[i]);
+                    put(o->ln_k, i, cand->log_k[i]);
+                    put(o->ln_phi_l, i, cand->liquid.activity.ln_phi[i]);
+                    put(o->ln_phi_v, i, cand->vapor.activity.ln_phi[i]);
+                } else if (st == 0) {
+                    put(o->x, i, split.solution.initial_stability.feed[i]);
+                    put(o->y, i, nan);
+                    put(o->ln_k, i, nan);
+                    put(o->ln_phi_l, i, split.solution.initial_stability.reference->ln_phi[i]);
+                    put(o->ln_phi_v, i, nan);
+                } else {
+                    for (double* arr : {o->x, o->y, o->ln_k, o->ln_phi_l, o->ln_phi_v}) put(arr, i, nan);
+                }
+            }
+            put(o->z_l, 0, pair ? cand->liquid.z : zl);
+            put(o->z_v, 0, pair ? cand->vapor.z : nan);
+            if (o->counters) {
+                int64_t cnt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+                if (!invalid) {
+                    cnt[0] = static_cast<int64_t>(split.solution.initial_stability.evaluations);
+                    cnt[1] = static_cast<int64_t>(split.solution.split_evaluations);
+                    cnt[2] = split.solution.final_stability
+                                 ? static_cast<int64_t>(split.solution.final_stability->evaluations)
+                                 : 0;
+                    for (const auto& a : split.solution.attempts) cnt[3] += a.iterations;
+                    cnt[6] = static_cast<int64_t>(split.solution.attempts.size());
+                    for (const auto& tr : split.solution.initial_stability.trials) cnt[7] += tr.iterations;
+                    if (split.solution.final_stability)
+                        for (const auto& tr : split.solution.final_stability->trials) cnt[7] += tr.iterations;
+                }
+                for (int k = 0; k < 8; ++k) o->counters[k * ncell + c] = cnt[k];
+            }
+            if (!want_sensitivity) continue;
+            const int q = n + 1;
+            int sstat = 1;
+            std::vector<double> dlnk, dx, dy, dbeta, dzl, dzv, drl, drv, jl, jv;
+            if (!invalid && st == 1) {
+                const auto sens = fl::differentiate_pr76_pt_vle(split, evaluator);
+                sstat = static_cast<int>(sens.sensitivity.status);
+                if (sstat == 0) {
+                    dlnk = sens.sensitivity.log_k_jacobian;
+                    dx = sens.sensitivity.liquid_jacobian;
+                    dy = sens.sensitivity.vapor_jacobian;
+                    dbeta = sens.sensitivity.vapor_fraction_gradient;
+                    const auto closure = ph::build_pr76_pt_vle_closure(split, evaluator);
+                    if (closure.linearization) {
+                        dzl = closure.linearization->liquid_compressibility_gradient;
+                        dzv = closure.linearization->vapor_compressibility_gradient;
+                        drl = closure.linearization->liquid_molar_density_gradient;
+                        drv = closure.linearization->vapor_molar_density_gradient;
+                    }
+                    th::Pr76PhaseAdWorkspace<double, 4> ad;
+                    const auto lj = ad.value_and_jacobian_full(model, p[c], t[c], cand->fractions.liquid,
+                                                               cand->liquid.activity.branch);
+                    const auto vj = ad.value_and_jacobian_full(model, p[c], t[c], cand->fractions.vapor,
+                                                               cand->vapor.activity.branch);
+                    jl = lj.jacobian;
+                    jv = vj.jacobian;
+                }
+            }
+            if (o->sens_status) o->sens_status[c] = sstat;
+            auto copy = [&](double* arr, const std::vector<double>& v, int count) {
+                for (int k = 0; k < count; ++k) put(arr, k, k < static_cast<int>(v.size()) ? v[k] : nan);
+            };
+            copy(o->dlnk, dlnk, n * q);
+            copy(o->dx, dx, n * q);
+            copy(o->dy, dy, n * q);
+            copy(o->dbeta, dbeta, q);
+            copy(o->dzl, dzl, q);
+            copy(o->dzv, dzv, q);
+            copy(o->drhol, drl, q);
+            copy(o->drhov, drv, q);
+            copy(o->jl, jl, (n + 1) * (n + 2));
+            copy(o->jv, jv, (n + 1) * (n + 2));
+        }
+    };
+    if (threads < 1) threads = 1;
+    if (threads > ncell) threads = static_cast<int>(ncell > 0 ? ncell : 1);
+    std::vector<std::thread> pool;
+    const int64_t chunk = (ncell + threads - 1) / threads;
+    for (int k = 0; k < threads; ++k) {
+        const int64_t lo = k * chunk, hi = std::min<int64_t>(ncell, lo + chunk);
+        if (lo < hi) pool.emplace_back(run, lo, hi);
+    }
+    for (auto& th : pool) th.join();
+    return 0;
+}
+
+// The reference's unified backend entry point (max-3-phase orchestration),
+// returning only the published status and phase count per cell; used for
+// timing and to count cells that leave the two-phase path.
+int ref_backend_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                      int64_t ncell, const double* p, const double* t, const double* z, int threads,
+                      int32_t* status, int32_t* phase_count) {
+    std::vector<std::string> order;
+    const th::PrParameterSet params = make_parameters(n, tc, pc, omega, kij, order);
+    const auto model = th::Pr76Phase<double>::from_parameters(params);
+    auto run = [&](int64_t lo, int64_t hi) {
+        fl::Pr76VleEvaluator evaluator(model);
+        fl::Pr76PtFlashBackend backend(evaluator);
+        for (int64_t c = lo; c < hi; ++c) {
+            fl::PtFlashRequest req;
+            req.pressure_pa = p[c];
+            req.temperature_k = t[c];
+            req.feed.resize(n);
+            for (int i = 0; i < n; ++i) req.feed[i] = z[i * ncell + c];
+            try {
+                const auto r = backend.solve(req);
+                status[c] = static_cast<int32_t>(r.solution.status);
+                phase_count[c] = static_cast<int32_t>(r.solution.accepted_phase_count());
+            } catch (const std::exception&) {
+                status[c] = -1;
+                phase_count[c] = 0;
+            }
+        }
+    };
+    if (threads < 1) threads = 1;
+    std::vector<std::thread> pool;
+    const int64_t chunk = (ncell + threads - 1) / threads;
+    for (int k = 0; k < threads; ++k) {
+        const int64_t lo = k * chunk, hi = std::min<int64_t>(ncell, lo + chunk);
+        if (lo < hi) pool.emplace_back(run, lo, hi);
+    }
+    for (auto& th : pool) th.join();
+    return 0;
+}
+
+}  // extern "C"
