@@ -1,0 +1,175 @@
+/*
+ * mpmc_gb300_flash.h -- C ABI of the GB300 PR76 two-phase PT flash.
+ *
+ * This is the drop-in boundary for MPMC_HNU's unified flash backend.  In the
+ * reference, callers reach the per-cell flash through the virtual
+ *   mpmc::flash::PtFlashBackend::solve(const PtFlashRequest&)
+ *     (modules/flash/include/mpmc/flash/pt_flash_backend.hpp:187-195)
+ * implemented by
+ *   mpmc::flash::Pr76PtFlashBackend
+ *     (modules/flash/include/mpmc/flash/pr76_pt_flash_backend.hpp:177-282),
+ * one request (= one cell) at a time.  The entry points below take a whole
+ * batch of cells of one mixture in structure-of-arrays form, solve them on one
+ * GPU, and return the per-cell phase-set status, phase fractions, compositions,
+ * ln K, ln phi, Z and, optionally, the implicit sensitivities of
+ *   mpmc::flash::differentiate_pr76_pt_vle
+ *     (modules/flash/include/mpmc/flash/pr76_sensitivity.hpp:51-390)
+ * plus the closure linearisation of
+ *   mpmc::physics::build_pr76_pt_vle_closure
+ *     (modules/physics/include/mpmc/physics/pr76_thermodynamic_closure.hpp:148-381).
+ * The C++ adapter mpmc_hnu_gb300/cpp/gpu_pr76_pt_flash_backend.hpp wraps this
+ * ABI behind the reference's PtFlashBackend interface.
+ *
+ * Conventions
+ *  - No exceptions cross this boundary; every function returns an
+ *    mpmc_status (0 = success).  mpmc_gpu_flash_last_error() describes the
+ *    most recent failure of the calling thread.
+ *  - Arrays are structure-of-arrays with the cell index fastest:
+ *    element k of cell c lives at a[k * n_cells + c].  Compositions have
+ *    k = component; Jacobians have k = row * columns + column.
+ *  - Every output pointer may be NULL (that output is skipped).
+ *  - Numerical failure of a cell is never an error of the call: it is that
+ *    cell's status (MPMC_FLASH_INDETERMINATE), exactly as the reference
+ *    publishes PtPhaseSetStatus::indeterminate.
+ *  - A handle owns device copies of one mixture's PR76 parameters and is not
+ *    reentrant: concurrent calls on one handle must be serialised by the
+ *    caller, as for the reference evaluators (pr76_split.hpp:16-18).
+ */
+#ifndef MPMC_GB300_FLASH_H
+#define MPMC_GB300_FLASH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPMC_GB300_FLASH_ABI_VERSION 1
+#define MPMC_MAX_COMPONENTS 20
+
+/* Return codes of the ABI functions. */
+typedef enum mpmc_status {
+    MPMC_OK = 0,
+    MPMC_ERR_INVALID_ARGUMENT = 1, /* reference: std::invalid_argument / length_error */
+    MPMC_ERR_DOMAIN = 2,           /* reference: std::domain_error (bad mixture data) */
+    MPMC_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+    MPMC_ERR_UNSUPPORTED = 4,      /* component count or option outside this build */
+    MPMC_ERR_TIMEOUT = 5           /* a bounded device wait gave up */
+} mpmc_status;
+
+/* Per-cell phase-set status, mirroring PtSplitStatus
+ * (modules/flash/include/mpmc/flash/pt_split.hpp:71-74). */
+enum {
+    MPMC_FLASH_SINGLE_PHASE = 0,    /* single_phase_no_instability_found: accepted, 1 phase */
+    MPMC_FLASH_TWO_PHASE = 1,       /* two_phase_no_instability_found:   accepted, 2 phases */
+    MPMC_FLASH_PHASE_SET_UNSTABLE = 2, /* final common-tangent review found a lower-Gibbs trial */
+    MPMC_FLASH_INDETERMINATE = 3,   /* finite search did not settle the phase set */
+    MPMC_FLASH_INVALID_REQUEST = -1 /* p, T or feed violate the request contract */
+};
+
+/* Algorithm forms (same fixed points, different execution). */
+enum {
+    MPMC_FORM_PLAIN_FP64 = 0, /* one thread per cell, reference algorithm in FP64 */
+    MPMC_FORM_BATCHED = 1,    /* persistent work-queue kernel, FP64 */
+    MPMC_FORM_MIXED = 2       /* work queue, FP32 bulk iterations + FP64 polish/decisions */
+};
+
+/* Work counters per cell (int32 rows of the counters array). */
+enum {
+    MPMC_COUNTER_INIT_EVALS = 0,   /* property evaluations, initial stability */
+    MPMC_COUNTER_SPLIT_EVALS = 1,  /* property evaluations, split attempts */
+    MPMC_COUNTER_FINAL_EVALS = 2,  /* property evaluations, final phase-set review */
+    MPMC_COUNTER_SPLIT_ITERS = 3,  /* accepted split iterations */
+    MPMC_COUNTER_RR_ITERS = 4,     /* Rachford-Rice iterations */
+    MPMC_COUNTER_ROOT_ITERS = 5,   /* cubic root iterations */
+    MPMC_COUNTER_ATTEMPTS = 6,     /* split attempts */
+    MPMC_COUNTER_TRIAL_ITERS = 7,  /* accepted TPD descent iterations */
+    MPMC_COUNTER_COUNT = 8
+};
+
+/* One mixture: PR76 pure-component data in component order and the
+ * row-major symmetric kij matrix (zero diagonal).  Mirrors the numeric
+ * content of mpmc::thermodynamics::PrParameterSet
+ * (modules/thermodynamics/include/mpmc/thermodynamics/pr_parameters.hpp:46-199). */
+typedef struct mpmc_pr76_mixture {
+    int32_t n_components;
+    const double* critical_temperature_k; /* [n] */
+    const double* critical_pressure_pa;   /* [n] */
+    const double* acentric_factor;        /* [n] */
+    const double* kij;                    /* [n*n] */
+} mpmc_pr76_mixture;
+
+typedef struct mpmc_flash_options {
+    int32_t form;              /* MPMC_FORM_* */
+    int32_t want_sensitivity;  /* nonzero: compute the implicit derivatives */
+    int32_t device;            /* CUDA device ordinal */
+    int32_t reserved;
+} mpmc_flash_options;
+
+/* Outputs; layout a[k * n_cells + c].  q = n + 1 reduced columns
+ * (p, T, z_0 .. z_{n-2}); the full chart of the per-phase ln phi Jacobians
+ * has n + 2 columns (p, T, x_0 .. x_{n-1}) and n + 1 rows (Z, ln phi_0..). */
+typedef struct mpmc_flash_outputs {
+    int32_t* status;          /* [n_cells]  MPMC_FLASH_* */
+    double* vapor_fraction;   /* [n_cells]  beta of the two-phase pair, NaN otherwise */
+    double* liquid;           /* [n*n_cells] x (single phase: the feed) */
+    double* vapor;            /* [n*n_cells] y */
+    double* ln_k;             /* [n*n_cells] ln(y/x) */
+    double* ln_phi_liquid;    /* [n*n_cells] (single phase: the feed phase) */
+    double* ln_phi_vapor;     /* [n*n_cells] */
+    double* z_liquid;         /* [n_cells]  (single phase: Z of the feed phase) */
+    double* z_vapor;          /* [n_cells] */
+    int32_t* counters;        /* [MPMC_COUNTER_COUNT*n_cells] */
+    int32_t* sensitivity_status; /* [n_cells] PtSensitivityStatus, 0 = success */
+    double* d_ln_k;           /* [n*q*n_cells] */
+    double* d_vapor_fraction; /* [q*n_cells] */
+    double* d_liquid;         /* [n*q*n_cells] */
+    double* d_vapor;          /* [n*q*n_cells] */
+    double* d_z_liquid;       /* [q*n_cells] */
+    double* d_z_vapor;        /* [q*n_cells] */
+    double* d_rho_liquid;     /* [q*n_cells] molar density gradient */
+    double* d_rho_vapor;      /* [q*n_cells] */
+    double* jac_liquid;       /* [(n+1)*(n+2)*n_cells] d[Z, ln phi]/d[p, T, x] */
+    double* jac_vapor;        /* [(n+1)*(n+2)*n_cells] */
+} mpmc_flash_outputs;
+
+typedef struct mpmc_gpu_flash mpmc_gpu_flash;
+
+/* Create a handle for one mixture on options->device.  Replaces constructing
+ * Pr76Phase/Pr76VleEvaluator/Pr76PtFlashBackend for a parameter snapshot
+ * (pr76_pt_flash_backend.hpp:179-183; pr76_split.hpp:21-23).  Validates the
+ * data the way PrParameterSet::create and Pr76Pure do (finite Tc > 0, Pc > 0,
+ * finite omega and kij, symmetric kij with zero diagonal). */
+int mpmc_gpu_flash_create(const mpmc_pr76_mixture* mixture, const mpmc_flash_options* options,
+                          mpmc_gpu_flash** out);
+
+/* Release the handle and its device memory. */
+int mpmc_gpu_flash_destroy(mpmc_gpu_flash* handle);
+
+/* Solve n_cells cells from HOST buffers and write HOST outputs; copies in and
+ * out inside the call and returns when the results are on the host.  The
+ * batched replacement of PtFlashBackend::solve (pt_flash_backend.hpp:193).
+ * p [n_cells] Pa, t [n_cells] K, z [n*n_cells] feed mole fractions. */
+int mpmc_gpu_flash_solve(mpmc_gpu_flash* handle, int64_t n_cells, const double* p, const double* t,
+                         const double* z, const mpmc_flash_outputs* out);
+
+/* Same, with every pointer (inputs and outputs) in DEVICE memory; enqueued
+ * on `stream` (a cudaStream_t, NULL = legacy default stream) and returns
+ * without synchronising.  Uses per-handle device scratch that it allocates on
+ * first use (and grows as needed). */
+int mpmc_gpu_flash_solve_device(mpmc_gpu_flash* handle, int64_t n_cells, const double* p, const double* t,
+                                const double* z, const mpmc_flash_outputs* out, void* stream);
+
+/* Number of components of the handle's mixture. */
+int mpmc_gpu_flash_components(const mpmc_gpu_flash* handle);
+
+/* Thread-local description of the last failure ("" if none). */
+const char* mpmc_gpu_flash_last_error(void);
+
+/* ABI version (MPMC_GB300_FLASH_ABI_VERSION). */
+int mpmc_gpu_flash_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MPMC_GB300_FLASH_H */

@@ -1,0 +1,314 @@
+// C ABI of the GB300 PR76 PT flash (include/mpmc_gb300_flash.h).
+//
+// Owns the per-mixture device state, validates requests the way the reference
+// contracts do, stages host buffers for the host-buffer entry point and
+// dispatches to the kernels of the selected algorithm form.  No exception
+// crosses the boundary; failures set a thread-local message.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "../../include/mpmc_gb300_flash.h"
+#include "launch.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& what) {
+    g_last_error = what;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+    return fail(MPMC_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+// Device buffer that only grows.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need) {
+        if (need <= bytes) return cudaSuccess;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        const cudaError_t e = cudaMalloc(&ptr, need);
+        if (e == cudaSuccess) bytes = need;
+        return e;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+};
+
+constexpr int kOutputFields = 21;
+
+}  // namespace
+
+struct mpmc_gpu_flash {
+    int n = 0;
+    int device = 0;
+    int form = MPMC_FORM_PLAIN_FP64;
+    int want_sensitivity = 0;
+    pr76::Mixture host_mixture{};
+    pr76::Mixture* d_mixture = nullptr;
+    cudaStream_t stream = nullptr;
+    DevBuf in_p, in_t, in_z;
+    DevBuf outs[kOutputFields];
+};
+
+namespace {
+
+// Build the prepared constants exactly as Pr76Pure's constructor does
+// (modules/thermodynamics/include/mpmc/thermodynamics/pr76_pure.hpp:181-199)
+// and the binary factors of Pr76Mixture (pr76_mixture.hpp:229-251).
+int prepare_mixture(const mpmc_pr76_mixture* mix, pr76::Mixture& m) {
+    const int n = mix->n_components;
+    if (n < 1 || n > MPMC_MAX_COMPONENTS)
+        return fail(MPMC_ERR_UNSUPPORTED, "component count must be in [1, " +
+                                              std::to_string(MPMC_MAX_COMPONENTS) + "]");
+    if (!mix->critical_temperature_k || !mix->critical_pressure_pa || !mix->acentric_factor || !mix->kij)
+        return fail(MPMC_ERR_INVALID_ARGUMENT, "mixture arrays must not be null");
+    std::memset(&m, 0, sizeof(m));
+    m.n = n;
+    for (int i = 0; i < n; ++i) {
+        const double tc = mix->critical_temperature_k[i];
+        const double pc = mix->critical_pressure_pa[i];
+        const double omega = mix->acentric_factor[i];
+        if (!std::isfinite(tc) || !(tc > 0) || !std::isfinite(pc) || !(pc > 0) || !std::isfinite(omega))
+            return fail(MPMC_ERR_DOMAIN, "component " + std::to_string(i) +
+                                             ": finite Tc > 0, Pc > 0 and finite omega required");
+        m.sqrt_tc[i] = std::sqrt(tc);
+        m.kappa[i] = 0.37464 + omega * (1.54226 - 0.26992 * omega);
+        const double rtc = pr76::kR * tc;
+        m.ac[i] = (0.45724 * rtc) * (rtc / pc);
+        m.b[i] = (0.07780 * rtc) / pc;
+        if (!std::isfinite(m.kappa[i]) || !std::isfinite(m.ac[i]) || !(m.ac[i] > 0) || !std::isfinite(m.b[i]) ||
+            !(m.b[i] > 0))
+            return fail(MPMC_ERR_DOMAIN, "component " + std::to_string(i) + ": coefficient outside range");
+    }
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) {
+            const double k = mix->kij[i * n + j];
+            if (!std::isfinite(k)) return fail(MPMC_ERR_DOMAIN, "kij must be finite");
+            if (i == j && k != 0.0) return fail(MPMC_ERR_DOMAIN, "kij diagonal must be zero");
+            if (k != mix->kij[j * n + i]) return fail(MPMC_ERR_DOMAIN, "kij must be symmetric");
+            m.factor[i * n + j] = 1.0 - k;
+        }
+    return MPMC_OK;
+}
+
+pr76::DeviceOutputs to_device_outputs(const mpmc_flash_outputs* o) {
+    pr76::DeviceOutputs d{};
+    if (!o) return d;
+    d.status = o->status;
+    d.beta = o->vapor_fraction;
+    d.x = o->liquid;
+    d.y = o->vapor;
+    d.lnk = o->ln_k;
+    d.lnphi_l = o->ln_phi_liquid;
+    d.lnphi_v = o->ln_phi_vapor;
+    d.z_l = o->z_liquid;
+    d.z_v = o->z_vapor;
+    d.counters = o->counters;
+    d.sens_status = o->sensitivity_status;
+    d.dlnk = o->d_ln_k;
+    d.dbeta = o->d_vapor_fraction;
+    d.dx = o->d_liquid;
+    d.dy = o->d_vapor;
+    d.dzl = o->d_z_liquid;
+    d.dzv = o->d_z_vapor;
+    d.drhol = o->d_rho_liquid;
+    d.drhov = o->d_rho_vapor;
+    d.jl = o->jac_liquid;
+    d.jv = o->jac_vapor;
+    return d;
+}
+
+// Element counts per cell of every output field, in mpmc_flash_outputs order.
+void field_sizes(int n, size_t* per_cell, size_t* elem) {
+    const size_t q = static_cast<size_t>(n) + 1;
+    const size_t counts[kOutputFields] = {1, 1, (size_t)n, (size_t)n, (size_t)n, (size_t)n, (size_t)n, 1, 1,
+                                          MPMC_COUNTER_COUNT, 1, n * q, q, n * q, n * q, q, q, q, q,
+                                          (n + 1) * (q + 1), (n + 1) * (q + 1)};
+    for (int k = 0; k < kOutputFields; ++k) {
+        per_cell[k] = counts[k];
+        elem[k] = (k == 0 || k == 9 || k == 10) ? 4 : 8;
+    }
+}
+
+void** field_ptr(mpmc_flash_outputs* o, int k) {
+    void** base = reinterpret_cast<void**>(o);
+    return base + k;
+}
+
+int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
+               const pr76::DeviceOutputs& d, cudaStream_t stream) {
+    cudaError_t e;
+    switch (h->form) {
+    case MPMC_FORM_PLAIN_FP64:
+        e = pr76::launch_plain(h->n, h->d_mixture, ncell, p, t, z, d, stream);
+        break;
+    default:
+        return fail(MPMC_ERR_UNSUPPORTED, "algorithm form not available in this build");
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "flash kernel launch");
+    return MPMC_OK;
+}
+
+}  // namespace
+
+namespace pr76 {
+LaunchShape plain_launch_shape() {
+    LaunchShape s{64, 2};
+    if (const char* v = std::getenv("MPMC_PLAIN_BLOCK")) s.block = std::atoi(v);
+    if (const char* v = std::getenv("MPMC_PLAIN_BLOCKS_PER_SM")) s.blocks_per_sm = std::atoi(v);
+    if (s.block != 32 && s.block != 64 && s.block != 128) s.block = 64;
+    if (s.blocks_per_sm < 1 || s.blocks_per_sm > 32) s.blocks_per_sm = 2;
+    return s;
+}
+
+int capacity_for(int n) {
+    if (n < 1) return 0;
+    if (n <= 4) return 4;
+    if (n <= 8) return 8;
+    if (n <= 12) return 12;
+    if (n <= 16) return 16;
+    if (n <= 20) return 20;
+    return 0;
+}
+
+cudaError_t launch_plain(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
+                         const double* z, const DeviceOutputs& out, cudaStream_t stream) {
+    switch (capacity_for(n)) {
+    case 4: return launch_plain_nm4(d_mix, ncell, p, t, z, out, stream);
+    case 8: return launch_plain_nm8(d_mix, ncell, p, t, z, out, stream);
+    case 12: return launch_plain_nm12(d_mix, ncell, p, t, z, out, stream);
+    case 16: return launch_plain_nm16(d_mix, ncell, p, t, z, out, stream);
+    case 20: return launch_plain_nm20(d_mix, ncell, p, t, z, out, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+}  // namespace pr76
+
+extern "C" {
+
+int mpmc_gpu_flash_abi_version(void) { return MPMC_GB300_FLASH_ABI_VERSION; }
+
+const char* mpmc_gpu_flash_last_error(void) { return g_last_error.c_str(); }
+
+int mpmc_gpu_flash_components(const mpmc_gpu_flash* h) { return h ? h->n : 0; }
+
+int mpmc_gpu_flash_create(const mpmc_pr76_mixture* mixture, const mpmc_flash_options* options,
+                          mpmc_gpu_flash** out) {
+    if (!mixture || !out) return fail(MPMC_ERR_INVALID_ARGUMENT, "mixture and out must not be null");
+    *out = nullptr;
+    mpmc_flash_options opt{};
+    if (options) opt = *options;
+    if (opt.form != MPMC_FORM_PLAIN_FP64 && opt.form != MPMC_FORM_BATCHED && opt.form != MPMC_FORM_MIXED)
+        return fail(MPMC_ERR_INVALID_ARGUMENT, "unknown algorithm form");
+    pr76::Mixture m;
+    const int rc = prepare_mixture(mixture, m);
+    if (rc != MPMC_OK) return rc;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDeviceCount");
+    if (opt.device < 0 || opt.device >= count) return fail(MPMC_ERR_INVALID_ARGUMENT, "device ordinal out of range");
+    e = cudaSetDevice(opt.device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    mpmc_gpu_flash* h = new mpmc_gpu_flash();
+    h->n = m.n;
+    h->device = opt.device;
+    h->form = opt.form;
+    h->want_sensitivity = opt.want_sensitivity;
+    h->host_mixture = m;
+    e = cudaMalloc(&h->d_mixture, sizeof(pr76::Mixture));
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_mixture, &m, sizeof(pr76::Mixture), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        mpmc_gpu_flash_destroy(h);
+        return cuda_fail(e, "mpmc_gpu_flash_create");
+    }
+    *out = h;
+    g_last_error.clear();
+    return MPMC_OK;
+}
+
+int mpmc_gpu_flash_destroy(mpmc_gpu_flash* h) {
+    if (!h) return MPMC_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    h->in_p.release();
+    h->in_t.release();
+    h->in_z.release();
+    for (auto& b : h->outs) b.release();
+    if (h->d_mixture) cudaFree(h->d_mixture);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return MPMC_OK;
+}
+
+int mpmc_gpu_flash_solve_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t,
+                                const double* z, const mpmc_flash_outputs* out, void* stream) {
+    if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
+    if (ncell < 0) return fail(MPMC_ERR_INVALID_ARGUMENT, "negative cell count");
+    if (ncell == 0) return MPMC_OK;
+    if (!p || !t || !z) return fail(MPMC_ERR_INVALID_ARGUMENT, "p, t and z must not be null");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    return run_device(h, ncell, p, t, z, to_device_outputs(out), static_cast<cudaStream_t>(stream));
+}
+
+int mpmc_gpu_flash_solve(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
+                         const mpmc_flash_outputs* out) {
+    if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
+    if (ncell < 0) return fail(MPMC_ERR_INVALID_ARGUMENT, "negative cell count");
+    if (ncell == 0) return MPMC_OK;
+    if (!p || !t || !z) return fail(MPMC_ERR_INVALID_ARGUMENT, "p, t and z must not be null");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    const size_t nc = static_cast<size_t>(ncell);
+    const size_t n = static_cast<size_t>(h->n);
+    if ((e = h->in_p.ensure(nc * 8)) != cudaSuccess || (e = h->in_t.ensure(nc * 8)) != cudaSuccess ||
+        (e = h->in_z.ensure(n * nc * 8)) != cudaSuccess)
+        return cuda_fail(e, "input staging allocation");
+    size_t per_cell[kOutputFields], elem[kOutputFields];
+    field_sizes(h->n, per_cell, elem);
+    mpmc_flash_outputs host_out{};
+    if (out) host_out = *out;
+    mpmc_flash_outputs dev_out{};
+    for (int k = 0; k < kOutputFields; ++k) {
+        void* hp = *field_ptr(&host_out, k);
+        if (!hp) continue;
+        if ((e = h->outs[k].ensure(per_cell[k] * elem[k] * nc)) != cudaSuccess)
+            return cuda_fail(e, "output staging allocation");
+        *field_ptr(&dev_out, k) = h->outs[k].ptr;
+    }
+    cudaStream_t s = h->stream;
+    if ((e = cudaMemcpyAsync(h->in_p.ptr, p, nc * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(h->in_t.ptr, t, nc * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(h->in_z.ptr, z, n * nc * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "input copy");
+    const int rc = run_device(h, ncell, static_cast<const double*>(h->in_p.ptr),
+                              static_cast<const double*>(h->in_t.ptr), static_cast<const double*>(h->in_z.ptr),
+                              to_device_outputs(&dev_out), s);
+    if (rc != MPMC_OK) return rc;
+    for (int k = 0; k < kOutputFields; ++k) {
+        void* hp = *field_ptr(&host_out, k);
+        if (!hp) continue;
+        if ((e = cudaMemcpyAsync(hp, h->outs[k].ptr, per_cell[k] * elem[k] * nc, cudaMemcpyDeviceToHost, s)) !=
+            cudaSuccess)
+            return cuda_fail(e, "output copy");
+    }
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "flash execution");
+    return MPMC_OK;
+}
+
+}  // extern "C"

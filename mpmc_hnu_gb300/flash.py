@@ -1,0 +1,162 @@
+"""Python binding of the C ABI in include/mpmc_gb300_flash.h (ctypes).
+
+`GpuFlash` mirrors the reference's per-mixture backend object
+(mpmc::flash::Pr76PtFlashBackend, modules/flash/include/mpmc/flash/
+pr76_pt_flash_backend.hpp:177-282) for a batch of cells: construct it once per
+mixture, then call `solve()` with host arrays (copies in and out inside the
+call) or `solve_device()` with device pointers on a CUDA stream.  The compiled
+library must exist: there is no CPU fallback, and a missing library raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_lib", "libmpmc_gb300_flash.so")
+
+FORM_PLAIN_FP64 = 0
+FORM_BATCHED = 1
+FORM_MIXED = 2
+FORMS = {"plain": FORM_PLAIN_FP64, "batched": FORM_BATCHED, "mixed": FORM_MIXED}
+
+SINGLE_PHASE, TWO_PHASE, PHASE_SET_UNSTABLE, INDETERMINATE, INVALID_REQUEST = 0, 1, 2, 3, -1
+COUNTER_NAMES = ["init_evals", "split_evals", "final_evals", "split_iters", "rr_iters", "root_iters",
+                 "attempts", "trial_iters"]
+MAX_COMPONENTS = 20
+
+
+class _Mixture(ctypes.Structure):
+    _fields_ = [("n_components", ctypes.c_int32), ("critical_temperature_k", ctypes.c_void_p),
+                ("critical_pressure_pa", ctypes.c_void_p), ("acentric_factor", ctypes.c_void_p),
+                ("kij", ctypes.c_void_p)]
+
+
+class _Options(ctypes.Structure):
+    _fields_ = [("form", ctypes.c_int32), ("want_sensitivity", ctypes.c_int32), ("device", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+# (field, dtype, rows(n)) in mpmc_flash_outputs order
+OUTPUT_FIELDS = [
+    ("status", np.int32, lambda n: 1), ("vapor_fraction", np.float64, lambda n: 1),
+    ("liquid", np.float64, lambda n: n), ("vapor", np.float64, lambda n: n),
+    ("ln_k", np.float64, lambda n: n), ("ln_phi_liquid", np.float64, lambda n: n),
+    ("ln_phi_vapor", np.float64, lambda n: n), ("z_liquid", np.float64, lambda n: 1),
+    ("z_vapor", np.float64, lambda n: 1), ("counters", np.int32, lambda n: 8),
+    ("sensitivity_status", np.int32, lambda n: 1), ("d_ln_k", np.float64, lambda n: n * (n + 1)),
+    ("d_vapor_fraction", np.float64, lambda n: n + 1), ("d_liquid", np.float64, lambda n: n * (n + 1)),
+    ("d_vapor", np.float64, lambda n: n * (n + 1)), ("d_z_liquid", np.float64, lambda n: n + 1),
+    ("d_z_vapor", np.float64, lambda n: n + 1), ("d_rho_liquid", np.float64, lambda n: n + 1),
+    ("d_rho_vapor", np.float64, lambda n: n + 1), ("jac_liquid", np.float64, lambda n: (n + 1) * (n + 2)),
+    ("jac_vapor", np.float64, lambda n: (n + 1) * (n + 2)),
+]
+FLASH_FIELDS = [f for f, _, _ in OUTPUT_FIELDS[:10]]
+SENSITIVITY_FIELDS = [f for f, _, _ in OUTPUT_FIELDS[10:]]
+
+
+class _Outputs(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_void_p) for f, _, _ in OUTPUT_FIELDS]
+
+
+EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu_flash_solve",
+                    "mpmc_gpu_flash_solve_device", "mpmc_gpu_flash_components", "mpmc_gpu_flash_last_error",
+                    "mpmc_gpu_flash_abi_version"]
+
+_LIB = None
+
+
+def library() -> ctypes.CDLL:
+    """Load the compiled library (raises if it was not built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} missing: run `python -m mpmc_hnu_gb300.build` (no CPU fallback)")
+        lib = ctypes.CDLL(LIB_PATH)
+        lib.mpmc_gpu_flash_create.argtypes = [ctypes.POINTER(_Mixture), ctypes.POINTER(_Options),
+                                              ctypes.POINTER(ctypes.c_void_p)]
+        lib.mpmc_gpu_flash_destroy.argtypes = [ctypes.c_void_p]
+        lib.mpmc_gpu_flash_solve.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 3 + \
+            [ctypes.POINTER(_Outputs)]
+        lib.mpmc_gpu_flash_solve_device.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 3 + \
+            [ctypes.POINTER(_Outputs), ctypes.c_void_p]
+        lib.mpmc_gpu_flash_components.argtypes = [ctypes.c_void_p]
+        for name in EXPORTED_SYMBOLS:
+            getattr(lib, name).restype = ctypes.c_int
+        lib.mpmc_gpu_flash_last_error.restype = ctypes.c_char_p
+        _LIB = lib
+    return _LIB
+
+
+class FlashError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"mpmc_gpu_flash error {code}: {message}")
+        self.code = code
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise FlashError(rc, library().mpmc_gpu_flash_last_error().decode())
+
+
+def output_rows(n: int) -> dict[str, int]:
+    return {f: rows(n) for f, _, rows in OUTPUT_FIELDS}
+
+
+class GpuFlash:
+    """One mixture on one GPU; batches of cells per call."""
+
+    def __init__(self, mixture, form: str | int = "plain", sensitivity: bool = False, device: int = 0):
+        self.mixture = mixture
+        self.n = int(mixture.n)
+        self.form = FORMS[form] if isinstance(form, str) else int(form)
+        self.sensitivity = bool(sensitivity)
+        self._keep = [np.ascontiguousarray(a, dtype=np.float64) for a in
+                      (mixture.tc, mixture.pc, mixture.omega, np.asarray(mixture.kij).reshape(-1))]
+        m = _Mixture(self.n, *(a.ctypes.data for a in self._keep))
+        o = _Options(self.form, int(self.sensitivity), device, 0)
+        h = ctypes.c_void_p()
+        _check(library().mpmc_gpu_flash_create(ctypes.byref(m), ctypes.byref(o), ctypes.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            library().mpmc_gpu_flash_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def fields(self, want_sensitivity: bool | None = None) -> list[str]:
+        sens = self.sensitivity if want_sensitivity is None else want_sensitivity
+        return FLASH_FIELDS + (SENSITIVITY_FIELDS if sens else [])
+
+    def solve(self, p, t, z, fields: list[str] | None = None) -> dict[str, np.ndarray]:
+        """Host arrays in, host arrays out (the copies happen inside the call)."""
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        z = np.ascontiguousarray(z, dtype=np.float64)
+        if z.shape != (self.n, p.shape[0]) or t.shape != p.shape:
+            raise ValueError("expected p[ncell], t[ncell], z[n, ncell]")
+        ncell = p.shape[0]
+        fields = fields or self.fields()
+        rows = output_rows(self.n)
+        dtypes = {f: d for f, d, _ in OUTPUT_FIELDS}
+        out = {f: np.empty((rows[f], ncell), dtypes[f]) for f in fields}
+        s = _Outputs(**{f: out[f].ctypes.data for f in fields})
+        _check(library().mpmc_gpu_flash_solve(self._h, ncell, p.ctypes.data, t.ctypes.data, z.ctypes.data,
+                                              ctypes.byref(s)))
+        return {f: (v[0] if rows[f] == 1 else v) for f, v in out.items()}
+
+    def solve_device(self, ncell: int, p_ptr: int, t_ptr: int, z_ptr: int, out_ptrs: dict[str, int],
+                     stream: int = 0) -> None:
+        """Device pointers in and out; enqueued on `stream` (no synchronisation)."""
+        s = _Outputs(**out_ptrs)
+        _check(library().mpmc_gpu_flash_solve_device(self._h, ncell, p_ptr, t_ptr, z_ptr, ctypes.byref(s),
+                                                     stream))
