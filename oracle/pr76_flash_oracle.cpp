@@ -1582,6 +1582,110 @@ inline void differentiate(const Model& m, const FlashResult& fr, double p, doubl
     }
 }
 
+// Index of the liquid (smallest) or vapor (largest) mechanically admissible
+// root at composition x, pr76_split.hpp:54-59; -1 if none.
+inline int role_branch(const Model& m, Work& wk, double p, double t, const double* x, bool vapor) {
+    double amix, bmix, A, B;
+    if (!mix(m, wk.tc, x, amix, bmix, wk.sums.data()) || !coefficients(p, t, amix, bmix, A, B)) return -1;
+    const RootSet roots = solve_roots(A, B);
+    if (roots.status != kRootSuccess) return -1;
+    int selected = -1;
+    for (int k = 0; k < roots.count; ++k) {
+        if (roots.roots[k].slope_sign <= 0) continue;
+        selected = k;
+        if (!vapor) break;
+    }
+    return selected;
+}
+
+// Newton polish of the two-phase equilibrium equations
+//   F_i(ln K) = ln x_i - ln y_i + ln phi_L,i(x) - ln phi_V,i(y) = 0
+// with x, y from Rachford-Rice and the liquid/vapor root roles of the split.
+// Test instrument only: two converged solutions of the same equilibrium
+// (each stopped at the reference's |F| <= 1e-11) polish to the same point, so
+// comparing polished states checks "same fixed point" independently of where
+// each iteration happened to stop.  dF/dlnK uses the RR linearisation of
+// detail/pt_sensitivity_detail.hpp:46-143 and forward-mode ln phi.  Returns
+// false if RR or a phase evaluation fails.
+inline bool polish(const Model& m, Work& wk, double p, double t, const std::vector<double>& z,
+                   std::vector<double>& lnk, double& beta, std::vector<double>& x, std::vector<double>& y,
+                   double& res_norm, double& ainv_norm) {
+    const int n = m.n;
+    res_norm = kNaN;
+    ainv_norm = kNaN;
+    for (int it = 0; it < 12; ++it) {
+        RrResult rr = solve_rr(z, lnk, wk);
+        if (rr.status != kRrInterior) return false;
+        beta = rr.beta;
+        x = rr.x;
+        y = rr.y;
+        const int bl = role_branch(m, wk, p, t, x.data(), false);
+        const int bv = role_branch(m, wk, p, t, y.data(), true);
+        if (bl < 0 || bv < 0) return false;
+        double h = 0;
+        for (int i = 0; i < n; ++i)
+            if (z[i] > 0) h += (y[i] - x[i]) * (y[i] - x[i]) / z[i];
+        std::vector<double> F(n), A(n * n);
+        for (int v = 0; v < n; ++v) {
+            double num = 0;
+            for (int i = 0; i < n; ++i)
+                if (z[i] > 0 && i == v) num += x[i] * y[i] / z[i];
+            const double dbeta = num / h;
+            std::vector<D1> xl(n), yv(n);
+            for (int i = 0; i < n; ++i) {
+                if (z[i] == 0) {
+                    xl[i] = D1(0.0);
+                    yv[i] = D1(0.0);
+                    continue;
+                }
+                const double dlk = i == v ? 1.0 : 0.0;
+                const double dlx = -((y[i] - x[i]) / z[i]) * dbeta - beta * (y[i] / z[i]) * dlk;
+                xl[i] = D1(x[i], x[i] * dlx);
+                yv[i] = D1(y[i], y[i] * (dlx + dlk));
+            }
+            D1 zl, zv;
+            std::vector<D1> pl, pv;
+            if (!phase_eval_ad(m, D1(p), D1(t), xl, bl, zl, pl) || !phase_eval_ad(m, D1(p), D1(t), yv, bv, zv, pv))
+                return false;
+            for (int i = 0; i < n; ++i) {
+                if (z[i] == 0) {
+                    F[i] = 0;
+                    A[i * n + v] = i == v ? 1.0 : 0.0;
+                    continue;
+                }
+                const D1 fi = log(xl[i]) - log(yv[i]) + pl[i] - pv[i];
+                F[i] = fi.v;
+                A[i * n + v] = fi.d;
+            }
+        }
+        double fn = 0;
+        for (double f : F) fn = std::max(fn, std::abs(f));
+        res_norm = fn;
+        Lu f;
+        if (!lu_factor(A, n, f)) return false;
+        const double rc = lu_rcond(f);
+        ainv_norm = rc > 0 ? 1.0 / (rc * f.norm_inf) : kNaN;
+        if (fn <= 4 * kEps) return true;
+        std::vector<double> d(n);
+        for (int i = 0; i < n; ++i) d[i] = -F[i];
+        if (!lu_solve(f, d)) return false;
+        for (int i = 0; i < n; ++i) lnk[i] += d[i];
+        if (it >= 4) {
+            double dn = 0;
+            for (double v : d) dn = std::max(dn, std::abs(v));
+            if (dn <= 1e-15 * 16) {
+                RrResult r2 = solve_rr(z, lnk, wk);
+                if (r2.status != kRrInterior) return false;
+                beta = r2.beta;
+                x = r2.x;
+                y = r2.y;
+                return true;
+            }
+        }
+    }
+    return true;
+}
+
 }  // namespace oracle
 
 // ===========================================================================
@@ -1732,6 +1836,54 @@ int oracle_stability_phase(int n, const double* tc, const double* pc, const doub
     *z_out = ph.z;
     *branch = ph.branch;
     *smooth = ph.smooth ? 1 : 0;
+    return 0;
+}
+
+// Newton-polish two-phase states (see oracle::polish) of `ncell` cells given
+// their ln K (layout [i*ncell + c]); cells with ok[c] == 0 are skipped.
+// Writes polished ln K, beta, x, y, the final max |F| and ||(dF/dlnK)^-1||_inf
+// (NaN where the polish failed).
+int oracle_polish_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                        int64_t ncell, const double* p, const double* t, const double* z, const int32_t* ok,
+                        const double* lnk_in, int threads, double* lnk_out, double* beta_out, double* x_out,
+                        double* y_out, double* res_out, double* ainv_out) {
+    using namespace oracle;
+    const Model m = make_model(n, tc, pc, omega, kij);
+    auto run = [&](int64_t lo, int64_t hi) {
+        Work wk;
+        wk.init(n);
+        for (int64_t c = lo; c < hi; ++c) {
+            for (int i = 0; i < n; ++i) lnk_out[i * ncell + c] = x_out[i * ncell + c] = y_out[i * ncell + c] = kNaN;
+            beta_out[c] = res_out[c] = ainv_out[c] = kNaN;
+            if (!ok[c]) continue;
+            std::vector<double> zz(n), lk(n), x, y;
+            double sum = 0, cs = 0;
+            for (int i = 0; i < n; ++i) kahan_add(z[i * ncell + c], sum, cs);
+            for (int i = 0; i < n; ++i) {
+                zz[i] = z[i * ncell + c] / sum;
+                lk[i] = zz[i] > 0 ? lnk_in[i * ncell + c] : 0.0;
+            }
+            if (!make_temp_cache(m, t[c], wk.tc)) continue;
+            double beta, res, ainv;
+            if (!polish(m, wk, p[c], t[c], zz, lk, beta, x, y, res, ainv)) continue;
+            for (int i = 0; i < n; ++i) {
+                lnk_out[i * ncell + c] = lk[i];
+                x_out[i * ncell + c] = x[i];
+                y_out[i * ncell + c] = y[i];
+            }
+            beta_out[c] = beta;
+            res_out[c] = res;
+            ainv_out[c] = ainv;
+        }
+    };
+    if (threads < 1) threads = 1;
+    std::vector<std::thread> pool;
+    const int64_t chunk = (ncell + threads - 1) / threads;
+    for (int k = 0; k < threads; ++k) {
+        const int64_t lo = k * chunk, hi = std::min<int64_t>(ncell, lo + chunk);
+        if (lo < hi) pool.emplace_back(run, lo, hi);
+    }
+    for (auto& th : pool) th.join();
     return 0;
 }
 

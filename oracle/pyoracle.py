@@ -126,3 +126,28 @@ def reference_backend(mix, p, t, z, threads: int = 1):
        *(ctypes.c_void_p(a.ctypes.data) for a in (p, t, z)), ctypes.c_int(threads),
        ctypes.c_void_p(status.ctypes.data), ctypes.c_void_p(count.ctypes.data))
     return status, count
+
+
+def polish(mix, p, t, z, ln_k, ok, threads: int = 8):
+    """Newton-polish two-phase states (test instrument, see oracle::polish).
+
+    Returns dict with polished ln_k, beta, x, y, residual (max |F|) and
+    ainv (||(dF/dlnK)^-1||_inf); NaN where skipped or failed."""
+    build()
+    tc, pc, omega, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
+    z = np.ascontiguousarray(z, dtype=np.float64)
+    n, ncell = z.shape
+    lk = np.ascontiguousarray(np.nan_to_num(np.asarray(ln_k, dtype=np.float64)))
+    okv = np.ascontiguousarray(np.asarray(ok, dtype=np.int32))
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    out = {"ln_k": np.empty((n, ncell)), "beta": np.empty(ncell), "x": np.empty((n, ncell)),
+           "y": np.empty((n, ncell)), "residual": np.empty(ncell), "ainv": np.empty(ncell)}
+    fn = _lib(ORACLE_SO).oracle_polish_batch
+    fn.restype = ctypes.c_int
+    args = [ctypes.c_int(n)] + [ctypes.c_void_p(a.ctypes.data) for a in (tc, pc, omega, kij)] + \
+        [ctypes.c_int64(ncell)] + [ctypes.c_void_p(a.ctypes.data) for a in (p, t, z, okv, lk)] + \
+        [ctypes.c_int(threads)] + [ctypes.c_void_p(out[k].ctypes.data) for k in
+                                   ("ln_k", "beta", "x", "y", "residual", "ainv")]
+    fn(*args)
+    return out

@@ -1,0 +1,164 @@
+"""The CPU oracle against the reference's golden vectors and recorded outputs.
+
+kat.json holds the reference test tree's independent Decimal-precision golden
+vectors (ternary split, binary boundary paths, sensitivities, closure);
+reference_outputs.npz holds outputs of the reference headers themselves on the
+same states and on seeded synthetic cells (tests/golden/make_golden.py).
+"""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from mpmc_hnu_gb300 import synth
+from tests import parity
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def kat():
+    with open(os.path.join(GOLDEN, "kat.json")) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="module")
+def recorded():
+    return dict(np.load(os.path.join(GOLDEN, "reference_outputs.npz")))
+
+
+class Mix:
+    def __init__(self, d):
+        self.tc = np.array(d["tc"], float)
+        self.pc = np.array(d["pc"], float)
+        self.omega = np.array(d["omega"], float)
+        self.kij = np.array(d["kij"], float)
+        self.n = len(self.tc)
+
+    def as_tuple(self):
+        return self.tc, self.pc, self.omega, self.kij
+
+
+def _run_cases(oracle_lib, kat, cases, sens=False):
+    out = []
+    for case in cases:
+        mix = Mix(kat["mixtures"][case["mixture"]])
+        z = np.array(case["feed"], float)[:, None]
+        res = oracle_lib.flash(mix, np.array([case["p"]]), np.array([case["t"]]), z, sens=sens)
+        out.append(res)
+    return out
+
+
+def test_oracle_flash_kats(oracle_lib, kat):
+    """Ternary split anchors and binary boundary paths (x, y, beta, Z)."""
+    results = _run_cases(oracle_lib, kat, kat["flash"])
+    checked = 0
+    for case, r in zip(kat["flash"], results):
+        status = int(r["status"][0])
+        if case["must"] == "two":
+            assert status == 1, case["name"]
+        elif case["must"] == "not_two":
+            assert status != 1, case["name"]
+        if status != 1 and case["must"] != "two":
+            continue
+        n = 1 if case.get("first_only") else len(case["x"])
+        for key, got in (("x", r["x"][:n, 0]), ("y", r["y"][:n, 0])):
+            exp = np.array(case[key][:n])
+            tol = case["abs_tol"] * ((1 + np.abs(exp)) if case["rel_scale"] else 1)
+            assert np.all(np.abs(got - exp) <= tol), (case["name"], key, got, exp)
+        for key, got in (("zl", r["z_l"][0]), ("zv", r["z_v"][0])):
+            exp = case[key]
+            tol = case["abs_tol"] * ((1 + abs(exp)) if case["rel_scale"] else 1)
+            assert abs(got - exp) <= tol, (case["name"], key, got, exp)
+        tol = case["beta_tol"] * ((1 + case["beta"]) if case["rel_scale"] else 1)
+        assert abs(r["beta"][0] - case["beta"]) <= tol, (case["name"], r["beta"][0], case["beta"])
+        checked += 1
+    assert checked >= 40
+
+
+def test_oracle_sensitivity_kats(oracle_lib, kat):
+    """Implicit sensitivities d(beta, ln K, x, y)/d(p, T, z_red): 2e-8 * max(1e-7, |e|)."""
+    for case, r in zip(kat["sensitivity"], _run_cases(oracle_lib, kat, kat["sensitivity"], sens=True)):
+        assert int(r["sens_status"][0]) == 0, case["name"]
+        n = len(case["feed"])
+        q = n + 1
+
+        def near(got, exp):
+            exp = np.asarray(exp, float)
+            return np.abs(got - exp) <= case["tol"] * np.maximum(1e-7, np.abs(exp))
+
+        assert np.all(near(r["dbeta"][:, 0], case["dbeta"])), case["name"]
+        for key in ("dlnk", "dx", "dy"):
+            got = r[key][:, 0].reshape(n, q)
+            assert np.all(near(got, case[key])), (case["name"], key)
+
+
+def test_oracle_closure_kats(oracle_lib, kat):
+    """Closure primal (Z_L, Z_V, rho_L, rho_V) and dZ, d(rho) gradients."""
+    R = 8.31446261815324
+    for case, r in zip(kat["closure"], _run_cases(oracle_lib, kat, kat["closure"], sens=True)):
+        zl, zv = r["z_l"][0], r["z_v"][0]
+        primal = [zl, zv, case["p"] / (zl * R * case["t"]), case["p"] / (zv * R * case["t"])]
+        for got, exp in zip(primal, case["primal"]):
+            assert abs(got - exp) <= case["primal_tol"] * (1 + abs(exp)), case["name"]
+        for key in ("dzl", "dzv", "drhol", "drhov"):
+            exp = np.array(case[key])
+            got = r[key][:, 0]
+            assert np.all(np.abs(got - exp) <= case["tol"] * np.maximum(1e-7, np.abs(exp))), (case["name"], key)
+
+
+def _compare_recorded(out, rec, prefix, mix=None, p=None, t=None, z=None):
+    ref = {k: rec[f"{prefix}_{k}"] for k in ("status", "beta", "x", "y", "ln_k", "ln_phi_l", "ln_phi_v",
+                                                 "z_l", "z_v")}
+    gpu_like = {"status": out["status"], **{g: out[r] for g, r in parity.FLASH_MAP.items()}}
+    rep = parity.flash_report(gpu_like, ref, mix, p, t, z)
+    parity.assert_flash_parity(rep)
+    return rep
+
+
+def test_oracle_matches_recorded_kat_states(oracle_lib, kat, recorded):
+    """Oracle == the reference headers on every KAT and dew-limit edge state."""
+    for name, d in kat["mixtures"].items():
+        mix = Mix(d)
+        p, t, z = (recorded[f"kat_{name}_{k}"] for k in ("p", "t", "z"))
+        out = oracle_lib.flash(mix, p, t, z, sens=True)
+        _compare_recorded(out, recorded, f"kat_{name}", mix, p, t, z)
+        # work counters of the search are reproduced exactly as well
+        cnt = recorded[f"kat_{name}_counters"]
+        for row in (0, 1, 2, 3, 6, 7):
+            assert np.array_equal(out["counters"][row], cnt[row]), (name, row)
+
+
+@pytest.mark.parametrize("n", [3, 4, 6, 10, 12, 20])
+def test_oracle_matches_recorded_synthetic(oracle_lib, recorded, n):
+    seed, ncell = (int(v) for v in recorded[f"synth_n{n}_seed"])
+    mix = synth.make_mixture(n, seed)
+    p, t, z = synth.make_cells(n, ncell, seed)
+    sens = f"synth_n{n}_dlnk" in recorded
+    out = oracle_lib.flash(mix, p, t, z, threads=4, sens=sens)
+    _compare_recorded(out, recorded, f"synth_n{n}", mix, p, t, z)
+    if sens:
+        ref = {k: recorded[f"synth_n{n}_{k}"] for k in ("sens_status",) + tuple(parity.SENS_MAP.values())}
+        gl = {"sensitivity_status": out["sens_status"], **{g: out[r] for g, r in parity.SENS_MAP.items()}}
+        rep = parity.sensitivity_report(gl, ref)
+        assert rep["status_match"] == 1.0
+        for g, v in rep["max"].items():
+            assert v <= parity.SENS_TOL, (g, rep)
+
+
+def test_oracle_bit_identical_to_reference_here(oracle_lib, recorded):
+    """Where the reference was compiled on this host, the oracle reproduces its
+    flash outputs bit for bit (same operation order, same libm)."""
+    from oracle import pyoracle
+
+    if not pyoracle.reference_available():
+        pytest.skip("reference sources not present on this host")
+    for n, ncell, seed in [(4, 64, 6), (10, 48, 2)]:
+        mix = synth.make_mixture(n, seed)
+        p, t, z = synth.make_cells(n, ncell, seed)
+        a = oracle_lib.flash(mix, p, t, z)
+        b = pyoracle.reference_flash(mix, p, t, z)
+        for k in ("status", "beta", "x", "y", "ln_k", "ln_phi_l", "ln_phi_v", "z_l", "z_v"):
+            assert np.array_equal(a[k], b[k], equal_nan=True), k
