@@ -25,7 +25,7 @@ PROBE_LIB = os.path.join(LIBDIR, "libmpmc_gb300_probe.so")
 
 CAPACITIES = (4, 8, 12, 16, 20)
 # translation units compiled once per capacity
-PER_CAPACITY = ("flash_plain.cu",)
+PER_CAPACITY = ("flash_plain.cu", "sensitivity.cu", "flash_batched.cu")
 # translation units compiled once
 SINGLE = ("capi.cu", "peak_probe.cu")
 

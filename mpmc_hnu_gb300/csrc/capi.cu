@@ -62,6 +62,8 @@ struct mpmc_gpu_flash {
     cudaStream_t stream = nullptr;
     DevBuf in_p, in_t, in_z;
     DevBuf outs[kOutputFields];
+    DevBuf sens_inputs[7];
+    DevBuf workspace;  // batched-form stage buffers and work queues
 };
 
 namespace {
@@ -149,17 +151,56 @@ void** field_ptr(mpmc_flash_outputs* o, int k) {
     return base + k;
 }
 
+// The sensitivity kernel reads the accepted pair back from the flash outputs;
+// fields the caller did not request are routed to per-handle scratch.
+int with_sensitivity_inputs(mpmc_gpu_flash* h, int64_t ncell, pr76::DeviceOutputs& d) {
+    const size_t nc = static_cast<size_t>(ncell), n = static_cast<size_t>(h->n);
+    struct Need {
+        void** field;
+        size_t bytes;
+    } needs[] = {{reinterpret_cast<void**>(&d.status), 4 * nc}, {reinterpret_cast<void**>(&d.beta), 8 * nc},
+                 {reinterpret_cast<void**>(&d.x), 8 * n * nc},  {reinterpret_cast<void**>(&d.y), 8 * n * nc},
+                 {reinterpret_cast<void**>(&d.lnk), 8 * n * nc}, {reinterpret_cast<void**>(&d.z_l), 8 * nc},
+                 {reinterpret_cast<void**>(&d.z_v), 8 * nc}};
+    for (int k = 0; k < 7; ++k) {
+        if (*needs[k].field) continue;
+        const cudaError_t e = h->sens_inputs[k].ensure(needs[k].bytes);
+        if (e != cudaSuccess) return cuda_fail(e, "sensitivity scratch allocation");
+        *needs[k].field = h->sens_inputs[k].ptr;
+    }
+    return MPMC_OK;
+}
+
 int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
-               const pr76::DeviceOutputs& d, cudaStream_t stream) {
+               const pr76::DeviceOutputs& d_in, cudaStream_t stream) {
+    pr76::DeviceOutputs d = d_in;
+    if (h->want_sensitivity) {
+        const int rc = with_sensitivity_inputs(h, ncell, d);
+        if (rc != MPMC_OK) return rc;
+    }
     cudaError_t e;
     switch (h->form) {
     case MPMC_FORM_PLAIN_FP64:
         e = pr76::launch_plain(h->n, h->d_mixture, ncell, p, t, z, d, stream);
         break;
+    case MPMC_FORM_MIXED: {
+        const size_t need = pr76::batched_workspace_bytes(h->n, ncell);
+        if ((e = h->workspace.ensure(need)) != cudaSuccess) return cuda_fail(e, "batched workspace allocation");
+        pr76::BatchedShape shape{0, 0};
+        if (const char* v = std::getenv("MPMC_TRIAL_BLOCKS_PER_SM")) shape.trial_blocks_per_sm = std::atoi(v);
+        if (const char* v = std::getenv("MPMC_SPLIT_BLOCKS_PER_SM")) shape.split_blocks_per_sm = std::atoi(v);
+        e = pr76::launch_batched(h->n, h->d_mixture, ncell, p, t, z, d, h->workspace.ptr, h->workspace.bytes, shape,
+                                 stream);
+        break;
+    }
     default:
         return fail(MPMC_ERR_UNSUPPORTED, "algorithm form not available in this build");
     }
     if (e != cudaSuccess) return cuda_fail(e, "flash kernel launch");
+    if (h->want_sensitivity) {
+        e = pr76::launch_sensitivity(h->n, h->d_mixture, ncell, p, t, z, d, stream);
+        if (e != cudaSuccess) return cuda_fail(e, "sensitivity kernel launch");
+    }
     return MPMC_OK;
 }
 
@@ -183,6 +224,42 @@ int capacity_for(int n) {
     if (n <= 16) return 16;
     if (n <= 20) return 20;
     return 0;
+}
+
+size_t batched_workspace_bytes(int n, int64_t ncell) {
+    switch (capacity_for(n)) {
+    case 4: return batched_workspace_bytes_nm4(n, ncell);
+    case 8: return batched_workspace_bytes_nm8(n, ncell);
+    case 12: return batched_workspace_bytes_nm12(n, ncell);
+    case 16: return batched_workspace_bytes_nm16(n, ncell);
+    case 20: return batched_workspace_bytes_nm20(n, ncell);
+    default: return 0;
+    }
+}
+
+cudaError_t launch_batched(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
+                           const double* z, const DeviceOutputs& out, void* scratch, size_t scratch_bytes,
+                           const BatchedShape& shape, cudaStream_t stream) {
+    switch (capacity_for(n)) {
+    case 4: return launch_batched_nm4(d_mix, n, ncell, p, t, z, out, scratch, scratch_bytes, shape, stream);
+    case 8: return launch_batched_nm8(d_mix, n, ncell, p, t, z, out, scratch, scratch_bytes, shape, stream);
+    case 12: return launch_batched_nm12(d_mix, n, ncell, p, t, z, out, scratch, scratch_bytes, shape, stream);
+    case 16: return launch_batched_nm16(d_mix, n, ncell, p, t, z, out, scratch, scratch_bytes, shape, stream);
+    case 20: return launch_batched_nm20(d_mix, n, ncell, p, t, z, out, scratch, scratch_bytes, shape, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
+                               const double* z, const DeviceOutputs& out, cudaStream_t stream) {
+    switch (capacity_for(n)) {
+    case 4: return launch_sensitivity_nm4(d_mix, ncell, p, t, z, out, stream);
+    case 8: return launch_sensitivity_nm8(d_mix, ncell, p, t, z, out, stream);
+    case 12: return launch_sensitivity_nm12(d_mix, ncell, p, t, z, out, stream);
+    case 16: return launch_sensitivity_nm16(d_mix, ncell, p, t, z, out, stream);
+    case 20: return launch_sensitivity_nm20(d_mix, ncell, p, t, z, out, stream);
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 cudaError_t launch_plain(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
@@ -214,6 +291,8 @@ int mpmc_gpu_flash_create(const mpmc_pr76_mixture* mixture, const mpmc_flash_opt
     if (options) opt = *options;
     if (opt.form != MPMC_FORM_PLAIN_FP64 && opt.form != MPMC_FORM_BATCHED && opt.form != MPMC_FORM_MIXED)
         return fail(MPMC_ERR_INVALID_ARGUMENT, "unknown algorithm form");
+    if (opt.form == MPMC_FORM_BATCHED)
+        return fail(MPMC_ERR_UNSUPPORTED, "the batched FP64 form is not part of this build; use MPMC_FORM_MIXED");
     pr76::Mixture m;
     const int rc = prepare_mixture(mixture, m);
     if (rc != MPMC_OK) return rc;
@@ -249,6 +328,8 @@ int mpmc_gpu_flash_destroy(mpmc_gpu_flash* h) {
     h->in_t.release();
     h->in_z.release();
     for (auto& b : h->outs) b.release();
+    for (auto& b : h->sens_inputs) b.release();
+    h->workspace.release();
     if (h->d_mixture) cudaFree(h->d_mixture);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;

@@ -1,0 +1,105 @@
+// Host orchestration of the batched mixed-precision flash (pr76_batched.cuh).
+// Compiled once per component capacity (-DMPMC_NM).  Every stage is enqueued
+// on one stream with fixed launch shapes; the work sizes live in device
+// counters, so the sequence needs no host synchronisation and can be
+// captured into a CUDA graph by the caller.
+#include "launch.h"
+#include "pr76_batched.cuh"
+
+#ifndef MPMC_NM
+#error "compile with -DMPMC_NM=<capacity>"
+#endif
+#define MPMC_CAT2(a, b) a##b
+#define MPMC_CAT(a, b) MPMC_CAT2(a, b)
+
+namespace pr76 {
+namespace MPMC_CAT(batched_host_nm, MPMC_NM) {
+
+constexpr int NM = MPMC_NM;
+
+size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
+
+// Carves the workspace arrays out of one scratch allocation; with base ==
+// nullptr only computes the size.
+size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell) {
+    const size_t nc = static_cast<size_t>(ncell);
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char* p = base ? base + off : nullptr;
+        off += align256(bytes);
+        return p;
+    };
+    ws.ncell = ncell;
+    ws.n = n;
+    ws.counters = reinterpret_cast<int*>(take(sizeof(int) * batched::qSlots));
+    ws.phase = reinterpret_cast<int*>(take(sizeof(int) * nc));
+    ws.trial_cells = reinterpret_cast<int*>(take(sizeof(int) * nc));
+    ws.attempt_items = reinterpret_cast<int*>(take(sizeof(int) * batched::kMaxAttempts * nc));
+    ws.z = reinterpret_cast<double*>(take(sizeof(double) * NM * nc));
+    ws.ref_lnphi = reinterpret_cast<double*>(take(sizeof(double) * NM * nc));
+    ws.ref_z = reinterpret_cast<double*>(take(sizeof(double) * nc));
+    ws.tw = reinterpret_cast<float*>(take(sizeof(float) * (NM + 4) * NM * nc));
+    ws.tclass = reinterpret_cast<signed char*>(take((NM + 4) * nc));
+    ws.att_lnk = reinterpret_cast<float*>(take(sizeof(float) * batched::kMaxAttempts * NM * nc));
+    ws.att_gibbs = reinterpret_cast<float*>(take(sizeof(float) * batched::kMaxAttempts * nc));
+    ws.att_class = reinterpret_cast<signed char*>(take(batched::kMaxAttempts * nc));
+    ws.att_count = reinterpret_cast<int*>(take(sizeof(int) * nc));
+    ws.cand = reinterpret_cast<double*>(take(sizeof(double) * 7 * NM * nc));
+    ws.cand_s = reinterpret_cast<double*>(take(sizeof(double) * 8 * nc));
+    ws.counters_out = reinterpret_cast<int*>(take(sizeof(int) * cCount * nc));
+    return off;
+}
+
+template <typename K>
+int resident_blocks(K kernel, int block) {
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kernel, block, 0) != cudaSuccess || blocks < 1) blocks = 1;
+    return blocks;
+}
+
+}  // namespace batched_host_nm<NM>
+using namespace MPMC_CAT(batched_host_nm, MPMC_NM);
+
+size_t MPMC_CAT(batched_workspace_bytes_nm, MPMC_NM)(int n, int64_t ncell) {
+    batched::Workspace ws;
+    return carve(ws, nullptr, n, ncell);
+}
+
+cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, int64_t ncell, const double* p,
+                                                   const double* t, const double* z, const DeviceOutputs& out,
+                                                   void* scratch, size_t scratch_bytes, const BatchedShape& shape,
+                                                   cudaStream_t stream) {
+    using namespace batched;
+    if (ncell <= 0) return cudaSuccess;
+    Workspace ws;
+    if (carve(ws, nullptr, n, ncell) > scratch_bytes || scratch == nullptr) return cudaErrorInvalidValue;
+    carve(ws, static_cast<char*>(scratch), n, ncell);
+    int device = 0, sms = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaError_t e = cudaMemsetAsync(ws.counters, 0, sizeof(int) * qSlots, stream);
+    if (e != cudaSuccess) return e;
+    const int cell_block = 64;
+    const int64_t cell_grid_max = static_cast<int64_t>(sms) * 8;
+    auto cell_grid = [&](int64_t items) {
+        int64_t g = (items + cell_block - 1) / cell_block;
+        return static_cast<unsigned>(g < cell_grid_max ? (g > 0 ? g : 1) : cell_grid_max);
+    };
+    const int qblock = 128;
+    const int trial_res = shape.trial_blocks_per_sm > 0 ? shape.trial_blocks_per_sm
+                                                        : resident_blocks(trials32_kernel<NM>, qblock);
+    const int split_res = shape.split_blocks_per_sm > 0 ? shape.split_blocks_per_sm
+                                                        : resident_blocks(split32_kernel<NM>, qblock);
+    setup_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, p, t, z, out);
+    trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 0);
+    decide_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+    split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t);
+    polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+    relist_kernel<NM><<<1, 1024, 0, stream>>>(ws);
+    trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 1);
+    finish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+    fallback_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, z, out);
+    return cudaGetLastError();
+}
+
+}  // namespace pr76

@@ -43,6 +43,20 @@ struct LaunchShape {
 };
 LaunchShape plain_launch_shape();
 
+// Persistent-kernel residency of the batched form (0 = from the occupancy
+// calculator).
+struct BatchedShape {
+    int trial_blocks_per_sm;
+    int split_blocks_per_sm;
+};
+
+// Batched mixed-precision flash (flash_batched.cu): scratch bytes needed for
+// ncell cells, and the launch sequence using that scratch.
+size_t batched_workspace_bytes(int n, int64_t ncell);
+cudaError_t launch_batched(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
+                           const double* z, const DeviceOutputs& out, void* scratch, size_t scratch_bytes,
+                           const BatchedShape& shape, cudaStream_t stream);
+
 // Smallest compiled component capacity >= n (0 if unsupported).
 int capacity_for(int n);
 
@@ -50,9 +64,20 @@ int capacity_for(int n);
 cudaError_t launch_plain(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
                          const double* z, const DeviceOutputs& out, cudaStream_t stream);
 
+// Implicit sensitivity of accepted two-phase cells (sensitivity.cu); reads the
+// flash fields of `out` (status, beta, x, y, lnk, z_l, z_v), which must be set.
+cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
+                               const double* z, const DeviceOutputs& out, cudaStream_t stream);
+
 #define MPMC_DECLARE_PLAIN(NM)                                                                         \
     cudaError_t launch_plain_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t, \
-                                    const double* z, const DeviceOutputs& out, cudaStream_t stream);
+                                    const double* z, const DeviceOutputs& out, cudaStream_t stream); \
+    cudaError_t launch_sensitivity_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t, \
+                                          const double* z, const DeviceOutputs& out, cudaStream_t stream); \
+    size_t batched_workspace_bytes_nm##NM(int n, int64_t ncell);                                              \
+    cudaError_t launch_batched_nm##NM(const Mixture* d_mix, int n, int64_t ncell, const double* p,            \
+                                      const double* t, const double* z, const DeviceOutputs& out, void* scratch, \
+                                      size_t scratch_bytes, const BatchedShape& shape, cudaStream_t stream);
 MPMC_DECLARE_PLAIN(4)
 MPMC_DECLARE_PLAIN(8)
 MPMC_DECLARE_PLAIN(12)

@@ -1,0 +1,975 @@
+// Batched mixed-precision PR76 flash: device workspace, work queues and the
+// stage kernels.
+//
+// Execution model (one stream, no host synchronisation between stages, so
+// the whole sequence can be captured in a CUDA graph):
+//   setup       per cell   FP64 feed phase (reference phase of the TPD test),
+//                          enqueue the cell's N+2 automatic TPD trials
+//   trials32    per trial  persistent FP32 TPD descent; each loop iteration
+//                          of every lane performs exactly one property
+//                          evaluation, lanes whose trial ended refill from
+//                          the queue, so warps stay full (work queue with
+//                          implicit compaction)
+//   decide      per cell   FP64 re-run of every trial FP32 could not decide;
+//                          phase-set decision of the feed test; enqueue split
+//                          attempts (witness order x {vapor, liquid}, <= 16)
+//   split32     per attempt persistent FP32 ln K successive substitution
+//   polish      per cell   minimum-Gibbs attempt, FP64 Newton polish of ln K
+//                          (FP64 residual, FP32 Jacobian: iterative
+//                          refinement), reference acceptance rules in FP64,
+//                          enqueue the N+4 common-tangent review trials
+//   trials32    per trial  review trials against the FP64 common tangent
+//   finish      per cell   FP64 re-run of undecided review trials, final
+//                          status, outputs
+//   fallback    per cell   cells flagged by any stage rerun the plain FP64
+//                          reference algorithm
+// The reference decisions these stages reproduce are cited in pr76_fp64.cuh.
+#pragma once
+
+#include "pr76_ad.cuh"
+#include "pr76_fp32.cuh"
+
+namespace pr76 {
+namespace batched {
+
+constexpr int kMaxAttempts = 16;
+
+// Queue/counter slots in Workspace::counters.
+enum Slot : int {
+    qTrialCells = 0,   // cells listed for the current trial stage
+    qTrialCursor = 1,  // next trial item to fetch
+    qAttempts = 2,     // attempt items listed
+    qAttemptCursor = 3,
+    qFallback = 4,     // cells listed for the FP64 fallback
+    qSlots = 8
+};
+
+// Cell phases kept in Workspace::phase.
+enum Phase : int {
+    pInvalid = -1, pSingle = 0, pTwo = 1, pUnstable = 2, pIndeterminate = 3,
+    pPending = 10, pSplit = 11, pReview = 12, pFallback = 13
+};
+
+// Device workspace for one batch (all arrays entry-major, cell fastest).
+struct Workspace {
+    int64_t ncell;
+    int n;
+    int* counters;          // [qSlots]
+    int* phase;             // [ncell]
+    int* trial_cells;       // [ncell] compacted cell list of the current trial stage
+    int* attempt_items;     // [kMaxAttempts * ncell] (cell << 5 | order)
+    double* z;              // [NM * ncell] normalised feed
+    double* ref_lnphi;      // [NM * ncell] feed phase ln phi (FP64)
+    double* ref_z;          // [ncell]
+    float* tw;              // [(NM+4) * NM * ncell] trial end compositions
+    signed char* tclass;    // [(NM+4) * ncell] trial classes
+    float* att_lnk;         // [kMaxAttempts * NM * ncell]
+    float* att_gibbs;       // [kMaxAttempts * ncell]
+    signed char* att_class; // [kMaxAttempts * ncell]
+    int* att_count;         // [ncell]
+    double* cand;           // [7 * NM * ncell]: x, y, lnk, lnphi_l, lnphi_v, common, imposed
+    double* cand_s;         // [8 * ncell]: beta, z_l, z_v, fug, gibbs_change, gibbs_guard, tpd_tol, spare
+    int* counters_out;      // [cCount * ncell] work counters (FP32 evaluations are in row 1/0/2)
+};
+
+__device__ __forceinline__ int64_t idx(int k, int64_t ncell, int64_t c) { return static_cast<int64_t>(k) * ncell + c; }
+
+// Number of automatic TPD starts for `active` components (pt_stability.hpp:254).
+__device__ __forceinline__ int auto_starts(int active) { return active == 1 ? 1 : active + 2; }
+
+// ---------------------------------------------------------------------------
+// Loading a cell's FP32 and FP64 context.
+template <int NM>
+__device__ bool load_cell32(const Mixture& m, const Workspace& ws, int64_t c, const double* p, const double* t,
+                            fp32::Cell<NM>& cf, int& active) {
+    cf.n = m.n;
+    cf.p = static_cast<float>(p[c]);
+    cf.t = static_cast<float>(t[c]);
+    cf.evals = 0;
+    active = 0;
+    for (int i = 0; i < cf.n; ++i) {
+        const double zi = ws.z[idx(i, ws.ncell, c)];
+        cf.z[i] = static_cast<float>(zi);
+        cf.lz[i] = zi > 0.0 ? static_cast<float>(log(zi)) : 0.f;
+        active += zi > 0.0;
+    }
+    return fp32::temp_setup(m, cf);
+}
+
+template <int NM>
+__device__ bool load_cell64(const Mixture& m, const Workspace& ws, int64_t c, const double* p, const double* t,
+                            fp64::Cell<NM>& c64) {
+    c64.n = m.n;
+    c64.p = p[c];
+    c64.t = t[c];
+    for (int k = 0; k < cCount; ++k) c64.counters[k] = 0;
+    for (int i = 0; i < c64.n; ++i) {
+        c64.z[i] = ws.z[idx(i, ws.ncell, c)];
+        c64.lz[i] = c64.z[i] > 0.0 ? log(c64.z[i]) : 0.0;
+    }
+    return fp64::temp_setup(m, c64);
+}
+
+// ---------------------------------------------------------------------------
+// Stage 1: per-cell setup and the FP64 feed phase.
+template <int NM>
+__global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ mix_g, Workspace ws,
+                                                    const double* __restrict__ p, const double* __restrict__ t,
+                                                    const double* __restrict__ z, DeviceOutputs out) {
+    __shared__ Mixture m;
+    stage_mixture(mix_g, m);
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; c < ws.ncell; c += stride) {
+        fp64::Cell<NM> cell;
+        cell.n = m.n;
+        cell.p = p[c];
+        cell.t = t[c];
+        for (int k = 0; k < cCount; ++k) cell.counters[k] = 0;
+        double feed[NM];
+        for (int i = 0; i < cell.n; ++i) feed[i] = z[idx(i, ws.ncell, c)];
+        int ph = pPending;
+        if (!isfinite(cell.p) || cell.p <= 0.0 || !isfinite(cell.t) || cell.t <= 0.0 ||
+            !fp64::normalise_feed(cell, feed) || !fp64::temp_setup(m, cell)) {
+            ph = pInvalid;
+        } else {
+            for (int i = 0; i < cell.n; ++i)
+                if (feed[i] > 0.0 && cell.z[i] == 0.0) ph = pIndeterminate;
+        }
+        for (int i = 0; i < cell.n; ++i) ws.z[idx(i, ws.ncell, c)] = ph == pInvalid ? 0.0 : cell.z[i];
+        if (ph == pPending) {
+            double lp[NM], zref = 0.0;
+            bool smooth;
+            const int is = fp64::stability_provider(m, cell, cell.z, lp, smooth, &zref, cInitEvals);
+            if (is != kOk) {
+                ph = is == kDomain ? pInvalid : pIndeterminate;
+            } else {
+                for (int i = 0; i < cell.n; ++i) ws.ref_lnphi[idx(i, ws.ncell, c)] = lp[i];
+                ws.ref_z[c] = zref;
+                // a nonsmooth feed reference makes every trial ambiguous: reference rules in FP64
+                if (!smooth) ph = pFallback;
+            }
+        }
+        ws.phase[c] = ph;
+        ws.att_count[c] = 0;
+        for (int k = 0; k < cCount; ++k) ws.counters_out[idx(k, ws.ncell, c)] = cell.counters[k];
+        if (ph == pInvalid || ph == pIndeterminate) {
+            const double nan = __longlong_as_double(0x7ff8000000000000LL);
+            if (out.status) out.status[c] = ph == pInvalid ? static_cast<int>(kInvalid) : static_cast<int>(kIndeterminate);
+            if (out.beta) out.beta[c] = nan;
+            for (int i = 0; i < cell.n; ++i) {
+                const int64_t k = idx(i, ws.ncell, c);
+                if (out.x) out.x[k] = nan;
+                if (out.y) out.y[k] = nan;
+                if (out.lnk) out.lnk[k] = nan;
+                if (out.lnphi_l) out.lnphi_l[k] = nan;
+                if (out.lnphi_v) out.lnphi_v[k] = nan;
+            }
+            if (out.z_l) out.z_l[c] = nan;
+            if (out.z_v) out.z_v[c] = nan;
+            if (out.counters)
+                for (int k = 0; k < cCount; ++k) out.counters[idx(k, ws.ncell, c)] = cell.counters[k];
+        }
+        if (ph == pPending) {
+            const int slot = atomicAdd(&ws.counters[qTrialCells], 1);
+            ws.trial_cells[slot] = static_cast<int>(c);
+        } else if (ph == pFallback) {
+            atomicAdd(&ws.counters[qFallback], 1);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Stage 2/6: FP32 TPD trials as a flat per-lane state machine.
+//
+// review == false: feed test, reference = feed phase, starts = automatic.
+// review == true:  common-tangent test, reference = imposed ln(x phi) of the
+//                  polished pair, starts = automatic + x + y.
+template <int NM>
+struct TrialLane {
+    fp32::Cell<NM> cell;
+    fp32::TpdPoint<NM> point, next;
+    float dir[NM], lnphi[NM], ref[NM], lrefs[2 * NM];
+    int nrefs;
+    int64_t item;
+    int c, k, iter, bt, stage;  // stage: 0 = evaluate start, 1 = line search, 2 = finished
+    float alpha, slope, scale;
+    int result;
+};
+
+template <int NM>
+__device__ void trial_begin(const Mixture& m, const Workspace& ws, const double* p, const double* t, bool review,
+                            int ntrial, TrialLane<NM>& L) {
+    const int64_t c = ws.trial_cells[L.item / ntrial];
+    const int k = static_cast<int>(L.item % ntrial);
+    L.c = static_cast<int>(c);
+    L.k = k;
+    L.iter = 0;
+    L.bt = 0;
+    L.stage = 0;
+    L.result = fp32::tMarginal;
+    int active;
+    if (!load_cell32(m, ws, c, p, t, L.cell, active)) {
+        L.stage = 2;
+        return;
+    }
+    const int n = L.cell.n;
+    const int n_auto = auto_starts(active);
+    if (k >= n_auto + (review ? 2 : 0)) {  // not a start of this cell (fewer active components)
+        L.result = fp32::tTangent;  // neutral: an unused slot
+        L.stage = 3;
+        return;
+    }
+    if (!review) {
+        for (int i = 0; i < n; ++i) L.ref[i] = static_cast<float>(ws.ref_lnphi[idx(i, ws.ncell, c)]);
+        L.nrefs = 1;
+        for (int i = 0; i < n; ++i) L.lrefs[i] = L.cell.lz[i];
+    } else {
+        // imposed reference ln phi_eq = common - ln z (pt_stability.hpp:319-322), stored in FP64
+        for (int i = 0; i < n; ++i) L.ref[i] = static_cast<float>(ws.cand[idx(6 * NM + i, ws.ncell, c)]);
+        L.nrefs = 2;
+        for (int i = 0; i < n; ++i) {
+            const double x = ws.cand[idx(0 * NM + i, ws.ncell, c)], y = ws.cand[idx(1 * NM + i, ws.ncell, c)];
+            L.lrefs[i] = x > 0.0 ? static_cast<float>(log(x)) : 0.f;
+            L.lrefs[NM + i] = y > 0.0 ? static_cast<float>(log(y)) : 0.f;
+        }
+    }
+    // start composition (pt_stability.hpp:294-311)
+    float* w = L.next.w;
+    if (k >= n_auto) {
+        const int which = k - n_auto;
+        for (int i = 0; i < n; ++i) w[i] = static_cast<float>(ws.cand[idx(which * NM + i, ws.ncell, c)]);
+    } else if (k == 0) {
+        for (int i = 0; i < n; ++i) w[i] = L.cell.z[i];
+    } else if (k == 1) {
+        for (int i = 0; i < n; ++i) w[i] = L.cell.z[i] > 0.f ? 1.f / static_cast<float>(active) : 0.f;
+    } else {
+        int target = k - 2, pick = 0;
+        for (int i = 0; i < n; ++i)
+            if (L.cell.z[i] > 0.f) {
+                if (target == 0) {
+                    pick = i;
+                    break;
+                }
+                --target;
+            }
+        for (int i = 0; i < n; ++i) w[i] = 0.1f * L.cell.z[i];
+        w[pick] += 0.9f;
+    }
+    float s = 0.f;
+    for (int i = 0; i < n; ++i) s += w[i];
+    for (int i = 0; i < n; ++i) w[i] /= s;
+}
+
+template <int NM>
+__device__ __forceinline__ bool trial_prepare_candidate(TrialLane<NM>& L) {
+    const int n = L.cell.n;
+    float largest = -INFINITY;
+    for (int i = 0; i < n; ++i)
+        if (L.cell.z[i] > 0.f) {
+            L.next.w[i] = fmaf(L.alpha, L.dir[i], L.point.lw[i]);
+            largest = fmaxf(largest, L.next.w[i]);
+        }
+    float sum = 0.f;
+    for (int i = 0; i < n; ++i) {
+        L.next.w[i] = L.cell.z[i] > 0.f ? expf(L.next.w[i] - largest) : 0.f;
+        sum += L.next.w[i];
+    }
+    const float inv = 1.f / sum;
+    bool positive = isfinite(inv);
+    for (int i = 0; i < n; ++i) {
+        L.next.w[i] *= inv;
+        positive = positive && (L.cell.z[i] == 0.f || L.next.w[i] > 0.f);
+    }
+    return positive;
+}
+
+// Decide at the current point or set up the next line search.
+template <int NM>
+__device__ void trial_step_or_finish(TrialLane<NM>& L) {
+    const fp32::ScreenOptions so = fp32::screen_options();
+    const int n = L.cell.n;
+    const float margin = so.decide * L.point.mag;
+    if (L.point.value < -margin) {
+        L.result = fp32::tNegative;
+        L.stage = 2;
+        return;
+    }
+    if (L.point.stat <= so.stat_tol || L.iter >= 400) {
+        L.stage = 2;
+        L.result = -1;  // classify below
+        return;
+    }
+    L.scale = fmaxf(1.f, L.point.stat / 4.f);
+    float slope = 0.f;
+    for (int i = 0; i < n; ++i) {
+        L.dir[i] = 0.f;
+        if (L.cell.z[i] == 0.f) continue;
+        L.dir[i] = -L.point.res[i] / L.scale;
+        slope = fmaf(L.point.w[i] * L.point.res[i], L.dir[i], slope);
+    }
+    if (!(slope < 0.f)) {
+        L.stage = 2;
+        L.result = -1;
+        return;
+    }
+    L.slope = slope;
+    L.alpha = 1.f;
+    L.bt = 0;
+    L.stage = 1;
+}
+
+template <int NM>
+__device__ int trial_classify(const TrialLane<NM>& L) {
+    const fp32::ScreenOptions so = fp32::screen_options();
+    const int n = L.cell.n;
+    const float margin = so.decide * L.point.mag;
+    if (L.point.value < -margin) return fp32::tNegative;
+    if (L.point.stat > 10.f * so.stat_tol || L.iter >= 400) return fp32::tMarginal;
+    for (int r = 0; r < L.nrefs; ++r) {
+        float dist = 0.f;
+        for (int i = 0; i < n; ++i)
+            if (L.cell.z[i] > 0.f) dist = fmaxf(dist, fabsf(L.point.lw[i] - L.lrefs[r * NM + i]));
+        if (dist <= so.near_ref) return fp32::tTangent;
+    }
+    if (L.point.value > margin) return fp32::tPositive;
+    return fp32::tMarginal;
+}
+
+template <int NM>
+__global__ void __launch_bounds__(128) trials32_kernel(const Mixture* __restrict__ mix_g, Workspace ws,
+                                                       const double* __restrict__ p, const double* __restrict__ t,
+                                                       int review) {
+    __shared__ Mixture m;
+    stage_mixture(mix_g, m);
+    const int ntrial = m.n + 4;  // slots per cell (auto starts <= n + 2, review adds 2)
+    const int64_t total = static_cast<int64_t>(ws.counters[qTrialCells]) * ntrial;
+    TrialLane<NM> L;
+    L.stage = 3;  // idle: fetch first
+    L.item = -1;
+    bool live = true;
+    for (;;) {
+        if (live && L.stage >= 2) {
+            if (L.item >= 0 && L.stage == 2) {
+                const int cls = L.result >= 0 ? L.result : trial_classify(L);
+                const int64_t c = L.c;
+                ws.tclass[idx(L.k, ws.ncell, c)] = static_cast<signed char>(cls);
+                for (int i = 0; i < L.cell.n; ++i) ws.tw[idx(L.k * NM + i, ws.ncell, c)] = L.point.w[i];
+                atomicAdd(&ws.counters_out[idx(review ? cFinalEvals : cInitEvals, ws.ncell, c)], L.cell.evals);
+                atomicAdd(&ws.counters_out[idx(cTrialIters, ws.ncell, c)], L.iter);
+            } else if (L.item >= 0 && L.stage == 3) {
+                ws.tclass[idx(L.k, ws.ncell, L.c)] = static_cast<signed char>(-1);  // unused slot
+            }
+            L.item = atomicAdd(&ws.counters[qTrialCursor], 1);
+            if (L.item >= total) {
+                live = false;
+            } else {
+                trial_begin(m, ws, p, t, review != 0, ntrial, L);
+            }
+        }
+        if (__all_sync(0xffffffffu, !live)) break;
+        if (!live || L.stage >= 2) continue;
+        // one property evaluation per lane per loop iteration
+        bool ok = true;
+        if (L.stage == 1) ok = trial_prepare_candidate(L);
+        bool tie = false;
+        if (ok) ok = fp32::stability_provider(m, L.cell, L.next.w, L.lnphi, tie) && !tie &&
+                     fp32::tpd(L.cell, L.lnphi, L.ref, L.next);
+        if (L.stage == 0) {
+            if (!ok) {
+                L.result = fp32::tMarginal;
+                L.stage = 2;
+                for (int i = 0; i < L.cell.n; ++i) L.point.w[i] = L.next.w[i];
+                continue;
+            }
+            L.point = L.next;
+            trial_step_or_finish(L);
+            continue;
+        }
+        // line search
+        bool accept = false;
+        if (ok) {
+            const float predicted = -L.alpha * L.slope;
+            const float guard = 64.f * fp32::kEpsF * (L.point.mag + L.next.mag);
+            if (predicted <= guard)
+                accept = L.next.value <= L.point.value + guard && L.next.stat < L.point.stat;
+            else
+                accept = L.next.value <= L.point.value - 1e-4f * predicted;
+            if (L.next.value < -fp32::screen_options().decide * L.next.mag) accept = true;
+        }
+        if (accept) {
+            L.point = L.next;
+            ++L.iter;
+            trial_step_or_finish(L);
+        } else if (++L.bt >= 24) {
+            L.stage = 2;
+            L.result = -1;
+        } else {
+            L.alpha *= 0.5f;
+        }
+    }
+}
+
+
+// ---------------------------------------------------------------------------
+// Output helpers (layout of include/mpmc_gb300_flash.h).
+template <int NM>
+__device__ void write_single(const DeviceOutputs& out, const Workspace& ws, int64_t c) {
+    const int n = ws.n;
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    if (out.status) out.status[c] = kSinglePhase;
+    if (out.beta) out.beta[c] = nan;
+    for (int i = 0; i < n; ++i) {
+        const int64_t k = idx(i, ws.ncell, c);
+        if (out.x) out.x[k] = ws.z[k];
+        if (out.y) out.y[k] = nan;
+        if (out.lnk) out.lnk[k] = nan;
+        if (out.lnphi_l) out.lnphi_l[k] = ws.ref_lnphi[k];
+        if (out.lnphi_v) out.lnphi_v[k] = nan;
+    }
+    if (out.z_l) out.z_l[c] = ws.ref_z[c];
+    if (out.z_v) out.z_v[c] = nan;
+}
+
+template <int NM>
+__device__ void write_status_only(const DeviceOutputs& out, const Workspace& ws, int64_t c, int status,
+                                  bool with_pair) {
+    const int n = ws.n;
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    if (out.status) out.status[c] = status;
+    if (out.beta) out.beta[c] = with_pair ? ws.cand_s[idx(0, ws.ncell, c)] : nan;
+    for (int i = 0; i < n; ++i) {
+        const int64_t k = idx(i, ws.ncell, c);
+        if (out.x) out.x[k] = with_pair ? ws.cand[idx(0 * NM + i, ws.ncell, c)] : nan;
+        if (out.y) out.y[k] = with_pair ? ws.cand[idx(1 * NM + i, ws.ncell, c)] : nan;
+        if (out.lnk) out.lnk[k] = with_pair ? ws.cand[idx(2 * NM + i, ws.ncell, c)] : nan;
+        if (out.lnphi_l) out.lnphi_l[k] = with_pair ? ws.cand[idx(3 * NM + i, ws.ncell, c)] : nan;
+        if (out.lnphi_v) out.lnphi_v[k] = with_pair ? ws.cand[idx(4 * NM + i, ws.ncell, c)] : nan;
+    }
+    if (out.z_l) out.z_l[c] = with_pair ? ws.cand_s[idx(1, ws.ncell, c)] : nan;
+    if (out.z_v) out.z_v[c] = with_pair ? ws.cand_s[idx(2, ws.ncell, c)] : nan;
+}
+
+template <int NM>
+__device__ void write_counters(const DeviceOutputs& out, const Workspace& ws, int64_t c) {
+    if (!out.counters) return;
+    for (int k = 0; k < cCount; ++k) out.counters[idx(k, ws.ncell, c)] = ws.counters_out[idx(k, ws.ncell, c)];
+}
+
+// Exact FP64 re-run of trial k of a stability test (the plain algorithm from
+// the trial's original start), pt_stability.hpp:343-457.
+template <int NM>
+__device__ int rerun_trial64(const Mixture& m, fp64::Cell<NM>& c, int k, int active, const double* ref,
+                             double tol, int row, const double* ex0, const double* ex1, fp64::TpdPoint<NM>& pt,
+                             fp64::TpdPoint<NM>& nx, double* dir, double* lp) {
+    const int n_auto = auto_starts(active);
+    fp64::make_start(c, k, active, ex0, ex1, n_auto, pt.w);
+    fp64::StabilityOptions o{tol, row};
+    int evals = 0;
+    return fp64::run_trial(m, c, ref, o, pt, nx, dir, lp, evals);
+}
+
+// ---------------------------------------------------------------------------
+// Stage 3: feed-test decision per cell and split-attempt enumeration.
+template <int NM>
+struct DecideScratch {
+    fp64::TpdPoint<NM> pt, nx;
+    double dir[NM], lp[NM], ref[NM], w[NM], other[NM], lk[NM];
+};
+
+template <int NM>
+__global__ void __launch_bounds__(64) decide_kernel(const Mixture* __restrict__ mix_g, Workspace ws,
+                                                    const double* __restrict__ p, const double* __restrict__ t,
+                                                    DeviceOutputs out) {
+    __shared__ Mixture m;
+    stage_mixture(mix_g, m);
+    const int cells = ws.counters[qTrialCells];
+    const int n = m.n;
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < cells; slot += gridDim.x * blockDim.x) {
+        const int64_t c = ws.trial_cells[slot];
+        fp64::Cell<NM> cell;
+        DecideScratch<NM> s;
+        if (!load_cell64(m, ws, c, p, t, cell)) {
+            ws.phase[c] = pFallback;
+            atomicAdd(&ws.counters[qFallback], 1);
+            continue;
+        }
+        int active = 0;
+        for (int i = 0; i < n; ++i) active += cell.z[i] > 0.0;
+        const int n_auto = auto_starts(active);
+        for (int i = 0; i < n; ++i) s.ref[i] = ws.ref_lnphi[idx(i, ws.ncell, c)];
+        bool negative = false, all_stationary = true;
+        int nattempt = 0;
+        for (int k = 0; k < n_auto; ++k) {
+            int cls = ws.tclass[idx(k, ws.ncell, c)];
+            bool witness = false;
+            if (cls == fp32::tMarginal) {
+                const int ts = rerun_trial64(m, cell, k, active, s.ref, 1e-10, cInitEvals, nullptr, nullptr, s.pt, s.nx,
+                                             s.dir, s.lp);
+                if (ts < 0) {
+                    all_stationary = false;
+                } else if (ts == fp64::kNegativeTpd) {
+                    witness = true;
+                    for (int i = 0; i < n; ++i) s.w[i] = s.pt.w[i];
+                } else if (ts != fp64::kStationary) {
+                    all_stationary = false;
+                }
+            } else if (cls == fp32::tNegative) {
+                witness = true;
+                double sum = 0.0, cs = 0.0;
+                for (int i = 0; i < n; ++i) {
+                    s.w[i] = ws.tw[idx(k * NM + i, ws.ncell, c)];
+                    kahan_add(s.w[i], sum, cs);
+                }
+                for (int i = 0; i < n; ++i) s.w[i] /= sum;
+            }
+            if (!witness) continue;
+            negative = true;
+            for (int role = 0; role < 2 && nattempt < kMaxAttempts; ++role) {
+                // split_seed (pt_split.hpp:245-267) in FP64
+                const bool ok = fp64::split_seed(cell, s.w, role == 0, s.other, s.lk);
+                const int order = nattempt++;
+                if (ok) {
+                    for (int i = 0; i < n; ++i) ws.att_lnk[idx(order * NM + i, ws.ncell, c)] = static_cast<float>(s.lk[i]);
+                    const int item = atomicAdd(&ws.counters[qAttempts], 1);
+                    ws.attempt_items[item] = (static_cast<int>(c) << 5) | order;
+                    ws.att_class[idx(order, ws.ncell, c)] = fp32::aFailed;  // overwritten by split32
+                } else {
+                    ws.att_class[idx(order, ws.ncell, c)] = fp32::aTrivial;  // unrepresentable seed: not a candidate
+                }
+            }
+        }
+        ws.att_count[c] = nattempt;
+        atomicAdd(&ws.counters_out[idx(cInitEvals, ws.ncell, c)], cell.counters[cInitEvals]);
+        if (negative) {
+            ws.phase[c] = pSplit;
+            atomicAdd(&ws.counters_out[idx(cAttempts, ws.ncell, c)], nattempt);
+        } else if (all_stationary) {
+            ws.phase[c] = pSingle;
+            write_single<NM>(out, ws, c);
+            write_counters<NM>(out, ws, c);
+        } else {
+            ws.phase[c] = pIndeterminate;
+            write_status_only<NM>(out, ws, c, kIndeterminate, false);
+            write_counters<NM>(out, ws, c);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Stage 4: FP32 split attempts as a per-lane state machine.
+template <int NM>
+struct SplitLane {
+    fp32::Cell<NM> cell;
+    fp32::SplitState<NM> point, next;
+    float lk[NM];
+    int item, c, order, iter, bt, stage;  // stage 0 = evaluate seed, 1 = line search, 2 = finished
+    float alpha, slope, scale;
+};
+
+template <int NM>
+__device__ void split_step_or_finish(SplitLane<NM>& L) {
+    const int n = L.cell.n;
+    if (L.point.fug <= 2e-5f || L.iter >= 512) {
+        L.stage = 2;
+        return;
+    }
+    L.scale = fmaxf(1.f, L.point.fug / 2.f);
+    float h = 0.f, first = 0.f, second = 0.f;
+    for (int i = 0; i < n; ++i) {
+        if (L.cell.z[i] == 0.f) continue;
+        const float cc = (L.point.x[i] / L.cell.z[i]) * L.point.y[i];
+        const float d = L.point.y[i] - L.point.x[i];
+        h += d * (d / L.cell.z[i]);
+        first += cc * L.point.res[i];
+        second += (cc * L.point.res[i]) * L.point.res[i];
+    }
+    const float slope = -(L.point.beta * (1.f - L.point.beta) * second + (first / h) * first) / L.scale;
+    if (!(slope < 0.f) || !isfinite(slope)) {
+        L.stage = 2;
+        return;
+    }
+    L.slope = slope;
+    L.alpha = 1.f;
+    L.bt = 0;
+    L.stage = 1;
+}
+
+template <int NM>
+__global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict__ mix_g, Workspace ws,
+                                                      const double* __restrict__ p, const double* __restrict__ t) {
+    __shared__ Mixture m;
+    stage_mixture(mix_g, m);
+    const int total = ws.counters[qAttempts];
+    SplitLane<NM> L;
+    L.stage = 3;
+    L.item = -1;
+    bool live = true;
+    for (;;) {
+        if (live && L.stage >= 2) {
+            if (L.item >= 0 && L.stage == 2) {
+                int cls = fp32::aFailed;
+                const int n = L.cell.n;
+                float contrast = 0.f;
+                for (int i = 0; i < n; ++i) contrast = fmaxf(contrast, fabsf(L.point.lnk[i]));
+                if (L.iter >= 0) {
+                    if (contrast < 1e-4f || L.point.z_v - L.point.z_l <= 1e-5f * fmaxf(L.point.z_v, L.point.z_l))
+                        cls = fp32::aTrivial;
+                    else if (L.point.fug <= 1e-3f)
+                        cls = fp32::aConverged;
+                }
+                const int64_t c = L.c;
+                ws.att_class[idx(L.order, ws.ncell, c)] = static_cast<signed char>(cls);
+                ws.att_gibbs[idx(L.order, ws.ncell, c)] = L.point.gibbs;
+                for (int i = 0; i < n; ++i) ws.att_lnk[idx(L.order * NM + i, ws.ncell, c)] = L.point.lnk[i];
+                atomicAdd(&ws.counters_out[idx(cSplitEvals, ws.ncell, c)], L.cell.evals);
+                atomicAdd(&ws.counters_out[idx(cSplitIters, ws.ncell, c)], L.iter);
+            }
+            L.item = atomicAdd(&ws.counters[qAttemptCursor], 1);
+            if (L.item >= total) {
+                live = false;
+            } else {
+                const int code = ws.attempt_items[L.item];
+                L.c = code >> 5;
+                L.order = code & 31;
+                int active;
+                L.iter = 0;
+                L.stage = 0;
+                if (!load_cell32(m, ws, L.c, p, t, L.cell, active)) {
+                    L.iter = -1;
+                    L.stage = 2;
+                } else {
+                    for (int i = 0; i < L.cell.n; ++i) L.lk[i] = ws.att_lnk[idx(L.order * NM + i, ws.ncell, L.c)];
+                }
+            }
+        }
+        if (__all_sync(0xffffffffu, !live)) break;
+        if (!live || L.stage >= 2) continue;
+        const int n = L.cell.n;
+        if (L.stage == 1)
+            for (int i = 0; i < n; ++i) L.lk[i] = fmaf(L.alpha / L.scale, L.point.res[i], L.point.lnk[i]);
+        const bool ok = fp32::split_evaluate(m, L.cell, L.lk, L.next);
+        if (L.stage == 0) {
+            if (!ok) {
+                L.iter = -1;
+                L.stage = 2;
+                continue;
+            }
+            fp32::copy_state(L.point, L.next, n);
+            split_step_or_finish(L);
+            continue;
+        }
+        bool accept = false;
+        if (ok) {
+            const float predicted = -L.alpha * L.slope;
+            const float guard = 64.f * fp32::kEpsF * (L.point.mag + L.next.mag);
+            accept = predicted > guard ? L.next.gibbs <= L.point.gibbs - 1e-4f * predicted
+                                       : (L.next.gibbs <= L.point.gibbs + guard &&
+                                          L.point.fug - L.next.fug > 1e-4f * (L.alpha / L.scale) * L.point.fug);
+        }
+        if (accept) {
+            fp32::copy_state(L.point, L.next, n);
+            ++L.iter;
+            split_step_or_finish(L);
+        } else if (++L.bt >= 20) {
+            L.stage = 2;
+        } else {
+            L.alpha *= 0.5f;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Stage 5: FP64 polish of the minimum-Gibbs attempt and the acceptance rules.
+template <int NM>
+struct PolishScratch {
+    fp64::SplitState<NM> st;
+    fp32::SplitState<NM> f32;
+    double lnk[NM], e[NM], num[NM], J[NM * NM], d[NM];
+    float lk32[NM], fp[NM], fm[NM];
+    int piv[NM];
+};
+
+// Newton refinement of ln K: FP64 residual F(ln K) (RR + role phases,
+// pt_split.hpp:300-341), FP32 central-difference Jacobian dF/dln K taken once
+// at the FP32 solution.  Returns true with `s.st` the FP64 state at the
+// refined ln K (|F| <= 1e-13 or no further decrease).
+template <int NM>
+__device__ bool polish_split(const Mixture& m, fp64::Cell<NM>& c64, fp32::Cell<NM>& c32, PolishScratch<NM>& s) {
+    const int n = c64.n;
+    // Jacobian in FP32 by central differences on the FP32 residual map
+    const float h = 2e-3f;
+    for (int j = 0; j < n; ++j) {
+        if (c32.z[j] == 0.f) {
+            for (int i = 0; i < n; ++i) s.J[i * n + j] = i == j ? 1.0 : 0.0;
+            continue;
+        }
+        float save = s.lk32[j];
+        s.lk32[j] = save + h;
+        if (!fp32::split_evaluate(m, c32, s.lk32, s.f32)) return false;
+        for (int i = 0; i < n; ++i) s.fp[i] = s.f32.res[i];
+        s.lk32[j] = save - h;
+        if (!fp32::split_evaluate(m, c32, s.lk32, s.f32)) return false;
+        for (int i = 0; i < n; ++i) s.fm[i] = s.f32.res[i];
+        s.lk32[j] = save;
+        for (int i = 0; i < n; ++i)
+            s.J[i * n + j] = c32.z[i] == 0.f ? (i == j ? 1.0 : 0.0) : static_cast<double>((s.fp[i] - s.fm[i]) / (2.f * h));
+    }
+    double norm;
+    if (!ad::lu_factor(s.J, s.piv, n, norm)) return false;
+    int evals = 0;
+    double prev = INFINITY;
+    for (int it = 0; it < 8; ++it) {
+        const int st = fp64::split_evaluate(m, c64, s.lnk, s.st, evals, 1 << 30, s.e, s.num, true);
+        if (st != fp64::kConverged) return false;
+        if (s.st.fug <= 1e-13 || !(s.st.fug < 0.5 * prev)) return s.st.fug <= 1e-11;
+        prev = s.st.fug;
+        for (int i = 0; i < n; ++i) s.d[i] = -s.st.res[i];
+        if (!ad::lu_solve(s.J, s.piv, n, s.d)) return false;
+        for (int i = 0; i < n; ++i) s.lnk[i] = s.st.lnk[i] + s.d[i];
+    }
+    return s.st.fug <= 1e-11;
+}
+
+template <int NM>
+__global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ mix_g, Workspace ws,
+                                                    const double* __restrict__ p, const double* __restrict__ t,
+                                                    DeviceOutputs out) {
+    __shared__ Mixture m;
+    stage_mixture(mix_g, m);
+    const int cells = ws.counters[qTrialCells];  // the feed-test list; only pSplit cells act
+    const int n = m.n;
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < cells; slot += gridDim.x * blockDim.x) {
+        const int64_t c = ws.trial_cells[slot];
+        if (ws.phase[c] != pSplit) continue;
+        fp64::Cell<NM> c64;
+        fp32::Cell<NM> c32;
+        PolishScratch<NM> s;
+        int active;
+        if (!load_cell64(m, ws, c, p, t, c64) || !load_cell32(m, ws, c, p, t, c32, active)) {
+            ws.phase[c] = pFallback;
+            atomicAdd(&ws.counters[qFallback], 1);
+            continue;
+        }
+        // rank converged attempts by FP32 Gibbs energy (ties in FP32 resolved in FP64 below)
+        const int na = ws.att_count[c];
+        int best = -1, second = -1;
+        bool any_failed = false;
+        for (int a = 0; a < na; ++a) {
+            const int cls = ws.att_class[idx(a, ws.ncell, c)];
+            if (cls == fp32::aFailed) any_failed = true;
+            if (cls != fp32::aConverged) continue;
+            const float g = ws.att_gibbs[idx(a, ws.ncell, c)];
+            if (best < 0 || g < ws.att_gibbs[idx(best, ws.ncell, c)]) {
+                second = best;
+                best = a;
+            } else if (second < 0 || g < ws.att_gibbs[idx(second, ws.ncell, c)]) {
+                second = a;
+            }
+        }
+        if (best < 0) {
+            if (any_failed) {
+                ws.phase[c] = pFallback;  // FP32 could not settle an attempt: reference rules in FP64
+                atomicAdd(&ws.counters[qFallback], 1);
+            } else {
+                ws.phase[c] = pIndeterminate;  // every attempt collapsed to the trivial solution
+                write_status_only<NM>(out, ws, c, kIndeterminate, false);
+                write_counters<NM>(out, ws, c);
+            }
+            continue;
+        }
+        // a second converged attempt at a different composition with a Gibbs
+        // energy FP32 cannot separate from the best: let FP64 arbitrate
+        int candidates[2] = {best, -1};
+        if (second >= 0) {
+            const float gb = ws.att_gibbs[idx(best, ws.ncell, c)], gs = ws.att_gibbs[idx(second, ws.ncell, c)];
+            float dist = 0.f;
+            for (int i = 0; i < n; ++i)
+                dist = fmaxf(dist, fabsf(ws.att_lnk[idx(best * NM + i, ws.ncell, c)] -
+                                         ws.att_lnk[idx(second * NM + i, ws.ncell, c)]));
+            if (gs - gb <= 1e-4f * (1.f + fabsf(gb)) && dist > 1e-2f) candidates[1] = second;
+        }
+        bool have = false;
+        double best_g = 0.0;
+        for (int k = 0; k < 2 && candidates[k] >= 0; ++k) {
+            const int a = candidates[k];
+            for (int i = 0; i < n; ++i) {
+                s.lk32[i] = ws.att_lnk[idx(a * NM + i, ws.ncell, c)];
+                s.lnk[i] = s.lk32[i];
+            }
+            if (!polish_split(m, c64, c32, s)) continue;
+            // acceptance of a fugacity-converged state, pt_split.hpp:351-362
+            const fp64::SplitState<NM>& st = s.st;
+            double contrast = 0.0;
+            for (int i = 0; i < n; ++i) contrast = fmax(contrast, fabs(st.lnk[i]));
+            const bool converged = st.mass_abs <= 1e-12 && st.mass_rel <= 1e-10 && st.beta > 1e-10 &&
+                                   1.0 - st.beta > 1e-10 && contrast > 1e-7 &&
+                                   st.z_v - st.z_l > 1e-8 * fmax(st.z_v, st.z_l);
+            if (!converged) continue;
+            if (have && !(st.gibbs < best_g)) continue;
+            have = true;
+            best_g = st.gibbs;
+            for (int i = 0; i < n; ++i) {
+                ws.cand[idx(0 * NM + i, ws.ncell, c)] = st.x[i];
+                ws.cand[idx(1 * NM + i, ws.ncell, c)] = st.y[i];
+                ws.cand[idx(2 * NM + i, ws.ncell, c)] = st.lnk[i];
+                ws.cand[idx(3 * NM + i, ws.ncell, c)] = st.lnphi_l[i];
+                ws.cand[idx(4 * NM + i, ws.ncell, c)] = st.lnphi_v[i];
+                ws.cand[idx(5 * NM + i, ws.ncell, c)] = st.common[i];
+            }
+            ws.cand_s[idx(0, ws.ncell, c)] = st.beta;
+            ws.cand_s[idx(1, ws.ncell, c)] = st.z_l;
+            ws.cand_s[idx(2, ws.ncell, c)] = st.z_v;
+            ws.cand_s[idx(3, ws.ncell, c)] = st.fug;
+            ws.cand_s[idx(7, ws.ncell, c)] = st.guard;
+        }
+        atomicAdd(&ws.counters_out[idx(cSplitEvals, ws.ncell, c)], c64.counters[cSplitEvals]);
+        atomicAdd(&ws.counters_out[idx(cRrIters, ws.ncell, c)], c64.counters[cRrIters]);
+        if (!have) {
+            ws.phase[c] = pFallback;
+            atomicAdd(&ws.counters[qFallback], 1);
+            continue;
+        }
+        // phase-set review set-up, pt_split.hpp:490-512
+        double feed_g = 0.0, corr = 0.0, magnitude = 1.0;
+        for (int i = 0; i < n; ++i) {
+            if (c64.z[i] == 0.0) continue;
+            const double phi = ws.ref_lnphi[idx(i, ws.ncell, c)];
+            kahan_add(c64.z[i] * (c64.lz[i] + phi), feed_g, corr);
+            magnitude += c64.z[i] * (fabs(c64.lz[i]) + fabs(phi));
+        }
+        const double fug = ws.cand_s[idx(3, ws.ncell, c)];
+        ws.cand_s[idx(4, ws.ncell, c)] = best_g - feed_g;
+        ws.cand_s[idx(5, ws.ncell, c)] = ws.cand_s[idx(7, ws.ncell, c)] + 256.0 * kEps * magnitude;
+        ws.cand_s[idx(6, ws.ncell, c)] = 1e-10 + 0.5 * fug;
+        // the review normalises the feed once more (pt_stability.hpp:242, :278)
+        double zz[NM];
+        for (int i = 0; i < n; ++i) zz[i] = c64.z[i];
+        fp64::normalise_feed(c64, zz);
+        for (int i = 0; i < n; ++i)
+            ws.cand[idx(6 * NM + i, ws.ncell, c)] =
+                c64.z[i] > 0.0 ? ws.cand[idx(5 * NM + i, ws.ncell, c)] - c64.lz[i] : 0.0;
+        ws.phase[c] = pReview;
+    }
+}
+
+// Compacts the review cells into trial_cells (after the feed-test list is no
+// longer needed) and resets the trial cursor.
+template <int NM>
+__global__ void relist_kernel(Workspace ws) {
+    // single block: compaction order does not matter
+    if (threadIdx.x == 0) {
+        ws.counters[qTrialCells] = 0;
+        ws.counters[qTrialCursor] = 0;
+    }
+    __syncthreads();
+    for (int64_t c = threadIdx.x; c < ws.ncell; c += blockDim.x) {
+        if (ws.phase[c] == pReview) {
+            const int slot = atomicAdd(&ws.counters[qTrialCells], 1);
+            ws.trial_cells[slot] = static_cast<int>(c);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Stage 7: review decision, final status and outputs.
+template <int NM>
+__global__ void __launch_bounds__(64) finish_kernel(const Mixture* __restrict__ mix_g, Workspace ws,
+                                                    const double* __restrict__ p, const double* __restrict__ t,
+                                                    DeviceOutputs out) {
+    __shared__ Mixture m;
+    stage_mixture(mix_g, m);
+    const int cells = ws.counters[qTrialCells];
+    const int n = m.n;
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < cells; slot += gridDim.x * blockDim.x) {
+        const int64_t c = ws.trial_cells[slot];
+        fp64::Cell<NM> cell;
+        DecideScratch<NM> s;
+        if (!load_cell64(m, ws, c, p, t, cell)) {
+            ws.phase[c] = pFallback;
+            atomicAdd(&ws.counters[qFallback], 1);
+            continue;
+        }
+        // the review runs on the twice-normalised feed
+        double zz[NM], ex0[NM], ex1[NM];
+        for (int i = 0; i < n; ++i) zz[i] = cell.z[i];
+        fp64::normalise_feed(cell, zz);
+        for (int i = 0; i < n; ++i) {
+            s.ref[i] = ws.cand[idx(6 * NM + i, ws.ncell, c)];
+            ex0[i] = ws.cand[idx(0 * NM + i, ws.ncell, c)];
+            ex1[i] = ws.cand[idx(1 * NM + i, ws.ncell, c)];
+        }
+        int active = 0;
+        for (int i = 0; i < n; ++i) active += cell.z[i] > 0.0;
+        const int ntr = auto_starts(active) + 2;
+        const double tol = ws.cand_s[idx(6, ws.ncell, c)];
+        bool negative = false, stationary = true;
+        for (int k = 0; k < ntr; ++k) {
+            const int cls = ws.tclass[idx(k, ws.ncell, c)];
+            if (cls == fp32::tNegative) {
+                negative = true;
+            } else if (cls == fp32::tMarginal) {
+                const int ts = rerun_trial64(m, cell, k, active, s.ref, tol, cFinalEvals, ex0, ex1, s.pt, s.nx, s.dir,
+                                             s.lp);
+                if (ts == fp64::kNegativeTpd) negative = true;
+                else if (ts != fp64::kStationary) stationary = false;
+            }
+        }
+        atomicAdd(&ws.counters_out[idx(cFinalEvals, ws.ncell, c)], cell.counters[cFinalEvals]);
+        int status;
+        if (negative) status = kPhaseSetUnstable;
+        else if (ws.cand_s[idx(4, ws.ncell, c)] > ws.cand_s[idx(5, ws.ncell, c)]) status = kIndeterminate;
+        else status = stationary ? kTwoPhase : kIndeterminate;
+        ws.phase[c] = status;
+        write_status_only<NM>(out, ws, c, status, true);
+        write_counters<NM>(out, ws, c);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fallback: the plain FP64 reference algorithm for flagged cells.
+template <int NM>
+__global__ void __launch_bounds__(64) fallback_kernel(const Mixture* __restrict__ mix_g, Workspace ws,
+                                                      const double* __restrict__ p, const double* __restrict__ t,
+                                                      const double* __restrict__ z, DeviceOutputs out) {
+    __shared__ Mixture m;
+    stage_mixture(mix_g, m);
+    if (ws.counters[qFallback] == 0) return;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; c < ws.ncell; c += stride) {
+        if (ws.phase[c] != pFallback) continue;
+        using namespace fp64;
+        Cell<NM> cell;
+        cell.n = m.n;
+        cell.p = p[c];
+        cell.t = t[c];
+        for (int k = 0; k < cCount; ++k) cell.counters[k] = 0;
+        double feed[NM];
+        for (int i = 0; i < cell.n; ++i) feed[i] = z[idx(i, ws.ncell, c)];
+        Scratch<NM> w;
+        CellResult<NM> r;
+        const int status = solve_cell(m, cell, feed, w, r);
+        const int n = cell.n;
+        const double nan = __longlong_as_double(0x7ff8000000000000LL);
+        if (out.status) out.status[c] = status;
+        const bool pair = r.has_pair && status != kSinglePhase && status != kInvalid;
+        const SplitState<NM>& b = w.best;
+        if (out.beta) out.beta[c] = pair ? b.beta : nan;
+        for (int i = 0; i < n; ++i) {
+            const int64_t k = idx(i, ws.ncell, c);
+            const bool single = status == kSinglePhase;
+            if (out.x) out.x[k] = pair ? b.x[i] : (single ? cell.z[i] : nan);
+            if (out.y) out.y[k] = pair ? b.y[i] : nan;
+            if (out.lnk) out.lnk[k] = pair ? b.lnk[i] : nan;
+            if (out.lnphi_l) out.lnphi_l[k] = pair ? b.lnphi_l[i] : (single ? r.ref_lnphi[i] : nan);
+            if (out.lnphi_v) out.lnphi_v[k] = pair ? b.lnphi_v[i] : nan;
+        }
+        if (out.z_l) out.z_l[c] = pair ? b.z_l : (status == kSinglePhase ? r.ref_z : nan);
+        if (out.z_v) out.z_v[c] = pair ? b.z_v : nan;
+        if (out.counters)
+            for (int k = 0; k < cCount; ++k)
+                out.counters[idx(k, ws.ncell, c)] = ws.counters_out[idx(k, ws.ncell, c)] + cell.counters[k];
+    }
+}
+
+}  // namespace batched
+}  // namespace pr76

@@ -1,0 +1,552 @@
+// FP32 screening arithmetic for the mixed-precision flash.
+//
+// The same PR76 property chain as pr76_fp64.cuh (mixing with row sums,
+// scaled cubic in y = (Z - B)/s, ln phi with the log1p(u)/u series, TPD,
+// Rachford-Rice, ln K successive substitution with the Gibbs line search of
+// pt_split.hpp:367-405) in single precision, with two numerical changes that
+// keep FP32 robust and branch-light:
+//  * each monotone interval of the cubic is solved by bracketed Newton
+//    (bisection only as a safeguard) instead of pure bisection;
+//  * Rachford-Rice is solved by bracketed Newton on the reference's
+//    overflow-safe residual (rachford_rice.hpp:53-63).
+// These screening iterations only make decisions that are clear by a margin
+// far above FP32 rounding; everything else is re-decided in FP64.
+#pragma once
+
+#include "pr76_common.cuh"
+
+namespace pr76 {
+namespace fp32 {
+
+constexpr float kEpsF = 1.1920928955078125e-07f;
+constexpr float kRf = 8.31446261815324f;
+
+template <int NM>
+struct Cell {
+    int n;
+    float p, t;
+    float a[NM], root[NM];
+    float z[NM], lz[NM];
+    float sums[NM];
+    float lnphi[2][NM];
+    float b[NM];
+    int evals;
+};
+
+template <int NM>
+__device__ bool temp_setup(const Mixture& m, Cell<NM>& c) {
+    const double st = sqrt(static_cast<double>(c.t));
+    for (int i = 0; i < c.n; ++i) {
+        // a_i(T) formed in FP64 once per cell, then rounded
+        const double bracket = 1.0 + m.kappa[i] * (1.0 - st / m.sqrt_tc[i]);
+        const double attraction = (bracket * m.ac[i]) * bracket;
+        if (!isfinite(attraction) || !(attraction > 0.0)) return false;
+        c.a[i] = static_cast<float>(attraction);
+        c.root[i] = static_cast<float>(sqrt(attraction));
+        c.b[i] = static_cast<float>(m.b[i]);
+    }
+    return true;
+}
+
+template <int NM>
+__device__ __forceinline__ bool mix(const Mixture& m, Cell<NM>& c, const float* x, float& amix, float& bmix) {
+    const int n = c.n;
+    float attraction = 0.f, covolume = 0.f;
+    for (int i = 0; i < n; ++i) {
+        attraction = fmaf(x[i] * c.a[i], x[i], attraction);
+        covolume = fmaf(x[i], c.b[i], covolume);
+        c.sums[i] = x[i] * c.a[i];
+    }
+    for (int i = 0; i < n; ++i) {
+        const float xr_i = x[i] * c.root[i];
+        const float r_i = c.root[i];
+        const float x_i = x[i];
+        float s_i = c.sums[i];
+        for (int j = i + 1; j < n; ++j) {
+            const float f = static_cast<float>(m.factor[i * n + j]);
+            const float aij = (r_i * f) * c.root[j];
+            attraction = fmaf(2.f * xr_i, x[j] * c.root[j] * f, attraction);
+            s_i = fmaf(x[j], aij, s_i);
+            c.sums[j] = fmaf(x_i, aij, c.sums[j]);
+        }
+        c.sums[i] = s_i;
+    }
+    amix = attraction;
+    bmix = covolume;
+    return isfinite(attraction) && isfinite(covolume) && covolume > 0.f;
+}
+
+struct Root {
+    float z, free_volume;
+    int slope_sign;
+    bool derivative_valid;
+};
+struct RootSet {
+    Root r[3];
+    int count;
+    bool ok;
+};
+
+// All positive-free-volume roots of the scaled PR cubic (pr76_roots.hpp:46-58
+// coefficients), bracketed Newton per monotone interval.
+__device__ inline void solve_roots(float a, float b, RootSet& rs) {
+    rs.count = 0;
+    rs.ok = false;
+    if (!isfinite(a) || !isfinite(b) || !(b > 0.f)) return;
+    const float scale = fmaxf(fmaxf(1.f, b), sqrtf(fabsf(a)));
+    const float bs = b / scale, inv = 1.f / scale;
+    const float c2 = 4.f * bs - inv;
+    const float c1 = (a * inv) * inv + 2.f * bs * bs - 4.f * bs * inv;
+    const float c0 = ((-2.f * bs) * bs) * inv;
+    if (!(c0 < 0.f)) return;
+    const float upper = 1.f + fmaxf(fmaxf(fabsf(c2), fabsf(c1)), fabsf(c0));
+    float ep[4];
+    int ne = 1;
+    ep[0] = 0.f;
+    const float disc = fmaf(c2, c2, -3.f * c1);
+    if (disc > 0.f) {
+        const float q = -c2 - copysignf(sqrtf(disc), c2);
+        float s0 = q / 3.f, s1 = c1 / q;
+        if (s1 < s0) {
+            const float tmp = s0;
+            s0 = s1;
+            s1 = tmp;
+        }
+        if (s0 > 0.f && s0 < upper) ep[ne++] = s0;
+        if (s1 > 0.f && s1 < upper) ep[ne++] = s1;
+    }
+    ep[ne++] = upper;
+    auto h = [&](float y) { return fmaf(fmaf(y + c2, y, c1), y, c0); };
+    auto dh = [&](float y) { return fmaf(3.f * y + 2.f * c2, y, c1); };
+    for (int iv = 1; iv < ne; ++iv) {
+        float lo = ep[iv - 1], hi = ep[iv];
+        float flo = h(lo), fhi = h(hi);
+        if (signbit(flo) == signbit(fhi)) continue;
+        const bool increasing = fhi > flo;
+        float y = 0.5f * (lo + hi);
+        for (int it = 0; it < 40; ++it) {
+            const float fy = h(y);
+            if (fy == 0.f) break;
+            if ((fy > 0.f) == increasing)
+                hi = y;
+            else
+                lo = y;
+            const float d = dh(y);
+            float yn = y - fy / d;
+            if (!(yn > lo && yn < hi)) yn = 0.5f * (lo + hi);
+            if (fabsf(yn - y) <= 2.f * kEpsF * yn || hi - lo <= 2.f * kEpsF * y) {
+                y = yn;
+                break;
+            }
+            y = yn;
+        }
+        if (rs.count == 3) return;
+        const float d = dh(y);
+        const float dscale = 3.f * y * y + 2.f * fabsf(c2) * y + fabsf(c1);
+        Root& r = rs.r[rs.count++];
+        r.free_volume = y * scale;
+        r.z = r.free_volume + b;
+        r.slope_sign = d > 0.f ? 1 : (d < 0.f ? -1 : 0);
+        r.derivative_valid = dscale > 0.f && fabsf(d) > 1e-3f * dscale;
+    }
+    rs.ok = rs.count > 0;
+}
+
+__device__ __forceinline__ float log1p_over_x(float u) {
+    if (fabsf(u) <= 0.125f) {
+        // degree-9 truncation of the same alternating series (below FP32 eps at |u| <= 1/8)
+        float v = -1.f / 10.f;
+#pragma unroll
+        for (int k = 8; k >= 0; --k) v = ((k % 2 == 0) ? 1.f : -1.f) / static_cast<float>(k + 1) + u * v;
+        return v;
+    }
+    return log1pf(u) / u;
+}
+
+template <int NM>
+__device__ __forceinline__ bool ln_phi_of_root(const Cell<NM>& c, float amix, float bmix, float A, float B,
+                                               const Root& root, float* ln_phi) {
+    const float fv = root.free_volume;
+    const float z = fv + B;
+    const float sqrt2 = 1.41421356f;
+    const float den = fv + (2.f - sqrt2) * B;
+    const float u = (2.f * sqrt2) * (B / den);
+    const float log_factor = log1p_over_x(u) / den;
+    float zm1 = z - 1.f;
+    float log_free = logf(fv);
+    if (fabsf(zm1) < 0.25f && B < 0.125f) {
+        const float bz = B / z;
+        zm1 = B / fv - (A / z) / (1.f + 2.f * bz - bz * bz);
+        log_free = log1pf(zm1 - B);
+    }
+    const float rt = kRf * c.t;
+    const float prt = c.p / rt;
+    const float inv_b = 1.f / bmix;
+    for (int i = 0; i < c.n; ++i) {
+        const float ratio = c.b[i] * inv_b;
+        const float coefficient = ((2.f * c.sums[i] - amix * ratio) / rt) * prt;
+        ln_phi[i] = ratio * zm1 - log_free - coefficient * log_factor;
+    }
+    return isfinite(z) && isfinite(log_free);
+}
+
+// Stability provider in FP32: minimum-Gibbs admissible root.  `near_tie`
+// reports branch energies too close for FP32 to order; the caller then
+// re-decides in FP64.
+template <int NM>
+__device__ bool stability_provider(const Mixture& m, Cell<NM>& c, const float* x, float* out, bool& near_tie) {
+    ++c.evals;
+    near_tie = false;
+    float amix, bmix;
+    if (!mix(m, c, x, amix, bmix)) return false;
+    const float rt = kRf * c.t;
+    const float prt = c.p / rt;
+    const float A = (amix / rt) * prt, B = bmix * prt;
+    RootSet rs;
+    solve_roots(A, B, rs);
+    if (!rs.ok) return false;
+    int cand[3], nc = 0;
+    for (int k = 0; k < rs.count; ++k) {
+        if (rs.r[k].slope_sign <= 0) continue;
+        if (nc == 2) return false;
+        if (!ln_phi_of_root(c, amix, bmix, A, B, rs.r[k], c.lnphi[nc])) return false;
+        cand[nc++] = k;
+    }
+    if (nc == 0) return false;
+    int best = 0;
+    if (nc == 2) {
+        float d = 0.f, mag = 1.f;
+        for (int i = 0; i < c.n; ++i) {
+            d = fmaf(x[i], c.lnphi[1][i] - c.lnphi[0][i], d);
+            mag = fmaf(x[i], fabsf(c.lnphi[1][i]) + fabsf(c.lnphi[0][i]), mag);
+        }
+        if (d < 0.f) best = 1;
+        if (fabsf(d) <= 64.f * kEpsF * mag) near_tie = true;
+    }
+    if (!rs.r[cand[best]].derivative_valid) return false;
+    for (int i = 0; i < c.n; ++i) out[i] = c.lnphi[best][i];
+    return true;
+}
+
+template <int NM>
+__device__ bool role_provider(const Mixture& m, Cell<NM>& c, const float* x, bool vapor, float* ln_phi, float& z_out) {
+    ++c.evals;
+    float amix, bmix;
+    if (!mix(m, c, x, amix, bmix)) return false;
+    const float rt = kRf * c.t;
+    const float prt = c.p / rt;
+    const float A = (amix / rt) * prt, B = bmix * prt;
+    RootSet rs;
+    solve_roots(A, B, rs);
+    if (!rs.ok) return false;
+    int sel = -1;
+    for (int k = 0; k < rs.count; ++k) {
+        if (rs.r[k].slope_sign <= 0) continue;
+        sel = k;
+        if (!vapor) break;
+    }
+    if (sel < 0 || !rs.r[sel].derivative_valid) return false;
+    if (!ln_phi_of_root(c, amix, bmix, A, B, rs.r[sel], ln_phi)) return false;
+    z_out = rs.r[sel].z;
+    return z_out > 0.f;
+}
+
+// ---------------------------------------------------------------------------
+// TPD trial in FP32 with the reference's log-composition steepest descent and
+// backtracking (pt_stability.hpp:373-455).
+template <int NM>
+struct TpdPoint {
+    float w[NM], res[NM], lw[NM];
+    float value, mag, stat;
+};
+
+template <int NM>
+__device__ bool tpd(const Cell<NM>& c, const float* lnphi_w, const float* ref, TpdPoint<NM>& pt) {
+    const int n = c.n;
+    float value = 0.f, mag = 1.f, sum = 0.f;
+    for (int i = 0; i < n; ++i) sum += pt.w[i];
+    for (int i = 0; i < n; ++i) {
+        pt.res[i] = 0.f;
+        if (c.z[i] == 0.f) continue;
+        const float w = pt.w[i];
+        if (!(w > 0.f)) return false;
+        const float lw = logf(w);
+        pt.lw[i] = lw;
+        const float q = (lw - c.lz[i]) + (lnphi_w[i] - ref[i]);
+        pt.res[i] = q;
+        value = fmaf(w, q, value);
+        mag = fmaf(w, fabsf(lw) + fabsf(c.lz[i]) + fabsf(lnphi_w[i]) + fabsf(ref[i]), mag);
+    }
+    const float mean = value / sum;
+    float stat = 0.f;
+    for (int i = 0; i < n; ++i) {
+        if (c.z[i] == 0.f) continue;
+        pt.res[i] -= mean;
+        stat = fmaxf(stat, fabsf(pt.res[i]));
+    }
+    pt.value = value;
+    pt.mag = mag;
+    pt.stat = stat;
+    return isfinite(value) && isfinite(stat);
+}
+
+// Screening outcome of one FP32 trial.
+enum TrialClass : int {
+    tNegative = 0,   // TPD clearly below zero (margin >> FP32 rounding)
+    tPositive = 1,   // stationary at TPD clearly above zero
+    tTangent = 2,    // stationary at one of the reference compositions (TPD = 0 there by construction)
+    tMarginal = 3,   // anything FP32 cannot decide: re-run in FP64 from the end point
+};
+
+// FP32 screening tolerances.
+struct ScreenOptions {
+    float stat_tol;     // FP32 stationarity at which the descent stops
+    float decide;       // |TPD| margin (relative to the TPD magnitude scale) for a decision
+    float near_ref;     // max |ln(w_i / ref_i)| to call the end point "at a reference composition"
+};
+__device__ __forceinline__ ScreenOptions screen_options() { return {2e-5f, 2e-5f, 2e-3f}; }
+
+// Runs one trial from point.w; `refs` are up to two reference compositions
+// (log) at which TPD vanishes exactly (the feed for the feed test; x and y
+// for the common-tangent review).  Returns the class; point holds the end.
+template <int NM>
+__device__ int run_trial(const Mixture& m, Cell<NM>& c, const float* ref_lnphi, const float* lrefs, int nrefs,
+                         TpdPoint<NM>& point, TpdPoint<NM>& next, float* dir, float* lnphi) {
+    const int n = c.n;
+    const ScreenOptions so = screen_options();
+    bool tie;
+    if (!stability_provider(m, c, point.w, lnphi, tie) || tie || !tpd(c, lnphi, ref_lnphi, point)) return tMarginal;
+    for (int it = 0; it < 512; ++it) {
+        const float margin = so.decide * point.mag;
+        if (point.value < -margin) return tNegative;
+        if (point.stat <= so.stat_tol) break;
+        const float scale = fmaxf(1.f, point.stat / 4.f);
+        float slope = 0.f;
+        for (int i = 0; i < n; ++i) {
+            dir[i] = 0.f;
+            if (c.z[i] == 0.f) continue;
+            dir[i] = -point.res[i] / scale;
+            slope = fmaf(point.w[i] * point.res[i], dir[i], slope);
+        }
+        if (!(slope < 0.f)) break;
+        bool accepted = false;
+        float alpha = 1.f;
+        for (int bt = 0; bt < 24; ++bt, alpha *= 0.5f) {
+            float largest = -INFINITY;
+            for (int i = 0; i < n; ++i)
+                if (c.z[i] > 0.f) {
+                    next.w[i] = fmaf(alpha, dir[i], point.lw[i]);
+                    largest = fmaxf(largest, next.w[i]);
+                }
+            float sum = 0.f;
+            for (int i = 0; i < n; ++i) {
+                next.w[i] = c.z[i] > 0.f ? expf(next.w[i] - largest) : 0.f;
+                sum += next.w[i];
+            }
+            const float inv = 1.f / sum;
+            bool positive = true;
+            for (int i = 0; i < n; ++i) {
+                next.w[i] *= inv;
+                positive = positive && (c.z[i] == 0.f || next.w[i] > 0.f);
+            }
+            if (!positive) continue;
+            if (!stability_provider(m, c, next.w, lnphi, tie) || tie || !tpd(c, lnphi, ref_lnphi, next)) continue;
+            const float predicted = -alpha * slope;
+            const float guard = 64.f * kEpsF * (point.mag + next.mag);
+            bool accept;
+            if (predicted <= guard)
+                accept = next.value <= point.value + guard && next.stat < point.stat;
+            else
+                accept = next.value <= point.value - 1e-4f * predicted;
+            if (accept) {
+                for (int i = 0; i < n; ++i) {
+                    point.w[i] = next.w[i];
+                    point.res[i] = next.res[i];
+                    point.lw[i] = next.lw[i];
+                }
+                point.value = next.value;
+                point.mag = next.mag;
+                point.stat = next.stat;
+                accepted = true;
+                break;
+            }
+        }
+        if (!accepted) break;
+    }
+    // decide at the end point
+    const float margin = so.decide * point.mag;
+    if (point.value < -margin) return tNegative;
+    if (point.stat > 10.f * so.stat_tol) return tMarginal;
+    for (int r = 0; r < nrefs; ++r) {
+        float dist = 0.f;
+        for (int i = 0; i < n; ++i)
+            if (c.z[i] > 0.f) dist = fmaxf(dist, fabsf(point.lw[i] - lrefs[r * NM + i]));
+        if (dist <= so.near_ref) return tTangent;
+    }
+    if (point.value > margin) return tPositive;
+    return tMarginal;
+}
+
+// ---------------------------------------------------------------------------
+// Rachford-Rice by bracketed Newton on the overflow-safe residual.
+template <int NM>
+struct SplitState {
+    float x[NM], y[NM], lnk[NM], res[NM], lnphi_l[NM], lnphi_v[NM];
+    float beta, z_l, z_v, gibbs, mag, fug;
+};
+
+template <int NM>
+__device__ bool solve_rr(const Cell<NM>& c, const float* lk, SplitState<NM>& s) {
+    const int n = c.n;
+    float e[NM], num[NM];
+    float gl = 0.f, gr = 0.f;  // residual at beta = 0+ and 1-
+    bool any = false;
+    for (int i = 0; i < n; ++i) {
+        if (c.z[i] == 0.f) continue;
+        any = any || lk[i] != 0.f;
+        e[i] = expf(-fabsf(lk[i]));
+        num[i] = lk[i] >= 0.f ? -expm1f(-lk[i]) : expm1f(lk[i]);
+    }
+    if (!any) return false;
+    // g(0) = sum z (K - 1), g(1) = sum z (1 - 1/K): interior root iff g(0) > 0 > g(1)
+    for (int i = 0; i < n; ++i) {
+        if (c.z[i] == 0.f) continue;
+        const float d0 = lk[i] >= 0.f ? e[i] : 1.f;
+        const float d1 = lk[i] >= 0.f ? 1.f : e[i];
+        gl += c.z[i] * num[i] / d0;
+        gr += c.z[i] * num[i] / d1;
+    }
+    if (!(gl > 0.f && gr < 0.f)) return false;
+    float lo = 0.f, hi = 1.f, beta = 0.5f;
+    for (int it = 0; it < 60; ++it) {
+        float g = 0.f, dg = 0.f;
+        for (int i = 0; i < n; ++i) {
+            if (c.z[i] == 0.f) continue;
+            const float den = lk[i] >= 0.f ? fmaf(1.f - e[i], beta, e[i]) : fmaf(e[i] - 1.f, beta, 1.f);
+            const float dd = lk[i] >= 0.f ? 1.f - e[i] : e[i] - 1.f;
+            const float t = c.z[i] * num[i] / den;
+            g += t;
+            dg -= t * dd / den;
+        }
+        if (g > 0.f) lo = beta; else hi = beta;
+        float bn = beta - g / dg;
+        if (!(bn > lo && bn < hi)) bn = 0.5f * (lo + hi);
+        const float step = fabsf(bn - beta);
+        beta = bn;
+        if (step <= 4.f * kEpsF * fminf(beta, 1.f - beta) || hi - lo <= 4.f * kEpsF * fminf(beta, 1.f - beta)) break;
+    }
+    float sx = 0.f, sy = 0.f;
+    for (int i = 0; i < n; ++i) {
+        s.x[i] = s.y[i] = 0.f;
+        if (c.z[i] == 0.f) continue;
+        const float den = lk[i] >= 0.f ? fmaf(1.f - e[i], beta, e[i]) : fmaf(e[i] - 1.f, beta, 1.f);
+        const float larger = c.z[i] / den;
+        s.x[i] = lk[i] >= 0.f ? larger * e[i] : larger;
+        s.y[i] = lk[i] >= 0.f ? larger : larger * e[i];
+        if (!(s.x[i] > 0.f && s.y[i] > 0.f)) return false;
+        sx += s.x[i];
+        sy += s.y[i];
+    }
+    for (int i = 0; i < n; ++i) {
+        s.x[i] /= sx;
+        s.y[i] /= sy;
+    }
+    s.beta = beta;
+    return beta > 0.f && beta < 1.f;
+}
+
+template <int NM>
+__device__ bool split_evaluate(const Mixture& m, Cell<NM>& c, const float* lk, SplitState<NM>& s) {
+    const int n = c.n;
+    if (!solve_rr(c, lk, s)) return false;
+    if (!role_provider(m, c, s.x, false, s.lnphi_l, s.z_l)) return false;
+    if (!role_provider(m, c, s.y, true, s.lnphi_v, s.z_v)) return false;
+    float gibbs = 0.f, mag = 1.f, fug = 0.f;
+    const float beta = s.beta;
+    for (int i = 0; i < n; ++i) {
+        s.lnk[i] = 0.f;
+        s.res[i] = 0.f;
+        if (c.z[i] == 0.f) continue;
+        const float lx = logf(s.x[i]), ly = logf(s.y[i]);
+        const float mu_l = lx + s.lnphi_l[i], mu_v = ly + s.lnphi_v[i];
+        s.lnk[i] = ly - lx;
+        s.res[i] = (lx - ly) + (s.lnphi_l[i] - s.lnphi_v[i]);
+        fug = fmaxf(fug, fabsf(s.res[i]));
+        gibbs += (1.f - beta) * s.x[i] * mu_l + beta * s.y[i] * mu_v;
+        mag += (1.f - beta) * s.x[i] * (fabsf(lx) + fabsf(s.lnphi_l[i])) + beta * s.y[i] * (fabsf(ly) + fabsf(s.lnphi_v[i]));
+    }
+    s.gibbs = gibbs;
+    s.mag = mag;
+    s.fug = fug;
+    return isfinite(gibbs) && isfinite(fug);
+}
+
+template <int NM>
+__device__ __forceinline__ void copy_state(SplitState<NM>& d, const SplitState<NM>& s, int n) {
+    for (int i = 0; i < n; ++i) {
+        d.x[i] = s.x[i];
+        d.y[i] = s.y[i];
+        d.lnk[i] = s.lnk[i];
+        d.res[i] = s.res[i];
+        d.lnphi_l[i] = s.lnphi_l[i];
+        d.lnphi_v[i] = s.lnphi_v[i];
+    }
+    d.beta = s.beta;
+    d.z_l = s.z_l;
+    d.z_v = s.z_v;
+    d.gibbs = s.gibbs;
+    d.mag = s.mag;
+    d.fug = s.fug;
+}
+
+// FP32 split attempt outcomes.
+enum SplitClass : int { aConverged = 0, aTrivial = 1, aFailed = 2 };
+
+// ln K successive substitution with the Gibbs line search (pt_split.hpp:349-407),
+// run until FP32 resolution (|r| <= 1e-5) or stagnation.
+template <int NM>
+__device__ int iterate_split(const Mixture& m, Cell<NM>& c, const float* lk0, SplitState<NM>& point,
+                             SplitState<NM>& next, float* next_lk) {
+    const int n = c.n;
+    if (!split_evaluate(m, c, lk0, point)) return aFailed;
+    for (int it = 0; it < 512; ++it) {
+        if (point.fug <= 2e-5f) break;
+        const float scale = fmaxf(1.f, point.fug / 2.f);
+        float h = 0.f, first = 0.f, second = 0.f;
+        for (int i = 0; i < n; ++i) {
+            if (c.z[i] == 0.f) continue;
+            const float cc = (point.x[i] / c.z[i]) * point.y[i];
+            const float d = point.y[i] - point.x[i];
+            h += d * (d / c.z[i]);
+            first += cc * point.res[i];
+            second += (cc * point.res[i]) * point.res[i];
+        }
+        const float slope = -(point.beta * (1.f - point.beta) * second + (first / h) * first) / scale;
+        if (!(slope < 0.f) || !isfinite(slope)) break;
+        bool accepted = false;
+        float alpha = 1.f;
+        for (int bt = 0; bt < 20; ++bt, alpha *= 0.5f) {
+            for (int i = 0; i < n; ++i) next_lk[i] = fmaf(alpha / scale, point.res[i], point.lnk[i]);
+            if (!split_evaluate(m, c, next_lk, next)) continue;
+            const float predicted = -alpha * slope;
+            const float guard = 64.f * kEpsF * (point.mag + next.mag);
+            const bool accept = predicted > guard
+                                    ? next.gibbs <= point.gibbs - 1e-4f * predicted
+                                    : (next.gibbs <= point.gibbs + guard &&
+                                       point.fug - next.fug > 1e-4f * (alpha / scale) * point.fug);
+            if (accept) {
+                copy_state(point, next, n);
+                accepted = true;
+                break;
+            }
+        }
+        if (!accepted) break;
+    }
+    float contrast = 0.f;
+    for (int i = 0; i < n; ++i) contrast = fmaxf(contrast, fabsf(point.lnk[i]));
+    if (contrast < 1e-4f || point.z_v - point.z_l <= 1e-5f * fmaxf(point.z_v, point.z_l)) return aTrivial;
+    return point.fug <= 1e-3f ? aConverged : aFailed;
+}
+
+}  // namespace fp32
+}  // namespace pr76

@@ -525,8 +525,13 @@ struct SplitState {
     int branch_l, branch_v;
 };
 
+// `newton` selects a bracketed Newton iteration on the same residual instead of
+// bisection (used by the mixed form's polish; the plain form uses bisection,
+// rachford_rice.hpp:93-107).  Both stop at the reference's width test
+// 8 eps min(beta, 1 - beta) and apply the same residual and balance checks.
 template <int NM>
-__device__ int solve_rr(Cell<NM>& c, const double* lk, SplitState<NM>& s, double* e, double* num) {
+__device__ int solve_rr(Cell<NM>& c, const double* lk, SplitState<NM>& s, double* e, double* num,
+                        bool newton = false) {
     const int n = c.n;
     double contrast = 0.0;
     for (int i = 0; i < n; ++i)
@@ -553,7 +558,43 @@ __device__ int solve_rr(Cell<NM>& c, const double* lk, SplitState<NM>& s, double
     }
     double left = 0.0, right = 1.0, beta = 0.5, value = 0.0;
     bool resolved = false;
-    for (int it = 0; it < 192; ++it) {
+    if (newton) {
+        for (int it = 0; it < 64; ++it) {
+            ++c.counters[cRrIters];
+            double v = 0.0, dv = 0.0;
+            for (int i = 0; i < n; ++i) {
+                if (c.z[i] == 0.0) continue;
+                const double den = lk[i] >= 0.0 ? beta + (1.0 - beta) * e[i] : (1.0 - beta) + beta * e[i];
+                const double dd = lk[i] >= 0.0 ? 1.0 - e[i] : e[i] - 1.0;
+                const double term = (c.z[i] / den) * num[i];
+                v += term;
+                dv -= term * dd / den;
+            }
+            value = v;
+            if (!isfinite(value)) return kRrUnrepresentable;
+            if (value == 0.0) {
+                resolved = true;
+                break;
+            }
+            if (value > 0.0) left = beta; else right = beta;
+            double bn = beta - value / dv;
+            if (!(bn > left && bn < right)) bn = (left + right) * 0.5;
+            const double step = fabs(bn - beta);
+            beta = bn;
+            if (step <= 8.0 * kEps * fmin(beta, 1.0 - beta) || right - left <= 8.0 * kEps * fmin(beta, 1.0 - beta)) {
+                double v2 = 0.0, cc = 0.0;
+                for (int i = 0; i < n; ++i) {
+                    if (c.z[i] == 0.0) continue;
+                    const double den = lk[i] >= 0.0 ? beta + (1.0 - beta) * e[i] : (1.0 - beta) + beta * e[i];
+                    kahan_add((c.z[i] / den) * num[i], v2, cc);
+                }
+                value = v2;
+                resolved = true;
+                break;
+            }
+        }
+    }
+    for (int it = 0; it < 192 && !resolved; ++it) {
         ++c.counters[cRrIters];
         beta = (left + right) * 0.5;
         if (!(beta > 0.0 && beta < 1.0)) break;
@@ -618,9 +659,9 @@ enum AttemptStatus : int { kConverged = 0, kNoInteriorRr, kRrFailure, kIndisting
 // or the failure class.
 template <int NM>
 __device__ int split_evaluate(const Mixture& m, Cell<NM>& c, const double* lk, SplitState<NM>& s, int& evals,
-                              int budget, double* e, double* num) {
+                              int budget, double* e, double* num, bool newton_rr = false) {
     const int n = c.n;
-    const int rr = solve_rr(c, lk, s, e, num);
+    const int rr = solve_rr(c, lk, s, e, num, newton_rr);
     if (rr != kRrInterior)
         return rr == kRrDegenerate ? kIndistinguishable : (rr == kRrNoInterior ? kNoInteriorRr : kRrFailure);
     if (evals >= budget) return kAttemptEvaluationLimit;

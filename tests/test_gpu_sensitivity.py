@@ -1,0 +1,127 @@
+"""GPU implicit sensitivities (forward AD) against the oracle, the reference's
+Decimal golden vectors and central finite differences."""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from mpmc_hnu_gb300 import synth
+from tests import parity
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+class Mix:
+    def __init__(self, d):
+        self.tc = np.array(d["tc"], float)
+        self.pc = np.array(d["pc"], float)
+        self.omega = np.array(d["omega"], float)
+        self.kij = np.array(d["kij"], float)
+        self.n = len(self.tc)
+
+    def as_tuple(self):
+        return self.tc, self.pc, self.omega, self.kij
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,ncell,seed", [(3, 128, 5), (4, 128, 6), (6, 192, 1), (10, 128, 2), (20, 48, 4)])
+def test_sensitivity_matches_oracle(gpu_lib, oracle_lib, n, ncell, seed):
+    mix = synth.make_mixture(n, seed)
+    p, t, z = synth.make_cells(n, ncell, seed)
+    ref = oracle_lib.flash(mix, p, t, z, threads=8, sens=True)
+    g = gpu_lib.GpuFlash(mix, form="plain", sensitivity=True)
+    out = g.solve(p, t, z)
+    assert np.array_equal(out["status"], ref["status"])
+    rep = parity.sensitivity_report(out, ref)
+    print(n, rep)
+    assert rep["status_match"] == 1.0, rep
+    assert rep["both_ok"] > 0
+    for f, v in rep["max"].items():
+        assert v <= parity.SENS_TOL, (f, rep)
+
+
+@pytest.mark.gpu
+def test_sensitivity_and_closure_kats(gpu_lib):
+    with open(os.path.join(GOLDEN, "kat.json")) as f:
+        kat = json.load(f)
+    R = 8.31446261815324
+    for case in kat["sensitivity"] + kat["closure"]:
+        mix = Mix(kat["mixtures"][case["mixture"]])
+        n = mix.n
+        q = n + 1
+        g = gpu_lib.GpuFlash(mix, form="plain", sensitivity=True)
+        r = g.solve(np.array([case["p"]]), np.array([case["t"]]), np.array(case["feed"], float)[:, None])
+        assert int(r["status"][0]) == 1 and int(r["sensitivity_status"][0]) == 0, case["name"]
+
+        def near(got, exp, tol):
+            exp = np.asarray(exp, float)
+            return np.all(np.abs(got - exp) <= tol * np.maximum(1e-7, np.abs(exp)))
+
+        if "dlnk" in case:
+            assert near(r["d_vapor_fraction"][:, 0], case["dbeta"], case["tol"]), case["name"]
+            for key, gk in (("dlnk", "d_ln_k"), ("dx", "d_liquid"), ("dy", "d_vapor")):
+                assert near(r[gk][:, 0].reshape(n, q), case[key], case["tol"]), (case["name"], key)
+        else:
+            zl, zv = r["z_liquid"][0], r["z_vapor"][0]
+            primal = [zl, zv, case["p"] / (zl * R * case["t"]), case["p"] / (zv * R * case["t"])]
+            for got, exp in zip(primal, case["primal"]):
+                assert abs(got - exp) <= case["primal_tol"] * (1 + abs(exp)), case["name"]
+            for key, gk in (("dzl", "d_z_liquid"), ("dzv", "d_z_vapor"), ("drhol", "d_rho_liquid"),
+                            ("drhov", "d_rho_vapor")):
+                assert near(r[gk][:, 0], case[key], case["tol"]), (case["name"], key)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,seed", [(4, 6), (10, 2)])
+def test_sensitivity_matches_central_differences(gpu_lib, oracle_lib, n, seed):
+    """AD columns vs central differences of the equilibrium.  The perturbed
+    states are solved by the GPU flash and then Newton-polished to |F| ~ 1e-15
+    so that the difference quotient is not swamped by the 1e-11 stopping band;
+    h = 1e-5 relative, tolerance 1e-6 relative to the column scale."""
+    mix = synth.make_mixture(n, seed)
+    p, t, z = synth.make_cells(n, 256, seed)
+    g = gpu_lib.GpuFlash(mix, form="plain", sensitivity=True)
+    base = g.solve(p, t, z)
+    ok = (base["sensitivity_status"] == 0) & (base["vapor_fraction"] > 0.05) & (base["vapor_fraction"] < 0.95)
+    cells = np.nonzero(ok)[0][:24]
+    assert cells.size >= 4
+    q = n + 1
+    worst = 0.0
+    for col in range(q):
+        h_rel = 1e-5
+        pp, tp, zp = p[cells].copy(), t[cells].copy(), z[:, cells].copy()
+        pm, tm, zm = pp.copy(), tp.copy(), zp.copy()
+        if col == 0:
+            h = h_rel * pp
+            pp += h
+            pm -= h
+        elif col == 1:
+            h = h_rel * tp
+            tp += h
+            tm -= h
+        else:
+            j = col - 2
+            h = h_rel * np.minimum(zp[j], zp[n - 1])
+            zp[j] += h
+            zp[n - 1] -= h
+            zm[j] -= h
+            zm[n - 1] += h
+        res = []
+        for (pa, ta, za) in ((pp, tp, zp), (pm, tm, zm)):
+            r = g.solve(pa, ta, za)
+            assert np.all(r["status"] == 1)
+            pol = oracle_lib.polish(mix, pa, ta, za, r["ln_k"], np.ones(len(cells), np.int32))
+            res.append(pol)
+        for gk, pk in (("d_ln_k", "ln_k"), ("d_liquid", "x"), ("d_vapor", "y")):
+            fd = (res[0][pk] - res[1][pk]) / (2 * h)
+            ad = base[gk].reshape(n, q, -1)[:, col, cells]
+            scale = np.maximum(np.abs(ad).max(axis=0), 1e-12)
+            err = np.abs(fd - ad) / scale
+            worst = max(worst, float(err.max()))
+        fd_b = (res[0]["beta"] - res[1]["beta"]) / (2 * h)
+        ad_b = base["d_vapor_fraction"][col, cells]
+        worst = max(worst, float((np.abs(fd_b - ad_b) / np.maximum(np.abs(ad_b), 1e-12 + np.abs(ad_b).max())).max()))
+    print("max relative FD discrepancy", worst)
+    assert worst <= 1e-6
