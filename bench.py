@@ -1,0 +1,411 @@
+"""Benchmark of the GB300 PR76 PT flash (one JSON line on rank 0).
+
+Workload (default): 1,048,576 cells of one seeded Nc = 10 mixture, FP64 outputs
+plus the forward-AD implicit derivatives (d ln K, d beta, d x, d y over
+q = (p, T, z_0..z_8), the closure dZ/d rho and the per-phase full-chart
+d[Z, ln phi]/d[p, T, x]).  70 % of the cells have p log-uniform on
+[0.5, 40] MPa; 30 % sit within +-2 % of their own phase-count change pressure
+(found by bisection with the flash itself on the GPU before timing).  Mixture
+and cell distributions: Tc ~ U[190, 620] K, Pc ~ U[2.5, 4.6] MPa,
+omega ~ U[0.01, 0.35], kij ~ U[0, 0.12], z ~ Dirichlet(1), T ~ U[280, 450] K.
+
+A step is one pass of the chosen form (batched mixed precision) over all
+cells, flash + derivatives, inputs already resident in HBM.  `e2e` times the
+same step through the host-buffer C ABI entry (pinned host inputs, every
+output copied back).  Inputs (96 MB) and outputs (~5 GB) exceed the 126 MB L2,
+so no extra flush is needed between steps.  The plain FP64 form is timed on a
+bounded sample of the same cells; the CPU oracle (the reference algorithm
+restated in C++) is timed on a bounded sample with every host thread.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MIXTURE_SEED = 1001
+CELL_SEED = 2001
+
+
+# ---------------------------------------------------------------------------
+# workload
+def f_eval(n: int) -> float:
+    """Algorithmic flops of one property evaluation (mixing with row sums,
+    cubic set-up, ln phi, TPD bookkeeping)."""
+    return 12 * n * (n - 1) / 2 + 6 * n + 10 * n + 40 + 14 * n + 30
+
+
+def f_ad(n: int) -> float:
+    return (2 / 3) * n ** 3 + 2 * n * n * (n + 1) + 2 * n * (2 * n + 1) * (n + 1) + 2 * (n + 2) * f_eval(n)
+
+
+def make_workload(n: int, ncell: int, near_fraction: float, rank: int, torch, flash, synth, log):
+    """Seeded cells; the near-saturation subset is placed by GPU bisection."""
+    mix = synth.make_mixture(n, MIXTURE_SEED)
+    offset = rank * (4 * ncell)
+    p, t, z = synth.make_cells(n, ncell, CELL_SEED, offset=offset)
+    n_near = int(round(near_fraction * ncell))
+    if n_near == 0:
+        return mix, p, t, z, 0
+    cache_dir = os.path.join(os.path.expanduser("~"), ".cache", "mpmc_gb300")
+    key = f"near_n{n}_c{ncell}_f{near_fraction}_r{rank}_m{MIXTURE_SEED}_s{CELL_SEED}.npz"
+    path = os.path.join(cache_dir, key)
+    if os.path.exists(path):
+        d = np.load(path)
+        return mix, d["p"], d["t"], d["z"], int(d["placed"])
+    t0 = time.time()
+    g = flash.GpuFlash(mix, "mixed")
+    idx = np.arange(n_near)  # the first n_near cells become near-saturation cells
+    # coarse log-p grid: phase count (1 or 2) at 9 pressures per cell
+    grid = np.exp(np.linspace(np.log(0.5e6), np.log(40e6), 9))
+    tt = np.repeat(t[idx], len(grid))
+    zz = np.repeat(z[:, idx], len(grid), axis=1)
+    pp = np.tile(grid, len(idx))
+    st = g.solve(pp, tt, zz, fields=["status"])["status"].reshape(len(idx), len(grid))
+    two = st == 1
+    lo = np.full(len(idx), np.nan)
+    hi = np.full(len(idx), np.nan)
+    lo_two = np.zeros(len(idx), bool)
+    for j in range(len(grid) - 1):
+        change = (two[:, j] != two[:, j + 1]) & ((st[:, j] <= 1) & (st[:, j + 1] <= 1)) & np.isnan(lo)
+        lo[change] = np.log(grid[j])
+        hi[change] = np.log(grid[j + 1])
+        lo_two[change] = two[change, j]
+    ok = np.isfinite(lo)
+    sel = np.nonzero(ok)[0]
+    for _ in range(7):  # bisection in ln p: bracket width 0.55 * 2**-7 < 0.5 %
+        mid = 0.5 * (lo[sel] + hi[sel])
+        s = g.solve(np.exp(mid), t[idx[sel]], z[:, idx[sel]], fields=["status"])["status"]
+        same_as_lo = (s == 1) == lo_two[sel]
+        lo[sel] = np.where(same_as_lo, mid, lo[sel])
+        hi[sel] = np.where(same_as_lo, hi[sel], mid)
+    from mpmc_hnu_gb300.synth import uniform, S_NEAR
+
+    u = uniform(CELL_SEED, S_NEAR, np.arange(offset, offset + n_near))
+    pb = np.exp(0.5 * (lo + hi))
+    placed = ok.copy()
+    p = p.copy()
+    p[idx[placed]] = pb[placed] * (1.0 + 0.04 * (u[placed] - 0.5))
+    g.close()
+    log(f"near-saturation placement: {int(placed.sum())}/{n_near} cells bracketed "
+        f"({time.time() - t0:.1f} s); the rest keep log-uniform p")
+    os.makedirs(cache_dir, exist_ok=True)
+    np.savez(path, p=p, t=t, z=z, placed=int(placed.sum()))
+    return mix, p, t, z, int(placed.sum())
+
+
+# ---------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, device: int):
+        self.samples = []
+        self.proc = None
+        self.device = device
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        reasons = set()
+        for s in self.samples:
+            for name, v in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"],
+                               s[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.samples)}
+
+
+def measured_peaks(flash_pkg):
+    lib = ctypes.CDLL(os.path.join(os.path.dirname(flash_pkg.__file__), "_lib", "libmpmc_gb300_probe.so"))
+    lib.mpmc_probe_fp64_flops.restype = ctypes.c_double
+    lib.mpmc_probe_fp32_flops.restype = ctypes.c_double
+    return lib.mpmc_probe_fp64_flops(200) / 1e12, lib.mpmc_probe_fp32_flops(2000) / 1e12
+
+
+def cpu_flash_rate(mix, p, t, z, sample: int, threads: int, sens: bool):
+    """The CPU oracle (reference algorithm in C++) on a bounded sample."""
+    from oracle import pyoracle
+
+    pyoracle.build()
+    sel = slice(0, sample)
+    t0 = time.perf_counter()
+    pyoracle.flash(mix, p[sel], t[sel], z[:, sel], threads=threads, sens=sens)
+    dt = time.perf_counter() - t0
+    return sample / dt, dt
+
+
+# ---------------------------------------------------------------------------
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--form", default="mixed", choices=["mixed", "plain"])
+    ap.add_argument("--n", type=int, default=10)
+    ap.add_argument("--cells", type=int, default=1 << 20)
+    ap.add_argument("--near-fraction", type=float, default=0.3)
+    ap.add_argument("--no-ad", action="store_true")
+    ap.add_argument("--plain-sample", type=int, default=32768)
+    ap.add_argument("--cpu-sample", type=int, default=16384)
+    ap.add_argument("--profile", action="store_true", help="one untimed solve of the workload (for ncu)")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    log = (lambda m: print(f"[bench] {m}", file=sys.stderr, flush=True)) if rank == 0 else (lambda m: None)
+    sens = not args.no_ad
+    threads = os.cpu_count() or 1
+
+    from mpmc_hnu_gb300 import synth
+
+    workload = {"workload": f"PR76 two-phase PT flash + implicit AD, Nc={args.n}, {args.cells} cells per GPU, "
+                            f"{int(args.near_fraction * 100)}% within 2% of the phase-boundary pressure",
+                "cells_per_gpu": args.cells, "components": args.n, "sensitivity": sens,
+                "form": args.form, "l2_flush": "inputs+outputs larger than L2", "parallelism": f"replicas{world}"}
+
+    if args.impl == "reference":
+        # the reference's CPU flash (C++ restatement; the reference sources are
+        # not present on the GPU host) on every host core; rank 0 only
+        if rank != 0:
+            return
+        mix = synth.make_mixture(args.n, MIXTURE_SEED)
+        p, t, z = synth.make_cells(args.n, args.cpu_sample, CELL_SEED)
+        rates = []
+        for k in range(args.warmup + args.steps):
+            r, _ = cpu_flash_rate(mix, p, t, z, args.cpu_sample, threads, sens)
+            if k >= args.warmup:
+                rates.append(r)
+        v = statistics.median(rates)
+        line = {"impl": "reference", "metric": "PT flashes/s (Nc=10, 1M cells)", "value": v, "unit": "flashes/s",
+                "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": args.cpu_sample / v * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded generator; log-uniform p sample)",
+                "config": {**workload, "cells_per_step": args.cpu_sample},
+                "cpu_baseline": {"value": v, "unit": "flashes/s", "cores": threads, "kind": "port",
+                                 "sample": f"{args.cpu_sample} cells of the same mixture per step"},
+                "e2e": {"value": v, "unit": "flashes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import torch
+
+    from mpmc_hnu_gb300 import build, flash
+
+    build.build()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local_rank)
+    device = torch.cuda.current_device()
+    torch.zeros(1, device="cuda")
+
+    mix, p, t, z, placed = make_workload(args.n, args.cells, args.near_fraction, rank, torch, flash, synth, log)
+    n, ncell = args.n, args.cells
+    g = flash.GpuFlash(mix, args.form, sensitivity=sens, device=device)
+    fields = g.fields()
+    rows = flash.output_rows(n)
+    dtypes = {f: d for f, d, _ in flash.OUTPUT_FIELDS}
+    dp = torch.tensor(p, device="cuda")
+    dt = torch.tensor(t, device="cuda")
+    dz = torch.tensor(z, device="cuda")
+    outs = {f: torch.empty((rows[f], ncell), device="cuda",
+                           dtype=torch.int32 if dtypes[f] == np.int32 else torch.float64) for f in fields}
+    ptrs = {f: v.data_ptr() for f, v in outs.items()}
+    stream = torch.cuda.current_stream()
+
+    def step():
+        g.solve_device(ncell, dp.data_ptr(), dt.data_ptr(), dz.data_ptr(), ptrs, stream.cuda_stream)
+
+    if args.profile:
+        step()
+        torch.cuda.synchronize()
+        log("profile solve done")
+        return
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with Clocks(device) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        tt_ = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(tt_, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt_.item())
+    value = world * ncell / (ms * 1e-3)
+    status = outs["status"][0].cpu().numpy()
+    counters = outs["counters"].cpu().numpy().astype(np.float64)
+
+    # end-to-end: pinned host inputs -> C ABI host entry -> every output back on the host
+    hp = torch.tensor(p).pin_memory()
+    ht = torch.tensor(t).pin_memory()
+    hz = torch.tensor(z).pin_memory()
+    houts = {f: torch.empty((rows[f], ncell), dtype=torch.int32 if dtypes[f] == np.int32 else torch.float64)
+             .pin_memory() for f in fields}
+    hptrs = {f: v.data_ptr() for f, v in houts.items()}
+    h2d = (2 + n) * 8 * ncell
+    d2h = sum(v.numel() * v.element_size() for v in houts.values())
+    g.solve_host_ptrs(ncell, hp.data_ptr(), ht.data_ptr(), hz.data_ptr(), hptrs)  # warm-up
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        g.solve_host_ptrs(ncell, hp.data_ptr(), ht.data_ptr(), hz.data_ptr(), hptrs)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if world > 1:
+        tt_ = torch.tensor([e2e_s], device="cuda")
+        torch.distributed.all_reduce(tt_, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(tt_.item())
+    e2e = {"value": world * ncell / e2e_s, "unit": "flashes/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    # per-stage device times (separate instrumented pass) for the roofline
+    gt = flash.GpuFlash(mix, args.form, sensitivity=sens, device=device, stage_timing=True)
+    gt.solve_device(ncell, dp.data_ptr(), dt.data_ptr(), dz.data_ptr(), ptrs, stream.cuda_stream)
+    stages = gt.stage_timings()
+    counters_t = outs["counters"].cpu().numpy().astype(np.float64)
+    gt.close()
+
+    # plain FP64 form on a bounded sample of the same cells
+    plain = None
+    if args.form == "mixed" and args.plain_sample > 0 and rank == 0:
+        ns = min(args.plain_sample, ncell)
+        gp = flash.GpuFlash(mix, "plain", sensitivity=sens, device=device)
+        sub = {f: v[:, :ns].contiguous() for f, v in outs.items()}
+        sp = {f: v.data_ptr() for f, v in sub.items()}
+        dps, dts, dzs = dp[:ns].contiguous(), dt[:ns].contiguous(), dz[:, :ns].contiguous()
+        gp.solve_device(min(ns, 4096), dps.data_ptr(), dts.data_ptr(), dzs.data_ptr(), sp, stream.cuda_stream)
+        torch.cuda.synchronize()
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        gp.solve_device(ns, dps.data_ptr(), dts.data_ptr(), dzs.data_ptr(), sp, stream.cuda_stream)
+        a1.record(stream)
+        torch.cuda.synchronize()
+        pms = a0.elapsed_time(a1)
+        ps = sub["status"][0].cpu().numpy()
+        plain = {"value": ns / (pms * 1e-3), "unit": "flashes/s", "cells": ns,
+                 "status_agreement_with_chosen": float((ps == status[:ns]).mean())}
+        gp.close()
+
+    fp64_tf, fp32_tf = measured_peaks(flash)
+    # roofline of the dominant stage: FP32 screening kernels on the FP32 pipe
+    ev32 = counters_t[0] + counters_t[1] + counters_t[2]
+    ev64 = counters_t[5]
+    fe = f_eval(n)
+    if args.form == "mixed":
+        dominant = max((k for k in stages if k != "sensitivity"), key=lambda k: stages[k])
+        fp32_stage = {"feed_trials": counters_t[0], "split": counters_t[1], "review_trials": counters_t[2]}
+        if dominant in fp32_stage:
+            flops = float(fp32_stage[dominant].sum()) * (fe + (6 * n if dominant == "split" else 0))
+            bound, peak = "fp32", fp32_tf
+        else:
+            flops = float(ev64.sum()) * fe
+            bound, peak = "fp64", fp64_tf
+    else:
+        dominant = "flash"
+        flops = float(ev32.sum()) * fe + float(counters_t[4].sum()) * 6 * n + float(counters_t[5].sum()) * 8
+        bound, peak = "fp64", fp64_tf
+    dom_ms = stages.get(dominant, ms)
+    achieved = flops / (dom_ms * 1e-3) / 1e12
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "dram_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tr = json.load(f)
+        key = f"{args.form}:{dominant}:n{n}"
+        if key in tr:
+            traffic = tr[key]["bytes_per_cell"] * ncell
+    roofline = {"bound": bound, "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": dominant, "kernel_ms": dom_ms,
+                "peak_source": "measured in this run by mpmc_hnu_gb300/csrc/peak_probe.cu (FMA chains)",
+                "flops_per_launch": flops, "stage_ms": stages,
+                "fp64_evals_per_cell": float(ev64.mean()), "fp32_evals_per_cell": float(ev32.mean())}
+
+    cpu = None
+    if rank == 0:
+        rate, secs = cpu_flash_rate(mix, p, t, z, min(args.cpu_sample, ncell), threads, sens)
+        cpu = {"value": rate, "unit": "flashes/s", "cores": threads, "kind": "port",
+               "sample": f"first {min(args.cpu_sample, ncell)} cells of this workload, flash + AD, "
+                         f"{secs:.1f} s wall on {threads} threads"}
+
+    if rank == 0:
+        line = {"metric": "PT flashes/s (Nc=10, 1M cells) mixed vs plain FP64", "value": value,
+                "unit": "flashes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 iterations + f64 decisions/polish/AD" if args.form == "mixed" else "f64",
+                "data": f"synthetic (seeded generator; {placed} near-boundary cells placed by GPU bisection)",
+                "config": workload, "e2e": e2e, "gpu_launches": len(stages) * args.steps,
+                "roofline": roofline, "cpu_baseline": cpu, "plain_fp64": plain,
+                "phase_counts": {"single": int((status == 0).sum()), "two": int((status == 1).sum()),
+                                 "unstable": int((status == 2).sum()), "indeterminate": int((status == 3).sum()),
+                                 "invalid": int((status == -1).sum())},
+                "clocks": clk.summary()}
+        print(json.dumps(line), flush=True)
+    g.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

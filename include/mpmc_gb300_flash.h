@@ -70,11 +70,13 @@ enum {
 /* Algorithm forms (same fixed points, different execution). */
 enum {
     MPMC_FORM_PLAIN_FP64 = 0, /* one thread per cell, reference algorithm in FP64 */
-    MPMC_FORM_BATCHED = 1,    /* persistent work-queue kernel, FP64 */
+    MPMC_FORM_BATCHED = 1,    /* reserved: work-queue form in FP64 (MPMC_ERR_UNSUPPORTED in this build) */
     MPMC_FORM_MIXED = 2       /* work queue, FP32 bulk iterations + FP64 polish/decisions */
 };
 
-/* Work counters per cell (int32 rows of the counters array). */
+/* Work counters per cell (int32 rows of the counters array).  In the mixed
+ * form rows 0-2 count FP32 property evaluations and row 5 counts every FP64
+ * property evaluation (the cubic is solved by Newton there). */
 enum {
     MPMC_COUNTER_INIT_EVALS = 0,   /* property evaluations, initial stability */
     MPMC_COUNTER_SPLIT_EVALS = 1,  /* property evaluations, split attempts */
@@ -99,11 +101,14 @@ typedef struct mpmc_pr76_mixture {
     const double* kij;                    /* [n*n] */
 } mpmc_pr76_mixture;
 
+/* Option flags (mpmc_flash_options.flags). */
+#define MPMC_FLAG_STAGE_TIMING 1 /* record CUDA events around every device stage */
+
 typedef struct mpmc_flash_options {
     int32_t form;              /* MPMC_FORM_* */
     int32_t want_sensitivity;  /* nonzero: compute the implicit derivatives */
     int32_t device;            /* CUDA device ordinal */
-    int32_t reserved;
+    int32_t flags;             /* MPMC_FLAG_* */
 } mpmc_flash_options;
 
 /* Outputs; layout a[k * n_cells + c].  q = n + 1 reduced columns
@@ -159,6 +164,16 @@ int mpmc_gpu_flash_solve(mpmc_gpu_flash* handle, int64_t n_cells, const double* 
  * first use (and grows as needed). */
 int mpmc_gpu_flash_solve_device(mpmc_gpu_flash* handle, int64_t n_cells, const double* p, const double* t,
                                 const double* z, const mpmc_flash_outputs* out, void* stream);
+
+/* Device time in milliseconds of every stage of the last solve on a handle
+ * created with MPMC_FLAG_STAGE_TIMING (waits for that solve to finish).
+ * Stages, in order -- plain form: flash, sensitivity; mixed form: setup,
+ * feed_trials, decide, split, polish, relist, review_trials, finish,
+ * fallback, sensitivity.  Writes up to `capacity` values and returns the
+ * number of stages (0 if timing is off or nothing ran).  Diagnostic entry
+ * point with no counterpart in the reference (whose solver results carry
+ * work counters only, pt_stability.hpp:66-76). */
+int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* handle, float* ms, int capacity);
 
 /* Number of components of the handle's mixture. */
 int mpmc_gpu_flash_components(const mpmc_gpu_flash* handle);

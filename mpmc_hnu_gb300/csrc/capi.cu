@@ -64,6 +64,9 @@ struct mpmc_gpu_flash {
     DevBuf outs[kOutputFields];
     DevBuf sens_inputs[7];
     DevBuf workspace;  // batched-form stage buffers and work queues
+    bool stage_timing = false;
+    cudaEvent_t events[16] = {};
+    int n_events = 0;   // events recorded by the last solve (stages + 1)
 };
 
 namespace {
@@ -179,18 +182,30 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
         if (rc != MPMC_OK) return rc;
     }
     cudaError_t e;
+    h->n_events = 0;
+    if (h->stage_timing && !h->events[0]) {
+        for (auto& ev : h->events)
+            if ((e = cudaEventCreate(&ev)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+    }
+    int next_event = 0;
+    auto record = [&]() {
+        if (h->stage_timing && next_event < 16) cudaEventRecord(h->events[next_event++], stream);
+    };
     switch (h->form) {
     case MPMC_FORM_PLAIN_FP64:
+        record();
         e = pr76::launch_plain(h->n, h->d_mixture, ncell, p, t, z, d, stream);
+        record();
         break;
     case MPMC_FORM_MIXED: {
         const size_t need = pr76::batched_workspace_bytes(h->n, ncell);
         if ((e = h->workspace.ensure(need)) != cudaSuccess) return cuda_fail(e, "batched workspace allocation");
-        pr76::BatchedShape shape{0, 0};
+        pr76::BatchedShape shape{0, 0, h->stage_timing ? h->events : nullptr};
         if (const char* v = std::getenv("MPMC_TRIAL_BLOCKS_PER_SM")) shape.trial_blocks_per_sm = std::atoi(v);
         if (const char* v = std::getenv("MPMC_SPLIT_BLOCKS_PER_SM")) shape.split_blocks_per_sm = std::atoi(v);
         e = pr76::launch_batched(h->n, h->d_mixture, ncell, p, t, z, d, h->workspace.ptr, h->workspace.bytes, shape,
                                  stream);
+        next_event = h->stage_timing ? pr76::kBatchedStages + 1 : 0;
         break;
     }
     default:
@@ -200,7 +215,11 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
     if (h->want_sensitivity) {
         e = pr76::launch_sensitivity(h->n, h->d_mixture, ncell, p, t, z, d, stream);
         if (e != cudaSuccess) return cuda_fail(e, "sensitivity kernel launch");
+    } else if (h->stage_timing) {
+        record();  // zero-length sensitivity stage keeps the stage list fixed
     }
+    if (h->want_sensitivity) record();
+    h->n_events = next_event;
     return MPMC_OK;
 }
 
@@ -283,6 +302,18 @@ const char* mpmc_gpu_flash_last_error(void) { return g_last_error.c_str(); }
 
 int mpmc_gpu_flash_components(const mpmc_gpu_flash* h) { return h ? h->n : 0; }
 
+int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* h, float* ms, int capacity) {
+    if (!h || !h->stage_timing || h->n_events < 2) return 0;
+    if (cudaEventSynchronize(h->events[h->n_events - 1]) != cudaSuccess) return 0;
+    const int stages = h->n_events - 1;
+    for (int k = 0; k < stages && k < capacity; ++k) {
+        float v = 0.f;
+        cudaEventElapsedTime(&v, h->events[k], h->events[k + 1]);
+        if (ms) ms[k] = v;
+    }
+    return stages;
+}
+
 int mpmc_gpu_flash_create(const mpmc_pr76_mixture* mixture, const mpmc_flash_options* options,
                           mpmc_gpu_flash** out) {
     if (!mixture || !out) return fail(MPMC_ERR_INVALID_ARGUMENT, "mixture and out must not be null");
@@ -307,6 +338,7 @@ int mpmc_gpu_flash_create(const mpmc_pr76_mixture* mixture, const mpmc_flash_opt
     h->device = opt.device;
     h->form = opt.form;
     h->want_sensitivity = opt.want_sensitivity;
+    h->stage_timing = (opt.flags & MPMC_FLAG_STAGE_TIMING) != 0;
     h->host_mixture = m;
     e = cudaMalloc(&h->d_mixture, sizeof(pr76::Mixture));
     if (e == cudaSuccess) e = cudaMemcpy(h->d_mixture, &m, sizeof(pr76::Mixture), cudaMemcpyHostToDevice);
@@ -330,6 +362,8 @@ int mpmc_gpu_flash_destroy(mpmc_gpu_flash* h) {
     for (auto& b : h->outs) b.release();
     for (auto& b : h->sens_inputs) b.release();
     h->workspace.release();
+    for (auto& ev : h->events)
+        if (ev) cudaEventDestroy(ev);
     if (h->d_mixture) cudaFree(h->d_mixture);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;

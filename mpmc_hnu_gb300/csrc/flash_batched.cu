@@ -90,15 +90,30 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
                                                         : resident_blocks(trials32_kernel<NM>, qblock);
     const int split_res = shape.split_blocks_per_sm > 0 ? shape.split_blocks_per_sm
                                                         : resident_blocks(split32_kernel<NM>, qblock);
+    int stage = 0;
+    auto mark = [&]() {
+        if (shape.events) cudaEventRecord(shape.events[stage], stream);
+        ++stage;
+    };
+    mark();
     setup_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, p, t, z, out);
+    mark();
     trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 0);
+    mark();
     decide_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+    mark();
     split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t);
+    mark();
     polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+    mark();
     relist_kernel<NM><<<1, 1024, 0, stream>>>(ws);
+    mark();
     trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 1);
+    mark();
     finish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+    mark();
     fallback_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, z, out);
+    mark();
     return cudaGetLastError();
 }
 

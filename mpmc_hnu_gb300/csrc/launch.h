@@ -48,7 +48,9 @@ LaunchShape plain_launch_shape();
 struct BatchedShape {
     int trial_blocks_per_sm;
     int split_blocks_per_sm;
+    cudaEvent_t* events;  // optional: kBatchedStages + 1 events recorded around the stages
 };
+constexpr int kBatchedStages = 9;
 
 // Batched mixed-precision flash (flash_batched.cu): scratch bytes needed for
 // ncell cells, and the launch sequence using that scratch.

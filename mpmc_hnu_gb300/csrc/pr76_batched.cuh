@@ -33,6 +33,10 @@ namespace pr76 {
 namespace batched {
 
 constexpr int kMaxAttempts = 16;
+// In the mixed form, counter rows 0-2 hold FP32 property evaluations of the
+// feed trials, split attempts and review trials, and this row (the plain
+// form's cubic-iteration row) holds every FP64 property evaluation.
+constexpr int kFp64EvalRow = cRootIters;
 
 // Queue/counter slots in Workspace::counters.
 enum Slot : int {
@@ -151,7 +155,8 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
         }
         ws.phase[c] = ph;
         ws.att_count[c] = 0;
-        for (int k = 0; k < cCount; ++k) ws.counters_out[idx(k, ws.ncell, c)] = cell.counters[k];
+        for (int k = 0; k < cCount; ++k) ws.counters_out[idx(k, ws.ncell, c)] = 0;
+        ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)] = cell.counters[cInitEvals];
         if (ph == pInvalid || ph == pIndeterminate) {
             const double nan = __longlong_as_double(0x7ff8000000000000LL);
             if (out.status) out.status[c] = ph == pInvalid ? static_cast<int>(kInvalid) : static_cast<int>(kIndeterminate);
@@ -194,6 +199,9 @@ struct TrialLane {
     int c, k, iter, bt, stage;  // stage: 0 = evaluate start, 1 = line search, 2 = finished
     float alpha, slope, scale;
     int result;
+    // convergence-rate checkpoints: stationarity at the last two multiples of 8 iterations
+    float ck_stat, ck_prev_stat;
+    int ck_iter, ck_prev_iter;
 };
 
 template <int NM>
@@ -207,6 +215,8 @@ __device__ void trial_begin(const Mixture& m, const Workspace& ws, const double*
     L.bt = 0;
     L.stage = 0;
     L.result = fp32::tMarginal;
+    L.ck_stat = L.ck_prev_stat = INFINITY;
+    L.ck_iter = L.ck_prev_iter = 0;
     int active;
     if (!load_cell32(m, ws, c, p, t, L.cell, active)) {
         L.stage = 2;
@@ -318,6 +328,18 @@ __device__ void trial_step_or_finish(TrialLane<NM>& L) {
     L.stage = 1;
 }
 
+// Iterations the reference's FP64 descent would still need to reach its
+// stationarity tolerance 1e-8 (pt_stability.hpp:384), extrapolated from the
+// linear contraction rate over the last checkpoint window.
+template <int NM>
+__device__ float projected_fp64_iterations(const TrialLane<NM>& L) {
+    if (!(L.point.stat > 1e-8f)) return static_cast<float>(L.iter);
+    const int span = L.iter - L.ck_prev_iter;
+    if (span < 4 || !(L.ck_prev_stat < INFINITY) || !(L.ck_prev_stat > L.point.stat)) return 1e9f;
+    const float rate = logf(L.ck_prev_stat / L.point.stat) / static_cast<float>(span);  // per iteration
+    return static_cast<float>(L.iter) + logf(L.point.stat / 1e-8f) / rate;
+}
+
 template <int NM>
 __device__ int trial_classify(const TrialLane<NM>& L) {
     const fp32::ScreenOptions so = fp32::screen_options();
@@ -325,6 +347,9 @@ __device__ int trial_classify(const TrialLane<NM>& L) {
     const float margin = so.decide * L.point.mag;
     if (L.point.value < -margin) return fp32::tNegative;
     if (L.point.stat > 10.f * so.stat_tol || L.iter >= 400) return fp32::tMarginal;
+    // a descent that would exhaust the reference's 512-iteration budget ends
+    // "iteration_limit" there: re-run it exactly in FP64
+    if (projected_fp64_iterations(L) > 320.f) return fp32::tMarginal;
     for (int r = 0; r < L.nrefs; ++r) {
         float dist = 0.f;
         for (int i = 0; i < n; ++i)
@@ -399,6 +424,12 @@ __global__ void __launch_bounds__(128) trials32_kernel(const Mixture* __restrict
         if (accept) {
             L.point = L.next;
             ++L.iter;
+            if ((L.iter & 7) == 0) {
+                L.ck_prev_stat = L.ck_stat;
+                L.ck_prev_iter = L.ck_iter;
+                L.ck_stat = L.point.stat;
+                L.ck_iter = L.iter;
+            }
             trial_step_or_finish(L);
         } else if (++L.bt >= 24) {
             L.stage = 2;
@@ -539,7 +570,7 @@ __global__ void __launch_bounds__(64) decide_kernel(const Mixture* __restrict__ 
             }
         }
         ws.att_count[c] = nattempt;
-        atomicAdd(&ws.counters_out[idx(cInitEvals, ws.ncell, c)], cell.counters[cInitEvals]);
+        atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], cell.counters[cInitEvals]);
         if (negative) {
             ws.phase[c] = pSplit;
             atomicAdd(&ws.counters_out[idx(cAttempts, ws.ncell, c)], nattempt);
@@ -822,7 +853,7 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
             ws.cand_s[idx(3, ws.ncell, c)] = st.fug;
             ws.cand_s[idx(7, ws.ncell, c)] = st.guard;
         }
-        atomicAdd(&ws.counters_out[idx(cSplitEvals, ws.ncell, c)], c64.counters[cSplitEvals]);
+        atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], c64.counters[cSplitEvals]);
         atomicAdd(&ws.counters_out[idx(cRrIters, ws.ncell, c)], c64.counters[cRrIters]);
         if (!have) {
             ws.phase[c] = pFallback;
@@ -914,7 +945,7 @@ __global__ void __launch_bounds__(64) finish_kernel(const Mixture* __restrict__ 
                 else if (ts != fp64::kStationary) stationary = false;
             }
         }
-        atomicAdd(&ws.counters_out[idx(cFinalEvals, ws.ncell, c)], cell.counters[cFinalEvals]);
+        atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], cell.counters[cFinalEvals]);
         int status;
         if (negative) status = kPhaseSetUnstable;
         else if (ws.cand_s[idx(4, ws.ncell, c)] > ws.cand_s[idx(5, ws.ncell, c)]) status = kIndeterminate;

@@ -37,7 +37,7 @@ class _Mixture(ctypes.Structure):
 
 class _Options(ctypes.Structure):
     _fields_ = [("form", ctypes.c_int32), ("want_sensitivity", ctypes.c_int32), ("device", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("flags", ctypes.c_int32)]
 
 
 # (field, dtype, rows(n)) in mpmc_flash_outputs order
@@ -64,7 +64,11 @@ class _Outputs(ctypes.Structure):
 
 EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu_flash_solve",
                     "mpmc_gpu_flash_solve_device", "mpmc_gpu_flash_components", "mpmc_gpu_flash_last_error",
-                    "mpmc_gpu_flash_abi_version"]
+                    "mpmc_gpu_flash_abi_version", "mpmc_gpu_flash_stage_timings"]
+FLAG_STAGE_TIMING = 1
+STAGES = {FORM_PLAIN_FP64: ["flash", "sensitivity"],
+          FORM_MIXED: ["setup", "feed_trials", "decide", "split", "polish", "relist", "review_trials", "finish",
+                       "fallback", "sensitivity"]}
 
 _LIB = None
 
@@ -84,6 +88,7 @@ def library() -> ctypes.CDLL:
         lib.mpmc_gpu_flash_solve_device.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 3 + \
             [ctypes.POINTER(_Outputs), ctypes.c_void_p]
         lib.mpmc_gpu_flash_components.argtypes = [ctypes.c_void_p]
+        lib.mpmc_gpu_flash_stage_timings.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         for name in EXPORTED_SYMBOLS:
             getattr(lib, name).restype = ctypes.c_int
         lib.mpmc_gpu_flash_last_error.restype = ctypes.c_char_p
@@ -109,7 +114,8 @@ def output_rows(n: int) -> dict[str, int]:
 class GpuFlash:
     """One mixture on one GPU; batches of cells per call."""
 
-    def __init__(self, mixture, form: str | int = "plain", sensitivity: bool = False, device: int = 0):
+    def __init__(self, mixture, form: str | int = "plain", sensitivity: bool = False, device: int = 0,
+                 stage_timing: bool = False):
         self.mixture = mixture
         self.n = int(mixture.n)
         self.form = FORMS[form] if isinstance(form, str) else int(form)
@@ -117,7 +123,7 @@ class GpuFlash:
         self._keep = [np.ascontiguousarray(a, dtype=np.float64) for a in
                       (mixture.tc, mixture.pc, mixture.omega, np.asarray(mixture.kij).reshape(-1))]
         m = _Mixture(self.n, *(a.ctypes.data for a in self._keep))
-        o = _Options(self.form, int(self.sensitivity), device, 0)
+        o = _Options(self.form, int(self.sensitivity), device, FLAG_STAGE_TIMING if stage_timing else 0)
         h = ctypes.c_void_p()
         _check(library().mpmc_gpu_flash_create(ctypes.byref(m), ctypes.byref(o), ctypes.byref(h)))
         self._h = h
@@ -153,6 +159,18 @@ class GpuFlash:
         _check(library().mpmc_gpu_flash_solve(self._h, ncell, p.ctypes.data, t.ctypes.data, z.ctypes.data,
                                               ctypes.byref(s)))
         return {f: (v[0] if rows[f] == 1 else v) for f, v in out.items()}
+
+    def solve_host_ptrs(self, ncell: int, p_ptr: int, t_ptr: int, z_ptr: int, out_ptrs: dict[str, int]) -> None:
+        """Host-buffer entry with caller-owned (e.g. pinned) host pointers."""
+        s = _Outputs(**out_ptrs)
+        _check(library().mpmc_gpu_flash_solve(self._h, ncell, p_ptr, t_ptr, z_ptr, ctypes.byref(s)))
+
+    def stage_timings(self) -> dict[str, float]:
+        """Per-stage device milliseconds of the last solve (stage_timing=True)."""
+        ms = np.zeros(16, np.float32)
+        k = library().mpmc_gpu_flash_stage_timings(self._h, ms.ctypes.data, 16)
+        names = STAGES.get(self.form, [])
+        return {names[i] if i < len(names) else f"stage{i}": float(ms[i]) for i in range(max(k, 0))}
 
     def solve_device(self, ncell: int, p_ptr: int, t_ptr: int, z_ptr: int, out_ptrs: dict[str, int],
                      stream: int = 0) -> None:

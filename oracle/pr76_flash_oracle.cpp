@@ -1887,6 +1887,90 @@ int oracle_polish_batch(int n, const double* tc, const double* pc, const double*
     return 0;
 }
 
+// Sensitivities (differentiate_pr76_pt_vle + closure + per-phase Jacobians) at
+// GIVEN accepted two-phase states (x, y, ln K, beta per cell), so that a
+// device implementation can be compared at identical base points.  Only
+// cells with ok[c] != 0 are processed; `out` uses the OracleOutputs layout
+// (sensitivity fields only).
+int oracle_sensitivity_at(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                          int64_t ncell, const double* p, const double* t, const double* z, const int32_t* ok,
+                          const double* x, const double* y, const double* lnk, const double* beta, int threads,
+                          const OracleOutputs* o) {
+    using namespace oracle;
+    const Model m = make_model(n, tc, pc, omega, kij);
+    auto run = [&](int64_t lo, int64_t hi) {
+        Work wk;
+        wk.init(n);
+        for (int64_t c = lo; c < hi; ++c) {
+            auto put = [&](double* arr, int k, double v) {
+                if (arr) arr[k * ncell + c] = v;
+            };
+            Sensitivity s;
+            s.status = 1;
+            if (ok[c] && make_temp_cache(m, t[c], wk.tc)) {
+                FlashResult fr;
+                fr.status = kTwoPhase;
+                fr.has_candidate = true;
+                std::vector<double> feed(n);
+                double sum = 0, cs = 0;
+                for (int i = 0; i < n; ++i) kahan_add(z[i * ncell + c], sum, cs);
+                for (int i = 0; i < n; ++i) feed[i] = z[i * ncell + c] / sum;
+                fr.initial.feed = feed;
+                SplitState& st = fr.candidate;
+                st.rr.x.resize(n);
+                st.rr.y.resize(n);
+                st.log_k.resize(n);
+                for (int i = 0; i < n; ++i) {
+                    st.rr.x[i] = x[i * ncell + c];
+                    st.rr.y[i] = y[i * ncell + c];
+                    st.log_k[i] = lnk[i * ncell + c];
+                }
+                st.rr.beta = beta[c];
+                Issue a = role_provider(m, wk, p[c], t[c], st.rr.x.data(), false, st.liquid);
+                Issue b = role_provider(m, wk, p[c], t[c], st.rr.y.data(), true, st.vapor);
+                if (a == kOk && b == kOk) {
+                    st.fug_norm = 0;
+                    for (int i = 0; i < n; ++i)
+                        st.fug_norm = std::max(st.fug_norm, std::abs(std::log(st.rr.x[i]) - std::log(st.rr.y[i]) +
+                                                                     st.liquid.ln_phi[i] - st.vapor.ln_phi[i]));
+                    differentiate(m, fr, p[c], t[c], s);
+                } else {
+                    s.status = 4;
+                }
+            }
+            if (o->sens_status) o->sens_status[c] = s.status;
+            const int q = n + 1;
+            const bool good = s.status == 0;
+            const double nan = kNaN;
+            for (int k = 0; k < n * q; ++k) {
+                put(o->dlnk, k, good ? s.dlnk[k] : nan);
+                put(o->dx, k, good ? s.dx[k] : nan);
+                put(o->dy, k, good ? s.dy[k] : nan);
+            }
+            for (int k = 0; k < q; ++k) {
+                put(o->dbeta, k, good ? s.dbeta[k] : nan);
+                put(o->dzl, k, good ? s.dzl[k] : nan);
+                put(o->dzv, k, good ? s.dzv[k] : nan);
+                put(o->drhol, k, good ? s.drhol[k] : nan);
+                put(o->drhov, k, good ? s.drhov[k] : nan);
+            }
+            for (int k = 0; k < (n + 1) * (n + 2); ++k) {
+                put(o->jl, k, good ? s.jl[k] : nan);
+                put(o->jv, k, good ? s.jv[k] : nan);
+            }
+        }
+    };
+    if (threads < 1) threads = 1;
+    std::vector<std::thread> pool;
+    const int64_t chunk = (ncell + threads - 1) / threads;
+    for (int k = 0; k < threads; ++k) {
+        const int64_t lo = k * chunk, hi = std::min<int64_t>(ncell, lo + chunk);
+        if (lo < hi) pool.emplace_back(run, lo, hi);
+    }
+    for (auto& th : pool) th.join();
+    return 0;
+}
+
 // Rachford-Rice at fixed ln K.  Returns the RR status code.
 int oracle_rachford_rice(int n, const double* z, const double* ln_k, double* beta, double* x, double* y) {
     std::vector<double> zz(z, z + n), lk(ln_k, ln_k + n);

@@ -151,3 +151,25 @@ def polish(mix, p, t, z, ln_k, ok, threads: int = 8):
                                    ("ln_k", "beta", "x", "y", "residual", "ainv")]
     fn(*args)
     return out
+
+
+def sensitivity_at(mix, p, t, z, ok, x, y, ln_k, beta, threads: int = 8):
+    """Oracle sensitivities at GIVEN accepted two-phase states (see
+    oracle_sensitivity_at): isolates the derivative computation from the
+    convergence noise of the flash that produced the state."""
+    build()
+    tc, pc, omega, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
+    z = np.ascontiguousarray(z, dtype=np.float64)
+    n, ncell = z.shape
+    out, s = _alloc(n, ncell, True)
+    arrays = [np.ascontiguousarray(np.nan_to_num(np.asarray(a, dtype=np.float64), nan=0.5)) for a in (x, y, ln_k)]
+    b = np.ascontiguousarray(np.nan_to_num(np.asarray(beta, dtype=np.float64), nan=0.5))
+    okv = np.ascontiguousarray(np.asarray(ok, dtype=np.int32))
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    fn = _lib(ORACLE_SO).oracle_sensitivity_at
+    fn.restype = ctypes.c_int
+    fn(ctypes.c_int(n), *(ctypes.c_void_p(a.ctypes.data) for a in (tc, pc, omega, kij)), ctypes.c_int64(ncell),
+       *(ctypes.c_void_p(a.ctypes.data) for a in (p, t, z, okv)), *(ctypes.c_void_p(a.ctypes.data) for a in arrays),
+       ctypes.c_void_p(b.ctypes.data), ctypes.c_int(threads), ctypes.byref(s))
+    return out

@@ -26,16 +26,22 @@ class Mix:
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("form", ["plain", "mixed"])
 @pytest.mark.parametrize("n,ncell,seed", [(3, 128, 5), (4, 128, 6), (6, 192, 1), (10, 128, 2), (20, 48, 4)])
-def test_sensitivity_matches_oracle(gpu_lib, oracle_lib, n, ncell, seed):
+def test_sensitivity_matches_oracle(gpu_lib, oracle_lib, n, ncell, seed, form):
+    """Device AD vs the oracle's differentiate_pr76_pt_vle restatement at the
+    SAME accepted states (the GPU's), so only the derivative computation is
+    compared; 1e-8 relative to each column's scale."""
     mix = synth.make_mixture(n, seed)
     p, t, z = synth.make_cells(n, ncell, seed)
-    ref = oracle_lib.flash(mix, p, t, z, threads=8, sens=True)
-    g = gpu_lib.GpuFlash(mix, form="plain", sensitivity=True)
+    g = gpu_lib.GpuFlash(mix, form=form, sensitivity=True)
     out = g.solve(p, t, z)
-    assert np.array_equal(out["status"], ref["status"])
+    two = out["status"] == 1
+    ref = oracle_lib.sensitivity_at(mix, p, t, z, two, out["liquid"], out["vapor"], out["ln_k"],
+                                    out["vapor_fraction"])
+    ref["sens_status"] = np.where(two, ref["sens_status"], 1)
     rep = parity.sensitivity_report(out, ref)
-    print(n, rep)
+    print(form, n, rep)
     assert rep["status_match"] == 1.0, rep
     assert rep["both_ok"] > 0
     for f, v in rep["max"].items():
@@ -79,7 +85,9 @@ def test_sensitivity_matches_central_differences(gpu_lib, oracle_lib, n, seed):
     """AD columns vs central differences of the equilibrium.  The perturbed
     states are solved by the GPU flash and then Newton-polished to |F| ~ 1e-15
     so that the difference quotient is not swamped by the 1e-11 stopping band;
-    h = 1e-5 relative, tolerance 1e-6 relative to the column scale."""
+    h = 1e-5 relative for p and T, 1e-4 of the smaller of the two moved feed
+    fractions for composition columns; tolerance 1e-6 relative to the column
+    scale."""
     mix = synth.make_mixture(n, seed)
     p, t, z = synth.make_cells(n, 256, seed)
     g = gpu_lib.GpuFlash(mix, form="plain", sensitivity=True)
@@ -103,7 +111,7 @@ def test_sensitivity_matches_central_differences(gpu_lib, oracle_lib, n, seed):
             tm -= h
         else:
             j = col - 2
-            h = h_rel * np.minimum(zp[j], zp[n - 1])
+            h = 1e-4 * np.minimum(zp[j], zp[n - 1])
             zp[j] += h
             zp[n - 1] -= h
             zm[j] -= h
