@@ -175,6 +175,17 @@ int mpmc_gpu_flash_solve_device(mpmc_gpu_flash* handle, int64_t n_cells, const d
  * work counters only, pt_stability.hpp:66-76). */
 int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* handle, float* ms, int capacity);
 
+/* Work statistics of the last mixed-form solve on a handle (waits for the
+ * device): [0] feed trials continued in FP64 from their FP32 end point,
+ * [1] feed trials re-run exactly in FP64, [2] review trials continued,
+ * [3] review trials re-run, [4..8] cells sent to the FP64 fallback because
+ * of a nonsmooth feed phase / no settled FP32 attempt / a polish that did not
+ * converge / a polished pair rejected by the acceptance rules / unusable
+ * cell constants, [9] cells whose two best attempts were both polished.
+ * Writes up to `capacity` values; returns the number available (0 for the
+ * plain form).  Diagnostic entry point with no counterpart in the reference. */
+int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* handle, int64_t* out, int capacity);
+
 /* Number of components of the handle's mixture. */
 int mpmc_gpu_flash_components(const mpmc_gpu_flash* handle);
 

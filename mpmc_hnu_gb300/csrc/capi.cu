@@ -106,7 +106,9 @@ int prepare_mixture(const mpmc_pr76_mixture* mix, pr76::Mixture& m) {
             if (i == j && k != 0.0) return fail(MPMC_ERR_DOMAIN, "kij diagonal must be zero");
             if (k != mix->kij[j * n + i]) return fail(MPMC_ERR_DOMAIN, "kij must be symmetric");
             m.factor[i * n + j] = 1.0 - k;
+            m.factor32[i * n + j] = static_cast<float>(m.factor[i * n + j]);
         }
+    for (int i = 0; i < n; ++i) m.b32[i] = static_cast<float>(m.b[i]);
     return MPMC_OK;
 }
 
@@ -301,6 +303,20 @@ int mpmc_gpu_flash_abi_version(void) { return MPMC_GB300_FLASH_ABI_VERSION; }
 const char* mpmc_gpu_flash_last_error(void) { return g_last_error.c_str(); }
 
 int mpmc_gpu_flash_components(const mpmc_gpu_flash* h) { return h ? h->n : 0; }
+
+int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* h, int64_t* out, int capacity) {
+    if (!h || h->form != MPMC_FORM_MIXED || !h->workspace.ptr) return 0;
+    constexpr int kFirst = 8, kCount = 10;  // workspace counter slots 8..17
+    int vals[kCount] = {};
+    if (cudaSetDevice(h->device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return 0;
+    // the counters are the first array of the workspace
+    if (cudaMemcpy(vals, static_cast<int*>(h->workspace.ptr) + kFirst, sizeof(vals), cudaMemcpyDeviceToHost) !=
+        cudaSuccess)
+        return 0;
+    for (int k = 0; k < kCount && k < capacity; ++k)
+        if (out) out[k] = vals[k];
+    return kCount;
+}
 
 int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* h, float* ms, int capacity) {
     if (!h || !h->stage_timing || h->n_events < 2) return 0;

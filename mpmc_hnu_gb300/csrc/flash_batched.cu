@@ -47,6 +47,8 @@ size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell) {
     ws.cand = reinterpret_cast<double*>(take(sizeof(double) * 7 * NM * nc));
     ws.cand_s = reinterpret_cast<double*>(take(sizeof(double) * 8 * nc));
     ws.counters_out = reinterpret_cast<int*>(take(sizeof(int) * cCount * nc));
+    ws.c32 = reinterpret_cast<float*>(take(sizeof(float) * 4 * NM * nc));
+    ws.ref32 = reinterpret_cast<float*>(take(sizeof(float) * NM * nc));
     return off;
 }
 

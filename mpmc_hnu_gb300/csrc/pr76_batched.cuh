@@ -45,7 +45,18 @@ enum Slot : int {
     qAttempts = 2,     // attempt items listed
     qAttemptCursor = 3,
     qFallback = 4,     // cells listed for the FP64 fallback
-    qSlots = 8
+    // diagnostic statistics of the last batch
+    sFeedContinued = 8,    // feed trials finished in FP64 from the FP32 end point
+    sFeedRerun = 9,        // feed trials re-run exactly in FP64
+    sReviewContinued = 10,
+    sReviewRerun = 11,
+    sFbNonsmooth = 12,     // fallback: nonsmooth feed reference
+    sFbNoAttempt = 13,     // fallback: no FP32 attempt converged, some failed
+    sFbPolish = 14,        // fallback: FP64 polish did not converge
+    sFbRejected = 15,      // fallback: polished pair failed the acceptance rules
+    sFbLoad = 16,          // fallback: cell constants unrepresentable
+    sCandidates2 = 17,     // cells whose two best attempts were both polished
+    qSlots = 32
 };
 
 // Cell phases kept in Workspace::phase.
@@ -74,6 +85,8 @@ struct Workspace {
     double* cand;           // [7 * NM * ncell]: x, y, lnk, lnphi_l, lnphi_v, common, imposed
     double* cand_s;         // [8 * ncell]: beta, z_l, z_v, fug, gibbs_change, gibbs_guard, tpd_tol, spare
     int* counters_out;      // [cCount * ncell] work counters (FP32 evaluations are in row 1/0/2)
+    float* c32;             // [4 * NM * ncell] FP32 cell constants: z, ln z, a_i(T), sqrt(a_i)
+    float* ref32;           // [NM * ncell] feed-phase ln phi rounded to FP32
 };
 
 __device__ __forceinline__ int64_t idx(int k, int64_t ncell, int64_t c) { return static_cast<int64_t>(k) * ncell + c; }
@@ -92,12 +105,14 @@ __device__ bool load_cell32(const Mixture& m, const Workspace& ws, int64_t c, co
     cf.evals = 0;
     active = 0;
     for (int i = 0; i < cf.n; ++i) {
-        const double zi = ws.z[idx(i, ws.ncell, c)];
-        cf.z[i] = static_cast<float>(zi);
-        cf.lz[i] = zi > 0.0 ? static_cast<float>(log(zi)) : 0.f;
-        active += zi > 0.0;
+        cf.z[i] = ws.c32[idx(0 * NM + i, ws.ncell, c)];
+        cf.lz[i] = ws.c32[idx(1 * NM + i, ws.ncell, c)];
+        cf.a[i] = ws.c32[idx(2 * NM + i, ws.ncell, c)];
+        cf.root[i] = ws.c32[idx(3 * NM + i, ws.ncell, c)];
+        cf.b[i] = m.b32[i];
+        active += cf.z[i] > 0.f;
     }
-    return fp32::temp_setup(m, cf);
+    return cf.a[0] > 0.f;
 }
 
 template <int NM>
@@ -147,10 +162,20 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
             if (is != kOk) {
                 ph = is == kDomain ? pInvalid : pIndeterminate;
             } else {
-                for (int i = 0; i < cell.n; ++i) ws.ref_lnphi[idx(i, ws.ncell, c)] = lp[i];
+                for (int i = 0; i < cell.n; ++i) {
+                    ws.ref_lnphi[idx(i, ws.ncell, c)] = lp[i];
+                    ws.ref32[idx(i, ws.ncell, c)] = static_cast<float>(lp[i]);
+                    ws.c32[idx(0 * NM + i, ws.ncell, c)] = static_cast<float>(cell.z[i]);
+                    ws.c32[idx(1 * NM + i, ws.ncell, c)] = static_cast<float>(cell.lz[i]);
+                    ws.c32[idx(2 * NM + i, ws.ncell, c)] = static_cast<float>(cell.a[i]);
+                    ws.c32[idx(3 * NM + i, ws.ncell, c)] = static_cast<float>(cell.root[i]);
+                }
                 ws.ref_z[c] = zref;
                 // a nonsmooth feed reference makes every trial ambiguous: reference rules in FP64
-                if (!smooth) ph = pFallback;
+                if (!smooth) {
+                    ph = pFallback;
+                    atomicAdd(&ws.counters[sFbNonsmooth], 1);
+                }
             }
         }
         ws.phase[c] = ph;
@@ -214,7 +239,7 @@ __device__ void trial_begin(const Mixture& m, const Workspace& ws, const double*
     L.iter = 0;
     L.bt = 0;
     L.stage = 0;
-    L.result = fp32::tMarginal;
+    L.result = fp32::tRerun;
     L.ck_stat = L.ck_prev_stat = INFINITY;
     L.ck_iter = L.ck_prev_iter = 0;
     int active;
@@ -230,7 +255,7 @@ __device__ void trial_begin(const Mixture& m, const Workspace& ws, const double*
         return;
     }
     if (!review) {
-        for (int i = 0; i < n; ++i) L.ref[i] = static_cast<float>(ws.ref_lnphi[idx(i, ws.ncell, c)]);
+        for (int i = 0; i < n; ++i) L.ref[i] = ws.ref32[idx(i, ws.ncell, c)];
         L.nrefs = 1;
         for (int i = 0; i < n; ++i) L.lrefs[i] = L.cell.lz[i];
     } else {
@@ -346,10 +371,10 @@ __device__ int trial_classify(const TrialLane<NM>& L) {
     const int n = L.cell.n;
     const float margin = so.decide * L.point.mag;
     if (L.point.value < -margin) return fp32::tNegative;
-    if (L.point.stat > 10.f * so.stat_tol || L.iter >= 400) return fp32::tMarginal;
     // a descent that would exhaust the reference's 512-iteration budget ends
     // "iteration_limit" there: re-run it exactly in FP64
-    if (projected_fp64_iterations(L) > 320.f) return fp32::tMarginal;
+    if (L.iter >= 400 || projected_fp64_iterations(L) > 320.f) return fp32::tRerun;
+    if (L.point.stat > 10.f * so.stat_tol) return fp32::tMarginal;
     for (int r = 0; r < L.nrefs; ++r) {
         float dist = 0.f;
         for (int i = 0; i < n; ++i)
@@ -401,7 +426,7 @@ __global__ void __launch_bounds__(128) trials32_kernel(const Mixture* __restrict
                      fp32::tpd(L.cell, L.lnphi, L.ref, L.next);
         if (L.stage == 0) {
             if (!ok) {
-                L.result = fp32::tMarginal;
+                L.result = fp32::tRerun;
                 L.stage = 2;
                 for (int i = 0; i < L.cell.n; ++i) L.point.w[i] = L.next.w[i];
                 continue;
@@ -499,6 +524,25 @@ __device__ int rerun_trial64(const Mixture& m, fp64::Cell<NM>& c, int k, int act
     return fp64::run_trial(m, c, ref, o, pt, nx, dir, lp, evals);
 }
 
+// FP64 continuation of a trial from its FP32 end point (stored in ws.tw): the
+// reference descent and stopping rules (pt_stability.hpp:373-455) run on from a
+// point already inside the trial's basin, so only the FP64 tail is paid.
+template <int NM>
+__device__ int continue_trial64(const Mixture& m, fp64::Cell<NM>& c, const Workspace& ws, int64_t cell, int k,
+                                const double* ref, double tol, int row, fp64::TpdPoint<NM>& pt,
+                                fp64::TpdPoint<NM>& nx, double* dir, double* lp) {
+    const int n = c.n;
+    double sum = 0.0, cs = 0.0;
+    for (int i = 0; i < n; ++i) {
+        pt.w[i] = c.z[i] > 0.0 ? static_cast<double>(ws.tw[idx(k * NM + i, ws.ncell, cell)]) : 0.0;
+        kahan_add(pt.w[i], sum, cs);
+    }
+    for (int i = 0; i < n; ++i) pt.w[i] /= sum;
+    fp64::StabilityOptions o{tol, row};
+    int evals = 0;
+    return fp64::run_trial(m, c, ref, o, pt, nx, dir, lp, evals);
+}
+
 // ---------------------------------------------------------------------------
 // Stage 3: feed-test decision per cell and split-attempt enumeration.
 template <int NM>
@@ -533,9 +577,16 @@ __global__ void __launch_bounds__(64) decide_kernel(const Mixture* __restrict__ 
         for (int k = 0; k < n_auto; ++k) {
             int cls = ws.tclass[idx(k, ws.ncell, c)];
             bool witness = false;
-            if (cls == fp32::tMarginal) {
-                const int ts = rerun_trial64(m, cell, k, active, s.ref, 1e-10, cInitEvals, nullptr, nullptr, s.pt, s.nx,
-                                             s.dir, s.lp);
+            if (cls == fp32::tMarginal || cls == fp32::tRerun) {
+                int ts;
+                if (cls == fp32::tRerun) {
+                    atomicAdd(&ws.counters[sFeedRerun], 1);
+                    ts = rerun_trial64(m, cell, k, active, s.ref, 1e-10, cInitEvals, nullptr, nullptr, s.pt, s.nx,
+                                       s.dir, s.lp);
+                } else {
+                    atomicAdd(&ws.counters[sFeedContinued], 1);
+                    ts = continue_trial64(m, cell, ws, c, k, s.ref, 1e-10, cInitEvals, s.pt, s.nx, s.dir, s.lp);
+                }
                 if (ts < 0) {
                     all_stationary = false;
                 } else if (ts == fp64::kNegativeTpd) {
@@ -779,6 +830,7 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
         if (!load_cell64(m, ws, c, p, t, c64) || !load_cell32(m, ws, c, p, t, c32, active)) {
             ws.phase[c] = pFallback;
             atomicAdd(&ws.counters[qFallback], 1);
+            atomicAdd(&ws.counters[sFbLoad], 1);
             continue;
         }
         // rank converged attempts by FP32 Gibbs energy (ties in FP32 resolved in FP64 below)
@@ -801,6 +853,7 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
             if (any_failed) {
                 ws.phase[c] = pFallback;  // FP32 could not settle an attempt: reference rules in FP64
                 atomicAdd(&ws.counters[qFallback], 1);
+                atomicAdd(&ws.counters[sFbNoAttempt], 1);
             } else {
                 ws.phase[c] = pIndeterminate;  // every attempt collapsed to the trivial solution
                 write_status_only<NM>(out, ws, c, kIndeterminate, false);
@@ -819,15 +872,19 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
                                          ws.att_lnk[idx(second * NM + i, ws.ncell, c)]));
             if (gs - gb <= 1e-4f * (1.f + fabsf(gb)) && dist > 1e-2f) candidates[1] = second;
         }
-        bool have = false;
+        bool have = false, polish_failed = false;
         double best_g = 0.0;
+        if (candidates[1] >= 0) atomicAdd(&ws.counters[sCandidates2], 1);
         for (int k = 0; k < 2 && candidates[k] >= 0; ++k) {
             const int a = candidates[k];
             for (int i = 0; i < n; ++i) {
                 s.lk32[i] = ws.att_lnk[idx(a * NM + i, ws.ncell, c)];
                 s.lnk[i] = s.lk32[i];
             }
-            if (!polish_split(m, c64, c32, s)) continue;
+            if (!polish_split(m, c64, c32, s)) {
+                polish_failed = true;
+                continue;
+            }
             // acceptance of a fugacity-converged state, pt_split.hpp:351-362
             const fp64::SplitState<NM>& st = s.st;
             double contrast = 0.0;
@@ -858,6 +915,7 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
         if (!have) {
             ws.phase[c] = pFallback;
             atomicAdd(&ws.counters[qFallback], 1);
+            atomicAdd(&ws.counters[polish_failed ? sFbPolish : sFbRejected], 1);
             continue;
         }
         // phase-set review set-up, pt_split.hpp:490-512
@@ -938,9 +996,15 @@ __global__ void __launch_bounds__(64) finish_kernel(const Mixture* __restrict__ 
             const int cls = ws.tclass[idx(k, ws.ncell, c)];
             if (cls == fp32::tNegative) {
                 negative = true;
-            } else if (cls == fp32::tMarginal) {
-                const int ts = rerun_trial64(m, cell, k, active, s.ref, tol, cFinalEvals, ex0, ex1, s.pt, s.nx, s.dir,
-                                             s.lp);
+            } else if (cls == fp32::tMarginal || cls == fp32::tRerun) {
+                int ts;
+                if (cls == fp32::tRerun) {
+                    atomicAdd(&ws.counters[sReviewRerun], 1);
+                    ts = rerun_trial64(m, cell, k, active, s.ref, tol, cFinalEvals, ex0, ex1, s.pt, s.nx, s.dir, s.lp);
+                } else {
+                    atomicAdd(&ws.counters[sReviewContinued], 1);
+                    ts = continue_trial64(m, cell, ws, c, k, s.ref, tol, cFinalEvals, s.pt, s.nx, s.dir, s.lp);
+                }
                 if (ts == fp64::kNegativeTpd) negative = true;
                 else if (ts != fp64::kStationary) stationary = false;
             }

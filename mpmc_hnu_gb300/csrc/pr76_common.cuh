@@ -28,6 +28,8 @@ struct Mixture {
     double ac[kMaxC];      // 0.45724 (R Tc)^2 / Pc
     double b[kMaxC];       // 0.07780 R Tc / Pc
     double factor[kMaxC * kMaxC];  // 1 - kij, row-major
+    float factor32[kMaxC * kMaxC]; // the same, rounded to FP32 for the FP32 stages
+    float b32[kMaxC];
 };
 
 // Failure classes standing in for the reference's exception/issue types

@@ -43,7 +43,7 @@ __device__ bool temp_setup(const Mixture& m, Cell<NM>& c) {
         if (!isfinite(attraction) || !(attraction > 0.0)) return false;
         c.a[i] = static_cast<float>(attraction);
         c.root[i] = static_cast<float>(sqrt(attraction));
-        c.b[i] = static_cast<float>(m.b[i]);
+        c.b[i] = m.b32[i];
     }
     return true;
 }
@@ -63,7 +63,7 @@ __device__ __forceinline__ bool mix(const Mixture& m, Cell<NM>& c, const float* 
         const float x_i = x[i];
         float s_i = c.sums[i];
         for (int j = i + 1; j < n; ++j) {
-            const float f = static_cast<float>(m.factor[i * n + j]);
+            const float f = m.factor32[i * n + j];
             const float aij = (r_i * f) * c.root[j];
             attraction = fmaf(2.f * xr_i, x[j] * c.root[j] * f, attraction);
             s_i = fmaf(x[j], aij, s_i);
@@ -295,7 +295,8 @@ enum TrialClass : int {
     tNegative = 0,   // TPD clearly below zero (margin >> FP32 rounding)
     tPositive = 1,   // stationary at TPD clearly above zero
     tTangent = 2,    // stationary at one of the reference compositions (TPD = 0 there by construction)
-    tMarginal = 3,   // anything FP32 cannot decide: re-run in FP64 from the end point
+    tMarginal = 3,   // TPD sign not resolvable in FP32: continue in FP64 from the end point
+    tRerun = 4,      // descent failed or would exhaust the FP64 iteration budget: exact FP64 re-run
 };
 
 // FP32 screening tolerances.

@@ -64,7 +64,9 @@ class _Outputs(ctypes.Structure):
 
 EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu_flash_solve",
                     "mpmc_gpu_flash_solve_device", "mpmc_gpu_flash_components", "mpmc_gpu_flash_last_error",
-                    "mpmc_gpu_flash_abi_version", "mpmc_gpu_flash_stage_timings"]
+                    "mpmc_gpu_flash_abi_version", "mpmc_gpu_flash_stage_timings", "mpmc_gpu_flash_batch_stats"]
+BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun", "fallback_nonsmooth",
+               "fallback_no_attempt", "fallback_polish", "fallback_rejected", "fallback_load", "two_candidates"]
 FLAG_STAGE_TIMING = 1
 STAGES = {FORM_PLAIN_FP64: ["flash", "sensitivity"],
           FORM_MIXED: ["setup", "feed_trials", "decide", "split", "polish", "relist", "review_trials", "finish",
@@ -89,6 +91,7 @@ def library() -> ctypes.CDLL:
             [ctypes.POINTER(_Outputs), ctypes.c_void_p]
         lib.mpmc_gpu_flash_components.argtypes = [ctypes.c_void_p]
         lib.mpmc_gpu_flash_stage_timings.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        lib.mpmc_gpu_flash_batch_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         for name in EXPORTED_SYMBOLS:
             getattr(lib, name).restype = ctypes.c_int
         lib.mpmc_gpu_flash_last_error.restype = ctypes.c_char_p
@@ -164,6 +167,12 @@ class GpuFlash:
         """Host-buffer entry with caller-owned (e.g. pinned) host pointers."""
         s = _Outputs(**out_ptrs)
         _check(library().mpmc_gpu_flash_solve(self._h, ncell, p_ptr, t_ptr, z_ptr, ctypes.byref(s)))
+
+    def batch_stats(self) -> dict[str, int]:
+        """Work statistics of the last mixed-form solve."""
+        out = np.zeros(16, np.int64)
+        k = library().mpmc_gpu_flash_batch_stats(self._h, out.ctypes.data, 16)
+        return {BATCH_STATS[i]: int(out[i]) for i in range(min(k, len(BATCH_STATS)))}
 
     def stage_timings(self) -> dict[str, float]:
         """Per-stage device milliseconds of the last solve (stage_timing=True)."""
