@@ -225,7 +225,7 @@ struct TrialLane {
     float alpha, slope, scale;
     int result;
     // convergence-rate checkpoints: stationarity at the last two multiples of 8 iterations
-    float ck_stat, ck_prev_stat;
+    float ck_stat, ck_prev_stat, stat0;
     int ck_iter, ck_prev_iter;
 };
 
@@ -359,9 +359,17 @@ __device__ void trial_step_or_finish(TrialLane<NM>& L) {
 template <int NM>
 __device__ float projected_fp64_iterations(const TrialLane<NM>& L) {
     if (!(L.point.stat > 1e-8f)) return static_cast<float>(L.iter);
-    const int span = L.iter - L.ck_prev_iter;
-    if (span < 4 || !(L.ck_prev_stat < INFINITY) || !(L.ck_prev_stat > L.point.stat)) return 1e9f;
-    const float rate = logf(L.ck_prev_stat / L.point.stat) / static_cast<float>(span);  // per iteration
+    // contraction per iteration over the last checkpoint window, or over the
+    // whole descent when it was shorter than a window
+    float from = L.ck_prev_stat;
+    int span = L.iter - L.ck_prev_iter;
+    if (span < 4 || !(from < INFINITY)) {
+        from = L.stat0;
+        span = L.iter;
+    }
+    if (span < 1) return static_cast<float>(L.iter);
+    if (!(from > L.point.stat)) return 1e9f;  // no progress at all: let FP64 decide from the start
+    const float rate = logf(from / L.point.stat) / static_cast<float>(span);
     return static_cast<float>(L.iter) + logf(L.point.stat / 1e-8f) / rate;
 }
 
@@ -432,6 +440,7 @@ __global__ void __launch_bounds__(128) trials32_kernel(const Mixture* __restrict
                 continue;
             }
             L.point = L.next;
+            L.stat0 = L.point.stat;
             trial_step_or_finish(L);
             continue;
         }
@@ -764,52 +773,109 @@ __global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict_
 // Stage 5: FP64 polish of the minimum-Gibbs attempt and the acceptance rules.
 template <int NM>
 struct PolishScratch {
-    fp64::SplitState<NM> st;
-    fp32::SplitState<NM> f32;
-    double lnk[NM], e[NM], num[NM], J[NM * NM], d[NM];
-    float lk32[NM], fp[NM], fm[NM];
+    fp64::SplitState<NM> st, nx;
+    double lnk[NM], e[NM], num[NM], J[NM * NM], d[NM], other[NM];
+    double jl[(NM + 1) * (NM + 2)], jv[(NM + 1) * (NM + 2)];
     int piv[NM];
 };
 
-// Newton refinement of ln K: FP64 residual F(ln K) (RR + role phases,
-// pt_split.hpp:300-341), FP32 central-difference Jacobian dF/dln K taken once
-// at the FP32 solution.  Returns true with `s.st` the FP64 state at the
-// refined ln K (|F| <= 1e-13 or no further decrease).
+// dF/dln K of F = ln x - ln y + ln phi_L(x) - ln phi_V(y) at a Rachford-Rice
+// state: the RR linearisation of detail/pt_sensitivity_detail.hpp:291-345 (no
+// feed variation) composed with the forward-AD full-chart ln phi Jacobians.
 template <int NM>
-__device__ bool polish_split(const Mixture& m, fp64::Cell<NM>& c64, fp32::Cell<NM>& c32, PolishScratch<NM>& s) {
-    const int n = c64.n;
-    // Jacobian in FP32 by central differences on the FP32 residual map
-    const float h = 2e-3f;
+__device__ bool equilibrium_jacobian(const Mixture& m, const fp64::Cell<NM>& c, PolishScratch<NM>& s) {
+    const int n = c.n;
+    const fp64::SplitState<NM>& st = s.st;
+    if (!ad::phase_jacobian<NM>(m, n, c.p, c.t, st.x, st.branch_l, s.jl) ||
+        !ad::phase_jacobian<NM>(m, n, c.p, c.t, st.y, st.branch_v, s.jv))
+        return false;
+    double h = 0.0;
+    for (int i = 0; i < n; ++i)
+        if (c.z[i] > 0.0) h += (st.y[i] - st.x[i]) * (st.y[i] - st.x[i]) / c.z[i];
+    if (!(h > 0.0) || !isfinite(h)) return false;
+    const int cols = n + 2;
     for (int j = 0; j < n; ++j) {
-        if (c32.z[j] == 0.f) {
+        if (c.z[j] == 0.0) {
             for (int i = 0; i < n; ++i) s.J[i * n + j] = i == j ? 1.0 : 0.0;
             continue;
         }
-        float save = s.lk32[j];
-        s.lk32[j] = save + h;
-        if (!fp32::split_evaluate(m, c32, s.lk32, s.f32)) return false;
-        for (int i = 0; i < n; ++i) s.fp[i] = s.f32.res[i];
-        s.lk32[j] = save - h;
-        if (!fp32::split_evaluate(m, c32, s.lk32, s.f32)) return false;
-        for (int i = 0; i < n; ++i) s.fm[i] = s.f32.res[i];
-        s.lk32[j] = save;
-        for (int i = 0; i < n; ++i)
-            s.J[i * n + j] = c32.z[i] == 0.f ? (i == j ? 1.0 : 0.0) : static_cast<double>((s.fp[i] - s.fm[i]) / (2.f * h));
+        const double db = (st.x[j] * st.y[j] / c.z[j]) / h;
+        double dx[NM], dy[NM];
+        for (int i = 0; i < n; ++i) {
+            if (c.z[i] == 0.0) {
+                dx[i] = dy[i] = 0.0;
+                continue;
+            }
+            const double dlk = i == j ? 1.0 : 0.0;
+            const double dlx = -((st.y[i] - st.x[i]) / c.z[i]) * db - st.beta * (st.y[i] / c.z[i]) * dlk;
+            dx[i] = st.x[i] * dlx;
+            dy[i] = st.y[i] * (dlx + dlk);
+        }
+        for (int i = 0; i < n; ++i) {
+            if (c.z[i] == 0.0) {
+                s.J[i * n + j] = i == j ? 1.0 : 0.0;
+                continue;
+            }
+            double v = dx[i] / st.x[i] - dy[i] / st.y[i];
+            for (int k = 0; k < n; ++k) v += s.jl[(1 + i) * cols + 2 + k] * dx[k] - s.jv[(1 + i) * cols + 2 + k] * dy[k];
+            s.J[i * n + j] = v;
+        }
     }
+    return true;
+}
+
+// Newton polish of ln K from the FP32 solution: FP64 residual F(ln K) (RR +
+// role phases, pt_split.hpp:300-341) and the exact FP64 Jacobian taken at the
+// first FP64 state (chord iterations).  On success `s.st` holds the FP64 state
+// at |F| <= 1e-13, or at the point where F stopped decreasing below 1e-11.
+template <int NM>
+__device__ bool polish_split(const Mixture& m, fp64::Cell<NM>& c64, PolishScratch<NM>& s) {
+    const int n = c64.n;
+    int evals = 0;
+    if (fp64::split_evaluate(m, c64, s.lnk, s.st, evals, 1 << 30, s.e, s.num, true) != fp64::kConverged) return false;
+    if (s.st.fug <= 1e-13) return true;
+    if (!equilibrium_jacobian(m, c64, s)) return false;
     double norm;
     if (!ad::lu_factor(s.J, s.piv, n, norm)) return false;
-    int evals = 0;
-    double prev = INFINITY;
+    double prev = s.st.fug;
     for (int it = 0; it < 8; ++it) {
-        const int st = fp64::split_evaluate(m, c64, s.lnk, s.st, evals, 1 << 30, s.e, s.num, true);
-        if (st != fp64::kConverged) return false;
-        if (s.st.fug <= 1e-13 || !(s.st.fug < 0.5 * prev)) return s.st.fug <= 1e-11;
-        prev = s.st.fug;
         for (int i = 0; i < n; ++i) s.d[i] = -s.st.res[i];
         if (!ad::lu_solve(s.J, s.piv, n, s.d)) return false;
         for (int i = 0; i < n; ++i) s.lnk[i] = s.st.lnk[i] + s.d[i];
+        if (fp64::split_evaluate(m, c64, s.lnk, s.nx, evals, 1 << 30, s.e, s.num, true) != fp64::kConverged)
+            return prev <= 1e-11;
+        if (!(s.nx.fug < prev)) return prev <= 1e-11;
+        fp64::copy_state(s.st, s.nx, n);
+        prev = s.st.fug;
+        if (prev <= 1e-13) return true;
     }
-    return s.st.fug <= 1e-11;
+    return prev <= 1e-11;
+}
+
+// Acceptance of a fugacity-converged state, pt_split.hpp:351-362.
+template <int NM>
+__device__ bool split_accepted(const fp64::SplitState<NM>& st, int n) {
+    double contrast = 0.0;
+    for (int i = 0; i < n; ++i) contrast = fmax(contrast, fabs(st.lnk[i]));
+    return st.fug <= 1e-11 && st.mass_abs <= 1e-12 && st.mass_rel <= 1e-10 && st.beta > 1e-10 &&
+           1.0 - st.beta > 1e-10 && contrast > 1e-7 && st.z_v - st.z_l > 1e-8 * fmax(st.z_v, st.z_l);
+}
+
+template <int NM>
+__device__ void store_candidate(const Workspace& ws, int64_t c, const fp64::SplitState<NM>& st, int n) {
+    for (int i = 0; i < n; ++i) {
+        ws.cand[idx(0 * NM + i, ws.ncell, c)] = st.x[i];
+        ws.cand[idx(1 * NM + i, ws.ncell, c)] = st.y[i];
+        ws.cand[idx(2 * NM + i, ws.ncell, c)] = st.lnk[i];
+        ws.cand[idx(3 * NM + i, ws.ncell, c)] = st.lnphi_l[i];
+        ws.cand[idx(4 * NM + i, ws.ncell, c)] = st.lnphi_v[i];
+        ws.cand[idx(5 * NM + i, ws.ncell, c)] = st.common[i];
+    }
+    ws.cand_s[idx(0, ws.ncell, c)] = st.beta;
+    ws.cand_s[idx(1, ws.ncell, c)] = st.z_l;
+    ws.cand_s[idx(2, ws.ncell, c)] = st.z_v;
+    ws.cand_s[idx(3, ws.ncell, c)] = st.fug;
+    ws.cand_s[idx(7, ws.ncell, c)] = st.guard;
 }
 
 template <int NM>
@@ -824,10 +890,8 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
         const int64_t c = ws.trial_cells[slot];
         if (ws.phase[c] != pSplit) continue;
         fp64::Cell<NM> c64;
-        fp32::Cell<NM> c32;
         PolishScratch<NM> s;
-        int active;
-        if (!load_cell64(m, ws, c, p, t, c64) || !load_cell32(m, ws, c, p, t, c32, active)) {
+        if (!load_cell64(m, ws, c, p, t, c64)) {
             ws.phase[c] = pFallback;
             atomicAdd(&ws.counters[qFallback], 1);
             atomicAdd(&ws.counters[sFbLoad], 1);
@@ -836,11 +900,8 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
         // rank converged attempts by FP32 Gibbs energy (ties in FP32 resolved in FP64 below)
         const int na = ws.att_count[c];
         int best = -1, second = -1;
-        bool any_failed = false;
         for (int a = 0; a < na; ++a) {
-            const int cls = ws.att_class[idx(a, ws.ncell, c)];
-            if (cls == fp32::aFailed) any_failed = true;
-            if (cls != fp32::aConverged) continue;
+            if (ws.att_class[idx(a, ws.ncell, c)] != fp32::aConverged) continue;
             const float g = ws.att_gibbs[idx(a, ws.ncell, c)];
             if (best < 0 || g < ws.att_gibbs[idx(best, ws.ncell, c)]) {
                 second = best;
@@ -849,73 +910,65 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
                 second = a;
             }
         }
-        if (best < 0) {
-            if (any_failed) {
-                ws.phase[c] = pFallback;  // FP32 could not settle an attempt: reference rules in FP64
-                atomicAdd(&ws.counters[qFallback], 1);
-                atomicAdd(&ws.counters[sFbNoAttempt], 1);
-            } else {
-                ws.phase[c] = pIndeterminate;  // every attempt collapsed to the trivial solution
-                write_status_only<NM>(out, ws, c, kIndeterminate, false);
-                write_counters<NM>(out, ws, c);
-            }
-            continue;
-        }
         // a second converged attempt at a different composition with a Gibbs
         // energy FP32 cannot separate from the best: let FP64 arbitrate
         int candidates[2] = {best, -1};
-        if (second >= 0) {
+        if (best >= 0 && second >= 0) {
             const float gb = ws.att_gibbs[idx(best, ws.ncell, c)], gs = ws.att_gibbs[idx(second, ws.ncell, c)];
             float dist = 0.f;
             for (int i = 0; i < n; ++i)
                 dist = fmaxf(dist, fabsf(ws.att_lnk[idx(best * NM + i, ws.ncell, c)] -
                                          ws.att_lnk[idx(second * NM + i, ws.ncell, c)]));
-            if (gs - gb <= 1e-4f * (1.f + fabsf(gb)) && dist > 1e-2f) candidates[1] = second;
+            if (gs - gb <= 1e-4f * (1.f + fabsf(gb)) && dist > 1e-2f) {
+                candidates[1] = second;
+                atomicAdd(&ws.counters[sCandidates2], 1);
+            }
         }
         bool have = false, polish_failed = false;
         double best_g = 0.0;
-        if (candidates[1] >= 0) atomicAdd(&ws.counters[sCandidates2], 1);
         for (int k = 0; k < 2 && candidates[k] >= 0; ++k) {
             const int a = candidates[k];
-            for (int i = 0; i < n; ++i) {
-                s.lk32[i] = ws.att_lnk[idx(a * NM + i, ws.ncell, c)];
-                s.lnk[i] = s.lk32[i];
-            }
-            if (!polish_split(m, c64, c32, s)) {
+            for (int i = 0; i < n; ++i) s.lnk[i] = ws.att_lnk[idx(a * NM + i, ws.ncell, c)];
+            if (!polish_split(m, c64, s)) {
                 polish_failed = true;
                 continue;
             }
-            // acceptance of a fugacity-converged state, pt_split.hpp:351-362
-            const fp64::SplitState<NM>& st = s.st;
-            double contrast = 0.0;
-            for (int i = 0; i < n; ++i) contrast = fmax(contrast, fabs(st.lnk[i]));
-            const bool converged = st.mass_abs <= 1e-12 && st.mass_rel <= 1e-10 && st.beta > 1e-10 &&
-                                   1.0 - st.beta > 1e-10 && contrast > 1e-7 &&
-                                   st.z_v - st.z_l > 1e-8 * fmax(st.z_v, st.z_l);
-            if (!converged) continue;
-            if (have && !(st.gibbs < best_g)) continue;
+            if (!split_accepted(s.st, n)) continue;
+            if (have && !(s.st.gibbs < best_g)) continue;
             have = true;
-            best_g = st.gibbs;
-            for (int i = 0; i < n; ++i) {
-                ws.cand[idx(0 * NM + i, ws.ncell, c)] = st.x[i];
-                ws.cand[idx(1 * NM + i, ws.ncell, c)] = st.y[i];
-                ws.cand[idx(2 * NM + i, ws.ncell, c)] = st.lnk[i];
-                ws.cand[idx(3 * NM + i, ws.ncell, c)] = st.lnphi_l[i];
-                ws.cand[idx(4 * NM + i, ws.ncell, c)] = st.lnphi_v[i];
-                ws.cand[idx(5 * NM + i, ws.ncell, c)] = st.common[i];
+            best_g = s.st.gibbs;
+            store_candidate(ws, c, s.st, n);
+        }
+        if (!have) {
+            // FP64 continuation (reference ln K iteration, pt_split.hpp:275-408) of
+            // every attempt FP32 left unsettled, from its FP32 end point
+            for (int a = 0; a < na; ++a) {
+                const int cls = ws.att_class[idx(a, ws.ncell, c)];
+                if (cls == fp32::aTrivial) continue;
+                for (int i = 0; i < n; ++i) s.lnk[i] = ws.att_lnk[idx(a * NM + i, ws.ncell, c)];
+                int evals = 0;
+                const int st = fp64::iterate_split(m, c64, s.lnk, s.st, s.nx, s.other, evals, 20000, s.e, s.num);
+                if (st != fp64::kConverged) continue;
+                if (have && !(s.st.gibbs < best_g)) continue;
+                have = true;
+                best_g = s.st.gibbs;
+                store_candidate(ws, c, s.st, n);
             }
-            ws.cand_s[idx(0, ws.ncell, c)] = st.beta;
-            ws.cand_s[idx(1, ws.ncell, c)] = st.z_l;
-            ws.cand_s[idx(2, ws.ncell, c)] = st.z_v;
-            ws.cand_s[idx(3, ws.ncell, c)] = st.fug;
-            ws.cand_s[idx(7, ws.ncell, c)] = st.guard;
         }
         atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], c64.counters[cSplitEvals]);
         atomicAdd(&ws.counters_out[idx(cRrIters, ws.ncell, c)], c64.counters[cRrIters]);
         if (!have) {
+            bool any_failed = false;
+            for (int a = 0; a < na; ++a) any_failed = any_failed || ws.att_class[idx(a, ws.ncell, c)] != fp32::aTrivial;
+            if (!any_failed) {
+                ws.phase[c] = pIndeterminate;  // every attempt collapsed to the trivial solution
+                write_status_only<NM>(out, ws, c, kIndeterminate, false);
+                write_counters<NM>(out, ws, c);
+                continue;
+            }
             ws.phase[c] = pFallback;
             atomicAdd(&ws.counters[qFallback], 1);
-            atomicAdd(&ws.counters[polish_failed ? sFbPolish : sFbRejected], 1);
+            atomicAdd(&ws.counters[best < 0 ? sFbNoAttempt : (polish_failed ? sFbPolish : sFbRejected)], 1);
             continue;
         }
         // phase-set review set-up, pt_split.hpp:490-512
