@@ -32,6 +32,7 @@ __device__ void plain_cell(const Mixture& m, int64_t ncell, int64_t cell, const 
     using namespace fp64;
     Cell<NM> c;
     c.n = m.n;
+    c.newton = false;
     c.p = p[cell];
     c.t = t[cell];
     for (int k = 0; k < cCount; ++k) c.counters[k] = 0;

@@ -119,6 +119,7 @@ template <int NM>
 __device__ bool load_cell64(const Mixture& m, const Workspace& ws, int64_t c, const double* p, const double* t,
                             fp64::Cell<NM>& c64) {
     c64.n = m.n;
+    c64.newton = true;
     c64.p = p[c];
     c64.t = t[c];
     for (int k = 0; k < cCount; ++k) c64.counters[k] = 0;
@@ -141,6 +142,7 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
     for (int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; c < ws.ncell; c += stride) {
         fp64::Cell<NM> cell;
         cell.n = m.n;
+        cell.newton = true;
         cell.p = p[c];
         cell.t = t[c];
         for (int k = 0; k < cCount; ++k) cell.counters[k] = 0;
@@ -1088,6 +1090,7 @@ __global__ void __launch_bounds__(64) fallback_kernel(const Mixture* __restrict_
         using namespace fp64;
         Cell<NM> cell;
         cell.n = m.n;
+        cell.newton = true;
         cell.p = p[c];
         cell.t = t[c];
         for (int k = 0; k < cCount; ++k) cell.counters[k] = 0;

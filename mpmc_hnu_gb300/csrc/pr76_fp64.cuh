@@ -35,6 +35,7 @@ namespace fp64 {
 template <int NM>
 struct Cell {
     int n;
+    bool newton;              // bracketed Newton for the cubic and RR (mixed form's FP64 stages)
     double p, t;
     double a[NM], root[NM];   // a_i(T), sqrt(a_i(T))
     double z[NM], lz[NM];     // normalised feed and its log (0 where z_i = 0)
@@ -128,7 +129,7 @@ __device__ __forceinline__ double poly_scale(double y, const Cubic& c) {
     return ((fabs(y) + fabs(c.c2)) * fabs(y) + fabs(c.c1)) * fabs(y) + fabs(c.c0);
 }
 
-__device__ inline void solve_roots(double a, double b, RootSet& rs, int& iterations) {
+__device__ inline void solve_roots(double a, double b, RootSet& rs, int& iterations, bool newton = false) {
     rs.count = 0;
     rs.status = kRootUnrepresentable;
     rs.scale = 1.0;
@@ -178,7 +179,32 @@ __device__ inline void solve_roots(double a, double b, RootSet& rs, int& iterati
         double y = 0.0;
         bool converged = false;
         int it = 0;
-        for (; it < 2048; ++it) {
+        if (newton) {
+            // bracketed Newton on the same monotone interval: the iterate stays
+            // inside [left, right], a step leaving it is replaced by bisection,
+            // and the stopping test is the reference's 4 eps relative width
+            const bool increasing = signbit(fl);  // H(left) < 0 <=> increasing on this interval
+            y = (left + right) * 0.5;
+            for (; it < 100; ++it) {
+                const double fy = poly(y, c);
+                if (fy == 0.0) {
+                    converged = true;
+                    break;
+                }
+                if ((fy > 0.0) == increasing) right = y; else left = y;
+                const double dh = fma(3.0 * y + 2.0 * c.c2, y, c.c1);
+                double yn = y - fy / dh;
+                if (!(yn > left && yn < right)) yn = (left + right) * 0.5;
+                const bool done = fabs(yn - y) <= 2.0 * kEps * fmax(yn, kDblMin) ||
+                                  right - left <= 4.0 * kEps * fmax(y, kDblMin);
+                y = yn;
+                if (done) {
+                    converged = true;
+                    break;
+                }
+            }
+        }
+        for (; it < 2048 && !converged; ++it) {
             y = (left + right) * 0.5;
             const double fy = poly(y, c);
             if (fy == 0.0 || y == left || y == right || right - left <= 4.0 * kEps * fmax(y, kDblMin)) {
@@ -283,7 +309,7 @@ __device__ int stability_provider(const Mixture& m, Cell<NM>& c, const double* x
     if (!mix(m, c, x, amix, bmix)) return kRootRange;
     if (!coefficients(c.p, c.t, amix, bmix, A, B)) return kRootRange;
     RootSet rs;
-    solve_roots(A, B, rs, c.counters[cRootIters]);
+    solve_roots(A, B, rs, c.counters[cRootIters], c.newton);
     if (rs.status != kRootSuccess) return root_issue(rs.status);
     int cand[3];
     int ncand = 0;
@@ -327,7 +353,7 @@ __device__ int role_provider(const Mixture& m, Cell<NM>& c, const double* x, boo
     if (!mix(m, c, x, amix, bmix)) return kRootRange;
     if (!coefficients(c.p, c.t, amix, bmix, A, B)) return kRootRange;
     RootSet rs;
-    solve_roots(A, B, rs, c.counters[cRootIters]);
+    solve_roots(A, B, rs, c.counters[cRootIters], c.newton);
     if (rs.status != kRootSuccess) return root_issue(rs.status);
     int selected = -1;
     for (int k = 0; k < rs.count; ++k) {
@@ -661,7 +687,7 @@ template <int NM>
 __device__ int split_evaluate(const Mixture& m, Cell<NM>& c, const double* lk, SplitState<NM>& s, int& evals,
                               int budget, double* e, double* num, bool newton_rr = false) {
     const int n = c.n;
-    const int rr = solve_rr(c, lk, s, e, num, newton_rr);
+    const int rr = solve_rr(c, lk, s, e, num, newton_rr || c.newton);
     if (rr != kRrInterior)
         return rr == kRrDegenerate ? kIndistinguishable : (rr == kRrNoInterior ? kNoInteriorRr : kRrFailure);
     if (evals >= budget) return kAttemptEvaluationLimit;

@@ -46,6 +46,7 @@ __global__ void __launch_bounds__(64) sensitivity_kernel(const Mixture* __restri
         if (out.status[cell] == kTwoPhase) {
             fp64::Cell<NM> c;
             c.n = n;
+            c.newton = false;
             c.p = p[cell];
             c.t = t[cell];
             double feed[NM], x[NM], y[NM], lnk[NM];

@@ -125,4 +125,7 @@ def sensitivity_report(gpu: dict, ref: dict):
         scale = np.abs(b).max(axis=0, keepdims=True)
         err = np.abs(a - b) / np.maximum(np.abs(b), 1e-8 * scale + 1e-300)
         out["max"][g] = float(err.max())
+        w = np.unravel_index(int(np.argmax(err)), err.shape)
+        out.setdefault("worst", {})[g] = {"row": int(w[0]), "col": int(w[1]), "got": float(a[w]),
+                                          "ref": float(b[w]), "col_scale": float(scale[(0, w[1], w[2])])}
     return out
