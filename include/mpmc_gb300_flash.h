@@ -168,7 +168,8 @@ int mpmc_gpu_flash_solve_device(mpmc_gpu_flash* handle, int64_t n_cells, const d
 /* Device time in milliseconds of every stage of the last solve on a handle
  * created with MPMC_FLAG_STAGE_TIMING (waits for that solve to finish).
  * Stages, in order -- plain form: flash, sensitivity; mixed form: setup,
- * feed_trials, decide, split, polish, relist, review_trials, finish,
+ * feed_trials, feed_classify, feed_trials64, decide, split, polish, split64,
+ * select64, relist, review_trials, review_classify, review_trials64, finish,
  * fallback, sensitivity.  Writes up to `capacity` values and returns the
  * number of stages (0 if timing is off or nothing ran).  Diagnostic entry
  * point with no counterpart in the reference (whose solver results carry
@@ -178,10 +179,11 @@ int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* handle, float* ms, int capacity
 /* Work statistics of the last mixed-form solve on a handle (waits for the
  * device): [0] feed trials continued in FP64 from their FP32 end point,
  * [1] feed trials re-run exactly in FP64, [2] review trials continued,
- * [3] review trials re-run, [4..8] cells sent to the FP64 fallback because
- * of a nonsmooth feed phase / no settled FP32 attempt / a polish that did not
- * converge / a polished pair rejected by the acceptance rules / unusable
- * cell constants, [9] cells whose two best attempts were both polished.
+ * [3] review trials re-run, [4] cells sent to the plain FP64 fallback
+ * (nonsmooth feed phase), [5..7] cells whose split attempts were continued in
+ * FP64 because no FP32 attempt settled / the polish did not converge / the
+ * polished pair failed the acceptance rules, [8] cells with unusable
+ * constants, [9] cells whose two best attempts were both polished.
  * Writes up to `capacity` values; returns the number available (0 for the
  * plain form).  Diagnostic entry point with no counterpart in the reference. */
 int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* handle, int64_t* out, int capacity);

@@ -65,7 +65,7 @@ struct mpmc_gpu_flash {
     DevBuf sens_inputs[7];
     DevBuf workspace;  // batched-form stage buffers and work queues
     bool stage_timing = false;
-    cudaEvent_t events[16] = {};
+    cudaEvent_t events[24] = {};
     int n_events = 0;   // events recorded by the last solve (stages + 1)
 };
 
@@ -191,7 +191,7 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
     }
     int next_event = 0;
     auto record = [&]() {
-        if (h->stage_timing && next_event < 16) cudaEventRecord(h->events[next_event++], stream);
+        if (h->stage_timing && next_event < 24) cudaEventRecord(h->events[next_event++], stream);
     };
     switch (h->form) {
     case MPMC_FORM_PLAIN_FP64:
@@ -200,6 +200,8 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
         record();
         break;
     case MPMC_FORM_MIXED: {
+        if (ncell >= (int64_t{1} << 24))
+            return fail(MPMC_ERR_INVALID_ARGUMENT, "mixed form: at most 16,777,215 cells per call");
         const size_t need = pr76::batched_workspace_bytes(h->n, ncell);
         if ((e = h->workspace.ensure(need)) != cudaSuccess) return cuda_fail(e, "batched workspace allocation");
         pr76::BatchedShape shape{0, 0, h->stage_timing ? h->events : nullptr};

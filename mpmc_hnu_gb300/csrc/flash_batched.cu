@@ -4,7 +4,7 @@
 // counters, so the sequence needs no host synchronisation and can be
 // captured into a CUDA graph by the caller.
 #include "launch.h"
-#include "pr76_batched.cuh"
+#include "pr76_batched64.cuh"
 
 #ifndef MPMC_NM
 #error "compile with -DMPMC_NM=<capacity>"
@@ -49,6 +49,16 @@ size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell) {
     ws.counters_out = reinterpret_cast<int*>(take(sizeof(int) * cCount * nc));
     ws.c32 = reinterpret_cast<float*>(take(sizeof(float) * 4 * NM * nc));
     ws.ref32 = reinterpret_cast<float*>(take(sizeof(float) * NM * nc));
+    ws.t64_items = reinterpret_cast<int*>(take(sizeof(int) * (NM + 4) * nc));
+    ws.t64_status = reinterpret_cast<signed char*>(take((NM + 4) * nc));
+    ws.tw64 = reinterpret_cast<double*>(take(sizeof(double) * (NM + 4) * NM * nc));
+    ws.s64_capacity = static_cast<int>(nc < 4096 ? 4 * 4096 : nc);
+    const size_t cap = static_cast<size_t>(ws.s64_capacity);
+    ws.s64_items = reinterpret_cast<int*>(take(sizeof(int) * cap));
+    ws.s64_status = reinterpret_cast<signed char*>(take(cap));
+    ws.s64_state = reinterpret_cast<double*>(take(sizeof(double) * batched::S64Stride<NM>() * cap));
+    ws.s64_base = reinterpret_cast<int*>(take(sizeof(int) * nc));
+    ws.s64_count = reinterpret_cast<int*>(take(sizeof(int) * nc));
     return off;
 }
 
@@ -73,6 +83,7 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
                                                    cudaStream_t stream) {
     using namespace batched;
     if (ncell <= 0) return cudaSuccess;
+    if (ncell >= (int64_t{1} << 24)) return cudaErrorInvalidValue;  // work-item encodings hold 24-bit cells
     Workspace ws;
     if (carve(ws, nullptr, n, ncell) > scratch_bytes || scratch == nullptr) return cudaErrorInvalidValue;
     carve(ws, static_cast<char*>(scratch), n, ncell);
@@ -80,6 +91,8 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     cudaError_t e = cudaMemsetAsync(ws.counters, 0, sizeof(int) * qSlots, stream);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(ws.s64_items, 0xff, sizeof(int) * static_cast<size_t>(ws.s64_capacity), stream);
     if (e != cudaSuccess) return e;
     const int cell_block = 64;
     const int64_t cell_grid_max = static_cast<int64_t>(sms) * 8;
@@ -92,6 +105,8 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
                                                         : resident_blocks(trials32_kernel<NM>, qblock);
     const int split_res = shape.split_blocks_per_sm > 0 ? shape.split_blocks_per_sm
                                                         : resident_blocks(split32_kernel<NM>, qblock);
+    const int t64_res = resident_blocks(trials64_kernel<NM>, 64);
+    const int s64_res = resident_blocks(split64_kernel<NM>, 64);
     int stage = 0;
     auto mark = [&]() {
         if (shape.events) cudaEventRecord(shape.events[stage], stream);
@@ -102,15 +117,28 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     mark();
     trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 0);
     mark();
+    classify_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, 0);
+    mark();
+    trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+    mark();
     decide_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
     mark();
     split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t);
     mark();
     polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
     mark();
+    split64_kernel<NM><<<sms * s64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+    mark();
+    select64_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+    mark();
     relist_kernel<NM><<<1, 1024, 0, stream>>>(ws);
+    cudaMemsetAsync(ws.counters + qT64Items, 0, 2 * sizeof(int), stream);
     mark();
     trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 1);
+    mark();
+    classify_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, 1);
+    mark();
+    trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
     mark();
     finish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
     mark();

@@ -50,7 +50,7 @@ struct BatchedShape {
     int split_blocks_per_sm;
     cudaEvent_t* events;  // optional: kBatchedStages + 1 events recorded around the stages
 };
-constexpr int kBatchedStages = 9;
+constexpr int kBatchedStages = 15;
 
 // Batched mixed-precision flash (flash_batched.cu): scratch bytes needed for
 // ncell cells, and the launch sequence using that scratch.

@@ -56,13 +56,22 @@ enum Slot : int {
     sFbRejected = 15,      // fallback: polished pair failed the acceptance rules
     sFbLoad = 16,          // fallback: cell constants unrepresentable
     sCandidates2 = 17,     // cells whose two best attempts were both polished
+    qT64Items = 18,        // FP64 trial items listed
+    qT64Cursor = 19,
+    qS64Items = 20,        // FP64 attempt items listed
+    qS64Cursor = 21,
     qSlots = 32
 };
+
+// Doubles per FP64 attempt result: gibbs, guard, fug, beta, z_l, z_v, 2 spare,
+// then x, y, ln K, ln phi_L, ln phi_V, common log activity.
+template <int NM>
+__host__ __device__ constexpr int S64Stride() { return 8 + 6 * NM; }
 
 // Cell phases kept in Workspace::phase.
 enum Phase : int {
     pInvalid = -1, pSingle = 0, pTwo = 1, pUnstable = 2, pIndeterminate = 3,
-    pPending = 10, pSplit = 11, pReview = 12, pFallback = 13
+    pPending = 10, pSplit = 11, pReview = 12, pFallback = 13, pSplit64 = 14
 };
 
 // Device workspace for one batch (all arrays entry-major, cell fastest).
@@ -87,6 +96,15 @@ struct Workspace {
     int* counters_out;      // [cCount * ncell] work counters (FP32 evaluations are in row 1/0/2)
     float* c32;             // [4 * NM * ncell] FP32 cell constants: z, ln z, a_i(T), sqrt(a_i)
     float* ref32;           // [NM * ncell] feed-phase ln phi rounded to FP32
+    int* t64_items;         // [(NM+4) * ncell] FP64 trial items (cell << 7 | k << 2 | mode)
+    signed char* t64_status;// [(NM+4) * ncell] FP64 trial statuses (fp64::TrialStatus)
+    double* tw64;           // [(NM+4) * NM * ncell] FP64 witnesses of negative feed trials
+    int* s64_items;         // [s64_capacity] FP64 attempt items (cell << 5 | order)
+    signed char* s64_status;// [s64_capacity]
+    double* s64_state;      // [s64_capacity * S64Stride] converged attempt states
+    int* s64_base;          // [ncell] first FP64 attempt item of the cell
+    int* s64_count;         // [ncell]
+    int s64_capacity;
 };
 
 __device__ __forceinline__ int64_t idx(int k, int64_t ncell, int64_t c) { return static_cast<int64_t>(k) * ncell + c; }
@@ -522,38 +540,6 @@ __device__ void write_counters(const DeviceOutputs& out, const Workspace& ws, in
     for (int k = 0; k < cCount; ++k) out.counters[idx(k, ws.ncell, c)] = ws.counters_out[idx(k, ws.ncell, c)];
 }
 
-// Exact FP64 re-run of trial k of a stability test (the plain algorithm from
-// the trial's original start), pt_stability.hpp:343-457.
-template <int NM>
-__device__ int rerun_trial64(const Mixture& m, fp64::Cell<NM>& c, int k, int active, const double* ref,
-                             double tol, int row, const double* ex0, const double* ex1, fp64::TpdPoint<NM>& pt,
-                             fp64::TpdPoint<NM>& nx, double* dir, double* lp) {
-    const int n_auto = auto_starts(active);
-    fp64::make_start(c, k, active, ex0, ex1, n_auto, pt.w);
-    fp64::StabilityOptions o{tol, row};
-    int evals = 0;
-    return fp64::run_trial(m, c, ref, o, pt, nx, dir, lp, evals);
-}
-
-// FP64 continuation of a trial from its FP32 end point (stored in ws.tw): the
-// reference descent and stopping rules (pt_stability.hpp:373-455) run on from a
-// point already inside the trial's basin, so only the FP64 tail is paid.
-template <int NM>
-__device__ int continue_trial64(const Mixture& m, fp64::Cell<NM>& c, const Workspace& ws, int64_t cell, int k,
-                                const double* ref, double tol, int row, fp64::TpdPoint<NM>& pt,
-                                fp64::TpdPoint<NM>& nx, double* dir, double* lp) {
-    const int n = c.n;
-    double sum = 0.0, cs = 0.0;
-    for (int i = 0; i < n; ++i) {
-        pt.w[i] = c.z[i] > 0.0 ? static_cast<double>(ws.tw[idx(k * NM + i, ws.ncell, cell)]) : 0.0;
-        kahan_add(pt.w[i], sum, cs);
-    }
-    for (int i = 0; i < n; ++i) pt.w[i] /= sum;
-    fp64::StabilityOptions o{tol, row};
-    int evals = 0;
-    return fp64::run_trial(m, c, ref, o, pt, nx, dir, lp, evals);
-}
-
 // ---------------------------------------------------------------------------
 // Stage 3: feed-test decision per cell and split-attempt enumeration.
 template <int NM>
@@ -589,20 +575,11 @@ __global__ void __launch_bounds__(64) decide_kernel(const Mixture* __restrict__ 
             int cls = ws.tclass[idx(k, ws.ncell, c)];
             bool witness = false;
             if (cls == fp32::tMarginal || cls == fp32::tRerun) {
-                int ts;
-                if (cls == fp32::tRerun) {
-                    atomicAdd(&ws.counters[sFeedRerun], 1);
-                    ts = rerun_trial64(m, cell, k, active, s.ref, 1e-10, cInitEvals, nullptr, nullptr, s.pt, s.nx,
-                                       s.dir, s.lp);
-                } else {
-                    atomicAdd(&ws.counters[sFeedContinued], 1);
-                    ts = continue_trial64(m, cell, ws, c, k, s.ref, 1e-10, cInitEvals, s.pt, s.nx, s.dir, s.lp);
-                }
-                if (ts < 0) {
-                    all_stationary = false;
-                } else if (ts == fp64::kNegativeTpd) {
+                // decided in FP64 by the trials64 stage
+                const int ts = ws.t64_status[idx(k, ws.ncell, c)];
+                if (ts == fp64::kNegativeTpd) {
                     witness = true;
-                    for (int i = 0; i < n; ++i) s.w[i] = s.pt.w[i];
+                    for (int i = 0; i < n; ++i) s.w[i] = ws.tw64[idx(k * NM + i, ws.ncell, c)];
                 } else if (ts != fp64::kStationary) {
                     all_stationary = false;
                 }
@@ -863,6 +840,31 @@ __device__ bool split_accepted(const fp64::SplitState<NM>& st, int n) {
            1.0 - st.beta > 1e-10 && contrast > 1e-7 && st.z_v - st.z_l > 1e-8 * fmax(st.z_v, st.z_l);
 }
 
+// Phase-set review set-up for the selected pair (pt_split.hpp:490-512):
+// Gibbs change against the feed, its guard, the review tolerance and the
+// imposed reference ln(phi_eq) = common - ln z on the twice-normalised feed.
+template <int NM>
+__device__ void begin_review(const Workspace& ws, int64_t c, fp64::Cell<NM>& c64, double best_g) {
+    const int n = c64.n;
+    double feed_g = 0.0, corr = 0.0, magnitude = 1.0;
+    for (int i = 0; i < n; ++i) {
+        if (c64.z[i] == 0.0) continue;
+        const double phi = ws.ref_lnphi[idx(i, ws.ncell, c)];
+        kahan_add(c64.z[i] * (c64.lz[i] + phi), feed_g, corr);
+        magnitude += c64.z[i] * (fabs(c64.lz[i]) + fabs(phi));
+    }
+    const double fug = ws.cand_s[idx(3, ws.ncell, c)];
+    ws.cand_s[idx(4, ws.ncell, c)] = best_g - feed_g;
+    ws.cand_s[idx(5, ws.ncell, c)] = ws.cand_s[idx(7, ws.ncell, c)] + 256.0 * kEps * magnitude;
+    ws.cand_s[idx(6, ws.ncell, c)] = 1e-10 + 0.5 * fug;
+    double zz[NM];
+    for (int i = 0; i < n; ++i) zz[i] = c64.z[i];
+    fp64::normalise_feed(c64, zz);
+    for (int i = 0; i < n; ++i)
+        ws.cand[idx(6 * NM + i, ws.ncell, c)] = c64.z[i] > 0.0 ? ws.cand[idx(5 * NM + i, ws.ncell, c)] - c64.lz[i] : 0.0;
+    ws.phase[c] = pReview;
+}
+
 template <int NM>
 __device__ void store_candidate(const Workspace& ws, int64_t c, const fp64::SplitState<NM>& st, int n) {
     for (int i = 0; i < n; ++i) {
@@ -941,58 +943,36 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
             best_g = s.st.gibbs;
             store_candidate(ws, c, s.st, n);
         }
-        if (!have) {
-            // FP64 continuation (reference ln K iteration, pt_split.hpp:275-408) of
-            // every attempt FP32 left unsettled, from its FP32 end point
-            for (int a = 0; a < na; ++a) {
-                const int cls = ws.att_class[idx(a, ws.ncell, c)];
-                if (cls == fp32::aTrivial) continue;
-                for (int i = 0; i < n; ++i) s.lnk[i] = ws.att_lnk[idx(a * NM + i, ws.ncell, c)];
-                int evals = 0;
-                const int st = fp64::iterate_split(m, c64, s.lnk, s.st, s.nx, s.other, evals, 20000, s.e, s.num);
-                if (st != fp64::kConverged) continue;
-                if (have && !(s.st.gibbs < best_g)) continue;
-                have = true;
-                best_g = s.st.gibbs;
-                store_candidate(ws, c, s.st, n);
-            }
-        }
         atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], c64.counters[cSplitEvals]);
         atomicAdd(&ws.counters_out[idx(cRrIters, ws.ncell, c)], c64.counters[cRrIters]);
         if (!have) {
-            bool any_failed = false;
-            for (int a = 0; a < na; ++a) any_failed = any_failed || ws.att_class[idx(a, ws.ncell, c)] != fp32::aTrivial;
-            if (!any_failed) {
+            // FP64 continuation (reference ln K iteration, pt_split.hpp:275-408) of
+            // every attempt FP32 left unsettled, from its FP32 end point: split64 items
+            int cnt = 0;
+            for (int a = 0; a < na; ++a) cnt += ws.att_class[idx(a, ws.ncell, c)] != fp32::aTrivial;
+            if (cnt == 0) {
                 ws.phase[c] = pIndeterminate;  // every attempt collapsed to the trivial solution
                 write_status_only<NM>(out, ws, c, kIndeterminate, false);
                 write_counters<NM>(out, ws, c);
                 continue;
             }
-            ws.phase[c] = pFallback;
-            atomicAdd(&ws.counters[qFallback], 1);
+            const int base = atomicAdd(&ws.counters[qS64Items], cnt);
+            if (base + cnt > ws.s64_capacity) {
+                ws.phase[c] = pFallback;
+                atomicAdd(&ws.counters[qFallback], 1);
+                atomicAdd(&ws.counters[best < 0 ? sFbNoAttempt : (polish_failed ? sFbPolish : sFbRejected)], 1);
+                continue;
+            }
+            int k = 0;
+            for (int a = 0; a < na; ++a)
+                if (ws.att_class[idx(a, ws.ncell, c)] != fp32::aTrivial) ws.s64_items[base + k++] = (static_cast<int>(c) << 5) | a;
+            ws.s64_base[c] = base;
+            ws.s64_count[c] = cnt;
+            ws.phase[c] = pSplit64;
             atomicAdd(&ws.counters[best < 0 ? sFbNoAttempt : (polish_failed ? sFbPolish : sFbRejected)], 1);
             continue;
         }
-        // phase-set review set-up, pt_split.hpp:490-512
-        double feed_g = 0.0, corr = 0.0, magnitude = 1.0;
-        for (int i = 0; i < n; ++i) {
-            if (c64.z[i] == 0.0) continue;
-            const double phi = ws.ref_lnphi[idx(i, ws.ncell, c)];
-            kahan_add(c64.z[i] * (c64.lz[i] + phi), feed_g, corr);
-            magnitude += c64.z[i] * (fabs(c64.lz[i]) + fabs(phi));
-        }
-        const double fug = ws.cand_s[idx(3, ws.ncell, c)];
-        ws.cand_s[idx(4, ws.ncell, c)] = best_g - feed_g;
-        ws.cand_s[idx(5, ws.ncell, c)] = ws.cand_s[idx(7, ws.ncell, c)] + 256.0 * kEps * magnitude;
-        ws.cand_s[idx(6, ws.ncell, c)] = 1e-10 + 0.5 * fug;
-        // the review normalises the feed once more (pt_stability.hpp:242, :278)
-        double zz[NM];
-        for (int i = 0; i < n; ++i) zz[i] = c64.z[i];
-        fp64::normalise_feed(c64, zz);
-        for (int i = 0; i < n; ++i)
-            ws.cand[idx(6 * NM + i, ws.ncell, c)] =
-                c64.z[i] > 0.0 ? ws.cand[idx(5 * NM + i, ws.ncell, c)] - c64.lz[i] : 0.0;
-        ws.phase[c] = pReview;
+        begin_review(ws, c, c64, best_g);
     }
 }
 
@@ -1052,14 +1032,7 @@ __global__ void __launch_bounds__(64) finish_kernel(const Mixture* __restrict__ 
             if (cls == fp32::tNegative) {
                 negative = true;
             } else if (cls == fp32::tMarginal || cls == fp32::tRerun) {
-                int ts;
-                if (cls == fp32::tRerun) {
-                    atomicAdd(&ws.counters[sReviewRerun], 1);
-                    ts = rerun_trial64(m, cell, k, active, s.ref, tol, cFinalEvals, ex0, ex1, s.pt, s.nx, s.dir, s.lp);
-                } else {
-                    atomicAdd(&ws.counters[sReviewContinued], 1);
-                    ts = continue_trial64(m, cell, ws, c, k, s.ref, tol, cFinalEvals, s.pt, s.nx, s.dir, s.lp);
-                }
+                const int ts = ws.t64_status[idx(k, ws.ncell, c)];
                 if (ts == fp64::kNegativeTpd) negative = true;
                 else if (ts != fp64::kStationary) stationary = false;
             }

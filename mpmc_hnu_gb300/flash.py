@@ -66,11 +66,13 @@ EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu
                     "mpmc_gpu_flash_solve_device", "mpmc_gpu_flash_components", "mpmc_gpu_flash_last_error",
                     "mpmc_gpu_flash_abi_version", "mpmc_gpu_flash_stage_timings", "mpmc_gpu_flash_batch_stats"]
 BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun", "fallback_nonsmooth",
-               "fallback_no_attempt", "fallback_polish", "fallback_rejected", "fallback_load", "two_candidates"]
+               "fp64_attempts_no_fp32", "fp64_attempts_polish_failed", "fp64_attempts_rejected", "fallback_load",
+               "two_candidates"]
 FLAG_STAGE_TIMING = 1
 STAGES = {FORM_PLAIN_FP64: ["flash", "sensitivity"],
-          FORM_MIXED: ["setup", "feed_trials", "decide", "split", "polish", "relist", "review_trials", "finish",
-                       "fallback", "sensitivity"]}
+          FORM_MIXED: ["setup", "feed_trials", "feed_classify", "feed_trials64", "decide", "split", "polish",
+                       "split64", "select64", "relist", "review_trials", "review_classify", "review_trials64",
+                       "finish", "fallback", "sensitivity"]}
 
 _LIB = None
 
@@ -176,8 +178,8 @@ class GpuFlash:
 
     def stage_timings(self) -> dict[str, float]:
         """Per-stage device milliseconds of the last solve (stage_timing=True)."""
-        ms = np.zeros(16, np.float32)
-        k = library().mpmc_gpu_flash_stage_timings(self._h, ms.ctypes.data, 16)
+        ms = np.zeros(24, np.float32)
+        k = library().mpmc_gpu_flash_stage_timings(self._h, ms.ctypes.data, 24)
         names = STAGES.get(self.form, [])
         return {names[i] if i < len(names) else f"stage{i}": float(ms[i]) for i in range(max(k, 0))}
 
