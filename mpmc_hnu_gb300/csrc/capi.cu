@@ -204,9 +204,17 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
             return fail(MPMC_ERR_INVALID_ARGUMENT, "mixed form: at most 16,777,215 cells per call");
         const size_t need = pr76::batched_workspace_bytes(h->n, ncell);
         if ((e = h->workspace.ensure(need)) != cudaSuccess) return cuda_fail(e, "batched workspace allocation");
-        pr76::BatchedShape shape{0, 0, h->stage_timing ? h->events : nullptr};
-        if (const char* v = std::getenv("MPMC_TRIAL_BLOCKS_PER_SM")) shape.trial_blocks_per_sm = std::atoi(v);
-        if (const char* v = std::getenv("MPMC_SPLIT_BLOCKS_PER_SM")) shape.split_blocks_per_sm = std::atoi(v);
+        pr76::BatchedShape shape{0, 0, 0, 0, 0, h->stage_timing ? h->events : nullptr};
+        const struct {
+            const char* name;
+            int* field;
+        } knobs[] = {{"MPMC_TRIAL_BLOCKS_PER_SM", &shape.trial_blocks_per_sm},
+                     {"MPMC_SPLIT_BLOCKS_PER_SM", &shape.split_blocks_per_sm},
+                     {"MPMC_T64_BLOCKS_PER_SM", &shape.t64_blocks_per_sm},
+                     {"MPMC_S64_BLOCKS_PER_SM", &shape.s64_blocks_per_sm},
+                     {"MPMC_CELL_BLOCKS_PER_SM", &shape.cell_blocks_per_sm}};
+        for (const auto& k : knobs)
+            if (const char* v = std::getenv(k.name)) *k.field = std::atoi(v);
         e = pr76::launch_batched(h->n, h->d_mixture, ncell, p, t, z, d, h->workspace.ptr, h->workspace.bytes, shape,
                                  stream);
         next_event = h->stage_timing ? pr76::kBatchedStages + 1 : 0;

@@ -95,7 +95,7 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     e = cudaMemsetAsync(ws.s64_items, 0xff, sizeof(int) * static_cast<size_t>(ws.s64_capacity), stream);
     if (e != cudaSuccess) return e;
     const int cell_block = 64;
-    const int64_t cell_grid_max = static_cast<int64_t>(sms) * 8;
+    const int64_t cell_grid_max = static_cast<int64_t>(sms) * (shape.cell_blocks_per_sm > 0 ? shape.cell_blocks_per_sm : 8);
     auto cell_grid = [&](int64_t items) {
         int64_t g = (items + cell_block - 1) / cell_block;
         return static_cast<unsigned>(g < cell_grid_max ? (g > 0 ? g : 1) : cell_grid_max);
@@ -105,8 +105,8 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
                                                         : resident_blocks(trials32_kernel<NM>, qblock);
     const int split_res = shape.split_blocks_per_sm > 0 ? shape.split_blocks_per_sm
                                                         : resident_blocks(split32_kernel<NM>, qblock);
-    const int t64_res = resident_blocks(trials64_kernel<NM>, 64);
-    const int s64_res = resident_blocks(split64_kernel<NM>, 64);
+    const int t64_res = shape.t64_blocks_per_sm > 0 ? shape.t64_blocks_per_sm : resident_blocks(trials64_kernel<NM>, 64);
+    const int s64_res = shape.s64_blocks_per_sm > 0 ? shape.s64_blocks_per_sm : resident_blocks(split64_kernel<NM>, 64);
     int stage = 0;
     auto mark = [&]() {
         if (shape.events) cudaEventRecord(shape.events[stage], stream);

@@ -48,6 +48,9 @@ LaunchShape plain_launch_shape();
 struct BatchedShape {
     int trial_blocks_per_sm;
     int split_blocks_per_sm;
+    int t64_blocks_per_sm;    // FP64 trial items (64 threads per block)
+    int s64_blocks_per_sm;    // FP64 attempt items (64 threads per block)
+    int cell_blocks_per_sm;   // per-cell FP64 kernels (polish, decide, ...; 64 threads per block)
     cudaEvent_t* events;  // optional: kBatchedStages + 1 events recorded around the stages
 };
 constexpr int kBatchedStages = 15;
