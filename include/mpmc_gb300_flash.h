@@ -183,7 +183,11 @@ int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* handle, float* ms, int capacity
  * (nonsmooth feed phase), [5..7] cells whose split attempts were continued in
  * FP64 because no FP32 attempt settled / the polish did not converge / the
  * polished pair failed the acceptance rules, [8] cells with unusable
- * constants, [9] cells whose two best attempts were both polished.
+ * constants, [9] cells whose two best attempts were both polished,
+ * [10] FP64 trial items, [11] FP64 attempt items, [12] cells polished,
+ * [13] cells whose attempts were selected in FP64, [14] slow FP32 trials
+ * whose exact re-run was skipped because another trial of the same test was
+ * already negative.
  * Writes up to `capacity` values; returns the number available (0 for the
  * plain form).  Diagnostic entry point with no counterpart in the reference. */
 int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* handle, int64_t* out, int capacity);

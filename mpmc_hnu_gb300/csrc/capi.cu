@@ -316,15 +316,15 @@ int mpmc_gpu_flash_components(const mpmc_gpu_flash* h) { return h ? h->n : 0; }
 
 int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* h, int64_t* out, int capacity) {
     if (!h || h->form != MPMC_FORM_MIXED || !h->workspace.ptr) return 0;
-    constexpr int kFirst = 8, kCount = 10;  // workspace counter slots 8..17
-    int vals[kCount] = {};
+    // workspace counter slots (pr76_batched.cuh Slot) in the documented order
+    constexpr int kSlots[] = {8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 20, 22, 23, 24};
+    constexpr int kCount = static_cast<int>(sizeof(kSlots) / sizeof(kSlots[0]));
+    int vals[32] = {};
     if (cudaSetDevice(h->device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return 0;
     // the counters are the first array of the workspace
-    if (cudaMemcpy(vals, static_cast<int*>(h->workspace.ptr) + kFirst, sizeof(vals), cudaMemcpyDeviceToHost) !=
-        cudaSuccess)
-        return 0;
+    if (cudaMemcpy(vals, h->workspace.ptr, sizeof(vals), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
     for (int k = 0; k < kCount && k < capacity; ++k)
-        if (out) out[k] = vals[k];
+        if (out) out[k] = vals[kSlots[k]];
     return kCount;
 }
 

@@ -57,6 +57,8 @@ size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell) {
     ws.s64_items = reinterpret_cast<int*>(take(sizeof(int) * cap));
     ws.s64_status = reinterpret_cast<signed char*>(take(cap));
     ws.s64_state = reinterpret_cast<double*>(take(sizeof(double) * batched::S64Stride<NM>() * cap));
+    ws.split_cells = reinterpret_cast<int*>(take(sizeof(int) * nc));
+    ws.s64_cells = reinterpret_cast<int*>(take(sizeof(int) * nc));
     ws.s64_base = reinterpret_cast<int*>(take(sizeof(int) * nc));
     ws.s64_count = reinterpret_cast<int*>(take(sizeof(int) * nc));
     return off;
@@ -95,7 +97,9 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     e = cudaMemsetAsync(ws.s64_items, 0xff, sizeof(int) * static_cast<size_t>(ws.s64_capacity), stream);
     if (e != cudaSuccess) return e;
     const int cell_block = 64;
-    const int64_t cell_grid_max = static_cast<int64_t>(sms) * (shape.cell_blocks_per_sm > 0 ? shape.cell_blocks_per_sm : 8);
+    // per-cell FP64 kernels and FP64 work items run best at low residency
+    // (their per-thread local state then stays in L1/L2)
+    const int64_t cell_grid_max = static_cast<int64_t>(sms) * (shape.cell_blocks_per_sm > 0 ? shape.cell_blocks_per_sm : 2);
     auto cell_grid = [&](int64_t items) {
         int64_t g = (items + cell_block - 1) / cell_block;
         return static_cast<unsigned>(g < cell_grid_max ? (g > 0 ? g : 1) : cell_grid_max);
@@ -105,8 +109,8 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
                                                         : resident_blocks(trials32_kernel<NM>, qblock);
     const int split_res = shape.split_blocks_per_sm > 0 ? shape.split_blocks_per_sm
                                                         : resident_blocks(split32_kernel<NM>, qblock);
-    const int t64_res = shape.t64_blocks_per_sm > 0 ? shape.t64_blocks_per_sm : resident_blocks(trials64_kernel<NM>, 64);
-    const int s64_res = shape.s64_blocks_per_sm > 0 ? shape.s64_blocks_per_sm : resident_blocks(split64_kernel<NM>, 64);
+    const int t64_res = shape.t64_blocks_per_sm > 0 ? shape.t64_blocks_per_sm : 2;
+    const int s64_res = shape.s64_blocks_per_sm > 0 ? shape.s64_blocks_per_sm : 2;
     int stage = 0;
     auto mark = [&]() {
         if (shape.events) cudaEventRecord(shape.events[stage], stream);

@@ -37,6 +37,9 @@ constexpr int kMaxAttempts = 16;
 // feed trials, split attempts and review trials, and this row (the plain
 // form's cubic-iteration row) holds every FP64 property evaluation.
 constexpr int kFp64EvalRow = cRootIters;
+// Flag added to an FP32 trial class when its descent converges too slowly for
+// the reference's FP64 run to be sure of finishing within 512 iterations.
+constexpr int kSlowFlag = 8;
 
 // Queue/counter slots in Workspace::counters.
 enum Slot : int {
@@ -60,6 +63,9 @@ enum Slot : int {
     qT64Cursor = 19,
     qS64Items = 20,        // FP64 attempt items listed
     qS64Cursor = 21,
+    qSplitCells = 22,      // cells listed for the polish stage
+    qS64Cells = 23,        // cells listed for the FP64 attempt selection
+    sSlowSkipped = 24,     // slow trials whose outcome could not change the cell's status
     qSlots = 32
 };
 
@@ -102,6 +108,8 @@ struct Workspace {
     int* s64_items;         // [s64_capacity] FP64 attempt items (cell << 5 | order)
     signed char* s64_status;// [s64_capacity]
     double* s64_state;      // [s64_capacity * S64Stride] converged attempt states
+    int* split_cells;       // [ncell] cells that reached the split stage
+    int* s64_cells;         // [ncell] cells whose attempts were continued in FP64
     int* s64_base;          // [ncell] first FP64 attempt item of the cell
     int* s64_count;         // [ncell]
     int s64_capacity;
@@ -400,17 +408,18 @@ __device__ int trial_classify(const TrialLane<NM>& L) {
     const float margin = so.decide * L.point.mag;
     if (L.point.value < -margin) return fp32::tNegative;
     // a descent that would exhaust the reference's 512-iteration budget ends
-    // "iteration_limit" there: re-run it exactly in FP64
-    if (L.iter >= 400 || projected_fp64_iterations(L) > 320.f) return fp32::tRerun;
-    if (L.point.stat > 10.f * so.stat_tol) return fp32::tMarginal;
+    // "iteration_limit" there; the classify stage re-runs it exactly in FP64
+    // whenever its outcome can matter
+    const int slow = (L.iter >= 400 || projected_fp64_iterations(L) > 320.f) ? kSlowFlag : 0;
+    if (L.point.stat > 10.f * so.stat_tol) return fp32::tMarginal | slow;
     for (int r = 0; r < L.nrefs; ++r) {
         float dist = 0.f;
         for (int i = 0; i < n; ++i)
             if (L.cell.z[i] > 0.f) dist = fmaxf(dist, fabsf(L.point.lw[i] - L.lrefs[r * NM + i]));
-        if (dist <= so.near_ref) return fp32::tTangent;
+        if (dist <= so.near_ref) return fp32::tTangent | slow;
     }
-    if (L.point.value > margin) return fp32::tPositive;
-    return fp32::tMarginal;
+    if (L.point.value > margin) return fp32::tPositive | slow;
+    return fp32::tMarginal | slow;
 }
 
 template <int NM>
@@ -612,6 +621,7 @@ __global__ void __launch_bounds__(64) decide_kernel(const Mixture* __restrict__ 
         atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], cell.counters[cInitEvals]);
         if (negative) {
             ws.phase[c] = pSplit;
+            ws.split_cells[atomicAdd(&ws.counters[qSplitCells], 1)] = static_cast<int>(c);
             atomicAdd(&ws.counters_out[idx(cAttempts, ws.ncell, c)], nattempt);
         } else if (all_stationary) {
             ws.phase[c] = pSingle;
@@ -888,11 +898,10 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
                                                     DeviceOutputs out) {
     __shared__ Mixture m;
     stage_mixture(mix_g, m);
-    const int cells = ws.counters[qTrialCells];  // the feed-test list; only pSplit cells act
+    const int cells = ws.counters[qSplitCells];
     const int n = m.n;
     for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < cells; slot += gridDim.x * blockDim.x) {
-        const int64_t c = ws.trial_cells[slot];
-        if (ws.phase[c] != pSplit) continue;
+        const int64_t c = ws.split_cells[slot];
         fp64::Cell<NM> c64;
         PolishScratch<NM> s;
         if (!load_cell64(m, ws, c, p, t, c64)) {
@@ -969,6 +978,7 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
             ws.s64_base[c] = base;
             ws.s64_count[c] = cnt;
             ws.phase[c] = pSplit64;
+            ws.s64_cells[atomicAdd(&ws.counters[qS64Cells], 1)] = static_cast<int>(c);
             atomicAdd(&ws.counters[best < 0 ? sFbNoAttempt : (polish_failed ? sFbPolish : sFbRejected)], 1);
             continue;
         }

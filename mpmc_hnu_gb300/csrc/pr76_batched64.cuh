@@ -423,10 +423,29 @@ __global__ void __launch_bounds__(128) classify_kernel(const Mixture* __restrict
         int active = 0;
         for (int i = 0; i < n; ++i) active += ws.z[idx(i, ws.ncell, c)] > 0.0;
         const int ntr = auto_starts(active) + (review ? 2 : 0);
+        bool fp32_negative = false;
+        for (int k = 0; k < ntr; ++k) fp32_negative = fp32_negative || ws.tclass[idx(k, ws.ncell, c)] == fp32::tNegative;
         for (int k = 0; k < ntr; ++k) {
-            const int cls = ws.tclass[idx(k, ws.ncell, c)];
-            if (cls != fp32::tMarginal && cls != fp32::tRerun) continue;
-            const bool rerun = cls == fp32::tRerun;
+            const int raw = ws.tclass[idx(k, ws.ncell, c)];
+            if (raw < 0) continue;
+            const int cls = raw & (kSlowFlag - 1);
+            const bool slow = (raw & kSlowFlag) != 0;
+            bool rerun = cls == fp32::tRerun;
+            if (slow) {
+                // Another trial of this test is already negative, so the test is
+                // "unstable" whatever this one does; its FP32 end point has a
+                // nonnegative TPD (positive, or at a reference composition), so
+                // a monotone descent cannot turn it into a witness either.
+                if (fp32_negative && (cls == fp32::tPositive || cls == fp32::tTangent)) {
+                    ws.tclass[idx(k, ws.ncell, c)] = static_cast<signed char>(cls);
+                    atomicAdd(&ws.counters[sSlowSkipped], 1);
+                    continue;
+                }
+                rerun = true;
+            } else if (cls != fp32::tMarginal && cls != fp32::tRerun) {
+                continue;
+            }
+            ws.tclass[idx(k, ws.ncell, c)] = static_cast<signed char>(rerun ? fp32::tRerun : fp32::tMarginal);
             const int mode = review ? (rerun ? mReviewRerun : mReviewContinue) : (rerun ? mFeedRerun : mFeedContinue);
             const int item = atomicAdd(&ws.counters[qT64Items], 1);
             ws.t64_items[item] = trial_item(c, k, mode);
@@ -444,11 +463,10 @@ __global__ void __launch_bounds__(64) select64_kernel(const Mixture* __restrict_
                                                       DeviceOutputs out) {
     __shared__ Mixture m;
     stage_mixture(mix_g, m);
-    const int cells = ws.counters[qTrialCells];
+    const int cells = ws.counters[qS64Cells];
     const int n = m.n;
     for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < cells; slot += gridDim.x * blockDim.x) {
-        const int64_t c = ws.trial_cells[slot];
-        if (ws.phase[c] != pSplit64) continue;
+        const int64_t c = ws.s64_cells[slot];
         const int base = ws.s64_base[c], cnt = ws.s64_count[c];
         int best = -1;
         double best_g = 0.0;

@@ -67,7 +67,8 @@ EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu
                     "mpmc_gpu_flash_abi_version", "mpmc_gpu_flash_stage_timings", "mpmc_gpu_flash_batch_stats"]
 BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun", "fallback_nonsmooth",
                "fp64_attempts_no_fp32", "fp64_attempts_polish_failed", "fp64_attempts_rejected", "fallback_load",
-               "two_candidates"]
+               "two_candidates", "fp64_trial_items", "fp64_attempt_items", "polished_cells", "select64_cells",
+               "slow_trials_skipped"]
 FLAG_STAGE_TIMING = 1
 STAGES = {FORM_PLAIN_FP64: ["flash", "sensitivity"],
           FORM_MIXED: ["setup", "feed_trials", "feed_classify", "feed_trials64", "decide", "split", "polish",
@@ -172,8 +173,8 @@ class GpuFlash:
 
     def batch_stats(self) -> dict[str, int]:
         """Work statistics of the last mixed-form solve."""
-        out = np.zeros(16, np.int64)
-        k = library().mpmc_gpu_flash_batch_stats(self._h, out.ctypes.data, 16)
+        out = np.zeros(32, np.int64)
+        k = library().mpmc_gpu_flash_batch_stats(self._h, out.ctypes.data, 32)
         return {BATCH_STATS[i]: int(out[i]) for i in range(min(k, len(BATCH_STATS)))}
 
     def stage_timings(self) -> dict[str, float]:
