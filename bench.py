@@ -39,6 +39,7 @@ sys.path.insert(0, ROOT)
 
 MIXTURE_SEED = 1001
 CELL_SEED = 2001
+METRIC = "PT flashes/s (Nc=10, 1M cells) mixed vs plain FP64"
 
 
 # ---------------------------------------------------------------------------
@@ -53,29 +54,18 @@ def f_ad(n: int) -> float:
     return (2 / 3) * n ** 3 + 2 * n * n * (n + 1) + 2 * n * (2 * n + 1) * (n + 1) + 2 * (n + 2) * f_eval(n)
 
 
-def make_workload(n: int, ncell: int, near_fraction: float, rank: int, torch, flash, synth, log):
-    """Seeded cells; the near-saturation subset is placed by GPU bisection."""
-    mix = synth.make_mixture(n, MIXTURE_SEED)
-    offset = rank * (4 * ncell)
-    p, t, z = synth.make_cells(n, ncell, CELL_SEED, offset=offset)
-    n_near = int(round(near_fraction * ncell))
-    if n_near == 0:
-        return mix, p, t, z, 0
-    cache_dir = os.path.join(os.path.expanduser("~"), ".cache", "mpmc_gb300")
-    key = f"near_n{n}_c{ncell}_f{near_fraction}_r{rank}_m{MIXTURE_SEED}_s{CELL_SEED}.npz"
-    path = os.path.join(cache_dir, key)
-    if os.path.exists(path):
-        d = np.load(path)
-        return mix, d["p"], d["t"], d["z"], int(d["placed"])
-    t0 = time.time()
-    g = flash.GpuFlash(mix, "mixed")
-    idx = np.arange(n_near)  # the first n_near cells become near-saturation cells
-    # coarse log-p grid: phase count (1 or 2) at 9 pressures per cell
+def place_near(t, z, idx, noise_index, status_fn):
+    """Phase-count change pressure of cells `idx` by a 9-point log-p grid and 7
+    bisection steps in ln p (bracket width 0.55 * 2**-7 < 0.5 %) with
+    `status_fn(p, t, z) -> status`; returns (p of the placed cells, mask).
+    The +-2 % placement noise is drawn at the cells' global indices."""
+    from mpmc_hnu_gb300.synth import uniform, S_NEAR
+
     grid = np.exp(np.linspace(np.log(0.5e6), np.log(40e6), 9))
     tt = np.repeat(t[idx], len(grid))
     zz = np.repeat(z[:, idx], len(grid), axis=1)
     pp = np.tile(grid, len(idx))
-    st = g.solve(pp, tt, zz, fields=["status"])["status"].reshape(len(idx), len(grid))
+    st = status_fn(pp, tt, zz).reshape(len(idx), len(grid))
     two = st == 1
     lo = np.full(len(idx), np.nan)
     hi = np.full(len(idx), np.nan)
@@ -87,25 +77,69 @@ def make_workload(n: int, ncell: int, near_fraction: float, rank: int, torch, fl
         lo_two[change] = two[change, j]
     ok = np.isfinite(lo)
     sel = np.nonzero(ok)[0]
-    for _ in range(7):  # bisection in ln p: bracket width 0.55 * 2**-7 < 0.5 %
+    for _ in range(7):
         mid = 0.5 * (lo[sel] + hi[sel])
-        s = g.solve(np.exp(mid), t[idx[sel]], z[:, idx[sel]], fields=["status"])["status"]
+        s = status_fn(np.exp(mid), t[idx[sel]], z[:, idx[sel]])
         same_as_lo = (s == 1) == lo_two[sel]
         lo[sel] = np.where(same_as_lo, mid, lo[sel])
         hi[sel] = np.where(same_as_lo, hi[sel], mid)
-    from mpmc_hnu_gb300.synth import uniform, S_NEAR
+    u = uniform(CELL_SEED, S_NEAR, np.asarray(noise_index))
+    return np.exp(0.5 * (lo + hi)) * (1.0 + 0.04 * (u - 0.5)), ok
 
-    u = uniform(CELL_SEED, S_NEAR, np.arange(offset, offset + n_near))
-    pb = np.exp(0.5 * (lo + hi))
-    placed = ok.copy()
-    p = p.copy()
-    p[idx[placed]] = pb[placed] * (1.0 + 0.04 * (u[placed] - 0.5))
+
+def base_cells(n: int, ncell: int, near_fraction: float, rank: int, synth):
+    mix = synth.make_mixture(n, MIXTURE_SEED)
+    offset = rank * (4 * ncell)
+    p, t, z = synth.make_cells(n, ncell, CELL_SEED, offset=offset)
+    n_near = int(round(near_fraction * ncell))  # the first n_near cells go near their boundary
+    return mix, offset, p, t, z, n_near
+
+
+def stratified(ncell: int, sample: int) -> np.ndarray:
+    """Every (ncell / sample)-th cell: keeps the near/far mix of the workload."""
+    return np.unique(np.linspace(0, ncell - 1, min(sample, ncell)).astype(np.int64))
+
+
+def make_workload(n: int, ncell: int, near_fraction: float, rank: int, torch, flash, synth, log):
+    """Seeded cells; the near-saturation subset is placed by GPU bisection."""
+    mix, offset, p, t, z, n_near = base_cells(n, ncell, near_fraction, rank, synth)
+    if n_near == 0:
+        return mix, p, t, z, 0
+    cache_dir = os.path.join(os.path.expanduser("~"), ".cache", "mpmc_gb300")
+    key = f"near2_n{n}_c{ncell}_f{near_fraction}_r{rank}_m{MIXTURE_SEED}_s{CELL_SEED}.npz"
+    path = os.path.join(cache_dir, key)
+    if os.path.exists(path):
+        d = np.load(path)
+        return mix, d["p"], d["t"], d["z"], int(d["placed"])
+    t0 = time.time()
+    g = flash.GpuFlash(mix, "mixed")
+    idx = np.arange(n_near)
+    pb, placed = place_near(t, z, idx, offset + idx,
+                            lambda a, b, c: g.solve(a, b, c, fields=["status"])["status"])
     g.close()
+    p = p.copy()
+    p[idx[placed]] = pb[placed]
     log(f"near-saturation placement: {int(placed.sum())}/{n_near} cells bracketed "
         f"({time.time() - t0:.1f} s); the rest keep log-uniform p")
     os.makedirs(cache_dir, exist_ok=True)
     np.savez(path, p=p, t=t, z=z, placed=int(placed.sum()))
     return mix, p, t, z, int(placed.sum())
+
+
+def cpu_workload_sample(n: int, ncell: int, near_fraction: float, sample: int, threads: int, synth):
+    """The stratified sample of the workload placed by the CPU oracle alone
+    (same grid, bisection and noise as the GPU placement)."""
+    from oracle import pyoracle
+
+    mix, offset, p, t, z, n_near = base_cells(n, ncell, near_fraction, 0, synth)
+    idx = stratified(ncell, sample)
+    p, t, z = p[idx].copy(), t[idx], z[:, idx]
+    near = np.nonzero(idx < n_near)[0]
+    if near.size:
+        pb, placed = place_near(t, z, near, offset + idx[near],
+                                lambda a, b, c: pyoracle.flash(mix, a, b, c, threads=threads)["status"])
+        p[near[placed]] = pb[placed]
+    return mix, p, t, z
 
 
 # ---------------------------------------------------------------------------
@@ -167,16 +201,15 @@ def measured_peaks(flash_pkg):
     return lib.mpmc_probe_fp64_flops(200) / 1e12, lib.mpmc_probe_fp32_flops(2000) / 1e12
 
 
-def cpu_flash_rate(mix, p, t, z, sample: int, threads: int, sens: bool):
-    """The CPU oracle (reference algorithm in C++) on a bounded sample."""
+def cpu_flash_rate(mix, p, t, z, threads: int, sens: bool):
+    """The CPU oracle (reference algorithm in C++) over the given cells."""
     from oracle import pyoracle
 
     pyoracle.build()
-    sel = slice(0, sample)
     t0 = time.perf_counter()
-    pyoracle.flash(mix, p[sel], t[sel], z[:, sel], threads=threads, sens=sens)
+    pyoracle.flash(mix, p, t, z, threads=threads, sens=sens)
     dt = time.perf_counter() - t0
-    return sample / dt, dt
+    return p.shape[0] / dt, dt
 
 
 # ---------------------------------------------------------------------------
@@ -192,7 +225,7 @@ def main() -> None:
     ap.add_argument("--near-fraction", type=float, default=0.3)
     ap.add_argument("--no-ad", action="store_true")
     ap.add_argument("--plain-sample", type=int, default=32768)
-    ap.add_argument("--cpu-sample", type=int, default=16384)
+    ap.add_argument("--cpu-sample", type=int, default=65536)
     ap.add_argument("--profile", action="store_true", help="one untimed solve of the workload (for ncu)")
     args = ap.parse_args()
 
@@ -215,21 +248,25 @@ def main() -> None:
         # not present on the GPU host) on every host core; rank 0 only
         if rank != 0:
             return
-        mix = synth.make_mixture(args.n, MIXTURE_SEED)
-        p, t, z = synth.make_cells(args.n, args.cpu_sample, CELL_SEED)
+        t0 = time.time()
+        mix, p, t, z = cpu_workload_sample(args.n, args.cells, args.near_fraction, args.cpu_sample, threads, synth)
+        log(f"reference arm: {p.shape[0]} stratified cells placed in {time.time() - t0:.1f} s")
         rates = []
         for k in range(args.warmup + args.steps):
-            r, _ = cpu_flash_rate(mix, p, t, z, args.cpu_sample, threads, sens)
+            r, _ = cpu_flash_rate(mix, p, t, z, threads, sens)
             if k >= args.warmup:
                 rates.append(r)
         v = statistics.median(rates)
-        line = {"impl": "reference", "metric": "PT flashes/s (Nc=10, 1M cells)", "value": v, "unit": "flashes/s",
-                "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": args.cpu_sample / v * 1e3,
+        sample = (f"{p.shape[0]} stratified cells (every {args.cells // p.shape[0]}th) of the workload per step, "
+                  f"near-boundary cells placed by the same bisection with the CPU flash; flash"
+                  f"{' + AD' if sens else ''}")
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "flashes/s",
+                "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": p.shape[0] / v * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-                "data": "synthetic (seeded generator; log-uniform p sample)",
-                "config": {**workload, "cells_per_step": args.cpu_sample},
+                "data": "synthetic (seeded generator, stratified sample)",
+                "config": {**workload, "cells_per_step": int(p.shape[0])},
                 "cpu_baseline": {"value": v, "unit": "flashes/s", "cores": threads, "kind": "port",
-                                 "sample": f"{args.cpu_sample} cells of the same mixture per step"},
+                                 "sample": sample},
                 "e2e": {"value": v, "unit": "flashes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
@@ -329,11 +366,13 @@ def main() -> None:
     # plain FP64 form on a bounded sample of the same cells
     plain = None
     if args.form == "mixed" and args.plain_sample > 0 and rank == 0:
-        ns = min(args.plain_sample, ncell)
+        sel = stratified(ncell, args.plain_sample)
+        ns = int(sel.size)
+        isel = torch.from_numpy(sel).to(dp.device)
         gp = flash.GpuFlash(mix, "plain", sensitivity=sens, device=device)
-        sub = {f: v[:, :ns].contiguous() for f, v in outs.items()}
+        sub = {f: torch.empty((v.shape[0], ns), dtype=v.dtype, device=v.device) for f, v in outs.items()}
         sp = {f: v.data_ptr() for f, v in sub.items()}
-        dps, dts, dzs = dp[:ns].contiguous(), dt[:ns].contiguous(), dz[:, :ns].contiguous()
+        dps, dts, dzs = dp[isel].contiguous(), dt[isel].contiguous(), dz[:, isel].contiguous()
         gp.solve_device(min(ns, 4096), dps.data_ptr(), dts.data_ptr(), dzs.data_ptr(), sp, stream.cuda_stream)
         torch.cuda.synchronize()
         a0 = torch.cuda.Event(enable_timing=True)
@@ -345,7 +384,8 @@ def main() -> None:
         pms = a0.elapsed_time(a1)
         ps = sub["status"][0].cpu().numpy()
         plain = {"value": ns / (pms * 1e-3), "unit": "flashes/s", "cells": ns,
-                 "status_agreement_with_chosen": float((ps == status[:ns]).mean())}
+                 "sample": f"{ns} stratified cells (every {ncell // ns}th) of the workload, one launch",
+                 "status_agreement_with_chosen": float((ps == status[sel]).mean())}
         gp.close()
 
     fp64_tf, fp32_tf = measured_peaks(flash)
@@ -384,13 +424,14 @@ def main() -> None:
 
     cpu = None
     if rank == 0:
-        rate, secs = cpu_flash_rate(mix, p, t, z, min(args.cpu_sample, ncell), threads, sens)
+        sel = stratified(ncell, args.cpu_sample)
+        rate, secs = cpu_flash_rate(mix, p[sel], t[sel], z[:, sel], threads, sens)
         cpu = {"value": rate, "unit": "flashes/s", "cores": threads, "kind": "port",
-               "sample": f"first {min(args.cpu_sample, ncell)} cells of this workload, flash + AD, "
-                         f"{secs:.1f} s wall on {threads} threads"}
+               "sample": f"{sel.size} stratified cells (every {ncell // sel.size}th) of this workload, flash"
+                         f"{' + AD' if sens else ''}, {secs:.1f} s wall on {threads} threads"}
 
     if rank == 0:
-        line = {"metric": "PT flashes/s (Nc=10, 1M cells) mixed vs plain FP64", "value": value,
+        line = {"metric": METRIC, "value": value,
                 "unit": "flashes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32 iterations + f64 decisions/polish/AD" if args.form == "mixed" else "f64",

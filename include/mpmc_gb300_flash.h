@@ -165,6 +165,38 @@ int mpmc_gpu_flash_solve(mpmc_gpu_flash* handle, int64_t n_cells, const double* 
 int mpmc_gpu_flash_solve_device(mpmc_gpu_flash* handle, int64_t n_cells, const double* p, const double* t,
                                 const double* z, const mpmc_flash_outputs* out, void* stream);
 
+/* Largest device scratch, in bytes, of mpmc_gpu_flash_solve_device_noalloc:
+ * a fixed 48 MiB array in the library's device code. */
+#define MPMC_NOALLOC_SCRATCH_BYTES (48u << 20)
+
+/* mpmc_gpu_flash_solve_device for callers that must not allocate device memory
+ * during a solve: code that runs while a CUDA graph is being captured on its
+ * stream, a solver callback inside a host application whose memory pool owns
+ * every allocation, or a latency-bound request loop that cannot afford an
+ * allocation on its path.  No counterpart in the reference (whose backend
+ * allocates host vectors per solve, pt_flash_backend.hpp:125-182).
+ *
+ * Mixed-precision handles only (MPMC_FORM_MIXED; other forms return
+ * MPMC_ERR_UNSUPPORTED).  The work buffers of the solve live in one fixed
+ * MPMC_NOALLOC_SCRATCH_BYTES array of device memory per device; a batch whose
+ * buffers do not fit (about 4,900 cells at 20 components, 9,700 at 10, more
+ * with fewer components) returns MPMC_ERR_INVALID_ARGUMENT with the size in
+ * the message.  The first call on a device looks the array's address up
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture.  The call itself allocates nothing: it validates,
+ * enqueues its kernels and a zeroing of the work counters on `stream`, and
+ * returns without synchronising.  All handles on a device share the array, so
+ * calls whose work overlaps on the device (two streams, or two host threads)
+ * race and corrupt each other: serialise them, e.g. on one stream.  When the
+ * handle was created with want_sensitivity, the flash fields the sensitivity
+ * kernel reads back (status, vapor_fraction, liquid, vapor, ln_k, z_liquid,
+ * z_vapor) must be provided, because there is no scratch to route them to.
+ * Stage timing is not recorded.  Results equal those of
+ * mpmc_gpu_flash_solve_device on the same inputs. */
+int mpmc_gpu_flash_solve_device_noalloc(mpmc_gpu_flash* handle, int64_t n_cells, const double* p,
+                                        const double* t, const double* z, const mpmc_flash_outputs* out,
+                                        void* stream);
+
 /* Device time in milliseconds of every stage of the last solve on a handle
  * created with MPMC_FLAG_STAGE_TIMING (waits for that solve to finish).
  * Stages, in order -- plain form: flash, sensitivity; mixed form: setup,
@@ -187,7 +219,8 @@ int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* handle, float* ms, int capacity
  * [10] FP64 trial items, [11] FP64 attempt items, [12] cells polished,
  * [13] cells whose attempts were selected in FP64, [14] slow FP32 trials
  * whose exact re-run was skipped because another trial of the same test was
- * already negative.
+ * already negative, [15] split attempts classified as ending at the
+ * iteration limit without an FP64 run.
  * Writes up to `capacity` values; returns the number available (0 for the
  * plain form).  Diagnostic entry point with no counterpart in the reference. */
 int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* handle, int64_t* out, int capacity);

@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "../../include/mpmc_gb300_flash.h"
@@ -235,6 +236,28 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
     return MPMC_OK;
 }
 
+// ---- fixed scratch of the no-allocation entry point ----
+// One array per device, reserved when the library's device code is loaded;
+// its address is looked up once per device (with that device current).
+__device__ __align__(256) unsigned char g_noalloc_scratch[MPMC_NOALLOC_SCRATCH_BYTES];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_address[kMaxDevices] = {};
+
+int noalloc_scratch(int device, void** out) {
+    if (device < 0 || device >= kMaxDevices) return fail(MPMC_ERR_INVALID_ARGUMENT, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_address[device]) {
+        void* ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess || !ptr) return cuda_fail(e, "cudaGetSymbolAddress (no-allocation scratch)");
+        g_noalloc_address[device] = ptr;
+    }
+    *out = g_noalloc_address[device];
+    return MPMC_OK;
+}
+
 }  // namespace
 
 namespace pr76 {
@@ -317,7 +340,7 @@ int mpmc_gpu_flash_components(const mpmc_gpu_flash* h) { return h ? h->n : 0; }
 int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* h, int64_t* out, int capacity) {
     if (!h || h->form != MPMC_FORM_MIXED || !h->workspace.ptr) return 0;
     // workspace counter slots (pr76_batched.cuh Slot) in the documented order
-    constexpr int kSlots[] = {8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 20, 22, 23, 24};
+    constexpr int kSlots[] = {8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 20, 22, 23, 24, 25};
     constexpr int kCount = static_cast<int>(sizeof(kSlots) / sizeof(kSlots[0]));
     int vals[32] = {};
     if (cudaSetDevice(h->device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return 0;
@@ -405,6 +428,43 @@ int mpmc_gpu_flash_solve_device(mpmc_gpu_flash* h, int64_t ncell, const double* 
     cudaError_t e = cudaSetDevice(h->device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     return run_device(h, ncell, p, t, z, to_device_outputs(out), static_cast<cudaStream_t>(stream));
+}
+
+int mpmc_gpu_flash_solve_device_noalloc(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t,
+                                        const double* z, const mpmc_flash_outputs* out, void* stream) {
+    if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
+    if (h->form != MPMC_FORM_MIXED)
+        return fail(MPMC_ERR_UNSUPPORTED, "the no-allocation entry point serves mixed-precision handles only");
+    if (ncell < 0) return fail(MPMC_ERR_INVALID_ARGUMENT, "negative cell count");
+    if (ncell == 0) return MPMC_OK;
+    if (!p || !t || !z) return fail(MPMC_ERR_INVALID_ARGUMENT, "p, t and z must not be null");
+    if (ncell >= (int64_t{1} << 24))
+        return fail(MPMC_ERR_INVALID_ARGUMENT, "mixed form: at most 16,777,215 cells per call");
+    const size_t need = pr76::batched_workspace_bytes(h->n, ncell);
+    if (need > MPMC_NOALLOC_SCRATCH_BYTES)
+        return fail(MPMC_ERR_INVALID_ARGUMENT,
+                    "no-allocation entry point: " + std::to_string(ncell) + " cells of " + std::to_string(h->n) +
+                        " components need " + std::to_string(need) + " bytes of scratch, above the fixed " +
+                        std::to_string(MPMC_NOALLOC_SCRATCH_BYTES) + " (use mpmc_gpu_flash_solve_device)");
+    const pr76::DeviceOutputs d = to_device_outputs(out);
+    if (h->want_sensitivity && (!d.status || !d.beta || !d.x || !d.y || !d.lnk || !d.z_l || !d.z_v))
+        return fail(MPMC_ERR_INVALID_ARGUMENT,
+                    "no-allocation entry point with sensitivities: status, vapor_fraction, liquid, vapor, ln_k, "
+                    "z_liquid and z_vapor outputs are required");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    void* scratch = nullptr;
+    const int rc = noalloc_scratch(h->device, &scratch);
+    if (rc != MPMC_OK) return rc;
+    const cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const pr76::BatchedShape shape{0, 0, 0, 0, 0, nullptr};
+    e = pr76::launch_batched(h->n, h->d_mixture, ncell, p, t, z, d, scratch, MPMC_NOALLOC_SCRATCH_BYTES, shape, s);
+    if (e != cudaSuccess) return cuda_fail(e, "flash kernel launch");
+    if (h->want_sensitivity) {
+        e = pr76::launch_sensitivity(h->n, h->d_mixture, ncell, p, t, z, d, s);
+        if (e != cudaSuccess) return cuda_fail(e, "sensitivity kernel launch");
+    }
+    return MPMC_OK;
 }
 
 int mpmc_gpu_flash_solve(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,

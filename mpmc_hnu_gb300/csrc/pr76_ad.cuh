@@ -370,13 +370,22 @@ __device__ int sensitivity_cell(const Mixture& m, fp64::Cell<NM>& c, const doubl
         s.dxl[(n - 1) * nv + v] = -lsum;
         s.dyv[(n - 1) * nv + v] = -vsum;
     }
-    // dF/dv by the chain rule through the per-phase full-chart Jacobians
+    // dF/dv by the chain rule through the per-phase Jacobians taken in the
+    // reduced chart of the reference's phase evaluation (evaluate_reduced:
+    // x_{n-1} = 1 - sum of the others, pr76_sensitivity_local.hpp:70-79), i.e.
+    // d/dx_j - d/dx_{n-1} for j < n-1.  Contracting the full-chart columns
+    // with dx (whose entries sum to zero) instead would cancel large terms.
     double res_norm = 0.0;
     for (int i = 0; i < n; ++i) {
+        const double* rl = s.jl + (1 + i) * cols + 2;
+        const double* rv = s.jv + (1 + i) * cols + 2;
         for (int v = 0; v < nv; ++v) {
-            double d = s.dxl[i * nv + v] / xb[i] - s.dyv[i * nv + v] / yb[i];
-            for (int j = 0; j < n; ++j)
-                d += s.jl[(1 + i) * cols + 2 + j] * s.dxl[j * nv + v] - s.jv[(1 + i) * cols + 2 + j] * s.dyv[j * nv + v];
+            // d ln x_i - d ln y_i = -d ln K_i on the RR manifold (y_i = K_i x_i),
+            // taken exactly: the dependent last fractions would give it only up
+            // to a cancellation error of eps * sum|dx| / x_{n-1}
+            double d = v == i ? -1.0 : 0.0;
+            for (int j = 0; j + 1 < n; ++j)
+                d += (rl[j] - rl[n - 1]) * s.dxl[j * nv + v] - (rv[j] - rv[n - 1]) * s.dyv[j * nv + v];
             if (v == n) d += s.jl[(1 + i) * cols + 0] - s.jv[(1 + i) * cols + 0];
             if (v == n + 1) d += s.jl[(1 + i) * cols + 1] - s.jv[(1 + i) * cols + 1];
             if (v < n)

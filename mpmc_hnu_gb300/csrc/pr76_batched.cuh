@@ -66,6 +66,7 @@ enum Slot : int {
     qSplitCells = 22,      // cells listed for the polish stage
     qS64Cells = 23,        // cells listed for the FP64 attempt selection
     sSlowSkipped = 24,     // slow trials whose outcome could not change the cell's status
+    sLimitAttempts = 25,   // attempts classified as ending at the iteration limit
     qSlots = 32
 };
 
@@ -410,6 +411,9 @@ __device__ int trial_classify(const TrialLane<NM>& L) {
     // a descent that would exhaust the reference's 512-iteration budget ends
     // "iteration_limit" there; the classify stage re-runs it exactly in FP64
     // whenever its outcome can matter
+    // (the projection is only a screen: near the FP32 noise floor the measured
+    // contraction understates the FP64 rate, so no trial is declared
+    // "iteration_limit" from it without the FP64 run)
     const int slow = (L.iter >= 400 || projected_fp64_iterations(L) > 320.f) ? kSlowFlag : 0;
     if (L.point.stat > 10.f * so.stat_tol) return fp32::tMarginal | slow;
     for (int r = 0; r < L.nrefs; ++r) {
@@ -696,9 +700,12 @@ __global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict_
                         cls = fp32::aTrivial;
                     else if (L.point.fug <= 1e-3f)
                         cls = fp32::aConverged;
+                    else if (L.iter >= 512)
+                        cls = fp32::aLimit;
                 }
                 const int64_t c = L.c;
                 ws.att_class[idx(L.order, ws.ncell, c)] = static_cast<signed char>(cls);
+                if (cls == fp32::aLimit) atomicAdd(&ws.counters[sLimitAttempts], 1);
                 ws.att_gibbs[idx(L.order, ws.ncell, c)] = L.point.gibbs;
                 for (int i = 0; i < n; ++i) ws.att_lnk[idx(L.order * NM + i, ws.ncell, c)] = L.point.lnk[i];
                 atomicAdd(&ws.counters_out[idx(cSplitEvals, ws.ncell, c)], L.cell.evals);
@@ -842,6 +849,10 @@ __device__ bool polish_split(const Mixture& m, fp64::Cell<NM>& c64, PolishScratc
 }
 
 // Acceptance of a fugacity-converged state, pt_split.hpp:351-362.
+// Attempts the FP64 continuation must settle: every one except those that
+// collapsed to the trivial solution or provably end at the iteration limit.
+__device__ __forceinline__ bool unsettled(int cls) { return cls != fp32::aTrivial && cls != fp32::aLimit; }
+
 template <int NM>
 __device__ bool split_accepted(const fp64::SplitState<NM>& st, int n) {
     double contrast = 0.0;
@@ -958,7 +969,7 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
             // FP64 continuation (reference ln K iteration, pt_split.hpp:275-408) of
             // every attempt FP32 left unsettled, from its FP32 end point: split64 items
             int cnt = 0;
-            for (int a = 0; a < na; ++a) cnt += ws.att_class[idx(a, ws.ncell, c)] != fp32::aTrivial;
+            for (int a = 0; a < na; ++a) cnt += unsettled(ws.att_class[idx(a, ws.ncell, c)]);
             if (cnt == 0) {
                 ws.phase[c] = pIndeterminate;  // every attempt collapsed to the trivial solution
                 write_status_only<NM>(out, ws, c, kIndeterminate, false);
@@ -974,7 +985,7 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
             }
             int k = 0;
             for (int a = 0; a < na; ++a)
-                if (ws.att_class[idx(a, ws.ncell, c)] != fp32::aTrivial) ws.s64_items[base + k++] = (static_cast<int>(c) << 5) | a;
+                if (unsettled(ws.att_class[idx(a, ws.ncell, c)])) ws.s64_items[base + k++] = (static_cast<int>(c) << 5) | a;
             ws.s64_base[c] = base;
             ws.s64_count[c] = cnt;
             ws.phase[c] = pSplit64;

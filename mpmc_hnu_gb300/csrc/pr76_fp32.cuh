@@ -501,7 +501,10 @@ __device__ __forceinline__ void copy_state(SplitState<NM>& d, const SplitState<N
 }
 
 // FP32 split attempt outcomes.
-enum SplitClass : int { aConverged = 0, aTrivial = 1, aFailed = 2 };
+// aLimit: 512 iterations without reaching even FP32 resolution (|r| > 1e-3,
+// two orders above the FP32 floor), so the FP64 iteration from the same seed
+// also ends at its iteration limit (pt_split.hpp:364-366).
+enum SplitClass : int { aConverged = 0, aTrivial = 1, aFailed = 2, aLimit = 3 };
 
 // ln K successive substitution with the Gibbs line search (pt_split.hpp:349-407),
 // run until FP32 resolution (|r| <= 1e-5) or stagnation.

@@ -64,11 +64,13 @@ class _Outputs(ctypes.Structure):
 
 EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu_flash_solve",
                     "mpmc_gpu_flash_solve_device", "mpmc_gpu_flash_components", "mpmc_gpu_flash_last_error",
-                    "mpmc_gpu_flash_abi_version", "mpmc_gpu_flash_stage_timings", "mpmc_gpu_flash_batch_stats"]
+                    "mpmc_gpu_flash_abi_version", "mpmc_gpu_flash_stage_timings", "mpmc_gpu_flash_batch_stats",
+                    "mpmc_gpu_flash_solve_device_noalloc"]
+NOALLOC_SCRATCH_BYTES = 48 << 20
 BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun", "fallback_nonsmooth",
                "fp64_attempts_no_fp32", "fp64_attempts_polish_failed", "fp64_attempts_rejected", "fallback_load",
                "two_candidates", "fp64_trial_items", "fp64_attempt_items", "polished_cells", "select64_cells",
-               "slow_trials_skipped"]
+               "slow_trials_skipped", "limit_attempts"]
 FLAG_STAGE_TIMING = 1
 STAGES = {FORM_PLAIN_FP64: ["flash", "sensitivity"],
           FORM_MIXED: ["setup", "feed_trials", "feed_classify", "feed_trials64", "decide", "split", "polish",
@@ -92,6 +94,7 @@ def library() -> ctypes.CDLL:
             [ctypes.POINTER(_Outputs)]
         lib.mpmc_gpu_flash_solve_device.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 3 + \
             [ctypes.POINTER(_Outputs), ctypes.c_void_p]
+        lib.mpmc_gpu_flash_solve_device_noalloc.argtypes = lib.mpmc_gpu_flash_solve_device.argtypes
         lib.mpmc_gpu_flash_components.argtypes = [ctypes.c_void_p]
         lib.mpmc_gpu_flash_stage_timings.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         lib.mpmc_gpu_flash_batch_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
@@ -190,3 +193,12 @@ class GpuFlash:
         s = _Outputs(**out_ptrs)
         _check(library().mpmc_gpu_flash_solve_device(self._h, ncell, p_ptr, t_ptr, z_ptr, ctypes.byref(s),
                                                      stream))
+
+    def solve_device_noalloc(self, ncell: int, p_ptr: int, t_ptr: int, z_ptr: int, out_ptrs: dict[str, int],
+                             stream: int = 0) -> None:
+        """`solve_device` through the entry point that allocates no device memory
+        (fixed library scratch shared by every handle on the device: calls must
+        not overlap on the device)."""
+        s = _Outputs(**out_ptrs)
+        _check(library().mpmc_gpu_flash_solve_device_noalloc(self._h, ncell, p_ptr, t_ptr, z_ptr, ctypes.byref(s),
+                                                             stream))

@@ -898,7 +898,7 @@ struct Attempt {
 // Split evaluation, pt_split.hpp:300-341.  Returns false with `st` set to the
 // failure class (SplitStepError or property failure).
 inline bool split_evaluate(const Model& m, Work& wk, double p, double t, const std::vector<double>& z,
-                           const std::vector<double>& lk, const SplitOptions& o, long long& evals,
+                           const std::vector<double>& lk, const SplitOptions& /*options*/, long long& evals,
                            long long budget, SplitState& s, AttemptStatus& st) {
     const int n = m.n;
     s.rr = solve_rr(z, lk, wk);
@@ -1247,6 +1247,7 @@ struct Sensitivity {
     std::vector<double> dbeta;         // n+1
     std::vector<double> dzl, dzv, drhol, drhov;  // n+1 (closure linearisation)
     std::vector<double> jl, jv;        // (n+1) x (n+2): d[Z, ln phi]/d[p, T, x_full]
+    double rcond = 0.0;                // reciprocal condition estimate of dF/dln K (test diagnostics)
 };
 
 // LU with partial pivoting + rcond, pt_sensitivity_detail.hpp:364-471
@@ -1451,6 +1452,7 @@ inline void differentiate(const Model& m, const FlashResult& fr, double p, doubl
         return;
     }
     const double rc = lu_rcond(f);
+    s.rcond = rc;
     if (!std::isfinite(rc) || !(rc > 256.0 * kEps * n)) {
         s.status = 5;
         return;
@@ -1716,6 +1718,7 @@ struct OracleOutputs {
     double* drhov;          // [(n+1)*ncell]
     double* jl;             // [(n+1)*(n+2)*ncell]
     double* jv;             // [(n+1)*(n+2)*ncell]
+    double* rcond;          // [ncell] reciprocal condition estimate of dF/dln K (NaN if not factored)
 };
 
 static void oracle_cell(const oracle::Model& m, int64_t ncell, int64_t c, const double* p, const double* t,
@@ -1773,6 +1776,7 @@ static void oracle_cell(const oracle::Model& m, int64_t ncell, int64_t c, const 
     if (fr.status == kTwoPhase) differentiate(m, fr, p[c], t[c], s);
     else s.status = 1;
     if (o->sens_status) o->sens_status[c] = s.status;
+    if (o->rcond) o->rcond[c] = s.rcond > 0.0 ? s.rcond : nan;
     const int q = n + 1;
     const bool ok = s.status == 0;
     for (int k = 0; k < n * q; ++k) {
@@ -1938,10 +1942,11 @@ int oracle_sensitivity_at(int n, const double* tc, const double* pc, const doubl
                     s.status = 4;
                 }
             }
+            const double nan = kNaN;
             if (o->sens_status) o->sens_status[c] = s.status;
+            if (o->rcond) o->rcond[c] = s.rcond > 0.0 ? s.rcond : nan;
             const int q = n + 1;
             const bool good = s.status == 0;
-            const double nan = kNaN;
             for (int k = 0; k < n * q; ++k) {
                 put(o->dlnk, k, good ? s.dlnk[k] : nan);
                 put(o->dx, k, good ? s.dx[k] : nan);

@@ -27,6 +27,7 @@ FIELDS = [
     ("dbeta", ctypes.c_void_p), ("dx", ctypes.c_void_p), ("dy", ctypes.c_void_p),
     ("dzl", ctypes.c_void_p), ("dzv", ctypes.c_void_p), ("drhol", ctypes.c_void_p),
     ("drhov", ctypes.c_void_p), ("jl", ctypes.c_void_p), ("jv", ctypes.c_void_p),
+    ("rcond", ctypes.c_void_p),  # oracle only: the reference harness leaves it unset
 ]
 
 COUNTER_NAMES = ["init_evals", "split_evals", "final_evals", "split_iters", "rr_iters",
@@ -72,7 +73,7 @@ def _alloc(n: int, ncell: int, sens: bool):
             "dbeta": np.empty((q, ncell)), "dx": np.empty((n * q, ncell)), "dy": np.empty((n * q, ncell)),
             "dzl": np.empty((q, ncell)), "dzv": np.empty((q, ncell)), "drhol": np.empty((q, ncell)),
             "drhov": np.empty((q, ncell)), "jl": np.empty(((n + 1) * (n + 2), ncell)),
-            "jv": np.empty(((n + 1) * (n + 2), ncell)),
+            "jv": np.empty(((n + 1) * (n + 2), ncell)), "rcond": np.full(ncell, np.nan),
         })
     s = _Out()
     for name, _ in FIELDS:

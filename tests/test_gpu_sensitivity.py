@@ -31,7 +31,9 @@ class Mix:
 def test_sensitivity_matches_oracle(gpu_lib, oracle_lib, n, ncell, seed, form):
     """Device AD vs the oracle's differentiate_pr76_pt_vle restatement at the
     SAME accepted states (the GPU's), so only the derivative computation is
-    compared; 1e-8 relative to each column's scale."""
+    compared; 1e-8 normwise relative per derivative column, widened for
+    d ln K by the forward-error bound cond(dF/dln K) * eps of its linear
+    solve (parity.sensitivity_report)."""
     mix = synth.make_mixture(n, seed)
     p, t, z = synth.make_cells(n, ncell, seed)
     g = gpu_lib.GpuFlash(mix, form=form, sensitivity=True)
@@ -40,12 +42,16 @@ def test_sensitivity_matches_oracle(gpu_lib, oracle_lib, n, ncell, seed, form):
     ref = oracle_lib.sensitivity_at(mix, p, t, z, two, out["liquid"], out["vapor"], out["ln_k"],
                                     out["vapor_fraction"])
     ref["sens_status"] = np.where(two, ref["sens_status"], 1)
-    rep = parity.sensitivity_report(out, ref)
+    rep = parity.sensitivity_report(out, ref, rcond=ref["rcond"])
     print(form, n, rep)
     assert rep["status_match"] == 1.0, rep
     assert rep["both_ok"] > 0
+    for f, v in rep["bound_ratio"].items():
+        assert v <= 1.0, (f, rep)
+    # all but the conditioning-limited ln K derivatives meet 1e-8 outright
     for f, v in rep["max"].items():
-        assert v <= parity.SENS_TOL, (f, rep)
+        if f != "d_ln_k":
+            assert v <= parity.SENS_TOL, (f, rep)
 
 
 @pytest.mark.gpu
@@ -61,9 +67,9 @@ def test_sensitivity_and_closure_kats(gpu_lib):
         r = g.solve(np.array([case["p"]]), np.array([case["t"]]), np.array(case["feed"], float)[:, None])
         assert int(r["status"][0]) == 1 and int(r["sensitivity_status"][0]) == 0, case["name"]
 
-        def near(got, exp, tol):
+        def near(got, exp, tol, floor=1e-7):
             exp = np.asarray(exp, float)
-            return np.all(np.abs(got - exp) <= tol * np.maximum(1e-7, np.abs(exp)))
+            return np.all(np.abs(got - exp) <= tol * np.maximum(floor, np.abs(exp)))
 
         if "dlnk" in case:
             assert near(r["d_vapor_fraction"][:, 0], case["dbeta"], case["tol"]), case["name"]
@@ -74,9 +80,11 @@ def test_sensitivity_and_closure_kats(gpu_lib):
             primal = [zl, zv, case["p"] / (zl * R * case["t"]), case["p"] / (zv * R * case["t"])]
             for got, exp in zip(primal, case["primal"]):
                 assert abs(got - exp) <= case["primal_tol"] * (1 + abs(exp)), case["name"]
-            for key, gk in (("dzl", "d_z_liquid"), ("dzv", "d_z_vapor"), ("drhol", "d_rho_liquid"),
-                            ("drhov", "d_rho_vapor")):
-                assert near(r[gk][:, 0], case[key], case["tol"]), (case["name"], key)
+            # an exactly-zero derivative (binary: phase properties do not move
+            # with the feed) is compared on the scale of its own quantity
+            for (key, gk), value in zip((("dzl", "d_z_liquid"), ("dzv", "d_z_vapor"), ("drhol", "d_rho_liquid"),
+                                         ("drhov", "d_rho_vapor")), primal):
+                assert near(r[gk][:, 0], case[key], case["tol"], 1e-6 * abs(value)), (case["name"], key)
 
 
 @pytest.mark.gpu
