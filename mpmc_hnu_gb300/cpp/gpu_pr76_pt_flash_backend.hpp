@@ -1,0 +1,190 @@
+// Reference-side binding of the GB300 flash: a PtFlashBackend whose solve
+// calls the C ABI of include/mpmc_gb300_flash.h.
+//
+// A maintainer adds this header to a build of MPMC_HNU's flash module and
+// constructs it where a Pr76PtFlashBackend is constructed today
+// (modules/flash/include/mpmc/flash/pr76_pt_flash_backend.hpp:177-237; callers
+// pt_service.hpp:335, pr76_executable_model.hpp:219).  It keeps the interface
+// of modules/flash/include/mpmc/flash/pt_flash_backend.hpp:187-195 unchanged
+// and adds solve_batch() for the cell loops that own many requests.
+//
+// Contract differences from the PR76 max3 backend, stated in capability():
+// supported phase counts {1, 2} under a distinct backend id (the GPU path is
+// the two-phase contract; a cell whose two-phase set fails the final review is
+// published as phase_set_unstable with its candidate pair, where the max3
+// backend would continue into the three-phase search).
+//
+// Errors follow the reference's classes: an invalid request (feed size,
+// non-finite or non-positive p and T, a feed outside the simplex) throws
+// std::invalid_argument; invalid mixture data at construction throws
+// std::domain_error; a device failure throws std::runtime_error.  Numerical
+// failure is the indeterminate status, never an exception.
+//
+// Not reentrant, like the reference backend (pr76_split.hpp:16-18): one
+// instance per simultaneous caller.
+#pragma once
+
+#include <mpmc/flash/pt_flash_backend.hpp>
+
+#include <cmath>
+#include <cstdint>
+#include <span>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "mpmc_gb300_flash.h"
+
+namespace mpmc::flash {
+
+inline constexpr std::string_view gpu_pr76_pt_flash_backend_id = "GB300/PR76/PT/max2/phase-set-backend/v1";
+inline constexpr std::string_view gpu_pr76_pt_result_convention = "GB300/PR76/PT/max2/phase-set/v1";
+
+struct GpuPr76Mixture {
+    std::vector<std::string> component_ids;
+    std::vector<double> critical_temperature_k;
+    std::vector<double> critical_pressure_pa;
+    std::vector<double> acentric_factor;
+    std::vector<double> kij;  // row-major n x n, symmetric, zero diagonal
+    std::string dataset_id;
+    std::string revision;
+};
+
+class GpuPr76PtFlashBackend final : public PtFlashBackend {
+public:
+    explicit GpuPr76PtFlashBackend(const GpuPr76Mixture& mixture, int form = MPMC_FORM_MIXED, int device = 0)
+        : n_(mixture.component_ids.size()) {
+        if (n_ == 0 || mixture.critical_temperature_k.size() != n_ || mixture.critical_pressure_pa.size() != n_ ||
+            mixture.acentric_factor.size() != n_ || mixture.kij.size() != n_ * n_)
+            throw std::invalid_argument("GPU PR76 backend: mixture arrays do not match the component list");
+        mpmc_pr76_mixture m{static_cast<int32_t>(n_), mixture.critical_temperature_k.data(),
+                            mixture.critical_pressure_pa.data(), mixture.acentric_factor.data(), mixture.kij.data()};
+        mpmc_flash_options o{form, 0, device, 0};
+        check(mpmc_gpu_flash_create(&m, &o, &handle_));
+        capability_.backend_id = std::string(gpu_pr76_pt_flash_backend_id);
+        capability_.model_profile = "PR76";
+        capability_.algorithm_profile = "GB300/PR76/PT/two-phase/v1";
+        capability_.publication_profile = std::string(gpu_pr76_pt_result_convention);
+        capability_.configuration_profile = form == MPMC_FORM_MIXED ? "mixed-precision" : "plain-fp64";
+        capability_.dataset_id = mixture.dataset_id;
+        capability_.revision = mixture.revision;
+        capability_.component_ids = mixture.component_ids;
+        capability_.supported_phase_counts = {1U, 2U};
+        capability_.transition_capability.edges = {
+            {1U, 2U, PtPhaseTransitionSupport::fresh_target_resolve, true},
+            {2U, 1U, PtPhaseTransitionSupport::detection_only, true}};
+        capability_.performs_initial_stability_search = true;
+        capability_.performs_final_phase_set_review = true;
+        capability_.performs_boundary_neighbor_resolve = false;
+        capability_.global_stability_proven = false;
+    }
+
+    GpuPr76PtFlashBackend(const GpuPr76PtFlashBackend&) = delete;
+    GpuPr76PtFlashBackend& operator=(const GpuPr76PtFlashBackend&) = delete;
+    ~GpuPr76PtFlashBackend() override { mpmc_gpu_flash_destroy(handle_); }
+
+    [[nodiscard]] const PtFlashBackendCapability& capability() const noexcept override { return capability_; }
+
+    [[nodiscard]] PtFlashBackendResult solve(const PtFlashRequest& request) override {
+        return std::move(solve_batch(std::span<const PtFlashRequest>(&request, 1)).front());
+    }
+
+    // One device call for every request; results in request order.
+    [[nodiscard]] std::vector<PtFlashBackendResult> solve_batch(std::span<const PtFlashRequest> requests) {
+        const std::size_t cells = requests.size();
+        std::vector<double> p(cells), t(cells), z(n_ * cells);
+        for (std::size_t c = 0; c < cells; ++c) {
+            const PtFlashRequest& r = requests[c];
+            if (r.feed.size() != n_)
+                throw std::invalid_argument("GPU PR76 backend: feed size does not match the capability");
+            p[c] = r.pressure_pa;
+            t[c] = r.temperature_k;
+            for (std::size_t i = 0; i < n_; ++i) z[i * cells + c] = r.feed[i];
+        }
+        std::vector<int32_t> status(cells), counters(MPMC_COUNTER_COUNT * cells);
+        std::vector<double> beta(cells), x(n_ * cells), y(n_ * cells), lnk(n_ * cells), phil(n_ * cells),
+            phiv(n_ * cells), zl(cells), zv(cells);
+        mpmc_flash_outputs out{};
+        out.status = status.data();
+        out.vapor_fraction = beta.data();
+        out.liquid = x.data();
+        out.vapor = y.data();
+        out.ln_k = lnk.data();
+        out.ln_phi_liquid = phil.data();
+        out.ln_phi_vapor = phiv.data();
+        out.z_liquid = zl.data();
+        out.z_vapor = zv.data();
+        out.counters = counters.data();
+        if (cells > 0) check(mpmc_gpu_flash_solve(handle_, static_cast<int64_t>(cells), p.data(), t.data(), z.data(), &out));
+
+        std::vector<PtFlashBackendResult> results(cells);
+        for (std::size_t c = 0; c < cells; ++c) {
+            if (status[c] == MPMC_FLASH_INVALID_REQUEST)
+                throw std::invalid_argument("GPU PR76 backend: request " + std::to_string(c) +
+                                            " is outside the flash domain (p, T, feed)");
+            auto column = [&](const std::vector<double>& a) {
+                std::vector<double> v(n_);
+                for (std::size_t i = 0; i < n_; ++i) v[i] = a[i * cells + c];
+                return v;
+            };
+            PtFlashBackendResult& r = results[c];
+            r.capability = capability_;
+            r.provider_result_convention = std::string(gpu_pr76_pt_result_convention);
+            PtPhaseSetResult& s = r.solution;
+            s.capability.maximum_phase_count = 2U;
+            s.pressure_pa = requests[c].pressure_pa;
+            s.temperature_k = requests[c].temperature_k;
+            s.feed = requests[c].feed;
+            auto phase = [&](double fraction, std::vector<double> comp, std::vector<double> lnphi, double zf) {
+                PtCandidatePhase ph;
+                ph.mole_phase_fraction = fraction;
+                ph.composition = std::move(comp);
+                ph.activity.ln_phi = std::move(lnphi);
+                ph.activity.smooth = true;  // accepted roots are smooth by construction
+                ph.compressibility_factor = zf;
+                return ph;
+            };
+            switch (status[c]) {
+            case MPMC_FLASH_SINGLE_PHASE: {
+                PtCandidatePhaseSet set;
+                set.phases.push_back(phase(1.0, column(x), column(phil), zl[c]));
+                s.candidate_phase_set = std::move(set);
+                s.status = PtPhaseSetStatus::accepted;
+                break;
+            }
+            case MPMC_FLASH_TWO_PHASE:
+            case MPMC_FLASH_PHASE_SET_UNSTABLE: {
+                PtCandidatePhaseSet set;
+                set.phases.push_back(phase(1.0 - beta[c], column(x), column(phil), zl[c]));
+                set.phases.push_back(phase(beta[c], column(y), column(phiv), zv[c]));
+                s.candidate_phase_set = std::move(set);
+                s.status = status[c] == MPMC_FLASH_TWO_PHASE ? PtPhaseSetStatus::accepted
+                                                             : PtPhaseSetStatus::phase_set_unstable;
+                if (status[c] == MPMC_FLASH_PHASE_SET_UNSTABLE)
+                    s.diagnostic = "final phase-set review found a negative tangent-plane distance";
+                break;
+            }
+            default:
+                s.status = PtPhaseSetStatus::indeterminate;
+                s.diagnostic = "GB300 flash: no accepted phase set within the reference's iteration budgets";
+                break;
+            }
+        }
+        return results;
+    }
+
+private:
+    static void check(int rc) {
+        if (rc == MPMC_OK) return;
+        const std::string what = mpmc_gpu_flash_last_error();
+        if (rc == MPMC_ERR_DOMAIN) throw std::domain_error(what);
+        if (rc == MPMC_ERR_INVALID_ARGUMENT || rc == MPMC_ERR_UNSUPPORTED) throw std::invalid_argument(what);
+        throw std::runtime_error(what);
+    }
+
+    std::size_t n_;
+    mpmc_gpu_flash* handle_ = nullptr;
+    PtFlashBackendCapability capability_;
+};
+
+}  // namespace mpmc::flash
