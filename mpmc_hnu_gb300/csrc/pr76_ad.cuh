@@ -127,9 +127,11 @@ __device__ __forceinline__ Dual<K> log1p_over_x(const Dual<K>& u) {
 // Columns [first, first + K) of d[Z, ln phi]/d[p, T, x_0..x_{n-1}] at a fixed
 // root index; `jac` is row-major (n+1) x (n+2).  Returns false if the root set
 // no longer resolves or the selected root is not derivative-valid.
+// The primal of every chunk is the same, so the root set is solved by the
+// first chunk and reused (`have_roots`).
 template <int NM, int K>
 __device__ bool phase_jacobian_chunk(const Mixture& m, int n, double p, double t, const double* x, int branch,
-                                     int first, double* jac) {
+                                     int first, double* jac, fp64::RootSet& rs, bool have_roots) {
     const int cols = n + 2;
     auto seed = [&](int col, double v) {
         Dual<K> r = cst<K>(v);
@@ -167,9 +169,10 @@ __device__ bool phase_jacobian_chunk(const Mixture& m, int n, double p, double t
     const Dual<K> prt = P / rt;
     const Dual<K> A = (attraction / rt) * prt;
     const Dual<K> B = covolume * prt;
-    fp64::RootSet rs;
-    int dummy = 0;
-    fp64::solve_roots(A.v, B.v, rs, dummy);
+    if (!have_roots) {
+        int dummy = 0;
+        fp64::solve_roots(A.v, B.v, rs, dummy);
+    }
     if (rs.status != fp64::kRootSuccess || branch >= rs.count || !rs.r[branch].derivative_valid) return false;
     // root IFT, pr76_phase.hpp:214-221
     const double sc = rs.scale;
@@ -215,8 +218,9 @@ template <int NM>
 __device__ bool phase_jacobian(const Mixture& m, int n, double p, double t, const double* x, int branch,
                                double* jac) {
     constexpr int K = 4;
+    fp64::RootSet rs;
     for (int first = 0; first < n + 2; first += K)
-        if (!phase_jacobian_chunk<NM, K>(m, n, p, t, x, branch, first, jac)) return false;
+        if (!phase_jacobian_chunk<NM, K>(m, n, p, t, x, branch, first, jac, rs, first > 0)) return false;
     for (int k = 0; k < (n + 1) * (n + 2); ++k)
         if (!isfinite(jac[k])) return false;
     return true;

@@ -11,79 +11,80 @@
 namespace pr76 {
 
 template <int NM>
+__device__ void nan_fill(int n, int64_t ncell, int64_t cell, const DeviceOutputs& out) {
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    const int q = n + 1;
+    auto put = [&](double* a, int k) {
+        if (a) a[static_cast<int64_t>(k) * ncell + cell] = nan;
+    };
+    for (int k = 0; k < n * q; ++k) {
+        put(out.dlnk, k);
+        put(out.dx, k);
+        put(out.dy, k);
+    }
+    for (int k = 0; k < q; ++k) {
+        put(out.dbeta, k);
+        put(out.dzl, k);
+        put(out.dzv, k);
+        put(out.drhol, k);
+        put(out.drhov, k);
+    }
+    for (int k = 0; k < (n + 1) * (n + 2); ++k) {
+        put(out.jl, k);
+        put(out.jv, k);
+    }
+}
+
+// Every lane walks its own grid-stride sequence of cells, NaN-filling the
+// cells without an accepted pair, and stops at its next two-phase cell; then
+// the warp differentiates those cells together.  A quarter of the cells are
+// two-phase at the bench distribution, so a plain grid-stride loop would keep
+// three lanes of four idle through the FP64 work.
+template <int NM>
 __global__ void __launch_bounds__(64) sensitivity_kernel(const Mixture* __restrict__ mix_g, int64_t ncell,
                                                          const double* __restrict__ p,
                                                          const double* __restrict__ t,
                                                          const double* __restrict__ z, DeviceOutputs out) {
     __shared__ Mixture m;
     stage_mixture(mix_g, m);
+    const int n = m.n;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    const double nan = __longlong_as_double(0x7ff8000000000000LL);
-    for (int64_t cell = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; cell < ncell; cell += stride) {
-        const int n = m.n;
-        const int q = n + 1;
-        auto put = [&](double* a, int k, double v) {
-            if (a) a[static_cast<int64_t>(k) * ncell + cell] = v;
-        };
-        // NaN-fill first; a successful cell overwrites everything
-        for (int k = 0; k < n * q; ++k) {
-            put(out.dlnk, k, nan);
-            put(out.dx, k, nan);
-            put(out.dy, k, nan);
-        }
-        for (int k = 0; k < q; ++k) {
-            put(out.dbeta, k, nan);
-            put(out.dzl, k, nan);
-            put(out.dzv, k, nan);
-            put(out.drhol, k, nan);
-            put(out.drhov, k, nan);
-        }
-        for (int k = 0; k < (n + 1) * (n + 2); ++k) {
-            put(out.jl, k, nan);
-            put(out.jv, k, nan);
-        }
-        int st = ad::sNotAccepted;
-        if (out.status[cell] == kTwoPhase) {
-            fp64::Cell<NM> c;
-            c.n = n;
-            c.newton = false;
-            c.p = p[cell];
-            c.t = t[cell];
-            double feed[NM], x[NM], y[NM], lnk[NM];
-            for (int i = 0; i < n; ++i) {
-                const int64_t k = static_cast<int64_t>(i) * ncell + cell;
-                feed[i] = z[k];
-                x[i] = out.x[k];
-                y[i] = out.y[k];
-                lnk[i] = out.lnk[k];
+    int64_t next = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    for (;;) {
+        int64_t cell = -1;
+        while (next < ncell) {
+            const int64_t c = next;
+            next += stride;
+            if (out.status[c] == kTwoPhase) {
+                cell = c;
+                break;
             }
-            if (fp64::normalise_feed(c, feed) && fp64::temp_setup(m, c)) {
-                ad::SensScratch<NM> s;
-                st = ad::sensitivity_cell<NM>(m, c, x, y, lnk, out.beta[cell], out.z_l[cell], out.z_v[cell], s, out,
-                                              ncell, cell);
-                if (st != ad::sSuccess) {
-                    // a failure after partial writes must not leave stale values
-                    for (int k = 0; k < n * q; ++k) {
-                        put(out.dlnk, k, nan);
-                        put(out.dx, k, nan);
-                        put(out.dy, k, nan);
-                    }
-                    for (int k = 0; k < q; ++k) {
-                        put(out.dbeta, k, nan);
-                        put(out.dzl, k, nan);
-                        put(out.dzv, k, nan);
-                        put(out.drhol, k, nan);
-                        put(out.drhov, k, nan);
-                    }
-                    for (int k = 0; k < (n + 1) * (n + 2); ++k) {
-                        put(out.jl, k, nan);
-                        put(out.jv, k, nan);
-                    }
-                }
-            } else {
-                st = ad::sArithmetic;
-            }
+            nan_fill<NM>(n, ncell, c, out);
+            if (out.sens_status) out.sens_status[c] = ad::sNotAccepted;
         }
+        if (__all_sync(0xffffffffu, cell < 0)) break;
+        if (cell < 0) continue;
+        fp64::Cell<NM> c;
+        c.n = n;
+        c.newton = false;
+        c.p = p[cell];
+        c.t = t[cell];
+        double feed[NM], x[NM], y[NM], lnk[NM];
+        for (int i = 0; i < n; ++i) {
+            const int64_t k = static_cast<int64_t>(i) * ncell + cell;
+            feed[i] = z[k];
+            x[i] = out.x[k];
+            y[i] = out.y[k];
+            lnk[i] = out.lnk[k];
+        }
+        int st = ad::sArithmetic;
+        if (fp64::normalise_feed(c, feed) && fp64::temp_setup(m, c)) {
+            ad::SensScratch<NM> s;
+            st = ad::sensitivity_cell<NM>(m, c, x, y, lnk, out.beta[cell], out.z_l[cell], out.z_v[cell], s, out,
+                                          ncell, cell);
+        }
+        // a failure (possibly after partial writes) leaves no stale values
+        if (st != ad::sSuccess) nan_fill<NM>(n, ncell, cell, out);
         if (out.sens_status) out.sens_status[cell] = st;
     }
 }
@@ -98,7 +99,7 @@ cudaError_t MPMC_CAT(launch_sensitivity_nm, MPMC_NM)(const Mixture* d_mix, int64
     int device = 0, sms = 0;
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    const int block = 64;
+    const int block = 64;  // a multiple of the warp: every lane reaches the warp vote
     int64_t grid = static_cast<int64_t>(sms) * 4;
     const int64_t needed = (ncell + block - 1) / block;
     if (grid > needed) grid = needed;
