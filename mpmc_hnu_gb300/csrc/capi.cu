@@ -213,7 +213,8 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
                      {"MPMC_SPLIT_BLOCKS_PER_SM", &shape.split_blocks_per_sm},
                      {"MPMC_T64_BLOCKS_PER_SM", &shape.t64_blocks_per_sm},
                      {"MPMC_S64_BLOCKS_PER_SM", &shape.s64_blocks_per_sm},
-                     {"MPMC_CELL_BLOCKS_PER_SM", &shape.cell_blocks_per_sm}};
+                     {"MPMC_CELL_BLOCKS_PER_SM", &shape.cell_blocks_per_sm},
+                     {"MPMC_ITEM_FORM", &shape.item_form}};
         for (const auto& k : knobs)
             if (const char* v = std::getenv(k.name)) *k.field = std::atoi(v);
         e = pr76::launch_batched(h->n, h->d_mixture, ncell, p, t, z, d, h->workspace.ptr, h->workspace.bytes, shape,

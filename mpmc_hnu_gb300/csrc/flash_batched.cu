@@ -5,6 +5,7 @@
 // captured into a CUDA graph by the caller.
 #include "launch.h"
 #include "pr76_batched64.cuh"
+#include "pr76_warp64.cuh"
 
 #ifndef MPMC_NM
 #error "compile with -DMPMC_NM=<capacity>"
@@ -123,7 +124,8 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     mark();
     classify_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, 0);
     mark();
-    trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+    if (shape.item_form & 1) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+    else w64::trials64w_kernel<NM><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
     mark();
     decide_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
     mark();
@@ -131,7 +133,8 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     mark();
     polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
     mark();
-    split64_kernel<NM><<<sms * s64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+    if (shape.item_form & 4) split64_kernel<NM><<<sms * s64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+    else w64::split64w_kernel<NM><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t);
     mark();
     select64_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
     mark();
@@ -142,7 +145,8 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     mark();
     classify_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, 1);
     mark();
-    trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+    if (shape.item_form & 2) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+    else w64::trials64w_kernel<NM><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
     mark();
     finish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
     mark();

@@ -52,6 +52,8 @@ struct BatchedShape {
     int s64_blocks_per_sm;    // FP64 attempt items (64 threads per block)
     int cell_blocks_per_sm;   // per-cell FP64 kernels (polish, decide, ...; 64 threads per block)
     cudaEvent_t* events;  // optional: kBatchedStages + 1 events recorded around the stages
+    int item_form;        // FP64 item kernels: bit 0 feed trials, bit 1 review trials, bit 2 attempts
+                          // run one item per lane when set, one item per warp when clear
 };
 constexpr int kBatchedStages = 15;
 
