@@ -35,6 +35,9 @@ import time
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+# the flash server overlaps batches on up to 16 streams: give the device as
+# many hardware work queues (read when the CUDA context is created)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 sys.path.insert(0, ROOT)
 
 MIXTURE_SEED = 1001
@@ -213,6 +216,160 @@ def cpu_flash_rate(mix, p, t, z, threads: int, sens: bool):
 
 
 # ---------------------------------------------------------------------------
+# ---------------------------------------------------------------------------
+# serving (continuous batching through the flash server)
+SERVING_MIXTURES = [(3, 501), (3, 502), (6, 503), (6, 504), (10, 505), (10, 506), (20, 507), (20, 508)]
+
+
+def serving_pool(synth, count: int, seed: int = 77):
+    """Seeded requests: mixture among 8 (N in {3, 6, 10, 20}), cells per request
+    floor(exp(U ln 65536)), cells from the base distributions; half re-query
+    the previous request's mixture with p * exp(N(0, 0.02)), T + N(0, 1 K)."""
+    rng = np.random.default_rng(seed)
+    pool = []
+    for k in range(count):
+        ncell = max(1, int(np.exp(rng.uniform(0.0, np.log(65536.0)))))
+        if pool and rng.uniform() < 0.5:
+            j, p0, t0, z0 = pool[-1]
+            n = SERVING_MIXTURES[j][0]
+            src = rng.integers(0, p0.shape[0], ncell)
+            p = p0[src] * np.exp(rng.normal(0.0, 0.02, ncell))
+            t = t0[src] + rng.normal(0.0, 1.0, ncell)
+            z = np.ascontiguousarray(z0[:, src])
+        else:
+            j = int(rng.integers(0, len(SERVING_MIXTURES)))
+            n = SERVING_MIXTURES[j][0]
+            p, t, z = synth.make_cells(n, ncell, 9000 + k)
+        pool.append((j, np.ascontiguousarray(p), np.ascontiguousarray(t), z))
+    return pool
+
+
+def serving_closed(server, ids, pool, outstanding, seconds):
+    """Closed loop: keep `outstanding` requests queued for `seconds`, then drain.
+    Its throughput is the server's saturated rate at that queue depth."""
+    done = []
+    queue = []
+    k = 0
+    t0 = time.perf_counter()
+
+    def submit():
+        nonlocal k
+        j, p, t, z = pool[k % len(pool)]
+        k += 1
+        queue.append((server.submit(ids[j], p, t, z, fields=["status", "vapor_fraction"]), p.shape[0]))
+
+    for _ in range(outstanding):
+        submit()
+    while queue:
+        tk, ncell = queue.pop(0)
+        _, lat = server.wait(tk)
+        done.append((ncell, lat))
+        if time.perf_counter() - t0 < seconds:
+            submit()
+    return done, time.perf_counter() - t0
+
+
+def serving_run(server, ids, pool, rate, seconds):
+    """Open-loop Poisson arrivals at `rate` requests/s for `seconds` (rate None:
+    submit the whole pool at once, i.e. saturation).  Returns per-request
+    (cells, latency s) and the wall time to drain."""
+    rng = np.random.default_rng(4242)
+    done = []
+    tickets = []
+    lock = threading.Lock()
+    finished = threading.Event()
+
+    def waiter():
+        k = 0
+        while True:
+            with lock:
+                if k < len(tickets):
+                    tk, ncell = tickets[k]
+                else:
+                    tk = None
+            if tk is None:
+                if finished.is_set():
+                    with lock:
+                        if k >= len(tickets):
+                            return
+                    continue
+                time.sleep(0.0002)
+                continue
+            _, lat = server.wait(tk)
+            done.append((ncell, lat))
+            k += 1
+
+    th = threading.Thread(target=waiter)
+    th.start()
+    t0 = time.perf_counter()
+    k = 0
+    if rate is None:
+        for j, p, t, z in pool:
+            tk = server.submit(ids[j], p, t, z, fields=["status", "vapor_fraction"])
+            with lock:
+                tickets.append((tk, p.shape[0]))
+    else:
+        next_t = t0
+        while True:
+            next_t += rng.exponential(1.0 / rate)
+            if next_t - t0 > seconds:
+                break
+            delay = next_t - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            j, p, t, z = pool[k % len(pool)]
+            k += 1
+            tk = server.submit(ids[j], p, t, z, fields=["status", "vapor_fraction"])
+            with lock:
+                tickets.append((tk, p.shape[0]))
+    finished.set()
+    th.join()
+    return done, time.perf_counter() - t0
+
+
+def serving_summary(done, wall, offered=None):
+    cells = np.array([c for c, _ in done], dtype=np.float64)
+    lat = np.array([l for _, l in done]) * 1e3
+    small = cells <= 4096
+    out = {"requests": int(len(done)), "flashes_per_s": float(cells.sum() / wall),
+           "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}
+    if small.any():
+        out["p50_ms_le4096"] = float(np.percentile(lat[small], 50))
+        out["p99_ms_le4096"] = float(np.percentile(lat[small], 99))
+    if offered is not None:
+        out["offered_req_per_s"] = float(offered)
+    return out
+
+
+def serving_probe(flash, synth, device, seconds, fractions, log):
+    """Saturated throughput, then open-loop Poisson load at each fraction of it."""
+    slots = 16
+    server = flash.FlashServer(device=device, slots=slots, max_batch_cells=65536, memory_budget_bytes=40 << 30)
+    ids = [server.add_mixture(synth.make_mixture(n, s)) for n, s in SERVING_MIXTURES]
+    pool = serving_pool(synth, 256)
+    serving_run(server, ids, pool[:16], None, 0)  # warm-up
+    done, wall = serving_closed(server, ids, pool, 2 * slots, seconds)
+    sat = serving_summary(done, wall)
+    sat_req = len(done) / wall
+    log(f"serving: saturated {sat['flashes_per_s']:.0f} flashes/s, {sat_req:.1f} requests/s "
+        f"({2 * slots} requests outstanding)")
+    rates = []
+    for f in fractions:
+        d, w = serving_run(server, ids, pool, f * sat_req, seconds)
+        r = serving_summary(d, w, f * sat_req)
+        r["fraction_of_saturation"] = f
+        rates.append(r)
+        log(f"serving at {f:.0%}: {r}")
+    st = server.stats()
+    server.close()
+    return {"saturated_flashes_per_s": sat["flashes_per_s"], "saturated_req_per_s": sat_req,
+            "saturation": f"closed loop, {2 * slots} requests outstanding", "saturated_latency": sat,
+            "rates": rates, "slots": st.get("slots"), "max_batch_cells": 65536,
+            "workload": "8 seeded mixtures (N 3, 6, 10, 20), cells/request log-uniform 1-65536, "
+                        "half re-query the previous mixture with perturbed p, T; open-loop Poisson arrivals",
+            "seconds_per_rate": seconds}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -227,6 +384,10 @@ def main() -> None:
     ap.add_argument("--plain-sample", type=int, default=32768)
     ap.add_argument("--cpu-sample", type=int, default=65536)
     ap.add_argument("--profile", action="store_true", help="one untimed solve of the workload (for ncu)")
+    ap.add_argument("--serving-seconds", type=float, default=8.0,
+                    help="open-loop serving probe at 70%% of saturation (0 = skip)")
+    ap.add_argument("--serving-sweep", action="store_true",
+                    help="only the serving sweep: 10%%..100%% of saturation, --serving-seconds per rate")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -283,6 +444,15 @@ def main() -> None:
         torch.cuda.set_device(local_rank)
     device = torch.cuda.current_device()
     torch.zeros(1, device="cuda")
+
+    if args.serving_sweep:
+        if rank == 0:
+            sv = serving_probe(flash, synth, device, args.serving_seconds or 60.0,
+                               [0.1, 0.3, 0.5, 0.7, 0.9, 1.0], log)
+            print(json.dumps({"metric": "serving p50/p99 latency and flashes/s per arrival rate",
+                              "unit": "ms", "n_gpus": 1, "data": "synthetic (seeded generator)",
+                              "serving": sv}), flush=True)
+        return
 
     mix, p, t, z, placed = make_workload(args.n, args.cells, args.near_fraction, rank, torch, flash, synth, log)
     n, ncell = args.n, args.cells
@@ -430,6 +600,11 @@ def main() -> None:
                "sample": f"{sel.size} stratified cells (every {ncell // sel.size}th) of this workload, flash"
                          f"{' + AD' if sens else ''}, {secs:.1f} s wall on {threads} threads"}
 
+    serving = None
+    if rank == 0 and args.serving_seconds > 0:
+        g.close()
+        serving = serving_probe(flash, synth, device, args.serving_seconds, [0.7], log)
+
     if rank == 0:
         line = {"metric": METRIC, "value": value,
                 "unit": "flashes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -441,7 +616,7 @@ def main() -> None:
                 "phase_counts": {"single": int((status == 0).sum()), "two": int((status == 1).sum()),
                                  "unstable": int((status == 2).sum()), "indeterminate": int((status == 3).sum()),
                                  "invalid": int((status == -1).sum())},
-                "clocks": clk.summary()}
+                "clocks": clk.summary(), "serving": serving}
         print(json.dumps(line), flush=True)
     g.close()
     if world > 1:

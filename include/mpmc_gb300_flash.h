@@ -234,6 +234,64 @@ const char* mpmc_gpu_flash_last_error(void);
 /* ABI version (MPMC_GB300_FLASH_ABI_VERSION). */
 int mpmc_gpu_flash_abi_version(void);
 
+/* ------------------------------------------------------------------------
+ * Flash server: the PT service path as a device-resident request loop
+ * (replaces the per-request PtService::solve -> PtFlashBackend::solve calls,
+ * pt_service.hpp:335-369, for many concurrent clients).
+ *
+ * Requests (one mixture, any cell count up to max_batch_cells) are queued by
+ * mpmc_flash_server_submit from any thread and return a ticket at once.  A
+ * worker thread keeps `slots` device batches in flight, each on its own CUDA
+ * stream with its own device buffers: whenever a slot is free it takes the
+ * oldest waiting request and every other waiting request of the same mixture
+ * that still fits, copies them in, launches the flash and copies the results
+ * out, so requests that arrive while others run are admitted as slots free up
+ * and their work overlaps on the device (continuous batching).  Each mixture's
+ * prepared constants stay on the device from add_mixture to destroy.  Slots
+ * are admitted by memory: the server holds at most memory_budget_bytes of
+ * device memory and creates only as many slots as fit.  Results are per cell
+ * and independent of what else is in the batch: a request's outputs are the
+ * same alone and in any mix.  Flash fields only (status .. counters); the
+ * sensitivity fields of `out` must be NULL.  The reference has no ln K warm
+ * start (its hints are TPD start compositions), so none is applied: results
+ * equal those of mpmc_gpu_flash_solve. */
+typedef struct mpmc_server_options {
+    int32_t device;
+    int32_t slots;                /* batches in flight; 0 = 4 */
+    int64_t max_batch_cells;      /* cells per device batch (and per request); 0 = 65536 */
+    int64_t memory_budget_bytes;  /* device memory the server may hold; 0 = 40 GiB */
+    int32_t form;                 /* MPMC_FORM_MIXED or MPMC_FORM_PLAIN_FP64 (= 0): set it explicitly */
+    int32_t flags;                /* reserved, 0 */
+} mpmc_server_options;
+
+typedef struct mpmc_flash_server mpmc_flash_server;
+
+int mpmc_flash_server_create(const mpmc_server_options* options, mpmc_flash_server** out);
+
+/* Register a mixture (validated like mpmc_gpu_flash_create); its id is used
+ * by submit.  Up to 64 mixtures per server. */
+int mpmc_flash_server_add_mixture(mpmc_flash_server* server, const mpmc_pr76_mixture* mixture,
+                                  int32_t* mixture_id);
+
+/* Queue one request.  p, t, z and the output buffers are host memory owned by
+ * the caller and must stay valid until mpmc_flash_server_wait returns for the
+ * ticket; layouts as in mpmc_gpu_flash_solve for n_cells cells. */
+int mpmc_flash_server_submit(mpmc_flash_server* server, int32_t mixture_id, int64_t n_cells, const double* p,
+                             const double* t, const double* z, const mpmc_flash_outputs* out, uint64_t* ticket);
+
+/* Wait for a ticket (timeout_us < 0: no limit).  On return 0 the outputs are
+ * written and *latency_s (optional) is the time from submit to completion.
+ * MPMC_ERR_TIMEOUT if the time ran out; the request stays queued. */
+int mpmc_flash_server_wait(mpmc_flash_server* server, uint64_t ticket, int64_t timeout_us, double* latency_s);
+
+/* Counters: [0] submitted, [1] completed, [2] device batches, [3] cells,
+ * [4] slots, [5] device bytes per slot, [6] most requests in one batch,
+ * [7] most slots busy at once.  Returns the number written. */
+int mpmc_flash_server_stats(mpmc_flash_server* server, int64_t* out, int capacity);
+
+/* Finish the queued requests, stop the worker and free everything. */
+int mpmc_flash_server_destroy(mpmc_flash_server* server);
+
 #ifdef __cplusplus
 }
 #endif

@@ -27,7 +27,7 @@ CAPACITIES = (4, 8, 12, 16, 20)
 # translation units compiled once per capacity
 PER_CAPACITY = ("flash_plain.cu", "sensitivity.cu", "flash_batched.cu")
 # translation units compiled once
-SINGLE = ("capi.cu", "peak_probe.cu")
+SINGLE = ("capi.cu", "server.cu", "peak_probe.cu")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -77,7 +77,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     flash_objs = [o for o in objs if o != probe_obj]
     for lib, parts in ((LIB, flash_objs), (PROBE_LIB, [probe_obj])):
         if not os.path.exists(lib) or any(os.path.getmtime(o) > os.path.getmtime(lib) for o in parts):
-            cmd = [_nvcc()] + ARCH + ["-shared", "-o", lib] + parts
+            cmd = [_nvcc()] + ARCH + ["-shared", "-o", lib] + parts + ["-lpthread"]
             if verbose:
                 print(" ".join(cmd), flush=True)
             subprocess.check_call(cmd)

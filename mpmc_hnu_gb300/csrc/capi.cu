@@ -262,6 +262,12 @@ int noalloc_scratch(int device, void** out) {
 }  // namespace
 
 namespace pr76 {
+namespace host {
+int fail(int code, const std::string& what) { return ::fail(code, what); }
+int cuda_fail(cudaError_t e, const char* where) { return ::cuda_fail(e, where); }
+int prepare_mixture(const mpmc_pr76_mixture* mix, Mixture& m) { return ::prepare_mixture(mix, m); }
+}  // namespace host
+
 LaunchShape plain_launch_shape() {
     LaunchShape s{64, 2};
     if (const char* v = std::getenv("MPMC_PLAIN_BLOCK")) s.block = std::atoi(v);

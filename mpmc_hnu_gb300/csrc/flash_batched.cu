@@ -125,16 +125,17 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     classify_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, 0);
     mark();
     if (shape.item_form & 1) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
-    else w64::trials64w_kernel<NM><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
+    else w64::trials64w_kernel<NM, 32><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
     mark();
     decide_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
     mark();
     split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t);
     mark();
-    polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+    if (shape.item_form & 8) polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+    else w64::polishw_kernel<NM, w64::kSeg<NM>><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t, out);
     mark();
     if (shape.item_form & 4) split64_kernel<NM><<<sms * s64_res, 64, 0, stream>>>(d_mix, ws, p, t);
-    else w64::split64w_kernel<NM><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t);
+    else w64::split64w_kernel<NM, 32><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t);
     mark();
     select64_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
     mark();
@@ -146,7 +147,7 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     classify_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, 1);
     mark();
     if (shape.item_form & 2) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
-    else w64::trials64w_kernel<NM><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
+    else w64::trials64w_kernel<NM, 32><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
     mark();
     finish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
     mark();

@@ -5,6 +5,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
+#include "../../include/mpmc_gb300_flash.h"
 #include "pr76_common.cuh"
 
 namespace pr76 {
@@ -52,8 +55,8 @@ struct BatchedShape {
     int s64_blocks_per_sm;    // FP64 attempt items (64 threads per block)
     int cell_blocks_per_sm;   // per-cell FP64 kernels (polish, decide, ...; 64 threads per block)
     cudaEvent_t* events;  // optional: kBatchedStages + 1 events recorded around the stages
-    int item_form;        // FP64 item kernels: bit 0 feed trials, bit 1 review trials, bit 2 attempts
-                          // run one item per lane when set, one item per warp when clear
+    int item_form;        // FP64 item kernels: bit 0 feed trials, bit 1 review trials, bit 2 attempts,
+                          // bit 3 polish run one item per lane when set, one item per warp when clear
 };
 constexpr int kBatchedStages = 15;
 
@@ -91,5 +94,13 @@ MPMC_DECLARE_PLAIN(12)
 MPMC_DECLARE_PLAIN(16)
 MPMC_DECLARE_PLAIN(20)
 #undef MPMC_DECLARE_PLAIN
+
+// Helpers of the C ABI shared with the flash server (capi.cu): the error
+// message setters and the mixture preparation of mpmc_gpu_flash_create.
+namespace host {
+int fail(int code, const std::string& what);
+int cuda_fail(cudaError_t e, const char* where);
+int prepare_mixture(const mpmc_pr76_mixture* mix, Mixture& m);
+}  // namespace host
 
 }  // namespace pr76

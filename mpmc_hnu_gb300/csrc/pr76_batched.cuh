@@ -67,6 +67,7 @@ enum Slot : int {
     qS64Cells = 23,        // cells listed for the FP64 attempt selection
     sSlowSkipped = 24,     // slow trials whose outcome could not change the cell's status
     sLimitAttempts = 25,   // attempts classified as ending at the iteration limit
+    qPolishCursor = 26,    // warp queue over the polish list
     qSlots = 32
 };
 

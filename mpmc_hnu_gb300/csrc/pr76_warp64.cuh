@@ -1,11 +1,13 @@
-// Warp-cooperative FP64 work items of the mixed-precision flash.
+// Lane-group-cooperative FP64 work items of the mixed-precision flash.
 //
-// One warp runs one item (a TPD trial or a ln K split attempt) to its end,
-// with component i of the mixture on lane i: mixing row sums, ln phi, the TPD
-// terms, the Rachford-Rice terms and the ln K update are lane-parallel, the
-// sums and maxima are warp reductions, and the cubic is solved with one lane
-// per monotone interval.  Control flow is uniform across the warp (every
-// branch depends on reduced, warp-wide values), so no lane diverges.
+// A group of S lanes (S = the component capacity rounded up to a power of two:
+// 4, 8, 16 or 32, so a warp holds 32 / S groups) runs one item (a TPD trial, a
+// ln K split attempt or a cell's Newton polish) to its end, with component i of
+// the mixture on lane i of the group: mixing row sums, ln phi, the TPD terms,
+// the Rachford-Rice terms and the ln K update are lane-parallel, the sums and
+// maxima are group reductions, and the cubic is solved with one lane per
+// monotone interval.  Control flow is uniform within a group (every branch
+// depends on reduced, group-wide values); groups of one warp are independent.
 //
 // Why: a GB300 sub-partition retires an FP64 warp instruction in ~64 cycles
 // whatever its active-lane count.  The lane-per-item form keeps 1-5 lanes of
@@ -31,22 +33,51 @@
 namespace pr76 {
 namespace w64 {
 
-constexpr unsigned kFull = 0xffffffffu;
+// Lanes per item of the throughput-bound polish: the component capacity rounded
+// up to a power of two, so a warp runs 32 / S cells side by side (8 at four
+// components, 2 at ten, 1 at twenty).  The tail-latency-bound trial and attempt
+// items run one per warp (S = 32): items sharing a warp would share its issue.
+template <int NM>
+constexpr int kSeg = NM <= 4 ? 4 : (NM <= 8 ? 8 : (NM <= 16 ? 16 : 32));
 
+// first lane of this thread's item within the warp
+template <int S>
+__device__ __forceinline__ int seg_base() { return (threadIdx.x & 31) & ~(S - 1); }
+template <int S>
+__device__ __forceinline__ unsigned seg_mask() {
+    if constexpr (S == 32) return 0xffffffffu;
+    else return ((1u << S) - 1u) << seg_base<S>();
+}
+template <int S>
+__device__ __forceinline__ int seg_lane() { return threadIdx.x & (S - 1); }
+template <int S>
 __device__ __forceinline__ double wsum(double v) {
+    const unsigned m = seg_mask<S>();
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    for (int o = S / 2; o > 0; o >>= 1) v += __shfl_xor_sync(m, v, o, S);
     return v;
 }
+template <int S>
 __device__ __forceinline__ double wmax(double v) {
+    const unsigned m = seg_mask<S>();
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(kFull, v, o));
+    for (int o = S / 2; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(m, v, o, S));
     return v;
 }
-__device__ __forceinline__ bool wany(bool p) { return __any_sync(kFull, p); }
+template <int S>
+__device__ __forceinline__ bool wany(bool p) { return __any_sync(seg_mask<S>(), p); }
+template <int S, typename T>
+__device__ __forceinline__ T bcast(T v, int src) { return __shfl_sync(seg_mask<S>(), v, src, S); }
+// ballot of the item's lanes, bit i = lane i of the item
+template <int S>
+__device__ __forceinline__ unsigned seg_ballot(bool p) {
+    const unsigned b = __ballot_sync(seg_mask<S>(), p);
+    if constexpr (S == 32) return b;
+    else return (b >> seg_base<S>()) & ((1u << S) - 1u);
+}
 
 // Per-lane view of one cell: lane i holds component i (lanes >= n hold zeros).
-template <int NM>
+template <int NM, int S>
 struct WCell {
     int n, lane;
     bool comp;     // lane < n
@@ -59,10 +90,10 @@ struct WCell {
 
 // Feed, a_i(T) and the a_ij row of one cell (pr76_pure.hpp:146-165,
 // pr76_mixture.hpp:172-188).  False if the temperature terms are unusable.
-template <int NM>
+template <int NM, int S>
 __device__ bool load_cell(const Mixture& m, const batched::Workspace& ws, int64_t c, const double* p,
-                          const double* t, WCell<NM>& w) {
-    const int lane = threadIdx.x & 31;
+                          const double* t, WCell<NM, S>& w) {
+    const int lane = seg_lane<S>();
     w.n = m.n;
     w.lane = lane;
     w.comp = lane < m.n;
@@ -82,10 +113,10 @@ __device__ bool load_cell(const Mixture& m, const batched::Workspace& ws, int64_
         bad = !isfinite(a) || (a == 0.0 && bracket != 0.0) || (m.n > 1 && !(a > 0.0));
         root = sqrt(a);
     }
-    if (wany(bad)) return false;
+    if (wany<S>(bad)) return false;
 #pragma unroll
     for (int j = 0; j < NM; ++j) {
-        const double rj = __shfl_sync(kFull, root, j & 31);
+        const double rj = bcast<S>(root, j);
         w.aij[j] = (w.comp && j < m.n) ? (j == lane ? a : (root * m.factor[lane * m.n + j]) * rj) : 0.0;
     }
     return true;
@@ -93,27 +124,28 @@ __device__ bool load_cell(const Mixture& m, const batched::Workspace& ws, int64_
 
 // Mixing with row sums (pr76_mixture.hpp:170-218): s_i on each lane, a and b
 // warp-uniform.
-template <int NM>
-__device__ bool mix(const WCell<NM>& c, double x, double& s, double& amix, double& bmix) {
+template <int NM, int S>
+__device__ bool mix(const WCell<NM, S>& c, double x, double& s, double& amix, double& bmix) {
     double acc = 0.0;
 #pragma unroll
     for (int j = 0; j < NM; ++j) {
-        const double xj = __shfl_sync(kFull, x, j & 31);
+        const double xj = bcast<S>(x, j);
         if (j < c.n) acc = fma(xj, c.aij[j], acc);
     }
     s = c.comp ? acc : 0.0;
-    amix = wsum(c.comp ? x * s : 0.0);
-    bmix = wsum(c.comp ? x * c.b : 0.0);
-    return isfinite(amix) && isfinite(bmix) && bmix > 0.0 && !wany(!isfinite(s));
+    amix = wsum<S>(c.comp ? x * s : 0.0);
+    bmix = wsum<S>(c.comp ? x * c.b : 0.0);
+    return isfinite(amix) && isfinite(bmix) && bmix > 0.0 && !wany<S>(!isfinite(s));
 }
 
 // Cubic roots (pr76_roots.hpp:77-173) with one lane per monotone interval:
 // the bracketed Newton iteration of the reference's stopping width on each
 // interval runs concurrently, then the roots are checked and ordered exactly
 // as in the sequential solver.
+template <int S>
 __device__ inline void roots_by_interval(double a, double b, fp64::RootSet& rs, int& iterations) {
     using fp64::Cubic;
-    const int lane = threadIdx.x & 31;
+    const int lane = seg_lane<S>();
     rs.count = 0;
     rs.status = fp64::kRootUnrepresentable;
     rs.scale = 1.0;
@@ -227,13 +259,13 @@ __device__ inline void roots_by_interval(double a, double b, fp64::RootSet& rs, 
     }
     // sequential assembly in interval order
     for (int k = 0; k < intervals; ++k) {
-        const int st = __shfl_sync(kFull, state, k);
-        const int itk = __shfl_sync(kFull, it, k);
-        const double zk = __shfl_sync(kFull, z, k);
-        const double xk = __shfl_sync(kFull, xv, k);
-        const bool okk = __shfl_sync(kFull, ok_root ? 1 : 0, k) != 0;
-        const bool dvk = __shfl_sync(kFull, dvalid ? 1 : 0, k) != 0;
-        const int sk = __shfl_sync(kFull, sign, k);
+        const int st = bcast<S>(state, k);
+        const int itk = bcast<S>(it, k);
+        const double zk = bcast<S>(z, k);
+        const double xk = bcast<S>(xv, k);
+        const bool okk = bcast<S>(ok_root ? 1 : 0, k) != 0;
+        const bool dvk = bcast<S>(dvalid ? 1 : 0, k) != 0;
+        const int sk = bcast<S>(sign, k);
         if (st == 3) {
             rs.count = 0;
             rs.status = fp64::kRootUnrepresentable;
@@ -267,8 +299,8 @@ __device__ inline void roots_by_interval(double a, double b, fp64::RootSet& rs, 
 
 // ln phi_i at a resolved root (pr76_phase.hpp:223-253); true if every lane's
 // value and Z are finite.
-template <int NM>
-__device__ bool ln_phi(const WCell<NM>& c, double s, double amix, double bmix, double A, double B,
+template <int NM, int S>
+__device__ bool ln_phi(const WCell<NM, S>& c, double s, double amix, double bmix, double A, double B,
                        const fp64::Root& root, double& lnphi) {
     const double free_volume = root.free_volume;
     const double z = free_volume + B;
@@ -291,19 +323,19 @@ __device__ bool ln_phi(const WCell<NM>& c, double s, double amix, double bmix, d
         const double coefficient = ((2.0 * s - amix * ratio) / rt) * prt;
         lnphi = ratio * z_minus_one - log_free - coefficient * log_factor;
     }
-    return isfinite(z) && !wany(c.comp && !isfinite(lnphi));
+    return isfinite(z) && !wany<S>(c.comp && !isfinite(lnphi));
 }
 
 // Stability provider (pr76_stability.hpp:36-119): ln phi of the minimum-Gibbs
 // admissible root at x.
-template <int NM>
-__device__ int stability_provider(WCell<NM>& c, double x, double& out, bool& smooth, int counter_row) {
+template <int NM, int S>
+__device__ int stability_provider(WCell<NM, S>& c, double x, double& out, bool& smooth, int counter_row) {
     ++c.counters[counter_row];
     double s, amix, bmix, A, B;
     if (!mix(c, x, s, amix, bmix)) return kRootRange;
     if (!fp64::coefficients(c.p, c.t, amix, bmix, A, B)) return kRootRange;
     fp64::RootSet rs;
-    roots_by_interval(A, B, rs, c.counters[cRootIters]);
+    roots_by_interval<S>(A, B, rs, c.counters[cRootIters]);
     if (rs.status != fp64::kRootSuccess) return fp64::root_issue(rs.status);
     double phi[2] = {0.0, 0.0};
     int cand[2] = {0, 0};
@@ -320,14 +352,14 @@ __device__ int stability_provider(WCell<NM>& c, double x, double& out, bool& smo
     int best = 0;
     smooth = true;
     if (ncand == 2) {
-        const double v = wsum(c.comp ? x * (phi[1] - phi[0]) : 0.0);
+        const double v = wsum<S>(c.comp ? x * (phi[1] - phi[0]) : 0.0);
         if (!isfinite(v)) return kNonfinite;
         if (v < 0.0) best = 1;
         const double po = best == 1 ? phi[0] : phi[1];
         const double pb = best == 1 ? phi[1] : phi[0];
-        const double magnitude = 1.0 + wsum(c.comp ? x * (fabs(po) + fabs(pb)) : 0.0);
+        const double magnitude = 1.0 + wsum<S>(c.comp ? x * (fabs(po) + fabs(pb)) : 0.0);
         if (!isfinite(magnitude)) return kNonfinite;
-        const double d = wsum(c.comp ? x * (po - pb) : 0.0);
+        const double d = wsum<S>(c.comp ? x * (po - pb) : 0.0);
         if (!isfinite(d)) return kNonfinite;
         if (fabs(d) <= 256.0 * kEps * magnitude) smooth = false;
     }
@@ -338,14 +370,14 @@ __device__ int stability_provider(WCell<NM>& c, double x, double& out, bool& smo
 
 // Role provider (pr76_split.hpp:38-84): liquid = smallest, vapor = largest
 // admissible root.
-template <int NM>
-__device__ int role_provider(WCell<NM>& c, double x, bool vapor, double& lnphi, double& z_out, int& branch) {
+template <int NM, int S>
+__device__ int role_provider(WCell<NM, S>& c, double x, bool vapor, double& lnphi, double& z_out, int& branch) {
     ++c.counters[cSplitEvals];
     double s, amix, bmix, A, B;
     if (!mix(c, x, s, amix, bmix)) return kRootRange;
     if (!fp64::coefficients(c.p, c.t, amix, bmix, A, B)) return kRootRange;
     fp64::RootSet rs;
-    roots_by_interval(A, B, rs, c.counters[cRootIters]);
+    roots_by_interval<S>(A, B, rs, c.counters[cRootIters]);
     if (rs.status != fp64::kRootSuccess) return fp64::root_issue(rs.status);
     int selected = -1;
     for (int k = 0; k < rs.count; ++k) {
@@ -370,10 +402,10 @@ struct Tpd {
     bool smooth;
 };
 
-template <int NM>
-__device__ int tpd(const WCell<NM>& c, double phiw, double phiref, Tpd& pt) {
-    if (wany(c.comp && (!isfinite(pt.w) || pt.w < 0.0 || pt.w > 1.0))) return kDomain;
-    const double sum = wsum(c.comp ? pt.w : 0.0);
+template <int NM, int S>
+__device__ int tpd(const WCell<NM, S>& c, double phiw, double phiref, Tpd& pt) {
+    if (wany<S>(c.comp && (!isfinite(pt.w) || pt.w < 0.0 || pt.w > 1.0))) return kDomain;
+    const double sum = wsum<S>(c.comp ? pt.w : 0.0);
     if (!(fabs(sum - 1.0) <= 64.0 * kEps)) return kDomain;
     pt.res = 0.0;
     bool domain = false, boundary = false;
@@ -394,10 +426,10 @@ __device__ int tpd(const WCell<NM>& c, double phiw, double phiref, Tpd& pt) {
             mag = w * (fabs(lw) + fabs(c.lz) + fabs(phiw) + fabs(phiref));
         }
     }
-    if (wany(domain)) return kDomain;
-    const bool any_boundary = wany(boundary);
-    const double value = wsum(wq);
-    const double magnitude = 1.0 + wsum(mag);
+    if (wany<S>(domain)) return kDomain;
+    const bool any_boundary = wany<S>(boundary);
+    const double value = wsum<S>(wq);
+    const double magnitude = 1.0 + wsum<S>(mag);
     const double mean = value / sum;
     double r = 0.0;
     if (c.act) {
@@ -405,7 +437,7 @@ __device__ int tpd(const WCell<NM>& c, double phiw, double phiref, Tpd& pt) {
         r = fabs(pt.res);
     }
     pt.value = value;
-    pt.stat = wmax(r);
+    pt.stat = wmax<S>(r);
     pt.guard = 256.0 * kEps * magnitude;
     if (!isfinite(pt.value) || !isfinite(pt.guard) || (!any_boundary && !isfinite(pt.stat))) return kNonfinite;
     return kOk;
@@ -415,8 +447,8 @@ __device__ __forceinline__ bool tpd_negative(const Tpd& p, double tol) { return 
 
 // A TPD trial from `start` with the reference's descent and stopping rules
 // (pt_stability.hpp:343-457); provider calls are charged to `row`.
-template <int NM>
-__device__ int trial(WCell<NM>& c, double start, double ref, double tol, int row, Tpd& point) {
+template <int NM, int S>
+__device__ int trial(WCell<NM, S>& c, double start, double ref, double tol, int row, Tpd& point) {
     Tpd next;
     next.w = start;
     {
@@ -436,19 +468,19 @@ __device__ int trial(WCell<NM>& c, double start, double ref, double tol, int row
         if (iter >= 512) return fp64::kIterationLimit;
         const double scale = fmax(1.0, point.stat / 4.0);
         const double dir = c.act ? -point.res / scale : 0.0;
-        const double slope = wsum(c.act ? (point.w * point.res) * dir : 0.0);
+        const double slope = wsum<S>(c.act ? (point.w * point.res) * dir : 0.0);
         if (!isfinite(slope) || !(slope < 0.0)) return fp64::kLineSearchFailed;
         double alpha = 1.0;
         bool accepted = false;
         for (int bt = 0; bt < 32; ++bt, alpha *= 0.5) {
             const double cand = c.act ? point.lw + alpha * dir : -INFINITY;
-            const double largest = wmax(cand);
+            const double largest = wmax<S>(cand);
             next.w = c.act ? exp(cand - largest) : 0.0;
-            const double sum = wsum(next.w);
+            const double sum = wsum<S>(next.w);
             bool positive = isfinite(sum) && sum > 0.0;
             next.w /= sum;
             if (!c.act) next.w = 0.0;
-            positive = positive && !wany(c.act && !(next.w > 0.0));
+            positive = positive && !wany<S>(c.act && !(next.w > 0.0));
             if (!positive) continue;
             double phi;
             bool smooth = true;
@@ -486,16 +518,16 @@ struct Split {
 };
 
 // Rachford-Rice by bracketed Newton (rachford_rice.hpp:70-147 checks).
-template <int NM>
-__device__ int rachford_rice(WCell<NM>& c, double lk, Split& s) {
-    const double contrast = wmax(c.act ? fabs(lk) : 0.0);
+template <int NM, int S>
+__device__ int rachford_rice(WCell<NM, S>& c, double lk, Split& s) {
+    const double contrast = wmax<S>(c.act ? fabs(lk) : 0.0);
     if (contrast == 0.0) return fp64::kRrDegenerate;
     double ls[2];
     for (int k = 0; k < 2; ++k) {
         const double sign = k == 0 ? 1.0 : -1.0;
         const double arg = c.act ? c.lz + sign * lk : -INFINITY;
-        const double largest = wmax(arg);
-        const double sum = wsum(c.act ? exp(arg - largest) : 0.0);
+        const double largest = wmax<S>(arg);
+        const double sum = wsum<S>(c.act ? exp(arg - largest) : 0.0);
         ls[k] = largest + log(sum);
     }
     if (!isfinite(ls[0]) || !isfinite(ls[1])) return fp64::kRrUnrepresentable;
@@ -515,8 +547,8 @@ __device__ int rachford_rice(WCell<NM>& c, double lk, Split& s) {
             term = (c.z / den) * num;
             dterm = -term * dd / den;
         }
-        value = wsum(term);
-        const double dv = wsum(dterm);
+        value = wsum<S>(term);
+        const double dv = wsum<S>(dterm);
         if (!isfinite(value)) return fp64::kRrUnrepresentable;
         if (value == 0.0) {
             resolved = true;
@@ -528,7 +560,7 @@ __device__ int rachford_rice(WCell<NM>& c, double lk, Split& s) {
         const double step = fabs(bn - beta);
         beta = bn;
         if (step <= 8.0 * kEps * fmin(beta, 1.0 - beta) || right - left <= 8.0 * kEps * fmin(beta, 1.0 - beta)) {
-            value = wsum(c.act ? (c.z / den_at(beta)) * num : 0.0);
+            value = wsum<S>(c.act ? (c.z / den_at(beta)) * num : 0.0);
             resolved = true;
             break;
         }
@@ -537,7 +569,7 @@ __device__ int rachford_rice(WCell<NM>& c, double lk, Split& s) {
         ++c.counters[cRrIters];
         beta = (left + right) * 0.5;
         if (!(beta > 0.0 && beta < 1.0)) break;
-        value = wsum(c.act ? (c.z / den_at(beta)) * num : 0.0);
+        value = wsum<S>(c.act ? (c.z / den_at(beta)) * num : 0.0);
         if (!isfinite(value)) return fp64::kRrUnrepresentable;
         if (value == 0.0 || beta == left || beta == right || right - left <= 8.0 * kEps * fmin(beta, 1.0 - beta)) {
             resolved = true;
@@ -556,8 +588,8 @@ __device__ int rachford_rice(WCell<NM>& c, double lk, Split& s) {
         s.y = pos ? larger : larger * e;
         bad = !isfinite(larger) || !(s.x > 0.0 && s.y > 0.0);
     }
-    if (wany(bad)) return fp64::kRrUnrepresentable;
-    const double sx = wsum(s.x), sy = wsum(s.y);
+    if (wany<S>(bad)) return fp64::kRrUnrepresentable;
+    const double sx = wsum<S>(s.x), sy = wsum<S>(s.y);
     if (fabs(sx - 1.0) > 64.0 * kEps || fabs(sy - 1.0) > 64.0 * kEps) return fp64::kRrUnrepresentable;
     s.x /= sx;
     s.y /= sy;
@@ -573,16 +605,16 @@ __device__ int rachford_rice(WCell<NM>& c, double lk, Split& s) {
             bad = recovered != 0.0;
         }
     }
-    if (wany(bad)) return fp64::kRrUnrepresentable;
-    s.mass_abs = wmax(err_abs);
-    s.mass_rel = wmax(err_rel);
+    if (wany<S>(bad)) return fp64::kRrUnrepresentable;
+    s.mass_abs = wmax<S>(err_abs);
+    s.mass_rel = wmax<S>(err_rel);
     s.beta = beta;
     return fp64::kRrInterior;
 }
 
 // Split evaluation at ln K (pt_split.hpp:300-341).
-template <int NM>
-__device__ int split_evaluate(WCell<NM>& c, double lk, Split& s, int& evals, int budget) {
+template <int NM, int S>
+__device__ int split_evaluate(WCell<NM, S>& c, double lk, Split& s, int& evals, int budget) {
     const int rr = rachford_rice(c, lk, s);
     if (rr != fp64::kRrInterior)
         return rr == fp64::kRrDegenerate ? fp64::kIndistinguishable
@@ -609,10 +641,10 @@ __device__ int split_evaluate(WCell<NM>& c, double lk, Split& s, int& evals, int
         mag = (1.0 - s.beta) * s.x * (fabs(lx) + fabs(s.lnphi_l)) + s.beta * s.y * (fabs(ly) + fabs(s.lnphi_v));
         bad = !isfinite(s.res) || !isfinite(s.common);
     }
-    if (wany(bad)) return fp64::kAttemptPropertyFailure;
-    s.fug = wmax(r);
-    s.gibbs = wsum(g);
-    s.guard = 256.0 * kEps * (1.0 + wsum(mag));
+    if (wany<S>(bad)) return fp64::kAttemptPropertyFailure;
+    s.fug = wmax<S>(r);
+    s.gibbs = wsum<S>(g);
+    s.guard = 256.0 * kEps * (1.0 + wsum<S>(mag));
     if (!isfinite(s.gibbs) || !isfinite(s.guard)) return fp64::kAttemptPropertyFailure;
     return fp64::kConverged;
 }
@@ -620,8 +652,8 @@ __device__ int split_evaluate(WCell<NM>& c, double lk, Split& s, int& evals, int
 // A ln K attempt continued from `lk0` (pt_split.hpp:349-407): the reference's
 // convergence and acceptance tests, Gibbs line search with 24 halvings,
 // 512 iterations.  `point` holds the last accepted state.
-template <int NM>
-__device__ int attempt(WCell<NM>& c, double lk0, Split& point, int& evals) {
+template <int NM, int S>
+__device__ int attempt(WCell<NM, S>& c, double lk0, Split& point, int& evals) {
     Split next;
     int st = split_evaluate(c, lk0, next, evals, 20000);
     if (st != fp64::kConverged) return st;
@@ -629,7 +661,7 @@ __device__ int attempt(WCell<NM>& c, double lk0, Split& point, int& evals) {
     int iter = 0;
     for (;;) {
         if (point.fug <= 1e-11) {
-            const double contrast = wmax(c.act ? fabs(point.lnk) : 0.0);
+            const double contrast = wmax<S>(c.act ? fabs(point.lnk) : 0.0);
             if (!(point.mass_abs <= 1e-12 && point.mass_rel <= 1e-10)) return fp64::kBalanceFailure;
             if (point.beta <= 1e-10 || 1.0 - point.beta <= 1e-10) return fp64::kPhaseDisappearance;
             if (contrast <= 1e-7 || point.z_v - point.z_l <= 1e-8 * fmax(point.z_v, point.z_l))
@@ -646,7 +678,7 @@ __device__ int attempt(WCell<NM>& c, double lk0, Split& point, int& evals) {
             f1 = cc * point.res;
             f2 = (cc * point.res) * point.res;
         }
-        const double h = wsum(hh), first = wsum(f1), second = wsum(f2);
+        const double h = wsum<S>(hh), first = wsum<S>(f1), second = wsum<S>(f2);
         double slope = NAN;
         if (h > 0.0 && isfinite(h) && isfinite(first) && isfinite(second))
             slope = -(point.beta * (1.0 - point.beta) * second + (first / h) * first) / scale;
@@ -679,23 +711,204 @@ __device__ int attempt(WCell<NM>& c, double lk0, Split& point, int& evals) {
 }
 
 // ---------------------------------------------------------------------------
-// Kernels: one warp per item, items taken from the stage's queue.
-__device__ __forceinline__ int next_item(int* cursor) {
-    int item = 0;
-    if ((threadIdx.x & 31) == 0) item = atomicAdd(cursor, 1);
-    return __shfl_sync(kFull, item, 0);
+// Newton polish of ln K with the exact FP64 Jacobian in closed form.
+//
+// For one phase at composition x (mole fractions as independent variables,
+// the full chart of pr76_phase_ad.hpp:57-122) the PR76 ln phi_i =
+// r_i (Z - 1) - ln(Z - B) - q_i G, r_i = b_i/b, q_i = 2 s_i/a - r_i,
+// G = A ln((Z + (1+sqrt2)B)/(Z + (1-sqrt2)B)) / (2 sqrt2 B), has
+//     d ln phi_i / d x_j = cs_i s_j + cb_i b_j + ca a_ij
+// (dA/dx_j = 2 s_j p/(RT)^2, dB/dx_j = b_j p/RT, dZ from the cubic's implicit
+// derivative).  On the RR manifold at fixed feed (pt_sensitivity_detail.hpp:
+// 291-345) dbeta_j = (x_j y_j / z_j) / h, h = sum_k (y_k - x_k)^2 / z_k, and
+//     dF_i/dlnK_j = -delta_ij - (x_j y_j / z_j) [(U^L_i - U^V_i)/h
+//                   + beta dlnphiL_ij/dx_j + (1 - beta) dlnphiV_ij/dy_j]
+// with U^L_i = sum_k dlnphiL_i/dx_k x_k g_k, U^V_i = sum_k dlnphiV_i/dy_k y_k g_k,
+// g_k = (y_k - x_k)/z_k.  Row i lives on lane i.
+struct PhiCoeffs {
+    double s, cs, cb, ca;  // s and the two row coefficients per lane; ca uniform
+};
+
+template <int NM, int S>
+__device__ bool phi_coeffs(const WCell<NM, S>& c, double x, double Z, PhiCoeffs& f) {
+    double amix, bmix, A, B;
+    if (!mix(c, x, f.s, amix, bmix)) return false;
+    if (!fp64::coefficients(c.p, c.t, amix, bmix, A, B)) return false;
+    const double sqrt2 = 1.4142135623730951;
+    const double prt = c.p / (kR * c.t);
+    const double p1 = prt / (kR * c.t), p2 = prt;  // dA/da, dB/db
+    const double d1 = Z + (1.0 + sqrt2) * B, d2 = Z + (1.0 - sqrt2) * B;
+    const double L = log(d1 / d2);
+    const double G = A * L / (2.0 * sqrt2 * B);
+    const double fz = (3.0 * Z - 2.0 * (1.0 - B)) * Z + (A - 3.0 * B * B - 2.0 * B);
+    const double fa = Z - B;
+    const double fb = Z * Z - (6.0 * B + 2.0) * Z - A + 2.0 * B + 3.0 * B * B;
+    const double zs = -2.0 * fa * p1 / fz, zb = -fb * p2 / fz;
+    const double inv = 1.0 / d1 - 1.0 / d2;
+    const double ls = zs * inv, lb = zb * inv + p2 * ((1.0 + sqrt2) / d1 - (1.0 - sqrt2) / d2);
+    const double gs = (2.0 * p1 * L + A * ls) / (2.0 * sqrt2 * B), gb = A * lb / (2.0 * sqrt2 * B) - G * p2 / B;
+    f.ca = -2.0 * G / amix;
+    f.cs = 0.0;
+    f.cb = 0.0;
+    if (c.comp) {
+        const double r = c.b / bmix, q = 2.0 * f.s / amix - r;
+        f.cs = r * zs - zs / (Z - B) + 4.0 * G * f.s / (amix * amix) - q * gs;
+        f.cb = -r * (Z - 1.0) / bmix + r * zb - (zb - p2) / (Z - B) - G * r / bmix - q * gb;
+    }
+    return isfinite(f.ca) && !wany<S>(!isfinite(f.cs) || !isfinite(f.cb));
 }
 
-template <int NM>
+// Row-distributed LU with partial pivoting: lane i holds row i; pivot rows
+// stay in their lanes (piv lists them in elimination order) and multipliers
+// overwrite the eliminated entries.
+template <int NM, int S>
+__device__ bool lu_rows(double (&J)[NM], int n, int (&piv)[NM]) {
+    const int lane = seg_lane<S>();
+    bool used = lane >= n;
+#pragma unroll
+    for (int k = 0; k < NM; ++k) {
+        if (k >= n) break;
+        // pivot: largest |J_ik| among the rows not used yet (lowest lane on ties)
+        double best = used ? -1.0 : fabs(J[k]);
+        int who = lane;
+#pragma unroll
+        for (int o = S / 2; o > 0; o >>= 1) {
+            const double ob = __shfl_xor_sync(seg_mask<S>(), best, o, S);
+            const int ow = __shfl_xor_sync(seg_mask<S>(), who, o, S);
+            if (ob > best || (ob == best && ow < who)) {
+                best = ob;
+                who = ow;
+            }
+        }
+        if (!(best > 0.0) || !isfinite(best)) return false;
+        piv[k] = who;
+        const double pk = bcast<S>(J[k], who);
+        const double f = (!used && lane != who) ? J[k] / pk : 0.0;
+#pragma unroll
+        for (int j = 0; j < NM; ++j) {
+            const double rj = bcast<S>(J[j], who);
+            if (j > k && !used && lane != who) J[j] -= f * rj;
+        }
+        if (!used && lane != who) J[k] = f;
+        if (lane == who) used = true;
+    }
+    return true;
+}
+
+// Solve J d = rhs with the factors of lu_rows; rhs and d are per lane (row i /
+// component i).
+template <int NM, int S>
+__device__ double lu_solve_rows(const double (&J)[NM], int n, const int (&piv)[NM], double rhs) {
+    const int lane = seg_lane<S>();
+    double y = rhs;
+    // forward: lane piv[k] is final at step k; later rows subtract their multiplier
+    int order = NM;  // this lane's elimination position
+#pragma unroll
+    for (int k = 0; k < NM; ++k)
+        if (k < n && piv[k] == lane) order = k;
+#pragma unroll
+    for (int k = 0; k < NM; ++k) {
+        if (k >= n) break;
+        const double yk = bcast<S>(y, piv[k]);
+        if (order > k && order < NM) y -= J[k] * yk;
+    }
+    double d = 0.0;
+#pragma unroll
+    for (int k = NM - 1; k >= 0; --k) {
+        if (k >= n) continue;
+        const double xk = bcast<S>(order == k ? y / J[k] : 0.0, piv[k]);
+        if (order < k) y -= J[k] * xk;
+        if (lane == k) d = xk;
+    }
+    return d;
+}
+
+// Newton polish from ln K `lk` (the FP32 solution): FP64 residual (bracketed
+// Newton RR and roots), the closed-form Jacobian at the first FP64 state, at
+// most 8 chord steps while |F| decreases.  True with `st` at |F| <= 1e-13, or
+// where |F| stopped decreasing below 1e-11.
+template <int NM, int S>
+__device__ bool polish(WCell<NM, S>& c, double lk, Split& st) {
+    int evals = 0;
+    if (split_evaluate(c, lk, st, evals, 1 << 30) != fp64::kConverged) return false;
+    if (st.fug <= 1e-13) return true;
+    PhiCoeffs fl, fv;
+    if (!phi_coeffs(c, st.x, st.z_l, fl) || !phi_coeffs(c, st.y, st.z_v, fv)) return false;
+    const double g = c.act ? (st.y - st.x) / c.z : 0.0;
+    const double h = wsum<S>(c.act ? (st.y - st.x) * g : 0.0);
+    if (!(h > 0.0) || !isfinite(h)) return false;
+    const double xg = c.act ? st.x * g : 0.0, yg = c.act ? st.y * g : 0.0;
+    const double s1l = wsum<S>(fl.s * xg), s2l = wsum<S>(c.b * xg);
+    const double s1v = wsum<S>(fv.s * yg), s2v = wsum<S>(c.b * yg);
+    double tl = 0.0, tv = 0.0;
+#pragma unroll
+    for (int j = 0; j < NM; ++j) {
+        const double xgj = bcast<S>(xg, j), ygj = bcast<S>(yg, j);
+        if (j < c.n) {
+            tl = fma(c.aij[j], xgj, tl);
+            tv = fma(c.aij[j], ygj, tv);
+        }
+    }
+    const double u = ((fl.cs * s1l + fl.cb * s2l + fl.ca * tl) - (fv.cs * s1v + fv.cb * s2v + fv.ca * tv)) / h;
+    const double w = c.act ? st.x * st.y / c.z : 0.0;
+    const int lane = c.lane;
+    double J[NM];
+#pragma unroll
+    for (int j = 0; j < NM; ++j) {
+        const double wj = bcast<S>(w, j);
+        const double slj = bcast<S>(fl.s, j), svj = bcast<S>(fv.s, j);
+        const double bj = bcast<S>(c.b, j);
+        const bool actj = bcast<S>(c.act ? 1 : 0, j) != 0;
+        const double phil = fl.cs * slj + fl.cb * bj + fl.ca * c.aij[j];
+        const double phiv = fv.cs * svj + fv.cb * bj + fv.ca * c.aij[j];
+        double v = (j == lane) ? 1.0 : 0.0;  // identity rows/columns of absent components
+        if (c.act && actj) v = (j == lane ? -1.0 : 0.0) - wj * (u + st.beta * phil + (1.0 - st.beta) * phiv);
+        J[j] = j < c.n ? v : 0.0;
+    }
+    int piv[NM];
+    if (wany<S>(c.comp && !isfinite(J[0])) || !lu_rows<NM, S>(J, c.n, piv)) return false;
+    double prev = st.fug;
+    Split nx;
+    for (int it = 0; it < 8; ++it) {
+        const double d = lu_solve_rows<NM, S>(J, c.n, piv, c.act ? -st.res : 0.0);
+        if (wany<S>(c.comp && !isfinite(d))) return prev <= 1e-11;
+        const double next_lk = c.act ? st.lnk + d : 0.0;
+        if (split_evaluate(c, next_lk, nx, evals, 1 << 30) != fp64::kConverged) return prev <= 1e-11;
+        if (!(nx.fug < prev)) return prev <= 1e-11;
+        st = nx;
+        prev = st.fug;
+        if (prev <= 1e-13) return true;
+    }
+    return prev <= 1e-11;
+}
+
+// Acceptance of a fugacity-converged state (pt_split.hpp:351-362).
+template <int NM, int S>
+__device__ bool accepted(const WCell<NM, S>& c, const Split& st) {
+    const double contrast = wmax<S>(c.act ? fabs(st.lnk) : 0.0);
+    return st.fug <= 1e-11 && st.mass_abs <= 1e-12 && st.mass_rel <= 1e-10 && st.beta > 1e-10 &&
+           1.0 - st.beta > 1e-10 && contrast > 1e-7 && st.z_v - st.z_l > 1e-8 * fmax(st.z_v, st.z_l);
+}
+
+// ---------------------------------------------------------------------------
+// Kernels: one warp per item, items taken from the stage's queue.
+template <int S>
+__device__ __forceinline__ int next_item(int* cursor) {
+    int item = 0;
+    if (seg_lane<S>() == 0) item = atomicAdd(cursor, 1);
+    return bcast<S>(item, 0);
+}
+
+template <int NM, int S>
 __global__ void __launch_bounds__(128) trials64w_kernel(const Mixture* __restrict__ mix_g, batched::Workspace ws,
                                                         const double* __restrict__ p, const double* __restrict__ t) {
     using namespace batched;
     __shared__ Mixture m;
     stage_mixture(mix_g, m);
-    const int lane = threadIdx.x & 31;
+    const int lane = seg_lane<S>();
     const int total = ws.counters[qT64Items];
     for (;;) {
-        const int item = next_item(&ws.counters[qT64Cursor]);
+        const int item = next_item<S>(&ws.counters[qT64Cursor]);
         if (item >= total) break;
         const int code = ws.t64_items[item];
         const int64_t c = code >> 7;
@@ -703,19 +916,19 @@ __global__ void __launch_bounds__(128) trials64w_kernel(const Mixture* __restric
         const int mode = code & 3;
         const bool review = mode >= mReviewContinue;
         const int row = review ? cFinalEvals : cInitEvals;
-        WCell<NM> cell;
+        WCell<NM, S> cell;
         int status = fp64::kPropertyFailure;
         Tpd point;
         point.w = 0.0;
         if (load_cell(m, ws, c, p, t, cell)) {
-            const int active = __popc(__ballot_sync(kFull, cell.act));
+            const int active = __popc(seg_ballot<S>(cell.act));
             double ref, tol, ex0 = 0.0, ex1 = 0.0;
             bool ok = true;
             if (review) {
                 // the review normalises the feed once more (pt_stability.hpp:242, :278)
                 const bool bad = cell.comp && (!isfinite(cell.z) || cell.z < 0.0 || cell.z > 1.0);
-                const double sum = wsum(cell.comp ? cell.z : 0.0);
-                ok = !wany(bad) && fabs(sum - 1.0) <= 64.0 * kEps;
+                const double sum = wsum<S>(cell.comp ? cell.z : 0.0);
+                ok = !wany<S>(bad) && fabs(sum - 1.0) <= 64.0 * kEps;
                 if (ok && cell.comp) {
                     cell.z /= sum;
                     cell.lz = cell.z > 0.0 ? log(cell.z) : 0.0;
@@ -740,19 +953,19 @@ __global__ void __launch_bounds__(128) trials64w_kernel(const Mixture* __restric
                 } else if (k == 1) {
                     w = cell.act ? 1.0 / static_cast<double>(active) : 0.0;
                 } else {
-                    const unsigned mask = __ballot_sync(kFull, cell.act);
+                    const unsigned mask = seg_ballot<S>(cell.act);
                     const int rank = __popc(mask & ((1u << lane) - 1u));
                     w = cell.z * 0.1 + ((cell.act && rank == k - 2) ? 0.9 : 0.0);
                 }
                 if (!cell.comp) w = 0.0;
-                w /= wsum(w);
+                w /= wsum<S>(w);
             } else {
                 w = cell.act ? static_cast<double>(ws.tw[idx(k * NM + lane, ws.ncell, c)]) : 0.0;
-                w /= wsum(w);
+                w /= wsum<S>(w);
             }
             if (!cell.comp) w = 0.0;
             if (!ok) status = fp64::kPropertyFailure;
-            else if (wany(cell.act && w == 0.0)) status = fp64::kUnrepresentableComposition;
+            else if (wany<S>(cell.act && w == 0.0)) status = fp64::kUnrepresentableComposition;
             else status = trial(cell, w, ref, tol, row, point);
         }
         if (lane == 0) ws.t64_status[idx(k, ws.ncell, c)] = static_cast<signed char>(status);
@@ -762,24 +975,24 @@ __global__ void __launch_bounds__(128) trials64w_kernel(const Mixture* __restric
     }
 }
 
-template <int NM>
+template <int NM, int S>
 __global__ void __launch_bounds__(128) split64w_kernel(const Mixture* __restrict__ mix_g, batched::Workspace ws,
                                                        const double* __restrict__ p, const double* __restrict__ t) {
     using namespace batched;
     __shared__ Mixture m;
     stage_mixture(mix_g, m);
-    const int lane = threadIdx.x & 31;
+    const int lane = seg_lane<S>();
     // the counter can run past the capacity when a cell's block did not fit
     // (that cell went to the fallback); unreserved slots hold -1
     const int total = min(ws.counters[qS64Items], ws.s64_capacity);
     for (;;) {
-        const int item = next_item(&ws.counters[qS64Cursor]);
+        const int item = next_item<S>(&ws.counters[qS64Cursor]);
         if (item >= total) break;
         const int code = ws.s64_items[item];
         if (code < 0) continue;
         const int64_t c = code >> 5;
         const int order = code & 31;
-        WCell<NM> cell;
+        WCell<NM, S> cell;
         Split point;
         int evals = 0;
         int status = fp64::kAttemptPropertyFailure;
@@ -808,6 +1021,143 @@ __global__ void __launch_bounds__(128) split64w_kernel(const Mixture* __restrict
             }
         }
         if (lane == 0) atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], cell.counters[cSplitEvals]);
+    }
+}
+
+// Polish of every cell that reached the split stage (mirrors the lane-per-cell
+// polish_kernel of pr76_batched.cuh): the minimum-Gibbs FP32 attempt, or the
+// two best when FP32 cannot separate them, polished and accepted in FP64; cells
+// without an accepted pair queue their unsettled attempts for split64.
+template <int NM, int S>
+__global__ void __launch_bounds__(128) polishw_kernel(const Mixture* __restrict__ mix_g, batched::Workspace ws,
+                                                      const double* __restrict__ p, const double* __restrict__ t,
+                                                      DeviceOutputs out) {
+    using namespace batched;
+    __shared__ Mixture m;
+    stage_mixture(mix_g, m);
+    const int lane = seg_lane<S>();
+    const int cells = ws.counters[qSplitCells];
+    for (;;) {
+        const int slot = next_item<S>(&ws.counters[qPolishCursor]);
+        if (slot >= cells) break;
+        const int64_t c = ws.split_cells[slot];
+        WCell<NM, S> cell;
+        if (!load_cell(m, ws, c, p, t, cell)) {
+            if (lane == 0) {
+                ws.phase[c] = pFallback;
+                atomicAdd(&ws.counters[qFallback], 1);
+                atomicAdd(&ws.counters[sFbLoad], 1);
+            }
+            continue;
+        }
+        const int n = m.n;
+        const int na = ws.att_count[c];
+        int best = -1, second = -1;
+        for (int a = 0; a < na; ++a) {
+            if (ws.att_class[idx(a, ws.ncell, c)] != fp32::aConverged) continue;
+            const float g = ws.att_gibbs[idx(a, ws.ncell, c)];
+            if (best < 0 || g < ws.att_gibbs[idx(best, ws.ncell, c)]) {
+                second = best;
+                best = a;
+            } else if (second < 0 || g < ws.att_gibbs[idx(second, ws.ncell, c)]) {
+                second = a;
+            }
+        }
+        int candidates[2] = {best, -1};
+        if (best >= 0 && second >= 0) {
+            const float gb = ws.att_gibbs[idx(best, ws.ncell, c)], gs = ws.att_gibbs[idx(second, ws.ncell, c)];
+            const float dl = lane < n ? fabsf(ws.att_lnk[idx(best * NM + lane, ws.ncell, c)] -
+                                              ws.att_lnk[idx(second * NM + lane, ws.ncell, c)])
+                                      : 0.f;
+            const float dist = static_cast<float>(wmax<S>(dl));
+            if (gs - gb <= 1e-4f * (1.f + fabsf(gb)) && dist > 1e-2f) {
+                candidates[1] = second;
+                if (lane == 0) atomicAdd(&ws.counters[sCandidates2], 1);
+            }
+        }
+        bool have = false, polish_failed = false;
+        double best_g = 0.0;
+        Split st;
+        for (int k = 0; k < 2 && candidates[k] >= 0; ++k) {
+            const int a = candidates[k];
+            const double lk = cell.comp ? static_cast<double>(ws.att_lnk[idx(a * NM + lane, ws.ncell, c)]) : 0.0;
+            if (!polish(cell, lk, st)) {
+                polish_failed = true;
+                continue;
+            }
+            if (!accepted(cell, st)) continue;
+            if (have && !(st.gibbs < best_g)) continue;
+            have = true;
+            best_g = st.gibbs;
+            // store_candidate
+            if (lane < n) {
+                ws.cand[idx(0 * NM + lane, ws.ncell, c)] = st.x;
+                ws.cand[idx(1 * NM + lane, ws.ncell, c)] = st.y;
+                ws.cand[idx(2 * NM + lane, ws.ncell, c)] = st.lnk;
+                ws.cand[idx(3 * NM + lane, ws.ncell, c)] = st.lnphi_l;
+                ws.cand[idx(4 * NM + lane, ws.ncell, c)] = st.lnphi_v;
+                ws.cand[idx(5 * NM + lane, ws.ncell, c)] = st.common;
+            }
+            if (lane == 0) {
+                ws.cand_s[idx(0, ws.ncell, c)] = st.beta;
+                ws.cand_s[idx(1, ws.ncell, c)] = st.z_l;
+                ws.cand_s[idx(2, ws.ncell, c)] = st.z_v;
+                ws.cand_s[idx(3, ws.ncell, c)] = st.fug;
+                ws.cand_s[idx(7, ws.ncell, c)] = st.guard;
+            }
+        }
+        if (lane == 0) {
+            atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], cell.counters[cSplitEvals]);
+            atomicAdd(&ws.counters_out[idx(cRrIters, ws.ncell, c)], cell.counters[cRrIters]);
+        }
+        if (!have) {
+            if (lane == 0) {
+                // FP64 continuation of every attempt FP32 left unsettled (split64 items)
+                int cnt = 0;
+                for (int a = 0; a < na; ++a) cnt += unsettled(ws.att_class[idx(a, ws.ncell, c)]);
+                if (cnt == 0) {
+                    ws.phase[c] = pIndeterminate;  // every attempt collapsed or ended at the limit
+                    write_status_only<NM>(out, ws, c, kIndeterminate, false);
+                    write_counters<NM>(out, ws, c);
+                } else {
+                    const int base = atomicAdd(&ws.counters[qS64Items], cnt);
+                    const int reason = best < 0 ? sFbNoAttempt : (polish_failed ? sFbPolish : sFbRejected);
+                    if (base + cnt > ws.s64_capacity) {
+                        ws.phase[c] = pFallback;
+                        atomicAdd(&ws.counters[qFallback], 1);
+                    } else {
+                        int k = 0;
+                        for (int a = 0; a < na; ++a)
+                            if (unsettled(ws.att_class[idx(a, ws.ncell, c)]))
+                                ws.s64_items[base + k++] = (static_cast<int>(c) << 5) | a;
+                        ws.s64_base[c] = base;
+                        ws.s64_count[c] = cnt;
+                        ws.phase[c] = pSplit64;
+                        ws.s64_cells[atomicAdd(&ws.counters[qS64Cells], 1)] = static_cast<int>(c);
+                    }
+                    atomicAdd(&ws.counters[reason], 1);
+                }
+            }
+            continue;
+        }
+        // begin_review (pt_split.hpp:490-512): Gibbs change against the feed,
+        // its guard, the review tolerance and the imposed reference on the
+        // twice-normalised feed
+        const double phi = lane < n ? ws.ref_lnphi[idx(lane, ws.ncell, c)] : 0.0;
+        const double feed_g = wsum<S>(cell.act ? cell.z * (cell.lz + phi) : 0.0);
+        const double magnitude = 1.0 + wsum<S>(cell.act ? cell.z * (fabs(cell.lz) + fabs(phi)) : 0.0);
+        const double zsum = wsum<S>(cell.comp ? cell.z : 0.0);
+        const double z2 = cell.z / zsum;
+        const double lz2 = z2 > 0.0 ? log(z2) : 0.0;
+        if (lane < n)
+            ws.cand[idx(6 * NM + lane, ws.ncell, c)] = z2 > 0.0 ? ws.cand[idx(5 * NM + lane, ws.ncell, c)] - lz2 : 0.0;
+        if (lane == 0) {
+            const double fug = ws.cand_s[idx(3, ws.ncell, c)];
+            ws.cand_s[idx(4, ws.ncell, c)] = best_g - feed_g;
+            ws.cand_s[idx(5, ws.ncell, c)] = ws.cand_s[idx(7, ws.ncell, c)] + 256.0 * kEps * magnitude;
+            ws.cand_s[idx(6, ws.ncell, c)] = 1e-10 + 0.5 * fug;
+            ws.phase[c] = pReview;
+        }
     }
 }
 

@@ -62,10 +62,17 @@ class _Outputs(ctypes.Structure):
     _fields_ = [(f, ctypes.c_void_p) for f, _, _ in OUTPUT_FIELDS]
 
 
+class _ServerOptions(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("slots", ctypes.c_int32), ("max_batch_cells", ctypes.c_int64),
+                ("memory_budget_bytes", ctypes.c_int64), ("form", ctypes.c_int32), ("flags", ctypes.c_int32)]
+
+
 EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu_flash_solve",
                     "mpmc_gpu_flash_solve_device", "mpmc_gpu_flash_components", "mpmc_gpu_flash_last_error",
                     "mpmc_gpu_flash_abi_version", "mpmc_gpu_flash_stage_timings", "mpmc_gpu_flash_batch_stats",
-                    "mpmc_gpu_flash_solve_device_noalloc"]
+                    "mpmc_gpu_flash_solve_device_noalloc", "mpmc_flash_server_create", "mpmc_flash_server_add_mixture",
+                    "mpmc_flash_server_submit", "mpmc_flash_server_wait", "mpmc_flash_server_stats",
+                    "mpmc_flash_server_destroy"]
 NOALLOC_SCRATCH_BYTES = 48 << 20
 BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun", "fallback_nonsmooth",
                "fp64_attempts_no_fp32", "fp64_attempts_polish_failed", "fp64_attempts_rejected", "fallback_load",
@@ -98,6 +105,15 @@ def library() -> ctypes.CDLL:
         lib.mpmc_gpu_flash_components.argtypes = [ctypes.c_void_p]
         lib.mpmc_gpu_flash_stage_timings.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         lib.mpmc_gpu_flash_batch_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        lib.mpmc_flash_server_create.argtypes = [ctypes.POINTER(_ServerOptions), ctypes.POINTER(ctypes.c_void_p)]
+        lib.mpmc_flash_server_add_mixture.argtypes = [ctypes.c_void_p, ctypes.POINTER(_Mixture),
+                                                      ctypes.POINTER(ctypes.c_int32)]
+        lib.mpmc_flash_server_submit.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64] + \
+            [ctypes.c_void_p] * 3 + [ctypes.POINTER(_Outputs), ctypes.POINTER(ctypes.c_uint64)]
+        lib.mpmc_flash_server_wait.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int64,
+                                               ctypes.POINTER(ctypes.c_double)]
+        lib.mpmc_flash_server_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
+        lib.mpmc_flash_server_destroy.argtypes = [ctypes.c_void_p]
         for name in EXPORTED_SYMBOLS:
             getattr(lib, name).restype = ctypes.c_int
         lib.mpmc_gpu_flash_last_error.restype = ctypes.c_char_p
@@ -202,3 +218,74 @@ class GpuFlash:
         s = _Outputs(**out_ptrs)
         _check(library().mpmc_gpu_flash_solve_device_noalloc(self._h, ncell, p_ptr, t_ptr, z_ptr, ctypes.byref(s),
                                                              stream))
+
+
+SERVER_STATS = ["submitted", "completed", "batches", "cells", "slots", "slot_bytes", "most_requests_in_batch",
+                "most_slots_busy"]
+
+
+class FlashServer:
+    """Continuous-batching flash server (C ABI "Flash server").
+
+    `submit()` queues host arrays and returns a ticket at once; the arrays and
+    the output arrays it allocates are kept alive here until `wait()`."""
+
+    def __init__(self, device: int = 0, slots: int = 4, max_batch_cells: int = 65536,
+                 memory_budget_bytes: int = 40 << 30, form: str = "mixed"):
+        o = _ServerOptions(device, slots, max_batch_cells, memory_budget_bytes, FORMS[form], 0)
+        h = ctypes.c_void_p()
+        _check(library().mpmc_flash_server_create(ctypes.byref(o), ctypes.byref(h)))
+        self._h = h
+        self._n = {}
+        self._keep = {}
+        self._mix_keep = []
+
+    def add_mixture(self, mixture) -> int:
+        arrays = [np.ascontiguousarray(a, dtype=np.float64) for a in
+                  (mixture.tc, mixture.pc, mixture.omega, np.asarray(mixture.kij).reshape(-1))]
+        self._mix_keep.append(arrays)
+        m = _Mixture(int(mixture.n), *(a.ctypes.data for a in arrays))
+        mid = ctypes.c_int32()
+        _check(library().mpmc_flash_server_add_mixture(self._h, ctypes.byref(m), ctypes.byref(mid)))
+        self._n[mid.value] = int(mixture.n)
+        return mid.value
+
+    def submit(self, mixture_id: int, p, t, z, fields: list[str] | None = None) -> int:
+        n = self._n[mixture_id]
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        z = np.ascontiguousarray(z, dtype=np.float64)
+        ncell = p.shape[0]
+        rows = output_rows(n)
+        dtypes = {f: d for f, d, _ in OUTPUT_FIELDS}
+        out = {f: np.empty((rows[f], ncell), dtypes[f]) for f in (fields or FLASH_FIELDS)}
+        s = _Outputs(**{f: v.ctypes.data for f, v in out.items()})
+        ticket = ctypes.c_uint64()
+        _check(library().mpmc_flash_server_submit(self._h, mixture_id, ncell, p.ctypes.data, t.ctypes.data,
+                                                  z.ctypes.data, ctypes.byref(s), ctypes.byref(ticket)))
+        self._keep[ticket.value] = (p, t, z, out)
+        return ticket.value
+
+    def wait(self, ticket: int, timeout_s: float | None = None) -> tuple[dict[str, np.ndarray], float]:
+        """Outputs of the request and its submit-to-completion latency (s)."""
+        lat = ctypes.c_double()
+        tmo = -1 if timeout_s is None else int(timeout_s * 1e6)
+        _check(library().mpmc_flash_server_wait(self._h, ticket, tmo, ctypes.byref(lat)))
+        _, _, _, out = self._keep.pop(ticket)
+        return {f: (v[0] if v.shape[0] == 1 else v) for f, v in out.items()}, lat.value
+
+    def stats(self) -> dict[str, int]:
+        out = np.zeros(8, np.int64)
+        k = library().mpmc_flash_server_stats(self._h, out.ctypes.data, 8)
+        return {SERVER_STATS[i]: int(out[i]) for i in range(k)}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            library().mpmc_flash_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

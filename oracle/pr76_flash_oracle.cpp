@@ -18,6 +18,7 @@
 // -ffp-contract=off so x86-64 and aarch64 hosts round identically.
 
 #include <algorithm>
+#include <atomic>
 #include <array>
 #include <cmath>
 #include <cstddef>
@@ -1325,6 +1326,13 @@ inline double lu_rcond(const Lu& f) {
 // linearisation of detail/pt_sensitivity_detail.hpp:46-143; closure dZ/drho of
 // modules/physics/include/mpmc/physics/pr76_thermodynamic_closure.hpp:279-337;
 // per-phase full-chart Jacobians of pr76_phase_ad.hpp:57-122.
+// Test diagnostics: when set, d(ln x_i - ln y_i) is taken as -d ln K_i, the
+// exact value on the RR manifold (y_i = K_i x_i), instead of through the
+// dependent last fractions of the reference's RR linearisation, whose
+// cancellation error eps * sum|dx| / x_{n-1} is the reference's own rounding
+// noise in the last component's row.  Off by default (the restatement).
+inline std::atomic<int> g_manifold_identity{0};
+
 inline void differentiate(const Model& m, const FlashResult& fr, double p, double t, Sensitivity& s) {
     const int n = m.n;
     const int q = n + 1;
@@ -1420,8 +1428,10 @@ inline void differentiate(const Model& m, const FlashResult& fr, double p, doubl
             s.status = 4;  // property_failure
             return;
         }
+        const bool identity = g_manifold_identity.load() != 0;
         for (int i = 0; i < n; ++i) {
-            const D1 fi = log(xl[i]) - log(yv[i]) + pl[i] - pv[i];
+            D1 fi = log(xl[i]) - log(yv[i]) + pl[i] - pv[i];
+            if (identity) fi.d = -lk[i].d + pl[i].d - pv[i].d;
             J[i * nv + v] = fi.d;
             F[i] = fi.v;
         }
@@ -1896,6 +1906,8 @@ int oracle_polish_batch(int n, const double* tc, const double* pc, const double*
 // device implementation can be compared at identical base points.  Only
 // cells with ok[c] != 0 are processed; `out` uses the OracleOutputs layout
 // (sensitivity fields only).
+void oracle_set_manifold_identity(int on) { oracle::g_manifold_identity.store(on ? 1 : 0); }
+
 int oracle_sensitivity_at(int n, const double* tc, const double* pc, const double* omega, const double* kij,
                           int64_t ncell, const double* p, const double* t, const double* z, const int32_t* ok,
                           const double* x, const double* y, const double* lnk, const double* beta, int threads,

@@ -154,11 +154,16 @@ def polish(mix, p, t, z, ln_k, ok, threads: int = 8):
     return out
 
 
-def sensitivity_at(mix, p, t, z, ok, x, y, ln_k, beta, threads: int = 8):
+def sensitivity_at(mix, p, t, z, ok, x, y, ln_k, beta, threads: int = 8, manifold_identity: bool = False):
     """Oracle sensitivities at GIVEN accepted two-phase states (see
     oracle_sensitivity_at): isolates the derivative computation from the
-    convergence noise of the flash that produced the state."""
+    convergence noise of the flash that produced the state.
+
+    manifold_identity: take d(ln x_i - ln y_i) = -d ln K_i exactly instead of
+    through the reference's dependent last fractions (a diagnostic that
+    removes the reference's own cancellation noise in the last row)."""
     build()
+    _lib(ORACLE_SO).oracle_set_manifold_identity(ctypes.c_int(1 if manifold_identity else 0))
     tc, pc, omega, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
     z = np.ascontiguousarray(z, dtype=np.float64)
     n, ncell = z.shape
@@ -173,4 +178,5 @@ def sensitivity_at(mix, p, t, z, ok, x, y, ln_k, beta, threads: int = 8):
     fn(ctypes.c_int(n), *(ctypes.c_void_p(a.ctypes.data) for a in (tc, pc, omega, kij)), ctypes.c_int64(ncell),
        *(ctypes.c_void_p(a.ctypes.data) for a in (p, t, z, okv)), *(ctypes.c_void_p(a.ctypes.data) for a in arrays),
        ctypes.c_void_p(b.ctypes.data), ctypes.c_int(threads), ctypes.byref(s))
+    _lib(ORACLE_SO).oracle_set_manifold_identity(ctypes.c_int(0))
     return out

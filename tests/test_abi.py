@@ -22,7 +22,7 @@ def lib():
 
 def declared_functions():
     text = open(HEADER).read()
-    return sorted(set(re.findall(r"\b(mpmc_gpu_flash_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(mpmc_(?:gpu_flash|flash_server)_\w+)\s*\(", text)))
 
 
 def test_header_declares_the_abi():

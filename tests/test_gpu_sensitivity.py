@@ -31,27 +31,35 @@ class Mix:
 def test_sensitivity_matches_oracle(gpu_lib, oracle_lib, n, ncell, seed, form):
     """Device AD vs the oracle's differentiate_pr76_pt_vle restatement at the
     SAME accepted states (the GPU's), so only the derivative computation is
-    compared; 1e-8 normwise relative per derivative column, widened for
-    d ln K by the forward-error bound cond(dF/dln K) * eps of its linear
-    solve (parity.sensitivity_report)."""
+    compared (parity.sensitivity_report: 1e-8 normwise per derivative column,
+    widened by cond(dF/dln K) * eps).
+
+    The reference forms the last phase fractions as one minus the others, so
+    its d(ln x_{n-1} - ln y_{n-1}) carries a cancellation error of
+    eps * sum|dx| / x_{n-1}: up to ~1e-8 in the last row of d ln K when the
+    last component is scarce (the reference built with FMA contraction
+    differs from itself by 5e-9 there).  The kernel takes that term exactly
+    (-d ln K_{n-1} on the RR manifold).  So every field must meet the bar
+    against the oracle run with the same exact term, and against the faithful
+    restatement everything but d ln K must meet it, d ln K within 5e-8."""
     mix = synth.make_mixture(n, seed)
     p, t, z = synth.make_cells(n, ncell, seed)
     g = gpu_lib.GpuFlash(mix, form=form, sensitivity=True)
     out = g.solve(p, t, z)
     two = out["status"] == 1
-    ref = oracle_lib.sensitivity_at(mix, p, t, z, two, out["liquid"], out["vapor"], out["ln_k"],
-                                    out["vapor_fraction"])
-    ref["sens_status"] = np.where(two, ref["sens_status"], 1)
-    rep = parity.sensitivity_report(out, ref, rcond=ref["rcond"])
-    print(form, n, rep)
-    assert rep["status_match"] == 1.0, rep
-    assert rep["both_ok"] > 0
-    for f, v in rep["bound_ratio"].items():
-        assert v <= 1.0, (f, rep)
-    # all but the conditioning-limited ln K derivatives meet 1e-8 outright
-    for f, v in rep["max"].items():
-        if f != "d_ln_k":
-            assert v <= parity.SENS_TOL, (f, rep)
+    for exact in (True, False):
+        ref = oracle_lib.sensitivity_at(mix, p, t, z, two, out["liquid"], out["vapor"], out["ln_k"],
+                                        out["vapor_fraction"], manifold_identity=exact)
+        ref["sens_status"] = np.where(two, ref["sens_status"], 1)
+        rep = parity.sensitivity_report(out, ref, rcond=ref["rcond"])
+        print(form, n, "exact last row" if exact else "faithful", rep["max"])
+        assert rep["status_match"] == 1.0, rep
+        assert rep["both_ok"] > 0
+        for f, v in rep["bound_ratio"].items():
+            if exact or f != "d_ln_k":
+                assert v <= 1.0, (f, rep)
+            else:
+                assert rep["max"][f] <= 5e-8, (f, rep)
 
 
 @pytest.mark.gpu
