@@ -386,6 +386,7 @@ def main() -> None:
     ap.add_argument("--profile", action="store_true", help="one untimed solve of the workload (for ncu)")
     ap.add_argument("--serving-seconds", type=float, default=8.0,
                     help="open-loop serving probe at 70%% of saturation (0 = skip)")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--serving-sweep", action="store_true",
                     help="only the serving sweep: 10%%..100%% of saturation, --serving-seconds per rate")
     args = ap.parse_args()
@@ -456,7 +457,17 @@ def main() -> None:
 
     mix, p, t, z, placed = make_workload(args.n, args.cells, args.near_fraction, rank, torch, flash, synth, log)
     n, ncell = args.n, args.cells
-    g = flash.GpuFlash(mix, args.form, sensitivity=sens, device=device)
+    # the timed handle replays its launch sequence as a CUDA graph (same cells
+    # and buffers every step)
+    g = flash.GpuFlash(mix, args.form, sensitivity=sens, device=device, graphs=True)
+    tuned = None
+    if args.form == "mixed" and not args.no_autotune and not args.profile:
+        from mpmc_hnu_gb300 import autotune
+
+        tuned = autotune.tune(g, p, t, z, log=log)
+        log(f"autotuned launch shape {tuned['shape']}: {tuned['ms']:.1f} ms vs default {tuned['default_ms']:.1f} ms")
+        workload = {**workload, "launch_shape": tuned["shape"], "autotune_ms": round(tuned["ms"], 1),
+                    "default_shape_ms": round(tuned["default_ms"], 1)}
     fields = g.fields()
     rows = flash.output_rows(n)
     dtypes = {f: d for f, d, _ in flash.OUTPUT_FIELDS}
@@ -528,6 +539,8 @@ def main() -> None:
 
     # per-stage device times (separate instrumented pass) for the roofline
     gt = flash.GpuFlash(mix, args.form, sensitivity=sens, device=device, stage_timing=True)
+    if tuned is not None:
+        gt.set_launch_shape(tuned["shape"])
     gt.solve_device(ncell, dp.data_ptr(), dt.data_ptr(), dz.data_ptr(), ptrs, stream.cuda_stream)
     stages = gt.stage_timings()
     counters_t = outs["counters"].cpu().numpy().astype(np.float64)

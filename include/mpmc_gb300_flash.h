@@ -103,6 +103,7 @@ typedef struct mpmc_pr76_mixture {
 
 /* Option flags (mpmc_flash_options.flags). */
 #define MPMC_FLAG_STAGE_TIMING 1 /* record CUDA events around every device stage */
+#define MPMC_FLAG_CUDA_GRAPH 2   /* replay solves as CUDA graphs (see mpmc_gpu_flash_solve_device) */
 
 typedef struct mpmc_flash_options {
     int32_t form;              /* MPMC_FORM_* */
@@ -161,7 +162,13 @@ int mpmc_gpu_flash_solve(mpmc_gpu_flash* handle, int64_t n_cells, const double* 
 /* Same, with every pointer (inputs and outputs) in DEVICE memory; enqueued
  * on `stream` (a cudaStream_t, NULL = legacy default stream) and returns
  * without synchronising.  Uses per-handle device scratch that it allocates on
- * first use (and grows as needed). */
+ * first use (and grows as needed).  On a handle created with
+ * MPMC_FLAG_CUDA_GRAPH (and without stage timing) the first call for a given
+ * cell count and set of buffers captures the launch sequence into a CUDA graph
+ * and later identical calls replay it (the last 4 such graphs are kept): the
+ * form for a time-stepping loop that flashes the same cell arrays every step.
+ * A captured graph reads the buffers it was captured with, so their contents
+ * may change between calls but not their addresses. */
 int mpmc_gpu_flash_solve_device(mpmc_gpu_flash* handle, int64_t n_cells, const double* p, const double* t,
                                 const double* z, const mpmc_flash_outputs* out, void* stream);
 
@@ -196,6 +203,21 @@ int mpmc_gpu_flash_solve_device(mpmc_gpu_flash* handle, int64_t n_cells, const d
 int mpmc_gpu_flash_solve_device_noalloc(mpmc_gpu_flash* handle, int64_t n_cells, const double* p,
                                         const double* t, const double* z, const mpmc_flash_outputs* out,
                                         void* stream);
+
+/* Launch shape of the mixed form on this handle, as chosen by an autotuner
+ * (mpmc_hnu_gb300/autotune.py) or by hand; count values, the rest default.
+ *   [0] FP32 trial blocks per SM        [1] FP32 attempt blocks per SM
+ *   [2] FP64 trial-item blocks per SM   [3] FP64 attempt and polish blocks per SM
+ *   [4] per-cell kernel blocks per SM   [5] item form: bit 0 feed trials, bit 1
+ *       review trials, bit 2 attempts, bit 3 polish run one item per thread
+ *       instead of one per lane group
+ *   [6] successive-substitution -> Newton switch: the FP32 |r| (in units of
+ *       1e-6) at which the FP32 ln K iteration hands over to the FP64 polish
+ * 0 selects the default (occupancy-derived residency, lane-group items,
+ * switch at 2e-5).  Results do not depend on the shape beyond the rounding of
+ * where each iteration stops.  Drops the handle's captured graphs.  No
+ * counterpart in the reference. */
+int mpmc_gpu_flash_set_launch_shape(mpmc_gpu_flash* handle, const int32_t* values, int count);
 
 /* Device time in milliseconds of every stage of the last solve on a handle
  * created with MPMC_FLAG_STAGE_TIMING (waits for that solve to finish).

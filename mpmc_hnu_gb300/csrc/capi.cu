@@ -9,9 +9,11 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/mpmc_gb300_flash.h"
 #include "launch.h"
@@ -50,6 +52,16 @@ struct DevBuf {
 };
 
 constexpr int kOutputFields = 21;
+constexpr size_t kMaxGraphs = 4;
+
+// One captured solve: the cell count and every buffer are baked into it.
+struct GraphEntry {
+    int64_t ncell = 0;
+    const double *p = nullptr, *t = nullptr, *z = nullptr;
+    pr76::DeviceOutputs outputs{};
+    cudaGraphExec_t exec = nullptr;
+    uint64_t last_use = 0;
+};
 
 }  // namespace
 
@@ -68,6 +80,10 @@ struct mpmc_gpu_flash {
     bool stage_timing = false;
     cudaEvent_t events[24] = {};
     int n_events = 0;   // events recorded by the last solve (stages + 1)
+    int32_t shape[8] = {};  // explicit launch shape (mpmc_gpu_flash_set_launch_shape), 0 = default
+    bool use_graphs = false;
+    std::vector<GraphEntry> graphs;
+    uint64_t graph_clock = 0;
 };
 
 namespace {
@@ -177,64 +193,132 @@ int with_sensitivity_inputs(mpmc_gpu_flash* h, int64_t ncell, pr76::DeviceOutput
     return MPMC_OK;
 }
 
-int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
-               const pr76::DeviceOutputs& d_in, cudaStream_t stream) {
-    pr76::DeviceOutputs d = d_in;
+// Launch shape of the mixed form: defaults, then the MPMC_* environment knobs
+// (sweeps), then the handle's explicit shape (mpmc_gpu_flash_set_launch_shape).
+pr76::BatchedShape batched_shape(const mpmc_gpu_flash* h, cudaEvent_t* events) {
+    pr76::BatchedShape shape{0, 0, 0, 0, 0, events, 0, 0.0f};
+    const struct {
+        const char* name;
+        int* field;
+    } knobs[] = {{"MPMC_TRIAL_BLOCKS_PER_SM", &shape.trial_blocks_per_sm},
+                 {"MPMC_SPLIT_BLOCKS_PER_SM", &shape.split_blocks_per_sm},
+                 {"MPMC_T64_BLOCKS_PER_SM", &shape.t64_blocks_per_sm},
+                 {"MPMC_S64_BLOCKS_PER_SM", &shape.s64_blocks_per_sm},
+                 {"MPMC_CELL_BLOCKS_PER_SM", &shape.cell_blocks_per_sm},
+                 {"MPMC_ITEM_FORM", &shape.item_form}};
+    for (const auto& k : knobs)
+        if (const char* v = std::getenv(k.name)) *k.field = std::atoi(v);
+    int* fields[6] = {&shape.trial_blocks_per_sm, &shape.split_blocks_per_sm, &shape.t64_blocks_per_sm,
+                      &shape.s64_blocks_per_sm, &shape.cell_blocks_per_sm, &shape.item_form};
+    for (int k = 0; k < 6; ++k)
+        if (h->shape[k] > 0) *fields[k] = h->shape[k];
+    if (h->shape[6] > 0) shape.ss_switch = 1e-6f * static_cast<float>(h->shape[6]);
+    return shape;
+}
+
+// Device scratch of a solve (allocated before any launch, so that a graph
+// capture of the launches sees no allocation).
+int prepare_device(mpmc_gpu_flash* h, int64_t ncell, pr76::DeviceOutputs& d) {
     if (h->want_sensitivity) {
         const int rc = with_sensitivity_inputs(h, ncell, d);
         if (rc != MPMC_OK) return rc;
     }
+    if (h->form == MPMC_FORM_MIXED) {
+        if (ncell >= (int64_t{1} << 24))
+            return fail(MPMC_ERR_INVALID_ARGUMENT, "mixed form: at most 16,777,215 cells per call");
+        const cudaError_t e = h->workspace.ensure(pr76::batched_workspace_bytes(h->n, ncell));
+        if (e != cudaSuccess) return cuda_fail(e, "batched workspace allocation");
+    } else if (h->form != MPMC_FORM_PLAIN_FP64) {
+        return fail(MPMC_ERR_UNSUPPORTED, "algorithm form not available in this build");
+    }
+    return MPMC_OK;
+}
+
+// The launches of one solve on `stream` (no allocation, no synchronisation).
+cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
+                           const pr76::DeviceOutputs& d, cudaStream_t stream, bool timing) {
+    cudaError_t e;
+    int next_event = 0;
+    auto record = [&]() {
+        if (timing && next_event < 24) cudaEventRecord(h->events[next_event++], stream);
+    };
+    if (h->form == MPMC_FORM_PLAIN_FP64) {
+        record();
+        e = pr76::launch_plain(h->n, h->d_mixture, ncell, p, t, z, d, stream);
+        record();
+    } else {
+        const pr76::BatchedShape shape = batched_shape(h, timing ? h->events : nullptr);
+        e = pr76::launch_batched(h->n, h->d_mixture, ncell, p, t, z, d, h->workspace.ptr, h->workspace.bytes, shape,
+                                 stream);
+        next_event = timing ? pr76::kBatchedStages + 1 : 0;
+    }
+    if (e != cudaSuccess) return e;
+    if (h->want_sensitivity) {
+        e = pr76::launch_sensitivity(h->n, h->d_mixture, ncell, p, t, z, d, stream);
+        if (e != cudaSuccess) return e;
+    }
+    record();  // end of the sensitivity stage (zero length without sensitivities)
+    if (timing) h->n_events = next_event;
+    return cudaSuccess;
+}
+
+bool same_key(const GraphEntry& g, int64_t ncell, const double* p, const double* t, const double* z,
+              const pr76::DeviceOutputs& d) {
+    return g.ncell == ncell && g.p == p && g.t == t && g.z == z &&
+           std::memcmp(&g.outputs, &d, sizeof(pr76::DeviceOutputs)) == 0;
+}
+
+int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
+               const pr76::DeviceOutputs& d_in, cudaStream_t stream) {
+    pr76::DeviceOutputs d = d_in;
+    int rc = prepare_device(h, ncell, d);
+    if (rc != MPMC_OK) return rc;
     cudaError_t e;
     h->n_events = 0;
     if (h->stage_timing && !h->events[0]) {
         for (auto& ev : h->events)
             if ((e = cudaEventCreate(&ev)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
     }
-    int next_event = 0;
-    auto record = [&]() {
-        if (h->stage_timing && next_event < 24) cudaEventRecord(h->events[next_event++], stream);
-    };
-    switch (h->form) {
-    case MPMC_FORM_PLAIN_FP64:
-        record();
-        e = pr76::launch_plain(h->n, h->d_mixture, ncell, p, t, z, d, stream);
-        record();
-        break;
-    case MPMC_FORM_MIXED: {
-        if (ncell >= (int64_t{1} << 24))
-            return fail(MPMC_ERR_INVALID_ARGUMENT, "mixed form: at most 16,777,215 cells per call");
-        const size_t need = pr76::batched_workspace_bytes(h->n, ncell);
-        if ((e = h->workspace.ensure(need)) != cudaSuccess) return cuda_fail(e, "batched workspace allocation");
-        pr76::BatchedShape shape{0, 0, 0, 0, 0, h->stage_timing ? h->events : nullptr};
-        const struct {
-            const char* name;
-            int* field;
-        } knobs[] = {{"MPMC_TRIAL_BLOCKS_PER_SM", &shape.trial_blocks_per_sm},
-                     {"MPMC_SPLIT_BLOCKS_PER_SM", &shape.split_blocks_per_sm},
-                     {"MPMC_T64_BLOCKS_PER_SM", &shape.t64_blocks_per_sm},
-                     {"MPMC_S64_BLOCKS_PER_SM", &shape.s64_blocks_per_sm},
-                     {"MPMC_CELL_BLOCKS_PER_SM", &shape.cell_blocks_per_sm},
-                     {"MPMC_ITEM_FORM", &shape.item_form}};
-        for (const auto& k : knobs)
-            if (const char* v = std::getenv(k.name)) *k.field = std::atoi(v);
-        e = pr76::launch_batched(h->n, h->d_mixture, ncell, p, t, z, d, h->workspace.ptr, h->workspace.bytes, shape,
-                                 stream);
-        next_event = h->stage_timing ? pr76::kBatchedStages + 1 : 0;
-        break;
+    if (!h->use_graphs || h->stage_timing) {
+        e = enqueue_device(h, ncell, p, t, z, d, stream, h->stage_timing);
+        return e == cudaSuccess ? MPMC_OK : cuda_fail(e, "flash kernel launch");
     }
-    default:
-        return fail(MPMC_ERR_UNSUPPORTED, "algorithm form not available in this build");
+    // CUDA graph of the launch sequence, one per (cells, buffers): captured on
+    // the handle's stream at the first call, replayed on `stream` afterwards
+    for (GraphEntry& g : h->graphs) {
+        if (!same_key(g, ncell, p, t, z, d)) continue;
+        g.last_use = ++h->graph_clock;
+        e = cudaGraphLaunch(g.exec, stream);
+        return e == cudaSuccess ? MPMC_OK : cuda_fail(e, "cudaGraphLaunch");
     }
-    if (e != cudaSuccess) return cuda_fail(e, "flash kernel launch");
-    if (h->want_sensitivity) {
-        e = pr76::launch_sensitivity(h->n, h->d_mixture, ncell, p, t, z, d, stream);
-        if (e != cudaSuccess) return cuda_fail(e, "sensitivity kernel launch");
-    } else if (h->stage_timing) {
-        record();  // zero-length sensitivity stage keeps the stage list fixed
+    cudaGraph_t graph = nullptr;
+    if ((e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return cuda_fail(e, "cudaStreamBeginCapture");
+    const cudaError_t le = enqueue_device(h, ncell, p, t, z, d, h->stream, false);
+    e = cudaStreamEndCapture(h->stream, &graph);
+    if (le != cudaSuccess || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return cuda_fail(le != cudaSuccess ? le : e, "graph capture of the flash launches");
     }
-    if (h->want_sensitivity) record();
-    h->n_events = next_event;
-    return MPMC_OK;
+    GraphEntry entry;
+    e = cudaGraphInstantiate(&entry.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+    entry.ncell = ncell;
+    entry.p = p;
+    entry.t = t;
+    entry.z = z;
+    entry.outputs = d;
+    entry.last_use = ++h->graph_clock;
+    if (h->graphs.size() >= kMaxGraphs) {  // evict the least recently used
+        auto oldest = std::min_element(h->graphs.begin(), h->graphs.end(),
+                                       [](const GraphEntry& a, const GraphEntry& b) { return a.last_use < b.last_use; });
+        cudaGraphExecDestroy(oldest->exec);
+        h->graphs.erase(oldest);
+    }
+    h->graphs.push_back(entry);
+    e = cudaGraphLaunch(entry.exec, stream);
+    return e == cudaSuccess ? MPMC_OK : cuda_fail(e, "cudaGraphLaunch");
 }
 
 // ---- fixed scratch of the no-allocation entry point ----
@@ -395,6 +479,7 @@ int mpmc_gpu_flash_create(const mpmc_pr76_mixture* mixture, const mpmc_flash_opt
     h->form = opt.form;
     h->want_sensitivity = opt.want_sensitivity;
     h->stage_timing = (opt.flags & MPMC_FLAG_STAGE_TIMING) != 0;
+    h->use_graphs = (opt.flags & MPMC_FLAG_CUDA_GRAPH) != 0;
     h->host_mixture = m;
     e = cudaMalloc(&h->d_mixture, sizeof(pr76::Mixture));
     if (e == cudaSuccess) e = cudaMemcpy(h->d_mixture, &m, sizeof(pr76::Mixture), cudaMemcpyHostToDevice);
@@ -420,6 +505,7 @@ int mpmc_gpu_flash_destroy(mpmc_gpu_flash* h) {
     h->workspace.release();
     for (auto& ev : h->events)
         if (ev) cudaEventDestroy(ev);
+    for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
     if (h->d_mixture) cudaFree(h->d_mixture);
     if (h->stream) cudaStreamDestroy(h->stream);
     delete h;
@@ -435,6 +521,20 @@ int mpmc_gpu_flash_solve_device(mpmc_gpu_flash* h, int64_t ncell, const double* 
     cudaError_t e = cudaSetDevice(h->device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     return run_device(h, ncell, p, t, z, to_device_outputs(out), static_cast<cudaStream_t>(stream));
+}
+
+int mpmc_gpu_flash_set_launch_shape(mpmc_gpu_flash* h, const int32_t* values, int count) {
+    if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
+    if (count < 0 || count > 8 || (count > 0 && !values))
+        return fail(MPMC_ERR_INVALID_ARGUMENT, "launch shape: 0 to 8 values");
+    for (int k = 0; k < count; ++k)
+        if (values[k] < 0 || values[k] > (k == 6 ? 1000000 : 64))
+            return fail(MPMC_ERR_INVALID_ARGUMENT, "launch shape value out of range");
+    for (int k = 0; k < 8; ++k) h->shape[k] = k < count ? values[k] : 0;
+    cudaSetDevice(h->device);
+    for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);  // captured with the old shape
+    h->graphs.clear();
+    return MPMC_OK;
 }
 
 int mpmc_gpu_flash_solve_device_noalloc(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t,
@@ -464,7 +564,7 @@ int mpmc_gpu_flash_solve_device_noalloc(mpmc_gpu_flash* h, int64_t ncell, const 
     const int rc = noalloc_scratch(h->device, &scratch);
     if (rc != MPMC_OK) return rc;
     const cudaStream_t s = static_cast<cudaStream_t>(stream);
-    const pr76::BatchedShape shape{0, 0, 0, 0, 0, nullptr};
+    const pr76::BatchedShape shape = batched_shape(h, nullptr);
     e = pr76::launch_batched(h->n, h->d_mixture, ncell, p, t, z, d, scratch, MPMC_NOALLOC_SCRATCH_BYTES, shape, s);
     if (e != cudaSuccess) return cuda_fail(e, "flash kernel launch");
     if (h->want_sensitivity) {

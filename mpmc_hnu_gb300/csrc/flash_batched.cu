@@ -45,6 +45,8 @@ size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell) {
     ws.att_gibbs = reinterpret_cast<float*>(take(sizeof(float) * batched::kMaxAttempts * nc));
     ws.att_class = reinterpret_cast<signed char*>(take(batched::kMaxAttempts * nc));
     ws.att_count = reinterpret_cast<int*>(take(sizeof(int) * nc));
+    ws.att_iter = reinterpret_cast<short*>(take(sizeof(short) * batched::kMaxAttempts * nc));
+    ws.att_rate = reinterpret_cast<float*>(take(sizeof(float) * batched::kMaxAttempts * nc));
     ws.cand = reinterpret_cast<double*>(take(sizeof(double) * 7 * NM * nc));
     ws.cand_s = reinterpret_cast<double*>(take(sizeof(double) * 8 * nc));
     ws.counters_out = reinterpret_cast<int*>(take(sizeof(int) * cCount * nc));
@@ -129,7 +131,10 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     mark();
     decide_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
     mark();
-    split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t);
+    // FP32 successive substitution hands over to the FP64 Newton polish at
+    // |r| <= ss_switch (default 2e-5, a few times the FP32 rounding floor)
+    const float ss_switch = shape.ss_switch > 0.f ? shape.ss_switch : 2e-5f;
+    split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t, ss_switch);
     mark();
     if (shape.item_form & 8) polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
     else w64::polishw_kernel<NM, w64::kSeg<NM>><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t, out);

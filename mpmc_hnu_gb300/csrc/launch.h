@@ -57,6 +57,8 @@ struct BatchedShape {
     cudaEvent_t* events;  // optional: kBatchedStages + 1 events recorded around the stages
     int item_form;        // FP64 item kernels: bit 0 feed trials, bit 1 review trials, bit 2 attempts,
                           // bit 3 polish run one item per lane when set, one item per warp when clear
+    float ss_switch;      // FP32 |r| at which successive substitution hands over to the FP64
+                          // Newton polish (0 = 2e-5)
 };
 constexpr int kBatchedStages = 15;
 

@@ -110,6 +110,8 @@ struct Workspace {
     int* s64_items;         // [s64_capacity] FP64 attempt items (cell << 5 | order)
     signed char* s64_status;// [s64_capacity]
     double* s64_state;      // [s64_capacity * S64Stride] converged attempt states
+    short* att_iter;        // [kMaxAttempts * ncell] FP32 SS iterations of the attempt
+    float* att_rate;        // [kMaxAttempts * ncell] FP32 SS contraction per iteration, ln(|r| ratio)
     int* split_cells;       // [ncell] cells that reached the split stage
     int* s64_cells;         // [ncell] cells whose attempts were continued in FP64
     int* s64_base;          // [ncell] first FP64 attempt item of the cell
@@ -649,12 +651,21 @@ struct SplitLane {
     float lk[NM];
     int item, c, order, iter, bt, stage;  // stage 0 = evaluate seed, 1 = line search, 2 = finished
     float alpha, slope, scale;
+    float fug0, ck_fug, rate;  // |r| at the seed, at the last checkpoint; contraction per iteration
+    int ck_iter;
 };
 
 template <int NM>
-__device__ void split_step_or_finish(SplitLane<NM>& L) {
+__device__ void split_step_or_finish(SplitLane<NM>& L, float ss_switch) {
     const int n = L.cell.n;
-    if (L.point.fug <= 2e-5f || L.iter >= 512) {
+    // contraction rate of the iteration over 16-iteration windows, measured
+    // only while |r| is well above the FP32 rounding floor
+    if (L.iter - L.ck_iter >= 16 && L.point.fug > 10.f * ss_switch) {
+        if (L.ck_fug > L.point.fug) L.rate = logf(L.ck_fug / L.point.fug) / static_cast<float>(L.iter - L.ck_iter);
+        L.ck_fug = L.point.fug;
+        L.ck_iter = L.iter;
+    }
+    if (L.point.fug <= ss_switch || L.iter >= 512) {
         L.stage = 2;
         return;
     }
@@ -681,7 +692,8 @@ __device__ void split_step_or_finish(SplitLane<NM>& L) {
 
 template <int NM>
 __global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict__ mix_g, Workspace ws,
-                                                      const double* __restrict__ p, const double* __restrict__ t) {
+                                                      const double* __restrict__ p, const double* __restrict__ t,
+                                                      float ss_switch) {
     __shared__ Mixture m;
     stage_mixture(mix_g, m);
     const int total = ws.counters[qAttempts];
@@ -697,13 +709,23 @@ __global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict_
                 float contrast = 0.f;
                 for (int i = 0; i < n; ++i) contrast = fmaxf(contrast, fabsf(L.point.lnk[i]));
                 if (L.iter >= 0) {
+                    // contraction per iteration: the last window above the FP32
+                    // floor, else the whole descent from the seed
+                    float rate = L.rate;
+                    if (!(rate > 0.f) && L.iter > 0 && L.fug0 > L.point.fug)
+                        rate = logf(L.fug0 / L.point.fug) / static_cast<float>(L.iter);
+                    // iterations the reference's FP64 iteration still needs to |r| <= 1e-11
+                    const float needed = rate > 0.f ? logf(fmaxf(L.point.fug, 1e-11f) / 1e-11f) / rate : 1e9f;
                     if (contrast < 1e-4f || L.point.z_v - L.point.z_l <= 1e-5f * fmaxf(L.point.z_v, L.point.z_l))
                         cls = fp32::aTrivial;
-                    else if (L.point.fug <= 1e-3f)
-                        cls = fp32::aConverged;
                     else if (L.iter >= 512)
-                        cls = fp32::aLimit;
+                        cls = fp32::aLimit;  // FP32 and FP64 track each other far above the floor
+                    else if (L.point.fug <= 1e-3f && static_cast<float>(L.iter) + needed <= 448.f)
+                        cls = fp32::aConverged;  // converges well inside the 512-iteration budget
+                    // else: unsettled, continued exactly in FP64 with the remaining budget
+                    ws.att_rate[idx(L.order, ws.ncell, L.c)] = rate;
                 }
+                ws.att_iter[idx(L.order, ws.ncell, L.c)] = static_cast<short>(L.iter < 0 ? 0 : L.iter);
                 const int64_t c = L.c;
                 ws.att_class[idx(L.order, ws.ncell, c)] = static_cast<signed char>(cls);
                 if (cls == fp32::aLimit) atomicAdd(&ws.counters[sLimitAttempts], 1);
@@ -722,6 +744,8 @@ __global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict_
                 int active;
                 L.iter = 0;
                 L.stage = 0;
+                L.rate = 0.f;
+                L.ck_iter = 0;
                 if (!load_cell32(m, ws, L.c, p, t, L.cell, active)) {
                     L.iter = -1;
                     L.stage = 2;
@@ -743,7 +767,9 @@ __global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict_
                 continue;
             }
             fp32::copy_state(L.point, L.next, n);
-            split_step_or_finish(L);
+            L.fug0 = L.point.fug;
+            L.ck_fug = L.point.fug;
+            split_step_or_finish(L, ss_switch);
             continue;
         }
         bool accept = false;
@@ -757,7 +783,7 @@ __global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict_
         if (accept) {
             fp32::copy_state(L.point, L.next, n);
             ++L.iter;
-            split_step_or_finish(L);
+            split_step_or_finish(L, ss_switch);
         } else if (++L.bt >= 20) {
             L.stage = 2;
         } else {

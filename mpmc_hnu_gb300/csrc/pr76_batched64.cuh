@@ -254,7 +254,7 @@ struct Split64Lane {
     double lk[NM], e[NM], num[NM];
     double alpha, slope, scale;
     int64_t c;
-    int item, order, iter, bt, stage, status, evals;
+    int item, order, iter, bt, stage, status, evals, done;  // done: FP32 iterations already made
 };
 
 template <int NM>
@@ -271,7 +271,7 @@ __device__ void s64_check(Split64Lane<NM>& L) {
         L.stage = 2;
         return;
     }
-    if (L.iter >= 512) {
+    if (L.done + L.iter >= 512) {
         L.status = fp64::kAttemptIterationLimit;
         L.stage = 2;
         return;
@@ -355,6 +355,7 @@ __global__ void __launch_bounds__(64) split64_kernel(const Mixture* __restrict__
                     L.iter = 0;
                     L.stage = 0;
                     L.evals = 0;
+                    L.done = ws.att_iter[idx(L.order, ws.ncell, L.c)];
                     L.status = fp64::kAttemptPropertyFailure;
                     if (!load_cell64(m, ws, L.c, p, t, L.cell)) {
                         L.stage = 2;

@@ -650,10 +650,12 @@ __device__ int split_evaluate(WCell<NM, S>& c, double lk, Split& s, int& evals, 
 }
 
 // A ln K attempt continued from `lk0` (pt_split.hpp:349-407): the reference's
-// convergence and acceptance tests, Gibbs line search with 24 halvings,
-// 512 iterations.  `point` holds the last accepted state.
+// convergence and acceptance tests, Gibbs line search with 24 halvings, and
+// the iterations left of the reference's 512 after the `done` the attempt
+// already made in FP32 (whose iterates track the FP64 ones far above the FP32
+// floor).  `point` holds the last accepted state.
 template <int NM, int S>
-__device__ int attempt(WCell<NM, S>& c, double lk0, Split& point, int& evals) {
+__device__ int attempt(WCell<NM, S>& c, double lk0, Split& point, int& evals, int done) {
     Split next;
     int st = split_evaluate(c, lk0, next, evals, 20000);
     if (st != fp64::kConverged) return st;
@@ -668,7 +670,7 @@ __device__ int attempt(WCell<NM, S>& c, double lk0, Split& point, int& evals) {
                 return fp64::kIndistinguishable;
             return fp64::kConverged;
         }
-        if (iter >= 512) return fp64::kAttemptIterationLimit;
+        if (done + iter >= 512) return fp64::kAttemptIterationLimit;
         const double scale = fmax(1.0, point.fug / 2.0);
         double hh = 0.0, f1 = 0.0, f2 = 0.0;
         if (c.act) {
@@ -998,7 +1000,7 @@ __global__ void __launch_bounds__(128) split64w_kernel(const Mixture* __restrict
         int status = fp64::kAttemptPropertyFailure;
         if (load_cell(m, ws, c, p, t, cell)) {
             const double lk0 = cell.comp ? static_cast<double>(ws.att_lnk[idx(order * NM + lane, ws.ncell, c)]) : 0.0;
-            status = attempt(cell, lk0, point, evals);
+            status = attempt(cell, lk0, point, evals, ws.att_iter[idx(order, ws.ncell, c)]);
         }
         if (lane == 0) ws.s64_status[item] = static_cast<signed char>(status);
         if (status == fp64::kConverged) {

@@ -72,7 +72,8 @@ EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu
                     "mpmc_gpu_flash_abi_version", "mpmc_gpu_flash_stage_timings", "mpmc_gpu_flash_batch_stats",
                     "mpmc_gpu_flash_solve_device_noalloc", "mpmc_flash_server_create", "mpmc_flash_server_add_mixture",
                     "mpmc_flash_server_submit", "mpmc_flash_server_wait", "mpmc_flash_server_stats",
-                    "mpmc_flash_server_destroy"]
+                    "mpmc_flash_server_destroy", "mpmc_gpu_flash_set_launch_shape"]
+FLAG_CUDA_GRAPH = 2
 NOALLOC_SCRATCH_BYTES = 48 << 20
 BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun", "fallback_nonsmooth",
                "fp64_attempts_no_fp32", "fp64_attempts_polish_failed", "fp64_attempts_rejected", "fallback_load",
@@ -114,6 +115,7 @@ def library() -> ctypes.CDLL:
                                                ctypes.POINTER(ctypes.c_double)]
         lib.mpmc_flash_server_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         lib.mpmc_flash_server_destroy.argtypes = [ctypes.c_void_p]
+        lib.mpmc_gpu_flash_set_launch_shape.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         for name in EXPORTED_SYMBOLS:
             getattr(lib, name).restype = ctypes.c_int
         lib.mpmc_gpu_flash_last_error.restype = ctypes.c_char_p
@@ -140,7 +142,7 @@ class GpuFlash:
     """One mixture on one GPU; batches of cells per call."""
 
     def __init__(self, mixture, form: str | int = "plain", sensitivity: bool = False, device: int = 0,
-                 stage_timing: bool = False):
+                 stage_timing: bool = False, graphs: bool = False):
         self.mixture = mixture
         self.n = int(mixture.n)
         self.form = FORMS[form] if isinstance(form, str) else int(form)
@@ -148,7 +150,8 @@ class GpuFlash:
         self._keep = [np.ascontiguousarray(a, dtype=np.float64) for a in
                       (mixture.tc, mixture.pc, mixture.omega, np.asarray(mixture.kij).reshape(-1))]
         m = _Mixture(self.n, *(a.ctypes.data for a in self._keep))
-        o = _Options(self.form, int(self.sensitivity), device, FLAG_STAGE_TIMING if stage_timing else 0)
+        flags = (FLAG_STAGE_TIMING if stage_timing else 0) | (FLAG_CUDA_GRAPH if graphs else 0)
+        o = _Options(self.form, int(self.sensitivity), device, flags)
         h = ctypes.c_void_p()
         _check(library().mpmc_gpu_flash_create(ctypes.byref(m), ctypes.byref(o), ctypes.byref(h)))
         self._h = h
@@ -189,6 +192,11 @@ class GpuFlash:
         """Host-buffer entry with caller-owned (e.g. pinned) host pointers."""
         s = _Outputs(**out_ptrs)
         _check(library().mpmc_gpu_flash_solve(self._h, ncell, p_ptr, t_ptr, z_ptr, ctypes.byref(s)))
+
+    def set_launch_shape(self, values) -> None:
+        """Mixed-form launch shape (see mpmc_gpu_flash_set_launch_shape)."""
+        v = np.ascontiguousarray(values, dtype=np.int32)
+        _check(library().mpmc_gpu_flash_set_launch_shape(self._h, v.ctypes.data, int(v.size)))
 
     def batch_stats(self) -> dict[str, int]:
         """Work statistics of the last mixed-form solve."""
