@@ -57,6 +57,24 @@ def f_ad(n: int) -> float:
     return (2 / 3) * n ** 3 + 2 * n * n * (n + 1) + 2 * n * (2 * n + 1) * (n + 1) + 2 * (n + 2) * f_eval(n)
 
 
+# ---------------------------------------------------------------------------
+# replicas (one process per GPU; cells are independent, so no data exchange)
+def cell_offset(rank: int, ncell: int) -> int:
+    """First index of rank's cell stream: ranks draw disjoint cells."""
+    return rank * (4 * ncell)
+
+
+def max_over_ranks(value: float, world: int, device: str) -> float:
+    """The job's time is its slowest rank's (a MAX all-reduce; no-op at N=1)."""
+    if world <= 1:
+        return value
+    import torch
+
+    tt = torch.tensor([value], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+    return float(tt.item())
+
+
 def place_near(t, z, idx, noise_index, status_fn):
     """Phase-count change pressure of cells `idx` by a 9-point log-p grid and 7
     bisection steps in ln p (bracket width 0.55 * 2**-7 < 0.5 %) with
@@ -92,7 +110,7 @@ def place_near(t, z, idx, noise_index, status_fn):
 
 def base_cells(n: int, ncell: int, near_fraction: float, rank: int, synth):
     mix = synth.make_mixture(n, MIXTURE_SEED)
-    offset = rank * (4 * ncell)
+    offset = cell_offset(rank, ncell)
     p, t, z = synth.make_cells(n, ncell, CELL_SEED, offset=offset)
     n_near = int(round(near_fraction * ncell))  # the first n_near cells go near their boundary
     return mix, offset, p, t, z, n_near
@@ -387,6 +405,8 @@ def main() -> None:
     ap.add_argument("--serving-seconds", type=float, default=8.0,
                     help="open-loop serving probe at 70%% of saturation (0 = skip)")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
+    ap.add_argument("--launch-shape", default="",
+                    help="comma-separated mixed-form launch shape to use instead of autotuning")
     ap.add_argument("--serving-sweep", action="store_true",
                     help="only the serving sweep: 10%%..100%% of saturation, --serving-seconds per rate")
     args = ap.parse_args()
@@ -461,7 +481,12 @@ def main() -> None:
     # and buffers every step)
     g = flash.GpuFlash(mix, args.form, sensitivity=sens, device=device, graphs=True)
     tuned = None
-    if args.form == "mixed" and not args.no_autotune and not args.profile:
+    if args.form == "mixed" and args.launch_shape:
+        tuned = {"shape": [int(v) for v in args.launch_shape.split(",")], "ms": float("nan"),
+                 "default_ms": float("nan")}
+        g.set_launch_shape(tuned["shape"])
+        workload = {**workload, "launch_shape": tuned["shape"]}
+    elif args.form == "mixed" and not args.no_autotune and not args.profile:
         from mpmc_hnu_gb300 import autotune
 
         tuned = autotune.tune(g, p, t, z, log=log)
@@ -507,11 +532,7 @@ def main() -> None:
         torch.cuda.synchronize()
     barrier()
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        tt_ = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(tt_, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt_.item())
+    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, "cuda")
     value = world * ncell / (ms * 1e-3)
     status = outs["status"][0].cpu().numpy()
     counters = outs["counters"].cpu().numpy().astype(np.float64)
@@ -530,11 +551,7 @@ def main() -> None:
     t0 = time.perf_counter()
     for _ in range(args.steps):
         g.solve_host_ptrs(ncell, hp.data_ptr(), ht.data_ptr(), hz.data_ptr(), hptrs)
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if world > 1:
-        tt_ = torch.tensor([e2e_s], device="cuda")
-        torch.distributed.all_reduce(tt_, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(tt_.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world, "cuda")
     e2e = {"value": world * ncell / e2e_s, "unit": "flashes/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
 
     # per-stage device times (separate instrumented pass) for the roofline
