@@ -209,8 +209,9 @@ int mpmc_gpu_flash_solve_device_noalloc(mpmc_gpu_flash* handle, int64_t n_cells,
  *   [0] FP32 trial blocks per SM        [1] FP32 attempt blocks per SM
  *   [2] FP64 trial-item blocks per SM   [3] FP64 attempt and polish blocks per SM
  *   [4] per-cell kernel blocks per SM   [5] item form: bit 0 feed trials, bit 1
- *       review trials, bit 2 attempts, bit 3 polish run one item per thread
- *       instead of one per lane group
+ *       review trials, bit 2 attempts run one item per thread instead of one
+ *       per lane group; the polish runs one cell per thread with bit 3, one per
+ *       lane group with bit 4 (default: per thread up to 12 components)
  *   [6] successive-substitution -> Newton switch: the FP32 |r| (in units of
  *       1e-6) at which the FP32 ln K iteration hands over to the FP64 polish
  * 0 selects the default (occupancy-derived residency, lane-group items,

@@ -37,7 +37,7 @@ KNOBS = [
     ("fp64_trial_blocks_per_sm", 2, [1, 4]),
     ("fp64_attempt_and_polish_blocks_per_sm", 3, [1, 4]),
     ("cell_blocks_per_sm", 4, [4, 8]),
-    ("item_form", 5, [8]),          # 8: polish one cell per thread
+    ("item_form", 5, [8, 16]),      # polish one cell per thread (8) or per lane group (16)
     ("ss_switch_1e6", 6, [10, 50]),  # FP32 |r| handover at 1e-5 or 5e-5 (default 2e-5)
 ]
 

@@ -136,7 +136,10 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     const float ss_switch = shape.ss_switch > 0.f ? shape.ss_switch : 2e-5f;
     split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t, ss_switch);
     mark();
-    if (shape.item_form & 8) polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+    // polish: one cell per thread up to 12 components (its per-cell arrays
+    // still fit the cache), one cell per lane group above
+    const bool lane_polish = (shape.item_form & 8) ? true : ((shape.item_form & 16) ? false : NM <= 12);
+    if (lane_polish) polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
     else w64::polishw_kernel<NM, w64::kSeg<NM>><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t, out);
     mark();
     if (shape.item_form & 4) split64_kernel<NM><<<sms * s64_res, 64, 0, stream>>>(d_mix, ws, p, t);

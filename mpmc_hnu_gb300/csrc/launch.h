@@ -55,8 +55,10 @@ struct BatchedShape {
     int s64_blocks_per_sm;    // FP64 attempt items (64 threads per block)
     int cell_blocks_per_sm;   // per-cell FP64 kernels (polish, decide, ...; 64 threads per block)
     cudaEvent_t* events;  // optional: kBatchedStages + 1 events recorded around the stages
-    int item_form;        // FP64 item kernels: bit 0 feed trials, bit 1 review trials, bit 2 attempts,
-                          // bit 3 polish run one item per lane when set, one item per warp when clear
+    int item_form;        // FP64 item kernels: bit 0 feed trials, bit 1 review trials, bit 2 attempts
+                          // run one item per thread when set, one per lane group when clear; the
+                          // polish runs one cell per thread with bit 3, per lane group with bit 4,
+                          // and by component capacity (thread up to 12) with neither
     float ss_switch;      // FP32 |r| at which successive substitution hands over to the FP64
                           // Newton polish (0 = 2e-5)
 };

@@ -797,59 +797,111 @@ __global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict_
 template <int NM>
 struct PolishScratch {
     fp64::SplitState<NM> st, nx;
-    double lnk[NM], e[NM], num[NM], J[NM * NM], d[NM], other[NM];
-    double jl[(NM + 1) * (NM + 2)], jv[(NM + 1) * (NM + 2)];
+    double lnk[NM], e[NM], num[NM], J[NM * NM], d[NM];
+    double sl[NM], sv[NM];  // mixing row sums of the two phases
     int piv[NM];
 };
 
-// dF/dln K of F = ln x - ln y + ln phi_L(x) - ln phi_V(y) at a Rachford-Rice
-// state: the RR linearisation of detail/pt_sensitivity_detail.hpp:291-345 (no
-// feed variation) composed with the forward-AD full-chart ln phi Jacobians.
+// Closed-form full-chart d ln phi_i / d x_j = cs_i s_j + cb_i b_j + ca a_ij of
+// one PR76 phase at composition x with root Z (mole fractions as independent
+// variables, the chart of pr76_phase_ad.hpp:57-122): with r_i = b_i/b,
+// q_i = 2 s_i/a - r_i, G = A ln((Z+(1+sqrt2)B)/(Z+(1-sqrt2)B)) / (2 sqrt2 B),
+// ln phi_i = r_i (Z-1) - ln(Z-B) - q_i G, dA/dx_j = 2 s_j p/(RT)^2,
+// dB/dx_j = b_j p/RT and dZ from the cubic's implicit derivative.
 template <int NM>
-__device__ bool equilibrium_jacobian(const Mixture& m, const fp64::Cell<NM>& c, PolishScratch<NM>& s) {
+__device__ bool phi_coefficients(const Mixture& m, fp64::Cell<NM>& c, const double* x, double Z, double* s_out,
+                                 double* cs, double* cb, double& ca) {
+    double amix, bmix, A, B;
+    if (!fp64::mix(m, c, x, amix, bmix) || !fp64::coefficients(c.p, c.t, amix, bmix, A, B)) return false;
+    const int n = c.n;
+    const double sqrt2 = 1.4142135623730951;
+    const double prt = c.p / (kR * c.t);
+    const double p1 = prt / (kR * c.t), p2 = prt;
+    const double d1 = Z + (1.0 + sqrt2) * B, d2 = Z + (1.0 - sqrt2) * B;
+    const double L = log(d1 / d2);
+    const double G = A * L / (2.0 * sqrt2 * B);
+    const double fz = (3.0 * Z - 2.0 * (1.0 - B)) * Z + (A - 3.0 * B * B - 2.0 * B);
+    const double fa = Z - B;
+    const double fb = Z * Z - (6.0 * B + 2.0) * Z - A + 2.0 * B + 3.0 * B * B;
+    const double zs = -2.0 * fa * p1 / fz, zb = -fb * p2 / fz;
+    const double inv = 1.0 / d1 - 1.0 / d2;
+    const double ls = zs * inv, lb = zb * inv + p2 * ((1.0 + sqrt2) / d1 - (1.0 - sqrt2) / d2);
+    const double gs = (2.0 * p1 * L + A * ls) / (2.0 * sqrt2 * B), gb = A * lb / (2.0 * sqrt2 * B) - G * p2 / B;
+    ca = -2.0 * G / amix;
+    bool ok = isfinite(ca);
+    for (int i = 0; i < n; ++i) {
+        const double si = c.sums[i];
+        s_out[i] = si;
+        const double r = m.b[i] / bmix, q = 2.0 * si / amix - r;
+        cs[i] = r * zs - zs / (Z - B) + 4.0 * G * si / (amix * amix) - q * gs;
+        cb[i] = -r * (Z - 1.0) / bmix + r * zb - (zb - p2) / (Z - B) - G * r / bmix - q * gb;
+        ok = ok && isfinite(cs[i]) && isfinite(cb[i]);
+    }
+    return ok;
+}
+
+// dF/dln K of F = ln x - ln y + ln phi_L(x) - ln phi_V(y) on the RR manifold at
+// fixed feed (the RR linearisation of detail/pt_sensitivity_detail.hpp:291-345):
+// dbeta_j = (x_j y_j / z_j)/h, h = sum_k (y_k - x_k)^2 / z_k, and
+//   J_ij = -delta_ij - (x_j y_j / z_j) [(U^L_i - U^V_i)/h + beta PhiL_ij + (1-beta) PhiV_ij]
+// with U^L_i = sum_k PhiL_ik x_k g_k, U^V_i = sum_k PhiV_ik y_k g_k,
+// g_k = (y_k - x_k)/z_k, Phi the closed-form d ln phi / d x of each phase.
+template <int NM>
+__device__ bool equilibrium_jacobian(const Mixture& m, fp64::Cell<NM>& c, PolishScratch<NM>& s) {
     const int n = c.n;
     const fp64::SplitState<NM>& st = s.st;
-    if (!ad::phase_jacobian<NM>(m, n, c.p, c.t, st.x, st.branch_l, s.jl) ||
-        !ad::phase_jacobian<NM>(m, n, c.p, c.t, st.y, st.branch_v, s.jv))
+    double csl[NM], cbl[NM], csv[NM], cbv[NM], cal, cav;
+    if (!phi_coefficients(m, c, st.x, st.z_l, s.sl, csl, cbl, cal) ||
+        !phi_coefficients(m, c, st.y, st.z_v, s.sv, csv, cbv, cav))
         return false;
-    double h = 0.0;
-    for (int i = 0; i < n; ++i)
-        if (c.z[i] > 0.0) h += (st.y[i] - st.x[i]) * (st.y[i] - st.x[i]) / c.z[i];
+    double h = 0.0, s1l = 0.0, s2l = 0.0, s1v = 0.0, s2v = 0.0;
+    double xg[NM], yg[NM];
+    for (int k = 0; k < n; ++k) {
+        xg[k] = yg[k] = 0.0;
+        if (c.z[k] == 0.0) continue;
+        const double g = (st.y[k] - st.x[k]) / c.z[k];
+        h += (st.y[k] - st.x[k]) * g;
+        xg[k] = st.x[k] * g;
+        yg[k] = st.y[k] * g;
+        s1l += s.sl[k] * xg[k];
+        s2l += m.b[k] * xg[k];
+        s1v += s.sv[k] * yg[k];
+        s2v += m.b[k] * yg[k];
+    }
     if (!(h > 0.0) || !isfinite(h)) return false;
-    const int cols = n + 2;
-    for (int j = 0; j < n; ++j) {
-        if (c.z[j] == 0.0) {
-            for (int i = 0; i < n; ++i) s.J[i * n + j] = i == j ? 1.0 : 0.0;
+    for (int i = 0; i < n; ++i) {
+        if (c.z[i] == 0.0) {
+            for (int j = 0; j < n; ++j) s.J[i * n + j] = i == j ? 1.0 : 0.0;
             continue;
         }
-        const double db = (st.x[j] * st.y[j] / c.z[j]) / h;
-        double dx[NM], dy[NM];
-        for (int i = 0; i < n; ++i) {
-            if (c.z[i] == 0.0) {
-                dx[i] = dy[i] = 0.0;
-                continue;
-            }
-            const double dlk = i == j ? 1.0 : 0.0;
-            const double dlx = -((st.y[i] - st.x[i]) / c.z[i]) * db - st.beta * (st.y[i] / c.z[i]) * dlk;
-            dx[i] = st.x[i] * dlx;
-            dy[i] = st.y[i] * (dlx + dlk);
+        // row i of a_ij = sqrt(a_i a_j)(1 - k_ij), a_ii = a_i
+        double tl = 0.0, tv = 0.0;
+        for (int k = 0; k < n; ++k) {
+            const double aik = k == i ? c.a[i] : (c.root[i] * m.factor[i * n + k]) * c.root[k];
+            tl += aik * xg[k];
+            tv += aik * yg[k];
         }
-        for (int i = 0; i < n; ++i) {
-            if (c.z[i] == 0.0) {
-                s.J[i * n + j] = i == j ? 1.0 : 0.0;
+        const double u = ((csl[i] * s1l + cbl[i] * s2l + cal * tl) - (csv[i] * s1v + cbv[i] * s2v + cav * tv)) / h;
+        for (int j = 0; j < n; ++j) {
+            if (c.z[j] == 0.0) {
+                s.J[i * n + j] = 0.0;
                 continue;
             }
-            double v = dx[i] / st.x[i] - dy[i] / st.y[i];
-            for (int k = 0; k < n; ++k) v += s.jl[(1 + i) * cols + 2 + k] * dx[k] - s.jv[(1 + i) * cols + 2 + k] * dy[k];
-            s.J[i * n + j] = v;
+            const double aij = j == i ? c.a[i] : (c.root[i] * m.factor[i * n + j]) * c.root[j];
+            const double phil = csl[i] * s.sl[j] + cbl[i] * m.b[j] + cal * aij;
+            const double phiv = csv[i] * s.sv[j] + cbv[i] * m.b[j] + cav * aij;
+            const double w = st.x[j] * st.y[j] / c.z[j];
+            s.J[i * n + j] = (i == j ? -1.0 : 0.0) - w * (u + st.beta * phil + (1.0 - st.beta) * phiv);
         }
     }
+    for (int k = 0; k < n * n; ++k)
+        if (!isfinite(s.J[k])) return false;
     return true;
 }
 
 // Newton polish of ln K from the FP32 solution: FP64 residual F(ln K) (RR +
-// role phases, pt_split.hpp:300-341) and the exact FP64 Jacobian taken at the
-// first FP64 state (chord iterations).  On success `s.st` holds the FP64 state
+// role phases, pt_split.hpp:300-341) and the exact FP64 Jacobian in closed form
+// taken at the first FP64 state (chord iterations).  On success `s.st` holds the FP64 state
 // at |F| <= 1e-13, or at the point where F stopped decreasing below 1e-11.
 template <int NM>
 __device__ bool polish_split(const Mixture& m, fp64::Cell<NM>& c64, PolishScratch<NM>& s) {
