@@ -41,6 +41,7 @@ size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell) {
     ws.ref_z = reinterpret_cast<double*>(take(sizeof(double) * nc));
     ws.tw = reinterpret_cast<float*>(take(sizeof(float) * (NM + 4) * NM * nc));
     ws.tclass = reinterpret_cast<signed char*>(take((NM + 4) * nc));
+    ws.titer = reinterpret_cast<short*>(take(sizeof(short) * (NM + 4) * nc));
     ws.att_lnk = reinterpret_cast<float*>(take(sizeof(float) * batched::kMaxAttempts * NM * nc));
     ws.att_gibbs = reinterpret_cast<float*>(take(sizeof(float) * batched::kMaxAttempts * nc));
     ws.att_class = reinterpret_cast<signed char*>(take(batched::kMaxAttempts * nc));

@@ -40,6 +40,15 @@ constexpr int kFp64EvalRow = cRootIters;
 // Flag added to an FP32 trial class when its descent converges too slowly for
 // the reference's FP64 run to be sure of finishing within 512 iterations.
 constexpr int kSlowFlag = 8;
+// A descent whose projected FP64 iteration count (from its FP32 contraction)
+// exceeds this is re-run exactly from its start.  Below it, an undecided
+// trial continues in FP64 from its FP32 end point with the iterations left of
+// the reference's 512; the projection overstates the count near the FP32
+// rounding floor, so the margin to the limit is on the safe side.
+#ifndef MPMC_SLOW_PROJECTION
+#define MPMC_SLOW_PROJECTION 448.f
+#endif
+constexpr float kSlowProjection = MPMC_SLOW_PROJECTION;
 
 // Queue/counter slots in Workspace::counters.
 enum Slot : int {
@@ -95,6 +104,7 @@ struct Workspace {
     double* ref_z;          // [ncell]
     float* tw;              // [(NM+4) * NM * ncell] trial end compositions
     signed char* tclass;    // [(NM+4) * ncell] trial classes
+    short* titer;           // [(NM+4) * ncell] FP32 descent iterations of the trial
     float* att_lnk;         // [kMaxAttempts * NM * ncell]
     float* att_gibbs;       // [kMaxAttempts * ncell]
     signed char* att_class; // [kMaxAttempts * ncell]
@@ -417,7 +427,7 @@ __device__ int trial_classify(const TrialLane<NM>& L) {
     // (the projection is only a screen: near the FP32 noise floor the measured
     // contraction understates the FP64 rate, so no trial is declared
     // "iteration_limit" from it without the FP64 run)
-    const int slow = (L.iter >= 400 || projected_fp64_iterations(L) > 320.f) ? kSlowFlag : 0;
+    const int slow = (L.iter >= 400 || projected_fp64_iterations(L) > kSlowProjection) ? kSlowFlag : 0;
     if (L.point.stat > 10.f * so.stat_tol) return fp32::tMarginal | slow;
     for (int r = 0; r < L.nrefs; ++r) {
         float dist = 0.f;
@@ -447,6 +457,7 @@ __global__ void __launch_bounds__(128) trials32_kernel(const Mixture* __restrict
                 const int cls = L.result >= 0 ? L.result : trial_classify(L);
                 const int64_t c = L.c;
                 ws.tclass[idx(L.k, ws.ncell, c)] = static_cast<signed char>(cls);
+                ws.titer[idx(L.k, ws.ncell, c)] = static_cast<short>(L.iter);
                 for (int i = 0; i < L.cell.n; ++i) ws.tw[idx(L.k * NM + i, ws.ncell, c)] = L.point.w[i];
                 atomicAdd(&ws.counters_out[idx(review ? cFinalEvals : cInitEvals, ws.ncell, c)], L.cell.evals);
                 atomicAdd(&ws.counters_out[idx(cTrialIters, ws.ncell, c)], L.iter);

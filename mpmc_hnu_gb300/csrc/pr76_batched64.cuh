@@ -77,6 +77,7 @@ __device__ void t64_begin(const Mixture& m, const Workspace& ws, const double* p
     if (L.mode == mFeedRerun || L.mode == mReviewRerun) {
         fp64::make_start(c, L.k, active, ex0, ex1, auto_starts(active), L.next.w);
     } else {
+        L.iter = ws.titer[idx(L.k, ws.ncell, L.c)];  // the FP32 iterations count against the 512
         double sum = 0.0, cs = 0.0;
         for (int i = 0; i < n; ++i) {
             L.next.w[i] = c.z[i] > 0.0 ? static_cast<double>(ws.tw[idx(L.k * NM + i, ws.ncell, L.c)]) : 0.0;

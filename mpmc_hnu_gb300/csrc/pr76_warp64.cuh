@@ -446,9 +446,11 @@ __device__ int tpd(const WCell<NM, S>& c, double phiw, double phiref, Tpd& pt) {
 __device__ __forceinline__ bool tpd_negative(const Tpd& p, double tol) { return p.value < -tol - p.guard; }
 
 // A TPD trial from `start` with the reference's descent and stopping rules
-// (pt_stability.hpp:343-457); provider calls are charged to `row`.
+// (pt_stability.hpp:343-457); provider calls are charged to `row`.  `done`
+// iterations of the reference's 512 were already made (in FP32) to reach
+// `start`.
 template <int NM, int S>
-__device__ int trial(WCell<NM, S>& c, double start, double ref, double tol, int row, Tpd& point) {
+__device__ int trial(WCell<NM, S>& c, double start, double ref, double tol, int row, Tpd& point, int done) {
     Tpd next;
     next.w = start;
     {
@@ -460,7 +462,7 @@ __device__ int trial(WCell<NM, S>& c, double start, double ref, double tol, int 
         next.smooth = smooth;
         point = next;
     }
-    int iter = 0;
+    int iter = done;
     for (;;) {
         if (tpd_negative(point, tol)) return fp64::kNegativeTpd;
         if (!point.smooth) return fp64::kNonsmooth;
@@ -945,7 +947,8 @@ __global__ void __launch_bounds__(128) trials64w_kernel(const Mixture* __restric
                 tol = 1e-10;
             }
             double w = 0.0;
-            if (mode == mFeedRerun || mode == mReviewRerun) {
+            const bool rerun = mode == mFeedRerun || mode == mReviewRerun;
+            if (rerun) {
                 // trial starts (pt_stability.hpp:294-310, extra starts :263-272)
                 const int n_auto = auto_starts(active);
                 if (k >= n_auto) {
@@ -968,7 +971,7 @@ __global__ void __launch_bounds__(128) trials64w_kernel(const Mixture* __restric
             if (!cell.comp) w = 0.0;
             if (!ok) status = fp64::kPropertyFailure;
             else if (wany<S>(cell.act && w == 0.0)) status = fp64::kUnrepresentableComposition;
-            else status = trial(cell, w, ref, tol, row, point);
+            else status = trial(cell, w, ref, tol, row, point, rerun ? 0 : ws.titer[idx(k, ws.ncell, c)]);
         }
         if (lane == 0) ws.t64_status[idx(k, ws.ncell, c)] = static_cast<signed char>(status);
         if (!review && status == fp64::kNegativeTpd && lane < m.n)
