@@ -1,22 +1,21 @@
-// Forward-mode AD on the device and the implicit two-phase sensitivity.
+// Implicit two-phase sensitivities on the device.
 //
-//  * Dual<K>: value + K tangent lanes (the device counterpart of the
-//    reference's mpmc::ad::Dual<T,N>, modules/ad/include/mpmc/ad/dual.hpp:80).
-//  * phase_jacobian: d[Z, ln phi_0..]/d[p, T, x_0..x_{n-1}] of one phase at a
-//    fixed root index, i.e. Pr76PhaseAdWorkspace::value_and_jacobian_full
+//  * phase_jacobian_closed: d[Z, ln phi_0..]/d[p, T, x_0..x_{n-1}] of one phase
+//    at a fixed root index, the quantity of
+//    Pr76PhaseAdWorkspace::value_and_jacobian_full
 //    (modules/thermodynamics/include/mpmc/thermodynamics/pr76_phase_ad.hpp:57-122),
-//    computed in ceil((n+2)/K) passes of K lanes with the first-order root IFT
-//    of pr76_phase.hpp:208-222.
-//  * sensitivity: differentiate_pr76_pt_vle
+//    in closed form (the reference evaluates it by forward AD with Dual
+//    numbers through the same functions; the two agree to rounding).
+//  * sensitivity_cell: differentiate_pr76_pt_vle
 //    (modules/flash/include/mpmc/flash/pr76_sensitivity.hpp:51-390).  The
 //    reference differentiates F(lnK, p, T, z) = ln x - ln y + ln phi_L(x) -
 //    ln phi_V(y) through its RR linearisation
 //    (detail/pt_sensitivity_detail.hpp:257-355) with Dual<double,4> blocks over
 //    all 2n+1 variables; here the same derivatives are assembled by the chain
-//    rule from the two per-phase full-chart Jacobians (the reduced last
-//    fraction x_{n-1} = 1 - sum x_j contributes exactly the "full column minus
-//    last column" combination), followed by the same LU with partial pivoting,
-//    reciprocal condition, backward-error and normalisation checks
+//    rule from the two per-phase Jacobians taken in the reference's reduced
+//    chart (the last fraction x_{n-1} = 1 - sum x_j, i.e. "column minus last
+//    column"), followed by the same LU with partial pivoting, reciprocal
+//    condition, backward-error and normalisation checks
 //    (pt_sensitivity_detail.hpp:364-471, pr76_sensitivity.hpp:213-385) and the
 //    closure dZ, d(rho) of pr76_thermodynamic_closure.hpp:279-337.
 #pragma once
@@ -26,202 +25,94 @@
 namespace pr76 {
 namespace ad {
 
-template <int K>
-struct Dual {
-    double v;
-    double d[K];
-};
-
-template <int K>
-__device__ __forceinline__ Dual<K> cst(double v) {
-    Dual<K> r;
-    r.v = v;
-#pragma unroll
-    for (int k = 0; k < K; ++k) r.d[k] = 0.0;
-    return r;
-}
-template <int K>
-__device__ __forceinline__ Dual<K> operator+(const Dual<K>& a, const Dual<K>& b) {
-    Dual<K> r;
-    r.v = a.v + b.v;
-#pragma unroll
-    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] + b.d[k];
-    return r;
-}
-template <int K>
-__device__ __forceinline__ Dual<K> operator-(const Dual<K>& a, const Dual<K>& b) {
-    Dual<K> r;
-    r.v = a.v - b.v;
-#pragma unroll
-    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] - b.d[k];
-    return r;
-}
-template <int K>
-__device__ __forceinline__ Dual<K> operator*(const Dual<K>& a, const Dual<K>& b) {
-    Dual<K> r;
-    r.v = a.v * b.v;
-#pragma unroll
-    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
-    return r;
-}
-template <int K>
-__device__ __forceinline__ Dual<K> operator/(const Dual<K>& a, const Dual<K>& b) {
-    Dual<K> r;
-    r.v = a.v / b.v;
-    const double inv = 1.0 / b.v;
-#pragma unroll
-    for (int k = 0; k < K; ++k) r.d[k] = (a.d[k] - r.v * b.d[k]) * inv;
-    return r;
-}
-template <int K>
-__device__ __forceinline__ Dual<K> scale(const Dual<K>& a, double s) {
-    Dual<K> r;
-    r.v = a.v * s;
-#pragma unroll
-    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * s;
-    return r;
-}
-template <int K>
-__device__ __forceinline__ Dual<K> shift(const Dual<K>& a, double s) {
-    Dual<K> r = a;
-    r.v = a.v + s;
-    return r;
-}
-template <int K>
-__device__ __forceinline__ Dual<K> dsqrt(const Dual<K>& a) {
-    Dual<K> r;
-    r.v = sqrt(a.v);
-    const double f = 0.5 / r.v;
-#pragma unroll
-    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * f;
-    return r;
-}
-template <int K>
-__device__ __forceinline__ Dual<K> dlog(const Dual<K>& a) {
-    Dual<K> r;
-    r.v = log(a.v);
-    const double f = 1.0 / a.v;
-#pragma unroll
-    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * f;
-    return r;
-}
-template <int K>
-__device__ __forceinline__ Dual<K> dlog1p(const Dual<K>& a) {
-    Dual<K> r;
-    r.v = log1p(a.v);
-    const double f = 1.0 / (1.0 + a.v);
-#pragma unroll
-    for (int k = 0; k < K; ++k) r.d[k] = a.d[k] * f;
-    return r;
-}
-template <int K>
-__device__ __forceinline__ Dual<K> log1p_over_x(const Dual<K>& u) {
-    if (fabs(u.v) <= 0.125) {
-        Dual<K> value = cst<K>(-1.0 / 20.0);
-        for (int k = 18; k >= 0; --k) value = shift(u * value, ((k % 2 == 0) ? 1.0 : -1.0) / static_cast<double>(k + 1));
-        return value;
-    }
-    return dlog1p(u) / u;
-}
-
-// Columns [first, first + K) of d[Z, ln phi]/d[p, T, x_0..x_{n-1}] at a fixed
-// root index; `jac` is row-major (n+1) x (n+2).  Returns false if the root set
-// no longer resolves or the selected root is not derivative-valid.
-// The primal of every chunk is the same, so the root set is solved by the
-// first chunk and reused (`have_roots`).
-template <int NM, int K>
-__device__ bool phase_jacobian_chunk(const Mixture& m, int n, double p, double t, const double* x, int branch,
-                                     int first, double* jac, fp64::RootSet& rs, bool have_roots) {
-    const int cols = n + 2;
-    auto seed = [&](int col, double v) {
-        Dual<K> r = cst<K>(v);
-#pragma unroll
-        for (int k = 0; k < K; ++k) r.d[k] = (first + k == col) ? 1.0 : 0.0;
-        return r;
-    };
-    const Dual<K> P = seed(0, p), T = seed(1, t);
-    Dual<K> xs[NM], a[NM], root[NM], sums[NM];
-    Dual<K> attraction = cst<K>(0.0), covolume = cst<K>(0.0);
-    const Dual<K> st = dsqrt(T);
-    for (int i = 0; i < n; ++i) {
-        xs[i] = seed(2 + i, x[i]);
-        const Dual<K> reduced_root = scale(st, 1.0 / m.sqrt_tc[i]);
-        // pr76_pure.hpp:153-159: bracket = 1 + kappa (1 - sqrt(T)/sqrt(Tc)), a = (bracket ac) bracket
-        Dual<K> bracket = shift(scale(reduced_root, -m.kappa[i]), 1.0 + m.kappa[i]);
-        bracket.v = 1.0 + m.kappa[i] * (1.0 - st.v / m.sqrt_tc[i]);
-        a[i] = scale(bracket, m.ac[i]) * bracket;
-        attraction = attraction + (xs[i] * a[i]) * xs[i];
-        covolume = covolume + scale(xs[i], m.b[i]);
-        sums[i] = xs[i] * a[i];
-        root[i] = dsqrt(a[i]);
-    }
-    for (int i = 0; i < n; ++i)
-        for (int j = i + 1; j < n; ++j) {
-            const double f = m.factor[i * n + j];
-            const Dual<K> cross = scale((xs[i] * root[i]) * (xs[j] * root[j]), f);
-            attraction = attraction + cross;
-            attraction = attraction + cross;
-            const Dual<K> aij = scale(root[i], f) * root[j];
-            sums[i] = sums[i] + xs[j] * aij;
-            sums[j] = sums[j] + xs[i] * aij;
-        }
-    const Dual<K> rt = scale(T, kR);
-    const Dual<K> prt = P / rt;
-    const Dual<K> A = (attraction / rt) * prt;
-    const Dual<K> B = covolume * prt;
-    if (!have_roots) {
-        int dummy = 0;
-        fp64::solve_roots(A.v, B.v, rs, dummy);
-    }
-    if (rs.status != fp64::kRootSuccess || branch >= rs.count || !rs.r[branch].derivative_valid) return false;
-    // root IFT, pr76_phase.hpp:214-221
-    const double sc = rs.scale;
-    const double y0 = rs.r[branch].free_volume / sc;
-    const Dual<K> bs = scale(B, 1.0 / sc);
-    const double inv = 1.0 / sc;
-    const Dual<K> c2 = shift(scale(bs, 4.0), -inv);
-    const Dual<K> c1 = scale(scale(A, 1.0 / sc), 1.0 / sc) + scale(bs, 2.0) * bs - scale(bs, 4.0 * inv);
-    const Dual<K> c0 = scale(scale(bs, -2.0) * bs, inv);
-    const Dual<K> residual = scale(shift(scale(shift(c2, y0), y0) + c1, 0.0), y0) + c0;
-    const double dh = (3.0 * y0 + 2.0 * c2.v) * y0 + c1.v;
-    Dual<K> fv = cst<K>(rs.r[branch].free_volume);
-#pragma unroll
-    for (int k = 0; k < K; ++k) fv.d[k] = -(residual.d[k] / dh) * sc;
-    const Dual<K> z = fv + B;
-    const double sqrt2 = 1.4142135623730951;
-    const Dual<K> denominator = fv + scale(B, 2.0 - sqrt2);
-    const Dual<K> u = scale(B / denominator, 2.0 * sqrt2);
-    const Dual<K> log_factor = log1p_over_x(u) / denominator;
-    Dual<K> zm1 = shift(z, -1.0);
-    Dual<K> log_free = dlog(fv);
-    if (fabs(zm1.v) < 0.25 && B.v < 0.125) {
-        const Dual<K> bz = B / z;
-        zm1 = B / fv - (A / z) / (shift(scale(bz, 2.0), 1.0) - bz * bz);
-        log_free = dlog1p(zm1 - B);
-    }
-#pragma unroll
-    for (int k = 0; k < K; ++k)
-        if (first + k < cols) jac[0 * cols + first + k] = z.d[k];
-    for (int i = 0; i < n; ++i) {
-        const Dual<K> ratio = cst<K>(m.b[i]) / covolume;
-        const Dual<K> coefficient = ((scale(sums[i], 2.0) - attraction * ratio) / rt) * prt;
-        const Dual<K> lp = ratio * zm1 - log_free - coefficient * log_factor;
-        if (!isfinite(lp.v)) return false;
-#pragma unroll
-        for (int k = 0; k < K; ++k)
-            if (first + k < cols) jac[(1 + i) * cols + first + k] = lp.d[k];
-    }
-    return isfinite(z.v);
-}
-
+// d[Z, ln phi_0..]/d[p, T, x_0..x_{n-1}] of one phase in closed form, at a
+// fixed root index (the quantity of Pr76PhaseAdWorkspace::
+// value_and_jacobian_full, pr76_phase_ad.hpp:57-122; rows Z, ln phi_i; mole
+// fractions as independent variables).  With r_i = b_i/b, q_i = 2 s_i/a - r_i
+// and G = A ln((Z+(1+sqrt2)B)/(Z+(1-sqrt2)B)) / (2 sqrt2 B),
+//   ln phi_i = r_i (Z - 1) - ln(Z - B) - q_i G
+// and Z from the cubic's implicit derivative dZ = -(F_A dA + F_B dB)/F_Z.
+// Directions: p (dA = A/p, dB = B/p), T (dA = A (a'/a - 2/T), dB = -B/T,
+// ds_i = u_i s_i + sum_j a_ij u_j x_j, a' = 2 sum_i u_i x_i s_i with
+// u_i = a_i'/(2 a_i) from a_i = a_c,i (1 + kappa_i (1 - sqrt(T/Tc_i)))^2),
+// x_j (dA = 2 s_j p/(RT)^2, dB = b_j p/RT, ds_i = a_ij, da = 2 s_j, db = b_j).
+// Returns false if the roots no longer resolve or the root is not
+// derivative-valid.
 template <int NM>
-__device__ bool phase_jacobian(const Mixture& m, int n, double p, double t, const double* x, int branch,
-                               double* jac) {
-    constexpr int K = 4;
+__device__ bool phase_jacobian_closed(const Mixture& m, fp64::Cell<NM>& c, const double* x, int branch,
+                                      double* jac) {
+    const int n = c.n;
+    const int cols = n + 2;
+    double amix, bmix, A, B;
+    if (!fp64::mix(m, c, x, amix, bmix) || !fp64::coefficients(c.p, c.t, amix, bmix, A, B)) return false;
     fp64::RootSet rs;
-    for (int first = 0; first < n + 2; first += K)
-        if (!phase_jacobian_chunk<NM, K>(m, n, p, t, x, branch, first, jac, rs, first > 0)) return false;
-    for (int k = 0; k < (n + 1) * (n + 2); ++k)
+    int dummy = 0;
+    fp64::solve_roots(A, B, rs, dummy);
+    if (rs.status != fp64::kRootSuccess || branch >= rs.count || !rs.r[branch].derivative_valid) return false;
+    const double Z = rs.r[branch].z;
+    const double sqrt2 = 1.4142135623730951;
+    const double rt = kR * c.t;
+    const double prt = c.p / rt;
+    const double p1 = prt / rt, p2 = prt;  // dA/da, dB/db
+    const double d1 = Z + (1.0 + sqrt2) * B, d2 = Z + (1.0 - sqrt2) * B;
+    const double u = (2.0 * sqrt2) * (B / d2);
+    const double L = fp64::log1p_over_x(u) * u;  // ln(d1 / d2)
+    const double G = A * fp64::log1p_over_x(u) / d2;  // A L / (2 sqrt2 B)
+    const double fz = (3.0 * Z - 2.0 * (1.0 - B)) * Z + (A - 3.0 * B * B - 2.0 * B);
+    const double fa = Z - B;
+    const double fb = Z * Z - (6.0 * B + 2.0) * Z - A + 2.0 * B + 3.0 * B * B;
+    // per-direction helpers (db = 0 for p and T)
+    auto dz_of = [&](double dA, double dB) { return -(fa * dA + fb * dB) / fz; };
+    auto dg_of = [&](double dA, double dB, double dZ) {
+        const double dL = (dZ + (1.0 + sqrt2) * dB) / d1 - (dZ + (1.0 - sqrt2) * dB) / d2;
+        return (dA * L + A * dL) / (2.0 * sqrt2 * B) - G * dB / B;
+    };
+    // temperature terms
+    double uu[NM], tt[NM];
+    double ap = 0.0;
+    const double st = sqrt(c.t);
+    for (int i = 0; i < n; ++i) {
+        const double br = 1.0 + m.kappa[i] * (1.0 - st / m.sqrt_tc[i]);
+        const double dbr = -m.kappa[i] / (2.0 * st * m.sqrt_tc[i]);
+        uu[i] = dbr / br;
+    }
+    for (int i = 0; i < n; ++i) {
+        double ti = 0.0;
+        for (int j = 0; j < n; ++j) {
+            const double aij = j == i ? c.a[i] : (c.root[i] * m.factor[i * n + j]) * c.root[j];
+            ti += aij * uu[j] * x[j];
+        }
+        tt[i] = ti;
+        ap += 2.0 * uu[i] * x[i] * c.sums[i];
+    }
+    const double dAp = A / c.p, dBp = B / c.p;
+    const double dAt = A * (ap / amix - 2.0 / c.t), dBt = -B / c.t;
+    const double dZp = dz_of(dAp, dBp), dZt = dz_of(dAt, dBt);
+    const double dGp = dg_of(dAp, dBp, dZp), dGt = dg_of(dAt, dBt, dZt);
+    const double zs = -2.0 * fa * p1 / fz, zb = -fb * p2 / fz;  // dZ/dx_j = zs s_j + zb b_j
+    jac[0 * cols + 0] = dZp;
+    jac[0 * cols + 1] = dZt;
+    for (int j = 0; j < n; ++j) jac[0 * cols + 2 + j] = zs * c.sums[j] + zb * m.b[j];
+    // composition row coefficients (the polish's closed form)
+    const double inv = 1.0 / d1 - 1.0 / d2;
+    const double ls = zs * inv, lb = zb * inv + p2 * ((1.0 + sqrt2) / d1 - (1.0 - sqrt2) / d2);
+    const double gs = (2.0 * p1 * L + A * ls) / (2.0 * sqrt2 * B), gb = A * lb / (2.0 * sqrt2 * B) - G * p2 / B;
+    const double ca = -2.0 * G / amix;
+    for (int i = 0; i < n; ++i) {
+        const double si = c.sums[i];
+        const double r = m.b[i] / bmix, q = 2.0 * si / amix - r;
+        double* row = jac + (1 + i) * cols;
+        row[0] = r * dZp - (dZp - dBp) / (Z - B) - q * dGp;
+        const double dqt = 2.0 * (uu[i] * si + tt[i]) / amix - 2.0 * si * ap / (amix * amix);
+        row[1] = r * dZt - (dZt - dBt) / (Z - B) - dqt * G - q * dGt;
+        const double cs = r * zs - zs / (Z - B) + 4.0 * G * si / (amix * amix) - q * gs;
+        const double cb = -r * (Z - 1.0) / bmix + r * zb - (zb - p2) / (Z - B) - G * r / bmix - q * gb;
+        for (int j = 0; j < n; ++j) {
+            const double aij = j == i ? c.a[i] : (c.root[i] * m.factor[i * n + j]) * c.root[j];
+            row[2 + j] = cs * c.sums[j] + cb * m.b[j] + ca * aij;
+        }
+    }
+    for (int k = 0; k < (n + 1) * cols; ++k)
         if (!isfinite(jac[k])) return false;
     return true;
 }
@@ -348,7 +239,7 @@ __device__ int sensitivity_cell(const Mixture& m, fp64::Cell<NM>& c, const doubl
     const int bl = role_branch(m, c, xb, false);
     const int bv = role_branch(m, c, yb, true);
     if (bl < 0 || bv < 0) return sPropertyFailure;
-    if (!phase_jacobian<NM>(m, n, c.p, c.t, xb, bl, s.jl) || !phase_jacobian<NM>(m, n, c.p, c.t, yb, bv, s.jv))
+    if (!phase_jacobian_closed<NM>(m, c, xb, bl, s.jl) || !phase_jacobian_closed<NM>(m, c, yb, bv, s.jv))
         return sPropertyFailure;
     const int cols = n + 2;
     // RR linearisation for every variable v of [lnK (n), p, T, z_0..z_{n-2}]

@@ -74,3 +74,52 @@ def test_closed_form_matches_central_differences():
                 e[j] = h
                 fd[:, j] = (_lnphi(x + e, which, T, P, aij, bi) - _lnphi(x - e, which, T, P, aij, bi)) / (2 * h)
             assert np.abs(got - fd).max() <= 1e-7 * np.abs(fd).max(), (n, which)
+
+
+def _pt_closed_form(x, which, T, P, tc, pc, om, k):
+    """d[Z, ln phi]/d[p, T] at fixed x (phase_jacobian_closed in pr76_ad.cuh)."""
+    kap = 0.37464 + om * (1.54226 - 0.26992 * om)
+    ac = 0.45724 * (R * tc) ** 2 / pc
+    bi = 0.07780 * R * tc / pc
+    br = 1 + kap * (1 - np.sqrt(T) / np.sqrt(tc))
+    ai = ac * br ** 2
+    aij = np.sqrt(np.outer(ai, ai)) * (1 - k)
+    s, a, b, A, B, Z = _state(x, which, T, P, aij, bi)
+    uu = (-kap / (2 * np.sqrt(T) * np.sqrt(tc))) / br
+    tt = aij @ (uu * x)
+    ap = 2 * np.sum(uu * x * s)
+    d1, d2 = Z + (1 + SQ2) * B, Z + (1 - SQ2) * B
+    L = np.log(d1 / d2)
+    G = A * L / (2 * SQ2 * B)
+    fz = (3 * Z - 2 * (1 - B)) * Z + (A - 3 * B * B - 2 * B)
+    fa, fb = Z - B, Z * Z - (6 * B + 2) * Z - A + 2 * B + 3 * B * B
+    r, q = bi / b, 2 * s / a - bi / b
+    out = []
+    for dA, dB, dq in ((A / P, B / P, 0 * s), (A * (ap / a - 2 / T), -B / T, 2 * (uu * s + tt) / a - 2 * s * ap / a ** 2)):
+        dZ = -(fa * dA + fb * dB) / fz
+        dL = (dZ + (1 + SQ2) * dB) / d1 - (dZ + (1 - SQ2) * dB) / d2
+        dG = (dA * L + A * dL) / (2 * SQ2 * B) - G * dB / B
+        out.append(np.concatenate([[dZ], r * dZ - (dZ - dB) / (Z - B) - dq * G - q * dG]))
+    return np.array(out).T, aij, bi
+
+
+def test_pressure_and_temperature_columns_match_central_differences():
+    for n, seed, T, P in ((3, 1, 300.0, 3e6), (6, 5, 330.0, 6e6)):
+        tc, pc, om, k = _model(n, seed)
+        x = np.random.default_rng(seed + 1).dirichlet(np.ones(n))
+        for which in "lv":
+            got, _, _ = _pt_closed_form(x, which, T, P, tc, pc, om, k)
+
+            def zl(TT, PP):
+                kap = 0.37464 + om * (1.54226 - 0.26992 * om)
+                ac = 0.45724 * (R * tc) ** 2 / pc
+                bi = 0.07780 * R * tc / pc
+                ai = ac * (1 + kap * (1 - np.sqrt(TT / tc))) ** 2
+                aij = np.sqrt(np.outer(ai, ai)) * (1 - k)
+                Z = _state(x, which, TT, PP, aij, bi)[5]
+                return np.concatenate([[Z], _lnphi(x, which, TT, PP, aij, bi)])
+
+            fd_p = (zl(T, P * (1 + 1e-6)) - zl(T, P * (1 - 1e-6))) / (2e-6 * P)
+            fd_t = (zl(T * (1 + 1e-6), P) - zl(T * (1 - 1e-6), P)) / (2e-6 * T)
+            assert np.abs(got[:, 0] - fd_p).max() <= 1e-6 * np.abs(fd_p).max(), (n, which, "p")
+            assert np.abs(got[:, 1] - fd_t).max() <= 1e-6 * np.abs(fd_t).max(), (n, which, "T")
