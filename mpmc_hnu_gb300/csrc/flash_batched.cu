@@ -127,6 +127,8 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     mark();
     classify_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, 0);
     mark();
+    // one warp per trial item: items of slow descents dominate, so latency
+    // matters more than packing several items into a warp (measured)
     if (shape.item_form & 1) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
     else w64::trials64w_kernel<NM, 32><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
     mark();
