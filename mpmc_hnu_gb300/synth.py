@@ -24,6 +24,7 @@ _M2 = np.uint64(0x94D049BB133111EB)
 # stream identifiers
 S_TC, S_PC, S_OMEGA, S_KIJ = 1, 2, 3, 4
 S_Z, S_T, S_P, S_PICK, S_NEAR = 11, 12, 13, 14, 15
+S_CRIT_PICK, S_CRIT_T, S_CRIT_P = 16, 17, 18
 
 
 def _mix(x: np.ndarray) -> np.ndarray:
@@ -82,3 +83,17 @@ def make_cells(n: int, ncell: int, seed: int, offset: int = 0):
     t = 280.0 + 170.0 * uniform(seed, S_T, c)
     p = np.exp(np.log(0.5e6) + (np.log(40e6) - np.log(0.5e6)) * uniform(seed, S_P, c))
     return np.ascontiguousarray(p), np.ascontiguousarray(t), np.ascontiguousarray(z)
+
+
+def make_near_critical_cells(mixture, ncell: int, seed: int, fraction: float = 0.2, offset: int = 0):
+    """Cells with `fraction` of them near-critical: T = T_pc (1 + U[-0.01, 0.01])
+    with the pseudo-critical T_pc = sum_i z_i Tc_i (Kay's rule) and p
+    log-uniform on [10, 40] MPa; the rest as in make_cells."""
+    n = int(mixture.n)
+    p, t, z = make_cells(n, ncell, seed, offset)
+    c = np.arange(offset, offset + ncell, dtype=np.uint64)
+    pick = uniform(seed, S_CRIT_PICK, c) < fraction
+    tpc = np.asarray(mixture.tc) @ z
+    t = np.where(pick, tpc * (1.0 + 0.02 * (uniform(seed, S_CRIT_T, c) - 0.5)), t)
+    p = np.where(pick, np.exp(np.log(10e6) + (np.log(40e6) - np.log(10e6)) * uniform(seed, S_CRIT_P, c)), p)
+    return np.ascontiguousarray(p), np.ascontiguousarray(t), z
