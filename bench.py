@@ -394,12 +394,13 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--form", default="mixed", choices=["mixed", "plain"])
+    ap.add_argument("--form", default="mixed", choices=["mixed", "batched", "plain"])
     ap.add_argument("--n", type=int, default=10)
     ap.add_argument("--cells", type=int, default=1 << 20)
     ap.add_argument("--near-fraction", type=float, default=0.3)
     ap.add_argument("--no-ad", action="store_true")
     ap.add_argument("--plain-sample", type=int, default=32768)
+    ap.add_argument("--batched-sample", type=int, default=131072)
     ap.add_argument("--cpu-sample", type=int, default=65536)
     ap.add_argument("--profile", action="store_true", help="one untimed solve of the workload (for ncu)")
     ap.add_argument("--serving-seconds", type=float, default=8.0,
@@ -563,13 +564,12 @@ def main() -> None:
     counters_t = outs["counters"].cpu().numpy().astype(np.float64)
     gt.close()
 
-    # plain FP64 form on a bounded sample of the same cells
-    plain = None
-    if args.form == "mixed" and args.plain_sample > 0 and rank == 0:
-        sel = stratified(ncell, args.plain_sample)
+    # the all-FP64 forms on bounded samples of the same cells
+    def sample_leg(form, size):
+        sel = stratified(ncell, size)
         ns = int(sel.size)
         isel = torch.from_numpy(sel).to(dp.device)
-        gp = flash.GpuFlash(mix, "plain", sensitivity=sens, device=device)
+        gp = flash.GpuFlash(mix, form, sensitivity=sens, device=device)
         sub = {f: torch.empty((v.shape[0], ns), dtype=v.dtype, device=v.device) for f, v in outs.items()}
         sp = {f: v.data_ptr() for f, v in sub.items()}
         dps, dts, dzs = dp[isel].contiguous(), dt[isel].contiguous(), dz[:, isel].contiguous()
@@ -583,17 +583,24 @@ def main() -> None:
         torch.cuda.synchronize()
         pms = a0.elapsed_time(a1)
         ps = sub["status"][0].cpu().numpy()
-        plain = {"value": ns / (pms * 1e-3), "unit": "flashes/s", "cells": ns,
-                 "sample": f"{ns} stratified cells (every {ncell // ns}th) of the workload, one launch",
-                 "status_agreement_with_chosen": float((ps == status[sel]).mean())}
         gp.close()
+        return {"value": ns / (pms * 1e-3), "unit": "flashes/s", "cells": ns,
+                "sample": f"{ns} stratified cells (every {ncell // ns}th) of the workload, one launch",
+                "status_agreement_with_chosen": float((ps == status[sel]).mean())}
+
+    plain = batched = None
+    if args.form == "mixed" and rank == 0:
+        if args.plain_sample > 0:
+            plain = sample_leg("plain", args.plain_sample)
+        if args.batched_sample > 0:
+            batched = sample_leg("batched", args.batched_sample)
 
     fp64_tf, fp32_tf = measured_peaks(flash)
     # roofline of the dominant stage: FP32 screening kernels on the FP32 pipe
     ev32 = counters_t[0] + counters_t[1] + counters_t[2]
     ev64 = counters_t[5]
     fe = f_eval(n)
-    if args.form == "mixed":
+    if args.form in ("mixed", "batched"):
         dominant = max((k for k in stages if k != "sensitivity"), key=lambda k: stages[k])
         fp32_stage = {"feed_trials": counters_t[0], "split": counters_t[1], "review_trials": counters_t[2]}
         if dominant in fp32_stage:
@@ -642,7 +649,7 @@ def main() -> None:
                 "dtype": "f32 iterations + f64 decisions/polish/AD" if args.form == "mixed" else "f64",
                 "data": f"synthetic (seeded generator; {placed} near-boundary cells placed by GPU bisection)",
                 "config": workload, "e2e": e2e, "gpu_launches": len(stages) * args.steps,
-                "roofline": roofline, "cpu_baseline": cpu, "plain_fp64": plain,
+                "roofline": roofline, "cpu_baseline": cpu, "plain_fp64": plain, "batched_fp64": batched,
                 "phase_counts": {"single": int((status == 0).sum()), "two": int((status == 1).sum()),
                                  "unstable": int((status == 2).sum()), "indeterminate": int((status == 3).sum()),
                                  "invalid": int((status == -1).sum())},

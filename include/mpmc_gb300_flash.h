@@ -70,7 +70,7 @@ enum {
 /* Algorithm forms (same fixed points, different execution). */
 enum {
     MPMC_FORM_PLAIN_FP64 = 0, /* one thread per cell, reference algorithm in FP64 */
-    MPMC_FORM_BATCHED = 1,    /* reserved: work-queue form in FP64 (MPMC_ERR_UNSUPPORTED in this build) */
+    MPMC_FORM_BATCHED = 1,    /* work-queue form, every trial and split attempt an exact FP64 lane-group item */
     MPMC_FORM_MIXED = 2       /* work queue, FP32 bulk iterations + FP64 polish/decisions */
 };
 

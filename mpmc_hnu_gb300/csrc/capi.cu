@@ -196,7 +196,7 @@ int with_sensitivity_inputs(mpmc_gpu_flash* h, int64_t ncell, pr76::DeviceOutput
 // Launch shape of the mixed form: defaults, then the MPMC_* environment knobs
 // (sweeps), then the handle's explicit shape (mpmc_gpu_flash_set_launch_shape).
 pr76::BatchedShape batched_shape(const mpmc_gpu_flash* h, cudaEvent_t* events) {
-    pr76::BatchedShape shape{0, 0, 0, 0, 0, events, 0, 0.0f};
+    pr76::BatchedShape shape{0, 0, 0, 0, 0, events, 0, 0.0f, 0};
     const struct {
         const char* name;
         int* field;
@@ -223,10 +223,11 @@ int prepare_device(mpmc_gpu_flash* h, int64_t ncell, pr76::DeviceOutputs& d) {
         const int rc = with_sensitivity_inputs(h, ncell, d);
         if (rc != MPMC_OK) return rc;
     }
-    if (h->form == MPMC_FORM_MIXED) {
+    if (h->form == MPMC_FORM_MIXED || h->form == MPMC_FORM_BATCHED) {
         if (ncell >= (int64_t{1} << 24))
-            return fail(MPMC_ERR_INVALID_ARGUMENT, "mixed form: at most 16,777,215 cells per call");
-        const cudaError_t e = h->workspace.ensure(pr76::batched_workspace_bytes(h->n, ncell));
+            return fail(MPMC_ERR_INVALID_ARGUMENT, "batched forms: at most 16,777,215 cells per call");
+        const cudaError_t e =
+            h->workspace.ensure(pr76::batched_workspace_bytes(h->n, ncell, h->form == MPMC_FORM_BATCHED));
         if (e != cudaSuccess) return cuda_fail(e, "batched workspace allocation");
     } else if (h->form != MPMC_FORM_PLAIN_FP64) {
         return fail(MPMC_ERR_UNSUPPORTED, "algorithm form not available in this build");
@@ -247,7 +248,8 @@ cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, co
         e = pr76::launch_plain(h->n, h->d_mixture, ncell, p, t, z, d, stream);
         record();
     } else {
-        const pr76::BatchedShape shape = batched_shape(h, timing ? h->events : nullptr);
+        pr76::BatchedShape shape = batched_shape(h, timing ? h->events : nullptr);
+        shape.fp64_items = h->form == MPMC_FORM_BATCHED;
         e = pr76::launch_batched(h->n, h->d_mixture, ncell, p, t, z, d, h->workspace.ptr, h->workspace.bytes, shape,
                                  stream);
         next_event = timing ? pr76::kBatchedStages + 1 : 0;
@@ -371,13 +373,13 @@ int capacity_for(int n) {
     return 0;
 }
 
-size_t batched_workspace_bytes(int n, int64_t ncell) {
+size_t batched_workspace_bytes(int n, int64_t ncell, bool fp64_items) {
     switch (capacity_for(n)) {
-    case 4: return batched_workspace_bytes_nm4(n, ncell);
-    case 8: return batched_workspace_bytes_nm8(n, ncell);
-    case 12: return batched_workspace_bytes_nm12(n, ncell);
-    case 16: return batched_workspace_bytes_nm16(n, ncell);
-    case 20: return batched_workspace_bytes_nm20(n, ncell);
+    case 4: return batched_workspace_bytes_nm4(n, ncell, fp64_items);
+    case 8: return batched_workspace_bytes_nm8(n, ncell, fp64_items);
+    case 12: return batched_workspace_bytes_nm12(n, ncell, fp64_items);
+    case 16: return batched_workspace_bytes_nm16(n, ncell, fp64_items);
+    case 20: return batched_workspace_bytes_nm20(n, ncell, fp64_items);
     default: return 0;
     }
 }
@@ -429,7 +431,7 @@ const char* mpmc_gpu_flash_last_error(void) { return g_last_error.c_str(); }
 int mpmc_gpu_flash_components(const mpmc_gpu_flash* h) { return h ? h->n : 0; }
 
 int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* h, int64_t* out, int capacity) {
-    if (!h || h->form != MPMC_FORM_MIXED || !h->workspace.ptr) return 0;
+    if (!h || (h->form != MPMC_FORM_MIXED && h->form != MPMC_FORM_BATCHED) || !h->workspace.ptr) return 0;
     // workspace counter slots (pr76_batched.cuh Slot) in the documented order
     constexpr int kSlots[] = {8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 20, 22, 23, 24, 25};
     constexpr int kCount = static_cast<int>(sizeof(kSlots) / sizeof(kSlots[0]));
@@ -462,8 +464,6 @@ int mpmc_gpu_flash_create(const mpmc_pr76_mixture* mixture, const mpmc_flash_opt
     if (options) opt = *options;
     if (opt.form != MPMC_FORM_PLAIN_FP64 && opt.form != MPMC_FORM_BATCHED && opt.form != MPMC_FORM_MIXED)
         return fail(MPMC_ERR_INVALID_ARGUMENT, "unknown algorithm form");
-    if (opt.form == MPMC_FORM_BATCHED)
-        return fail(MPMC_ERR_UNSUPPORTED, "the batched FP64 form is not part of this build; use MPMC_FORM_MIXED");
     pr76::Mixture m;
     const int rc = prepare_mixture(mixture, m);
     if (rc != MPMC_OK) return rc;

@@ -22,7 +22,7 @@ size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
 
 // Carves the workspace arrays out of one scratch allocation; with base ==
 // nullptr only computes the size.
-size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell) {
+size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell, bool fp64_items) {
     const size_t nc = static_cast<size_t>(ncell);
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -47,6 +47,8 @@ size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell) {
     ws.att_class = reinterpret_cast<signed char*>(take(batched::kMaxAttempts * nc));
     ws.att_count = reinterpret_cast<int*>(take(sizeof(int) * nc));
     ws.att_iter = reinterpret_cast<short*>(take(sizeof(short) * batched::kMaxAttempts * nc));
+    ws.att_lnk64 = fp64_items ? reinterpret_cast<double*>(take(sizeof(double) * batched::kMaxAttempts * NM * nc))
+                              : nullptr;
     ws.att_rate = reinterpret_cast<float*>(take(sizeof(float) * batched::kMaxAttempts * nc));
     ws.cand = reinterpret_cast<double*>(take(sizeof(double) * 7 * NM * nc));
     ws.cand_s = reinterpret_cast<double*>(take(sizeof(double) * 8 * nc));
@@ -56,7 +58,9 @@ size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell) {
     ws.t64_items = reinterpret_cast<int*>(take(sizeof(int) * (NM + 4) * nc));
     ws.t64_status = reinterpret_cast<signed char*>(take((NM + 4) * nc));
     ws.tw64 = reinterpret_cast<double*>(take(sizeof(double) * (NM + 4) * NM * nc));
-    ws.s64_capacity = static_cast<int>(nc < 4096 ? 4 * 4096 : nc);
+    // FP64 attempt items: the unsettled attempts of the mixed form (capacity
+    // ncell, at least 16384); every attempt of every cell in the FP64 form
+    ws.s64_capacity = static_cast<int>(fp64_items ? batched::kMaxAttempts * nc : (nc < 4096 ? 4 * 4096 : nc));
     const size_t cap = static_cast<size_t>(ws.s64_capacity);
     ws.s64_items = reinterpret_cast<int*>(take(sizeof(int) * cap));
     ws.s64_status = reinterpret_cast<signed char*>(take(cap));
@@ -78,9 +82,9 @@ int resident_blocks(K kernel, int block) {
 }  // namespace batched_host_nm<NM>
 using namespace MPMC_CAT(batched_host_nm, MPMC_NM);
 
-size_t MPMC_CAT(batched_workspace_bytes_nm, MPMC_NM)(int n, int64_t ncell) {
+size_t MPMC_CAT(batched_workspace_bytes_nm, MPMC_NM)(int n, int64_t ncell, bool fp64_items) {
     batched::Workspace ws;
-    return carve(ws, nullptr, n, ncell);
+    return carve(ws, nullptr, n, ncell, fp64_items);
 }
 
 cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, int64_t ncell, const double* p,
@@ -91,8 +95,9 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     if (ncell <= 0) return cudaSuccess;
     if (ncell >= (int64_t{1} << 24)) return cudaErrorInvalidValue;  // work-item encodings hold 24-bit cells
     Workspace ws;
-    if (carve(ws, nullptr, n, ncell) > scratch_bytes || scratch == nullptr) return cudaErrorInvalidValue;
-    carve(ws, static_cast<char*>(scratch), n, ncell);
+    const bool fp64_items = shape.fp64_items != 0;
+    if (carve(ws, nullptr, n, ncell, fp64_items) > scratch_bytes || scratch == nullptr) return cudaErrorInvalidValue;
+    carve(ws, static_cast<char*>(scratch), n, ncell, fp64_items);
     int device = 0, sms = 0;
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -123,13 +128,16 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     mark();
     setup_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, p, t, z, out);
     mark();
-    trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 0);
+    // The FP64 form queues every trial and attempt as an exact FP64 item (the
+    // FP32 screening stages become empty), on the same stage slots.
+    if (fp64_items) rerun_all_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(ws, 0);
+    else trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 0);
     mark();
     classify_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, 0);
     mark();
     // one warp per trial item: items of slow descents dominate, so latency
     // matters more than packing several items into a warp (measured)
-    if (shape.item_form & 1) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+    if ((shape.item_form & 1) && !fp64_items) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
     else w64::trials64w_kernel<NM, 32><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
     mark();
     decide_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
@@ -137,7 +145,7 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     // FP32 successive substitution hands over to the FP64 Newton polish at
     // |r| <= ss_switch (default 2e-5, a few times the FP32 rounding floor)
     const float ss_switch = shape.ss_switch > 0.f ? shape.ss_switch : 2e-5f;
-    split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t, ss_switch);
+    if (!fp64_items) split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t, ss_switch);
     mark();
     // polish: one cell per thread up to 12 components (its per-cell arrays
     // still fit the cache), one cell per lane group above
@@ -145,7 +153,7 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     if (lane_polish) polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
     else w64::polishw_kernel<NM, w64::kSeg<NM>><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t, out);
     mark();
-    if (shape.item_form & 4) split64_kernel<NM><<<sms * s64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+    if ((shape.item_form & 4) && !fp64_items) split64_kernel<NM><<<sms * s64_res, 64, 0, stream>>>(d_mix, ws, p, t);
     else w64::split64w_kernel<NM, 32><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t);
     mark();
     select64_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
@@ -153,11 +161,12 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     relist_kernel<NM><<<1, 1024, 0, stream>>>(ws);
     cudaMemsetAsync(ws.counters + qT64Items, 0, 2 * sizeof(int), stream);
     mark();
-    trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 1);
+    if (fp64_items) rerun_all_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(ws, 1);
+    else trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 1);
     mark();
     classify_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, 1);
     mark();
-    if (shape.item_form & 2) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+    if ((shape.item_form & 2) && !fp64_items) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
     else w64::trials64w_kernel<NM, 32><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
     mark();
     finish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);

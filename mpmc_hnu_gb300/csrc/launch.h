@@ -61,12 +61,13 @@ struct BatchedShape {
                           // and by component capacity (thread up to 12) with neither
     float ss_switch;      // FP32 |r| at which successive substitution hands over to the FP64
                           // Newton polish (0 = 2e-5)
+    int fp64_items;       // batched FP64 form: every trial and attempt as an exact FP64 item
 };
 constexpr int kBatchedStages = 15;
 
 // Batched mixed-precision flash (flash_batched.cu): scratch bytes needed for
 // ncell cells, and the launch sequence using that scratch.
-size_t batched_workspace_bytes(int n, int64_t ncell);
+size_t batched_workspace_bytes(int n, int64_t ncell, bool fp64_items = false);
 cudaError_t launch_batched(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
                            const double* z, const DeviceOutputs& out, void* scratch, size_t scratch_bytes,
                            const BatchedShape& shape, cudaStream_t stream);
@@ -88,7 +89,7 @@ cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const
                                     const double* z, const DeviceOutputs& out, cudaStream_t stream); \
     cudaError_t launch_sensitivity_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t, \
                                           const double* z, const DeviceOutputs& out, cudaStream_t stream); \
-    size_t batched_workspace_bytes_nm##NM(int n, int64_t ncell);                                              \
+    size_t batched_workspace_bytes_nm##NM(int n, int64_t ncell, bool fp64_items);                             \
     cudaError_t launch_batched_nm##NM(const Mixture* d_mix, int n, int64_t ncell, const double* p,            \
                                       const double* t, const double* z, const DeviceOutputs& out, void* scratch, \
                                       size_t scratch_bytes, const BatchedShape& shape, cudaStream_t stream);

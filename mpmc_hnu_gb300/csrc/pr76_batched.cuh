@@ -121,6 +121,7 @@ struct Workspace {
     signed char* s64_status;// [s64_capacity]
     double* s64_state;      // [s64_capacity * S64Stride] converged attempt states
     short* att_iter;        // [kMaxAttempts * ncell] FP32 SS iterations of the attempt
+    double* att_lnk64;      // [kMaxAttempts * NM * ncell] FP64 seeds (batched FP64 form only, else null)
     float* att_rate;        // [kMaxAttempts * ncell] FP32 SS contraction per iteration, ln(|r| ratio)
     int* split_cells;       // [ncell] cells that reached the split stage
     int* s64_cells;         // [ncell] cells whose attempts were continued in FP64
@@ -568,6 +569,24 @@ __device__ void write_counters(const DeviceOutputs& out, const Workspace& ws, in
 }
 
 // ---------------------------------------------------------------------------
+// Batched FP64 form: instead of FP32 screening, every trial of the listed
+// cells is queued as an exact FP64 run from its start.
+template <int NM>
+__global__ void __launch_bounds__(128) rerun_all_kernel(Workspace ws, int review) {
+    const int cells = ws.counters[qTrialCells];
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < cells; slot += gridDim.x * blockDim.x) {
+        const int64_t c = ws.trial_cells[slot];
+        int active = 0;
+        for (int i = 0; i < ws.n; ++i) active += ws.z[idx(i, ws.ncell, c)] > 0.0;
+        const int ntr = auto_starts(active) + (review ? 2 : 0);
+        for (int k = 0; k < NM + 4; ++k) {
+            ws.tclass[idx(k, ws.ncell, c)] = static_cast<signed char>(k < ntr ? fp32::tRerun : -1);
+            ws.titer[idx(k, ws.ncell, c)] = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Stage 3: feed-test decision per cell and split-attempt enumeration.
 template <int NM>
 struct DecideScratch {
@@ -630,6 +649,10 @@ __global__ void __launch_bounds__(64) decide_kernel(const Mixture* __restrict__ 
                     const int item = atomicAdd(&ws.counters[qAttempts], 1);
                     ws.attempt_items[item] = (static_cast<int>(c) << 5) | order;
                     ws.att_class[idx(order, ws.ncell, c)] = fp32::aFailed;  // overwritten by split32
+                    if (ws.att_lnk64) {  // batched FP64 form: the attempt runs from its exact seed
+                        for (int i = 0; i < n; ++i) ws.att_lnk64[idx(order * NM + i, ws.ncell, c)] = s.lk[i];
+                        ws.att_iter[idx(order, ws.ncell, c)] = 0;
+                    }
                 } else {
                     ws.att_class[idx(order, ws.ncell, c)] = fp32::aTrivial;  // unrepresentable seed: not a candidate
                 }

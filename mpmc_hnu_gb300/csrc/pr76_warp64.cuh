@@ -1002,7 +1002,9 @@ __global__ void __launch_bounds__(128) split64w_kernel(const Mixture* __restrict
         int evals = 0;
         int status = fp64::kAttemptPropertyFailure;
         if (load_cell(m, ws, c, p, t, cell)) {
-            const double lk0 = cell.comp ? static_cast<double>(ws.att_lnk[idx(order * NM + lane, ws.ncell, c)]) : 0.0;
+            const double lk0 = !cell.comp ? 0.0
+                               : (ws.att_lnk64 ? ws.att_lnk64[idx(order * NM + lane, ws.ncell, c)]
+                                               : static_cast<double>(ws.att_lnk[idx(order * NM + lane, ws.ncell, c)]));
             status = attempt(cell, lk0, point, evals, ws.att_iter[idx(order, ws.ncell, c)]);
         }
         if (lane == 0) ws.s64_status[item] = static_cast<signed char>(status);

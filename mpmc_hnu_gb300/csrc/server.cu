@@ -183,7 +183,7 @@ int launch_batch(mpmc_flash_server* sv, Slot& s) {
     d.counters = static_cast<int32_t*>(s.d_out[9]);
     const pr76::Mixture* mix = sv->mixtures[s.mixture].d_mix;
     if (sv->form == MPMC_FORM_MIXED) {
-        const pr76::BatchedShape shape{0, 0, 0, 0, 0, nullptr, 0, 0.0f};
+        const pr76::BatchedShape shape{0, 0, 0, 0, 0, nullptr, 0, 0.0f, 0};
         e = pr76::launch_batched(n, mix, C, s.d_p, s.d_t, s.d_z, d, s.d_ws, s.ws_bytes, shape, s.stream);
     } else {
         e = pr76::launch_plain(n, mix, C, s.d_p, s.d_t, s.d_z, d, s.stream);

@@ -80,10 +80,12 @@ BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun
                "two_candidates", "fp64_trial_items", "fp64_attempt_items", "polished_cells", "select64_cells",
                "slow_trials_skipped", "limit_attempts"]
 FLAG_STAGE_TIMING = 1
-STAGES = {FORM_PLAIN_FP64: ["flash", "sensitivity"],
-          FORM_MIXED: ["setup", "feed_trials", "feed_classify", "feed_trials64", "decide", "split", "polish",
-                       "split64", "select64", "relist", "review_trials", "review_classify", "review_trials64",
-                       "finish", "fallback", "sensitivity"]}
+_QUEUE_STAGES = ["setup", "feed_trials", "feed_classify", "feed_trials64", "decide", "split", "polish",
+                 "split64", "select64", "relist", "review_trials", "review_classify", "review_trials64",
+                 "finish", "fallback", "sensitivity"]
+# the FP64 work-queue form runs on the same stage slots; its FP32 stages
+# (feed_trials, split, review_trials) only queue items or are empty
+STAGES = {FORM_PLAIN_FP64: ["flash", "sensitivity"], FORM_MIXED: _QUEUE_STAGES, FORM_BATCHED: _QUEUE_STAGES}
 
 _LIB = None
 

@@ -1,8 +1,9 @@
 """Accuracy on near-critical cells: 20 % of the cells at T = T_pc (1 +- 1 %)
 (Kay's rule) and p log-uniform on [10, 40] MPa, the rest log-uniform.
 
-The plain FP64 form must match the oracle's phase status on every cell.  The
-mixed form may differ on at most 1 cell in 8,192.  Each such cell has a
+The plain FP64 form and the FP64 work-queue form must match the oracle's
+phase status on every cell.  The mixed form may differ on at most 1 cell in
+8,192.  Each such cell has a
 reference ln K iteration that ends within a few iterations of its
 512-iteration limit, or a line search that stalls at |r| ~ 1e-8; there,
 precision-dependent rounding decides the status.  Every matched two-phase
@@ -22,7 +23,7 @@ def test_near_critical_cells(gpu_lib, oracle_lib, n, ncell):
     mix = synth.make_mixture(n, 3000 + n)
     p, t, z = synth.make_near_critical_cells(mix, ncell, 4000 + n)
     ref = oracle_lib.flash(mix, p, t, z, threads=8)
-    for form, allowed in (("plain", 0), ("mixed", ncell // 8192)):
+    for form, allowed in (("plain", 0), ("batched", 0), ("mixed", ncell // 8192)):
         g = gpu_lib.GpuFlash(mix, form=form)
         out = g.solve(p, t, z)
         g.close()

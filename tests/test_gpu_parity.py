@@ -11,7 +11,7 @@ CASES = [(3, 256, 5), (4, 256, 6), (6, 512, 1), (10, 384, 2), (12, 192, 3), (20,
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("n,ncell,seed", CASES)
-@pytest.mark.parametrize("form", ["plain", "mixed"])
+@pytest.mark.parametrize("form", ["plain", "batched", "mixed"])
 def test_flash_matches_oracle(gpu_lib, oracle_lib, n, ncell, seed, form):
     mix = synth.make_mixture(n, seed)
     p, t, z = synth.make_cells(n, ncell, seed)

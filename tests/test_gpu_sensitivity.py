@@ -26,7 +26,7 @@ class Mix:
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("form", ["plain", "mixed"])
+@pytest.mark.parametrize("form", ["plain", "batched", "mixed"])
 @pytest.mark.parametrize("n,ncell,seed", [(3, 128, 5), (4, 128, 6), (6, 192, 1), (10, 128, 2), (20, 48, 4)])
 def test_sensitivity_matches_oracle(gpu_lib, oracle_lib, n, ncell, seed, form):
     """Device AD vs the oracle's differentiate_pr76_pt_vle restatement at the
