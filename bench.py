@@ -13,9 +13,11 @@ A step is one pass of the chosen form (batched mixed precision) over all
 cells, flash + derivatives, inputs already resident in HBM.  `e2e` times the
 same step through the host-buffer C ABI entry (pinned host inputs, every
 output copied back).  Inputs (96 MB) and outputs (~5 GB) exceed the 126 MB L2,
-so no extra flush is needed between steps.  The plain FP64 form is timed on a
-bounded sample of the same cells; the CPU oracle (the reference algorithm
-restated in C++) is timed on a bounded sample with every host thread.
+so no extra flush is needed between steps.  The plain FP64 form and the FP64
+work-queue form are timed on bounded samples of the same cells; the ln K
+warm-start path is timed on the full workload (warm starts from the timed
+solve's own answers); the CPU oracle (the reference algorithm restated in
+C++) is timed on a bounded sample with every host thread.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -401,6 +403,8 @@ def main() -> None:
     ap.add_argument("--no-ad", action="store_true")
     ap.add_argument("--plain-sample", type=int, default=32768)
     ap.add_argument("--batched-sample", type=int, default=131072)
+    ap.add_argument("--warm-fraction", type=float, default=0.75,
+                    help="share of the two-phase cells given a ln K warm start in the warm-start leg (0 = skip)")
     ap.add_argument("--cpu-sample", type=int, default=65536)
     ap.add_argument("--profile", action="store_true", help="one untimed solve of the workload (for ncu)")
     ap.add_argument("--serving-seconds", type=float, default=8.0,
@@ -595,6 +599,43 @@ def main() -> None:
         if args.batched_sample > 0:
             batched = sample_leg("batched", args.batched_sample)
 
+    # ln K warm starts (continuation use): the timed solve's own ln K, perturbed
+    # by 0.1 N(0, 1) per component, on 75 % of the two-phase cells; the rest cold
+    warm_leg = None
+    if args.form in ("mixed", "batched") and args.warm_fraction > 0 and rank == 0:
+        gen = torch.Generator(device="cuda").manual_seed(7)
+        lnk = outs["ln_k"]
+        two = outs["status"][0] == 1
+        pick = two & (torch.rand(ncell, device="cuda", generator=gen) < args.warm_fraction)
+        warm = lnk + 0.1 * torch.randn(lnk.shape, device="cuda", dtype=lnk.dtype, generator=gen)
+        warm[:, ~pick] = float("nan")
+        warm = warm.contiguous()
+        cold_status = outs["status"][0].clone()
+        gw = flash.GpuFlash(mix, args.form, sensitivity=sens, device=device, graphs=True)
+        if tuned is not None:
+            gw.set_launch_shape(tuned["shape"])
+        wouts = {f: torch.empty_like(v) for f, v in outs.items()}
+        wptrs = {f: v.data_ptr() for f, v in wouts.items()}
+        wtimes = []
+        for k in range(2):  # capture, then replay
+            w0 = torch.cuda.Event(enable_timing=True)
+            w1 = torch.cuda.Event(enable_timing=True)
+            w0.record(stream)
+            gw.solve_device(ncell, dp.data_ptr(), dt.data_ptr(), dz.data_ptr(), wptrs, stream.cuda_stream,
+                            warm_ptr=warm.data_ptr())
+            w1.record(stream)
+            torch.cuda.synchronize()
+            wtimes.append(w0.elapsed_time(w1))
+        stats = gw.batch_stats()
+        gw.close()
+        wms = wtimes[-1]
+        warm_leg = {"value": ncell / (wms * 1e-3), "unit": "flashes/s", "ms": wms, "cold_ms": ms,
+                    "warm_cells": stats["warm_cells"], "sent_to_cold_pass": stats["warm_redo"],
+                    "status_agreement_with_cold": float((wouts["status"][0] == cold_status).float().mean().item()),
+                    "setup": f"ln K of the timed solve + 0.1 N(0,1) on {args.warm_fraction:.0%} of the two-phase "
+                             "cells, the rest cold; same cells and handle settings, one replayed graph"}
+        del wouts, warm
+
     fp64_tf, fp32_tf = measured_peaks(flash)
     # roofline of the dominant stage: FP32 screening kernels on the FP32 pipe
     ev32 = counters_t[0] + counters_t[1] + counters_t[2]
@@ -650,6 +691,7 @@ def main() -> None:
                 "data": f"synthetic (seeded generator; {placed} near-boundary cells placed by GPU bisection)",
                 "config": workload, "e2e": e2e, "gpu_launches": len(stages) * args.steps,
                 "roofline": roofline, "cpu_baseline": cpu, "plain_fp64": plain, "batched_fp64": batched,
+                "warm_start": warm_leg,
                 "phase_counts": {"single": int((status == 0).sum()), "two": int((status == 1).sum()),
                                  "unstable": int((status == 2).sum()), "indeterminate": int((status == 3).sum()),
                                  "invalid": int((status == -1).sum())},

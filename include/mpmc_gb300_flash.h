@@ -172,6 +172,35 @@ int mpmc_gpu_flash_solve(mpmc_gpu_flash* handle, int64_t n_cells, const double* 
 int mpmc_gpu_flash_solve_device(mpmc_gpu_flash* handle, int64_t n_cells, const double* p, const double* t,
                                 const double* z, const mpmc_flash_outputs* out, void* stream);
 
+/* mpmc_gpu_flash_solve / mpmc_gpu_flash_solve_device with ln K warm starts:
+ * ln_k_warm [n*n_cells] (same layout as z; host memory for the first call,
+ * device memory for the second) holds each cell's ln(y/x) guess, e.g. from
+ * the previous time step or continuation step.  A cell whose warm start has a
+ * non-finite entry on a component with z > 0, or is all zero, is solved cold.
+ * Work-queue forms only (MPMC_FORM_MIXED, MPMC_FORM_BATCHED; the plain form
+ * returns MPMC_ERR_UNSUPPORTED).  ln_k_warm = NULL is the cold solve.
+ *
+ * The reference has no ln K warm start: its solve hints are TPD start
+ * compositions (pt_solve_hints.hpp:26-43).  What a warm start does here is
+ * run one split attempt from the guess (pt_split.hpp:275-408), with the same
+ * iteration, polish and acceptance rules as a cold attempt, and go straight to
+ * the final common-tangent review of that pair (pt_split.hpp:490-512).  The
+ * initial stability test and the other attempts are skipped.  The cell is
+ * settled only when the review accepts the pair as two_phase, after the same
+ * Gibbs-energy check against the feed.  Every other cell (a collapsed or
+ * non-converged attempt, an unstable or indeterminate review, or a cold cell)
+ * then gets the full cold solve, in a second pass of the same launch. A
+ * settled cell's answer is the pair that passed the reference's own
+ * acceptance and review tests; a cold solve of the cell can differ from it
+ * only where the cold attempts would have selected another local minimum.
+ * Each stage time from mpmc_gpu_flash_stage_timings covers both passes;
+ * mpmc_gpu_flash_batch_stats counts the warm cells and the ones sent on. */
+int mpmc_gpu_flash_solve_warm(mpmc_gpu_flash* handle, int64_t n_cells, const double* p, const double* t,
+                              const double* z, const double* ln_k_warm, const mpmc_flash_outputs* out);
+int mpmc_gpu_flash_solve_device_warm(mpmc_gpu_flash* handle, int64_t n_cells, const double* p, const double* t,
+                                     const double* z, const double* ln_k_warm, const mpmc_flash_outputs* out,
+                                     void* stream);
+
 /* Largest device scratch, in bytes, of mpmc_gpu_flash_solve_device_noalloc:
  * a fixed 48 MiB array in the library's device code. */
 #define MPMC_NOALLOC_SCRATCH_BYTES (48u << 20)
@@ -231,7 +260,7 @@ int mpmc_gpu_flash_set_launch_shape(mpmc_gpu_flash* handle, const int32_t* value
  * work counters only, pt_stability.hpp:66-76). */
 int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* handle, float* ms, int capacity);
 
-/* Work statistics of the last mixed-form solve on a handle (waits for the
+/* Work statistics of the last work-queue solve on a handle (waits for the
  * device): [0] feed trials continued in FP64 from their FP32 end point,
  * [1] feed trials re-run exactly in FP64, [2] review trials continued,
  * [3] review trials re-run, [4] cells sent to the plain FP64 fallback
@@ -243,7 +272,9 @@ int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* handle, float* ms, int capacity
  * [13] cells whose attempts were selected in FP64, [14] slow FP32 trials
  * whose exact re-run was skipped because another trial of the same test was
  * already negative, [15] split attempts classified as ending at the
- * iteration limit without an FP64 run.
+ * iteration limit without an FP64 run, [16] cells run from their ln K warm
+ * start, [17] of those, cells whose pair was not accepted and that took the
+ * cold pass.  After a warm-start solve, [0]-[15] count the cold pass.
  * Writes up to `capacity` values; returns the number available (0 for the
  * plain form).  Diagnostic entry point with no counterpart in the reference. */
 int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* handle, int64_t* out, int capacity);

@@ -57,7 +57,7 @@ constexpr size_t kMaxGraphs = 4;
 // One captured solve: the cell count and every buffer are baked into it.
 struct GraphEntry {
     int64_t ncell = 0;
-    const double *p = nullptr, *t = nullptr, *z = nullptr;
+    const double *p = nullptr, *t = nullptr, *z = nullptr, *warm = nullptr;
     pr76::DeviceOutputs outputs{};
     cudaGraphExec_t exec = nullptr;
     uint64_t last_use = 0;
@@ -79,7 +79,10 @@ struct mpmc_gpu_flash {
     DevBuf workspace;  // batched-form stage buffers and work queues
     bool stage_timing = false;
     cudaEvent_t events[24] = {};
+    cudaEvent_t redo_events[24] = {};  // the cold pass after a warm pass
     int n_events = 0;   // events recorded by the last solve (stages + 1)
+    bool timed_warm = false;  // the last timed solve ran a warm and a cold pass
+    DevBuf in_warm;     // host entry: staged ln K warm starts
     int32_t shape[8] = {};  // explicit launch shape (mpmc_gpu_flash_set_launch_shape), 0 = default
     bool use_graphs = false;
     std::vector<GraphEntry> graphs;
@@ -237,7 +240,7 @@ int prepare_device(mpmc_gpu_flash* h, int64_t ncell, pr76::DeviceOutputs& d) {
 
 // The launches of one solve on `stream` (no allocation, no synchronisation).
 cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
-                           const pr76::DeviceOutputs& d, cudaStream_t stream, bool timing) {
+                           const double* warm, const pr76::DeviceOutputs& d, cudaStream_t stream, bool timing) {
     cudaError_t e;
     int next_event = 0;
     auto record = [&]() {
@@ -250,6 +253,8 @@ cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, co
     } else {
         pr76::BatchedShape shape = batched_shape(h, timing ? h->events : nullptr);
         shape.fp64_items = h->form == MPMC_FORM_BATCHED;
+        shape.warm_lnk = warm;
+        shape.redo_events = timing ? h->redo_events : nullptr;
         e = pr76::launch_batched(h->n, h->d_mixture, ncell, p, t, z, d, h->workspace.ptr, h->workspace.bytes, shape,
                                  stream);
         next_event = timing ? pr76::kBatchedStages + 1 : 0;
@@ -260,18 +265,25 @@ cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, co
         if (e != cudaSuccess) return e;
     }
     record();  // end of the sensitivity stage (zero length without sensitivities)
-    if (timing) h->n_events = next_event;
+    if (timing) {
+        h->n_events = next_event;
+        h->timed_warm = warm != nullptr;
+    }
     return cudaSuccess;
 }
 
 bool same_key(const GraphEntry& g, int64_t ncell, const double* p, const double* t, const double* z,
-              const pr76::DeviceOutputs& d) {
-    return g.ncell == ncell && g.p == p && g.t == t && g.z == z &&
+              const double* warm, const pr76::DeviceOutputs& d) {
+    return g.ncell == ncell && g.p == p && g.t == t && g.z == z && g.warm == warm &&
            std::memcmp(&g.outputs, &d, sizeof(pr76::DeviceOutputs)) == 0;
 }
 
 int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
-               const pr76::DeviceOutputs& d_in, cudaStream_t stream) {
+               const double* warm, const pr76::DeviceOutputs& d_in, cudaStream_t stream) {
+    if (warm && h->form == MPMC_FORM_PLAIN_FP64)
+        return fail(MPMC_ERR_UNSUPPORTED,
+                    "ln K warm starts need a work-queue form (MPMC_FORM_MIXED or MPMC_FORM_BATCHED); the plain "
+                    "form is the reference algorithm, which has no warm start");
     pr76::DeviceOutputs d = d_in;
     int rc = prepare_device(h, ncell, d);
     if (rc != MPMC_OK) return rc;
@@ -280,15 +292,17 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
     if (h->stage_timing && !h->events[0]) {
         for (auto& ev : h->events)
             if ((e = cudaEventCreate(&ev)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+        for (auto& ev : h->redo_events)
+            if ((e = cudaEventCreate(&ev)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
     }
     if (!h->use_graphs || h->stage_timing) {
-        e = enqueue_device(h, ncell, p, t, z, d, stream, h->stage_timing);
+        e = enqueue_device(h, ncell, p, t, z, warm, d, stream, h->stage_timing);
         return e == cudaSuccess ? MPMC_OK : cuda_fail(e, "flash kernel launch");
     }
     // CUDA graph of the launch sequence, one per (cells, buffers): captured on
     // the handle's stream at the first call, replayed on `stream` afterwards
     for (GraphEntry& g : h->graphs) {
-        if (!same_key(g, ncell, p, t, z, d)) continue;
+        if (!same_key(g, ncell, p, t, z, warm, d)) continue;
         g.last_use = ++h->graph_clock;
         e = cudaGraphLaunch(g.exec, stream);
         return e == cudaSuccess ? MPMC_OK : cuda_fail(e, "cudaGraphLaunch");
@@ -296,7 +310,7 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
     cudaGraph_t graph = nullptr;
     if ((e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
         return cuda_fail(e, "cudaStreamBeginCapture");
-    const cudaError_t le = enqueue_device(h, ncell, p, t, z, d, h->stream, false);
+    const cudaError_t le = enqueue_device(h, ncell, p, t, z, warm, d, h->stream, false);
     e = cudaStreamEndCapture(h->stream, &graph);
     if (le != cudaSuccess || e != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
@@ -310,6 +324,7 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
     entry.p = p;
     entry.t = t;
     entry.z = z;
+    entry.warm = warm;
     entry.outputs = d;
     entry.last_use = ++h->graph_clock;
     if (h->graphs.size() >= kMaxGraphs) {  // evict the least recently used
@@ -433,7 +448,7 @@ int mpmc_gpu_flash_components(const mpmc_gpu_flash* h) { return h ? h->n : 0; }
 int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* h, int64_t* out, int capacity) {
     if (!h || (h->form != MPMC_FORM_MIXED && h->form != MPMC_FORM_BATCHED) || !h->workspace.ptr) return 0;
     // workspace counter slots (pr76_batched.cuh Slot) in the documented order
-    constexpr int kSlots[] = {8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 20, 22, 23, 24, 25};
+    constexpr int kSlots[] = {8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 20, 22, 23, 24, 25, 27, 28};
     constexpr int kCount = static_cast<int>(sizeof(kSlots) / sizeof(kSlots[0]));
     int vals[32] = {};
     if (cudaSetDevice(h->device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return 0;
@@ -451,6 +466,15 @@ int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* h, float* ms, int capacity) {
     for (int k = 0; k < stages && k < capacity; ++k) {
         float v = 0.f;
         cudaEventElapsedTime(&v, h->events[k], h->events[k + 1]);
+        // after a warm pass, each stage's time is that of both passes
+        if (h->timed_warm && k < pr76::kBatchedStages) {
+            float r = 0.f;
+            cudaEventElapsedTime(&r, h->redo_events[k], h->redo_events[k + 1]);
+            v += r;
+        } else if (h->timed_warm && k == pr76::kBatchedStages) {
+            // the sensitivity stage follows the cold pass
+            cudaEventElapsedTime(&v, h->redo_events[pr76::kBatchedStages], h->events[k + 1]);
+        }
         if (ms) ms[k] = v;
     }
     return stages;
@@ -500,10 +524,13 @@ int mpmc_gpu_flash_destroy(mpmc_gpu_flash* h) {
     h->in_p.release();
     h->in_t.release();
     h->in_z.release();
+    h->in_warm.release();
     for (auto& b : h->outs) b.release();
     for (auto& b : h->sens_inputs) b.release();
     h->workspace.release();
     for (auto& ev : h->events)
+        if (ev) cudaEventDestroy(ev);
+    for (auto& ev : h->redo_events)
         if (ev) cudaEventDestroy(ev);
     for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
     if (h->d_mixture) cudaFree(h->d_mixture);
@@ -514,13 +541,19 @@ int mpmc_gpu_flash_destroy(mpmc_gpu_flash* h) {
 
 int mpmc_gpu_flash_solve_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t,
                                 const double* z, const mpmc_flash_outputs* out, void* stream) {
+    return mpmc_gpu_flash_solve_device_warm(h, ncell, p, t, z, nullptr, out, stream);
+}
+
+int mpmc_gpu_flash_solve_device_warm(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t,
+                                     const double* z, const double* ln_k_warm, const mpmc_flash_outputs* out,
+                                     void* stream) {
     if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
     if (ncell < 0) return fail(MPMC_ERR_INVALID_ARGUMENT, "negative cell count");
     if (ncell == 0) return MPMC_OK;
     if (!p || !t || !z) return fail(MPMC_ERR_INVALID_ARGUMENT, "p, t and z must not be null");
     cudaError_t e = cudaSetDevice(h->device);
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
-    return run_device(h, ncell, p, t, z, to_device_outputs(out), static_cast<cudaStream_t>(stream));
+    return run_device(h, ncell, p, t, z, ln_k_warm, to_device_outputs(out), static_cast<cudaStream_t>(stream));
 }
 
 int mpmc_gpu_flash_set_launch_shape(mpmc_gpu_flash* h, const int32_t* values, int count) {
@@ -576,6 +609,11 @@ int mpmc_gpu_flash_solve_device_noalloc(mpmc_gpu_flash* h, int64_t ncell, const 
 
 int mpmc_gpu_flash_solve(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
                          const mpmc_flash_outputs* out) {
+    return mpmc_gpu_flash_solve_warm(h, ncell, p, t, z, nullptr, out);
+}
+
+int mpmc_gpu_flash_solve_warm(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
+                              const double* ln_k_warm, const mpmc_flash_outputs* out) {
     if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
     if (ncell < 0) return fail(MPMC_ERR_INVALID_ARGUMENT, "negative cell count");
     if (ncell == 0) return MPMC_OK;
@@ -604,9 +642,16 @@ int mpmc_gpu_flash_solve(mpmc_gpu_flash* h, int64_t ncell, const double* p, cons
         (e = cudaMemcpyAsync(h->in_t.ptr, t, nc * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
         (e = cudaMemcpyAsync(h->in_z.ptr, z, n * nc * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess)
         return cuda_fail(e, "input copy");
+    const double* d_warm = nullptr;
+    if (ln_k_warm) {
+        if ((e = h->in_warm.ensure(n * nc * 8)) != cudaSuccess) return cuda_fail(e, "warm-start staging allocation");
+        if ((e = cudaMemcpyAsync(h->in_warm.ptr, ln_k_warm, n * nc * 8, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return cuda_fail(e, "warm-start copy");
+        d_warm = static_cast<const double*>(h->in_warm.ptr);
+    }
     const int rc = run_device(h, ncell, static_cast<const double*>(h->in_p.ptr),
                               static_cast<const double*>(h->in_t.ptr), static_cast<const double*>(h->in_z.ptr),
-                              to_device_outputs(&dev_out), s);
+                              d_warm, to_device_outputs(&dev_out), s);
     if (rc != MPMC_OK) return rc;
     for (int k = 0; k < kOutputFields; ++k) {
         void* hp = *field_ptr(&host_out, k);

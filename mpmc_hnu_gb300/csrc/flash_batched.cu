@@ -66,6 +66,7 @@ size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell, bool fp64
     ws.s64_status = reinterpret_cast<signed char*>(take(cap));
     ws.s64_state = reinterpret_cast<double*>(take(sizeof(double) * batched::S64Stride<NM>() * cap));
     ws.split_cells = reinterpret_cast<int*>(take(sizeof(int) * nc));
+    ws.warm_cell = reinterpret_cast<signed char*>(take(nc));
     ws.s64_cells = reinterpret_cast<int*>(take(sizeof(int) * nc));
     ws.s64_base = reinterpret_cast<int*>(take(sizeof(int) * nc));
     ws.s64_count = reinterpret_cast<int*>(take(sizeof(int) * nc));
@@ -101,10 +102,6 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     int device = 0, sms = 0;
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    cudaError_t e = cudaMemsetAsync(ws.counters, 0, sizeof(int) * qSlots, stream);
-    if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(ws.s64_items, 0xff, sizeof(int) * static_cast<size_t>(ws.s64_capacity), stream);
-    if (e != cudaSuccess) return e;
     const int cell_block = 64;
     // per-cell FP64 kernels and FP64 work items run best at low residency
     // (their per-thread local state then stays in L1/L2)
@@ -120,59 +117,78 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
                                                         : resident_blocks(split32_kernel<NM>, qblock);
     const int t64_res = shape.t64_blocks_per_sm > 0 ? shape.t64_blocks_per_sm : 2;
     const int s64_res = shape.s64_blocks_per_sm > 0 ? shape.s64_blocks_per_sm : 2;
-    int stage = 0;
-    auto mark = [&]() {
-        if (shape.events) cudaEventRecord(shape.events[stage], stream);
-        ++stage;
+    // one pass of the launch sequence over the cells `ws.pass` selects
+    auto run_pass = [&](cudaEvent_t* events) -> cudaError_t {
+        // the warm pass's statistics stay for the cold pass after it
+        const int clear = ws.pass == kPassRedo ? qPassSlots : qSlots;
+        cudaError_t e = cudaMemsetAsync(ws.counters, 0, sizeof(int) * clear, stream);
+        if (e != cudaSuccess) return e;
+        e = cudaMemsetAsync(ws.s64_items, 0xff, sizeof(int) * static_cast<size_t>(ws.s64_capacity), stream);
+        if (e != cudaSuccess) return e;
+        int stage = 0;
+        auto mark = [&]() {
+            if (events) cudaEventRecord(events[stage], stream);
+            ++stage;
+        };
+        mark();
+        setup_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, p, t, z, out);
+        mark();
+        // The FP64 form queues every trial and attempt as an exact FP64 item (the
+        // FP32 screening stages become empty), on the same stage slots.
+        if (fp64_items) rerun_all_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(ws, 0);
+        else trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 0);
+        mark();
+        classify_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, 0);
+        mark();
+        // one warp per trial item: items of slow descents dominate, so latency
+        // matters more than packing several items into a warp (measured)
+        if ((shape.item_form & 1) && !fp64_items) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+        else w64::trials64w_kernel<NM, 32><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
+        mark();
+        decide_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+        mark();
+        // FP32 successive substitution hands over to the FP64 Newton polish at
+        // |r| <= ss_switch (default 2e-5, a few times the FP32 rounding floor)
+        const float ss_switch = shape.ss_switch > 0.f ? shape.ss_switch : 2e-5f;
+        if (!fp64_items) split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t, ss_switch);
+        mark();
+        // polish: one cell per thread up to 12 components (its per-cell arrays
+        // still fit the cache), one cell per lane group above
+        const bool lane_polish = (shape.item_form & 8) ? true : ((shape.item_form & 16) ? false : NM <= 12);
+        if (lane_polish) polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+        else w64::polishw_kernel<NM, w64::kSeg<NM>><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t, out);
+        mark();
+        if ((shape.item_form & 4) && !fp64_items) split64_kernel<NM><<<sms * s64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+        else w64::split64w_kernel<NM, 32><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t);
+        mark();
+        select64_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+        mark();
+        relist_kernel<NM><<<1, 1024, 0, stream>>>(ws);
+        cudaMemsetAsync(ws.counters + qT64Items, 0, 2 * sizeof(int), stream);
+        mark();
+        if (fp64_items) rerun_all_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(ws, 1);
+        else trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 1);
+        mark();
+        classify_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, 1);
+        mark();
+        if ((shape.item_form & 2) && !fp64_items) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+        else w64::trials64w_kernel<NM, 32><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
+        mark();
+        finish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+        mark();
+        fallback_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, z, out);
+        mark();
+        return cudaGetLastError();
     };
-    mark();
-    setup_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, p, t, z, out);
-    mark();
-    // The FP64 form queues every trial and attempt as an exact FP64 item (the
-    // FP32 screening stages become empty), on the same stage slots.
-    if (fp64_items) rerun_all_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(ws, 0);
-    else trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 0);
-    mark();
-    classify_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, 0);
-    mark();
-    // one warp per trial item: items of slow descents dominate, so latency
-    // matters more than packing several items into a warp (measured)
-    if ((shape.item_form & 1) && !fp64_items) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
-    else w64::trials64w_kernel<NM, 32><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
-    mark();
-    decide_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
-    mark();
-    // FP32 successive substitution hands over to the FP64 Newton polish at
-    // |r| <= ss_switch (default 2e-5, a few times the FP32 rounding floor)
-    const float ss_switch = shape.ss_switch > 0.f ? shape.ss_switch : 2e-5f;
-    if (!fp64_items) split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t, ss_switch);
-    mark();
-    // polish: one cell per thread up to 12 components (its per-cell arrays
-    // still fit the cache), one cell per lane group above
-    const bool lane_polish = (shape.item_form & 8) ? true : ((shape.item_form & 16) ? false : NM <= 12);
-    if (lane_polish) polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
-    else w64::polishw_kernel<NM, w64::kSeg<NM>><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t, out);
-    mark();
-    if ((shape.item_form & 4) && !fp64_items) split64_kernel<NM><<<sms * s64_res, 64, 0, stream>>>(d_mix, ws, p, t);
-    else w64::split64w_kernel<NM, 32><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t);
-    mark();
-    select64_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
-    mark();
-    relist_kernel<NM><<<1, 1024, 0, stream>>>(ws);
-    cudaMemsetAsync(ws.counters + qT64Items, 0, 2 * sizeof(int), stream);
-    mark();
-    if (fp64_items) rerun_all_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(ws, 1);
-    else trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 1);
-    mark();
-    classify_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, 1);
-    mark();
-    if ((shape.item_form & 2) && !fp64_items) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
-    else w64::trials64w_kernel<NM, 32><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
-    mark();
-    finish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
-    mark();
-    fallback_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, z, out);
-    mark();
+    ws.warm_lnk = shape.warm_lnk;
+    ws.pass = shape.warm_lnk ? kPassWarm : kPassCold;
+    cudaError_t e = run_pass(shape.events);
+    if (e != cudaSuccess || !shape.warm_lnk) return e;
+    // the warm cells whose pair was not accepted: the full cold solve (a
+    // nearly empty pass when the warm starts are good)
+    ws.pass = kPassRedo;
+    e = run_pass(shape.redo_events);
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 

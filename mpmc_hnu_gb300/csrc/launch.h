@@ -62,6 +62,10 @@ struct BatchedShape {
     float ss_switch;      // FP32 |r| at which successive substitution hands over to the FP64
                           // Newton polish (0 = 2e-5)
     int fp64_items;       // batched FP64 form: every trial and attempt as an exact FP64 item
+    // per call: ln K warm starts (device, [n * ncell], a non-finite entry makes
+    // the cell cold); null = cold solve of every cell
+    const double* warm_lnk;
+    cudaEvent_t* redo_events;  // optional: the events of the cold pass after a warm pass
 };
 constexpr int kBatchedStages = 15;
 

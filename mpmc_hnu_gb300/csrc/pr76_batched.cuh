@@ -77,6 +77,9 @@ enum Slot : int {
     sSlowSkipped = 24,     // slow trials whose outcome could not change the cell's status
     sLimitAttempts = 25,   // attempts classified as ending at the iteration limit
     qPolishCursor = 26,    // warp queue over the polish list
+    qPassSlots = 27,       // slots above are cleared at the start of every pass
+    sWarmCells = 27,       // cells run from their warm start (warm pass)
+    sWarmRedo = 28,        // of those, cells whose pair was not accepted (cold pass)
     qSlots = 32
 };
 
@@ -88,8 +91,16 @@ __host__ __device__ constexpr int S64Stride() { return 8 + 6 * NM; }
 // Cell phases kept in Workspace::phase.
 enum Phase : int {
     pInvalid = -1, pSingle = 0, pTwo = 1, pUnstable = 2, pIndeterminate = 3,
-    pPending = 10, pSplit = 11, pReview = 12, pFallback = 13, pSplit64 = 14
+    pPending = 10, pSplit = 11, pReview = 12, pFallback = 13, pSplit64 = 14,
+    pRedo = 15  // warm pass: the warm pair was not accepted, the cell runs the cold pass
 };
+
+// Passes of the launch sequence: the cold solve of every cell; the warm pass
+// (each cell with a usable ln K warm start runs one split attempt from it and
+// the common-tangent review, no feed test, while the other cells take the
+// cold path in the same pass); the cold solve of the warm cells whose pair was
+// not accepted.
+enum Pass : int { kPassCold = 0, kPassWarm = 1, kPassRedo = 2 };
 
 // Device workspace for one batch (all arrays entry-major, cell fastest).
 struct Workspace {
@@ -122,6 +133,9 @@ struct Workspace {
     double* s64_state;      // [s64_capacity * S64Stride] converged attempt states
     short* att_iter;        // [kMaxAttempts * ncell] FP32 SS iterations of the attempt
     double* att_lnk64;      // [kMaxAttempts * NM * ncell] FP64 seeds (batched FP64 form only, else null)
+    const double* warm_lnk; // [n * ncell] caller's ln K warm starts (NaN = cold), warm pass only
+    signed char* warm_cell; // [ncell] 1 = the cell runs from its warm start in the warm pass
+    int pass;               // Pass
     float* att_rate;        // [kMaxAttempts * ncell] FP32 SS contraction per iteration, ln(|r| ratio)
     int* split_cells;       // [ncell] cells that reached the split stage
     int* s64_cells;         // [ncell] cells whose attempts were continued in FP64
@@ -129,6 +143,12 @@ struct Workspace {
     int* s64_count;         // [ncell]
     int s64_capacity;
 };
+
+// A cell of the warm pass that runs from its warm start: a rejected pair sends
+// it to the cold pass instead of settling its status.
+__device__ __forceinline__ bool warm_cell(const Workspace& ws, int64_t c) {
+    return ws.pass == kPassWarm && ws.warm_cell[c] != 0;
+}
 
 __device__ __forceinline__ int64_t idx(int k, int64_t ncell, int64_t c) { return static_cast<int64_t>(k) * ncell + c; }
 
@@ -181,6 +201,7 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
     stage_mixture(mix_g, m);
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; c < ws.ncell; c += stride) {
+        if (ws.pass == kPassRedo && ws.phase[c] != pRedo) continue;  // settled by the warm pass
         fp64::Cell<NM> cell;
         cell.n = m.n;
         cell.newton = true;
@@ -198,6 +219,21 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
                 if (feed[i] > 0.0 && cell.z[i] == 0.0) ph = pIndeterminate;
         }
         for (int i = 0; i < cell.n; ++i) ws.z[idx(i, ws.ncell, c)] = ph == pInvalid ? 0.0 : cell.z[i];
+        bool warm = false;
+        if (ph == pPending && ws.pass == kPassWarm) {
+            // a usable warm start: finite on every component present, not all zero
+            warm = true;
+            double contrast = 0.0;
+            for (int i = 0; i < cell.n; ++i) {
+                if (cell.z[i] == 0.0) continue;
+                const double v = ws.warm_lnk[idx(i, ws.ncell, c)];
+                warm = warm && isfinite(v) && fabs(v) < 700.0;
+                contrast = fmax(contrast, fabs(v));
+            }
+            warm = warm && contrast > 0.0;  // else: the cold path in this pass
+        }
+        if (ws.pass != kPassRedo) ws.warm_cell[c] = warm ? 1 : 0;
+        if (warm) atomicAdd(&ws.counters[sWarmCells], 1);
         if (ph == pPending) {
             double lp[NM], zref = 0.0;
             bool smooth;
@@ -221,10 +257,30 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
                 }
             }
         }
-        ws.phase[c] = ph;
         ws.att_count[c] = 0;
-        for (int k = 0; k < cCount; ++k) ws.counters_out[idx(k, ws.ncell, c)] = 0;
-        ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)] = cell.counters[cInitEvals];
+        if (ph == pPending && warm) {
+            // one split attempt from the caller's ln K, entered as attempt 0
+            for (int i = 0; i < cell.n; ++i) {
+                const double v = cell.z[i] > 0.0 ? ws.warm_lnk[idx(i, ws.ncell, c)] : 0.0;
+                ws.att_lnk[idx(i, ws.ncell, c)] = static_cast<float>(v);
+                if (ws.att_lnk64) ws.att_lnk64[idx(i, ws.ncell, c)] = v;
+            }
+            ws.att_class[idx(0, ws.ncell, c)] = fp32::aFailed;  // overwritten by split32
+            ws.att_iter[idx(0, ws.ncell, c)] = 0;
+            ws.att_count[c] = 1;
+            ws.attempt_items[atomicAdd(&ws.counters[qAttempts], 1)] = static_cast<int>(c) << 5;
+            ws.split_cells[atomicAdd(&ws.counters[qSplitCells], 1)] = static_cast<int>(c);
+            ph = pSplit;
+        }
+        ws.phase[c] = ph;
+        if (ws.pass != kPassRedo) {
+            for (int k = 0; k < cCount; ++k) ws.counters_out[idx(k, ws.ncell, c)] = 0;
+            ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)] = cell.counters[cInitEvals];
+            if (ph == pSplit) ws.counters_out[idx(cAttempts, ws.ncell, c)] = 1;
+        } else {
+            // the warm attempt's work stays counted
+            ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)] += cell.counters[cInitEvals];
+        }
         if (ph == pInvalid || ph == pIndeterminate) {
             const double nan = __longlong_as_double(0x7ff8000000000000LL);
             if (out.status) out.status[c] = ph == pInvalid ? static_cast<int>(kInvalid) : static_cast<int>(kIndeterminate);
@@ -1084,6 +1140,11 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
             int cnt = 0;
             for (int a = 0; a < na; ++a) cnt += unsettled(ws.att_class[idx(a, ws.ncell, c)]);
             if (cnt == 0) {
+                if (warm_cell(ws, c)) {  // the warm attempt collapsed: solve the cell cold
+                    ws.phase[c] = pRedo;
+                    atomicAdd(&ws.counters[sWarmRedo], 1);
+                    continue;
+                }
                 ws.phase[c] = pIndeterminate;  // every attempt collapsed to the trivial solution
                 write_status_only<NM>(out, ws, c, kIndeterminate, false);
                 write_counters<NM>(out, ws, c);
@@ -1176,6 +1237,12 @@ __global__ void __launch_bounds__(64) finish_kernel(const Mixture* __restrict__ 
         if (negative) status = kPhaseSetUnstable;
         else if (ws.cand_s[idx(4, ws.ncell, c)] > ws.cand_s[idx(5, ws.ncell, c)]) status = kIndeterminate;
         else status = stationary ? kTwoPhase : kIndeterminate;
+        if (warm_cell(ws, c) && status != kTwoPhase) {
+            // only an accepted warm pair settles a cell; anything else gets the full cold solve
+            ws.phase[c] = pRedo;
+            atomicAdd(&ws.counters[sWarmRedo], 1);
+            continue;
+        }
         ws.phase[c] = status;
         write_status_only<NM>(out, ws, c, status, true);
         write_counters<NM>(out, ws, c);
@@ -1206,6 +1273,7 @@ __global__ void __launch_bounds__(64) fallback_kernel(const Mixture* __restrict_
         Scratch<NM> w;
         CellResult<NM> r;
         const int status = solve_cell(m, cell, feed, w, r);
+        ws.phase[c] = status;  // settled: a later pass of the same launch leaves it alone
         const int n = cell.n;
         const double nan = __longlong_as_double(0x7ff8000000000000LL);
         if (out.status) out.status[c] = status;

@@ -481,6 +481,11 @@ __global__ void __launch_bounds__(64) select64_kernel(const Mixture* __restrict_
             }
         }
         if (best < 0) {
+            if (warm_cell(ws, c)) {  // no converged warm attempt: solve the cell cold
+                ws.phase[c] = pRedo;
+                atomicAdd(&ws.counters[sWarmRedo], 1);
+                continue;
+            }
             ws.phase[c] = pIndeterminate;
             write_status_only<NM>(out, ws, c, kIndeterminate, false);
             write_counters<NM>(out, ws, c);

@@ -1122,7 +1122,10 @@ __global__ void __launch_bounds__(128) polishw_kernel(const Mixture* __restrict_
                 // FP64 continuation of every attempt FP32 left unsettled (split64 items)
                 int cnt = 0;
                 for (int a = 0; a < na; ++a) cnt += unsettled(ws.att_class[idx(a, ws.ncell, c)]);
-                if (cnt == 0) {
+                if (cnt == 0 && warm_cell(ws, c)) {
+                    ws.phase[c] = pRedo;  // the warm attempt collapsed: solve the cell cold
+                    atomicAdd(&ws.counters[sWarmRedo], 1);
+                } else if (cnt == 0) {
                     ws.phase[c] = pIndeterminate;  // every attempt collapsed or ended at the limit
                     write_status_only<NM>(out, ws, c, kIndeterminate, false);
                     write_counters<NM>(out, ws, c);

@@ -72,13 +72,14 @@ EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu
                     "mpmc_gpu_flash_abi_version", "mpmc_gpu_flash_stage_timings", "mpmc_gpu_flash_batch_stats",
                     "mpmc_gpu_flash_solve_device_noalloc", "mpmc_flash_server_create", "mpmc_flash_server_add_mixture",
                     "mpmc_flash_server_submit", "mpmc_flash_server_wait", "mpmc_flash_server_stats",
-                    "mpmc_flash_server_destroy", "mpmc_gpu_flash_set_launch_shape"]
+                    "mpmc_flash_server_destroy", "mpmc_gpu_flash_set_launch_shape", "mpmc_gpu_flash_solve_warm",
+                    "mpmc_gpu_flash_solve_device_warm"]
 FLAG_CUDA_GRAPH = 2
 NOALLOC_SCRATCH_BYTES = 48 << 20
 BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun", "fallback_nonsmooth",
                "fp64_attempts_no_fp32", "fp64_attempts_polish_failed", "fp64_attempts_rejected", "fallback_load",
                "two_candidates", "fp64_trial_items", "fp64_attempt_items", "polished_cells", "select64_cells",
-               "slow_trials_skipped", "limit_attempts"]
+               "slow_trials_skipped", "limit_attempts", "warm_cells", "warm_redo"]
 FLAG_STAGE_TIMING = 1
 _QUEUE_STAGES = ["setup", "feed_trials", "feed_classify", "feed_trials64", "decide", "split", "polish",
                  "split64", "select64", "relist", "review_trials", "review_classify", "review_trials64",
@@ -105,6 +106,10 @@ def library() -> ctypes.CDLL:
         lib.mpmc_gpu_flash_solve_device.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 3 + \
             [ctypes.POINTER(_Outputs), ctypes.c_void_p]
         lib.mpmc_gpu_flash_solve_device_noalloc.argtypes = lib.mpmc_gpu_flash_solve_device.argtypes
+        lib.mpmc_gpu_flash_solve_warm.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 4 + \
+            [ctypes.POINTER(_Outputs)]
+        lib.mpmc_gpu_flash_solve_device_warm.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 4 + \
+            [ctypes.POINTER(_Outputs), ctypes.c_void_p]
         lib.mpmc_gpu_flash_components.argtypes = [ctypes.c_void_p]
         lib.mpmc_gpu_flash_stage_timings.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         lib.mpmc_gpu_flash_batch_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
@@ -173,21 +178,28 @@ class GpuFlash:
         sens = self.sensitivity if want_sensitivity is None else want_sensitivity
         return FLASH_FIELDS + (SENSITIVITY_FIELDS if sens else [])
 
-    def solve(self, p, t, z, fields: list[str] | None = None) -> dict[str, np.ndarray]:
-        """Host arrays in, host arrays out (the copies happen inside the call)."""
+    def solve(self, p, t, z, fields: list[str] | None = None, ln_k_warm=None) -> dict[str, np.ndarray]:
+        """Host arrays in, host arrays out (the copies happen inside the call).
+        `ln_k_warm` [n, ncell] (optional): ln K warm starts, NaN columns cold
+        (mpmc_gpu_flash_solve_warm)."""
         p = np.ascontiguousarray(p, dtype=np.float64)
         t = np.ascontiguousarray(t, dtype=np.float64)
         z = np.ascontiguousarray(z, dtype=np.float64)
         if z.shape != (self.n, p.shape[0]) or t.shape != p.shape:
             raise ValueError("expected p[ncell], t[ncell], z[n, ncell]")
+        warm = None
+        if ln_k_warm is not None:
+            warm = np.ascontiguousarray(ln_k_warm, dtype=np.float64)
+            if warm.shape != z.shape:
+                raise ValueError("expected ln_k_warm[n, ncell]")
         ncell = p.shape[0]
         fields = fields or self.fields()
         rows = output_rows(self.n)
         dtypes = {f: d for f, d, _ in OUTPUT_FIELDS}
         out = {f: np.empty((rows[f], ncell), dtypes[f]) for f in fields}
         s = _Outputs(**{f: out[f].ctypes.data for f in fields})
-        _check(library().mpmc_gpu_flash_solve(self._h, ncell, p.ctypes.data, t.ctypes.data, z.ctypes.data,
-                                              ctypes.byref(s)))
+        _check(library().mpmc_gpu_flash_solve_warm(self._h, ncell, p.ctypes.data, t.ctypes.data, z.ctypes.data,
+                                                   None if warm is None else warm.ctypes.data, ctypes.byref(s)))
         return {f: (v[0] if rows[f] == 1 else v) for f, v in out.items()}
 
     def solve_host_ptrs(self, ncell: int, p_ptr: int, t_ptr: int, z_ptr: int, out_ptrs: dict[str, int]) -> None:
@@ -214,11 +226,16 @@ class GpuFlash:
         return {names[i] if i < len(names) else f"stage{i}": float(ms[i]) for i in range(max(k, 0))}
 
     def solve_device(self, ncell: int, p_ptr: int, t_ptr: int, z_ptr: int, out_ptrs: dict[str, int],
-                     stream: int = 0) -> None:
-        """Device pointers in and out; enqueued on `stream` (no synchronisation)."""
+                     stream: int = 0, warm_ptr: int = 0) -> None:
+        """Device pointers in and out; enqueued on `stream` (no synchronisation).
+        `warm_ptr`: device ln K warm starts [n, ncell] (0 = cold solve)."""
         s = _Outputs(**out_ptrs)
-        _check(library().mpmc_gpu_flash_solve_device(self._h, ncell, p_ptr, t_ptr, z_ptr, ctypes.byref(s),
-                                                     stream))
+        if warm_ptr:
+            _check(library().mpmc_gpu_flash_solve_device_warm(self._h, ncell, p_ptr, t_ptr, z_ptr, warm_ptr,
+                                                              ctypes.byref(s), stream))
+        else:
+            _check(library().mpmc_gpu_flash_solve_device(self._h, ncell, p_ptr, t_ptr, z_ptr, ctypes.byref(s),
+                                                         stream))
 
     def solve_device_noalloc(self, ncell: int, p_ptr: int, t_ptr: int, z_ptr: int, out_ptrs: dict[str, int],
                              stream: int = 0) -> None:
