@@ -1007,7 +1007,9 @@ __device__ bool polish_split(const Mixture& m, fp64::Cell<NM>& c64, PolishScratc
         for (int i = 0; i < n; ++i) s.d[i] = -s.st.res[i];
         if (!ad::lu_solve(s.J, s.piv, n, s.d)) return false;
         for (int i = 0; i < n; ++i) s.lnk[i] = s.st.lnk[i] + s.d[i];
-        if (fp64::split_evaluate(m, c64, s.lnk, s.nx, evals, 1 << 30, s.e, s.num, true) != fp64::kConverged)
+        // RR Newton from the current beta: a chord step moves ln K by |F| or less
+        if (fp64::split_evaluate(m, c64, s.lnk, s.nx, evals, 1 << 30, s.e, s.num, true, s.st.beta) !=
+            fp64::kConverged)
             return prev <= 1e-11;
         if (!(s.nx.fug < prev)) return prev <= 1e-11;
         fp64::copy_state(s.st, s.nx, n);

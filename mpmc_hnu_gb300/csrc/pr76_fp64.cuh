@@ -555,9 +555,11 @@ struct SplitState {
 // bisection (used by the mixed form's polish; the plain form uses bisection,
 // rachford_rice.hpp:93-107).  Both stop at the reference's width test
 // 8 eps min(beta, 1 - beta) and apply the same residual and balance checks.
+// Newton starts at `beta0` (the root of a nearby ln K, e.g. the previous
+// chord step's) inside the bracket (0, 1), else at 1/2.
 template <int NM>
 __device__ int solve_rr(Cell<NM>& c, const double* lk, SplitState<NM>& s, double* e, double* num,
-                        bool newton = false) {
+                        bool newton = false, double beta0 = 0.5) {
     const int n = c.n;
     double contrast = 0.0;
     for (int i = 0; i < n; ++i)
@@ -585,6 +587,7 @@ __device__ int solve_rr(Cell<NM>& c, const double* lk, SplitState<NM>& s, double
     double left = 0.0, right = 1.0, beta = 0.5, value = 0.0;
     bool resolved = false;
     if (newton) {
+        if (beta0 > 0.0 && beta0 < 1.0) beta = beta0;
         for (int it = 0; it < 64; ++it) {
             ++c.counters[cRrIters];
             double v = 0.0, dv = 0.0;
@@ -685,9 +688,9 @@ enum AttemptStatus : int { kConverged = 0, kNoInteriorRr, kRrFailure, kIndisting
 // or the failure class.
 template <int NM>
 __device__ int split_evaluate(const Mixture& m, Cell<NM>& c, const double* lk, SplitState<NM>& s, int& evals,
-                              int budget, double* e, double* num, bool newton_rr = false) {
+                              int budget, double* e, double* num, bool newton_rr = false, double beta0 = 0.5) {
     const int n = c.n;
-    const int rr = solve_rr(c, lk, s, e, num, newton_rr || c.newton);
+    const int rr = solve_rr(c, lk, s, e, num, newton_rr || c.newton, beta0);
     if (rr != kRrInterior)
         return rr == kRrDegenerate ? kIndistinguishable : (rr == kRrNoInterior ? kNoInteriorRr : kRrFailure);
     if (evals >= budget) return kAttemptEvaluationLimit;

@@ -521,7 +521,7 @@ struct Split {
 
 // Rachford-Rice by bracketed Newton (rachford_rice.hpp:70-147 checks).
 template <int NM, int S>
-__device__ int rachford_rice(WCell<NM, S>& c, double lk, Split& s) {
+__device__ int rachford_rice(WCell<NM, S>& c, double lk, Split& s, double beta0 = 0.5) {
     const double contrast = wmax<S>(c.act ? fabs(lk) : 0.0);
     if (contrast == 0.0) return fp64::kRrDegenerate;
     double ls[2];
@@ -538,7 +538,8 @@ __device__ int rachford_rice(WCell<NM, S>& c, double lk, Split& s) {
     const double num = c.act ? (lk >= 0.0 ? -expm1(-lk) : expm1(lk)) : 0.0;
     const bool pos = lk >= 0.0;
     auto den_at = [&](double beta) { return pos ? beta + (1.0 - beta) * e : (1.0 - beta) + beta * e; };
-    double left = 0.0, right = 1.0, beta = 0.5, value = 0.0;
+    // Newton from beta0 (the root of a nearby ln K: the previous iterate's)
+    double left = 0.0, right = 1.0, beta = beta0 > 0.0 && beta0 < 1.0 ? beta0 : 0.5, value = 0.0;
     bool resolved = false;
     for (int it = 0; it < 64; ++it) {
         ++c.counters[cRrIters];
@@ -616,8 +617,8 @@ __device__ int rachford_rice(WCell<NM, S>& c, double lk, Split& s) {
 
 // Split evaluation at ln K (pt_split.hpp:300-341).
 template <int NM, int S>
-__device__ int split_evaluate(WCell<NM, S>& c, double lk, Split& s, int& evals, int budget) {
-    const int rr = rachford_rice(c, lk, s);
+__device__ int split_evaluate(WCell<NM, S>& c, double lk, Split& s, int& evals, int budget, double beta0 = 0.5) {
+    const int rr = rachford_rice(c, lk, s, beta0);
     if (rr != fp64::kRrInterior)
         return rr == fp64::kRrDegenerate ? fp64::kIndistinguishable
                                          : (rr == fp64::kRrNoInterior ? fp64::kNoInteriorRr : fp64::kRrFailure);
@@ -691,7 +692,7 @@ __device__ int attempt(WCell<NM, S>& c, double lk0, Split& point, int& evals, in
         bool accepted = false;
         for (int bt = 0; bt < 24; ++bt, alpha *= 0.5) {
             const double lk = c.act ? point.lnk + (alpha / scale) * point.res : 0.0;
-            st = split_evaluate(c, lk, next, evals, 20000);
+            st = split_evaluate(c, lk, next, evals, 20000, point.beta);
             if (st == fp64::kAttemptEvaluationLimit) return st;
             if (st != fp64::kConverged) continue;
             const double predicted = -alpha * slope;
@@ -877,7 +878,7 @@ __device__ bool polish(WCell<NM, S>& c, double lk, Split& st) {
         const double d = lu_solve_rows<NM, S>(J, c.n, piv, c.act ? -st.res : 0.0);
         if (wany<S>(c.comp && !isfinite(d))) return prev <= 1e-11;
         const double next_lk = c.act ? st.lnk + d : 0.0;
-        if (split_evaluate(c, next_lk, nx, evals, 1 << 30) != fp64::kConverged) return prev <= 1e-11;
+        if (split_evaluate(c, next_lk, nx, evals, 1 << 30, st.beta) != fp64::kConverged) return prev <= 1e-11;
         if (!(nx.fug < prev)) return prev <= 1e-11;
         st = nx;
         prev = st.fug;
