@@ -274,7 +274,9 @@ int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* handle, float* ms, int capacity
  * already negative, [15] split attempts classified as ending at the
  * iteration limit without an FP64 run, [16] cells run from their ln K warm
  * start, [17] of those, cells whose pair was not accepted and that took the
- * cold pass.  After a warm-start solve, [0]-[15] count the cold pass.
+ * cold pass, [18] of those, cells with no converged attempt, [19] of those,
+ * cells whose review found a negative TPD.  After a warm-start solve,
+ * [0]-[15] count the cold pass.
  * Writes up to `capacity` values; returns the number available (0 for the
  * plain form).  Diagnostic entry point with no counterpart in the reference. */
 int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* handle, int64_t* out, int capacity);

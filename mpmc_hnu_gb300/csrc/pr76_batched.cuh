@@ -80,6 +80,8 @@ enum Slot : int {
     qPassSlots = 27,       // slots above are cleared at the start of every pass
     sWarmCells = 27,       // cells run from their warm start (warm pass)
     sWarmRedo = 28,        // of those, cells whose pair was not accepted (cold pass)
+    sWarmNoPair = 29,      // ... because no attempt converged to an accepted pair
+    sWarmUnstable = 30,    // ... because the review found a negative TPD
     qSlots = 32
 };
 
@@ -259,9 +261,30 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
         }
         ws.att_count[c] = 0;
         if (ph == pPending && warm) {
-            // one split attempt from the caller's ln K, entered as attempt 0
+            // One split attempt from the caller's ln K, entered as attempt 0.
+            // A guess near the phase boundary (beta near 0 or 1) whose
+            // Rachford-Rice function has no root in (0, 1) (rachford_rice.hpp:
+            // 86-92: ln sum z K > 0 and ln sum z / K > 0) is moved by the
+            // smallest common shift of ln K that puts the root inside again.
+            double ls[2];
+            for (int k = 0; k < 2; ++k) {
+                const double sign = k == 0 ? 1.0 : -1.0;
+                double largest = -INFINITY, sum = 0.0;
+                for (int i = 0; i < cell.n; ++i)
+                    if (cell.z[i] > 0.0) largest = fmax(largest, cell.lz[i] + sign * ws.warm_lnk[idx(i, ws.ncell, c)]);
+                for (int i = 0; i < cell.n; ++i)
+                    if (cell.z[i] > 0.0) sum += exp(cell.lz[i] + sign * ws.warm_lnk[idx(i, ws.ncell, c)] - largest);
+                ls[k] = largest + log(sum);
+            }
+            double shift = 0.0;
+            const double room = ls[0] + ls[1];  // >= 0 (Cauchy-Schwarz), 0 only for equal K
+            if (isfinite(room) && room > 1e-9) {
+                const double margin = fmin(1e-2, 0.25 * room);
+                if (ls[0] < margin) shift = margin - ls[0];
+                else if (ls[1] < margin) shift = ls[1] - margin;
+            }
             for (int i = 0; i < cell.n; ++i) {
-                const double v = cell.z[i] > 0.0 ? ws.warm_lnk[idx(i, ws.ncell, c)] : 0.0;
+                const double v = cell.z[i] > 0.0 ? ws.warm_lnk[idx(i, ws.ncell, c)] + shift : 0.0;
                 ws.att_lnk[idx(i, ws.ncell, c)] = static_cast<float>(v);
                 if (ws.att_lnk64) ws.att_lnk64[idx(i, ws.ncell, c)] = v;
             }
@@ -1145,6 +1168,7 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
                 if (warm_cell(ws, c)) {  // the warm attempt collapsed: solve the cell cold
                     ws.phase[c] = pRedo;
                     atomicAdd(&ws.counters[sWarmRedo], 1);
+                    atomicAdd(&ws.counters[sWarmNoPair], 1);
                     continue;
                 }
                 ws.phase[c] = pIndeterminate;  // every attempt collapsed to the trivial solution
@@ -1243,6 +1267,7 @@ __global__ void __launch_bounds__(64) finish_kernel(const Mixture* __restrict__ 
             // only an accepted warm pair settles a cell; anything else gets the full cold solve
             ws.phase[c] = pRedo;
             atomicAdd(&ws.counters[sWarmRedo], 1);
+            if (status == kPhaseSetUnstable) atomicAdd(&ws.counters[sWarmUnstable], 1);
             continue;
         }
         ws.phase[c] = status;

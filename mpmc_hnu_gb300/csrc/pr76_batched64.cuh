@@ -484,6 +484,7 @@ __global__ void __launch_bounds__(64) select64_kernel(const Mixture* __restrict_
             if (warm_cell(ws, c)) {  // no converged warm attempt: solve the cell cold
                 ws.phase[c] = pRedo;
                 atomicAdd(&ws.counters[sWarmRedo], 1);
+                atomicAdd(&ws.counters[sWarmNoPair], 1);
                 continue;
             }
             ws.phase[c] = pIndeterminate;

@@ -1126,6 +1126,7 @@ __global__ void __launch_bounds__(128) polishw_kernel(const Mixture* __restrict_
                 if (cnt == 0 && warm_cell(ws, c)) {
                     ws.phase[c] = pRedo;  // the warm attempt collapsed: solve the cell cold
                     atomicAdd(&ws.counters[sWarmRedo], 1);
+                    atomicAdd(&ws.counters[sWarmNoPair], 1);
                 } else if (cnt == 0) {
                     ws.phase[c] = pIndeterminate;  // every attempt collapsed or ended at the limit
                     write_status_only<NM>(out, ws, c, kIndeterminate, false);
