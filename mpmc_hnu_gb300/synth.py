@@ -97,3 +97,37 @@ def make_near_critical_cells(mixture, ncell: int, seed: int, fraction: float = 0
     t = np.where(pick, tpc * (1.0 + 0.02 * (uniform(seed, S_CRIT_T, c) - 0.5)), t)
     p = np.where(pick, np.exp(np.log(10e6) + (np.log(40e6) - np.log(10e6)) * uniform(seed, S_CRIT_P, c)), p)
     return np.ascontiguousarray(p), np.ascontiguousarray(t), z
+
+
+def three_phase_fixture_mixture():
+    """The three-component PR76 mixture of the reference's max3 tests
+    (tests/flash/pr76_three_phase/synthetic_fixture.hpp:33-57): a light
+    component and two symmetric heavy ones with k_12 = 0.20, which split into
+    three phases at 1 MPa and 250 K."""
+    return Mixture(np.array([190.6, 500.0, 500.0]), np.array([4.6e6, 5.0e6, 5.0e6]), np.array([0.01, 0.10, 0.10]),
+                   np.array([[0.0, 0.05, 0.05], [0.05, 0.0, 0.20], [0.05, 0.20, 0.0]]))
+
+
+# the three phases of that fixture at 1 MPa, 250 K (synthetic_fixture.hpp:63-72,
+# an independent root/equality solve recorded by the reference's tests)
+THREE_PHASE_ANCHOR = np.array([[0.04844395156186141, 0.9076712804842868, 0.0438847679538518],
+                               [0.9696550397025219, 0.015172480148739028, 0.015172480148739028],
+                               [0.048443951561861175, 0.04388476795385164, 0.9076712804842871]])
+
+
+def make_three_phase_cells(ncell: int, seed: int, anchor_fraction: float = 0.25):
+    """Cells for the max-3-phase path on the fixture mixture: a share at the
+    anchor state (1 MPa, 250 K, feeds inside the tie triangle: barycentric
+    weights ~ Dirichlet(1) over the anchor phases), the rest with p
+    log-uniform on [0.2, 5] MPa, T ~ U[200, 300] K, z ~ Dirichlet(1)."""
+    rng = np.random.default_rng(seed)
+    na = int(round(anchor_fraction * ncell))
+    z = rng.dirichlet(np.ones(3), ncell).T.copy()
+    t = rng.uniform(200.0, 300.0, ncell)
+    p = np.exp(rng.uniform(np.log(2e5), np.log(5e6), ncell))
+    w = rng.dirichlet(np.ones(3), na)
+    z[:, :na] = (w @ THREE_PHASE_ANCHOR).T
+    z[:, :na] /= z[:, :na].sum(axis=0)
+    p[:na] = 1e6
+    t[:na] = 250.0
+    return p, t, z

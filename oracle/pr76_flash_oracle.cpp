@@ -503,6 +503,7 @@ struct TpdPoint {
     std::vector<double> w, residual;
     double value = 0, guard = 0, stationarity = 0;
     bool smooth = true;
+    int branch = 0;  // root branch of the stability phase at w
 };
 struct Trial {
     std::vector<double> initial;
@@ -661,6 +662,7 @@ inline bool stability_test(const Model& m, Work& wk, double p, double t, const s
                 if (!std::isfinite(v)) return kNonfinite;
             is = tpd(w, res.feed, phase.ln_phi, ref, n, out);
             out.smooth = phase.smooth;
+            out.branch = phase.branch;
             return is;
         };
         bool support_lost = false;
@@ -1083,7 +1085,12 @@ struct FlashResult {
     long long split_evaluations = 0;
 };
 
-inline FlashResult solve_vle(const Model& m, Work& wk, double p, double t, const std::vector<double>& feed) {
+// pt_split.hpp:415-525 with its optional extra starts: `initial_starts` join
+// the automatic feed-test starts, `final_starts` precede the pair's x and y in
+// the review.
+inline FlashResult solve_vle(const Model& m, Work& wk, double p, double t, const std::vector<double>& feed,
+                             const std::vector<std::vector<double>>& initial_starts = {},
+                             const std::vector<std::vector<double>>& final_starts = {}) {
     FlashResult res;
     const int n = m.n;
     double sum;
@@ -1094,7 +1101,7 @@ inline FlashResult solve_vle(const Model& m, Work& wk, double p, double t, const
     }
     StabilityOptions so;
     SplitOptions sp;
-    if (!stability_test(m, wk, p, t, feed, so, {}, {}, res.initial)) {
+    if (!stability_test(m, wk, p, t, feed, so, initial_starts, {}, res.initial)) {
         res.status = kInvalid;
         return res;
     }
@@ -1152,7 +1159,9 @@ inline FlashResult solve_vle(const Model& m, Work& wk, double p, double t, const
         res.status = kIndeterminate;
         return res;
     }
-    std::vector<std::vector<double>> starts{cand.rr.x, cand.rr.y};
+    std::vector<std::vector<double>> starts(final_starts.begin(), final_starts.end());
+    starts.push_back(cand.rr.x);
+    starts.push_back(cand.rr.y);
     if (!stability_test(m, wk, p, t, z, fo, starts, cand.common, res.final_review)) {
         res.status = kInvalid;
         return res;
@@ -1166,6 +1175,496 @@ inline FlashResult solve_vle(const Model& m, Work& wk, double p, double t, const
     else
         res.status = kIndeterminate;
     return res;
+}
+
+// ---------------------------------------------------------------------------
+// Three-phase continuation, modules/flash/include/mpmc/flash/pt_three_phase.hpp
+struct ThreeOptions {  // :23-38
+    double cp_tolerance = 1e-11;
+    double mass_absolute = 1e-12;
+    double mass_relative = 1e-10;
+    double balance_tolerance = 2e-13;
+    double minimum_phase_fraction = 1e-10;
+    double log_separation = 1e-7;
+    double max_log_step = 2.0;
+    double residual_decrease = 1e-4;
+    int max_iterations = 512;
+    int max_backtracks = 32;
+    int max_balance_iterations = 192;
+    int max_balance_backtracks = 48;
+    long long max_evaluations = 30000;
+};
+enum ThreeStatus {  // :40-53
+    kTConverged, kTNoBalance, kTBalanceDegenerate, kTBalanceIterLimit, kTBalanceLineSearch, kTBalanceFailure,
+    kTPhaseDisappearance, kTIndistinguishable, kTPropertyFailure, kTIterationLimit, kTEvaluationLimit,
+    kTLineSearchFailed
+};
+struct ThreeState {  // :68-84
+    double fraction[3] = {0, 0, 0};
+    std::vector<double> x[3], ln_phi[3];
+    double zf[3] = {0, 0, 0};
+    std::vector<double> lk1, lk2, r1, r2, common;
+    double cp_norm = 0, gibbs = 0, guard = 0, rr_residual = 0, mass_abs = 0, mass_rel = 0;
+    int balance_iterations = 0;
+};
+struct ThreeResult {
+    ThreeStatus status = kTNoBalance;
+    bool has_point = false;
+    ThreeState point;
+    int disappearing = -1;
+    int iterations = 0;
+    long long evaluations = 0;
+};
+
+inline bool rr3_feasible(double b0, double b1) {  // :176-181
+    return std::isfinite(b0) && std::isfinite(b1) && b0 >= 0 && b1 >= 0 && b0 + b1 <= 1.0;
+}
+
+// rr3_evaluate, :183-233: compositions of the three phases at (beta_1, beta_2)
+// and the two balance residuals with their symmetric Jacobian.
+inline bool rr3_evaluate(const std::vector<double>& feed, const std::vector<double>& lk1,
+                         const std::vector<double>& lk2, double b0, double b1, std::vector<double> comp[3],
+                         double res[2], double jac[3]) {
+    if (!rr3_feasible(b0, b1)) return false;
+    const int n = static_cast<int>(feed.size());
+    const double beta0 = 1.0 - b0 - b1;
+    for (int k = 0; k < 3; ++k) comp[k].assign(n, 0.0);
+    double f0 = 0, c0 = 0, f1 = 0, c1 = 0, j00 = 0, k00 = 0, j01 = 0, k01 = 0, j11 = 0, k11 = 0;
+    for (int i = 0; i < n; ++i) {
+        if (feed[i] == 0) continue;
+        const double shift = std::max({0.0, lk1[i], lk2[i]});
+        const double e0 = std::exp(-shift);
+        const double e1 = std::exp(lk1[i] - shift);
+        const double e2 = std::exp(lk2[i] - shift);
+        const double den = beta0 * e0 + b0 * e1 + b1 * e2;
+        if (!std::isfinite(den) || !(den > 0)) return false;
+        const double x0 = feed[i] * e0 / den, x1 = feed[i] * e1 / den, x2 = feed[i] * e2 / den;
+        if (!std::isfinite(x0) || !std::isfinite(x1) || !std::isfinite(x2) || !(x0 > 0) || !(x1 > 0) ||
+            !(x2 > 0))
+            return false;
+        comp[0][i] = x0;
+        comp[1][i] = x1;
+        comp[2][i] = x2;
+        const double d1 = x1 - x0, d2 = x2 - x0;
+        kahan_add(d1, f0, c0);
+        kahan_add(d2, f1, c1);
+        kahan_add(-(d1 * d1) / feed[i], j00, k00);
+        kahan_add(-(d1 * d2) / feed[i], j01, k01);
+        kahan_add(-(d2 * d2) / feed[i], j11, k11);
+    }
+    res[0] = f0;
+    res[1] = f1;
+    jac[0] = j00;
+    jac[1] = j01;
+    jac[2] = j11;
+    return true;
+}
+
+enum Rr3Status { kRr3Success, kRr3Degenerate, kRr3IterLimit, kRr3LineSearch, kRr3Unrepresentable };
+struct Rr3Result {
+    Rr3Status status = kRr3Unrepresentable;
+    double fraction[2] = {0, 0};
+    std::vector<double> comp[3];
+    double residual = std::numeric_limits<double>::infinity();
+    double mass_abs = 0, mass_rel = 0;
+    int iterations = 0;
+};
+
+// solve_generalized_rr3, :235-340: damped Newton on the two independent phase
+// fractions inside the closed simplex, then normalised compositions and the
+// material-balance errors.
+inline Rr3Result solve_rr3(const std::vector<double>& feed, const std::vector<double>& lk1,
+                           const std::vector<double>& lk2, const double init[2], const ThreeOptions& o) {
+    Rr3Result r;
+    const int n = static_cast<int>(feed.size());
+    if (n == 0 || !rr3_feasible(init[0], init[1])) return r;
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(lk1[i]) || !std::isfinite(lk2[i])) return r;
+    double beta[2] = {init[0], init[1]};
+    std::vector<double> comp[3], ncomp[3];
+    double res[2], jac[3], nres[2], njac[3];
+    for (int iteration = 0;; ++iteration) {
+        if (!rr3_evaluate(feed, lk1, lk2, beta[0], beta[1], comp, res, jac)) return r;
+        r.iterations = iteration;
+        const double norm = std::max(std::abs(res[0]), std::abs(res[1]));
+        if (!std::isfinite(norm)) return r;
+        if (norm <= o.balance_tolerance) {
+            r.status = kRr3Success;
+            r.residual = norm;
+            break;
+        }
+        if (iteration >= o.max_balance_iterations) {
+            r.status = kRr3IterLimit;
+            return r;
+        }
+        const double det = jac[0] * jac[2] - jac[1] * jac[1];
+        const double det_scale = std::abs(jac[0] * jac[2]) + std::abs(jac[1] * jac[1]) + 1.0;
+        if (!std::isfinite(det) || std::abs(det) <= 256.0 * kEps * det_scale) {
+            r.status = kRr3Degenerate;
+            return r;
+        }
+        const double step[2] = {(-res[0] * jac[2] + jac[1] * res[1]) / det, (jac[1] * res[0] - jac[0] * res[1]) / det};
+        if (!std::isfinite(step[0]) || !std::isfinite(step[1])) return r;
+        bool accepted = false;
+        double alpha = 1.0;
+        for (int bt = 0; bt < o.max_balance_backtracks; ++bt, alpha *= 0.5) {
+            const double cand[2] = {beta[0] + alpha * step[0], beta[1] + alpha * step[1]};
+            if (!rr3_feasible(cand[0], cand[1])) continue;
+            if (!rr3_evaluate(feed, lk1, lk2, cand[0], cand[1], ncomp, nres, njac)) continue;
+            const double next_norm = std::max(std::abs(nres[0]), std::abs(nres[1]));
+            if (!std::isfinite(next_norm)) continue;
+            if (next_norm < norm || next_norm <= o.balance_tolerance) {
+                beta[0] = cand[0];
+                beta[1] = cand[1];
+                accepted = true;
+                break;
+            }
+        }
+        if (!accepted) {
+            r.status = kRr3LineSearch;
+            return r;
+        }
+    }
+    if (!rr3_evaluate(feed, lk1, lk2, beta[0], beta[1], comp, res, jac)) {
+        r.status = kRr3Unrepresentable;
+        return r;
+    }
+    r.fraction[0] = beta[0];
+    r.fraction[1] = beta[1];
+    for (int k = 0; k < 3; ++k) {
+        const double sum = kahan_sum(comp[k].data(), n);
+        if (!std::isfinite(sum) || !(sum > 0)) {
+            r.status = kRr3Unrepresentable;
+            return r;
+        }
+        for (double& v : comp[k]) v /= sum;
+        r.comp[k] = comp[k];
+    }
+    const double fr[3] = {1.0 - beta[0] - beta[1], beta[0], beta[1]};
+    double abs_err = 0, rel_err = 0;
+    for (int i = 0; i < n; ++i) {
+        const double recovered = fr[0] * r.comp[0][i] + fr[1] * r.comp[1][i] + fr[2] * r.comp[2][i];
+        const double err = std::abs(recovered - feed[i]);
+        abs_err = std::max(abs_err, err);
+        if (feed[i] > 0)
+            rel_err = std::max(rel_err, err / feed[i]);
+        else if (recovered != 0)
+            rel_err = std::numeric_limits<double>::infinity();
+    }
+    r.mass_abs = abs_err;
+    r.mass_rel = rel_err;
+    return r;
+}
+
+// pt_three_phase_log_distance, :342-366
+inline double log_distance(const std::vector<double>& a, const std::vector<double>& b,
+                           const std::vector<double>& feed) {
+    double d = 0;
+    for (size_t i = 0; i < feed.size(); ++i) {
+        if (feed[i] == 0) {
+            if (a[i] != 0 || b[i] != 0) return std::numeric_limits<double>::infinity();
+            continue;
+        }
+        if (!(a[i] > 0) || !(b[i] > 0)) return std::numeric_limits<double>::infinity();
+        const double v = std::abs(std::log(a[i]) - std::log(b[i]));
+        if (!std::isfinite(v)) return std::numeric_limits<double>::infinity();
+        d = std::max(d, v);
+    }
+    return d;
+}
+
+// iterate_pt_three_phase, :399-676.  `upper[k]` selects phase k's root side
+// (pr76_three_phase.hpp:26-106: lower = smallest, upper = largest admissible
+// root); `feed` is the caller's normalised feed, normalised once more here.
+inline ThreeResult iterate_three(const Model& m, Work& wk, double p, double t, const std::vector<double>& feed_in,
+                                 const std::vector<double>& lk1_0, const std::vector<double>& lk2_0,
+                                 const double frac0[2], const bool upper[3], const ThreeOptions& o) {
+    ThreeResult res;
+    const int n = m.n;
+    double input_sum = 1.0;
+    if (!check_composition(feed_in.data(), n, input_sum)) return res;  // a domain_error in the reference
+    std::vector<double> feed(n);
+    for (int i = 0; i < n; ++i) feed[i] = feed_in[i] / input_sum;
+    for (int i = 0; i < n; ++i)
+        if (feed_in[i] > 0 && feed[i] == 0) {
+            res.status = kTBalanceFailure;
+            return res;
+        }
+    // the state at (ln K1, ln K2); returns kTConverged for "evaluated", a
+    // step-error status, or kTPropertyFailure
+    SplitPhase phase;
+    auto evaluate_state = [&](const std::vector<double>& lk1, const std::vector<double>& lk2, const double seed[2],
+                              ThreeState& st) -> ThreeStatus {
+        const Rr3Result bal = solve_rr3(feed, lk1, lk2, seed, o);
+        switch (bal.status) {
+        case kRr3Success: break;
+        case kRr3Degenerate: return kTBalanceDegenerate;
+        case kRr3IterLimit: return kTBalanceIterLimit;
+        case kRr3LineSearch: return kTBalanceLineSearch;
+        case kRr3Unrepresentable: return kTNoBalance;
+        }
+        st.fraction[0] = 1.0 - bal.fraction[0] - bal.fraction[1];
+        st.fraction[1] = bal.fraction[0];
+        st.fraction[2] = bal.fraction[1];
+        for (int k = 0; k < 3; ++k) {
+            st.x[k] = bal.comp[k];
+            if (res.evaluations >= o.max_evaluations) return kTEvaluationLimit;
+            ++res.evaluations;
+            if (role_provider(m, wk, p, t, st.x[k].data(), upper[k], phase) != kOk) return kTPropertyFailure;
+            for (double v : phase.ln_phi)
+                if (!std::isfinite(v)) return kTPropertyFailure;
+            st.ln_phi[k] = phase.ln_phi;
+            st.zf[k] = phase.z;
+        }
+        st.rr_residual = bal.residual;
+        st.mass_abs = bal.mass_abs;
+        st.mass_rel = bal.mass_rel;
+        st.balance_iterations = bal.iterations;
+        st.lk1.assign(n, 0.0);
+        st.lk2.assign(n, 0.0);
+        st.r1.assign(n, 0.0);
+        st.r2.assign(n, 0.0);
+        st.common.assign(n, 0.0);
+        st.cp_norm = 0;
+        st.gibbs = 0;
+        double gc = 0, magnitude = 1, mc = 0;
+        for (int i = 0; i < n; ++i) {
+            if (feed[i] == 0) continue;
+            const double l0 = std::log(st.x[0][i]), l1 = std::log(st.x[1][i]), l2 = std::log(st.x[2][i]);
+            const double mu0 = l0 + st.ln_phi[0][i], mu1 = l1 + st.ln_phi[1][i], mu2 = l2 + st.ln_phi[2][i];
+            st.lk1[i] = l1 - l0;
+            st.lk2[i] = l2 - l0;
+            st.r1[i] = mu0 - mu1;
+            st.r2[i] = mu0 - mu2;
+            st.common[i] = (mu0 + mu1 + mu2) / 3.0;
+            st.cp_norm = std::max({st.cp_norm, std::abs(st.r1[i]), std::abs(st.r2[i])});
+            for (int k = 0; k < 3; ++k) {
+                const double lx = std::log(st.x[k][i]);
+                const double mu = lx + st.ln_phi[k][i];
+                kahan_add(st.fraction[k] * st.x[k][i] * mu, st.gibbs, gc);
+                kahan_add(st.fraction[k] * st.x[k][i] * (std::abs(lx) + std::abs(st.ln_phi[k][i])), magnitude, mc);
+            }
+        }
+        st.guard = 256.0 * kEps * magnitude;
+        if (!std::isfinite(st.cp_norm) || !std::isfinite(st.gibbs) || !std::isfinite(st.guard))
+            return kTPropertyFailure;
+        return kTConverged;
+    };
+    {
+        const ThreeStatus s = evaluate_state(lk1_0, lk2_0, frac0, res.point);
+        if (s != kTConverged) {
+            res.status = s;
+            return res;
+        }
+        res.has_point = true;
+    }
+    ThreeState next;
+    std::vector<double> nk1(n), nk2(n);
+    for (;;) {
+        ThreeState& pt = res.point;
+        if (pt.cp_norm <= o.cp_tolerance) {
+            if (pt.rr_residual > o.balance_tolerance || pt.mass_abs > o.mass_absolute || pt.mass_rel > o.mass_relative) {
+                res.status = kTBalanceFailure;
+                return res;
+            }
+            for (int k = 0; k < 3; ++k)
+                if (pt.fraction[k] <= o.minimum_phase_fraction) {
+                    res.status = kTPhaseDisappearance;
+                    res.disappearing = k;
+                    return res;
+                }
+            const double d01 = log_distance(pt.x[0], pt.x[1], feed), d02 = log_distance(pt.x[0], pt.x[2], feed),
+                         d12 = log_distance(pt.x[1], pt.x[2], feed);
+            if (!(d01 > o.log_separation) || !(d02 > o.log_separation) || !(d12 > o.log_separation)) {
+                res.status = kTIndistinguishable;
+                return res;
+            }
+            res.status = kTConverged;
+            return res;
+        }
+        if (res.iterations >= o.max_iterations) {
+            res.status = kTIterationLimit;
+            return res;
+        }
+        const double scale = std::max(1.0, pt.cp_norm / o.max_log_step);
+        bool accepted = false;
+        double alpha = 1.0;
+        for (int bt = 0; bt < o.max_backtracks; ++bt, alpha *= 0.5) {
+            for (int i = 0; i < n; ++i) {
+                nk1[i] = pt.lk1[i] + (alpha / scale) * pt.r1[i];
+                nk2[i] = pt.lk2[i] + (alpha / scale) * pt.r2[i];
+            }
+            const double seed[2] = {pt.fraction[1], pt.fraction[2]};
+            const ThreeStatus s = evaluate_state(nk1, nk2, seed, next);
+            if (s == kTEvaluationLimit) {
+                res.status = s;
+                return res;
+            }
+            if (s != kTConverged) continue;  // rejected evaluation
+            const double required = o.residual_decrease * (alpha / scale) * pt.cp_norm;
+            const bool progress = next.cp_norm <= o.cp_tolerance || pt.cp_norm - next.cp_norm > required;
+            const bool gibbs_ok = next.gibbs <= pt.gibbs + pt.guard + next.guard;
+            if (progress && gibbs_ok) {
+                std::swap(res.point, next);
+                accepted = true;
+                break;
+            }
+        }
+        if (!accepted) {
+            res.status = kTLineSearchFailed;
+            return res;
+        }
+        ++res.iterations;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Max-3-phase orchestration, modules/flash/include/mpmc/flash/pr76_three_phase.hpp:328-561
+// with the backend's default options (pr76_pt_flash_backend.hpp:190-206: no
+// caller start hints, 16 automatic attempts, new-phase seed fraction 0.1).
+enum Max3Status { kM3Single = 0, kM3Two = 1, kM3Three = 2, kM3Boundary = 3, kM3Higher = 4, kM3Indeterminate = 5 };
+struct Max3Result {
+    int status = kM3Indeterminate;  // Max3Status, or -1 for an invalid request
+    FlashResult base;
+    bool has_three = false;
+    ThreeState three;
+    bool has_neighbor = false;
+    FlashResult neighbor;
+    int attempts = 0;
+};
+
+// ln(a_i / b_i) on the feed support, pr76_three_phase.hpp:246-268
+inline bool log_ratio(const std::vector<double>& a, const std::vector<double>& b, const std::vector<double>& feed,
+                      std::vector<double>& out) {
+    out.assign(feed.size(), 0.0);
+    for (size_t i = 0; i < feed.size(); ++i) {
+        if (feed[i] == 0) {
+            if (a[i] != 0 || b[i] != 0) return false;
+            continue;
+        }
+        if (!(a[i] > 0) || !(b[i] > 0)) return false;
+        out[i] = std::log(a[i]) - std::log(b[i]);
+        if (!std::isfinite(out[i])) return false;
+    }
+    return true;
+}
+
+// Root sides a witness may follow, pr76_three_phase.hpp:270-300: the side of
+// the admissible root the witness sits on, both when there is only one.
+inline int witness_sides(const Model& m, Work& wk, double p, double t, const std::vector<double>& w, int branch,
+                         bool sides[2]) {
+    double amix, bmix, A, B;
+    if (!mix(m, wk.tc, w.data(), amix, bmix, wk.sums.data()) || !coefficients(p, t, amix, bmix, A, B)) return 0;
+    const RootSet roots = solve_roots(A, B);
+    if (roots.status != kRootSuccess) return 0;
+    int adm[3], na = 0;
+    for (int k = 0; k < roots.count; ++k)
+        if (roots.roots[k].slope_sign > 0) adm[na++] = k;
+    bool found = false;
+    for (int k = 0; k < na; ++k) found = found || adm[k] == branch;
+    if (na == 0 || !found) return 0;
+    if (na == 1) {
+        sides[0] = false;
+        sides[1] = true;
+        return 2;
+    }
+    if (branch == adm[0]) {
+        sides[0] = false;
+        return 1;
+    }
+    if (branch == adm[na - 1]) {
+        sides[0] = true;
+        return 1;
+    }
+    return 0;
+}
+
+inline Max3Result solve_max3(const Model& m, Work& wk, double p, double t, const std::vector<double>& feed) {
+    Max3Result r;
+    r.base = solve_vle(m, wk, p, t, feed);
+    switch (r.base.status) {
+    case kInvalid: r.status = -1; return r;
+    case kSinglePhase: r.status = kM3Single; return r;
+    case kTwoPhase: r.status = kM3Two; return r;
+    case kIndeterminate: r.status = kM3Indeterminate; return r;
+    case kPhaseSetUnstable: break;
+    }
+    if (!r.base.has_candidate) {
+        r.status = kM3Indeterminate;
+        return r;
+    }
+    const SplitState& pair = r.base.candidate;
+    const StabilityResult& review = r.base.final_review;
+    const std::vector<double>& nfeed = r.base.initial.feed;
+    const ThreeOptions to;
+    bool saw_higher = false, saw_boundary = false, limit = false;
+    // run_attempt of pr76_three_phase.hpp:379-455; true when the cell is settled
+    auto run_attempt = [&](const std::vector<double>& lk1, const std::vector<double>& lk2, const double fr[2],
+                           const bool upper[3]) -> bool {
+        if (r.attempts >= 16) {
+            limit = true;
+            return false;
+        }
+        ++r.attempts;
+        const ThreeResult eq = iterate_three(m, wk, p, t, nfeed, lk1, lk2, fr, upper, to);
+        if (eq.status == kTPhaseDisappearance) {
+            saw_boundary = true;
+            std::vector<std::vector<double>> starts;
+            for (int k = 0; k < 3; ++k)
+                if (k != eq.disappearing) starts.push_back(eq.point.x[k]);
+            if (starts.size() == 2) {
+                FlashResult nb = solve_vle(m, wk, p, t, nfeed, starts, starts);
+                if (nb.status == kTwoPhase) {
+                    r.neighbor = nb;
+                    r.has_neighbor = true;
+                    r.status = kM3Two;
+                    return true;
+                }
+            }
+            return false;
+        }
+        const bool admissible = eq.status == kTConverged && eq.has_point && eq.point.cp_norm <= to.cp_tolerance &&
+                                eq.point.rr_residual <= to.balance_tolerance &&
+                                eq.point.mass_abs <= to.mass_absolute && eq.point.mass_rel <= to.mass_relative;
+        if (!admissible) return false;
+        const ThreeState& cand = eq.point;
+        StabilityOptions fo;
+        fo.tpd_tolerance += cand.cp_norm;
+        std::vector<std::vector<double>> starts{cand.x[0], cand.x[1], cand.x[2]};
+        StabilityResult fin;
+        if (!stability_test(m, wk, p, t, nfeed, fo, starts, cand.common, fin)) {
+            r.status = -1;  // a domain_error out of the reference's review
+            return true;
+        }
+        if (fin.status == kUnstable) {
+            saw_higher = true;
+        } else if (fin.status == kNoInstabilityFound) {
+            r.three = cand;
+            r.has_three = true;
+            r.status = kM3Three;
+            return true;
+        }
+        return false;
+    };
+    std::vector<double> lk1, lk2;
+    if (log_ratio(pair.rr.y, pair.rr.x, nfeed, lk1)) {
+        for (const Trial& wit : review.trials) {
+            if (wit.status != kNegativeTpd || !wit.has_point) continue;
+            if (!log_ratio(wit.point.w, pair.rr.x, nfeed, lk2)) continue;
+            bool sides[2];
+            const int ns = witness_sides(m, wk, p, t, wit.point.w, wit.point.branch, sides);
+            for (int k = 0; k < ns; ++k) {
+                const double beta_v = pair.rr.beta;
+                const double fr[2] = {(1.0 - 0.1) * beta_v, 0.1};
+                const bool upper[3] = {false, true, sides[k]};
+                if (run_attempt(lk1, lk2, fr, upper)) return r;
+                if (limit) break;
+            }
+            if (limit) break;
+        }
+    }
+    r.status = saw_higher ? kM3Higher : (saw_boundary ? kM3Boundary : kM3Indeterminate);
+    return r;
 }
 
 // ---------------------------------------------------------------------------
@@ -1824,6 +2323,109 @@ int oracle_flash_batch(int n, const double* tc, const double* pc, const double* 
         run(0, ncell);
         return 0;
     }
+    std::vector<std::thread> pool;
+    const int64_t chunk = (ncell + threads - 1) / threads;
+    for (int k = 0; k < threads; ++k) {
+        const int64_t lo = k * chunk, hi = std::min<int64_t>(ncell, lo + chunk);
+        if (lo < hi) pool.emplace_back(run, lo, hi);
+    }
+    for (auto& th : pool) th.join();
+    return 0;
+}
+
+// Max-3-phase orchestration per cell (the reference's PR76 backend default:
+// solve_pr76_pt_max3 with no start hints).  Same layout and codes as the
+// harness's ref_max3_batch: max3_status 0 single, 1 two, 2 three, 3 boundary
+// unresolved, 4 higher phase count or wrong candidate, 5 indeterminate, -1
+// invalid; published 0 single, 1 two, 2 phase set unstable, 3 indeterminate,
+// 4 three, -1 invalid (pt_phase_set.hpp:91-150).
+struct Max3Outputs {
+    int32_t* max3_status;
+    int32_t* published;
+    double* beta3;   // [3]
+    double* x3;      // [3 * n], phase-major
+    double* lnphi3;  // [3 * n]
+    double* z3;      // [3]
+    double* beta;    // published two-phase pair
+    double* x;       // [n]
+    double* y;       // [n]
+    int32_t* attempts;
+};
+
+int oracle_max3_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                      int64_t ncell, const double* p, const double* t, const double* z, int threads,
+                      const Max3Outputs* o) {
+    if (n < 1 || n > 256 || ncell < 0 || !tc || !pc || !omega || !kij || !p || !t || !z || !o) return -1;
+    const oracle::Model m = oracle::make_model(n, tc, pc, omega, kij);
+    auto run = [&](int64_t lo, int64_t hi) {
+        using namespace oracle;
+        Work wk;
+        wk.init(n);
+        std::vector<double> feed(n);
+        for (int64_t c = lo; c < hi; ++c) {
+            auto put = [&](double* arr, int k, double v) {
+                if (arr) arr[k * ncell + c] = v;
+            };
+            for (int k = 0; k < 3; ++k) {
+                put(o->beta3, k, kNaN);
+                put(o->z3, k, kNaN);
+                for (int i = 0; i < n; ++i) {
+                    put(o->x3, k * n + i, kNaN);
+                    put(o->lnphi3, k * n + i, kNaN);
+                }
+            }
+            put(o->beta, 0, kNaN);
+            for (int i = 0; i < n; ++i) {
+                put(o->x, i, kNaN);
+                put(o->y, i, kNaN);
+            }
+            for (int i = 0; i < n; ++i) feed[i] = z[i * ncell + c];
+            Max3Result r;
+            if (!std::isfinite(t[c]) || !(t[c] > 0) || !make_temp_cache(m, t[c], wk.tc))
+                r.status = -1;
+            else
+                r = solve_max3(m, wk, p[c], t[c], feed);
+            if (o->max3_status) o->max3_status[c] = r.status;
+            if (o->attempts) o->attempts[c] = r.attempts;
+            int pub = -1;
+            const SplitState* pair = nullptr;
+            switch (r.status) {
+            case kM3Single: pub = 0; break;
+            case kM3Two:
+                pub = 1;
+                pair = r.has_neighbor ? &r.neighbor.candidate : &r.base.candidate;
+                break;
+            case kM3Three: pub = 4; break;
+            case kM3Higher:
+                pub = 2;
+                pair = &r.base.candidate;
+                break;
+            case kM3Boundary:
+            case kM3Indeterminate: pub = 3; break;
+            default: pub = -1; break;
+            }
+            if (o->published) o->published[c] = pub;
+            if (pair) {
+                put(o->beta, 0, pair->rr.beta);
+                for (int i = 0; i < n; ++i) {
+                    put(o->x, i, pair->rr.x[i]);
+                    put(o->y, i, pair->rr.y[i]);
+                }
+            }
+            if (r.has_three) {
+                for (int k = 0; k < 3; ++k) {
+                    put(o->beta3, k, r.three.fraction[k]);
+                    put(o->z3, k, r.three.zf[k]);
+                    for (int i = 0; i < n; ++i) {
+                        put(o->x3, k * n + i, r.three.x[k][i]);
+                        put(o->lnphi3, k * n + i, r.three.ln_phi[k][i]);
+                    }
+                }
+            }
+        }
+    };
+    if (threads < 1) threads = 1;
+    if (threads > ncell) threads = static_cast<int>(std::max<int64_t>(ncell, 1));
     std::vector<std::thread> pool;
     const int64_t chunk = (ncell + threads - 1) / threads;
     for (int k = 0; k < threads; ++k) {

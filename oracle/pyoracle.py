@@ -180,3 +180,43 @@ def sensitivity_at(mix, p, t, z, ok, x, y, ln_k, beta, threads: int = 8, manifol
        ctypes.c_void_p(b.ctypes.data), ctypes.c_int(threads), ctypes.byref(s))
     _lib(ORACLE_SO).oracle_set_manifold_identity(ctypes.c_int(0))
     return out
+
+MAX3_FIELDS = [("max3_status", np.int32, 1), ("published", np.int32, 1), ("beta3", np.float64, 3),
+               ("x3", np.float64, -3), ("lnphi3", np.float64, -3), ("z3", np.float64, 3),
+               ("beta", np.float64, 1), ("x", np.float64, -1), ("y", np.float64, -1), ("attempts", np.int32, 1)]
+
+
+class _Max3(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_void_p) for f, _, _ in MAX3_FIELDS]
+
+
+def _max3(fn_name: str, so: str, mix, p, t, z, threads: int):
+    tc, pc, omega, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
+    z = np.ascontiguousarray(z, dtype=np.float64)
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    n, ncell = z.shape
+    out = {f: np.empty(((-r) * n if r < 0 else r, ncell), d) for f, d, r in MAX3_FIELDS}
+    o = _Max3(**{f: v.ctypes.data for f, v in out.items()})
+    fn = getattr(_lib(so), fn_name)
+    fn.restype = ctypes.c_int
+    fn(ctypes.c_int(n), *[ctypes.c_void_p(a.ctypes.data) for a in (tc, pc, omega, kij)], ctypes.c_int64(ncell),
+       *[ctypes.c_void_p(a.ctypes.data) for a in (p, t, z)], ctypes.c_int(threads), ctypes.byref(o))
+    return {f: (v[0] if v.shape[0] == 1 else v) for f, v in out.items()}
+
+
+def max3(mix, p, t, z, threads: int = 8):
+    """Max-3-phase orchestration (solve_pr76_pt_max3 restated, backend
+    defaults).  Statuses: max3_status 0 single, 1 two, 2 three, 3 boundary
+    unresolved, 4 higher phase count, 5 indeterminate, -1 invalid; published
+    0 single, 1 two, 2 phase set unstable, 3 indeterminate, 4 three."""
+    build()
+    return _max3("oracle_max3_batch", ORACLE_SO, mix, p, t, z, threads)
+
+
+def reference_max3(mix, p, t, z, threads: int = 8):
+    """The reference's solve_pr76_pt_max3 through oracle/_ref (only where the
+    reference sources were present to build it)."""
+    if not reference_available():
+        raise FileNotFoundError(REF_SO)
+    return _max3("ref_max3_batch", REF_SO, mix, p, t, z, threads)

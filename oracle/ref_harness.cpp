@@ -12,8 +12,10 @@
 //   mpmc::physics::build_pr76_pt_vle_closure       modules/physics/include/mpmc/physics/pr76_thermodynamic_closure.hpp:148
 //   mpmc::thermodynamics::Pr76PhaseAdWorkspace     modules/thermodynamics/include/mpmc/thermodynamics/pr76_phase_ad.hpp:43
 //   mpmc::flash::Pr76PtFlashBackend::solve         modules/flash/include/mpmc/flash/pr76_pt_flash_backend.hpp:190
+//   mpmc::flash::solve_pr76_pt_max3                modules/flash/include/mpmc/flash/pr76_three_phase.hpp:328
 
 #include <mpmc/flash/pr76_pt_flash_backend.hpp>
+#include <mpmc/flash/pr76_three_phase.hpp>
 #include <mpmc/flash/pr76_sensitivity.hpp>
 #include <mpmc/physics/pr76_thermodynamic_closure.hpp>
 #include <mpmc/thermodynamics/pr76_phase_ad.hpp>
@@ -258,6 +260,112 @@ int ref_backend_batch(int n, const double* tc, const double* pc, const double* o
             } catch (const std::exception&) {
                 status[c] = -1;
                 phase_count[c] = 0;
+            }
+        }
+    };
+    if (threads < 1) threads = 1;
+    std::vector<std::thread> pool;
+    const int64_t chunk = (ncell + threads - 1) / threads;
+    for (int k = 0; k < threads; ++k) {
+        const int64_t lo = k * chunk, hi = std::min<int64_t>(ncell, lo + chunk);
+        if (lo < hi) pool.emplace_back(run, lo, hi);
+    }
+    for (auto& th : pool) th.join();
+    return 0;
+}
+
+// Outputs of the max-3-phase orchestration per cell (layouts a[k * ncell + c];
+// phase-major for the three-phase fields: phase q, component i at
+// (q * n + i) * ncell + c).
+struct Max3Outputs {
+    int32_t* max3_status;  // Pr76PtMax3Status: 0 single, 1 two, 2 three, 3 boundary unresolved,
+                           // 4 higher phase count or wrong candidate, 5 indeterminate
+    int32_t* published;    // 0 single, 1 two, 2 phase set unstable, 3 indeterminate, 4 three, -1 invalid
+    double* beta3;         // [3] phase fractions of the accepted three-phase set
+    double* x3;            // [3 * n] compositions
+    double* lnphi3;        // [3 * n]
+    double* z3;            // [3]
+    double* beta;          // two-phase pair published for status two / higher (vapor fraction)
+    double* x;             // [n]
+    double* y;             // [n]
+    int32_t* attempts;     // three-phase attempts run
+};
+
+int ref_max3_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                   int64_t ncell, const double* p, const double* t, const double* z, int threads,
+                   const Max3Outputs* o) {
+    std::vector<std::string> order;
+    const th::PrParameterSet params = make_parameters(n, tc, pc, omega, kij, order);
+    const auto model = th::Pr76Phase<double>::from_parameters(params);
+    const double nan = std::numeric_limits<double>::quiet_NaN();
+    auto run = [&](int64_t lo, int64_t hi) {
+        fl::Pr76VleEvaluator evaluator(model);
+        for (int64_t c = lo; c < hi; ++c) {
+            auto put = [&](double* arr, int k, double v) {
+                if (arr) arr[k * ncell + c] = v;
+            };
+            for (int k = 0; k < 3; ++k) {
+                put(o->beta3, k, nan);
+                put(o->z3, k, nan);
+                for (int i = 0; i < n; ++i) {
+                    put(o->x3, k * n + i, nan);
+                    put(o->lnphi3, k * n + i, nan);
+                }
+            }
+            put(o->beta, 0, nan);
+            for (int i = 0; i < n; ++i) {
+                put(o->x, i, nan);
+                put(o->y, i, nan);
+            }
+            std::vector<double> feed(n);
+            for (int i = 0; i < n; ++i) feed[i] = z[i * ncell + c];
+            fl::Pr76PtMax3Result r;
+            try {
+                r = fl::solve_pr76_pt_max3(p[c], t[c], feed, evaluator);
+            } catch (const std::exception&) {
+                if (o->max3_status) o->max3_status[c] = -1;
+                if (o->published) o->published[c] = -1;
+                if (o->attempts) o->attempts[c] = 0;
+                continue;
+            }
+            const int ms = static_cast<int>(r.status);
+            if (o->max3_status) o->max3_status[c] = ms;
+            if (o->attempts) o->attempts[c] = static_cast<int32_t>(r.attempts.size());
+            const fl::PtSplitState* pair = nullptr;
+            int pub = 3;
+            switch (r.status) {
+            case fl::Pr76PtMax3Status::single_phase: pub = 0; break;
+            case fl::Pr76PtMax3Status::two_phase: {
+                const auto* nb = r.two_phase_neighbor();
+                pair = nb ? nb->solution.candidate() : r.base.solution.candidate();
+                pub = 1;
+                break;
+            }
+            case fl::Pr76PtMax3Status::three_phase: pub = 4; break;
+            case fl::Pr76PtMax3Status::higher_phase_count_or_wrong_candidate:
+                pair = r.base.solution.candidate();
+                pub = 2;
+                break;
+            default: pub = 3; break;
+            }
+            if (o->published) o->published[c] = pub;
+            if (pair) {
+                put(o->beta, 0, pair->fractions.vapor_fraction);
+                for (int i = 0; i < n; ++i) {
+                    put(o->x, i, pair->fractions.liquid[i]);
+                    put(o->y, i, pair->fractions.vapor[i]);
+                }
+            }
+            if (const auto* cand = r.three_phase_candidate()) {
+                for (int k = 0; k < 3; ++k) {
+                    const auto& ph = cand->phases[k];
+                    put(o->beta3, k, ph.mole_phase_fraction);
+                    put(o->z3, k, ph.z);
+                    for (int i = 0; i < n; ++i) {
+                        put(o->x3, k * n + i, ph.composition[i]);
+                        put(o->lnphi3, k * n + i, ph.activity.ln_phi[i]);
+                    }
+                }
             }
         }
     };
