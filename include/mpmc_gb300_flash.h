@@ -64,7 +64,19 @@ enum {
     MPMC_FLASH_TWO_PHASE = 1,       /* two_phase_no_instability_found:   accepted, 2 phases */
     MPMC_FLASH_PHASE_SET_UNSTABLE = 2, /* final common-tangent review found a lower-Gibbs trial */
     MPMC_FLASH_INDETERMINATE = 3,   /* finite search did not settle the phase set */
+    MPMC_FLASH_THREE_PHASE = 4,     /* accepted three-phase set (max-3-phase entry points only) */
     MPMC_FLASH_INVALID_REQUEST = -1 /* p, T or feed violate the request contract */
+};
+
+/* Outcome of the max-3-phase orchestration per cell, mirroring
+ * Pr76PtMax3Status (modules/flash/include/mpmc/flash/pr76_three_phase.hpp:128-135). */
+enum {
+    MPMC_MAX3_SINGLE_PHASE = 0,
+    MPMC_MAX3_TWO_PHASE = 1,             /* the two-phase answer, or a fresh two-phase neighbor */
+    MPMC_MAX3_THREE_PHASE = 2,
+    MPMC_MAX3_BOUNDARY_UNRESOLVED = 3,   /* a phase disappeared and no neighbor closed */
+    MPMC_MAX3_HIGHER_PHASE_COUNT = 4,    /* a three-phase candidate failed its final review */
+    MPMC_MAX3_INDETERMINATE = 5
 };
 
 /* Algorithm forms (same fixed points, different execution). */
@@ -139,6 +151,17 @@ typedef struct mpmc_flash_outputs {
     double* jac_vapor;        /* [(n+1)*(n+2)*n_cells] */
 } mpmc_flash_outputs;
 
+/* Three-phase outputs of the max-3-phase entry points; layout a[k * n_cells + c],
+ * phase q and component i at row q * n + i.  NaN where the cell has no
+ * accepted three-phase set. */
+typedef struct mpmc_three_phase_outputs {
+    int32_t* max3_status;    /* [n_cells] MPMC_MAX3_*, -1 for an invalid request */
+    double* phase_fraction;  /* [3*n_cells] */
+    double* composition;     /* [3*n*n_cells] */
+    double* ln_phi;          /* [3*n*n_cells] */
+    double* z_factor;        /* [3*n_cells] */
+} mpmc_three_phase_outputs;
+
 typedef struct mpmc_gpu_flash mpmc_gpu_flash;
 
 /* Create a handle for one mixture on options->device.  Replaces constructing
@@ -200,6 +223,34 @@ int mpmc_gpu_flash_solve_warm(mpmc_gpu_flash* handle, int64_t n_cells, const dou
 int mpmc_gpu_flash_solve_device_warm(mpmc_gpu_flash* handle, int64_t n_cells, const double* p, const double* t,
                                      const double* z, const double* ln_k_warm, const mpmc_flash_outputs* out,
                                      void* stream);
+
+/* mpmc_gpu_flash_solve / _solve_device followed by the reference backend's
+ * max-3-phase orchestration for the cells whose two-phase answer is
+ * MPMC_FLASH_PHASE_SET_UNSTABLE: Pr76PtFlashBackend::solve runs
+ * solve_pr76_pt_max3 (pr76_pt_flash_backend.hpp:190-237,
+ * pr76_three_phase.hpp:328-561).  Each such cell's negative witnesses of the
+ * final review seed three-phase attempts.  An attempt is a generalized
+ * Rachford-Rice balance of three phases and a ln K iteration on both
+ * ratios.  A converged three-phase set goes through its own common-tangent
+ * review.  A phase that disappears triggers a fresh two-phase solve from the
+ * two surviving phases.  The published status follows
+ * pt_phase_set.hpp:91-150:
+ *   three phases accepted     -> MPMC_FLASH_THREE_PHASE, the set in out3;
+ *   fresh two-phase neighbor  -> MPMC_FLASH_TWO_PHASE, its pair in `out`;
+ *   three-phase review failed -> MPMC_FLASH_PHASE_SET_UNSTABLE, the base pair kept;
+ *   otherwise                 -> MPMC_FLASH_INDETERMINATE, no pair.
+ * Cells that are not phase_set_unstable keep their two-phase answer, and
+ * out3->max3_status records every cell's outcome.  out->status and
+ * out->ln_k are required.  The continuation runs in FP64 with the
+ * reference's arithmetic, one cell per thread, for every form.  These calls
+ * do not use CUDA graphs, and the sensitivities of a handle created with
+ * want_sensitivity are taken after the continuation. */
+int mpmc_gpu_flash_solve_max3(mpmc_gpu_flash* handle, int64_t n_cells, const double* p, const double* t,
+                              const double* z, const mpmc_flash_outputs* out,
+                              const mpmc_three_phase_outputs* out3);
+int mpmc_gpu_flash_solve_device_max3(mpmc_gpu_flash* handle, int64_t n_cells, const double* p, const double* t,
+                                     const double* z, const mpmc_flash_outputs* out,
+                                     const mpmc_three_phase_outputs* out3, void* stream);
 
 /* Largest device scratch, in bytes, of mpmc_gpu_flash_solve_device_noalloc:
  * a fixed 48 MiB array in the library's device code. */

@@ -25,7 +25,10 @@ PROBE_LIB = os.path.join(LIBDIR, "libmpmc_gb300_probe.so")
 
 CAPACITIES = (4, 8, 12, 16, 20)
 # translation units compiled once per capacity
-PER_CAPACITY = ("flash_plain.cu", "sensitivity.cu", "flash_batched.cu")
+PER_CAPACITY = ("flash_plain.cu", "sensitivity.cu", "flash_batched.cu", "flash_max3.cu")
+# extra nvcc flags per translation unit: the max-3-phase continuation is a
+# rare, latency-irrelevant path whose large kernel takes ptxas minutes at -O3
+EXTRA_FLAGS = {"flash_max3.cu": ["-Xptxas", "-O1"]}
 # translation units compiled once
 SINGLE = ("capi.cu", "server.cu", "peak_probe.cu")
 
@@ -67,7 +70,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     for src in PER_CAPACITY:
         stem = os.path.splitext(src)[0]
         for nm in CAPACITIES:
-            tasks.append((src, os.path.join(BUILD, f"{stem}_nm{nm}.o"), [f"-DMPMC_NM={nm}"]))
+            tasks.append((src, os.path.join(BUILD, f"{stem}_nm{nm}.o"), [f"-DMPMC_NM={nm}"] + EXTRA_FLAGS.get(src, [])))
     for src in SINGLE:
         tasks.append((src, os.path.join(BUILD, os.path.splitext(src)[0] + ".o"), []))
     jobs = jobs or min(len(tasks), max(1, os.cpu_count() or 1))

@@ -83,6 +83,7 @@ struct mpmc_gpu_flash {
     int n_events = 0;   // events recorded by the last solve (stages + 1)
     bool timed_warm = false;  // the last timed solve ran a warm and a cold pass
     DevBuf in_warm;     // host entry: staged ln K warm starts
+    DevBuf outs3[5];    // host entry: staged three-phase outputs
     int32_t shape[8] = {};  // explicit launch shape (mpmc_gpu_flash_set_launch_shape), 0 = default
     bool use_graphs = false;
     std::vector<GraphEntry> graphs;
@@ -240,7 +241,8 @@ int prepare_device(mpmc_gpu_flash* h, int64_t ncell, pr76::DeviceOutputs& d) {
 
 // The launches of one solve on `stream` (no allocation, no synchronisation).
 cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
-                           const double* warm, const pr76::DeviceOutputs& d, cudaStream_t stream, bool timing) {
+                           const double* warm, const pr76::DeviceOutputs& d, cudaStream_t stream, bool timing,
+                           const pr76::Max3Outputs* max3 = nullptr) {
     cudaError_t e;
     int next_event = 0;
     auto record = [&]() {
@@ -260,6 +262,10 @@ cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, co
         next_event = timing ? pr76::kBatchedStages + 1 : 0;
     }
     if (e != cudaSuccess) return e;
+    if (max3) {  // before the sensitivities: a fresh two-phase neighbor is differentiated too
+        e = pr76::launch_max3(h->n, h->d_mixture, ncell, p, t, z, d, *max3, stream);
+        if (e != cudaSuccess) return e;
+    }
     if (h->want_sensitivity) {
         e = pr76::launch_sensitivity(h->n, h->d_mixture, ncell, p, t, z, d, stream);
         if (e != cudaSuccess) return e;
@@ -279,7 +285,8 @@ bool same_key(const GraphEntry& g, int64_t ncell, const double* p, const double*
 }
 
 int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
-               const double* warm, const pr76::DeviceOutputs& d_in, cudaStream_t stream) {
+               const double* warm, const pr76::DeviceOutputs& d_in, cudaStream_t stream,
+               const pr76::Max3Outputs* max3 = nullptr) {
     if (warm && h->form == MPMC_FORM_PLAIN_FP64)
         return fail(MPMC_ERR_UNSUPPORTED,
                     "ln K warm starts need a work-queue form (MPMC_FORM_MIXED or MPMC_FORM_BATCHED); the plain "
@@ -295,8 +302,8 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
         for (auto& ev : h->redo_events)
             if ((e = cudaEventCreate(&ev)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
     }
-    if (!h->use_graphs || h->stage_timing) {
-        e = enqueue_device(h, ncell, p, t, z, warm, d, stream, h->stage_timing);
+    if (!h->use_graphs || h->stage_timing || max3) {
+        e = enqueue_device(h, ncell, p, t, z, warm, d, stream, h->stage_timing, max3);
         return e == cudaSuccess ? MPMC_OK : cuda_fail(e, "flash kernel launch");
     }
     // CUDA graph of the launch sequence, one per (cells, buffers): captured on
@@ -424,6 +431,18 @@ cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const
     }
 }
 
+cudaError_t launch_max3(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
+                        const double* z, const DeviceOutputs& out, const Max3Outputs& out3, cudaStream_t stream) {
+    switch (capacity_for(n)) {
+    case 4: return launch_max3_nm4(d_mix, ncell, p, t, z, out, out3, stream);
+    case 8: return launch_max3_nm8(d_mix, ncell, p, t, z, out, out3, stream);
+    case 12: return launch_max3_nm12(d_mix, ncell, p, t, z, out, out3, stream);
+    case 16: return launch_max3_nm16(d_mix, ncell, p, t, z, out, out3, stream);
+    case 20: return launch_max3_nm20(d_mix, ncell, p, t, z, out, out3, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
 cudaError_t launch_plain(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
                          const double* z, const DeviceOutputs& out, cudaStream_t stream) {
     switch (capacity_for(n)) {
@@ -436,6 +455,12 @@ cudaError_t launch_plain(int n, const Mixture* d_mix, int64_t ncell, const doubl
     }
 }
 }  // namespace pr76
+
+namespace {
+int solve_host(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
+               const double* ln_k_warm, const mpmc_flash_outputs* out, const mpmc_three_phase_outputs* out3,
+               bool max3);
+}  // namespace
 
 extern "C" {
 
@@ -525,6 +550,7 @@ int mpmc_gpu_flash_destroy(mpmc_gpu_flash* h) {
     h->in_t.release();
     h->in_z.release();
     h->in_warm.release();
+    for (auto& b : h->outs3) b.release();
     for (auto& b : h->outs) b.release();
     for (auto& b : h->sens_inputs) b.release();
     h->workspace.release();
@@ -542,6 +568,22 @@ int mpmc_gpu_flash_destroy(mpmc_gpu_flash* h) {
 int mpmc_gpu_flash_solve_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t,
                                 const double* z, const mpmc_flash_outputs* out, void* stream) {
     return mpmc_gpu_flash_solve_device_warm(h, ncell, p, t, z, nullptr, out, stream);
+}
+
+int mpmc_gpu_flash_solve_device_max3(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t,
+                                     const double* z, const mpmc_flash_outputs* out,
+                                     const mpmc_three_phase_outputs* out3, void* stream) {
+    if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
+    if (ncell < 0) return fail(MPMC_ERR_INVALID_ARGUMENT, "negative cell count");
+    if (ncell == 0) return MPMC_OK;
+    if (!p || !t || !z) return fail(MPMC_ERR_INVALID_ARGUMENT, "p, t and z must not be null");
+    if (!out || !out->status || !out->ln_k)
+        return fail(MPMC_ERR_INVALID_ARGUMENT, "max-3-phase solve: the status and ln_k outputs are required");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    pr76::Max3Outputs m3{};
+    if (out3) m3 = {out3->max3_status, out3->phase_fraction, out3->composition, out3->ln_phi, out3->z_factor};
+    return run_device(h, ncell, p, t, z, nullptr, to_device_outputs(out), static_cast<cudaStream_t>(stream), &m3);
 }
 
 int mpmc_gpu_flash_solve_device_warm(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t,
@@ -612,9 +654,28 @@ int mpmc_gpu_flash_solve(mpmc_gpu_flash* h, int64_t ncell, const double* p, cons
     return mpmc_gpu_flash_solve_warm(h, ncell, p, t, z, nullptr, out);
 }
 
+int mpmc_gpu_flash_solve_max3(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
+                              const mpmc_flash_outputs* out, const mpmc_three_phase_outputs* out3) {
+    return solve_host(h, ncell, p, t, z, nullptr, out, out3, true);
+}
+
 int mpmc_gpu_flash_solve_warm(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
                               const double* ln_k_warm, const mpmc_flash_outputs* out) {
+    return solve_host(h, ncell, p, t, z, ln_k_warm, out, nullptr, false);
+}
+
+}  // extern "C"
+
+namespace {
+
+// The host-buffer entry: stage inputs, solve on the handle's stream, copy the
+// requested outputs back, synchronise.
+int solve_host(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
+               const double* ln_k_warm, const mpmc_flash_outputs* out, const mpmc_three_phase_outputs* out3,
+               bool max3) {
     if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
+    if (max3 && (!out || !out->status || !out->ln_k))
+        return fail(MPMC_ERR_INVALID_ARGUMENT, "max-3-phase solve: the status and ln_k outputs are required");
     if (ncell < 0) return fail(MPMC_ERR_INVALID_ARGUMENT, "negative cell count");
     if (ncell == 0) return MPMC_OK;
     if (!p || !t || !z) return fail(MPMC_ERR_INVALID_ARGUMENT, "p, t and z must not be null");
@@ -649,9 +710,32 @@ int mpmc_gpu_flash_solve_warm(mpmc_gpu_flash* h, int64_t ncell, const double* p,
             return cuda_fail(e, "warm-start copy");
         d_warm = static_cast<const double*>(h->in_warm.ptr);
     }
+    // three-phase outputs: staged like the others
+    void* host3[5] = {};
+    size_t bytes3[5] = {sizeof(int32_t), 3 * sizeof(double), 3 * n * sizeof(double), 3 * n * sizeof(double),
+                        3 * sizeof(double)};
+    pr76::Max3Outputs m3{};
+    if (max3) {
+        if (out3) {
+            host3[0] = out3->max3_status;
+            host3[1] = out3->phase_fraction;
+            host3[2] = out3->composition;
+            host3[3] = out3->ln_phi;
+            host3[4] = out3->z_factor;
+        }
+        void* dev3[5] = {};
+        for (int k = 0; k < 5; ++k) {
+            if (!host3[k]) continue;
+            if ((e = h->outs3[k].ensure(bytes3[k] * nc)) != cudaSuccess)
+                return cuda_fail(e, "three-phase output staging allocation");
+            dev3[k] = h->outs3[k].ptr;
+        }
+        m3 = {static_cast<int32_t*>(dev3[0]), static_cast<double*>(dev3[1]), static_cast<double*>(dev3[2]),
+              static_cast<double*>(dev3[3]), static_cast<double*>(dev3[4])};
+    }
     const int rc = run_device(h, ncell, static_cast<const double*>(h->in_p.ptr),
                               static_cast<const double*>(h->in_t.ptr), static_cast<const double*>(h->in_z.ptr),
-                              d_warm, to_device_outputs(&dev_out), s);
+                              d_warm, to_device_outputs(&dev_out), s, max3 ? &m3 : nullptr);
     if (rc != MPMC_OK) return rc;
     for (int k = 0; k < kOutputFields; ++k) {
         void* hp = *field_ptr(&host_out, k);
@@ -660,8 +744,14 @@ int mpmc_gpu_flash_solve_warm(mpmc_gpu_flash* h, int64_t ncell, const double* p,
             cudaSuccess)
             return cuda_fail(e, "output copy");
     }
+    for (int k = 0; k < 5; ++k) {
+        if (!host3[k]) continue;
+        if ((e = cudaMemcpyAsync(host3[k], h->outs3[k].ptr, bytes3[k] * nc, cudaMemcpyDeviceToHost, s)) !=
+            cudaSuccess)
+            return cuda_fail(e, "three-phase output copy");
+    }
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "flash execution");
     return MPMC_OK;
 }
 
-}  // extern "C"
+}  // namespace

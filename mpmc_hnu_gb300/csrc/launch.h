@@ -76,6 +76,24 @@ cudaError_t launch_batched(int n, const Mixture* d_mix, int64_t ncell, const dou
                            const double* z, const DeviceOutputs& out, void* scratch, size_t scratch_bytes,
                            const BatchedShape& shape, cudaStream_t stream);
 
+// Three-phase outputs of the max-3-phase continuation (layout a[k * ncell + c];
+// phase-major compositions: phase q, component i at row q * n + i).
+struct Max3Outputs {
+    int32_t* max3_status;  // Pr76PtMax3Status (0 single, 1 two, 2 three, 3 boundary unresolved,
+                           // 4 higher phase count, 5 indeterminate), -1 invalid
+    double* fraction;      // [3] phase fractions
+    double* x;             // [3 * n] compositions
+    double* lnphi;         // [3 * n]
+    double* z;             // [3] compressibility factors
+};
+
+// Max-3-phase continuation (flash_plain.cu) of the cells whose flash status in
+// `out` is phase_set_unstable; every cell gets its max3_status.  Reads and
+// rewrites the two-phase fields of `out` (status, pair) as the reference's
+// publication does.
+cudaError_t launch_max3(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
+                        const double* z, const DeviceOutputs& out, const Max3Outputs& out3, cudaStream_t stream);
+
 // Smallest compiled component capacity >= n (0 if unsupported).
 int capacity_for(int n);
 
@@ -93,6 +111,9 @@ cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const
                                     const double* z, const DeviceOutputs& out, cudaStream_t stream); \
     cudaError_t launch_sensitivity_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t, \
                                           const double* z, const DeviceOutputs& out, cudaStream_t stream); \
+    cudaError_t launch_max3_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t,      \
+                                   const double* z, const DeviceOutputs& out, const Max3Outputs& out3,           \
+                                   cudaStream_t stream);                                                          \
     size_t batched_workspace_bytes_nm##NM(int n, int64_t ncell, bool fp64_items);                             \
     cudaError_t launch_batched_nm##NM(const Mixture* d_mix, int n, int64_t ncell, const double* p,            \
                                       const double* t, const double* z, const DeviceOutputs& out, void* scratch, \

@@ -42,6 +42,8 @@ enum Issue : int {
 // Per-cell phase-set status (include/mpmc_gb300_flash.h).
 enum FlashStatus : int { kSinglePhase = 0, kTwoPhase = 1, kPhaseSetUnstable = 2,
                          kIndeterminate = 3, kInvalid = -1 };
+// accepted three-phase set (max-3-phase continuation only)
+constexpr int MPMC_THREE_PHASE_STATUS = 4;
 
 // Counter rows (include/mpmc_gb300_flash.h MPMC_COUNTER_*).
 enum Counter : int { cInitEvals = 0, cSplitEvals, cFinalEvals, cSplitIters, cRrIters,

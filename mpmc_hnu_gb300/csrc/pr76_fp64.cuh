@@ -27,6 +27,13 @@
 
 #include "pr76_common.cuh"
 
+// Call discipline of the large routines below: inlined by default; a
+// translation unit may define MPMC_FP64_CALL as __noinline__ (the rare
+// max-3-phase path) to keep its one kernel small and its build short.
+#ifndef MPMC_FP64_CALL
+#define MPMC_FP64_CALL
+#endif
+
 namespace pr76 {
 namespace fp64 {
 
@@ -302,8 +309,8 @@ __device__ bool ln_phi_of_root(const Mixture& m, const Cell<NM>& c, double amix,
 // Stability provider (minimum-Gibbs admissible root), pr76_stability.hpp:36-119.
 // Writes ln phi of the selected branch into `out`.
 template <int NM>
-__device__ int stability_provider(const Mixture& m, Cell<NM>& c, const double* x, double* out, bool& smooth,
-                                  double* z_out, int counter_row) {
+__device__ MPMC_FP64_CALL int stability_provider(const Mixture& m, Cell<NM>& c, const double* x, double* out, bool& smooth,
+                                  double* z_out, int counter_row, int* branch_out = nullptr) {
     ++c.counters[counter_row];
     double amix, bmix, A, B;
     if (!mix(m, c, x, amix, bmix)) return kRootRange;
@@ -340,13 +347,14 @@ __device__ int stability_provider(const Mixture& m, Cell<NM>& c, const double* x
     if (!rs.r[cand[best]].derivative_valid) return kIllConditionedRoot;
     for (int i = 0; i < n; ++i) out[i] = c.lnphi[best][i];
     if (z_out) *z_out = rs.r[cand[best]].z;
+    if (branch_out) *branch_out = cand[best];
     return kOk;
 }
 
 // Role provider (liquid = smallest, vapor = largest admissible root),
 // pr76_split.hpp:38-84 with split_check_phase (pt_split.hpp:197-203).
 template <int NM>
-__device__ int role_provider(const Mixture& m, Cell<NM>& c, const double* x, bool vapor, double* ln_phi,
+__device__ MPMC_FP64_CALL int role_provider(const Mixture& m, Cell<NM>& c, const double* x, bool vapor, double* ln_phi,
                              double& z_out, int& branch) {
     ++c.counters[cSplitEvals];
     double amix, bmix, A, B;
@@ -377,6 +385,7 @@ struct TpdPoint {
     double w[NM], res[NM], lw[NM];
     double value, guard, stat;
     bool smooth;
+    int branch;  // root branch of the stability phase at w
 };
 
 __device__ __forceinline__ bool check_composition(const double* x, int n, double& sum) {
@@ -445,7 +454,7 @@ __device__ __forceinline__ bool tpd_negative(const TpdPoint<NM>& p, double tol) 
 // One TPD trial from the composition already in `point.w`, pt_stability.hpp:343-457.
 // `evals` counts provider calls of this stability test against the 100000 budget.
 template <int NM>
-__device__ int run_trial(const Mixture& m, Cell<NM>& c, const double* ref, const StabilityOptions& o,
+__device__ MPMC_FP64_CALL int run_trial(const Mixture& m, Cell<NM>& c, const double* ref, const StabilityOptions& o,
                          TpdPoint<NM>& point, TpdPoint<NM>& next, double* direction, double* lnphi_scratch,
                          int& evals) {
     const int n = c.n;
@@ -456,7 +465,7 @@ __device__ int run_trial(const Mixture& m, Cell<NM>& c, const double* ref, const
     {
         ++evals;
         bool smooth;
-        int is = stability_provider(m, c, point.w, lnphi_scratch, smooth, nullptr, o.eval_row);
+        int is = stability_provider(m, c, point.w, lnphi_scratch, smooth, nullptr, o.eval_row, &point.branch);
         if (is == kOk) is = tpd(c, lnphi_scratch, ref, point);
         if (is == kDomain) return -1;
         if (is != kOk) return kPropertyFailure;
@@ -505,7 +514,7 @@ __device__ int run_trial(const Mixture& m, Cell<NM>& c, const double* ref, const
             }
             ++evals;
             bool smooth;
-            int is = stability_provider(m, c, next.w, lnphi_scratch, smooth, nullptr, o.eval_row);
+            int is = stability_provider(m, c, next.w, lnphi_scratch, smooth, nullptr, o.eval_row, &next.branch);
             if (is == kOk) is = tpd(c, lnphi_scratch, ref, next);
             if (is == kDomain) return -1;
             if (is != kOk) continue;
@@ -530,6 +539,7 @@ __device__ int run_trial(const Mixture& m, Cell<NM>& c, const double* ref, const
                 point.guard = next.guard;
                 point.stat = next.stat;
                 point.smooth = next.smooth;
+                point.branch = next.branch;
                 accepted = true;
                 break;
             }
@@ -687,7 +697,7 @@ enum AttemptStatus : int { kConverged = 0, kNoInteriorRr, kRrFailure, kIndisting
 // Split evaluation, pt_split.hpp:300-341.  Returns kConverged (= usable state)
 // or the failure class.
 template <int NM>
-__device__ int split_evaluate(const Mixture& m, Cell<NM>& c, const double* lk, SplitState<NM>& s, int& evals,
+__device__ MPMC_FP64_CALL int split_evaluate(const Mixture& m, Cell<NM>& c, const double* lk, SplitState<NM>& s, int& evals,
                               int budget, double* e, double* num, bool newton_rr = false, double beta0 = 0.5) {
     const int n = c.n;
     const int rr = solve_rr(c, lk, s, e, num, newton_rr || c.newton, beta0);
@@ -752,7 +762,7 @@ __device__ __forceinline__ void copy_state(SplitState<NM>& d, const SplitState<N
 
 // iterate_pt_split from ln K in `lk0`; the last accepted state ends in `point`.
 template <int NM>
-__device__ int iterate_split(const Mixture& m, Cell<NM>& c, const double* lk0, SplitState<NM>& point,
+__device__ MPMC_FP64_CALL int iterate_split(const Mixture& m, Cell<NM>& c, const double* lk0, SplitState<NM>& point,
                              SplitState<NM>& next, double* next_lk, int& evals, int budget, double* e, double* num) {
     const int n = c.n;
     int st = split_evaluate(m, c, lk0, point, evals, budget, e, num);
@@ -867,11 +877,10 @@ struct Scratch {
 // 1 = uniform over active components, 2.. = 0.1 z + 0.9 e_i for the (k-2)-th
 // active component; then extra starts.  Normalised by its compensated sum.
 template <int NM>
-__device__ void make_start(const Cell<NM>& c, int k, int active, const double* extra0, const double* extra1,
-                           int n_auto, double* w) {
+__device__ void make_start(const Cell<NM>& c, int k, int active, const double* const* extra, int n_auto, double* w) {
     const int n = c.n;
     if (k >= n_auto) {
-        const double* src = (k - n_auto == 0) ? extra0 : extra1;
+        const double* src = extra[k - n_auto];
         for (int i = 0; i < n; ++i) w[i] = src[i];
     } else if (k == 0) {
         for (int i = 0; i < n; ++i) w[i] = c.z[i];
@@ -895,6 +904,24 @@ __device__ void make_start(const Cell<NM>& c, int k, int active, const double* e
     for (int i = 0; i < n; ++i) w[i] /= sum;
 }
 
+template <int NM>
+__device__ void make_start(const Cell<NM>& c, int k, int active, const double* extra0, const double* extra1,
+                           int n_auto, double* w) {
+    const double* extra[2] = {extra0, extra1};
+    make_start(c, k, active, extra, n_auto, w);
+}
+
+// An extra start of a stability test must be a composition with exactly the
+// feed's support (pt_stability.hpp:263-272, a domain_error otherwise).
+template <int NM>
+__device__ bool start_matches_feed(const Cell<NM>& c, const double* s) {
+    double ssum;
+    if (!check_composition(s, c.n, ssum)) return false;
+    for (int i = 0; i < c.n; ++i)
+        if ((c.z[i] == 0.0) != (s[i] == 0.0)) return false;
+    return true;
+}
+
 // Normalise the feed the way test_pt_stability_impl does (:242, :278).
 template <int NM>
 __device__ bool normalise_feed(Cell<NM>& c, const double* feed) {
@@ -907,9 +934,13 @@ __device__ bool normalise_feed(Cell<NM>& c, const double* feed) {
     return true;
 }
 
+// `init_extra` (n_init of them) join the automatic feed-test starts and
+// `final_extra` (n_final, at most 2) precede the pair's x and y in the review,
+// as solve_pt_vle's initial_starts / final_starts (pt_split.hpp:415-419, 512).
 template <int NM>
-__device__ int solve_cell(const Mixture& m, Cell<NM>& c, const double* feed_in, Scratch<NM>& w,
-                          CellResult<NM>& out) {
+__device__ MPMC_FP64_CALL int solve_cell(const Mixture& m, Cell<NM>& c, const double* feed_in, Scratch<NM>& w,
+                          CellResult<NM>& out, const double* const* init_extra = nullptr, int n_init = 0,
+                          const double* const* final_extra = nullptr, int n_final = 0) {
     const int n = c.n;
     out.has_pair = false;
     if (!isfinite(c.p) || c.p <= 0.0 || !isfinite(c.t) || c.t <= 0.0) return kInvalid;
@@ -932,8 +963,10 @@ __device__ int solve_cell(const Mixture& m, Cell<NM>& c, const double* feed_in, 
     bool negative_found = false, all_stationary = true;
     int attempts = 0, split_evals = 0;
     bool limit = false;
-    for (int k = 0; k < n_auto; ++k) {
-        make_start(c, k, active, nullptr, nullptr, n_auto, w.point.w);
+    for (int k = 0; k < n_init; ++k)
+        if (!start_matches_feed(c, init_extra[k])) return kInvalid;
+    for (int k = 0; k < n_auto + n_init; ++k) {
+        make_start(c, k, active, init_extra, n_auto, w.point.w);
         const int ts = run_trial(m, c, out.ref_lnphi, so, w.point, w.next, w.direction, w.lnphi, evals);
         if (ts < 0) return kInvalid;
         all_stationary = all_stationary && ts == kStationary;
@@ -993,8 +1026,16 @@ __device__ int solve_cell(const Mixture& m, Cell<NM>& c, const double* feed_in, 
     for (int i = 0; i < n; ++i) w.imposed[i] = c.z[i] > 0.0 ? cand.common[i] - c.lz[i] : 0.0;
     bool final_negative = false, final_stationary = true;
     int fevals = 0;
-    for (int k = 0; k < n_auto + 2; ++k) {
-        make_start(c, k, active, cand.x, cand.y, n_auto, w.point.w);
+    const double* review_extra[4];
+    int n_review = 0;
+    for (int k = 0; k < n_final && k < 2; ++k) {
+        if (!start_matches_feed(c, final_extra[k])) return kInvalid;
+        review_extra[n_review++] = final_extra[k];
+    }
+    review_extra[n_review++] = cand.x;
+    review_extra[n_review++] = cand.y;
+    for (int k = 0; k < n_auto + n_review; ++k) {
+        make_start(c, k, active, review_extra, n_auto, w.point.w);
         const int ts = run_trial(m, c, w.imposed, fo, w.point, w.next, w.direction, w.lnphi, fevals);
         if (ts < 0) return kInvalid;
         final_stationary = final_stationary && ts == kStationary;

@@ -62,6 +62,19 @@ class _Outputs(ctypes.Structure):
     _fields_ = [(f, ctypes.c_void_p) for f, _, _ in OUTPUT_FIELDS]
 
 
+# three-phase outputs of the max-3-phase entry points (mpmc_three_phase_outputs)
+THREE_PHASE_FIELDS = [("max3_status", np.int32, lambda n: 1), ("phase_fraction", np.float64, lambda n: 3),
+                      ("composition", np.float64, lambda n: 3 * n), ("ln_phi", np.float64, lambda n: 3 * n),
+                      ("z_factor", np.float64, lambda n: 3)]
+MAX3_STATUS = {0: "single_phase", 1: "two_phase", 2: "three_phase", 3: "phase_boundary_unresolved",
+               4: "higher_phase_count_or_wrong_candidate", 5: "indeterminate", -1: "invalid"}
+FLASH_THREE_PHASE = 4
+
+
+class _ThreePhaseOutputs(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_void_p) for f, _, _ in THREE_PHASE_FIELDS]
+
+
 class _ServerOptions(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("slots", ctypes.c_int32), ("max_batch_cells", ctypes.c_int64),
                 ("memory_budget_bytes", ctypes.c_int64), ("form", ctypes.c_int32), ("flags", ctypes.c_int32)]
@@ -73,7 +86,7 @@ EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu
                     "mpmc_gpu_flash_solve_device_noalloc", "mpmc_flash_server_create", "mpmc_flash_server_add_mixture",
                     "mpmc_flash_server_submit", "mpmc_flash_server_wait", "mpmc_flash_server_stats",
                     "mpmc_flash_server_destroy", "mpmc_gpu_flash_set_launch_shape", "mpmc_gpu_flash_solve_warm",
-                    "mpmc_gpu_flash_solve_device_warm"]
+                    "mpmc_gpu_flash_solve_device_warm", "mpmc_gpu_flash_solve_max3", "mpmc_gpu_flash_solve_device_max3"]
 FLAG_CUDA_GRAPH = 2
 NOALLOC_SCRATCH_BYTES = 48 << 20
 BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun", "fallback_nonsmooth",
@@ -111,6 +124,10 @@ def library() -> ctypes.CDLL:
             [ctypes.POINTER(_Outputs)]
         lib.mpmc_gpu_flash_solve_device_warm.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 4 + \
             [ctypes.POINTER(_Outputs), ctypes.c_void_p]
+        lib.mpmc_gpu_flash_solve_max3.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 3 + \
+            [ctypes.POINTER(_Outputs), ctypes.POINTER(_ThreePhaseOutputs)]
+        lib.mpmc_gpu_flash_solve_device_max3.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 3 + \
+            [ctypes.POINTER(_Outputs), ctypes.POINTER(_ThreePhaseOutputs), ctypes.c_void_p]
         lib.mpmc_gpu_flash_components.argtypes = [ctypes.c_void_p]
         lib.mpmc_gpu_flash_stage_timings.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         lib.mpmc_gpu_flash_batch_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
@@ -202,6 +219,28 @@ class GpuFlash:
         _check(library().mpmc_gpu_flash_solve_warm(self._h, ncell, p.ctypes.data, t.ctypes.data, z.ctypes.data,
                                                    None if warm is None else warm.ctypes.data, ctypes.byref(s)))
         return {f: (v[0] if rows[f] == 1 else v) for f, v in out.items()}
+
+    def solve_max3(self, p, t, z, fields: list[str] | None = None):
+        """`solve` followed by the max-3-phase continuation of phase-set-unstable
+        cells (mpmc_gpu_flash_solve_max3).  Returns (flash outputs, three-phase
+        outputs); `status` is the published one (4 = three phases)."""
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        z = np.ascontiguousarray(z, dtype=np.float64)
+        if z.shape != (self.n, p.shape[0]) or t.shape != p.shape:
+            raise ValueError("expected p[ncell], t[ncell], z[n, ncell]")
+        ncell = p.shape[0]
+        fields = fields or self.fields()
+        rows = output_rows(self.n)
+        dtypes = {f: d for f, d, _ in OUTPUT_FIELDS}
+        out = {f: np.empty((rows[f], ncell), dtypes[f]) for f in fields}
+        out3 = {f: np.empty((r(self.n), ncell), d) for f, d, r in THREE_PHASE_FIELDS}
+        s = _Outputs(**{f: out[f].ctypes.data for f in fields})
+        s3 = _ThreePhaseOutputs(**{f: v.ctypes.data for f, v in out3.items()})
+        _check(library().mpmc_gpu_flash_solve_max3(self._h, ncell, p.ctypes.data, t.ctypes.data, z.ctypes.data,
+                                                   ctypes.byref(s), ctypes.byref(s3)))
+        return ({f: (v[0] if rows[f] == 1 else v) for f, v in out.items()},
+                {f: (v[0] if v.shape[0] == 1 else v) for f, v in out3.items()})
 
     def solve_host_ptrs(self, ncell: int, p_ptr: int, t_ptr: int, z_ptr: int, out_ptrs: dict[str, int]) -> None:
         """Host-buffer entry with caller-owned (e.g. pinned) host pointers."""
