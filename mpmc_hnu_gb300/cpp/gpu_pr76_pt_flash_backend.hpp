@@ -8,11 +8,14 @@
 // of modules/flash/include/mpmc/flash/pt_flash_backend.hpp:187-195 unchanged
 // and adds solve_batch() for the cell loops that own many requests.
 //
-// Contract differences from the PR76 max3 backend, stated in capability():
-// supported phase counts {1, 2} under a distinct backend id (the GPU path is
-// the two-phase contract; a cell whose two-phase set fails the final review is
-// published as phase_set_unstable with its candidate pair, where the max3
-// backend would continue into the three-phase search).
+// Contract: the PR76 max3 backend's (pr76_pt_flash_backend.hpp:190-237) with
+// its default options, under a distinct backend id.  Every request runs the
+// two-phase flash and, where the pair fails its final review, the
+// max-3-phase continuation (mpmc_gpu_flash_solve_max3), so phase counts
+// {1, 2, 3} are published as project_max3_solution does
+// (pt_phase_set.hpp:91-150).  Not carried: caller start hints
+// (three_phase_starts, initial/final starts), the transition report and the
+// phase metadata.
 //
 // Errors follow the reference's classes: an invalid request (feed size,
 // non-finite or non-positive p and T, a feed outside the simplex) throws
@@ -37,8 +40,8 @@
 
 namespace mpmc::flash {
 
-inline constexpr std::string_view gpu_pr76_pt_flash_backend_id = "GB300/PR76/PT/max2/phase-set-backend/v1";
-inline constexpr std::string_view gpu_pr76_pt_result_convention = "GB300/PR76/PT/max2/phase-set/v1";
+inline constexpr std::string_view gpu_pr76_pt_flash_backend_id = "GB300/PR76/PT/max3/phase-set-backend/v1";
+inline constexpr std::string_view gpu_pr76_pt_result_convention = "GB300/PR76/PT/max3/phase-set/v1";
 
 struct GpuPr76Mixture {
     std::vector<std::string> component_ids;
@@ -63,19 +66,22 @@ public:
         check(mpmc_gpu_flash_create(&m, &o, &handle_));
         capability_.backend_id = std::string(gpu_pr76_pt_flash_backend_id);
         capability_.model_profile = "PR76";
-        capability_.algorithm_profile = "GB300/PR76/PT/two-phase/v1";
+        capability_.algorithm_profile = "GB300/PR76/PT/max3/v1";
         capability_.publication_profile = std::string(gpu_pr76_pt_result_convention);
-        capability_.configuration_profile = form == MPMC_FORM_MIXED ? "mixed-precision" : "plain-fp64";
+        capability_.configuration_profile =
+            form == MPMC_FORM_MIXED ? "mixed-precision" : (form == MPMC_FORM_BATCHED ? "fp64-work-queue" : "plain-fp64");
         capability_.dataset_id = mixture.dataset_id;
         capability_.revision = mixture.revision;
         capability_.component_ids = mixture.component_ids;
-        capability_.supported_phase_counts = {1U, 2U};
+        capability_.supported_phase_counts = {1U, 2U, 3U};
         capability_.transition_capability.edges = {
             {1U, 2U, PtPhaseTransitionSupport::fresh_target_resolve, true},
-            {2U, 1U, PtPhaseTransitionSupport::detection_only, true}};
+            {2U, 1U, PtPhaseTransitionSupport::detection_only, true},
+            {2U, 3U, PtPhaseTransitionSupport::fresh_target_resolve, true},
+            {3U, 2U, PtPhaseTransitionSupport::fresh_target_resolve, true}};
         capability_.performs_initial_stability_search = true;
         capability_.performs_final_phase_set_review = true;
-        capability_.performs_boundary_neighbor_resolve = false;
+        capability_.performs_boundary_neighbor_resolve = true;
         capability_.global_stability_proven = false;
     }
 
@@ -115,7 +121,12 @@ public:
         out.z_liquid = zl.data();
         out.z_vapor = zv.data();
         out.counters = counters.data();
-        if (cells > 0) check(mpmc_gpu_flash_solve(handle_, static_cast<int64_t>(cells), p.data(), t.data(), z.data(), &out));
+        std::vector<int32_t> max3(cells);
+        std::vector<double> frac3(3 * cells), comp3(3 * n_ * cells), phi3(3 * n_ * cells), z3(3 * cells);
+        mpmc_three_phase_outputs out3{max3.data(), frac3.data(), comp3.data(), phi3.data(), z3.data()};
+        if (cells > 0)
+            check(mpmc_gpu_flash_solve_max3(handle_, static_cast<int64_t>(cells), p.data(), t.data(), z.data(), &out,
+                                            &out3));
 
         std::vector<PtFlashBackendResult> results(cells);
         for (std::size_t c = 0; c < cells; ++c) {
@@ -131,7 +142,7 @@ public:
             r.capability = capability_;
             r.provider_result_convention = std::string(gpu_pr76_pt_result_convention);
             PtPhaseSetResult& s = r.solution;
-            s.capability.maximum_phase_count = 2U;
+            s.capability.maximum_phase_count = 3U;
             s.pressure_pa = requests[c].pressure_pa;
             s.temperature_k = requests[c].temperature_k;
             s.feed = requests[c].feed;
@@ -161,7 +172,21 @@ public:
                 s.status = status[c] == MPMC_FLASH_TWO_PHASE ? PtPhaseSetStatus::accepted
                                                              : PtPhaseSetStatus::phase_set_unstable;
                 if (status[c] == MPMC_FLASH_PHASE_SET_UNSTABLE)
-                    s.diagnostic = "final phase-set review found a negative tangent-plane distance";
+                    s.diagnostic = "three-phase candidate final review found additional lower-Gibbs evidence";
+                break;
+            }
+            case MPMC_FLASH_THREE_PHASE: {
+                PtCandidatePhaseSet set;
+                for (std::size_t q = 0; q < 3; ++q) {
+                    std::vector<double> comp(n_), lnphi(n_);
+                    for (std::size_t i = 0; i < n_; ++i) {
+                        comp[i] = comp3[(q * n_ + i) * cells + c];
+                        lnphi[i] = phi3[(q * n_ + i) * cells + c];
+                    }
+                    set.phases.push_back(phase(frac3[q * cells + c], std::move(comp), std::move(lnphi), z3[q * cells + c]));
+                }
+                s.candidate_phase_set = std::move(set);
+                s.status = PtPhaseSetStatus::accepted;
                 break;
             }
             default:
