@@ -542,27 +542,23 @@ def main() -> None:
     status = outs["status"][0].cpu().numpy()
     counters = outs["counters"].cpu().numpy().astype(np.float64)
 
-    # end-to-end: pinned host inputs -> C ABI host entry -> every output back on
-    # the host, in page-locked buffers backed by huge pages (flash.pinned_host_array)
-    hp = flash.pinned_host_array(p.shape, np.float64)
-    ht = flash.pinned_host_array(t.shape, np.float64)
-    hz = flash.pinned_host_array(z.shape, np.float64)
-    hp[...] = p
-    ht[...] = t
-    hz[...] = z
-    houts = {f: flash.pinned_host_array((rows[f], ncell), np.int32 if dtypes[f] == np.int32 else np.float64)
-             for f in fields}
-    hptrs = {f: v.ctypes.data for f, v in houts.items()}
+    # end-to-end: pinned host inputs -> C ABI host entry -> every output back on the host
+    hp = torch.tensor(p).pin_memory()
+    ht = torch.tensor(t).pin_memory()
+    hz = torch.tensor(z).pin_memory()
+    houts = {f: torch.empty((rows[f], ncell), dtype=torch.int32 if dtypes[f] == np.int32 else torch.float64)
+             .pin_memory() for f in fields}
+    hptrs = {f: v.data_ptr() for f, v in houts.items()}
     h2d = (2 + n) * 8 * ncell
-    d2h = sum(v.nbytes for v in houts.values())
-    g.solve_host_ptrs(ncell, hp.ctypes.data, ht.ctypes.data, hz.ctypes.data, hptrs)  # warm-up
+    d2h = sum(v.numel() * v.element_size() for v in houts.values())
+    g.solve_host_ptrs(ncell, hp.data_ptr(), ht.data_ptr(), hz.data_ptr(), hptrs)  # warm-up
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        g.solve_host_ptrs(ncell, hp.ctypes.data, ht.ctypes.data, hz.ctypes.data, hptrs)
+        g.solve_host_ptrs(ncell, hp.data_ptr(), ht.data_ptr(), hz.data_ptr(), hptrs)
     e2e_s = max_over_ranks((time.perf_counter() - t0) / args.steps, world, "cuda")
     e2e = {"value": world * ncell / e2e_s, "unit": "flashes/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-           "host_buffers": "page-locked, transparent huge pages (flash.pinned_host_array)"}
+           "host_buffers": "pinned (cudaHostAlloc through torch), one per array"}
 
     # per-stage device times (separate instrumented pass) for the roofline
     gt = flash.GpuFlash(mix, args.form, sensitivity=sens, device=device, stage_timing=True)

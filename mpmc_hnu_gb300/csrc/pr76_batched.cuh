@@ -872,7 +872,7 @@ __global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict_
         const int n = L.cell.n;
         if (L.stage == 1)
             for (int i = 0; i < n; ++i) L.lk[i] = fmaf(L.alpha / L.scale, L.point.res[i], L.point.lnk[i]);
-        const bool ok = fp32::split_evaluate(m, L.cell, L.lk, L.next);
+        const bool ok = fp32::split_evaluate(m, L.cell, L.lk, L.next, L.stage == 1 ? L.point.beta : 0.5f);
         if (L.stage == 0) {
             if (!ok) {
                 L.iter = -1;

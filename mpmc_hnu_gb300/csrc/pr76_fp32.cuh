@@ -397,7 +397,9 @@ struct SplitState {
 };
 
 template <int NM>
-__device__ bool solve_rr(const Cell<NM>& c, const float* lk, SplitState<NM>& s) {
+// Bracketed Newton from `beta0` (the root at the current iterate: a line-search
+// candidate moves ln K by a small step) inside (0, 1), else from 1/2.
+__device__ bool solve_rr(const Cell<NM>& c, const float* lk, SplitState<NM>& s, float beta0 = 0.5f) {
     const int n = c.n;
     float e[NM], num[NM];
     float gl = 0.f, gr = 0.f;  // residual at beta = 0+ and 1-
@@ -418,7 +420,7 @@ __device__ bool solve_rr(const Cell<NM>& c, const float* lk, SplitState<NM>& s) 
         gr += c.z[i] * num[i] / d1;
     }
     if (!(gl > 0.f && gr < 0.f)) return false;
-    float lo = 0.f, hi = 1.f, beta = 0.5f;
+    float lo = 0.f, hi = 1.f, beta = beta0 > 0.f && beta0 < 1.f ? beta0 : 0.5f;
     for (int it = 0; it < 60; ++it) {
         float g = 0.f, dg = 0.f;
         for (int i = 0; i < n; ++i) {
@@ -457,9 +459,10 @@ __device__ bool solve_rr(const Cell<NM>& c, const float* lk, SplitState<NM>& s) 
 }
 
 template <int NM>
-__device__ bool split_evaluate(const Mixture& m, Cell<NM>& c, const float* lk, SplitState<NM>& s) {
+__device__ bool split_evaluate(const Mixture& m, Cell<NM>& c, const float* lk, SplitState<NM>& s,
+                               float beta0 = 0.5f) {
     const int n = c.n;
-    if (!solve_rr(c, lk, s)) return false;
+    if (!solve_rr(c, lk, s, beta0)) return false;
     if (!role_provider(m, c, s.x, false, s.lnphi_l, s.z_l)) return false;
     if (!role_provider(m, c, s.y, true, s.lnphi_v, s.z_v)) return false;
     float gibbs = 0.f, mag = 1.f, fug = 0.f;

@@ -356,44 +356,3 @@ class FlashServer:
             self.close()
         except Exception:
             pass
-
-
-# ---------------------------------------------------------------------------
-# Host buffers for the host-buffer entry points.
-_HOST_BUFFERS = []  # keeps the mappings (and their registrations) alive
-
-
-def pinned_host_array(shape, dtype) -> np.ndarray:
-    """A page-locked host array for mpmc_gpu_flash_solve and friends, backed
-    by transparent huge pages where the kernel allows it.
-
-    The copy engine translates every host page of a transfer; after a long
-    solve those translations are cold, and copying 6 GB of outputs into
-    buffers of 64 KB pages took 3-6x longer than into the same bytes mapped as
-    huge pages (measured on GB300 / Grace).  The array is an anonymous
-    mapping advised MADV_HUGEPAGE, touched, and registered with
-    cudaHostRegister; where either step is unavailable it falls back to
-    torch's pinned allocator.  The mapping lives as long as the process."""
-    import mmap
-
-    import torch
-
-    dtype = np.dtype(dtype)
-    size = int(np.prod(shape)) * dtype.itemsize
-    size = max(size, 1)
-    try:
-        m = mmap.mmap(-1, size, flags=mmap.MAP_PRIVATE | mmap.MAP_ANONYMOUS)
-        addr = ctypes.addressof(ctypes.c_char.from_buffer(m))
-        libc = ctypes.CDLL("libc.so.6", use_errno=True)
-        libc.madvise.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int]
-        libc.madvise(ctypes.c_void_p(addr), ctypes.c_size_t(size), 14)  # MADV_HUGEPAGE
-        arr = np.frombuffer(m, dtype=np.uint8, count=size)
-        arr[::4096] = 0  # fault the pages in before registering them
-        if int(torch.cuda.cudart().cudaHostRegister(addr, size, 0)) != 0:
-            raise OSError("cudaHostRegister failed")
-        _HOST_BUFFERS.append(m)
-        return np.frombuffer(m, dtype=dtype, count=int(np.prod(shape))).reshape(shape)
-    except (OSError, AttributeError, RuntimeError):
-        t = torch.empty(int(np.prod(shape)) * dtype.itemsize, dtype=torch.uint8).pin_memory()
-        _HOST_BUFFERS.append(t)
-        return t.numpy().view(dtype).reshape(shape)
