@@ -1031,7 +1031,7 @@ __device__ bool polish_split(const Mixture& m, fp64::Cell<NM>& c64, PolishScratc
         if (!ad::lu_solve(s.J, s.piv, n, s.d)) return false;
         for (int i = 0; i < n; ++i) s.lnk[i] = s.st.lnk[i] + s.d[i];
         // RR Newton from the current beta: a chord step moves ln K by |F| or less
-        if (fp64::split_evaluate(m, c64, s.lnk, s.nx, evals, 1 << 30, s.e, s.num, true, s.st.beta) !=
+        if (fp64::split_evaluate(m, c64, s.lnk, s.nx, evals, 1 << 30, s.e, s.num, true, s.st.beta, &s.st) !=
             fp64::kConverged)
             return prev <= 1e-11;
         if (!(s.nx.fug < prev)) return prev <= 1e-11;

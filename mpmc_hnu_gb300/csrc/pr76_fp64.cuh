@@ -136,7 +136,11 @@ __device__ __forceinline__ double poly_scale(double y, const Cubic& c) {
     return ((fabs(y) + fabs(c.c2)) * fabs(y) + fabs(c.c1)) * fabs(y) + fabs(c.c0);
 }
 
-__device__ inline void solve_roots(double a, double b, RootSet& rs, int& iterations, bool newton = false) {
+// `zhint` (nhint values): roots Z of a nearby evaluation.  Bracketed Newton
+// on an interval starts from a hint inside it instead of its midpoint; the
+// bracket, the bisection fallback and the stopping test are unchanged.
+__device__ inline void solve_roots(double a, double b, RootSet& rs, int& iterations, bool newton = false,
+                                   const double* zhint = nullptr, int nhint = 0) {
     rs.count = 0;
     rs.status = kRootUnrepresentable;
     rs.scale = 1.0;
@@ -192,6 +196,13 @@ __device__ inline void solve_roots(double a, double b, RootSet& rs, int& iterati
             // and the stopping test is the reference's 4 eps relative width
             const bool increasing = signbit(fl);  // H(left) < 0 <=> increasing on this interval
             y = (left + right) * 0.5;
+            for (int h = 0; h < nhint; ++h) {
+                const double yh = (zhint[h] - b) / rs.scale;
+                if (yh > left && yh < right) {
+                    y = yh;
+                    break;
+                }
+            }
             for (; it < 100; ++it) {
                 const double fy = poly(y, c);
                 if (fy == 0.0) {
@@ -355,13 +366,19 @@ __device__ MPMC_FP64_CALL int stability_provider(const Mixture& m, Cell<NM>& c, 
 // pr76_split.hpp:38-84 with split_check_phase (pt_split.hpp:197-203).
 template <int NM>
 __device__ MPMC_FP64_CALL int role_provider(const Mixture& m, Cell<NM>& c, const double* x, bool vapor, double* ln_phi,
-                             double& z_out, int& branch) {
+                             double& z_out, int& branch, double* roots = nullptr, int* nroots = nullptr) {
     ++c.counters[cSplitEvals];
     double amix, bmix, A, B;
     if (!mix(m, c, x, amix, bmix)) return kRootRange;
     if (!coefficients(c.p, c.t, amix, bmix, A, B)) return kRootRange;
     RootSet rs;
-    solve_roots(A, B, rs, c.counters[cRootIters], c.newton);
+    // roots (nroots of them) of this role's previous evaluation are the Newton starts;
+    // on return they hold this evaluation's roots
+    solve_roots(A, B, rs, c.counters[cRootIters], c.newton, roots, nroots ? *nroots : 0);
+    if (roots && nroots) {
+        *nroots = rs.status == kRootSuccess ? rs.count : 0;
+        for (int k = 0; k < *nroots; ++k) roots[k] = rs.r[k].z;
+    }
     if (rs.status != kRootSuccess) return root_issue(rs.status);
     int selected = -1;
     for (int k = 0; k < rs.count; ++k) {
@@ -559,6 +576,8 @@ struct SplitState {
     double x[NM], y[NM], lnk[NM], res[NM], common[NM], lnphi_l[NM], lnphi_v[NM];
     double beta, z_l, z_v, gibbs, guard, fug, mass_abs, mass_rel;
     int branch_l, branch_v;
+    double roots_l[3], roots_v[3];  // all cubic roots of each phase (Newton starts of a nearby state)
+    int nroots_l, nroots_v;
 };
 
 // `newton` selects a bracketed Newton iteration on the same residual instead of
@@ -695,20 +714,34 @@ enum AttemptStatus : int { kConverged = 0, kNoInteriorRr, kRrFailure, kIndisting
                            kAttemptLineSearchFailed, kUnrepresentableSeed, kBalanceFailure };
 
 // Split evaluation, pt_split.hpp:300-341.  Returns kConverged (= usable state)
-// or the failure class.
+// or the failure class.  `near` (optional): a nearby state whose beta and
+// cubic roots start the Rachford-Rice and root Newton iterations (bracketed
+// Newton only).
 template <int NM>
 __device__ MPMC_FP64_CALL int split_evaluate(const Mixture& m, Cell<NM>& c, const double* lk, SplitState<NM>& s, int& evals,
-                              int budget, double* e, double* num, bool newton_rr = false, double beta0 = 0.5) {
+                              int budget, double* e, double* num, bool newton_rr = false, double beta0 = 0.5,
+                              const SplitState<NM>* near = nullptr) {
     const int n = c.n;
     const int rr = solve_rr(c, lk, s, e, num, newton_rr || c.newton, beta0);
     if (rr != kRrInterior)
         return rr == kRrDegenerate ? kIndistinguishable : (rr == kRrNoInterior ? kNoInteriorRr : kRrFailure);
+    s.nroots_l = s.nroots_v = 0;
+    if (near && &s != near) {
+        s.nroots_l = near->nroots_l;
+        s.nroots_v = near->nroots_v;
+        for (int k = 0; k < 3; ++k) {
+            s.roots_l[k] = near->roots_l[k];
+            s.roots_v[k] = near->roots_v[k];
+        }
+    }
     if (evals >= budget) return kAttemptEvaluationLimit;
     ++evals;
-    if (role_provider(m, c, s.x, false, s.lnphi_l, s.z_l, s.branch_l) != kOk) return kAttemptPropertyFailure;
+    if (role_provider(m, c, s.x, false, s.lnphi_l, s.z_l, s.branch_l, s.roots_l, &s.nroots_l) != kOk)
+        return kAttemptPropertyFailure;
     if (evals >= budget) return kAttemptEvaluationLimit;
     ++evals;
-    if (role_provider(m, c, s.y, true, s.lnphi_v, s.z_v, s.branch_v) != kOk) return kAttemptPropertyFailure;
+    if (role_provider(m, c, s.y, true, s.lnphi_v, s.z_v, s.branch_v, s.roots_v, &s.nroots_v) != kOk)
+        return kAttemptPropertyFailure;
     double correction = 0.0, magnitude = 1.0, mc = 0.0, gibbs = 0.0, fug = 0.0;
     const double beta = s.beta;
     for (int i = 0; i < n; ++i) {
@@ -758,6 +791,12 @@ __device__ __forceinline__ void copy_state(SplitState<NM>& d, const SplitState<N
     d.mass_rel = s.mass_rel;
     d.branch_l = s.branch_l;
     d.branch_v = s.branch_v;
+    d.nroots_l = s.nroots_l;
+    d.nroots_v = s.nroots_v;
+    for (int k = 0; k < 3; ++k) {
+        d.roots_l[k] = s.roots_l[k];
+        d.roots_v[k] = s.roots_v[k];
+    }
 }
 
 // iterate_pt_split from ln K in `lk0`; the last accepted state ends in `point`.

@@ -142,8 +142,15 @@ __device__ bool mix(const WCell<NM, S>& c, double x, double& s, double& amix, do
 // the bracketed Newton iteration of the reference's stopping width on each
 // interval runs concurrently, then the roots are checked and ordered exactly
 // as in the sequential solver.
+// `hint` (per lane, in/out): the root Z this lane's interval had in a nearby
+// evaluation (NaN: none); Newton starts there when it lies inside the
+// interval, else at the midpoint.  On return, the lane's root of this call
+// (NaN where its interval holds none).
 template <int S>
-__device__ inline void roots_by_interval(double a, double b, fp64::RootSet& rs, int& iterations) {
+__device__ inline void roots_by_interval(double a, double b, fp64::RootSet& rs, int& iterations,
+                                         double* hint = nullptr) {
+    const double lane_hint = hint ? *hint : NAN;
+    if (hint) *hint = NAN;
     using fp64::Cubic;
     const int lane = seg_lane<S>();
     rs.count = 0;
@@ -201,6 +208,8 @@ __device__ inline void roots_by_interval(double a, double b, fp64::RootSet& rs, 
             bool converged = false;
             const bool increasing = signbit(fl);
             y = (left + right) * 0.5;
+            const double yh = (lane_hint - b) / rs.scale;
+            if (yh > left && yh < right) y = yh;  // false for a NaN hint
             for (; it < 100; ++it) {
                 const double fy = fp64::poly(y, c);
                 if (fy == 0.0) {
@@ -256,6 +265,7 @@ __device__ inline void roots_by_interval(double a, double b, fp64::RootSet& rs, 
                   pres <= 512.0 * kEps;
         dvalid = slope_ratio > 8.0 * 1.4901161193847656e-08;
         sign = dh > 0.0 ? 1 : (dh < 0.0 ? -1 : 0);
+        if (hint && ok_root) *hint = z;
     }
     // sequential assembly in interval order
     for (int k = 0; k < intervals; ++k) {
@@ -329,13 +339,14 @@ __device__ bool ln_phi(const WCell<NM, S>& c, double s, double amix, double bmix
 // Stability provider (pr76_stability.hpp:36-119): ln phi of the minimum-Gibbs
 // admissible root at x.
 template <int NM, int S>
-__device__ int stability_provider(WCell<NM, S>& c, double x, double& out, bool& smooth, int counter_row) {
+__device__ int stability_provider(WCell<NM, S>& c, double x, double& out, bool& smooth, int counter_row,
+                                  double* hint = nullptr) {
     ++c.counters[counter_row];
     double s, amix, bmix, A, B;
     if (!mix(c, x, s, amix, bmix)) return kRootRange;
     if (!fp64::coefficients(c.p, c.t, amix, bmix, A, B)) return kRootRange;
     fp64::RootSet rs;
-    roots_by_interval<S>(A, B, rs, c.counters[cRootIters]);
+    roots_by_interval<S>(A, B, rs, c.counters[cRootIters], hint);
     if (rs.status != fp64::kRootSuccess) return fp64::root_issue(rs.status);
     double phi[2] = {0.0, 0.0};
     int cand[2] = {0, 0};
@@ -371,13 +382,14 @@ __device__ int stability_provider(WCell<NM, S>& c, double x, double& out, bool& 
 // Role provider (pr76_split.hpp:38-84): liquid = smallest, vapor = largest
 // admissible root.
 template <int NM, int S>
-__device__ int role_provider(WCell<NM, S>& c, double x, bool vapor, double& lnphi, double& z_out, int& branch) {
+__device__ int role_provider(WCell<NM, S>& c, double x, bool vapor, double& lnphi, double& z_out, int& branch,
+                             double* hint = nullptr) {
     ++c.counters[cSplitEvals];
     double s, amix, bmix, A, B;
     if (!mix(c, x, s, amix, bmix)) return kRootRange;
     if (!fp64::coefficients(c.p, c.t, amix, bmix, A, B)) return kRootRange;
     fp64::RootSet rs;
-    roots_by_interval<S>(A, B, rs, c.counters[cRootIters]);
+    roots_by_interval<S>(A, B, rs, c.counters[cRootIters], hint);
     if (rs.status != fp64::kRootSuccess) return fp64::root_issue(rs.status);
     int selected = -1;
     for (int k = 0; k < rs.count; ++k) {
@@ -400,6 +412,7 @@ struct Tpd {
     double w, res, lw;  // per lane
     double value, guard, stat;
     bool smooth;
+    double root_hint;  // per lane: the cubic root of this lane's interval (Newton start of the next point)
 };
 
 template <int NM, int S>
@@ -453,10 +466,11 @@ template <int NM, int S>
 __device__ int trial(WCell<NM, S>& c, double start, double ref, double tol, int row, Tpd& point, int done) {
     Tpd next;
     next.w = start;
+    next.root_hint = NAN;
     {
         double phi;
         bool smooth = true;
-        int is = stability_provider(c, next.w, phi, smooth, row);
+        int is = stability_provider(c, next.w, phi, smooth, row, &next.root_hint);
         if (is == kOk) is = tpd(c, phi, ref, next);
         if (is != kOk) return fp64::kPropertyFailure;
         next.smooth = smooth;
@@ -486,7 +500,8 @@ __device__ int trial(WCell<NM, S>& c, double start, double ref, double tol, int 
             if (!positive) continue;
             double phi;
             bool smooth = true;
-            int is = stability_provider(c, next.w, phi, smooth, row);
+            next.root_hint = point.root_hint;
+            int is = stability_provider(c, next.w, phi, smooth, row, &next.root_hint);
             if (is == kOk) is = tpd(c, phi, ref, next);
             if (is != kOk) continue;
             next.smooth = smooth;
@@ -517,6 +532,7 @@ struct Split {
     double x, y, lnk, res, common, lnphi_l, lnphi_v;  // per lane
     double beta, z_l, z_v, gibbs, guard, fug, mass_abs, mass_rel;
     int branch_l, branch_v;
+    double hint_l, hint_v;  // per lane: each phase's cubic root of this lane's interval
 };
 
 // Rachford-Rice by bracketed Newton (rachford_rice.hpp:70-147 checks).
@@ -615,19 +631,26 @@ __device__ int rachford_rice(WCell<NM, S>& c, double lk, Split& s, double beta0 
     return fp64::kRrInterior;
 }
 
-// Split evaluation at ln K (pt_split.hpp:300-341).
+// Split evaluation at ln K (pt_split.hpp:300-341).  `near` (optional): a
+// nearby state whose beta and cubic roots start the Rachford-Rice and root
+// Newton iterations.
 template <int NM, int S>
-__device__ int split_evaluate(WCell<NM, S>& c, double lk, Split& s, int& evals, int budget, double beta0 = 0.5) {
+__device__ int split_evaluate(WCell<NM, S>& c, double lk, Split& s, int& evals, int budget, double beta0 = 0.5,
+                              const Split* near = nullptr) {
+    s.hint_l = near ? near->hint_l : NAN;
+    s.hint_v = near ? near->hint_v : NAN;
     const int rr = rachford_rice(c, lk, s, beta0);
     if (rr != fp64::kRrInterior)
         return rr == fp64::kRrDegenerate ? fp64::kIndistinguishable
                                          : (rr == fp64::kRrNoInterior ? fp64::kNoInteriorRr : fp64::kRrFailure);
     if (evals >= budget) return fp64::kAttemptEvaluationLimit;
     ++evals;
-    if (role_provider(c, s.x, false, s.lnphi_l, s.z_l, s.branch_l) != kOk) return fp64::kAttemptPropertyFailure;
+    if (role_provider(c, s.x, false, s.lnphi_l, s.z_l, s.branch_l, &s.hint_l) != kOk)
+        return fp64::kAttemptPropertyFailure;
     if (evals >= budget) return fp64::kAttemptEvaluationLimit;
     ++evals;
-    if (role_provider(c, s.y, true, s.lnphi_v, s.z_v, s.branch_v) != kOk) return fp64::kAttemptPropertyFailure;
+    if (role_provider(c, s.y, true, s.lnphi_v, s.z_v, s.branch_v, &s.hint_v) != kOk)
+        return fp64::kAttemptPropertyFailure;
     s.lnk = 0.0;
     s.res = 0.0;
     s.common = 0.0;
@@ -692,7 +715,7 @@ __device__ int attempt(WCell<NM, S>& c, double lk0, Split& point, int& evals, in
         bool accepted = false;
         for (int bt = 0; bt < 24; ++bt, alpha *= 0.5) {
             const double lk = c.act ? point.lnk + (alpha / scale) * point.res : 0.0;
-            st = split_evaluate(c, lk, next, evals, 20000, point.beta);
+            st = split_evaluate(c, lk, next, evals, 20000, point.beta, &point);
             if (st == fp64::kAttemptEvaluationLimit) return st;
             if (st != fp64::kConverged) continue;
             const double predicted = -alpha * slope;
@@ -878,7 +901,7 @@ __device__ bool polish(WCell<NM, S>& c, double lk, Split& st) {
         const double d = lu_solve_rows<NM, S>(J, c.n, piv, c.act ? -st.res : 0.0);
         if (wany<S>(c.comp && !isfinite(d))) return prev <= 1e-11;
         const double next_lk = c.act ? st.lnk + d : 0.0;
-        if (split_evaluate(c, next_lk, nx, evals, 1 << 30, st.beta) != fp64::kConverged) return prev <= 1e-11;
+        if (split_evaluate(c, next_lk, nx, evals, 1 << 30, st.beta, &st) != fp64::kConverged) return prev <= 1e-11;
         if (!(nx.fug < prev)) return prev <= 1e-11;
         st = nx;
         prev = st.fug;
