@@ -1,0 +1,31 @@
+"""Ordered-path continuation on the GPU: 96 feeds of the three-phase fixture
+mixture stepped along p = 0.2 .. 5 MPa at 250 K with ln K warm starts.  Every
+point's published status equals a fresh cold max-3-phase solve of that point,
+so the transition brackets are the cold scan's."""
+
+import numpy as np
+import pytest
+
+from mpmc_hnu_gb300 import continuation, synth
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", ["mixed", "batched"])
+def test_continuation_equals_fresh_solves(gpu_lib, form):
+    mix = synth.three_phase_fixture_mixture()
+    _, _, z = synth.make_three_phase_cells(96, seed=51, anchor_fraction=0.5)
+    npoint = 10
+    p = np.tile(np.exp(np.linspace(np.log(2e5), np.log(5e6), npoint)), (96, 1))
+    t = np.full_like(p, 250.0)
+    res = continuation.solve_paths(mix, z, p, t, form=form)
+    g = gpu_lib.GpuFlash(mix, form=form)
+    cold = np.empty_like(res["status"])
+    for k in range(npoint):
+        out, _ = g.solve_max3(np.ascontiguousarray(p[:, k]), np.ascontiguousarray(t[:, k]), z)
+        cold[:, k] = out["status"]
+    g.close()
+    print(form, "phase counts", np.bincount(res["phase_count"].ravel(), minlength=4), "brackets",
+          len(res["brackets"]))
+    assert np.array_equal(res["status"], cold)
+    assert res["brackets"] == continuation.transition_brackets(continuation.phase_counts(cold))
+    assert (res["phase_count"] == 3).any() and len(res["brackets"]) > 0
