@@ -53,7 +53,7 @@ typedef enum mpmc_status {
     MPMC_ERR_INVALID_ARGUMENT = 1, /* reference: std::invalid_argument / length_error */
     MPMC_ERR_DOMAIN = 2,           /* reference: std::domain_error (bad mixture data) */
     MPMC_ERR_CUDA = 3,             /* a CUDA runtime call failed */
-    MPMC_ERR_UNSUPPORTED = 4,      /* component count or option outside this build */
+    MPMC_ERR_UNSUPPORTED = 4,      /* component count or option outside this library */
     MPMC_ERR_TIMEOUT = 5           /* a bounded device wait gave up */
 } mpmc_status;
 

@@ -234,7 +234,7 @@ int prepare_device(mpmc_gpu_flash* h, int64_t ncell, pr76::DeviceOutputs& d) {
             h->workspace.ensure(pr76::batched_workspace_bytes(h->n, ncell, h->form == MPMC_FORM_BATCHED));
         if (e != cudaSuccess) return cuda_fail(e, "batched workspace allocation");
     } else if (h->form != MPMC_FORM_PLAIN_FP64) {
-        return fail(MPMC_ERR_UNSUPPORTED, "algorithm form not available in this build");
+        return fail(MPMC_ERR_UNSUPPORTED, "algorithm form not available in this library");
     }
     return MPMC_OK;
 }

@@ -19,8 +19,8 @@ reference_outputs.npz
     dew-limit edge states of tests/flash/pt_split/dew_limit_references.hpp and
     (b) seeded synthetic cells for N in {3, 4, 6, 10, 12, 20}.
 
-The GPU machine does not have the reference; the committed outputs of this script
-are what the tests read there.
+Machines without the reference sources run the tests against the committed
+outputs of this script.
 """
 
 from __future__ import annotations
