@@ -1579,9 +1579,42 @@ inline int witness_sides(const Model& m, Work& wk, double p, double t, const std
     return 0;
 }
 
-inline Max3Result solve_max3(const Model& m, Work& wk, double p, double t, const std::vector<double>& feed) {
+// A caller's three-phase start (pr76_three_phase.hpp:110-116): three
+// compositions and the independent fractions (beta_1, beta_2).
+struct ThreeStart {
+    std::vector<double> x[3];
+    double fraction[2] = {1.0 / 3.0, 1.0 / 3.0};
+};
+
+// `initial_starts` / `final_starts` are the two-phase solve's extra stability
+// starts and `three_starts` the caller's three-phase starts
+// (pr76_three_phase.hpp:328-336, 457-486); each start class has its own
+// quota of 16 attempts.
+inline Max3Result solve_max3(const Model& m, Work& wk, double p, double t, const std::vector<double>& feed,
+                             const std::vector<std::vector<double>>& initial_starts = {},
+                             const std::vector<std::vector<double>>& final_starts = {},
+                             const std::vector<ThreeStart>& three_starts = {}) {
     Max3Result r;
-    r.base = solve_vle(m, wk, p, t, feed);
+    // pr76_pt_max3_check_starts, :211-244: a bad start is a domain_error
+    for (const ThreeStart& st : three_starts) {
+        if (!rr3_feasible(st.fraction[0], st.fraction[1])) {
+            r.status = -1;
+            return r;
+        }
+        for (int k = 0; k < 3; ++k) {
+            double sum;
+            if (static_cast<int>(st.x[k].size()) != m.n || !check_composition(st.x[k].data(), m.n, sum)) {
+                r.status = -1;
+                return r;
+            }
+            for (int i = 0; i < m.n; ++i)
+                if ((feed[i] > 0) != (st.x[k][i] > 0)) {
+                    r.status = -1;
+                    return r;
+                }
+        }
+    }
+    r.base = solve_vle(m, wk, p, t, feed, initial_starts, final_starts);
     switch (r.base.status) {
     case kInvalid: r.status = -1; return r;
     case kSinglePhase: r.status = kM3Single; return r;
@@ -1597,14 +1630,17 @@ inline Max3Result solve_max3(const Model& m, Work& wk, double p, double t, const
     const StabilityResult& review = r.base.final_review;
     const std::vector<double>& nfeed = r.base.initial.feed;
     const ThreeOptions to;
-    bool saw_higher = false, saw_boundary = false, limit = false;
+    bool saw_higher = false, saw_boundary = false, limit = false, hint_limit = false;
+    int automatic = 0, supplied = 0;
     // run_attempt of pr76_three_phase.hpp:379-455; true when the cell is settled
     auto run_attempt = [&](const std::vector<double>& lk1, const std::vector<double>& lk2, const double fr[2],
-                           const bool upper[3]) -> bool {
-        if (r.attempts >= 16) {
-            limit = true;
+                           const bool upper[3], bool from_hint = false) -> bool {
+        int& used = from_hint ? supplied : automatic;
+        if (used >= 16) {
+            (from_hint ? hint_limit : limit) = true;
             return false;
         }
+        ++used;
         ++r.attempts;
         const ThreeResult eq = iterate_three(m, wk, p, t, nfeed, lk1, lk2, fr, upper, to);
         if (eq.status == kTPhaseDisappearance) {
@@ -1647,6 +1683,17 @@ inline Max3Result solve_max3(const Model& m, Work& wk, double p, double t, const
         return false;
     };
     std::vector<double> lk1, lk2;
+    // caller starts first, every combination of root sides (:457-486)
+    for (const ThreeStart& st : three_starts) {
+        if (!log_ratio(st.x[1], st.x[0], nfeed, lk1) || !log_ratio(st.x[2], st.x[0], nfeed, lk2)) continue;
+        for (int s0 = 0; s0 < 2 && !hint_limit; ++s0)
+            for (int s1 = 0; s1 < 2 && !hint_limit; ++s1)
+                for (int s2 = 0; s2 < 2 && !hint_limit; ++s2) {
+                    const bool upper[3] = {s0 == 1, s1 == 1, s2 == 1};
+                    if (run_attempt(lk1, lk2, st.fraction, upper, true)) return r;
+                }
+        if (hint_limit) break;
+    }
     if (log_ratio(pair.rr.y, pair.rr.x, nfeed, lk1)) {
         for (const Trial& wit : review.trials) {
             if (wit.status != kNegativeTpd || !wit.has_point) continue;
@@ -1665,6 +1712,63 @@ inline Max3Result solve_max3(const Model& m, Work& wk, double p, double t, const
     }
     r.status = saw_higher ? kM3Higher : (saw_boundary ? kM3Boundary : kM3Indeterminate);
     return r;
+}
+
+// Ordered-path continuation, pr76_pt_continuation.hpp:183-306 (default
+// options): every point is a max3 solve whose extra stability starts are the
+// previous accepted point's phase compositions and whose three-phase start
+// is the previous three-phase set; hints reset after an unresolved point.
+// Writes each point's max3 status; false for an invalid path or feed (the
+// reference throws).
+inline bool solve_continuation(const Model& m, Work& wk, const double* p, const double* t, int npoint,
+                               const std::vector<double>& feed_in, int* status) {
+    for (int k = 0; k < npoint; ++k)
+        if (!std::isfinite(p[k]) || !(p[k] > 0) || !std::isfinite(t[k]) || !(t[k] > 0)) return false;
+    double sum;
+    if (!check_composition(feed_in.data(), m.n, sum)) return false;
+    std::vector<double> feed(m.n);
+    for (int i = 0; i < m.n; ++i) feed[i] = feed_in[i] / sum;
+    bool have_prev = false, have_three = false;
+    std::vector<std::vector<double>> prev;
+    ThreeStart three;
+    for (int k = 0; k < npoint; ++k) {
+        std::vector<std::vector<double>> starts;
+        if (have_prev)
+            for (const auto& c : prev) {  // pr76_pt_continuation_append_unique, :106-118
+                bool dup = false;
+                for (const auto& e : starts) dup = dup || e == c;
+                if (!dup) starts.push_back(c);
+            }
+        std::vector<ThreeStart> hints;
+        if (have_three) hints.push_back(three);
+        if (!make_temp_cache(m, t[k], wk.tc)) return false;
+        const Max3Result r = solve_max3(m, wk, p[k], t[k], feed, starts, starts, hints);
+        if (r.status < 0) return false;
+        status[k] = r.status;
+        prev.clear();
+        have_three = false;
+        switch (r.status) {  // phase compositions of the accepted point, :118-146
+        case kM3Single: prev.push_back(r.base.initial.feed); break;
+        case kM3Two: {
+            const FlashResult& src = r.has_neighbor ? r.neighbor : r.base;
+            if (src.has_candidate) {
+                prev.push_back(src.candidate.rr.x);
+                prev.push_back(src.candidate.rr.y);
+            }
+            break;
+        }
+        case kM3Three:
+            for (int q = 0; q < 3; ++q) prev.push_back(r.three.x[q]);
+            for (int q = 0; q < 3; ++q) three.x[q] = r.three.x[q];
+            three.fraction[0] = r.three.fraction[1];
+            three.fraction[1] = r.three.fraction[2];
+            have_three = true;
+            break;
+        default: break;
+        }
+        have_prev = r.status == kM3Single || r.status == kM3Two || r.status == kM3Three;
+    }
+    return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -2430,6 +2534,37 @@ int oracle_max3_batch(int n, const double* tc, const double* pc, const double* o
     const int64_t chunk = (ncell + threads - 1) / threads;
     for (int k = 0; k < threads; ++k) {
         const int64_t lo = k * chunk, hi = std::min<int64_t>(ncell, lo + chunk);
+        if (lo < hi) pool.emplace_back(run, lo, hi);
+    }
+    for (auto& th : pool) th.join();
+    return 0;
+}
+
+// Ordered-path continuation of npath feeds z [n * npath], each along its own
+// npoint states (p, t [npath * npoint], path-major): per point the max3 status
+// (codes of oracle_max3_batch; -1 on every point of an invalid path).
+int oracle_continuation_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                              int64_t npath, int64_t npoint, const double* p, const double* t, const double* z,
+                              int threads, int32_t* max3_status) {
+    if (n < 1 || n > 256 || npath < 0 || npoint < 1 || !p || !t || !z || !max3_status) return -1;
+    const oracle::Model m = oracle::make_model(n, tc, pc, omega, kij);
+    auto run = [&](int64_t lo, int64_t hi) {
+        oracle::Work wk;
+        wk.init(n);
+        std::vector<double> feed(n);
+        std::vector<int> st(static_cast<size_t>(npoint));
+        for (int64_t path = lo; path < hi; ++path) {
+            for (int i = 0; i < n; ++i) feed[i] = z[i * npath + path];
+            const bool ok = oracle::solve_continuation(m, wk, p + path * npoint, t + path * npoint,
+                                                       static_cast<int>(npoint), feed, st.data());
+            for (int64_t k = 0; k < npoint; ++k) max3_status[path * npoint + k] = ok ? st[k] : -1;
+        }
+    };
+    if (threads < 1) threads = 1;
+    std::vector<std::thread> pool;
+    const int64_t chunk = (npath + threads - 1) / threads;
+    for (int k = 0; k < threads; ++k) {
+        const int64_t lo = k * chunk, hi = std::min<int64_t>(npath, lo + chunk);
         if (lo < hi) pool.emplace_back(run, lo, hi);
     }
     for (auto& th : pool) th.join();

@@ -220,3 +220,45 @@ def reference_max3(mix, p, t, z, threads: int = 8):
     if not reference_available():
         raise FileNotFoundError(REF_SO)
     return _max3("ref_max3_batch", REF_SO, mix, p, t, z, threads)
+
+
+def reference_continuation(mix, pressures, temperatures, z, threads: int = 8):
+    """The reference's solve_pr76_pt_continuation (default options) of feeds
+    z [n, npath] along paths pressures / temperatures [npath, npoint]; returns
+    (max3_status, published) [npath, npoint] with ref_max3_batch's codes."""
+    if not reference_available():
+        raise FileNotFoundError(REF_SO)
+    tc, pc, omega, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
+    z = np.ascontiguousarray(z, dtype=np.float64)
+    p = np.ascontiguousarray(pressures, dtype=np.float64)
+    t = np.ascontiguousarray(temperatures, dtype=np.float64)
+    n, npath = z.shape
+    npoint = p.shape[1]
+    ms = np.empty((npath, npoint), np.int32)
+    pub = np.empty((npath, npoint), np.int32)
+    fn = _lib(REF_SO).ref_continuation_batch
+    fn.restype = ctypes.c_int
+    fn(ctypes.c_int(n), *[ctypes.c_void_p(a.ctypes.data) for a in (tc, pc, omega, kij)], ctypes.c_int64(npath),
+       ctypes.c_int64(npoint), *[ctypes.c_void_p(a.ctypes.data) for a in (p, t, z)], ctypes.c_int(threads),
+       ctypes.c_void_p(ms.ctypes.data), ctypes.c_void_p(pub.ctypes.data))
+    return ms, pub
+
+
+def continuation(mix, pressures, temperatures, z, threads: int = 8):
+    """The oracle's restatement of solve_pr76_pt_continuation (default
+    options): max3 status [npath, npoint] of feeds z [n, npath] along paths
+    pressures / temperatures [npath, npoint]."""
+    build()
+    tc, pc, omega, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
+    z = np.ascontiguousarray(z, dtype=np.float64)
+    p = np.ascontiguousarray(pressures, dtype=np.float64)
+    t = np.ascontiguousarray(temperatures, dtype=np.float64)
+    n, npath = z.shape
+    npoint = p.shape[1]
+    ms = np.empty((npath, npoint), np.int32)
+    fn = _lib(ORACLE_SO).oracle_continuation_batch
+    fn.restype = ctypes.c_int
+    fn(ctypes.c_int(n), *[ctypes.c_void_p(a.ctypes.data) for a in (tc, pc, omega, kij)], ctypes.c_int64(npath),
+       ctypes.c_int64(npoint), *[ctypes.c_void_p(a.ctypes.data) for a in (p, t, z)], ctypes.c_int(threads),
+       ctypes.c_void_p(ms.ctypes.data))
+    return ms

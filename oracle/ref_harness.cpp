@@ -13,9 +13,11 @@
 //   mpmc::thermodynamics::Pr76PhaseAdWorkspace     modules/thermodynamics/include/mpmc/thermodynamics/pr76_phase_ad.hpp:43
 //   mpmc::flash::Pr76PtFlashBackend::solve         modules/flash/include/mpmc/flash/pr76_pt_flash_backend.hpp:190
 //   mpmc::flash::solve_pr76_pt_max3                modules/flash/include/mpmc/flash/pr76_three_phase.hpp:328
+//   mpmc::flash::solve_pr76_pt_continuation        modules/flash/include/mpmc/flash/pr76_pt_continuation.hpp:183
 
 #include <mpmc/flash/pr76_pt_flash_backend.hpp>
 #include <mpmc/flash/pr76_three_phase.hpp>
+#include <mpmc/flash/pr76_pt_continuation.hpp>
 #include <mpmc/flash/pr76_sensitivity.hpp>
 #include <mpmc/physics/pr76_thermodynamic_closure.hpp>
 #include <mpmc/thermodynamics/pr76_phase_ad.hpp>
@@ -374,6 +376,59 @@ int ref_max3_batch(int n, const double* tc, const double* pc, const double* omeg
     const int64_t chunk = (ncell + threads - 1) / threads;
     for (int k = 0; k < threads; ++k) {
         const int64_t lo = k * chunk, hi = std::min<int64_t>(ncell, lo + chunk);
+        if (lo < hi) pool.emplace_back(run, lo, hi);
+    }
+    for (auto& th : pool) th.join();
+    return 0;
+}
+
+// The reference's ordered-path continuation (default options: previous phase
+// compositions and three-phase state carried as hints) of npath feeds, each
+// along its own npoint states; per point the max3 status and the published
+// status (codes of ref_max3_batch).  p, t are [npath * npoint] path-major,
+// z is [n * npath].
+int ref_continuation_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                           int64_t npath, int64_t npoint, const double* p, const double* t, const double* z,
+                           int threads, int32_t* max3_status, int32_t* published) {
+    std::vector<std::string> order;
+    const th::PrParameterSet params = make_parameters(n, tc, pc, omega, kij, order);
+    const auto model = th::Pr76Phase<double>::from_parameters(params);
+    auto run = [&](int64_t lo, int64_t hi) {
+        fl::Pr76VleEvaluator evaluator(model);
+        for (int64_t path = lo; path < hi; ++path) {
+            std::vector<fl::Pr76PtPathState> states(static_cast<size_t>(npoint));
+            for (int64_t k = 0; k < npoint; ++k) states[k] = {p[path * npoint + k], t[path * npoint + k]};
+            std::vector<double> feed(n);
+            for (int i = 0; i < n; ++i) feed[i] = z[i * npath + path];
+            try {
+                const auto r = fl::solve_pr76_pt_continuation(states, feed, evaluator);
+                for (int64_t k = 0; k < npoint; ++k) {
+                    const auto& pt = r.points[static_cast<size_t>(k)];
+                    const int ms = static_cast<int>(pt.solve.status);
+                    int pub = 3;
+                    switch (pt.solve.status) {
+                    case fl::Pr76PtMax3Status::single_phase: pub = 0; break;
+                    case fl::Pr76PtMax3Status::two_phase: pub = 1; break;
+                    case fl::Pr76PtMax3Status::three_phase: pub = 4; break;
+                    case fl::Pr76PtMax3Status::higher_phase_count_or_wrong_candidate: pub = 2; break;
+                    default: pub = 3; break;
+                    }
+                    max3_status[path * npoint + k] = ms;
+                    published[path * npoint + k] = pub;
+                }
+            } catch (const std::exception&) {
+                for (int64_t k = 0; k < npoint; ++k) {
+                    max3_status[path * npoint + k] = -1;
+                    published[path * npoint + k] = -1;
+                }
+            }
+        }
+    };
+    if (threads < 1) threads = 1;
+    std::vector<std::thread> pool;
+    const int64_t chunk = (npath + threads - 1) / threads;
+    for (int k = 0; k < threads; ++k) {
+        const int64_t lo = k * chunk, hi = std::min<int64_t>(npath, lo + chunk);
         if (lo < hi) pool.emplace_back(run, lo, hi);
     }
     for (auto& th : pool) th.join();

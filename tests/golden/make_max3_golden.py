@@ -11,6 +11,10 @@ a quarter at the fixture's anchor state (1 MPa, 250 K, feeds inside the tie
 triangle), the rest spread over p in [0.2, 5] MPa and T in [200, 300] K;
 feeds on and near the triangle's edges; and the cells of a wide scan whose
 three-phase candidate failed its final review, with a sample of the others.
+Also writes tests/golden/continuation_reference.npz: the reference's
+ordered-path continuation (solve_pr76_pt_continuation, default options) of
+96 fixture feeds along p = 0.2 .. 5 MPa at 250 K, with the fresh (cold)
+max3 status of every point beside it.
 """
 
 from __future__ import annotations
@@ -63,6 +67,17 @@ def main() -> None:
                         **{f"ref_{k}": v for k, v in ref.items()})
     counts = np.bincount(ref["max3_status"] + 1, minlength=7)
     print("max3 status counts (invalid, single, two, three, boundary, higher, indeterminate):", counts)
+    # the reference's ordered-path continuation (pr76_pt_continuation.hpp:183-306,
+    # default options) of 96 fixture feeds along p = 0.2 .. 5 MPa at 250 K
+    _, _, zc = synth.make_three_phase_cells(96, seed=51, anchor_fraction=0.5)
+    pc = np.tile(np.exp(np.linspace(np.log(2e5), np.log(5e6), 10)), (96, 1))
+    tc = np.full_like(pc, 250.0)
+    ms, pub = pyoracle.reference_continuation(mix, pc, tc, zc, threads=16)
+    cold = np.stack([pyoracle.reference_max3(mix, np.ascontiguousarray(pc[:, k]), np.ascontiguousarray(tc[:, k]),
+                                             zc, threads=16)["max3_status"] for k in range(pc.shape[1])], axis=1)
+    np.savez_compressed(os.path.join(HERE, "continuation_reference.npz"), p=pc, t=tc, z=zc, ref_max3_status=ms,
+                        ref_published=pub, ref_cold_max3_status=cold)
+    print("continuation: points whose hint-seeded status differs from a fresh solve:", int((ms != cold).sum()))
 
 
 if __name__ == "__main__":
