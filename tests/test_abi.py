@@ -79,3 +79,12 @@ def test_null_arguments_are_rejected(lib):
     assert lib.mpmc_gpu_flash_solve(None, 1, None, None, None, None) == 1
     assert lib.mpmc_gpu_flash_solve_device(None, 1, None, None, None, None, None) == 1
     assert lib.mpmc_gpu_flash_destroy(None) == 0
+
+
+def test_null_arguments_of_the_warm_and_max3_entries(lib):
+    """The warm-start and max-3-phase entries validate before any device work."""
+    assert lib.mpmc_gpu_flash_solve_warm(None, 1, None, None, None, None, None) == 1
+    assert lib.mpmc_gpu_flash_solve_device_warm(None, 1, None, None, None, None, None, None) == 1
+    assert lib.mpmc_gpu_flash_solve_max3(None, 1, None, None, None, None, None) == 1
+    assert lib.mpmc_gpu_flash_solve_device_max3(None, 1, None, None, None, None, None, None) == 1
+    assert b"null handle" in lib.mpmc_gpu_flash_last_error()
