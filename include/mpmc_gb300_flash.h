@@ -252,6 +252,95 @@ int mpmc_gpu_flash_solve_device_max3(mpmc_gpu_flash* handle, int64_t n_cells, co
                                      const double* z, const mpmc_flash_outputs* out,
                                      const mpmc_three_phase_outputs* out3, void* stream);
 
+/* ------------------------------------------------------------------------
+ * Selected-phase property chart: the flow module's per-cell property and
+ * Jacobian publication on a frozen natural-variable chart,
+ *   mpmc::flow::evaluate_pr76_selected_phase_property_chart
+ *     (modules/flow/include/mpmc/flow/pr76_selected_phase_property_closure.hpp:533-822)
+ * over the fixed-selected-branch closure Pr76SelectedPhasePropertyClosure
+ * (:258-475), which the production cell evaluators call once per cell
+ * (Pr76ProductionCellEvaluatorTraits::evaluate_property_chart,
+ * modules/flow/discretization/petsc/include/mpmc/flow_discretization_petsc/
+ * pr76_production_cell_evaluator.hpp:88-101).  Here one call evaluates a
+ * whole batch of cells that share the closure (phase count, selected roots,
+ * molar masses and transport/caloric model).
+ *
+ * Chart of a cell with P phases and n components (the layout of
+ * NaturalVariableLayoutDescriptor, natural_variable_cell_state.hpp:66-216),
+ * q = P n + 1 unknowns:
+ *   q[0] = p [Pa], q[1] = T [K], q[2 .. P] = saturations of phases 0..P-2,
+ *   then per phase k the n - 1 independent mole fractions in component order
+ *   with the phase's dependent (pivot) component left out; the dependent
+ *   fraction is 1 - sum of the others.
+ * Outputs per cell, rows in this order (P (5 + n) + (P - 1) n rows):
+ *   per phase k, at row k (5 + n): molar density [mol/m3], mass density
+ *   [kg/m3], dynamic viscosity [Pa s], specific enthalpy [J/kg], specific
+ *   internal energy u = h - p / rho_mass [J/kg], ln phi_0 .. ln phi_{n-1};
+ *   then per phase k >= 1 and component i the equilibrium residual
+ *   ln(x_0,i / x_k,i) + ln phi_0,i - ln phi_k,i.
+ * values[row * n_cells + c] holds the value and
+ * jacobian[(row * q + column) * n_cells + c] its derivative by chart column.
+ *
+ * The viscosity and enthalpy are the caller's model in the reference (the
+ * closure's TransportCaloricProvider, :258-270).  This library evaluates the
+ * affine model
+ *   f = c[0] + c[1] p + c[2] T + sum_i c[7+i] x_i + c[3] rho + c[4] M
+ *       + c[5] rho_mass + c[6] root_index
+ * with M = sum_i x_i M_i, once with the viscosity and once with the enthalpy
+ * coefficients (7 + n each).  A nonlinear correlation is not available on the
+ * device; such a caller evaluates it from the published density, composition
+ * and their Jacobians. */
+typedef struct mpmc_property_chart_spec {
+    int32_t phase_count;           /* P, 1..3 */
+    int32_t root_index[3];         /* Pr76SelectedPhase::root_index of phase 0..P-1: the
+                                      index into the PR76 roots ordered by increasing Z */
+    const double* molar_mass;      /* [n] kg/mol, finite and > 0 */
+    const double* viscosity;       /* [7 + n] affine coefficients */
+    const double* enthalpy;        /* [7 + n] affine coefficients */
+} mpmc_property_chart_spec;
+
+/* Per-cell status of the chart.  The reference throws; the class of each
+ * throw is kept so the production evaluator's mapping (domain errors ->
+ * NaturalVariableSnesEvaluationStatus3D::domain_error, std::out_of_range ->
+ * PETSC_ERR_PLIB, pr76_production_cell_evaluator.hpp:42-86) applies. */
+typedef enum mpmc_chart_status {
+    MPMC_CHART_OK = 0,
+    MPMC_CHART_INPUT_DOMAIN = 1,     /* non-finite chart entry; p, T, a mole fraction or
+                                        M not finite and positive (range/domain_error) */
+    MPMC_CHART_EOS_DOMAIN = 2,       /* the EOS rejected the state: A, B, ln phi or Z not
+                                        representable (range/domain_error) */
+    MPMC_CHART_ROOT_UNRESOLVED = 3,  /* Pr76PhaseError: near-multiple, iteration limit or
+                                        unrepresentable root set */
+    MPMC_CHART_ROOT_INDEX = 4,       /* std::out_of_range: the selected root does not exist */
+    MPMC_CHART_ILL_CONDITIONED = 5,  /* Pr76PhaseError: selected root without a reliable
+                                        derivative */
+    MPMC_CHART_PROPERTY_DOMAIN = 6   /* density, mass density or viscosity not positive, or
+                                        a non-finite property or derivative (range/domain_error) */
+} mpmc_chart_status;
+
+typedef struct mpmc_property_chart_outputs {
+    int32_t* status;   /* [n_cells] mpmc_chart_status */
+    double* values;    /* [rows * n_cells]; NaN rows for a failed cell */
+    double* jacobian;  /* [rows * q * n_cells]; NaN for a failed cell */
+} mpmc_property_chart_outputs;
+
+/* Property chart of n_cells cells: q [(P n + 1) * n_cells] chart values;
+ * dependent [P * n_cells] the dependent component of phase k of cell c at
+ * dependent[k * n_cells + c], or NULL for the last component everywhere
+ * (NaturalVariableCompositionPivot3P::fixed_last).  Host buffers: the call
+ * copies, evaluates and copies back before returning.  One thread per cell in
+ * FP64; the Jacobian is the closed form of the reference's forward-AD
+ * quantity. */
+int mpmc_gpu_flash_property_chart(mpmc_gpu_flash* handle, int64_t n_cells, const mpmc_property_chart_spec* spec,
+                                  const double* q, const int32_t* dependent,
+                                  const mpmc_property_chart_outputs* out);
+/* The same on device buffers, enqueued on `stream` (NULL = default stream);
+ * returns without synchronising. */
+int mpmc_gpu_flash_property_chart_device(mpmc_gpu_flash* handle, int64_t n_cells,
+                                         const mpmc_property_chart_spec* spec, const double* q,
+                                         const int32_t* dependent, const mpmc_property_chart_outputs* out,
+                                         void* stream);
+
 /* Largest device scratch, in bytes, of mpmc_gpu_flash_solve_device_noalloc:
  * a fixed 48 MiB array in the library's device code. */
 #define MPMC_NOALLOC_SCRATCH_BYTES (48u << 20)

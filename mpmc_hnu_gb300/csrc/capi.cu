@@ -84,6 +84,8 @@ struct mpmc_gpu_flash {
     bool timed_warm = false;  // the last timed solve ran a warm and a cold pass
     DevBuf in_warm;     // host entry: staged ln K warm starts
     DevBuf outs3[5];    // host entry: staged three-phase outputs
+    DevBuf chart_in[2];   // host property-chart entry: staged chart values, dependent components
+    DevBuf chart_out[3];  // host property-chart entry: staged status, values, Jacobian
     int32_t shape[8] = {};  // explicit launch shape (mpmc_gpu_flash_set_launch_shape), 0 = default
     bool use_graphs = false;
     std::vector<GraphEntry> graphs;
@@ -443,6 +445,18 @@ cudaError_t launch_max3(int n, const Mixture* d_mix, int64_t ncell, const double
     }
 }
 
+cudaError_t launch_chart(int n, const Mixture* d_mix, const ChartParams& params, int64_t ncell, const double* q,
+                         const int32_t* dep, const ChartOutputs& out, cudaStream_t stream) {
+    switch (capacity_for(n)) {
+    case 4: return launch_chart_nm4(d_mix, params, ncell, q, dep, out, stream);
+    case 8: return launch_chart_nm8(d_mix, params, ncell, q, dep, out, stream);
+    case 12: return launch_chart_nm12(d_mix, params, ncell, q, dep, out, stream);
+    case 16: return launch_chart_nm16(d_mix, params, ncell, q, dep, out, stream);
+    case 20: return launch_chart_nm20(d_mix, params, ncell, q, dep, out, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
 cudaError_t launch_plain(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
                          const double* z, const DeviceOutputs& out, cudaStream_t stream) {
     switch (capacity_for(n)) {
@@ -460,6 +474,41 @@ namespace {
 int solve_host(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
                const double* ln_k_warm, const mpmc_flash_outputs* out, const mpmc_three_phase_outputs* out3,
                bool max3);
+
+// Validates a property-chart call and fills the kernel's closure constants
+// (the checks of the closure's constructor, pr76_selected_phase_property_closure.hpp:274-319,
+// and of the chart's shape, :553-562).
+int chart_params(const mpmc_gpu_flash* h, int64_t ncell, const mpmc_property_chart_spec* spec, const double* q,
+                 pr76::ChartParams& params) {
+    if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
+    if (ncell < 0) return fail(MPMC_ERR_INVALID_ARGUMENT, "negative cell count");
+    if (!spec) return fail(MPMC_ERR_INVALID_ARGUMENT, "property chart: null spec");
+    if (spec->phase_count < 1 || spec->phase_count > 3)
+        return fail(MPMC_ERR_INVALID_ARGUMENT, "property chart: phase_count must be 1, 2 or 3");
+    if (h->n < 2) return fail(MPMC_ERR_INVALID_ARGUMENT, "property chart: at least two components required");
+    if (!spec->molar_mass || !spec->viscosity || !spec->enthalpy)
+        return fail(MPMC_ERR_INVALID_ARGUMENT, "property chart: molar_mass, viscosity and enthalpy must not be null");
+    std::memset(&params, 0, sizeof(params));
+    params.phases = spec->phase_count;
+    for (int k = 0; k < spec->phase_count; ++k) {
+        if (spec->root_index[k] < 0) return fail(MPMC_ERR_INVALID_ARGUMENT, "property chart: negative root index");
+        params.root_index[k] = spec->root_index[k];
+    }
+    for (int i = 0; i < h->n; ++i) {
+        const double mw = spec->molar_mass[i];
+        if (!std::isfinite(mw) || !(mw > 0))
+            return fail(MPMC_ERR_INVALID_ARGUMENT, "property chart: every molar mass must be finite and positive");
+        params.molar_mass[i] = mw;
+    }
+    for (int k = 0; k < 7 + h->n; ++k) {
+        if (!std::isfinite(spec->viscosity[k]) || !std::isfinite(spec->enthalpy[k]))
+            return fail(MPMC_ERR_INVALID_ARGUMENT, "property chart: model coefficients must be finite");
+        params.visc[k] = spec->viscosity[k];
+        params.enth[k] = spec->enthalpy[k];
+    }
+    if (ncell > 0 && !q) return fail(MPMC_ERR_INVALID_ARGUMENT, "property chart: null chart values");
+    return MPMC_OK;
+}
 }  // namespace
 
 extern "C" {
@@ -551,6 +600,8 @@ int mpmc_gpu_flash_destroy(mpmc_gpu_flash* h) {
     h->in_z.release();
     h->in_warm.release();
     for (auto& b : h->outs3) b.release();
+    for (auto& b : h->chart_in) b.release();
+    for (auto& b : h->chart_out) b.release();
     for (auto& b : h->outs) b.release();
     for (auto& b : h->sens_inputs) b.release();
     h->workspace.release();
@@ -662,6 +713,69 @@ int mpmc_gpu_flash_solve_max3(mpmc_gpu_flash* h, int64_t ncell, const double* p,
 int mpmc_gpu_flash_solve_warm(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
                               const double* ln_k_warm, const mpmc_flash_outputs* out) {
     return solve_host(h, ncell, p, t, z, ln_k_warm, out, nullptr, false);
+}
+
+int mpmc_gpu_flash_property_chart_device(mpmc_gpu_flash* h, int64_t ncell, const mpmc_property_chart_spec* spec,
+                                         const double* q, const int32_t* dependent,
+                                         const mpmc_property_chart_outputs* out, void* stream) {
+    pr76::ChartParams params;
+    const int rc = chart_params(h, ncell, spec, q, params);
+    if (rc != MPMC_OK || ncell == 0) return rc;
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    pr76::ChartOutputs d{};
+    if (out) d = {out->status, out->values, out->jacobian};
+    e = pr76::launch_chart(h->n, h->d_mixture, params, ncell, q, dependent, d, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "property chart launch");
+    return MPMC_OK;
+}
+
+int mpmc_gpu_flash_property_chart(mpmc_gpu_flash* h, int64_t ncell, const mpmc_property_chart_spec* spec,
+                                  const double* q, const int32_t* dependent, const mpmc_property_chart_outputs* out) {
+    pr76::ChartParams params;
+    const int rc = chart_params(h, ncell, spec, q, params);
+    if (rc != MPMC_OK || ncell == 0) return rc;
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    const size_t nc = static_cast<size_t>(ncell);
+    const size_t cols = static_cast<size_t>(params.phases) * h->n + 1;
+    const size_t rows = static_cast<size_t>(params.phases) * (5 + h->n) + static_cast<size_t>(params.phases - 1) * h->n;
+    const size_t bytes_in[2] = {cols * nc * sizeof(double), dependent ? params.phases * nc * sizeof(int32_t) : 0};
+    void* host_out[3] = {};
+    if (out) {
+        host_out[0] = out->status;
+        host_out[1] = out->values;
+        host_out[2] = out->jacobian;
+    }
+    const size_t bytes_out[3] = {nc * sizeof(int32_t), rows * nc * sizeof(double), rows * cols * nc * sizeof(double)};
+    for (int k = 0; k < 2; ++k)
+        if (bytes_in[k] && (e = h->chart_in[k].ensure(bytes_in[k])) != cudaSuccess)
+            return cuda_fail(e, "property chart input staging allocation");
+    void* dev_out[3] = {};
+    for (int k = 0; k < 3; ++k) {
+        if (!host_out[k]) continue;
+        if ((e = h->chart_out[k].ensure(bytes_out[k])) != cudaSuccess)
+            return cuda_fail(e, "property chart output staging allocation");
+        dev_out[k] = h->chart_out[k].ptr;
+    }
+    cudaStream_t s = h->stream;
+    if ((e = cudaMemcpyAsync(h->chart_in[0].ptr, q, bytes_in[0], cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "property chart input copy");
+    if (dependent &&
+        (e = cudaMemcpyAsync(h->chart_in[1].ptr, dependent, bytes_in[1], cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(e, "property chart input copy");
+    const pr76::ChartOutputs d{static_cast<int32_t*>(dev_out[0]), static_cast<double*>(dev_out[1]),
+                               static_cast<double*>(dev_out[2])};
+    e = pr76::launch_chart(h->n, h->d_mixture, params, ncell, static_cast<const double*>(h->chart_in[0].ptr),
+                           dependent ? static_cast<const int32_t*>(h->chart_in[1].ptr) : nullptr, d, s);
+    if (e != cudaSuccess) return cuda_fail(e, "property chart launch");
+    for (int k = 0; k < 3; ++k) {
+        if (!host_out[k]) continue;
+        if ((e = cudaMemcpyAsync(host_out[k], dev_out[k], bytes_out[k], cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+            return cuda_fail(e, "property chart output copy");
+    }
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "property chart execution");
+    return MPMC_OK;
 }
 
 }  // extern "C"

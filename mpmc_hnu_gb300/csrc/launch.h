@@ -94,6 +94,29 @@ struct Max3Outputs {
 cudaError_t launch_max3(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
                         const double* z, const DeviceOutputs& out, const Max3Outputs& out3, cudaStream_t stream);
 
+// Closure constants of a selected-phase property chart call (pr76_chart.cuh),
+// passed to the kernel by value.
+struct ChartParams {
+    int phases;
+    int root_index[3];
+    double molar_mass[kMaxC];
+    double visc[7 + kMaxC];  // affine model: constant, p, T, rho, M, rho_mass, root index, x_i
+    double enth[7 + kMaxC];
+};
+
+// Device outputs of the chart (mpmc_property_chart_outputs), any may be null.
+struct ChartOutputs {
+    int32_t* status;
+    double* values;    // [rows * ncell]
+    double* jacobian;  // [rows * q * ncell]
+};
+
+// Selected-phase property chart of ncell cells (chart.cu): q [(P n + 1) *
+// ncell] chart values, dep [P * ncell] dependent components or null (the last
+// component).
+cudaError_t launch_chart(int n, const Mixture* d_mix, const ChartParams& params, int64_t ncell, const double* q,
+                         const int32_t* dep, const ChartOutputs& out, cudaStream_t stream);
+
 // Smallest compiled component capacity >= n (0 if unsupported).
 int capacity_for(int n);
 
@@ -114,6 +137,9 @@ cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const
     cudaError_t launch_max3_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t,      \
                                    const double* z, const DeviceOutputs& out, const Max3Outputs& out3,           \
                                    cudaStream_t stream);                                                          \
+    cudaError_t launch_chart_nm##NM(const Mixture* d_mix, const ChartParams& params, int64_t ncell,           \
+                                    const double* q, const int32_t* dep, const ChartOutputs& out,               \
+                                    cudaStream_t stream);                                                        \
     size_t batched_workspace_bytes_nm##NM(int n, int64_t ncell, bool fp64_items);                             \
     cudaError_t launch_batched_nm##NM(const Mixture* d_mix, int n, int64_t ncell, const double* p,            \
                                       const double* t, const double* z, const DeviceOutputs& out, void* scratch, \

@@ -75,6 +75,53 @@ class _ThreePhaseOutputs(ctypes.Structure):
     _fields_ = [(f, ctypes.c_void_p) for f, _, _ in THREE_PHASE_FIELDS]
 
 
+# selected-phase property chart (mpmc_property_chart_spec / _outputs)
+class _ChartSpec(ctypes.Structure):
+    _fields_ = [("phase_count", ctypes.c_int32), ("root_index", ctypes.c_int32 * 3),
+                ("molar_mass", ctypes.c_void_p), ("viscosity", ctypes.c_void_p), ("enthalpy", ctypes.c_void_p)]
+
+
+class _ChartOutputs(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_void_p), ("values", ctypes.c_void_p), ("jacobian", ctypes.c_void_p)]
+
+
+CHART_STATUS = {0: "ok", 1: "input_domain", 2: "eos_domain", 3: "root_unresolved", 4: "root_index",
+                5: "ill_conditioned_root", 6: "property_domain"}
+CHART_PROPERTIES = ["molar_density", "mass_density", "viscosity", "enthalpy", "internal_energy"]
+
+
+def chart_shape(n: int, phases: int) -> tuple[int, int]:
+    """(rows, columns) of a property chart: P (5 + n) + (P - 1) n output rows
+    and P n + 1 natural variables."""
+    return phases * (5 + n) + (phases - 1) * n, phases * n + 1
+
+
+class PropertyChartSpec:
+    """Closure of a selected-phase property chart (mpmc_property_chart_spec):
+    phase count, selected root index per phase, molar masses [n] in kg/mol and
+    the affine viscosity and enthalpy models [7 + n] each (constant, p, T,
+    molar density, molar mass, mass density, root index, then x_i)."""
+
+    def __init__(self, phases: int, root_index, molar_mass, viscosity, enthalpy):
+        self.phases = int(phases)
+        self.root_index = [int(r) for r in root_index]
+        self.molar_mass = np.ascontiguousarray(molar_mass, dtype=np.float64)
+        self.viscosity = np.ascontiguousarray(viscosity, dtype=np.float64)
+        self.enthalpy = np.ascontiguousarray(enthalpy, dtype=np.float64)
+        if len(self.root_index) != self.phases:
+            raise ValueError("one root index per phase")
+
+    def _struct(self) -> _ChartSpec:
+        s = _ChartSpec()
+        s.phase_count = self.phases
+        for k, r in enumerate(self.root_index):
+            s.root_index[k] = r
+        s.molar_mass = self.molar_mass.ctypes.data
+        s.viscosity = self.viscosity.ctypes.data
+        s.enthalpy = self.enthalpy.ctypes.data
+        return s
+
+
 class _ServerOptions(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("slots", ctypes.c_int32), ("max_batch_cells", ctypes.c_int64),
                 ("memory_budget_bytes", ctypes.c_int64), ("form", ctypes.c_int32), ("flags", ctypes.c_int32)]
@@ -86,7 +133,8 @@ EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu
                     "mpmc_gpu_flash_solve_device_noalloc", "mpmc_flash_server_create", "mpmc_flash_server_add_mixture",
                     "mpmc_flash_server_submit", "mpmc_flash_server_wait", "mpmc_flash_server_stats",
                     "mpmc_flash_server_destroy", "mpmc_gpu_flash_set_launch_shape", "mpmc_gpu_flash_solve_warm",
-                    "mpmc_gpu_flash_solve_device_warm", "mpmc_gpu_flash_solve_max3", "mpmc_gpu_flash_solve_device_max3"]
+                    "mpmc_gpu_flash_solve_device_warm", "mpmc_gpu_flash_solve_max3", "mpmc_gpu_flash_solve_device_max3",
+                    "mpmc_gpu_flash_property_chart", "mpmc_gpu_flash_property_chart_device"]
 FLAG_CUDA_GRAPH = 2
 NOALLOC_SCRATCH_BYTES = 48 << 20
 BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun", "fallback_nonsmooth",
@@ -128,6 +176,11 @@ def library() -> ctypes.CDLL:
             [ctypes.POINTER(_Outputs), ctypes.POINTER(_ThreePhaseOutputs)]
         lib.mpmc_gpu_flash_solve_device_max3.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 3 + \
             [ctypes.POINTER(_Outputs), ctypes.POINTER(_ThreePhaseOutputs), ctypes.c_void_p]
+        lib.mpmc_gpu_flash_property_chart.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(_ChartSpec),
+                                                      ctypes.c_void_p, ctypes.c_void_p,
+                                                      ctypes.POINTER(_ChartOutputs)]
+        lib.mpmc_gpu_flash_property_chart_device.argtypes = lib.mpmc_gpu_flash_property_chart.argtypes + \
+            [ctypes.c_void_p]
         lib.mpmc_gpu_flash_components.argtypes = [ctypes.c_void_p]
         lib.mpmc_gpu_flash_stage_timings.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         lib.mpmc_gpu_flash_batch_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
@@ -241,6 +294,40 @@ class GpuFlash:
                                                    ctypes.byref(s), ctypes.byref(s3)))
         return ({f: (v[0] if rows[f] == 1 else v) for f, v in out.items()},
                 {f: (v[0] if v.shape[0] == 1 else v) for f, v in out3.items()})
+
+    def property_chart(self, spec: PropertyChartSpec, q, dependent=None, jacobian: bool = True) -> dict:
+        """Selected-phase property chart of every cell (mpmc_gpu_flash_property_chart):
+        q [(P n + 1), ncell] natural variables, dependent [P, ncell] pivot
+        components or None (the last component).  Returns status [ncell],
+        values [rows, ncell] and jacobian [rows, q, ncell]."""
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        rows, cols = chart_shape(self.n, spec.phases)
+        if q.ndim != 2 or q.shape[0] != cols:
+            raise ValueError(f"expected q of shape [{cols}, ncell]")
+        ncell = q.shape[1]
+        dep = None
+        if dependent is not None:
+            dep = np.ascontiguousarray(dependent, dtype=np.int32)
+            if dep.shape != (spec.phases, ncell):
+                raise ValueError(f"expected dependent of shape [{spec.phases}, ncell]")
+        out = {"status": np.empty(ncell, np.int32), "values": np.empty((rows, ncell))}
+        if jacobian:
+            out["jacobian"] = np.empty((rows, cols, ncell))
+        o = _ChartOutputs(**{k: v.ctypes.data for k, v in out.items()})
+        st = spec._struct()
+        _check(library().mpmc_gpu_flash_property_chart(self._h, ncell, ctypes.byref(st), q.ctypes.data,
+                                                       dep.ctypes.data if dep is not None else None,
+                                                       ctypes.byref(o)))
+        return out
+
+    def property_chart_device(self, spec: PropertyChartSpec, ncell: int, q_ptr: int, dep_ptr: int,
+                              out_ptrs: dict[str, int], stream: int = 0) -> None:
+        """Device pointers in and out (keys status, values, jacobian; 0 skips);
+        enqueued on `stream` without synchronisation."""
+        o = _ChartOutputs(**out_ptrs)
+        st = spec._struct()
+        _check(library().mpmc_gpu_flash_property_chart_device(self._h, ncell, ctypes.byref(st), q_ptr,
+                                                              dep_ptr or None, ctypes.byref(o), stream))
 
     def solve_host_ptrs(self, ncell: int, p_ptr: int, t_ptr: int, z_ptr: int, out_ptrs: dict[str, int]) -> None:
         """Host-buffer entry with caller-owned (e.g. pinned) host pointers."""

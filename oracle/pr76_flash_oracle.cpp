@@ -1774,9 +1774,14 @@ inline bool solve_continuation(const Model& m, Work& wk, const double* p, const 
 // ---------------------------------------------------------------------------
 // Forward-mode phase evaluation (generic Number), pr76_mixture.hpp:125-219 and
 // pr76_phase.hpp:193-258.  x holds all n fractions already in Number form.
+// Returns 0 or the class of the reference's throw: 2 a range/domain error of
+// the mixing or the coefficients, 3 an unresolved root set (Pr76PhaseError),
+// 4 a root index out of range, 5 a root without a reliable derivative, 2 a
+// non-representable ln phi or Z (the codes of the selected-phase chart).
+enum EvalIssue { kEvalOk = 0, kEvalDomain = 2, kEvalRootSet = 3, kEvalRootIndex = 4, kEvalIllConditioned = 5 };
 template <class Num>
-inline bool phase_eval_ad(const Model& m, const Num& p, const Num& t, const std::vector<Num>& x,
-                          int root_index, Num& z_out, std::vector<Num>& ln_phi) {
+inline int phase_eval_status(const Model& m, const Num& p, const Num& t, const std::vector<Num>& x,
+                             int root_index, Num& z_out, std::vector<Num>& ln_phi) {
     const int n = m.n;
     std::vector<Num> a(n), root(n), sums(n);
     Num attraction(0.0), covolume(0.0);
@@ -1787,7 +1792,10 @@ inline bool phase_eval_ad(const Model& m, const Num& p, const Num& t, const std:
         attraction = attraction + (x[i] * a[i]) * x[i];
         covolume = covolume + x[i] * m.b[i];
         sums[i] = x[i] * a[i];
-        if (n > 1) root[i] = sqrt(a[i]);
+        if (n > 1) {
+            if (!(val(a[i]) > 0.0)) return kEvalDomain;  // pr76_mixture.hpp:180-182
+            root[i] = sqrt(a[i]);
+        }
     }
     for (int i = 0; i < n; ++i)
         for (int j = i + 1; j < n; ++j) {
@@ -1798,18 +1806,22 @@ inline bool phase_eval_ad(const Model& m, const Num& p, const Num& t, const std:
             sums[i] = sums[i] + x[j] * aij;
             sums[j] = sums[j] + x[i] * aij;
         }
+    if (!finite(attraction) || !finite(covolume) || !(val(covolume) > 0.0)) return kEvalDomain;
     const Num rt = kR * t;
     const Num prt = p / rt;
     const Num A = (attraction / rt) * prt;
     const Num B = covolume * prt;
+    if (!finite(A) || !finite(B) || !(val(B) > 0.0) || (val(A) == 0.0 && val(attraction) != 0.0))
+        return kEvalDomain;  // pr76_phase.hpp:175-191
     const RootSet roots = solve_roots(val(A), val(B));
-    if (roots.status != kRootSuccess || root_index >= roots.count) return false;
+    if (roots.status != kRootSuccess) return kEvalRootSet;
+    if (root_index < 0 || root_index >= roots.count) return kEvalRootIndex;
     const Root& rootv = roots.roots[root_index];
     Num free_volume(rootv.free_volume);
     {
         // First-order implicit function theorem on the scaled cubic,
         // pr76_phase.hpp:208-222.
-        if (!rootv.derivative_valid) return false;
+        if (!rootv.derivative_valid) return kEvalIllConditioned;
         const double y0 = rootv.free_volume / roots.scale;
         const double scale = roots.scale;
         const Num bs = B / scale;
@@ -1838,10 +1850,16 @@ inline bool phase_eval_ad(const Model& m, const Num& p, const Num& t, const std:
         const Num ratio = Num(m.b[i]) / covolume;
         const Num coefficient = ((2.0 * sums[i] - attraction * ratio) / rt) * prt;
         ln_phi[i] = ratio * z_minus_one - log_free - coefficient * log_factor;
-        if (!finite(ln_phi[i])) return false;
+        if (!finite(ln_phi[i])) return kEvalDomain;
     }
     z_out = z;
-    return finite(z);
+    return finite(z) ? kEvalOk : kEvalDomain;
+}
+
+template <class Num>
+inline bool phase_eval_ad(const Model& m, const Num& p, const Num& t, const std::vector<Num>& x,
+                          int root_index, Num& z_out, std::vector<Num>& ln_phi) {
+    return phase_eval_status(m, p, t, x, root_index, z_out, ln_phi) == kEvalOk;
 }
 
 // Sensitivity outputs (reduced chart q = p, T, z_0..z_{n-2}).
@@ -2301,6 +2319,108 @@ inline bool polish(const Model& m, Work& wk, double p, double t, const std::vect
     return true;
 }
 
+// ---------------------------------------------------------------------------
+// Selected-phase property chart, evaluate_pr76_selected_phase_property_chart
+// (modules/flow/include/mpmc/flow/pr76_selected_phase_property_closure.hpp:533-822)
+// over Pr76SelectedPhasePropertyClosure::evaluate (:338-469), by forward mode
+// with one chart column per pass (the reference runs four per pass; the
+// first-order arithmetic per column is the same).  The closure's
+// transport/caloric provider is the affine model of the C ABI:
+//   f = c[0] + c[1] p + c[2] T + sum_i c[7+i] x_i + c[3] rho + c[4] M + c[5] rho_mass + c[6] root_index.
+// Statuses: 0 ok, 1 chart input (non-finite entry, fractions, p, T, M),
+// 2..5 the EOS classes of phase_eval_status, 6 a property check.
+struct ChartSpec {
+    int phases = 1;
+    int root_index[3] = {0, 0, 0};
+    std::vector<double> molar_mass, visc, enth;
+};
+
+template <class Num>
+inline Num affine_model(const std::vector<double>& c, const Num& p, const Num& t, const std::vector<Num>& x,
+                        const Num& rho, const Num& mm, const Num& rhom, int root) {
+    Num f = Num(c[0]) + c[1] * p + c[2] * t;
+    for (size_t i = 0; i < x.size(); ++i) f = f + c[7 + i] * x[i];
+    return f + c[3] * rho + c[4] * mm + c[5] * rhom + c[6] * static_cast<double>(root);
+}
+
+inline int property_chart(const Model& m, const ChartSpec& spec, const double* qv, const int* dep, double* values,
+                          double* jac) {
+    const int n = m.n, P = spec.phases;
+    const int q = P * n + 1;
+    const int prop = P * (5 + n);
+    const int rows = prop + (P - 1) * n;
+    for (int k = 0; k < q; ++k)
+        if (!std::isfinite(qv[k])) return 1;  // ad/runtime_differentiate.hpp:105-108
+    for (int col = 0; col < q; ++col) {
+        auto seed = [&](int k) { return D1(qv[k], k == col ? 1.0 : 0.0); };
+        const D1 p = seed(0), t = seed(1);
+        std::vector<std::vector<D1>> x(P, std::vector<D1>(n));
+        std::vector<std::vector<D1>> lnphi(P);
+        std::vector<D1> out(rows);
+        for (int ph = 0; ph < P; ++ph) {
+            // reconstruct_composition, :115-157
+            const int d = dep[ph];
+            if (d < 0 || d >= n) return 1;
+            const int start = 2 + (P - 1) + ph * (n - 1);
+            D1 sum(0.0);
+            for (int i = 0; i < n; ++i) {
+                if (i == d) continue;
+                x[ph][i] = seed(start + (i < d ? i : i - 1));
+                if (!(x[ph][i].v > 0.0)) return 1;
+                sum = sum + x[ph][i];
+            }
+            x[ph][d] = 1.0 - sum;
+            if (!std::isfinite(x[ph][d].v) || !(x[ph][d].v > 0.0)) return 1;
+            // closure evaluate, :339-469
+            if (!(p.v > 0.0) || !(t.v > 0.0)) return 1;
+            D1 mm(0.0);
+            for (int i = 0; i < n; ++i) mm = mm + x[ph][i] * spec.molar_mass[i];
+            if (!std::isfinite(mm.v) || !(mm.v > 0.0)) return 1;
+            // Pr76Mixture fraction checks, pr76_mixture.hpp:146-158 and :221-227
+            long double xs = 0, xc = 0;
+            for (int i = 0; i < n; ++i) {
+                if (x[ph][i].v > 1.0) return 2;
+                const long double inc = x[ph][i].v - xc;
+                const long double next = xs + inc;
+                xc = (next - xs) - inc;
+                xs = next;
+            }
+            if (std::abs(xs - 1.0L) > static_cast<long double>(64.0 * kEps)) return 2;
+            D1 z;
+            const int ri = spec.root_index[ph];
+            const int st = phase_eval_status(m, p, t, x[ph], ri, z, lnphi[ph]);
+            if (st != kEvalOk) return st;
+            const D1 rho = p / ((z * kR) * t);  // selected_phase_density.hpp:27-34
+            const D1 rhom = rho * mm;
+            if (!std::isfinite(rho.v) || !(rho.v > 0.0) || !std::isfinite(rhom.v) || !(rhom.v > 0.0)) return 6;
+            const D1 mu = affine_model(spec.visc, p, t, x[ph], rho, mm, rhom, ri);
+            const D1 h = affine_model(spec.enth, p, t, x[ph], rho, mm, rhom, ri);
+            if (!std::isfinite(mu.v) || !(mu.v > 0.0) || !std::isfinite(h.v)) return 6;
+            const D1 u = h - p / rhom;
+            if (!std::isfinite(u.v)) return 6;
+            const int base = ph * (5 + n);
+            out[base + 0] = rho;
+            out[base + 1] = rhom;
+            out[base + 2] = mu;
+            out[base + 3] = h;
+            out[base + 4] = u;
+            for (int i = 0; i < n; ++i) out[base + 5 + i] = lnphi[ph][i];
+        }
+        // equilibrium rows, :660-681
+        for (int ph = 1; ph < P; ++ph)
+            for (int i = 0; i < n; ++i)
+                out[prop + (ph - 1) * n + i] =
+                    (log(x[0][i] / x[ph][i]) + lnphi[0][i]) - lnphi[ph][i] + log(p / p);
+        // the driver's output checks, runtime_differentiate.hpp:138-156
+        for (int r = 0; r < rows; ++r) {
+            if (!finite(out[r])) return 6;
+            if (col == 0 && values) values[r] = out[r].v;
+            if (jac) jac[static_cast<size_t>(r) * q + col] = out[r].d;
+        }
+    }
+    return 0;
+}
+
 }  // namespace oracle
 
 // ===========================================================================
@@ -2455,6 +2575,56 @@ struct Max3Outputs {
     double* y;       // [n]
     int32_t* attempts;
 };
+
+// Selected-phase property chart of `ncell` cells (oracle::property_chart).
+// q [(P n + 1) * ncell] and dep [P * ncell] (null = the last component) in
+// the cell-fastest layout; writes status [ncell], values [rows * ncell] and
+// jac [rows * q * ncell] (element (r, col) of cell c at (r * q + col) * ncell
+// + c), NaN for a failed cell.
+int oracle_property_chart_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                                int phases, const int* root_index, const double* molar_mass, const double* visc,
+                                const double* enth, int64_t ncell, const double* q, const int* dep, int threads,
+                                int* status, double* values, double* jac) {
+    if (phases < 1 || phases > 3 || n < 2) return 1;
+    const oracle::Model m = oracle::make_model(n, tc, pc, omega, kij);
+    oracle::ChartSpec spec;
+    spec.phases = phases;
+    for (int k = 0; k < phases; ++k) spec.root_index[k] = root_index[k];
+    spec.molar_mass.assign(molar_mass, molar_mass + n);
+    spec.visc.assign(visc, visc + 7 + n);
+    spec.enth.assign(enth, enth + 7 + n);
+    const int cols = phases * n + 1;
+    const int rows = phases * (5 + n) + (phases - 1) * n;
+    auto run = [&](int64_t lo, int64_t hi) {
+        std::vector<double> qc(cols), v(rows), j(static_cast<size_t>(rows) * cols);
+        int dc[3];
+        for (int64_t c = lo; c < hi; ++c) {
+            for (int k = 0; k < cols; ++k) qc[k] = q[k * ncell + c];
+            for (int k = 0; k < phases; ++k) dc[k] = dep ? dep[k * ncell + c] : n - 1;
+            const int st = oracle::property_chart(m, spec, qc.data(), dc, v.data(), j.data());
+            if (status) status[c] = st;
+            for (int r = 0; r < rows; ++r) {
+                if (values) values[r * ncell + c] = st == 0 ? v[r] : oracle::kNaN;
+                if (jac)
+                    for (int k = 0; k < cols; ++k)
+                        jac[(static_cast<int64_t>(r) * cols + k) * ncell + c] =
+                            st == 0 ? j[static_cast<size_t>(r) * cols + k] : oracle::kNaN;
+            }
+        }
+    };
+    if (threads <= 1 || ncell < 64) {
+        run(0, ncell);
+        return 0;
+    }
+    std::vector<std::thread> pool;
+    const int64_t per = (ncell + threads - 1) / threads;
+    for (int w = 0; w < threads; ++w) {
+        const int64_t lo = w * per, hi = std::min<int64_t>(ncell, lo + per);
+        if (lo < hi) pool.emplace_back(run, lo, hi);
+    }
+    for (auto& th : pool) th.join();
+    return 0;
+}
 
 int oracle_max3_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
                       int64_t ncell, const double* p, const double* t, const double* z, int threads,

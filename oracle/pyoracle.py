@@ -38,12 +38,19 @@ class _Out(ctypes.Structure):
     _fields_ = FIELDS
 
 
+_built = False
+
+
 def build(force: bool = False) -> None:
-    """Compile the oracle (always) and the reference harness (if sources exist)."""
-    if force or not os.path.exists(ORACLE_SO):
-        subprocess.check_call(["make", "-s", "-C", HERE, "all"])
-    if os.path.isdir("/root/reference/modules") and (force or not os.path.exists(REF_SO)):
+    """Compile the oracle (always) and the reference harness (if sources
+    exist); make rebuilds whatever is older than its source."""
+    global _built
+    if _built and not force:
+        return
+    subprocess.check_call(["make", "-s", "-C", HERE, "all"])
+    if os.path.isdir("/root/reference/modules"):
         subprocess.check_call(["make", "-s", "-C", HERE, "ref"])
+    _built = True
 
 
 _libs: dict[str, ctypes.CDLL] = {}
@@ -56,6 +63,7 @@ def _lib(path: str) -> ctypes.CDLL:
 
 
 def reference_available() -> bool:
+    build()
     return os.path.exists(REF_SO)
 
 
@@ -262,3 +270,53 @@ def continuation(mix, pressures, temperatures, z, threads: int = 8):
        ctypes.c_int64(npoint), *[ctypes.c_void_p(a.ctypes.data) for a in (p, t, z)], ctypes.c_int(threads),
        ctypes.c_void_p(ms.ctypes.data))
     return ms
+
+
+def _property_chart(fn_name: str, so: str, mix, phases: int, root_index, molar_mass, viscosity, enthalpy, q,
+                    dependent=None, threads: int = 8):
+    tc, pc, omega, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
+    n = len(tc)
+    q = np.ascontiguousarray(q, dtype=np.float64)
+    cols, ncell = q.shape
+    if cols != phases * n + 1:
+        raise ValueError(f"expected {phases * n + 1} chart rows, got {cols}")
+    rows = phases * (5 + n) + (phases - 1) * n
+    ri = np.zeros(3, np.int32)
+    ri[:phases] = root_index
+    mm = np.ascontiguousarray(molar_mass, dtype=np.float64)
+    cv = np.ascontiguousarray(viscosity, dtype=np.float64)
+    ce = np.ascontiguousarray(enthalpy, dtype=np.float64)
+    dep = None if dependent is None else np.ascontiguousarray(dependent, dtype=np.int32)
+    status = np.full(ncell, -9, np.int32)
+    values = np.empty((rows, ncell))
+    jac = np.empty((rows * cols, ncell))
+    fn = getattr(_lib(so), fn_name)
+    fn.restype = ctypes.c_int
+    fn(ctypes.c_int(n), *[ctypes.c_void_p(a.ctypes.data) for a in (tc, pc, omega, kij)], ctypes.c_int(phases),
+       ctypes.c_void_p(ri.ctypes.data), *[ctypes.c_void_p(a.ctypes.data) for a in (mm, cv, ce)],
+       ctypes.c_int64(ncell), ctypes.c_void_p(q.ctypes.data),
+       ctypes.c_void_p(dep.ctypes.data) if dep is not None else ctypes.c_void_p(None), ctypes.c_int(threads),
+       *[ctypes.c_void_p(a.ctypes.data) for a in (status, values, jac)])
+    return {"status": status, "values": values, "jacobian": jac.reshape(rows, cols, ncell)}
+
+
+def property_chart(mix, phases: int, root_index, molar_mass, viscosity, enthalpy, q, dependent=None,
+                   threads: int = 8):
+    """The oracle's restatement of evaluate_pr76_selected_phase_property_chart
+    with the affine transport/caloric model: q [(P n + 1), ncell] chart
+    values, dependent [P, ncell] or None (last component).  Returns status
+    [ncell] (mpmc_chart_status codes), values [rows, ncell] and jacobian
+    [rows, q, ncell]."""
+    build()
+    return _property_chart("oracle_property_chart_batch", ORACLE_SO, mix, phases, root_index, molar_mass,
+                           viscosity, enthalpy, q, dependent, threads)
+
+
+def reference_property_chart(mix, phases: int, root_index, molar_mass, viscosity, enthalpy, q, dependent=None,
+                             threads: int = 8):
+    """The reference's evaluate_pr76_selected_phase_property_chart through
+    oracle/_ref (status 7 = an unexpected exception)."""
+    if not reference_available():
+        raise FileNotFoundError(REF_SO)
+    return _property_chart("ref_property_chart_batch", REF_SO, mix, phases, root_index, molar_mass, viscosity,
+                           enthalpy, q, dependent, threads)

@@ -14,11 +14,14 @@
 //   mpmc::flash::Pr76PtFlashBackend::solve         modules/flash/include/mpmc/flash/pr76_pt_flash_backend.hpp:190
 //   mpmc::flash::solve_pr76_pt_max3                modules/flash/include/mpmc/flash/pr76_three_phase.hpp:328
 //   mpmc::flash::solve_pr76_pt_continuation        modules/flash/include/mpmc/flash/pr76_pt_continuation.hpp:183
+//   mpmc::flow::evaluate_pr76_selected_phase_property_chart
+//                                                  modules/flow/include/mpmc/flow/pr76_selected_phase_property_closure.hpp:533
 
 #include <mpmc/flash/pr76_pt_flash_backend.hpp>
 #include <mpmc/flash/pr76_three_phase.hpp>
 #include <mpmc/flash/pr76_pt_continuation.hpp>
 #include <mpmc/flash/pr76_sensitivity.hpp>
+#include <mpmc/flow/pr76_selected_phase_property_closure.hpp>
 #include <mpmc/physics/pr76_thermodynamic_closure.hpp>
 #include <mpmc/thermodynamics/pr76_phase_ad.hpp>
 
@@ -47,7 +50,8 @@ th::Provenance synthetic_source() {
 }
 
 th::PrParameterSet make_parameters(int n, const double* tc, const double* pc, const double* omega,
-                                   const double* kij, std::vector<std::string>& order) {
+                                   const double* kij, std::vector<std::string>& order,
+                                   const double* molar_mass = nullptr) {
     const auto src = synthetic_source();
     std::vector<th::Component> catalog;
     th::PrParameterInput input;
@@ -59,7 +63,9 @@ th::PrParameterSet make_parameters(int n, const double* tc, const double* pc, co
     for (int i = 0; i < n; ++i) {
         const std::string id = "c" + std::to_string(i);
         order.push_back(id);
-        catalog.push_back({id, id, th::ComponentKind::pure, src, {}});
+        std::optional<th::SourcedScalar> mw;
+        if (molar_mass) mw = th::SourcedScalar{molar_mass[i], th::Unit::kilogram_per_mole, src, "kg/mol", "identity"};
+        catalog.push_back({id, id, th::ComponentKind::pure, src, std::move(mw)});
         input.pure.push_back({id, th::SourcedScalar{tc[i], th::Unit::kelvin, src, "K", "identity"},
                               th::SourcedScalar{pc[i], th::Unit::pascal, src, "Pa", "identity"},
                               th::SourcedScalar{omega[i], th::Unit::dimensionless, src, "1", "identity"}});
@@ -429,6 +435,128 @@ int ref_continuation_batch(int n, const double* tc, const double* pc, const doub
     const int64_t chunk = (npath + threads - 1) / threads;
     for (int k = 0; k < threads; ++k) {
         const int64_t lo = k * chunk, hi = std::min<int64_t>(npath, lo + chunk);
+        if (lo < hi) pool.emplace_back(run, lo, hi);
+    }
+    for (auto& th : pool) th.join();
+    return 0;
+}
+
+// The reference's selected-phase property chart of `ncell` cells with the
+// affine transport/caloric provider of the C ABI (the same arithmetic order as
+// oracle::affine_model).  Layouts and status codes as
+// oracle_property_chart_batch; 7 = an unexpected exception.
+int ref_property_chart_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                             int phases, const int* root_index, const double* molar_mass, const double* visc,
+                             const double* enth, int64_t ncell, const double* q, const int* dep, int threads,
+                             int* status, double* values, double* jac) {
+    namespace fw = mpmc::flow;
+    std::vector<std::string> order;
+    const th::PrParameterSet params = make_parameters(n, tc, pc, omega, kij, order, molar_mass);
+    const auto model = th::Pr76Phase<double>::from_parameters(params);
+    const std::vector<double> cv(visc, visc + 7 + n), ce(enth, enth + 7 + n);
+    const auto provider = [cv, ce](const th::Pr76SelectedPhase& selection, const auto& p, const auto& t,
+                                   auto x, const auto& mm, const auto& rho, const auto& rhom) {
+        using Number = std::decay_t<decltype(p)>;
+        auto affine = [&](const std::vector<double>& c) {
+            Number f = Number{c[0]} + p * c[1] + t * c[2];
+            for (size_t i = 0; i < x.size(); ++i) f += x[i] * c[7 + i];
+            return f + rho * c[3] + mm * c[4] + rhom * c[5] + Number{c[6] * static_cast<double>(selection.root_index)};
+        };
+        return fw::SelectedPhaseTransportCaloricValues<Number>{affine(cv), affine(ce)};
+    };
+    std::vector<th::Pr76SelectedPhase> selections;
+    for (int k = 0; k < phases; ++k) selections.push_back({static_cast<std::size_t>(root_index[k]), {}});
+    const fw::SelectedPhasePropertyProvenance provenance{{"affine test model", "mpmc-gb300-synthetic", "v1"},
+                                                         {"affine test model", "mpmc-gb300-synthetic", "v1"},
+                                                         {"affine test model", "mpmc-gb300-synthetic", "v1"},
+                                                         {"u = h - p/rho_mass", "mpmc-gb300-synthetic", "v1"}};
+    const auto closure = fw::make_pr76_selected_phase_property_closure(model, selections, provider, provenance);
+    const int cols = phases * n + 1;
+    const int rows = phases * (5 + n) + (phases - 1) * n;
+    const double nan = std::numeric_limits<double>::quiet_NaN();
+    auto classify = [](const std::exception& e) {
+        const std::string what = e.what();
+        auto has = [&](const char* s) { return what.find(s) != std::string::npos; };
+        if (has("mpmc::ad::runtime: nonfinite input")) return 1;
+        if (has("mpmc::ad::runtime:")) return 6;
+        if (has("mpmc::flow: PR76 selected-phase")) {
+            if (has("composition") || has("pressure [Pa]") || has("temperature [K]") || has("molar mass"))
+                return 1;
+            return 6;
+        }
+        return 2;
+    };
+    auto run = [&](int64_t lo, int64_t hi) {
+        mpmc::ad::RuntimeJacobianWorkspace<double, 4U> workspace;
+        std::vector<double> qc(cols);
+        for (int64_t c = lo; c < hi; ++c) {
+            for (int k = 0; k < cols; ++k) qc[k] = q[k * ncell + c];
+            std::vector<std::size_t> pivots(phases);
+            for (int k = 0; k < phases; ++k) pivots[k] = dep ? static_cast<std::size_t>(dep[k * ncell + c]) : n - 1;
+            int st = 0;
+            try {
+                const fw::NaturalVariableLayoutDescriptor layout(static_cast<std::size_t>(n),
+                                                                 static_cast<std::size_t>(phases), pivots);
+                const auto r = fw::evaluate_pr76_selected_phase_property_chart(layout, closure.component_ids(), qc,
+                                                                               closure, workspace);
+                for (int ph = 0; ph < phases; ++ph) {
+                    const int base = ph * (5 + n);
+                    const auto& pp = r.phase_properties[ph];
+                    const double v5[5] = {pp.molar_density_mol_per_m3, pp.mass_density_kg_per_m3,
+                                          pp.dynamic_viscosity_pa_s, pp.specific_enthalpy_j_per_kg,
+                                          pp.specific_internal_energy_j_per_kg};
+                    const std::vector<double>* g5[5] = {&r.molar_density_gradient[ph], &r.mass_density_gradient[ph],
+                                                        &r.viscosity_gradient[ph], &r.enthalpy_gradient[ph],
+                                                        &r.internal_energy_gradient[ph]};
+                    for (int k = 0; k < 5; ++k) {
+                        if (values) values[(base + k) * ncell + c] = v5[k];
+                        if (jac)
+                            for (int col = 0; col < cols; ++col)
+                                jac[(static_cast<int64_t>(base + k) * cols + col) * ncell + c] = (*g5[k])[col];
+                    }
+                    for (int i = 0; i < n; ++i) {
+                        if (values) values[(base + 5 + i) * ncell + c] = r.ln_phi[ph][i];
+                        if (jac)
+                            for (int col = 0; col < cols; ++col)
+                                jac[(static_cast<int64_t>(base + 5 + i) * cols + col) * ncell + c] =
+                                    r.ln_phi_jacobian[ph][static_cast<size_t>(i) * cols + col];
+                    }
+                }
+                const int prop = phases * (5 + n);
+                for (int e = 0; e < (phases - 1) * n; ++e) {
+                    if (values) values[(prop + e) * ncell + c] = r.equilibrium_residual[e];
+                    if (jac)
+                        for (int col = 0; col < cols; ++col)
+                            jac[(static_cast<int64_t>(prop + e) * cols + col) * ncell + c] =
+                                r.equilibrium_jacobian[static_cast<size_t>(e) * cols + col];
+                }
+            } catch (const th::Pr76PhaseError& e) {
+                st = e.code() == th::Pr76PhaseErrorCode::ill_conditioned_derivative ? 5 : 3;
+            } catch (const std::out_of_range&) {
+                st = 4;
+            } catch (const std::range_error& e) {
+                st = classify(e);
+            } catch (const std::domain_error& e) {
+                st = classify(e);
+            } catch (const std::invalid_argument& e) {
+                st = classify(e);
+            } catch (const std::exception&) {
+                st = 7;
+            }
+            if (status) status[c] = st;
+            if (st != 0)
+                for (int r = 0; r < rows; ++r) {
+                    if (values) values[r * ncell + c] = nan;
+                    if (jac)
+                        for (int col = 0; col < cols; ++col) jac[(static_cast<int64_t>(r) * cols + col) * ncell + c] = nan;
+                }
+        }
+    };
+    if (threads < 1) threads = 1;
+    std::vector<std::thread> pool;
+    const int64_t chunk = (ncell + threads - 1) / threads;
+    for (int k = 0; k < threads; ++k) {
+        const int64_t lo = k * chunk, hi = std::min<int64_t>(ncell, lo + chunk);
         if (lo < hi) pool.emplace_back(run, lo, hi);
     }
     for (auto& th : pool) th.join();

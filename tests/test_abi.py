@@ -88,3 +88,18 @@ def test_null_arguments_of_the_warm_and_max3_entries(lib):
     assert lib.mpmc_gpu_flash_solve_max3(None, 1, None, None, None, None, None) == 1
     assert lib.mpmc_gpu_flash_solve_device_max3(None, 1, None, None, None, None, None, None) == 1
     assert b"null handle" in lib.mpmc_gpu_flash_last_error()
+
+
+def test_null_arguments_of_the_property_chart_entries(lib):
+    """The property-chart entries validate before any device work."""
+    assert lib.mpmc_gpu_flash_property_chart(None, 1, None, None, None, None) == 1
+    assert lib.mpmc_gpu_flash_property_chart_device(None, 1, None, None, None, None, None) == 1
+    assert b"null handle" in lib.mpmc_gpu_flash_last_error()
+
+
+def test_chart_shape():
+    from mpmc_hnu_gb300 import flash
+
+    assert flash.chart_shape(10, 1) == (15, 11)
+    assert flash.chart_shape(10, 2) == (40, 21)
+    assert flash.chart_shape(3, 3) == (30, 10)
