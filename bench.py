@@ -236,6 +236,85 @@ def cpu_flash_rate(mix, p, t, z, threads: int, sens: bool):
 
 
 # ---------------------------------------------------------------------------
+# selected-phase property chart (the flow module's per-cell property and
+# Jacobian publication, mpmc_gpu_flash_property_chart)
+CHART_N, CHART_PHASES = 10, 2
+
+
+def chart_states(n: int, phases: int, ncell: int, seed: int):
+    """Two-phase chart states: p log-uniform on [0.5, 40] MPa, T ~ U[280, 450] K,
+    a saturation ~ U[0.05, 0.95], each phase's composition ~ Dirichlet(1) with
+    the last component as the pivot (rows [P n + 1, ncell])."""
+    rng = np.random.default_rng(seed)
+    p = np.exp(rng.uniform(np.log(5.0e5), np.log(4.0e7), ncell))
+    t = rng.uniform(280.0, 450.0, ncell)
+    sat = rng.uniform(0.05, 0.95, (phases - 1, ncell))
+    blocks = [rng.dirichlet(np.ones(n), ncell).T[:n - 1] for _ in range(phases)]
+    return np.ascontiguousarray(np.vstack([p[None], t[None], sat] + blocks))
+
+
+def chart_leg(flash, synth, torch, device: int, stream, ncell: int, threads: int, cpu_sample: int, peaks):
+    """Device-resident chart of `ncell` two-phase cells at 10 components (roots
+    0 and 0, affine viscosity/enthalpy model): cells/s over 5 launches timed
+    with CUDA events on the launching stream, the algorithmic bytes per cell
+    (chart read, status, values and Jacobian written) against the measured
+    copy bandwidth, and the CPU oracle on a sample of the same cells."""
+    n, phases = CHART_N, CHART_PHASES
+    rows, cols = flash.chart_shape(n, phases)
+    mix = synth.make_mixture(n, 1001)
+    rng = np.random.default_rng(33)
+    visc = np.concatenate([[8.0e-6, 1.0e-12, 1.0e-8, 1.0e-12, 1.0e-4, 1.0e-9, 1.0e-7], rng.uniform(0, 1e-6, n)])
+    enth = np.concatenate([[0.0, 2.0e-4, 1200.0, 0.5, 1.0e4, 0.1, 10.0], rng.uniform(0, 2000.0, n)])
+    spec = flash.PropertyChartSpec(phases, [0, 0], rng.uniform(0.016, 0.2, n), visc, enth)
+    q = chart_states(n, phases, ncell, 34)
+    dev = torch.device(f"cuda:{device}")
+    dq = torch.from_numpy(q).to(dev)
+    st = torch.empty(ncell, dtype=torch.int32, device=dev)
+    vals = torch.empty((rows, ncell), dtype=torch.float64, device=dev)
+    jac = torch.empty((rows, cols, ncell), dtype=torch.float64, device=dev)
+    ptrs = {"status": st.data_ptr(), "values": vals.data_ptr(), "jacobian": jac.data_ptr()}
+    g = flash.GpuFlash(mix, "plain", device=device)
+    stream.wait_stream(torch.cuda.current_stream(dev))
+    for _ in range(2):
+        g.property_chart_device(spec, ncell, dq.data_ptr(), 0, ptrs, stream.cuda_stream)
+    torch.cuda.synchronize()
+    launches = 5
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(launches):
+        g.property_chart_device(spec, ncell, dq.data_ptr(), 0, ptrs, stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    g.close()
+    ms = e0.elapsed_time(e1) / launches
+    status = st.cpu().numpy()
+    bytes_per_cell = cols * 8 + 4 + rows * 8 + rows * cols * 8
+    achieved = bytes_per_cell * ncell / (ms * 1e-3) / 1e9
+    leg = {"value": ncell / (ms * 1e-3), "unit": "cells/s", "cells": ncell, "ms_per_launch": ms,
+           "components": n, "phases": phases,
+           "statuses": {str(k): int(v) for k, v in enumerate(np.bincount(status, minlength=7)) if v},
+           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks, "unit": "GB/s",
+                        "frac": achieved / peaks if peaks else None, "bytes_per_cell": bytes_per_cell,
+                        "peak_source": "hbm_gbs of MEASURED_PEAKS.json (measured copy bandwidth)"},
+           "dtype": "f64", "l2_flush": f"outputs {bytes_per_cell * ncell / 1e9:.1f} GB per launch, far above L2"}
+    del dq, vals, jac
+    if cpu_sample > 0:
+        from oracle import pyoracle
+
+        sel = q[:, :: max(1, ncell // cpu_sample)][:, :cpu_sample]
+        sel = np.ascontiguousarray(sel)
+        pyoracle.build()
+        t0 = time.perf_counter()
+        pyoracle.property_chart(mix, phases, [0, 0], spec.molar_mass, visc, enth, sel, None, threads=threads)
+        dt = time.perf_counter() - t0
+        leg["cpu_baseline"] = {"value": sel.shape[1] / dt, "unit": "cells/s", "cores": threads, "kind": "reference",
+                               "sample": f"{sel.shape[1]} of the same cells (every {ncell // sel.shape[1]}th), "
+                                         f"{dt:.1f} s wall; the oracle is bit-identical to the reference's chart"}
+    return leg
+
+
+# ---------------------------------------------------------------------------
 # ---------------------------------------------------------------------------
 # serving (continuous batching through the flash server)
 SERVING_MIXTURES = [(3, 501), (3, 502), (6, 503), (6, 504), (10, 505), (10, 506), (20, 507), (20, 508)]
@@ -412,6 +491,8 @@ def main() -> None:
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--launch-shape", default="",
                     help="comma-separated mixed-form launch shape to use instead of autotuning")
+    ap.add_argument("--chart-cells", type=int, default=1 << 20,
+                    help="cells of the selected-phase property chart leg (0 = skip)")
     ap.add_argument("--serving-sweep", action="store_true",
                     help="only the serving sweep: 10%%..100%% of saturation, --serving-seconds per rate")
     args = ap.parse_args()
@@ -684,6 +765,17 @@ def main() -> None:
         g.close()
         serving = serving_probe(flash, synth, device, args.serving_seconds, [0.7], log)
 
+    # the property chart runs last: a failure there leaves the flash line intact
+    chart = None
+    if rank == 0 and args.chart_cells > 0:
+        try:
+            peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+            hbm = json.load(open(peaks_path)).get("hbm_gbs") if os.path.exists(peaks_path) else None
+            chart = chart_leg(flash, synth, torch, device, stream, args.chart_cells, threads,
+                              min(args.cpu_sample, 65536), hbm)
+        except Exception as e:  # noqa: BLE001 - reported in the line
+            chart = {"error": f"{type(e).__name__}: {e}"}
+
     if rank == 0:
         line = {"metric": METRIC, "value": value,
                 "unit": "flashes/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -692,7 +784,7 @@ def main() -> None:
                 "data": f"synthetic (seeded generator; {placed} near-boundary cells placed by GPU bisection)",
                 "config": workload, "e2e": e2e, "gpu_launches": len(stages) * args.steps,
                 "roofline": roofline, "cpu_baseline": cpu, "plain_fp64": plain, "batched_fp64": batched,
-                "warm_start": warm_leg,
+                "warm_start": warm_leg, "property_chart": chart,
                 "phase_counts": {"single": int((status == 0).sum()), "two": int((status == 1).sum()),
                                  "unstable": int((status == 2).sum()), "indeterminate": int((status == 3).sum()),
                                  "invalid": int((status == -1).sum())},

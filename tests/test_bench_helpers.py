@@ -45,3 +45,23 @@ def test_rank_offsets_are_disjoint_and_reduction_is_identity_on_one_rank():
     for a, b in zip(spans, spans[1:]):
         assert a[1] <= b[0]
     assert bench.max_over_ranks(3.5, 1, "cpu") == 3.5
+
+
+def test_chart_states_are_valid_two_phase_charts(oracle_lib):
+    """The chart leg's states: [P n + 1, ncell], positive fractions whose
+    dependent (last) one stays positive; the oracle evaluates them."""
+    import numpy as np
+
+    import bench
+    from mpmc_hnu_gb300 import synth
+
+    n, phases = bench.CHART_N, bench.CHART_PHASES
+    q = bench.chart_states(n, phases, 500, 34)
+    assert q.shape == (phases * n + 1, 500)
+    for ph in range(phases):
+        block = q[phases + 1 + ph * (n - 1):phases + 1 + (ph + 1) * (n - 1)]
+        assert (block > 0).all() and (block.sum(axis=0) < 1).all()
+    visc = np.concatenate([[8.0e-6, 1e-12, 1e-8, 1e-12, 1e-4, 1e-9, 1e-7], np.full(n, 1e-7)])
+    enth = np.concatenate([[0.0, 2e-4, 1200.0, 0.5, 1e4, 0.1, 10.0], np.full(n, 100.0)])
+    out = oracle_lib.property_chart(synth.make_mixture(n, 1001), phases, [0, 0], np.full(n, 0.05), visc, enth, q)
+    assert (out["status"] == 0).mean() > 0.99
