@@ -13,9 +13,14 @@
 // two-phase flash and, where the pair fails its final review, the
 // max-3-phase continuation (mpmc_gpu_flash_solve_max3), so phase counts
 // {1, 2, 3} are published as project_max3_solution does
-// (pt_phase_set.hpp:91-150).  Not carried: caller start hints
-// (three_phase_starts, initial/final starts), the transition report and the
-// phase metadata.
+// (pt_phase_set.hpp:91-150).  The transition report carries the evidence
+// project_pr76_pt_max3_transition_report (pr76_pt_flash_backend.hpp:94-175)
+// gives every accepted, phase-set-unstable and boundary-unresolved result,
+// which is what the flow module's transition candidates need
+// (phase_set_transition_flash_adapter.hpp:130-248); an indeterminate result
+// from an unresolved two-phase or three-phase search carries none, since the
+// C ABI does not return the attempts behind it.  Not carried: caller start
+// hints (three_phase_starts, initial/final starts) and the phase metadata.
 //
 // Errors follow the reference's classes: an invalid request (feed size,
 // non-finite or non-positive p and T, a feed outside the simplex) throws
@@ -31,6 +36,7 @@
 
 #include <cmath>
 #include <cstdint>
+#include <optional>
 #include <span>
 #include <stdexcept>
 #include <string>
@@ -42,6 +48,8 @@ namespace mpmc::flash {
 
 inline constexpr std::string_view gpu_pr76_pt_flash_backend_id = "GB300/PR76/PT/max3/phase-set-backend/v1";
 inline constexpr std::string_view gpu_pr76_pt_result_convention = "GB300/PR76/PT/max3/phase-set/v1";
+inline constexpr std::string_view gpu_pr76_pt_transition_evidence_profile =
+    "GB300/PR76/PT/max3/phase-transition-evidence/v1";
 
 struct GpuPr76Mixture {
     std::vector<std::string> component_ids;
@@ -95,8 +103,27 @@ public:
         return std::move(solve_batch(std::span<const PtFlashRequest>(&request, 1)).front());
     }
 
-    // One device call for every request; results in request order.
+    // One device call for every request; results in request order.  Throws
+    // std::invalid_argument for the first request outside the flash domain.
     [[nodiscard]] std::vector<PtFlashBackendResult> solve_batch(std::span<const PtFlashRequest> requests) {
+        auto cells = solve_cells(requests);
+        std::vector<PtFlashBackendResult> results;
+        results.reserve(cells.size());
+        for (std::size_t c = 0; c < cells.size(); ++c) {
+            if (!cells[c])
+                throw std::invalid_argument("GPU PR76 backend: request " + std::to_string(c) +
+                                            " is outside the flash domain (p, T, feed)");
+            results.push_back(std::move(*cells[c]));
+        }
+        return results;
+    }
+
+    // One device call for every request; an empty entry marks a request
+    // outside the flash domain, where the reference's solve throws
+    // std::invalid_argument for that request alone.  Feed-size mismatches
+    // still throw for the whole batch.
+    [[nodiscard]] std::vector<std::optional<PtFlashBackendResult>> solve_cells(
+        std::span<const PtFlashRequest> requests) {
         const std::size_t cells = requests.size();
         std::vector<double> p(cells), t(cells), z(n_ * cells);
         for (std::size_t c = 0; c < cells; ++c) {
@@ -128,18 +155,18 @@ public:
             check(mpmc_gpu_flash_solve_max3(handle_, static_cast<int64_t>(cells), p.data(), t.data(), z.data(), &out,
                                             &out3));
 
-        std::vector<PtFlashBackendResult> results(cells);
+        std::vector<std::optional<PtFlashBackendResult>> results(cells);
         for (std::size_t c = 0; c < cells; ++c) {
-            if (status[c] == MPMC_FLASH_INVALID_REQUEST)
-                throw std::invalid_argument("GPU PR76 backend: request " + std::to_string(c) +
-                                            " is outside the flash domain (p, T, feed)");
+            if (status[c] == MPMC_FLASH_INVALID_REQUEST) continue;
+            results[c].emplace();
             auto column = [&](const std::vector<double>& a) {
                 std::vector<double> v(n_);
                 for (std::size_t i = 0; i < n_; ++i) v[i] = a[i * cells + c];
                 return v;
             };
-            PtFlashBackendResult& r = results[c];
+            PtFlashBackendResult& r = *results[c];
             r.capability = capability_;
+            r.transition_report = transition_report(status[c], max3[c]);
             r.provider_result_convention = std::string(gpu_pr76_pt_result_convention);
             PtPhaseSetResult& s = r.solution;
             s.capability.maximum_phase_count = 3U;
@@ -196,6 +223,53 @@ public:
             }
         }
         return results;
+    }
+
+    // The evidence of project_pr76_pt_max3_transition_report
+    // (pr76_pt_flash_backend.hpp:94-175) for a published status and its max3
+    // status, with the backend's default options (no caller hints, so a
+    // max3 two-phase answer is always the base pair).
+    [[nodiscard]] static PtPhaseTransitionReport transition_report(int32_t status, int32_t max3_status) {
+        PtPhaseTransitionReport report;
+        auto add = [&report](std::size_t from, std::optional<std::size_t> to, PtPhaseTransitionTrigger trigger,
+                             PtPhaseTransitionResolution resolution, bool fresh, bool closed, const char* why) {
+            report.evidence.push_back({from, to, trigger, resolution, fresh, closed,
+                                       std::string(gpu_pr76_pt_transition_evidence_profile), why});
+        };
+        using Trigger = PtPhaseTransitionTrigger;
+        using Resolution = PtPhaseTransitionResolution;
+        const auto unstable_pair = [&] {
+            add(1U, 2U, Trigger::initial_stability_witness, Resolution::candidate_not_accepted, true, false,
+                "the first two-phase candidate failed its final common-tangent review");
+        };
+        switch (status) {
+        case MPMC_FLASH_TWO_PHASE:
+            add(1U, 2U, Trigger::initial_stability_witness, Resolution::accepted_target, true, true,
+                "negative feed-stability evidence was followed by a fresh two-phase solve and final review");
+            break;
+        case MPMC_FLASH_THREE_PHASE:
+            unstable_pair();
+            add(2U, 3U, Trigger::final_phase_set_instability, Resolution::accepted_target, true, true,
+                "negative final-stability evidence triggered a fresh three-phase solve that passed its final review");
+            break;
+        case MPMC_FLASH_PHASE_SET_UNSTABLE:
+            unstable_pair();
+            add(3U, std::nullopt, Trigger::final_phase_set_instability, Resolution::broader_topology_required, true,
+                false, "the three-phase candidate failed its final review");
+            break;
+        case MPMC_FLASH_INDETERMINATE:
+            if (max3_status == MPMC_MAX3_BOUNDARY_UNRESOLVED) {
+                unstable_pair();
+                add(2U, 3U, Trigger::final_phase_set_instability, Resolution::candidate_not_accepted, true, false,
+                    "additional-phase evidence reached a three-phase disappearance boundary");
+                add(3U, 2U, Trigger::phase_disappearance, Resolution::target_resolve_failed, true, false,
+                    "no fresh two-phase neighbor closed");
+            }
+            break;
+        default:
+            break;
+        }
+        return report;
     }
 
 private:

@@ -19,6 +19,7 @@
 
 #include <mpmc/flash/pr76_pt_flash_backend.hpp>
 #include <mpmc/flash/pr76_three_phase.hpp>
+#include <mpmc/flash/pr76_max3_phase_set.hpp>
 #include <mpmc/flash/pr76_pt_continuation.hpp>
 #include <mpmc/flash/pr76_sensitivity.hpp>
 #include <mpmc/flow/pr76_selected_phase_property_closure.hpp>
@@ -438,6 +439,56 @@ int ref_continuation_batch(int n, const double* tc, const double* pc, const doub
         if (lo < hi) pool.emplace_back(run, lo, hi);
     }
     for (auto& th : pool) th.join();
+    return 0;
+}
+
+// The reference backend's transition report (project_pr76_pt_max3_transition_report,
+// modules/flash/include/mpmc/flash/pr76_pt_flash_backend.hpp:94-175) of each
+// cell, with its published status (0 single, 1 two, 2 unstable, 3
+// indeterminate, 4 three) and max3 status.  Evidence k of cell c occupies
+// evidence[(c * 8 + k) * 6 ..]: source, target (0 = none), trigger,
+// resolution, fresh target solve attempted, target topology closed; count[c]
+// evidence entries (at most 8).
+int ref_transition_reports(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                           int64_t ncell, const double* p, const double* t, const double* z, int32_t* published,
+                           int32_t* max3_status, int32_t* count, int32_t* evidence) {
+    std::vector<std::string> order;
+    const th::PrParameterSet params = make_parameters(n, tc, pc, omega, kij, order);
+    const auto model = th::Pr76Phase<double>::from_parameters(params);
+    fl::Pr76VleEvaluator evaluator(model);
+    for (int64_t c = 0; c < ncell; ++c) {
+        std::vector<double> feed(n);
+        for (int i = 0; i < n; ++i) feed[i] = z[i * ncell + c];
+        count[c] = -1;
+        try {
+            const auto source = fl::solve_pr76_pt_max3(p[c], t[c], feed, evaluator);
+            const auto set = fl::project_pr76_pt_max3_phase_set(source);
+            const auto report = fl::project_pr76_pt_max3_transition_report(source);
+            int pub = 3;
+            if (set.solution.status == fl::PtPhaseSetStatus::accepted && set.solution.candidate_phase_set) {
+                const auto k = set.solution.candidate_phase_set->phases.size();
+                pub = k == 1 ? 0 : (k == 2 ? 1 : 4);
+            } else if (set.solution.status == fl::PtPhaseSetStatus::phase_set_unstable) {
+                pub = 2;
+            }
+            published[c] = pub;
+            max3_status[c] = static_cast<int32_t>(source.status);
+            count[c] = static_cast<int32_t>(std::min<std::size_t>(report.evidence.size(), 8));
+            for (int k = 0; k < count[c]; ++k) {
+                const auto& e = report.evidence[k];
+                int32_t* row = evidence + (c * 8 + k) * 6;
+                row[0] = static_cast<int32_t>(e.source_phase_count);
+                row[1] = e.target_phase_count ? static_cast<int32_t>(*e.target_phase_count) : 0;
+                row[2] = static_cast<int32_t>(e.trigger);
+                row[3] = static_cast<int32_t>(e.resolution);
+                row[4] = e.fresh_target_solve_attempted ? 1 : 0;
+                row[5] = e.target_topology_closed ? 1 : 0;
+            }
+        } catch (const std::exception&) {
+            published[c] = -1;
+            max3_status[c] = -1;
+        }
+    }
     return 0;
 }
 

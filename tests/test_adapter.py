@@ -31,7 +31,14 @@ std::unique_ptr<mpmc::flash::PtFlashBackend> make(const mpmc::flash::GpuPr76Mixt
 
 CHART_SOURCE = r"""
 #include "gpu_pr76_selected_phase_property_chart.hpp"
+#include "gpu_post_snes_pt_flash_scan.hpp"
 #include <memory>
+mpmc::flow::ScanSummary scan(std::span<const mpmc::flow::ScanSourceCell> cells,
+                             mpmc::flash::GpuPr76PtFlashBackend& gpu) {
+    auto r = mpmc::flow::scan_pt_flash_source_cells_batched(
+        cells, gpu, [](const mpmc::flash::PtFlashBackendResult&, std::optional<std::vector<double>>*) { return 0; });
+    return mpmc::flow::summarize(cells, r);
+}
 namespace fw = mpmc::flow;
 std::unique_ptr<fw::GpuPr76SelectedPhasePropertyChart> make(const mpmc::flash::GpuPr76Mixture& m,
                                                              std::vector<double> mm,
@@ -60,7 +67,7 @@ void cpu(const mpmc::thermodynamics::Pr76Phase<double>& model, fw::AffineTranspo
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "modules", "flow", "include")),
                     reason="reference headers not present")
 @pytest.mark.skipif(shutil.which("g++") is None, reason="no g++")
-def test_chart_binding_compiles_against_reference_flow_module(tmp_path):
+def test_flow_bindings_compile_against_reference_flow_module(tmp_path):
     src = tmp_path / "chart_binding_check.cpp"
     src.write_text(CHART_SOURCE)
     cmd = ["g++", "-std=c++20", "-fsyntax-only", "-Wall", "-Wextra", "-Werror",
@@ -81,3 +88,91 @@ def test_adapter_compiles_against_reference_interface(tmp_path):
     cmd += ["-I" + os.path.join(REFERENCE, "modules", m, "include") for m in MODULES]
     res = subprocess.run(cmd + [str(src)], capture_output=True, text=True)
     assert res.returncode == 0, res.stderr
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "modules", "flash", "include")),
+                    reason="reference headers not present")
+@pytest.mark.skipif(shutil.which("g++") is None, reason="no g++")
+def test_transition_report_matches_reference(tmp_path, oracle_lib):
+    """The binding's transition report for each published status equals the
+    reference backend's project_pr76_pt_max3_transition_report on the same
+    cells (source, target, trigger, resolution, fresh solve, closed), except
+    for indeterminate results, which the binding leaves without evidence."""
+    import ctypes
+
+    import numpy as np
+
+    from mpmc_hnu_gb300 import synth
+
+    if not oracle_lib.reference_available():
+        pytest.skip("reference harness not built")
+    so = str(tmp_path / "libreport_host.so")
+    cmd = ["g++", "-std=c++20", "-O1", "-fPIC", "-shared", "-I" + os.path.join(ROOT, "include"),
+           "-I" + os.path.join(ROOT, "mpmc_hnu_gb300", "cpp")]
+    cmd += ["-I" + os.path.join(REFERENCE, "modules", m, "include") for m in MODULES]
+    subprocess.check_call(cmd + [os.path.join(ROOT, "tests", "host_build", "report_host.cpp"), "-o", so])
+    ours = ctypes.CDLL(so)
+    ref = ctypes.CDLL(oracle_lib.REF_SO)
+    d = np.load(os.path.join(ROOT, "tests", "golden", "max3_reference.npz"))
+    cases = [(synth.three_phase_fixture_mixture(), d["p"][::2], d["t"][::2], d["z"][:, ::2])]
+    mix10 = synth.make_mixture(10, 1001)
+    p10, t10, z10 = synth.make_cells(10, 300, 2001)
+    cases.append((mix10, p10, t10, z10))
+    seen = set()
+    for mix, p, t, z in cases:
+        tc, pc, om, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
+        p, t, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (p, t, z))
+        n, ncell = z.shape
+        pub = np.empty(ncell, np.int32)
+        m3 = np.empty(ncell, np.int32)
+        cnt = np.empty(ncell, np.int32)
+        ev = np.zeros((ncell, 8, 6), np.int32)
+        ref.ref_transition_reports(ctypes.c_int(n), *[ctypes.c_void_p(a.ctypes.data) for a in (tc, pc, om, kij)],
+                                   ctypes.c_int64(ncell), *[ctypes.c_void_p(a.ctypes.data) for a in (p, t, z)],
+                                   *[ctypes.c_void_p(a.ctypes.data) for a in (pub, m3, cnt, ev)])
+        for c in range(ncell):
+            assert cnt[c] >= 0
+            mine = np.zeros((8, 6), np.int32)
+            k = ours.our_transition_report(ctypes.c_int32(int(pub[c])), ctypes.c_int32(int(m3[c])),
+                                           ctypes.c_void_p(mine.ctypes.data))
+            seen.add((int(pub[c]), int(m3[c])))
+            if pub[c] == 3 and m3[c] == 5:
+                assert k == 0
+                continue
+            assert k == cnt[c] and np.array_equal(mine[:k], ev[c, :k]), (c, int(pub[c]), int(m3[c]))
+    assert {(0, 0), (1, 1), (4, 2), (2, 4)} <= seen
+
+
+SCAN_EXPECTED = {
+    # a cell already in its accepted phase count proposes nothing
+    "steady": "cells complete:0 complete:0 summary complete 2 0",
+    # a one-phase source cell that flashes to two phases proposes 1 -> 2
+    "appear": "cells complete:0 complete:2 complete:0 summary complete 3 0 proposal 2 1->2",
+    # the PR76 backend publishes no disappearance evidence for 2 -> 1, so the
+    # reference's candidate adapter rejects it (std::invalid_argument)
+    "vanish": "cells complete:0 incompatible:0 summary incompatible 1 0",
+    "malformed": "cells complete:2 incompatible:0 summary incompatible 1 0",
+    "no_density": "cells indeterminate:0 summary indeterminate 0 0",
+    "resolver": "cells complete:0 resolver_error:0 summary resolver_error 1 42",
+    # the first cell that is not complete decides, as the loop's early return does
+    "indeterminate_first": "cells indeterminate:0 incompatible:0 complete:0 summary indeterminate 0 0",
+}
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "modules", "flow", "include")),
+                    reason="reference headers not present")
+@pytest.mark.skipif(shutil.which("g++") is None, reason="no g++")
+def test_batched_scan_follows_the_reference_rules(tmp_path):
+    """mpmc_hnu_gb300/cpp/gpu_post_snes_pt_flash_scan.hpp over the reference's
+    own Pr76PtFlashBackend (tests/host_build/scan_host.cpp) on a methane /
+    n-butane mixture: per-cell statuses, proposals and the loop verdict of the
+    reference scanner (post_snes_pt_flash_phase_transition_scanner.hpp:207-421)
+    in each scenario."""
+    exe = str(tmp_path / "scan_host")
+    cmd = ["g++", "-std=c++20", "-O1", "-I" + os.path.join(ROOT, "include"),
+           "-I" + os.path.join(ROOT, "mpmc_hnu_gb300", "cpp")]
+    cmd += ["-I" + os.path.join(REFERENCE, "modules", m, "include") for m in MODULES]
+    subprocess.check_call(cmd + [os.path.join(ROOT, "tests", "host_build", "scan_host.cpp"), "-o", exe])
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.splitlines()
+    got = {line.split(" ", 1)[0]: line.split(" ", 1)[1] for line in out}
+    assert got == SCAN_EXPECTED
