@@ -59,6 +59,15 @@ def f_ad(n: int) -> float:
     return (2 / 3) * n ** 3 + 2 * n * n * (n + 1) + 2 * n * (2 * n + 1) * (n + 1) + 2 * (n + 2) * f_eval(n)
 
 
+def f_chart(n: int, phases: int) -> float:
+    """Algorithmic flops of one selected-phase property chart: per phase one
+    property evaluation, its closed-form d[Z, ln phi]/d[p, T, x]
+    (6 n^2 + 40 n + 60) and the chain rule of the five properties
+    (5 (n + 2) x 8), plus 3 n per equilibrium row."""
+    per_phase = f_eval(n) + 6 * n * n + 40 * n + 60 + 40 * (n + 2)
+    return phases * per_phase + 3 * n * (phases - 1)
+
+
 # ---------------------------------------------------------------------------
 # replicas (one process per GPU; cells are independent, so no data exchange)
 def cell_offset(rank: int, ncell: int) -> int:
@@ -253,12 +262,14 @@ def chart_states(n: int, phases: int, ncell: int, seed: int):
     return np.ascontiguousarray(np.vstack([p[None], t[None], sat] + blocks))
 
 
-def chart_leg(flash, synth, torch, device: int, stream, ncell: int, threads: int, cpu_sample: int, peaks):
+def chart_leg(flash, synth, torch, device: int, stream, ncell: int, threads: int, cpu_sample: int, hbm_gbs,
+              fp64_tf):
     """Device-resident chart of `ncell` two-phase cells at 10 components (roots
     0 and 0, affine viscosity/enthalpy model): cells/s over 5 launches timed
-    with CUDA events on the launching stream, the algorithmic bytes per cell
-    (chart read, status, values and Jacobian written) against the measured
-    copy bandwidth, and the CPU oracle on a sample of the same cells."""
+    with CUDA events on the launching stream; its algorithmic FP64 flops
+    (f_chart) against the measured FP64 peak, its algorithmic bytes (chart
+    read, status, values and Jacobian written) against the measured copy
+    bandwidth; and the CPU oracle on a sample of the same cells."""
     n, phases = CHART_N, CHART_PHASES
     rows, cols = flash.chart_shape(n, phases)
     mix = synth.make_mixture(n, 1001)
@@ -290,13 +301,18 @@ def chart_leg(flash, synth, torch, device: int, stream, ncell: int, threads: int
     ms = e0.elapsed_time(e1) / launches
     status = st.cpu().numpy()
     bytes_per_cell = cols * 8 + 4 + rows * 8 + rows * cols * 8
-    achieved = bytes_per_cell * ncell / (ms * 1e-3) / 1e9
+    gbs = bytes_per_cell * ncell / (ms * 1e-3) / 1e9
+    flops = f_chart(n, phases) * ncell
+    tfs = flops / (ms * 1e-3) / 1e12
     leg = {"value": ncell / (ms * 1e-3), "unit": "cells/s", "cells": ncell, "ms_per_launch": ms,
            "components": n, "phases": phases,
            "statuses": {str(k): int(v) for k, v in enumerate(np.bincount(status, minlength=7)) if v},
-           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks, "unit": "GB/s",
-                        "frac": achieved / peaks if peaks else None, "bytes_per_cell": bytes_per_cell,
-                        "peak_source": "hbm_gbs of MEASURED_PEAKS.json (measured copy bandwidth)"},
+           "roofline": {"bound": "fp64", "achieved": tfs, "peak": fp64_tf, "unit": "TFLOP/s",
+                        "frac": tfs / fp64_tf if fp64_tf else None, "flops_per_cell": f_chart(n, phases),
+                        "peak_source": "measured in this run by mpmc_hnu_gb300/csrc/peak_probe.cu (FMA chains)",
+                        "hbm": {"achieved": gbs, "peak": hbm_gbs, "unit": "GB/s",
+                                "frac": gbs / hbm_gbs if hbm_gbs else None, "bytes_per_cell": bytes_per_cell,
+                                "peak_source": "hbm_gbs of MEASURED_PEAKS.json"}},
            "dtype": "f64", "l2_flush": f"outputs {bytes_per_cell * ncell / 1e9:.1f} GB per launch, far above L2"}
     del dq, vals, jac
     if cpu_sample > 0:
@@ -772,7 +788,7 @@ def main() -> None:
             peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
             hbm = json.load(open(peaks_path)).get("hbm_gbs") if os.path.exists(peaks_path) else None
             chart = chart_leg(flash, synth, torch, device, stream, args.chart_cells, threads,
-                              min(args.cpu_sample, 65536), hbm)
+                              min(args.cpu_sample, 65536), hbm, fp64_tf)
         except Exception as e:  # noqa: BLE001 - reported in the line
             chart = {"error": f"{type(e).__name__}: {e}"}
 
