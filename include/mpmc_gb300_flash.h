@@ -252,6 +252,36 @@ int mpmc_gpu_flash_solve_device_max3(mpmc_gpu_flash* handle, int64_t n_cells, co
                                      const double* z, const mpmc_flash_outputs* out,
                                      const mpmc_three_phase_outputs* out3, void* stream);
 
+/* Caller start hints of a max-3-phase solve: the hints the reference's
+ * ordered-path continuation passes from one accepted point to the next
+ * (modules/flash/include/mpmc/flash/pr76_pt_continuation.hpp:106-146; the
+ * Pr76PtFlashBackendOptions initial_starts, final_starts and
+ * three_phase_starts of pr76_pt_flash_backend.hpp:26-40).  Per cell, count
+ * (0..3) compositions join the feed stability test and the final review as
+ * extra starts; where three_phase is nonzero (count must be 3) they also form a
+ * three-phase start, with the fractions of phases 1 and 2, whose attempts
+ * run before the automatic ones.  A three-phase start outside the simplex or
+ * off the feed's support makes the cell MPMC_FLASH_INVALID_REQUEST, as the
+ * reference's start check throws. */
+typedef struct mpmc_start_hints {
+    const int32_t* count;        /* [n_cells] */
+    const double* composition;   /* [3 * n * n_cells]: composition k, component i at (k * n + i) * n_cells + c */
+    const int32_t* three_phase;  /* [n_cells] or NULL (then fraction is NULL too) */
+    const double* fraction;      /* [2 * n_cells]: phase 1 at c, phase 2 at n_cells + c */
+} mpmc_start_hints;
+
+/* mpmc_gpu_flash_solve_max3 / _device_max3 with caller start hints.  These
+ * run the plain FP64 kernel -- the reference algorithm -- for every form,
+ * followed by the max-3-phase continuation with the same hints.  out->status
+ * and out->ln_k are required. */
+int mpmc_gpu_flash_solve_hinted(mpmc_gpu_flash* handle, int64_t n_cells, const double* p, const double* t,
+                                const double* z, const mpmc_start_hints* hints, const mpmc_flash_outputs* out,
+                                const mpmc_three_phase_outputs* out3);
+int mpmc_gpu_flash_solve_device_hinted(mpmc_gpu_flash* handle, int64_t n_cells, const double* p, const double* t,
+                                       const double* z, const mpmc_start_hints* hints,
+                                       const mpmc_flash_outputs* out, const mpmc_three_phase_outputs* out3,
+                                       void* stream);
+
 /* ------------------------------------------------------------------------
  * Selected-phase property chart: the flow module's per-cell property and
  * Jacobian publication on a frozen natural-variable chart,

@@ -84,6 +84,7 @@ struct mpmc_gpu_flash {
     bool timed_warm = false;  // the last timed solve ran a warm and a cold pass
     DevBuf in_warm;     // host entry: staged ln K warm starts
     DevBuf outs3[5];    // host entry: staged three-phase outputs
+    DevBuf in_hints[4];   // host hinted entry: staged count, compositions, three-phase flags, fractions
     DevBuf chart_in[2];   // host property-chart entry: staged chart values, dependent components
     DevBuf chart_out[3];  // host property-chart entry: staged status, values, Jacobian
     int32_t shape[8] = {};  // explicit launch shape (mpmc_gpu_flash_set_launch_shape), 0 = default
@@ -244,15 +245,16 @@ int prepare_device(mpmc_gpu_flash* h, int64_t ncell, pr76::DeviceOutputs& d) {
 // The launches of one solve on `stream` (no allocation, no synchronisation).
 cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
                            const double* warm, const pr76::DeviceOutputs& d, cudaStream_t stream, bool timing,
-                           const pr76::Max3Outputs* max3 = nullptr) {
+                           const pr76::Max3Outputs* max3 = nullptr, const pr76::Hints* hints = nullptr) {
     cudaError_t e;
     int next_event = 0;
     auto record = [&]() {
         if (timing && next_event < 24) cudaEventRecord(h->events[next_event++], stream);
     };
-    if (h->form == MPMC_FORM_PLAIN_FP64) {
+    if (h->form == MPMC_FORM_PLAIN_FP64 || hints) {
+        // caller start hints run the reference algorithm itself, for every form
         record();
-        e = pr76::launch_plain(h->n, h->d_mixture, ncell, p, t, z, d, stream);
+        e = pr76::launch_plain(h->n, h->d_mixture, ncell, p, t, z, d, stream, hints ? *hints : pr76::Hints{});
         record();
     } else {
         pr76::BatchedShape shape = batched_shape(h, timing ? h->events : nullptr);
@@ -265,7 +267,7 @@ cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, co
     }
     if (e != cudaSuccess) return e;
     if (max3) {  // before the sensitivities: a fresh two-phase neighbor is differentiated too
-        e = pr76::launch_max3(h->n, h->d_mixture, ncell, p, t, z, d, *max3, stream);
+        e = pr76::launch_max3(h->n, h->d_mixture, ncell, p, t, z, d, *max3, stream, hints ? *hints : pr76::Hints{});
         if (e != cudaSuccess) return e;
     }
     if (h->want_sensitivity) {
@@ -288,7 +290,7 @@ bool same_key(const GraphEntry& g, int64_t ncell, const double* p, const double*
 
 int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
                const double* warm, const pr76::DeviceOutputs& d_in, cudaStream_t stream,
-               const pr76::Max3Outputs* max3 = nullptr) {
+               const pr76::Max3Outputs* max3 = nullptr, const pr76::Hints* hints = nullptr) {
     if (warm && h->form == MPMC_FORM_PLAIN_FP64)
         return fail(MPMC_ERR_UNSUPPORTED,
                     "ln K warm starts need a work-queue form (MPMC_FORM_MIXED or MPMC_FORM_BATCHED); the plain "
@@ -305,7 +307,7 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
             if ((e = cudaEventCreate(&ev)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
     }
     if (!h->use_graphs || h->stage_timing || max3) {
-        e = enqueue_device(h, ncell, p, t, z, warm, d, stream, h->stage_timing, max3);
+        e = enqueue_device(h, ncell, p, t, z, warm, d, stream, h->stage_timing, max3, hints);
         return e == cudaSuccess ? MPMC_OK : cuda_fail(e, "flash kernel launch");
     }
     // CUDA graph of the launch sequence, one per (cells, buffers): captured on
@@ -434,13 +436,14 @@ cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const
 }
 
 cudaError_t launch_max3(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
-                        const double* z, const DeviceOutputs& out, const Max3Outputs& out3, cudaStream_t stream) {
+                        const double* z, const DeviceOutputs& out, const Max3Outputs& out3, cudaStream_t stream,
+                        const Hints& hints) {
     switch (capacity_for(n)) {
-    case 4: return launch_max3_nm4(d_mix, ncell, p, t, z, out, out3, stream);
-    case 8: return launch_max3_nm8(d_mix, ncell, p, t, z, out, out3, stream);
-    case 12: return launch_max3_nm12(d_mix, ncell, p, t, z, out, out3, stream);
-    case 16: return launch_max3_nm16(d_mix, ncell, p, t, z, out, out3, stream);
-    case 20: return launch_max3_nm20(d_mix, ncell, p, t, z, out, out3, stream);
+    case 4: return launch_max3_nm4(d_mix, ncell, p, t, z, out, out3, stream, hints);
+    case 8: return launch_max3_nm8(d_mix, ncell, p, t, z, out, out3, stream, hints);
+    case 12: return launch_max3_nm12(d_mix, ncell, p, t, z, out, out3, stream, hints);
+    case 16: return launch_max3_nm16(d_mix, ncell, p, t, z, out, out3, stream, hints);
+    case 20: return launch_max3_nm20(d_mix, ncell, p, t, z, out, out3, stream, hints);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -458,13 +461,13 @@ cudaError_t launch_chart(int n, const Mixture* d_mix, const ChartParams& params,
 }
 
 cudaError_t launch_plain(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
-                         const double* z, const DeviceOutputs& out, cudaStream_t stream) {
+                         const double* z, const DeviceOutputs& out, cudaStream_t stream, const Hints& hints) {
     switch (capacity_for(n)) {
-    case 4: return launch_plain_nm4(d_mix, ncell, p, t, z, out, stream);
-    case 8: return launch_plain_nm8(d_mix, ncell, p, t, z, out, stream);
-    case 12: return launch_plain_nm12(d_mix, ncell, p, t, z, out, stream);
-    case 16: return launch_plain_nm16(d_mix, ncell, p, t, z, out, stream);
-    case 20: return launch_plain_nm20(d_mix, ncell, p, t, z, out, stream);
+    case 4: return launch_plain_nm4(d_mix, ncell, p, t, z, out, stream, hints);
+    case 8: return launch_plain_nm8(d_mix, ncell, p, t, z, out, stream, hints);
+    case 12: return launch_plain_nm12(d_mix, ncell, p, t, z, out, stream, hints);
+    case 16: return launch_plain_nm16(d_mix, ncell, p, t, z, out, stream, hints);
+    case 20: return launch_plain_nm20(d_mix, ncell, p, t, z, out, stream, hints);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -473,7 +476,7 @@ cudaError_t launch_plain(int n, const Mixture* d_mix, int64_t ncell, const doubl
 namespace {
 int solve_host(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
                const double* ln_k_warm, const mpmc_flash_outputs* out, const mpmc_three_phase_outputs* out3,
-               bool max3);
+               bool max3, const mpmc_start_hints* hints = nullptr);
 
 // Validates a property-chart call and fills the kernel's closure constants
 // (the checks of the closure's constructor, pr76_selected_phase_property_closure.hpp:274-319,
@@ -600,6 +603,7 @@ int mpmc_gpu_flash_destroy(mpmc_gpu_flash* h) {
     h->in_z.release();
     h->in_warm.release();
     for (auto& b : h->outs3) b.release();
+    for (auto& b : h->in_hints) b.release();
     for (auto& b : h->chart_in) b.release();
     for (auto& b : h->chart_out) b.release();
     for (auto& b : h->outs) b.release();
@@ -715,6 +719,40 @@ int mpmc_gpu_flash_solve_warm(mpmc_gpu_flash* h, int64_t ncell, const double* p,
     return solve_host(h, ncell, p, t, z, ln_k_warm, out, nullptr, false);
 }
 
+int mpmc_gpu_flash_solve_hinted(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
+                                const mpmc_start_hints* hints, const mpmc_flash_outputs* out,
+                                const mpmc_three_phase_outputs* out3) {
+    if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
+    if (!hints || (ncell > 0 && (!hints->count || !hints->composition)) ||
+        (hints->three_phase != nullptr) != (hints->fraction != nullptr))
+        return fail(MPMC_ERR_INVALID_ARGUMENT, "hinted solve: count and composition required, three_phase and "
+                                               "fraction together");
+    return solve_host(h, ncell, p, t, z, nullptr, out, out3, true, hints);
+}
+
+int mpmc_gpu_flash_solve_device_hinted(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t,
+                                       const double* z, const mpmc_start_hints* hints,
+                                       const mpmc_flash_outputs* out, const mpmc_three_phase_outputs* out3,
+                                       void* stream) {
+    if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
+    if (ncell < 0) return fail(MPMC_ERR_INVALID_ARGUMENT, "negative cell count");
+    if (ncell == 0) return MPMC_OK;
+    if (!p || !t || !z) return fail(MPMC_ERR_INVALID_ARGUMENT, "p, t and z must not be null");
+    if (!hints || !hints->count || !hints->composition ||
+        (hints->three_phase != nullptr) != (hints->fraction != nullptr))
+        return fail(MPMC_ERR_INVALID_ARGUMENT, "hinted solve: count and composition required, three_phase and "
+                                               "fraction together");
+    if (!out || !out->status || !out->ln_k)
+        return fail(MPMC_ERR_INVALID_ARGUMENT, "hinted solve: the status and ln_k outputs are required");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    pr76::Max3Outputs m3{};
+    if (out3) m3 = {out3->max3_status, out3->phase_fraction, out3->composition, out3->ln_phi, out3->z_factor};
+    const pr76::Hints dh{hints->count, hints->composition, hints->three_phase, hints->fraction};
+    return run_device(h, ncell, p, t, z, nullptr, to_device_outputs(out), static_cast<cudaStream_t>(stream), &m3,
+                      &dh);
+}
+
 int mpmc_gpu_flash_property_chart_device(mpmc_gpu_flash* h, int64_t ncell, const mpmc_property_chart_spec* spec,
                                          const double* q, const int32_t* dependent,
                                          const mpmc_property_chart_outputs* out, void* stream) {
@@ -786,7 +824,7 @@ namespace {
 // requested outputs back, synchronise.
 int solve_host(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
                const double* ln_k_warm, const mpmc_flash_outputs* out, const mpmc_three_phase_outputs* out3,
-               bool max3) {
+               bool max3, const mpmc_start_hints* hints) {
     if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
     if (max3 && (!out || !out->status || !out->ln_k))
         return fail(MPMC_ERR_INVALID_ARGUMENT, "max-3-phase solve: the status and ln_k outputs are required");
@@ -847,9 +885,26 @@ int solve_host(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
         m3 = {static_cast<int32_t*>(dev3[0]), static_cast<double*>(dev3[1]), static_cast<double*>(dev3[2]),
               static_cast<double*>(dev3[3]), static_cast<double*>(dev3[4])};
     }
+    // caller start hints: staged like the inputs
+    pr76::Hints dh{};
+    if (hints) {
+        const size_t bytes[4] = {nc * sizeof(int32_t), 3 * n * nc * sizeof(double),
+                                 hints->three_phase ? nc * sizeof(int32_t) : 0,
+                                 hints->three_phase ? 2 * nc * sizeof(double) : 0};
+        const void* src[4] = {hints->count, hints->composition, hints->three_phase, hints->fraction};
+        for (int k = 0; k < 4; ++k) {
+            if (!bytes[k]) continue;
+            if ((e = h->in_hints[k].ensure(bytes[k])) != cudaSuccess) return cuda_fail(e, "hint staging allocation");
+            if ((e = cudaMemcpyAsync(h->in_hints[k].ptr, src[k], bytes[k], cudaMemcpyHostToDevice, s)) != cudaSuccess)
+                return cuda_fail(e, "hint copy");
+        }
+        dh = {static_cast<const int32_t*>(h->in_hints[0].ptr), static_cast<const double*>(h->in_hints[1].ptr),
+              hints->three_phase ? static_cast<const int32_t*>(h->in_hints[2].ptr) : nullptr,
+              hints->three_phase ? static_cast<const double*>(h->in_hints[3].ptr) : nullptr};
+    }
     const int rc = run_device(h, ncell, static_cast<const double*>(h->in_p.ptr),
                               static_cast<const double*>(h->in_t.ptr), static_cast<const double*>(h->in_z.ptr),
-                              d_warm, to_device_outputs(&dev_out), s, max3 ? &m3 : nullptr);
+                              d_warm, to_device_outputs(&dev_out), s, max3 ? &m3 : nullptr, hints ? &dh : nullptr);
     if (rc != MPMC_OK) return rc;
     for (int k = 0; k < kOutputFields; ++k) {
         void* hp = *field_ptr(&host_out, k);

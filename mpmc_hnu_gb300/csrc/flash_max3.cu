@@ -3,7 +3,7 @@
 // unit is compiled with light ptxas optimisation to keep the build short.
 #define MPMC_FP64_CALL __noinline__
 #include "launch.h"
-#include "pr76_max3.cuh"
+#include "pr76_hints.cuh"
 
 namespace pr76 {
 
@@ -14,7 +14,7 @@ template <int NM>
 __global__ void __launch_bounds__(64) max3_kernel(const Mixture* __restrict__ mix_g, int64_t ncell,
                                                   const double* __restrict__ p, const double* __restrict__ t,
                                                   const double* __restrict__ z, DeviceOutputs out,
-                                                  Max3Outputs out3) {
+                                                  Max3Outputs out3, Hints hints) {
     __shared__ Mixture m;
     stage_mixture(mix_g, m);
     using namespace fp64;
@@ -52,8 +52,13 @@ __global__ void __launch_bounds__(64) max3_kernel(const Mixture* __restrict__ mi
             }
             Max3Scratch<NM> s;
             Max3Result r{kM3Indeterminate, false, false};
+            // the caller's hints, as the base solve ran with them (the plain
+            // kernel has already rejected a cell whose three-phase start fails)
+            CellHints<NM> hs;
+            load_hints<NM>(hints, feed, n, ncell, cell, hs);
             if (temp_setup(m, c))
-                r = max3_cell(m, c, feed, lnk, s);
+                r = max3_cell(m, c, feed, lnk, s, hs.count > 0 ? hs.ptr : nullptr, hs.count,
+                              hs.has_three ? hs.three : nullptr);
             else
                 r.status = -1;
             m3 = r.status;
@@ -117,7 +122,7 @@ __global__ void __launch_bounds__(64) max3_kernel(const Mixture* __restrict__ mi
 
 cudaError_t MPMC_CAT(launch_max3_nm, MPMC_NM)(const Mixture* d_mix, int64_t ncell, const double* p,
                                                 const double* t, const double* z, const DeviceOutputs& out,
-                                                const Max3Outputs& out3, cudaStream_t stream) {
+                                                const Max3Outputs& out3, cudaStream_t stream, const Hints& hints) {
     if (ncell <= 0) return cudaSuccess;
     if (!out.status || !out.lnk) return cudaErrorInvalidValue;
     int device = 0, sms = 0;
@@ -127,7 +132,8 @@ cudaError_t MPMC_CAT(launch_max3_nm, MPMC_NM)(const Mixture* d_mix, int64_t ncel
     int64_t grid = static_cast<int64_t>(sms) * 2;
     const int64_t needed = (ncell + block - 1) / block;
     if (grid > needed) grid = needed;
-    max3_kernel<MPMC_NM><<<static_cast<unsigned>(grid), block, 0, stream>>>(d_mix, ncell, p, t, z, out, out3);
+    max3_kernel<MPMC_NM><<<static_cast<unsigned>(grid), block, 0, stream>>>(d_mix, ncell, p, t, z, out, out3,
+                                                                             hints);
     return cudaGetLastError();
 }
 

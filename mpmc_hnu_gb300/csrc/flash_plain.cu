@@ -3,13 +3,14 @@
 // (cell index fastest); the mixture constants are staged into shared memory
 // once per block.
 #include "launch.h"
-#include "pr76_fp64.cuh"
+#include "pr76_hints.cuh"
 
 namespace pr76 {
 
 template <int NM>
 __device__ void plain_cell(const Mixture& m, int64_t ncell, int64_t cell, const double* __restrict__ p,
-                           const double* __restrict__ t, const double* __restrict__ z, const DeviceOutputs& out);
+                           const double* __restrict__ t, const double* __restrict__ z, const DeviceOutputs& out,
+                           const Hints& hints);
 
 // Persistent grid-stride launch: the grid is sized to the SM count times a
 // residency target so that every thread's local state stays in L1/L2.
@@ -17,18 +18,20 @@ template <int NM>
 __global__ void __launch_bounds__(128) flash_plain_kernel(const Mixture* __restrict__ mix_g, int64_t ncell,
                                                           const double* __restrict__ p,
                                                           const double* __restrict__ t,
-                                                          const double* __restrict__ z, DeviceOutputs out) {
+                                                          const double* __restrict__ z, DeviceOutputs out,
+                                                          Hints hints) {
     __shared__ Mixture m;
     stage_mixture(mix_g, m);
     using namespace fp64;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t cell = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; cell < ncell; cell += stride)
-        plain_cell<NM>(m, ncell, cell, p, t, z, out);
+        plain_cell<NM>(m, ncell, cell, p, t, z, out, hints);
 }
 
 template <int NM>
 __device__ void plain_cell(const Mixture& m, int64_t ncell, int64_t cell, const double* __restrict__ p,
-                           const double* __restrict__ t, const double* __restrict__ z, const DeviceOutputs& out) {
+                           const double* __restrict__ t, const double* __restrict__ z, const DeviceOutputs& out,
+                           const Hints& hints) {
     using namespace fp64;
     Cell<NM> c;
     c.n = m.n;
@@ -40,7 +43,13 @@ __device__ void plain_cell(const Mixture& m, int64_t ncell, int64_t cell, const 
     for (int i = 0; i < c.n; ++i) feed[i] = z[static_cast<int64_t>(i) * ncell + cell];
     Scratch<NM> w;
     CellResult<NM> r;
-    const int status = solve_cell(m, c, feed, w, r);
+    r.has_pair = false;
+    // caller hints: extra starts of the feed test and of the final review
+    // (solve_pt_vle's initial_starts and final_starts, pt_split.hpp:415-419)
+    CellHints<NM> hs;
+    const bool hints_ok = load_hints<NM>(hints, feed, c.n, ncell, cell, hs);
+    const double* const* extra = hs.count > 0 ? hs.ptr : nullptr;
+    const int status = hints_ok ? solve_cell(m, c, feed, w, r, extra, hs.count, extra, hs.count) : kInvalid;
     const int n = c.n;
     const double nan = __longlong_as_double(0x7ff8000000000000LL);
     auto put = [&](double* a, int k, double v) {
@@ -87,7 +96,7 @@ __device__ void plain_cell(const Mixture& m, int64_t ncell, int64_t cell, const 
 
 cudaError_t MPMC_CAT(launch_plain_nm, MPMC_NM)(const Mixture* d_mix, int64_t ncell, const double* p,
                                                  const double* t, const double* z, const DeviceOutputs& out,
-                                                 cudaStream_t stream) {
+                                                 cudaStream_t stream, const Hints& hints) {
     if (ncell <= 0) return cudaSuccess;
     int device = 0, sms = 0;
     cudaGetDevice(&device);
@@ -97,7 +106,8 @@ cudaError_t MPMC_CAT(launch_plain_nm, MPMC_NM)(const Mixture* d_mix, int64_t nce
     int64_t grid = static_cast<int64_t>(sms) * shape.blocks_per_sm;
     const int64_t needed = (ncell + block - 1) / block;
     if (grid > needed) grid = needed;
-    flash_plain_kernel<MPMC_NM><<<static_cast<unsigned>(grid), block, 0, stream>>>(d_mix, ncell, p, t, z, out);
+    flash_plain_kernel<MPMC_NM><<<static_cast<unsigned>(grid), block, 0, stream>>>(d_mix, ncell, p, t, z, out,
+                                                                                   hints);
     return cudaGetLastError();
 }
 

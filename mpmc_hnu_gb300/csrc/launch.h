@@ -76,6 +76,20 @@ cudaError_t launch_batched(int n, const Mixture* d_mix, int64_t ncell, const dou
                            const double* z, const DeviceOutputs& out, void* scratch, size_t scratch_bytes,
                            const BatchedShape& shape, cudaStream_t stream);
 
+// Caller start hints of a solve (the hints of the reference's ordered-path
+// continuation, pr76_pt_continuation.hpp:106-146): per cell count[c] (0..3)
+// compositions at x[(k * n + i) * ncell + c], used as extra starts of the
+// feed stability test and of the final review; where three[c] is nonzero the
+// three compositions are also a three-phase start whose phase-1 and phase-2
+// fractions are fraction[k * ncell + c].  Device pointers; count == null
+// means no hints.
+struct Hints {
+    const int32_t* count;
+    const double* x;
+    const int32_t* three;
+    const double* fraction;
+};
+
 // Three-phase outputs of the max-3-phase continuation (layout a[k * ncell + c];
 // phase-major compositions: phase q, component i at row q * n + i).
 struct Max3Outputs {
@@ -92,7 +106,8 @@ struct Max3Outputs {
 // rewrites the two-phase fields of `out` (status, pair) as the reference's
 // publication does.
 cudaError_t launch_max3(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
-                        const double* z, const DeviceOutputs& out, const Max3Outputs& out3, cudaStream_t stream);
+                        const double* z, const DeviceOutputs& out, const Max3Outputs& out3, cudaStream_t stream,
+                        const Hints& hints = Hints{});
 
 // Closure constants of a selected-phase property chart call (pr76_chart.cuh),
 // passed to the kernel by value.
@@ -122,7 +137,8 @@ int capacity_for(int n);
 
 // Plain FP64 flash, one thread per cell (flash_plain.cu).
 cudaError_t launch_plain(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
-                         const double* z, const DeviceOutputs& out, cudaStream_t stream);
+                         const double* z, const DeviceOutputs& out, cudaStream_t stream,
+                         const Hints& hints = Hints{});
 
 // Implicit sensitivity of accepted two-phase cells (sensitivity.cu); reads the
 // flash fields of `out` (status, beta, x, y, lnk, z_l, z_v), which must be set.
@@ -131,12 +147,13 @@ cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const
 
 #define MPMC_DECLARE_PLAIN(NM)                                                                         \
     cudaError_t launch_plain_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t, \
-                                    const double* z, const DeviceOutputs& out, cudaStream_t stream); \
+                                    const double* z, const DeviceOutputs& out, cudaStream_t stream,       \
+                                    const Hints& hints);                                                  \
     cudaError_t launch_sensitivity_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t, \
                                           const double* z, const DeviceOutputs& out, cudaStream_t stream); \
     cudaError_t launch_max3_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t,      \
                                    const double* z, const DeviceOutputs& out, const Max3Outputs& out3,           \
-                                   cudaStream_t stream);                                                          \
+                                   cudaStream_t stream, const Hints& hints);                                      \
     cudaError_t launch_chart_nm##NM(const Mixture* d_mix, const ChartParams& params, int64_t ncell,           \
                                     const double* q, const int32_t* dep, const ChartOutputs& out,               \
                                     cudaStream_t stream);                                                        \

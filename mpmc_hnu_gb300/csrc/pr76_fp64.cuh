@@ -974,7 +974,7 @@ __device__ bool normalise_feed(Cell<NM>& c, const double* feed) {
 }
 
 // `init_extra` (n_init of them) join the automatic feed-test starts and
-// `final_extra` (n_final, at most 2) precede the pair's x and y in the review,
+// `final_extra` (n_final, at most 3) precede the pair's x and y in the review,
 // as solve_pt_vle's initial_starts / final_starts (pt_split.hpp:415-419, 512).
 template <int NM>
 __device__ MPMC_FP64_CALL int solve_cell(const Mixture& m, Cell<NM>& c, const double* feed_in, Scratch<NM>& w,
@@ -1065,9 +1065,9 @@ __device__ MPMC_FP64_CALL int solve_cell(const Mixture& m, Cell<NM>& c, const do
     for (int i = 0; i < n; ++i) w.imposed[i] = c.z[i] > 0.0 ? cand.common[i] - c.lz[i] : 0.0;
     bool final_negative = false, final_stationary = true;
     int fevals = 0;
-    const double* review_extra[4];
+    const double* review_extra[5];
     int n_review = 0;
-    for (int k = 0; k < n_final && k < 2; ++k) {
+    for (int k = 0; k < n_final && k < 3; ++k) {
         if (!start_matches_feed(c, final_extra[k])) return kInvalid;
         review_extra[n_review++] = final_extra[k];
     }

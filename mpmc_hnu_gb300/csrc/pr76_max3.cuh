@@ -397,9 +397,15 @@ __device__ MPMC_FP64_CALL int three_review(const Mixture& m, Cell<NM>& c, Max3Sc
 
 // solve_pr76_pt_max3 from a phase_set_unstable two-phase answer with ln K `lnk`.
 // `feed` is the raw feed; c.p, c.t and the temperature constants are set.
+// Caller starts (pr76_three_phase.hpp:328-358): `hints` (n_hints <= 3) are
+// the extra final-review starts the base solve ran with, ahead of the pair,
+// and `three_hint` (3 n compositions, then the fractions of phases 1 and 2)
+// is a three-phase start whose attempts run first, one per combination of
+// root sides (:457-486), with their own quota of 16.
 template <int NM>
 __device__ Max3Result max3_cell(const Mixture& m, Cell<NM>& c, const double* feed, const double* lnk,
-                                Max3Scratch<NM>& s) {
+                                Max3Scratch<NM>& s, const double* const* hints = nullptr, int n_hints = 0,
+                                const double* three_hint = nullptr) {
     const int n = c.n;
     Max3Result r{kM3Indeterminate, false, false};
     c.newton = false;  // the reference's bisection roots and RR
@@ -429,13 +435,94 @@ __device__ Max3Result max3_cell(const Mixture& m, Cell<NM>& c, const double* fee
     double common[NM];
     for (int i = 0; i < n; ++i) common[i] = s.lnphi[i];
     const StabilityOptions fo{1e-10 + 0.5 * base_fug, cFinalEvals};
-    const double* base_extra[2] = {s.fr_x, s.fr_y};
+    if (n_hints > 3) n_hints = 3;
+    const double* base_extra[5];
+    int n_extra = 0;
+    for (int k = 0; k < n_hints; ++k) base_extra[n_extra++] = hints[k];
+    base_extra[n_extra++] = s.fr_x;
+    base_extra[n_extra++] = s.fr_y;
     bool saw_higher = false, saw_boundary = false;
+    // One three-phase attempt from the seeds in s.t.lk1 / lk2, run_attempt of
+    // pr76_three_phase.hpp:379-455: true when it settles the cell (r is set).
+    auto attempt = [&](const double fr[2], const bool upper[3]) -> bool {
+        // the attempt iterates on the once-normalised feed normalised again
+        if (!normalise_feed(c, s.z1)) {
+            r.status = -1;
+            return true;
+        }
+        int disappearing = -1;
+        const int st = iterate_three(m, c, fr, upper, s.t, disappearing);
+        if (st == kTPhaseDisappearance) {
+            saw_boundary = true;
+            const double* starts[2];
+            int ns2 = 0;
+            for (int ph = 0; ph < 3; ++ph)
+                if (ph != disappearing) starts[ns2++] = s.t.point.x[ph];
+            if (ns2 == 2) {
+                // fresh two-phase solve with the surviving phases as initial and final starts
+                CellResult<NM> nb;
+                double nfeed[NM];
+                for (int i = 0; i < n; ++i) nfeed[i] = s.z1[i];
+                // the surviving compositions are copied out: solve_cell reuses s.w
+                double keep[2][NM];
+                for (int i = 0; i < n; ++i) {
+                    keep[0][i] = starts[0][i];
+                    keep[1][i] = starts[1][i];
+                }
+                const double* kst[2] = {keep[0], keep[1]};
+                const int nst = solve_cell(m, c, nfeed, s.w, nb, kst, 2, kst, 2);
+                c.newton = false;
+                if (nst == kTwoPhase) {
+                    r.status = kM3Two;
+                    r.has_pair = true;  // s.w.best
+                    return true;
+                }
+            }
+            // back to the base review's state for the next trials
+            if (!normalise_feed(c, s.z1)) {
+                r.status = -1;
+                return true;
+            }
+            // solve_cell changed the temperature constants only by recomputing them
+        } else if (st == kTConverged) {
+            const int fin = three_review(m, c, s);
+            if (fin < 0) {
+                r.status = -1;
+                return true;
+            }
+            if (fin == 1) {
+                r.status = kM3Three;
+                r.has_three = true;
+                return true;
+            }
+            if (fin == 0) saw_higher = true;
+        }
+        // the base review continues on its own feed
+        if (!normalise_feed(c, s.z1)) {
+            r.status = -1;
+            return true;
+        }
+        return false;
+    };
+    // the caller's three-phase start first, every combination of root sides
+    if (three_hint != nullptr) {
+        const double* x0 = three_hint;
+        const double* x1 = three_hint + n;
+        const double* x2 = three_hint + 2 * n;
+        const double fr[2] = {three_hint[3 * n], three_hint[3 * n + 1]};
+        if (log_ratio(c, x1, x0, s.t.lk1) && log_ratio(c, x2, x0, s.t.lk2)) {
+            for (int side = 0; side < 8; ++side) {
+                const bool upper[3] = {(side & 4) != 0, (side & 2) != 0, (side & 1) != 0};
+                // the seeds stay in s.t.lk1 / lk2: iterate_three only reads them
+                if (attempt(fr, upper)) return r;
+            }
+        }
+    }
     int attempts = 0;
     bool limit = false;
     int review_evals = 0;
     const bool have_lk1 = log_ratio(c, s.fr_y, s.fr_x, s.t.lk1);
-    for (int k = 0; k < n_auto + 2 && !limit; ++k) {
+    for (int k = 0; k < n_auto + n_extra && !limit; ++k) {
         // base review trial k (pt_split.hpp:509-510), as the reference ran it
         for (int i = 0; i < n; ++i) s.imposed[i] = c.z[i] > 0.0 ? common[i] - c.lz[i] : 0.0;
         make_start(c, k, active, base_extra, n_auto, s.witness.w);
@@ -454,66 +541,10 @@ __device__ Max3Result max3_cell(const Mixture& m, Cell<NM>& c, const double* fee
                 break;
             }
             ++attempts;
-            // the attempt iterates on the once-normalised feed normalised again
-            if (!normalise_feed(c, s.z1)) {
-                r.status = -1;
-                return r;
-            }
             const double fr[2] = {(1.0 - 0.1) * s.beta_v, 0.1};
             const bool upper[3] = {false, true, sides[q]};
             // the seeds: source ln K1 = ln(y/x), ln K2 = ln(witness/x) (kept in s.t.lk1 / lk2)
-            int disappearing = -1;
-            const int st = iterate_three(m, c, fr, upper, s.t, disappearing);
-            if (st == kTPhaseDisappearance) {
-                saw_boundary = true;
-                const double* starts[2];
-                int ns2 = 0;
-                for (int ph = 0; ph < 3; ++ph)
-                    if (ph != disappearing) starts[ns2++] = s.t.point.x[ph];
-                if (ns2 == 2) {
-                    // fresh two-phase solve with the surviving phases as initial and final starts
-                    CellResult<NM> nb;
-                    double nfeed[NM];
-                    for (int i = 0; i < n; ++i) nfeed[i] = s.z1[i];
-                    // the surviving compositions are copied out: solve_cell reuses s.w
-                    double keep[2][NM];
-                    for (int i = 0; i < n; ++i) {
-                        keep[0][i] = starts[0][i];
-                        keep[1][i] = starts[1][i];
-                    }
-                    const double* kst[2] = {keep[0], keep[1]};
-                    const int nst = solve_cell(m, c, nfeed, s.w, nb, kst, 2, kst, 2);
-                    c.newton = false;
-                    if (nst == kTwoPhase) {
-                        r.status = kM3Two;
-                        r.has_pair = true;  // s.w.best
-                        return r;
-                    }
-                }
-                // back to the base review's state for the next trials
-                if (!normalise_feed(c, s.z1)) {
-                    r.status = -1;
-                    return r;
-                }
-                // solve_cell changed the temperature constants only by recomputing them
-            } else if (st == kTConverged) {
-                const int fin = three_review(m, c, s);
-                if (fin < 0) {
-                    r.status = -1;
-                    return r;
-                }
-                if (fin == 1) {
-                    r.status = kM3Three;
-                    r.has_three = true;
-                    return r;
-                }
-                if (fin == 0) saw_higher = true;
-            }
-            // the base review continues on its own feed
-            if (!normalise_feed(c, s.z1)) {
-                r.status = -1;
-                return r;
-            }
+            if (attempt(fr, upper)) return r;
         }
     }
     r.status = saw_higher ? kM3Higher : (saw_boundary ? kM3Boundary : kM3Indeterminate);

@@ -75,6 +75,12 @@ class _ThreePhaseOutputs(ctypes.Structure):
     _fields_ = [(f, ctypes.c_void_p) for f, _, _ in THREE_PHASE_FIELDS]
 
 
+# caller start hints of the hinted max-3-phase solve (mpmc_start_hints)
+class _StartHints(ctypes.Structure):
+    _fields_ = [("count", ctypes.c_void_p), ("composition", ctypes.c_void_p), ("three_phase", ctypes.c_void_p),
+                ("fraction", ctypes.c_void_p)]
+
+
 # selected-phase property chart (mpmc_property_chart_spec / _outputs)
 class _ChartSpec(ctypes.Structure):
     _fields_ = [("phase_count", ctypes.c_int32), ("root_index", ctypes.c_int32 * 3),
@@ -134,7 +140,8 @@ EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu
                     "mpmc_flash_server_submit", "mpmc_flash_server_wait", "mpmc_flash_server_stats",
                     "mpmc_flash_server_destroy", "mpmc_gpu_flash_set_launch_shape", "mpmc_gpu_flash_solve_warm",
                     "mpmc_gpu_flash_solve_device_warm", "mpmc_gpu_flash_solve_max3", "mpmc_gpu_flash_solve_device_max3",
-                    "mpmc_gpu_flash_property_chart", "mpmc_gpu_flash_property_chart_device"]
+                    "mpmc_gpu_flash_property_chart", "mpmc_gpu_flash_property_chart_device",
+                    "mpmc_gpu_flash_solve_hinted", "mpmc_gpu_flash_solve_device_hinted"]
 FLAG_CUDA_GRAPH = 2
 NOALLOC_SCRATCH_BYTES = 48 << 20
 BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun", "fallback_nonsmooth",
@@ -176,6 +183,10 @@ def library() -> ctypes.CDLL:
             [ctypes.POINTER(_Outputs), ctypes.POINTER(_ThreePhaseOutputs)]
         lib.mpmc_gpu_flash_solve_device_max3.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 3 + \
             [ctypes.POINTER(_Outputs), ctypes.POINTER(_ThreePhaseOutputs), ctypes.c_void_p]
+        lib.mpmc_gpu_flash_solve_hinted.argtypes = [ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 3 + \
+            [ctypes.POINTER(_StartHints), ctypes.POINTER(_Outputs), ctypes.POINTER(_ThreePhaseOutputs)]
+        lib.mpmc_gpu_flash_solve_device_hinted.argtypes = lib.mpmc_gpu_flash_solve_hinted.argtypes + \
+            [ctypes.c_void_p]
         lib.mpmc_gpu_flash_property_chart.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(_ChartSpec),
                                                       ctypes.c_void_p, ctypes.c_void_p,
                                                       ctypes.POINTER(_ChartOutputs)]
@@ -292,6 +303,47 @@ class GpuFlash:
         s3 = _ThreePhaseOutputs(**{f: v.ctypes.data for f, v in out3.items()})
         _check(library().mpmc_gpu_flash_solve_max3(self._h, ncell, p.ctypes.data, t.ctypes.data, z.ctypes.data,
                                                    ctypes.byref(s), ctypes.byref(s3)))
+        return ({f: (v[0] if rows[f] == 1 else v) for f, v in out.items()},
+                {f: (v[0] if v.shape[0] == 1 else v) for f, v in out3.items()})
+
+    def solve_hinted(self, p, t, z, count, composition, three_phase=None, fraction=None,
+                     fields: list[str] | None = None):
+        """`solve_max3` with caller start hints (mpmc_gpu_flash_solve_hinted):
+        count [ncell] (0..3) compositions composition [3 n, ncell] per cell as
+        extra stability starts; three_phase [ncell] (nonzero: a three-phase
+        start, count 3) with its phase-1 and phase-2 fractions fraction
+        [2, ncell].  Runs the reference algorithm in FP64 for every form.
+        Returns (flash outputs, three-phase outputs)."""
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        z = np.ascontiguousarray(z, dtype=np.float64)
+        if z.shape != (self.n, p.shape[0]) or t.shape != p.shape:
+            raise ValueError("expected p[ncell], t[ncell], z[n, ncell]")
+        ncell = p.shape[0]
+        cnt = np.ascontiguousarray(count, dtype=np.int32)
+        comp = np.ascontiguousarray(composition, dtype=np.float64)
+        if cnt.shape != (ncell,) or comp.shape != (3 * self.n, ncell):
+            raise ValueError("expected count[ncell] and composition[3 n, ncell]")
+        three = frac = None
+        if three_phase is not None:
+            three = np.ascontiguousarray(three_phase, dtype=np.int32)
+            frac = np.ascontiguousarray(fraction, dtype=np.float64)
+            if three.shape != (ncell,) or frac.shape != (2, ncell):
+                raise ValueError("expected three_phase[ncell] and fraction[2, ncell]")
+        hints = _StartHints(cnt.ctypes.data, comp.ctypes.data, three.ctypes.data if three is not None else None,
+                            frac.ctypes.data if frac is not None else None)
+        fields = fields or self.fields()
+        for need in ("status", "ln_k"):
+            if need not in fields:
+                fields = fields + [need]
+        rows = output_rows(self.n)
+        dtypes = {f: d for f, d, _ in OUTPUT_FIELDS}
+        out = {f: np.empty((rows[f], ncell), dtypes[f]) for f in fields}
+        out3 = {f: np.empty((r(self.n), ncell), d) for f, d, r in THREE_PHASE_FIELDS}
+        s = _Outputs(**{f: out[f].ctypes.data for f in fields})
+        s3 = _ThreePhaseOutputs(**{f: v.ctypes.data for f, v in out3.items()})
+        _check(library().mpmc_gpu_flash_solve_hinted(self._h, ncell, p.ctypes.data, t.ctypes.data, z.ctypes.data,
+                                                     ctypes.byref(hints), ctypes.byref(s), ctypes.byref(s3)))
         return ({f: (v[0] if rows[f] == 1 else v) for f, v in out.items()},
                 {f: (v[0] if v.shape[0] == 1 else v) for f, v in out3.items()})
 

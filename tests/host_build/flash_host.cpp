@@ -1,0 +1,152 @@
+// Host build of the plain FP64 flash and the max-3-phase continuation with
+// caller start hints (test infrastructure only).
+//
+// Compiles the device functions the plain and max3 kernels run per cell --
+// fp64::solve_cell (pr76_fp64.cuh), fp64::max3_cell (pr76_max3.cuh) and the
+// hint loader (pr76_hints.cuh) -- with the host C++ compiler and applies the
+// kernels' per-cell sequence: the plain flash with the cell's hints as extra
+// feed-test and final-review starts, then, for a phase_set_unstable answer,
+// the continuation with the same hints and the three-phase start, and the
+// publication of pt_phase_set.hpp:91-150.  The tests check it against the
+// reference's recorded max3 statuses and hint-seeded continuation.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+
+using std::isfinite;
+struct HostDim3 {
+    unsigned x, y, z;
+};
+static HostDim3 threadIdx{0, 0, 0}, blockDim{1, 1, 1};
+static inline void __syncthreads() {}
+
+#include "launch.h"
+#include "pr76_hints.cuh"
+
+namespace {
+
+void prepare(int n, const double* tc, const double* pc, const double* omega, const double* kij, pr76::Mixture& m) {
+    std::memset(&m, 0, sizeof(m));
+    m.n = n;
+    for (int i = 0; i < n; ++i) {
+        m.sqrt_tc[i] = std::sqrt(tc[i]);
+        m.kappa[i] = 0.37464 + omega[i] * (1.54226 - 0.26992 * omega[i]);
+        const double rtc = pr76::kR * tc[i];
+        m.ac[i] = (0.45724 * rtc) * (rtc / pc[i]);
+        m.b[i] = (0.07780 * rtc) / pc[i];
+    }
+    for (int k = 0; k < n * n; ++k) m.factor[k] = 1.0 - kij[k];
+}
+
+struct Outputs {
+    int32_t* published;  // MPMC_FLASH_* (4 = three phases)
+    int32_t* max3;       // MPMC_MAX3_*, -1 invalid
+    double* x;           // [n * ncell] the published pair, or the feed for one phase
+    double* y;           // [n * ncell]
+    double* x3;          // [3 * n * ncell] the three-phase set
+    double* f3;          // [3 * ncell]
+};
+
+template <int NM>
+void run(const pr76::Mixture& m, int64_t ncell, const double* p, const double* t, const double* z,
+         const pr76::Hints& hints, const Outputs& o) {
+    using namespace pr76;
+    using namespace pr76::fp64;
+    const int n = m.n;
+    auto w = std::make_unique<Scratch<NM>>();
+    auto s = std::make_unique<Max3Scratch<NM>>();
+    for (int64_t cell = 0; cell < ncell; ++cell) {
+        const double nan = std::nan("");
+        for (int i = 0; i < n; ++i) o.x[i * ncell + cell] = o.y[i * ncell + cell] = nan;
+        for (int q = 0; q < 3; ++q) {
+            o.f3[q * ncell + cell] = nan;
+            for (int i = 0; i < n; ++i) o.x3[(q * n + i) * ncell + cell] = nan;
+        }
+        Cell<NM> c;
+        c.n = n;
+        c.newton = false;
+        c.p = p[cell];
+        c.t = t[cell];
+        for (int k = 0; k < cCount; ++k) c.counters[k] = 0;
+        double feed[NM];
+        for (int i = 0; i < n; ++i) feed[i] = z[i * ncell + cell];
+        CellResult<NM> r;
+        r.has_pair = false;
+        CellHints<NM> hs;
+        const bool ok = load_hints<NM>(hints, feed, n, ncell, cell, hs);
+        const double* const* extra = hs.count > 0 ? hs.ptr : nullptr;
+        const int status = ok ? solve_cell(m, c, feed, *w, r, extra, hs.count, extra, hs.count) : kInvalid;
+        int published = status;
+        int m3 = status == kSinglePhase ? kM3Single : status == kTwoPhase ? kM3Two : status == kInvalid ? -1
+                                                                                                  : kM3Indeterminate;
+        if (status == kSinglePhase)
+            for (int i = 0; i < n; ++i) o.x[i * ncell + cell] = c.z[i];
+        if (status == kTwoPhase || status == kPhaseSetUnstable)
+            for (int i = 0; i < n; ++i) {
+                o.x[i * ncell + cell] = w->best.x[i];
+                o.y[i * ncell + cell] = w->best.y[i];
+            }
+        if (status == kPhaseSetUnstable) {
+            double lnk[NM];
+            for (int i = 0; i < n; ++i) lnk[i] = w->best.lnk[i];
+            Cell<NM> c2;
+            c2.n = n;
+            c2.newton = false;
+            c2.p = p[cell];
+            c2.t = t[cell];
+            for (int k = 0; k < cCount; ++k) c2.counters[k] = 0;
+            Max3Result mr{kM3Indeterminate, false, false};
+            if (temp_setup(m, c2))
+                mr = max3_cell(m, c2, feed, lnk, *s, extra, hs.count, hs.has_three ? hs.three : nullptr);
+            else
+                mr.status = -1;
+            m3 = mr.status;
+            published = kIndeterminate;
+            bool clear = true;
+            if (m3 == kM3Three) {
+                published = MPMC_THREE_PHASE_STATUS;
+                for (int q = 0; q < 3; ++q) {
+                    o.f3[q * ncell + cell] = s->t.point.fraction[q];
+                    for (int i = 0; i < n; ++i) o.x3[(q * n + i) * ncell + cell] = s->t.point.x[q][i];
+                }
+            } else if (m3 == kM3Two && mr.has_pair) {
+                published = kTwoPhase;
+                clear = false;
+                for (int i = 0; i < n; ++i) {
+                    o.x[i * ncell + cell] = s->w.best.x[i];
+                    o.y[i * ncell + cell] = s->w.best.y[i];
+                }
+            } else if (m3 == kM3Higher) {
+                published = kPhaseSetUnstable;
+                clear = false;
+            } else if (m3 < 0) {
+                published = kInvalid;
+            }
+            if (clear)
+                for (int i = 0; i < n; ++i) o.x[i * ncell + cell] = o.y[i * ncell + cell] = nan;
+        }
+        o.published[cell] = published;
+        o.max3[cell] = m3;
+    }
+}
+
+}  // namespace
+
+extern "C" int host_hinted_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                                 int64_t ncell, const double* p, const double* t, const double* z,
+                                 const int32_t* hint_count, const double* hint_x, const int32_t* three,
+                                 const double* fraction, int32_t* published, int32_t* max3, double* x, double* y,
+                                 double* x3, double* f3) {
+    if (n < 2 || n > pr76::kMaxC) return 1;
+    pr76::Mixture m;
+    prepare(n, tc, pc, omega, kij, m);
+    const pr76::Hints hints{hint_count, hint_x, three, fraction};
+    const Outputs o{published, max3, x, y, x3, f3};
+    if (n <= 4) run<4>(m, ncell, p, t, z, hints, o);
+    else if (n <= 12) run<12>(m, ncell, p, t, z, hints, o);
+    else run<20>(m, ncell, p, t, z, hints, o);
+    return 0;
+}

@@ -103,3 +103,10 @@ def test_chart_shape():
     assert flash.chart_shape(10, 1) == (15, 11)
     assert flash.chart_shape(10, 2) == (40, 21)
     assert flash.chart_shape(3, 3) == (30, 10)
+
+
+def test_null_arguments_of_the_hinted_entries(lib):
+    """The hinted entries validate before any device work."""
+    assert lib.mpmc_gpu_flash_solve_hinted(None, 1, None, None, None, None, None, None) == 1
+    assert lib.mpmc_gpu_flash_solve_device_hinted(None, 1, None, None, None, None, None, None, None) == 1
+    assert b"null handle" in lib.mpmc_gpu_flash_last_error()

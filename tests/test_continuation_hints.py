@@ -1,0 +1,104 @@
+"""The device code of the hinted max-3-phase solve, built for the host, and
+the hint-seeded scan of mpmc_hnu_gb300/continuation.py over it.
+
+tests/host_build/flash_host.cpp compiles the per-cell functions of the plain
+and max3 kernels (fp64::solve_cell, fp64::max3_cell, fp64::load_hints) with
+the host compiler and applies the kernels' per-cell sequence.  On the CPU:
+
+1. without hints it reproduces every max3 status of the reference's
+   solve_pr76_pt_max3 on the recorded fixture cells
+   (tests/golden/max3_reference.npz);
+2. continuation.scan_with_hints over it reproduces the reference's
+   hint-seeded solve_pr76_pt_continuation on every recorded point
+   (tests/golden/continuation_reference.npz), including the 63 points where
+   the hints change the answer;
+3. a three-phase start outside the simplex makes the cell an invalid
+   request, as the reference's start check throws.
+"""
+
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from mpmc_hnu_gb300 import continuation, synth
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+@pytest.fixture(scope="module")
+def host_flash(tmp_path_factory):
+    cxx = shutil.which("g++")
+    cuda_inc = "/usr/local/cuda/include"
+    if not cxx or not os.path.exists(os.path.join(cuda_inc, "cuda_runtime.h")):
+        pytest.skip("host compiler or CUDA headers missing")
+    so = str(tmp_path_factory.mktemp("flash_host") / "libflash_host.so")
+    subprocess.check_call([cxx, "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-Wno-attributes",
+                           "-I" + cuda_inc, "-I" + os.path.join(ROOT, "include"),
+                           "-I" + os.path.join(ROOT, "mpmc_hnu_gb300", "csrc"),
+                           os.path.join(HERE, "host_build", "flash_host.cpp"), "-o", so])
+    lib = ctypes.CDLL(so)
+
+    def make_step(mix):
+        tc, pc, om, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
+
+        def step(p, t, z, count, hx, three, frac):
+            n, ncell = z.shape
+            outs = {"published": np.empty(ncell, np.int32), "max3": np.empty(ncell, np.int32),
+                    "x": np.empty((n, ncell)), "y": np.empty((n, ncell)), "x3": np.empty((3 * n, ncell)),
+                    "f3": np.empty((3, ncell))}
+            args = [np.ascontiguousarray(a, dtype=dt) for a, dt in
+                    ((p, np.float64), (t, np.float64), (z, np.float64), (count, np.int32), (hx, np.float64),
+                     (three, np.int32), (frac, np.float64))]
+            rc = lib.host_hinted_batch(ctypes.c_int(n), *[ctypes.c_void_p(a.ctypes.data) for a in (tc, pc, om, kij)],
+                                       ctypes.c_int64(ncell), *[ctypes.c_void_p(a.ctypes.data) for a in args],
+                                       *[ctypes.c_void_p(outs[k].ctypes.data)
+                                         for k in ("published", "max3", "x", "y", "x3", "f3")])
+            assert rc == 0
+            return outs
+
+        return step
+
+    return make_step
+
+
+def _no_hints(n, ncell):
+    return (np.zeros(ncell, np.int32), np.zeros((3 * n, ncell)), np.zeros(ncell, np.int32), np.zeros((2, ncell)))
+
+
+def test_device_max3_without_hints_matches_reference(host_flash):
+    d = np.load(os.path.join(HERE, "golden", "max3_reference.npz"))
+    mix = synth.three_phase_fixture_mixture()
+    z = np.ascontiguousarray(d["z"])
+    out = host_flash(mix)(d["p"], d["t"], z, *_no_hints(3, z.shape[1]))
+    assert np.array_equal(out["max3"], d["ref_max3_status"])
+    assert np.array_equal(out["published"], d["ref_published"])
+
+
+def test_hinted_scan_matches_reference_continuation(host_flash):
+    d = np.load(os.path.join(HERE, "golden", "continuation_reference.npz"))
+    mix = synth.three_phase_fixture_mixture()
+    res = continuation.scan_with_hints(host_flash(mix), d["z"], d["p"], d["t"])
+    assert np.array_equal(res["max3_status"], d["ref_max3_status"])
+    assert np.array_equal(res["status"], d["ref_published"])
+    settled = (d["ref_max3_status"] != d["ref_cold_max3_status"]) & (res["max3_status"] == 2)
+    assert settled.sum() == 63
+
+
+def test_invalid_three_phase_start_is_an_invalid_request(host_flash):
+    mix = synth.three_phase_fixture_mixture()
+    z = np.ascontiguousarray(synth.THREE_PHASE_ANCHOR.mean(axis=0)[:, None])
+    count, hx, three, frac = _no_hints(3, 1)
+    count[0] = 3
+    hx[:, 0] = synth.THREE_PHASE_ANCHOR.ravel()
+    three[0] = 1
+    frac[:, 0] = [0.7, 0.6]  # outside the simplex
+    out = host_flash(mix)(np.array([1e6]), np.array([250.0]), z, count, hx, three, frac)
+    assert out["published"][0] == -1 and out["max3"][0] == -1
+    frac[:, 0] = [0.3, 0.3]
+    out = host_flash(mix)(np.array([1e6]), np.array([250.0]), z, count, hx, three, frac)
+    assert out["published"][0] == 4 and out["max3"][0] == 2
