@@ -32,18 +32,16 @@ def test_continuation_equals_fresh_solves(gpu_lib, form):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("form", ["plain", "mixed"])
-def test_hinted_continuation_matches_reference(gpu_lib, form):
+def test_hinted_continuation_matches_reference(gpu_lib):
     """The reference's hint-seeded scan (mpmc_gpu_flash_solve_hinted) on the
     recorded fixture paths: every max3 and published status equals the
     reference's solve_pr76_pt_continuation, including the 63 points that the
-    hints settle as three-phase where a fresh solve ends indeterminate.  The
-    hinted entry runs the reference algorithm for every form."""
+    hints settle as three-phase where a fresh solve ends indeterminate."""
     import os
 
     d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "continuation_reference.npz"))
     mix = synth.three_phase_fixture_mixture()
-    res = continuation.solve_paths(mix, d["z"], d["p"], d["t"], form=form, hints=True)
+    res = continuation.solve_paths(mix, d["z"], d["p"], d["t"], hints=True)
     assert np.array_equal(res["max3_status"], d["ref_max3_status"])
     assert np.array_equal(res["status"], d["ref_published"])
     assert ((d["ref_max3_status"] != d["ref_cold_max3_status"]) & (res["max3_status"] == 2)).sum() == 63
