@@ -7,9 +7,9 @@ the live reference.
 
 The recorded scan also shows what the hints change: on these fixture paths
 the hint-seeded scan settles some points as three-phase that a fresh solve
-leaves indeterminate.  The GPU continuation (mpmc_hnu_gb300/continuation.py)
-reproduces fresh solves; carrying the reference's start hints through the C
-ABI is what would close that difference."""
+leaves indeterminate.  mpmc_hnu_gb300/continuation.py runs the same
+hint-seeded scan through mpmc_gpu_flash_solve_hinted
+(tests/test_continuation_hints.py, tests/test_gpu_continuation.py)."""
 
 import os
 
