@@ -245,6 +245,66 @@ def cpu_flash_rate(mix, p, t, z, threads: int, sens: bool):
 
 
 # ---------------------------------------------------------------------------
+# multi-mixture warm-start workload: 4 mixtures x cells at N = 4, 8, 12, 20
+CONFIG2_COMPONENTS = (4, 8, 12, 20)
+
+
+def multi_mixture_leg(flash, synth, torch, device: int, stream, ncell: int, form: str, warm_fraction: float):
+    """Per mixture (N = 4, 8, 12, 20; seeds 1104.., cells of the bench
+    generator): a cold solve gives each two-phase cell its converged ln K*;
+    then `warm_fraction` of ALL cells get ln K* + 0.1 N(0, 1) where they have
+    one (the rest start cold, Wilson K) and that warm solve is timed with CUDA
+    events on the launching stream, after one untimed warm-up of the same
+    call.  Flash without sensitivities.  Returns per-mixture and whole-job
+    flashes/s."""
+    rows_of = flash.output_rows
+    per, total_ms, total_cells = {}, 0.0, 0
+    dev = torch.device(f"cuda:{device}")
+    for n in CONFIG2_COMPONENTS:
+        mix = synth.make_mixture(n, 1100 + n)
+        p, t, z = synth.make_cells(n, ncell, 2100 + n)
+        dp, dt, dz = (torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (p, t, z))
+        rows = rows_of(n)
+        fields = ["status", "vapor_fraction", "liquid", "vapor", "ln_k", "z_liquid", "z_vapor"]
+        outs = {f: torch.empty((rows[f], ncell), dtype=torch.int32 if f == "status" else torch.float64, device=dev)
+                for f in fields}
+        ptrs = {f: v.data_ptr() for f, v in outs.items()}
+        g = flash.GpuFlash(mix, form, sensitivity=False, device=device)
+        stream.wait_stream(torch.cuda.current_stream(dev))
+        g.solve_device(ncell, dp.data_ptr(), dt.data_ptr(), dz.data_ptr(), ptrs, stream.cuda_stream)
+        torch.cuda.synchronize()
+        gen = torch.Generator(device=dev).manual_seed(17 + n)
+        two = outs["status"][0] == 1
+        pick = two & (torch.rand(ncell, device=dev, generator=gen) < warm_fraction)
+        warm = outs["ln_k"] + 0.1 * torch.randn(outs["ln_k"].shape, device=dev, dtype=torch.float64, generator=gen)
+        warm[:, ~pick] = float("nan")
+        warm = warm.contiguous()
+        cold_status = outs["status"][0].clone()
+        times = []
+        for _ in range(2):  # warm-up, then the timed call
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.solve_device(ncell, dp.data_ptr(), dt.data_ptr(), dz.data_ptr(), ptrs, stream.cuda_stream,
+                           warm_ptr=warm.data_ptr())
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        g.close()
+        ms = times[-1]
+        per[f"n{n}"] = {"value": ncell / (ms * 1e-3), "unit": "flashes/s", "ms": ms,
+                        "warm_cells": int(pick.sum().item()), "two_phase_cells": int(two.sum().item()),
+                        "status_agreement_with_cold": float((outs["status"][0] == cold_status).float().mean().item())}
+        total_ms += ms
+        total_cells += ncell
+        del outs, warm, dp, dt, dz
+    return {"value": total_cells / (total_ms * 1e-3), "unit": "flashes/s", "cells": total_cells, "form": form,
+            "per_mixture": per,
+            "setup": f"4 mixtures x {ncell} cells (N = 4, 8, 12, 20), ln K* of a cold solve + 0.1 N(0,1) on "
+                     f"{warm_fraction:.0%} of all cells where a pair converged, the rest cold; no sensitivities"}
+
+
+# ---------------------------------------------------------------------------
 # selected-phase property chart (the flow module's per-cell property and
 # Jacobian publication, mpmc_gpu_flash_property_chart)
 CHART_N, CHART_PHASES = 10, 2
@@ -507,6 +567,8 @@ def main() -> None:
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shape")
     ap.add_argument("--launch-shape", default="",
                     help="comma-separated mixed-form launch shape to use instead of autotuning")
+    ap.add_argument("--multi-mixture-cells", type=int, default=1 << 20,
+                    help="cells per mixture of the 4-mixture warm-start leg (0 = skip)")
     ap.add_argument("--chart-cells", type=int, default=1 << 20,
                     help="cells of the selected-phase property chart leg (0 = skip)")
     ap.add_argument("--serving-sweep", action="store_true",
@@ -781,7 +843,14 @@ def main() -> None:
         g.close()
         serving = serving_probe(flash, synth, device, args.serving_seconds, [0.7], log)
 
-    # the property chart runs last: a failure there leaves the flash line intact
+    # the secondary legs run last: a failure there leaves the flash line intact
+    multi = None
+    if rank == 0 and args.multi_mixture_cells > 0 and args.form in ("mixed", "batched"):
+        try:
+            multi = multi_mixture_leg(flash, synth, torch, device, stream, args.multi_mixture_cells, args.form,
+                                      args.warm_fraction)
+        except Exception as e:  # noqa: BLE001 - reported in the line
+            multi = {"error": f"{type(e).__name__}: {e}"}
     chart = None
     if rank == 0 and args.chart_cells > 0:
         try:
@@ -800,7 +869,7 @@ def main() -> None:
                 "data": f"synthetic (seeded generator; {placed} near-boundary cells placed by GPU bisection)",
                 "config": workload, "e2e": e2e, "gpu_launches": len(stages) * args.steps,
                 "roofline": roofline, "cpu_baseline": cpu, "plain_fp64": plain, "batched_fp64": batched,
-                "warm_start": warm_leg, "property_chart": chart,
+                "warm_start": warm_leg, "multi_mixture_warm": multi, "property_chart": chart,
                 "phase_counts": {"single": int((status == 0).sum()), "two": int((status == 1).sum()),
                                  "unstable": int((status == 2).sum()), "indeterminate": int((status == 3).sum()),
                                  "invalid": int((status == -1).sum())},
