@@ -1,6 +1,7 @@
 """The reference-side C++ bindings compile against the reference's own
 interfaces: mpmc_hnu_gb300/cpp/gpu_pr76_pt_flash_backend.hpp as a
-PtFlashBackend, and mpmc_hnu_gb300/cpp/gpu_pr76_selected_phase_property_chart.hpp
+PtFlashBackend, mpmc_hnu_gb300/cpp/gpu_pr76_pt_continuation.hpp with the
+reference's continuation types, and mpmc_hnu_gb300/cpp/gpu_pr76_selected_phase_property_chart.hpp
 beside the reference's flow property closure (its affine provider also
 instantiates the reference's own CPU closure and chart).
 
@@ -20,6 +21,12 @@ MODULES = ("ad", "thermodynamics", "flash", "physics", "flow", "mesh")
 
 SOURCE = r"""
 #include "gpu_pr76_pt_flash_backend.hpp"
+#include "gpu_pr76_pt_continuation.hpp"
+std::vector<mpmc::flash::GpuPr76PtContinuationResult> scan(
+    mpmc_gpu_flash* h, std::span<const std::vector<mpmc::flash::Pr76PtPathState>> paths,
+    std::span<const std::vector<double>> feeds) {
+    return mpmc::flash::solve_gpu_pr76_pt_continuation(h, paths, feeds);
+}
 #include <memory>
 #include <type_traits>
 static_assert(std::is_base_of_v<mpmc::flash::PtFlashBackend, mpmc::flash::GpuPr76PtFlashBackend>);
