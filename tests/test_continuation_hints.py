@@ -102,3 +102,39 @@ def test_invalid_three_phase_start_is_an_invalid_request(host_flash):
     frac[:, 0] = [0.3, 0.3]
     out = host_flash(mix)(np.array([1e6]), np.array([250.0]), z, count, hx, three, frac)
     assert out["published"][0] == 4 and out["max3"][0] == 2
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(os.environ.get("MPMC_REFERENCE_ROOT", "/root/reference"),
+                                                   "modules", "flash", "include")),
+                    reason="reference headers not present")
+def test_cpp_continuation_binding_matches_reference(tmp_path):
+    """mpmc_hnu_gb300/cpp/gpu_pr76_pt_continuation.hpp over the host build of
+    the device code (its three C-ABI calls provided by
+    tests/host_build/continuation_binding.cpp): every recorded point's max3
+    status and every path's brackets as the reference's continuation has them."""
+    ref_root = os.environ.get("MPMC_REFERENCE_ROOT", "/root/reference")
+    d = np.load(os.path.join(HERE, "golden", "continuation_reference.npz"))
+    exe = str(tmp_path / "continuation_binding")
+    cmd = ["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-Wno-attributes", "-I/usr/local/cuda/include",
+           "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "mpmc_hnu_gb300", "csrc"),
+           "-I" + os.path.join(ROOT, "mpmc_hnu_gb300", "cpp")]
+    cmd += ["-I" + os.path.join(ref_root, "modules", m, "include") for m in ("ad", "thermodynamics", "flash",
+                                                                               "physics")]
+    subprocess.check_call(cmd + [os.path.join(HERE, "host_build", "continuation_binding.cpp"),
+                                 os.path.join(HERE, "host_build", "flash_host.cpp"), "-o", exe])
+    inp = tmp_path / "paths.bin"
+    npath, npoint = d["p"].shape
+    with open(inp, "wb") as f:
+        f.write(np.array([npath, npoint], np.int64).tobytes())
+        for a in (d["p"], d["t"], d["z"]):
+            f.write(np.ascontiguousarray(a, np.float64).tobytes())
+    lines = subprocess.run([exe, str(inp)], capture_output=True, text=True, check=True).stdout.splitlines()
+    assert len(lines) == npath
+    ref = d["ref_max3_status"]
+    counts = continuation.phase_counts(d["ref_published"])
+    for k, line in enumerate(lines):
+        statuses, brackets = line.split("|")
+        assert [int(v) for v in statuses.split()] == list(ref[k])
+        expect = [(b[1], b[2]) for b in continuation.transition_brackets(counts[k:k + 1])]
+        got = [tuple(int(v) for v in b.split("-")) for b in brackets.split()[1:]]
+        assert got == expect
