@@ -138,3 +138,15 @@ def test_cpp_continuation_binding_matches_reference(tmp_path):
         expect = [(b[1], b[2]) for b in continuation.transition_brackets(counts[k:k + 1])]
         got = [tuple(int(v) for v in b.split("-")) for b in brackets.split()[1:]]
         assert got == expect
+
+
+def test_device_max3_on_six_components_matches_reference(host_flash):
+    """The six-component sour-gas fixture of the reference's tests
+    (tests/golden/max3_heringer_reference.npz): the host build of the device
+    code reproduces every max3 and published status."""
+    d = np.load(os.path.join(HERE, "golden", "max3_heringer_reference.npz"))
+    mix = synth.Mixture(d["tc"], d["pc"], d["omega"], d["kij"])
+    z = np.ascontiguousarray(d["z"])
+    out = host_flash(mix)(d["p"], d["t"], z, *_no_hints(6, z.shape[1]))
+    assert np.array_equal(out["max3"], d["ref_max3_status"])
+    assert np.array_equal(out["published"], d["ref_published"])

@@ -72,3 +72,27 @@ def test_max3_three_phase_sets_match_the_anchor(gpu_lib):
             worst = max(worst, np.abs(synth.THREE_PHASE_ANCHOR - x3[k, :, c]).max(axis=1).min())
     assert worst <= 1e-9, worst
     assert np.allclose(out3["phase_fraction"][:, three].sum(axis=0), 1.0, atol=1e-13)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", ["plain", "batched", "mixed"])
+def test_max3_matches_reference_on_six_components(gpu_lib, form):
+    """The reference tests' six-component Heringer-2026 sour-gas fixture along
+    its P-Z path (tests/golden/max3_heringer_reference.npz).  The plain form
+    reproduces every max3 status; the work-queue forms may differ where
+    their two-phase answer does (at most 1 in 200 here); three-phase sets
+    agree to 1e-9."""
+    d = np.load(os.path.join(os.path.dirname(GOLDEN), "max3_heringer_reference.npz"))
+    mix = synth.Mixture(d["tc"], d["pc"], d["omega"], d["kij"])
+    g = gpu_lib.GpuFlash(mix, form=form)
+    out, out3 = g.solve_max3(d["p"], d["t"], d["z"])
+    g.close()
+    ms, rs = out3["max3_status"], d["ref_max3_status"]
+    mismatch = np.nonzero(ms != rs)[0]
+    assert mismatch.size <= (0 if form == "plain" else len(ms) // 200)
+    same = ms == rs
+    assert np.array_equal(out["status"][same], d["ref_published"][same])
+    three = same & (rs == 2)
+    assert three.sum() > 50
+    err = np.abs(out3["composition"][:, three] - d["ref_x3"][:, three]).max()
+    assert err <= 1e-9, err

@@ -63,3 +63,16 @@ def test_oracle_max3_matches_live_reference(oracle_lib):
     b = oracle_lib.reference_max3(mix, p, t, z, threads=8)
     for k in a:
         assert _same(a[k], b[k]), k
+
+
+def test_oracle_max3_matches_recorded_reference_on_six_components(oracle_lib):
+    """The reference tests' six-component Heringer-2026 sour-gas fixture along
+    its own P-Z path (tests/golden/max3_heringer_reference.npz, written by
+    make_heringer_golden.py): every field bit-identical."""
+    d = np.load(os.path.join(os.path.dirname(GOLDEN), "max3_heringer_reference.npz"))
+    mix = synth.Mixture(d["tc"], d["pc"], d["omega"], d["kij"])
+    out = oracle_lib.max3(mix, d["p"], d["t"], d["z"], threads=8)
+    counts = np.bincount(d["ref_max3_status"] + 1, minlength=7)
+    assert counts[1] > 50 and counts[2] > 100 and counts[3] > 50
+    for k, v in out.items():
+        assert _same(v, d[f"ref_{k}"]), k
