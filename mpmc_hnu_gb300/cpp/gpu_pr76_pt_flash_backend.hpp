@@ -19,8 +19,9 @@
 // which is what the flow module's transition candidates need
 // (phase_set_transition_flash_adapter.hpp:130-248); an indeterminate result
 // from an unresolved two-phase or three-phase search carries none, since the
-// C ABI does not return the attempts behind it.  Not carried: caller start
-// hints (three_phase_starts, initial/final starts) and the phase metadata.
+// C ABI does not return the attempts behind it.  Caller starts are carried in
+// the form the C ABI takes (GpuPr76BackendStarts, below); not carried: the
+// phase metadata.
 //
 // Errors follow the reference's classes: an invalid request (feed size,
 // non-finite or non-positive p and T, a feed outside the simplex) throws
@@ -34,6 +35,7 @@
 
 #include <mpmc/flash/pt_flash_backend.hpp>
 
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <optional>
@@ -61,10 +63,28 @@ struct GpuPr76Mixture {
     std::string revision;
 };
 
+// Caller starts of the backend, the part of Pr76PtFlashBackendOptions
+// (pr76_pt_flash_backend.hpp:26-40) that the C ABI carries: up to three
+// compositions used as both initial_starts and final_starts and, when
+// `three_phase_fraction_seed` is set, one three-phase start made of the same
+// three compositions with that phase_fraction_seed (Pr76PtThreePhaseStart,
+// pr76_three_phase.hpp:114-117).  Every request of the backend gets them.
+struct GpuPr76BackendStarts {
+    std::vector<std::vector<double>> stability_starts;
+    std::optional<std::array<double, 2>> three_phase_fraction_seed;
+};
+
 class GpuPr76PtFlashBackend final : public PtFlashBackend {
 public:
-    explicit GpuPr76PtFlashBackend(const GpuPr76Mixture& mixture, int form = MPMC_FORM_MIXED, int device = 0)
-        : n_(mixture.component_ids.size()) {
+    explicit GpuPr76PtFlashBackend(const GpuPr76Mixture& mixture, int form = MPMC_FORM_MIXED, int device = 0,
+                                   GpuPr76BackendStarts starts = {})
+        : n_(mixture.component_ids.size()), starts_(std::move(starts)) {
+        if (starts_.stability_starts.size() > 3 ||
+            (starts_.three_phase_fraction_seed && starts_.stability_starts.size() != 3))
+            throw std::invalid_argument("GPU PR76 backend: at most three stability starts, exactly three with a "
+                                        "three-phase start");
+        for (const auto& st : starts_.stability_starts)
+            if (st.size() != n_) throw std::invalid_argument("GPU PR76 backend: start size does not match the mixture");
         if (n_ == 0 || mixture.critical_temperature_k.size() != n_ || mixture.critical_pressure_pa.size() != n_ ||
             mixture.acentric_factor.size() != n_ || mixture.kij.size() != n_ * n_)
             throw std::invalid_argument("GPU PR76 backend: mixture arrays do not match the component list");
@@ -151,9 +171,27 @@ public:
         std::vector<int32_t> max3(cells);
         std::vector<double> frac3(3 * cells), comp3(3 * n_ * cells), phi3(3 * n_ * cells), z3(3 * cells);
         mpmc_three_phase_outputs out3{max3.data(), frac3.data(), comp3.data(), phi3.data(), z3.data()};
-        if (cells > 0)
+        if (cells > 0 && starts_.stability_starts.empty()) {
             check(mpmc_gpu_flash_solve_max3(handle_, static_cast<int64_t>(cells), p.data(), t.data(), z.data(), &out,
                                             &out3));
+        } else if (cells > 0) {
+            // the backend's caller starts, the same for every request
+            const std::size_t k = starts_.stability_starts.size();
+            std::vector<int32_t> count(cells, static_cast<int32_t>(k)), three(cells, 0);
+            std::vector<double> comp(3 * n_ * cells, 0.0), frac(2 * cells, 0.0);
+            for (std::size_t c = 0; c < cells; ++c) {
+                for (std::size_t q = 0; q < k; ++q)
+                    for (std::size_t i = 0; i < n_; ++i) comp[(q * n_ + i) * cells + c] = starts_.stability_starts[q][i];
+                if (starts_.three_phase_fraction_seed) {
+                    three[c] = 1;
+                    frac[c] = (*starts_.three_phase_fraction_seed)[0];
+                    frac[cells + c] = (*starts_.three_phase_fraction_seed)[1];
+                }
+            }
+            const mpmc_start_hints hints{count.data(), comp.data(), three.data(), frac.data()};
+            check(mpmc_gpu_flash_solve_hinted(handle_, static_cast<int64_t>(cells), p.data(), t.data(), z.data(),
+                                              &hints, &out, &out3));
+        }
 
         std::vector<std::optional<PtFlashBackendResult>> results(cells);
         for (std::size_t c = 0; c < cells; ++c) {
@@ -282,6 +320,7 @@ private:
     }
 
     std::size_t n_;
+    GpuPr76BackendStarts starts_;
     mpmc_gpu_flash* handle_ = nullptr;
     PtFlashBackendCapability capability_;
 };

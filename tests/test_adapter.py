@@ -183,3 +183,28 @@ def test_batched_scan_follows_the_reference_rules(tmp_path):
     out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.splitlines()
     got = {line.split(" ", 1)[0]: line.split(" ", 1)[1] for line in out}
     assert got == SCAN_EXPECTED
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "tests", "flash", "pr76_three_phase")),
+                    reason="reference tests not present")
+@pytest.mark.skipif(shutil.which("g++") is None, reason="no g++")
+def test_seeded_backend_binding_matches_reference(tmp_path):
+    """GpuPr76PtFlashBackend with caller starts (GpuPr76BackendStarts) over the
+    host build of the device code, beside the reference's seeded
+    Pr76PtFlashBackend in the reference's own seeded-backend scenario
+    (pr76_max3_seeded_backend_test.cpp): both accept three phases with the
+    same compositions and publish the 2 -> 3 evidence."""
+    exe = str(tmp_path / "seeded_backend")
+    cmd = ["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-Wno-attributes", "-I/usr/local/cuda/include",
+           "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "mpmc_hnu_gb300", "csrc"),
+           "-I" + os.path.join(ROOT, "mpmc_hnu_gb300", "cpp"),
+           "-I" + os.path.join(REFERENCE, "tests", "flash", "pr76_three_phase")]
+    cmd += ["-I" + os.path.join(REFERENCE, "modules", m, "include") for m in ("ad", "thermodynamics", "flash",
+                                                                               "physics")]
+    subprocess.check_call(cmd + [os.path.join(ROOT, "tests", "host_build", "seeded_backend.cpp"),
+                                 os.path.join(ROOT, "tests", "host_build", "flash_host.cpp"), "-o", exe])
+    ref_status, got_status, ref_phases, got_phases, worst, ref_23, got_23 = \
+        subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    assert ref_status == got_status == "0" and ref_phases == got_phases == "3"
+    assert float(worst) <= 1e-12
+    assert ref_23 == got_23 == "1"
