@@ -384,7 +384,7 @@ def chart_leg(flash, synth, torch, device: int, stream, ncell: int, threads: int
         t0 = time.perf_counter()
         pyoracle.property_chart(mix, phases, [0, 0], spec.molar_mass, visc, enth, sel, None, threads=threads)
         dt = time.perf_counter() - t0
-        leg["cpu_baseline"] = {"value": sel.shape[1] / dt, "unit": "cells/s", "cores": threads, "kind": "reference",
+        leg["cpu_baseline"] = {"value": sel.shape[1] / dt, "unit": "cells/s", "cores": threads, "kind": "port",
                                "sample": f"{sel.shape[1]} of the same cells (every {ncell // sel.shape[1]}th), "
                                          f"{dt:.1f} s wall; the oracle is bit-identical to the reference's chart"}
     return leg
