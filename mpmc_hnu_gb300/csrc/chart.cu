@@ -37,7 +37,12 @@ cudaError_t MPMC_CAT(launch_chart_nm, MPMC_NM)(const Mixture* d_mix, const Chart
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const int block = 64;
-    int64_t grid = static_cast<int64_t>(sms) * 8;
+    // one wave: every SM holds as many blocks as its registers admit
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, chart_kernel<MPMC_NM>, block, 0) != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    int64_t grid = static_cast<int64_t>(sms) * per_sm;
     const int64_t needed = (ncell + block - 1) / block;
     if (grid > needed) grid = needed;
     chart_kernel<MPMC_NM><<<static_cast<unsigned>(grid), block, 0, stream>>>(d_mix, params, ncell, q, dep, out);
