@@ -2411,7 +2411,7 @@ inline int property_chart(const Model& m, const ChartSpec& spec, const double* q
             for (int i = 0; i < n; ++i)
                 out[prop + (ph - 1) * n + i] =
                     (log(x[0][i] / x[ph][i]) + lnphi[0][i]) - lnphi[ph][i] + log(p / p);
-        // the driver's output checks, runtime_differentiate.hpp:138-156
+        // the runtime Jacobian workspace's output checks, runtime_differentiate.hpp:138-156
         for (int r = 0; r < rows; ++r) {
             if (!finite(out[r])) return 6;
             if (col == 0 && values) values[r] = out[r].v;
