@@ -80,11 +80,11 @@ def test_max3_matches_reference_on_six_components(gpu_lib, form):
     """The reference tests' six-component Heringer-2026 sour-gas fixture along
     its P-Z path (tests/golden/max3_heringer_reference.npz).  The path
     crosses phase boundaries on purpose, and 26 of its 429 cells end
-    indeterminate at an iteration or evaluation limit.  The plain form may
-    differ on at most one cell, where the device's fused multiply-adds move
-    such a limit decision (its host build, without them, reproduces every
-    status); the work-queue forms may differ where their two-phase answer
-    does (at most 1 in 100); three-phase sets agree to 1e-9."""
+    indeterminate.  The plain form may differ on at most one cell, where the
+    device's fused multiply-adds move a decision of the finite search (its
+    host build, without them, reproduces every status); the work-queue forms
+    may differ where their two-phase answer does (at most 1 in 100);
+    three-phase sets agree to 1e-9."""
     d = np.load(os.path.join(os.path.dirname(GOLDEN), "max3_heringer_reference.npz"))
     mix = synth.Mixture(d["tc"], d["pc"], d["omega"], d["kij"])
     g = gpu_lib.GpuFlash(mix, form=form)
