@@ -388,8 +388,14 @@ int mpmc_gpu_flash_property_chart_device(mpmc_gpu_flash* handle, int64_t n_cells
  * buffers do not fit (about 4,900 cells at 20 components, 9,700 at 10, more
  * with fewer components) returns MPMC_ERR_INVALID_ARGUMENT with the size in
  * the message.  The first call on a device looks the array's address up
- * (cudaGetSymbolAddress, with that device current); make that first call
- * before any stream capture.  The call itself allocates nothing: it validates,
+ * (cudaGetSymbolAddress, with that device current), and the first launch of
+ * each of its kernels in the process lets the CUDA driver size the context's
+ * local-memory (stack) reservation for that kernel -- the implicit-sensitivity
+ * kernel has the largest frame, so with want_sensitivity the first call may
+ * grow that reservation.  Make one call of each kind (with and without
+ * sensitivities, at each component count used) before any stream capture
+ * and before entering code that must not allocate.  After that the call
+ * allocates nothing: it validates,
  * enqueues its kernels and a zeroing of the work counters on `stream`, and
  * returns without synchronising.  All handles on a device share the array, so
  * calls whose work overlaps on the device (two streams, or two host threads)
@@ -422,7 +428,7 @@ int mpmc_gpu_flash_set_launch_shape(mpmc_gpu_flash* handle, const int32_t* value
 /* Device time in milliseconds of every stage of the last solve on a handle
  * created with MPMC_FLAG_STAGE_TIMING (waits for that solve to finish).
  * Stages, in order -- plain form: flash, sensitivity; mixed form: setup,
- * feed_trials, feed_classify, feed_trials64, decide, split, polish, split64,
+ * feed_trials, feed_classify, feed_trials64, decide, split, polish, open32, compete, split64,
  * select64, relist, review_trials, review_classify, review_trials64, finish,
  * fallback, sensitivity.  Writes up to `capacity` values and returns the
  * number of stages (0 if timing is off or nothing ran).  Diagnostic entry
@@ -445,8 +451,10 @@ int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* handle, float* ms, int capacity
  * iteration limit without an FP64 run, [16] cells run from their ln K warm
  * start, [17] of those, cells whose pair was not accepted and that took the
  * cold pass, [18] of those, cells with no converged attempt, [19] of those,
- * cells whose review found a negative TPD.  After a warm-start solve,
- * [0]-[15] count the cold pass.
+ * cells whose review found a negative TPD, [20] cells whose polished pair
+ * waited on attempts that FP32 left open, [21] of those, cells where some open
+ * attempt could still change the selection and was continued in FP64.  After
+ * a warm-start solve, [0]-[15] count the cold pass and [20]-[21] both passes.
  * Writes up to `capacity` values; returns the number available (0 for the
  * plain form).  Diagnostic entry point with no counterpart in the reference. */
 int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* handle, int64_t* out, int capacity);

@@ -525,9 +525,9 @@ int mpmc_gpu_flash_components(const mpmc_gpu_flash* h) { return h ? h->n : 0; }
 int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* h, int64_t* out, int capacity) {
     if (!h || (h->form != MPMC_FORM_MIXED && h->form != MPMC_FORM_BATCHED) || !h->workspace.ptr) return 0;
     // workspace counter slots (pr76_batched.cuh Slot) in the documented order
-    constexpr int kSlots[] = {8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 20, 22, 23, 24, 25, 27, 28, 29, 30};
+    constexpr int kSlots[] = {8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 20, 22, 23, 24, 25, 27, 28, 29, 30, 31, 32};
     constexpr int kCount = static_cast<int>(sizeof(kSlots) / sizeof(kSlots[0]));
-    int vals[32] = {};
+    int vals[40] = {};
     if (cudaSetDevice(h->device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return 0;
     // the counters are the first array of the workspace
     if (cudaMemcpy(vals, h->workspace.ptr, sizeof(vals), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;

@@ -150,13 +150,19 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
         // FP32 successive substitution hands over to the FP64 Newton polish at
         // |r| <= ss_switch (default 2e-5, a few times the FP32 rounding floor)
         const float ss_switch = shape.ss_switch > 0.f ? shape.ss_switch : 2e-5f;
-        if (!fp64_items) split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t, ss_switch);
+        if (!fp64_items) split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t, ss_switch, 0);
         mark();
         // polish: one cell per thread up to 12 components (its per-cell arrays
         // still fit the cache), one cell per lane group above
         const bool lane_polish = (shape.item_form & 8) ? true : ((shape.item_form & 16) ? false : NM <= 12);
         if (lane_polish) polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
         else w64::polishw_kernel<NM, w64::kSeg<NM>><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t, out);
+        mark();
+        // attempts FP32 left open beside a polished pair: their FP32 prediction,
+        // then the pair's review or the FP64 continuation of what stays open
+        if (!fp64_items) split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t, ss_switch, 1);
+        mark();
+        compete_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t);
         mark();
         if ((shape.item_form & 4) && !fp64_items) split64_kernel<NM><<<sms * s64_res, 64, 0, stream>>>(d_mix, ws, p, t);
         else w64::split64w_kernel<NM, 32><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t);

@@ -67,7 +67,7 @@ struct BatchedShape {
     const double* warm_lnk;
     cudaEvent_t* redo_events;  // optional: the events of the cold pass after a warm pass
 };
-constexpr int kBatchedStages = 15;
+constexpr int kBatchedStages = 17;
 
 // Batched mixed-precision flash (flash_batched.cu): scratch bytes needed for
 // ncell cells, and the launch sequence using that scratch.

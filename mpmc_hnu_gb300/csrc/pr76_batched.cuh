@@ -15,9 +15,16 @@
 //                          attempts (witness order x {vapor, liquid}, <= 16)
 //   split32     per attempt persistent FP32 ln K successive substitution
 //   polish      per cell   minimum-Gibbs attempt, FP64 Newton polish of ln K
-//                          (FP64 residual, FP32 Jacobian: iterative
-//                          refinement), reference acceptance rules in FP64,
-//                          enqueue the N+4 common-tangent review trials
+//                          (closed-form FP64 Jacobian, chord iterations),
+//                          reference acceptance rules in FP64, enqueue the
+//                          N+4 common-tangent review trials
+//   open32      per attempt attempts FP32 left open near a pair beside a
+//                          polished one: FP32 prediction of where they
+//                          converge, pruning those that cannot change the
+//                          minimum-Gibbs selection
+//   compete     per cell   review the polished pair, or continue the attempts
+//                          still open exactly in FP64 (split64) and select
+//                          among them and the pair (select64)
 //   trials32    per trial  review trials against the FP64 common tangent
 //   finish      per cell   FP64 re-run of undecided review trials, final
 //                          status, outputs
@@ -57,6 +64,9 @@ enum Slot : int {
     qAttempts = 2,     // attempt items listed
     qAttemptCursor = 3,
     qFallback = 4,     // cells listed for the FP64 fallback
+    qOpenItems = 5,    // open attempts listed for the FP32 prediction (open32)
+    qOpenCursor = 6,
+    qCompeteCells = 7, // cells whose polished pair awaits the open attempts' outcome
     // diagnostic statistics of the last batch
     sFeedContinued = 8,    // feed trials finished in FP64 from the FP32 end point
     sFeedRerun = 9,        // feed trials re-run exactly in FP64
@@ -82,7 +92,9 @@ enum Slot : int {
     sWarmRedo = 28,        // of those, cells whose pair was not accepted (cold pass)
     sWarmNoPair = 29,      // ... because no attempt converged to an accepted pair
     sWarmUnstable = 30,    // ... because the review found a negative TPD
-    qSlots = 32
+    sCompeting = 31,       // cells whose polished pair waited on attempts FP32 left open
+    sCompeteFp64 = 32,     // ... of those, cells with open attempts left for the FP64 continuation
+    qSlots = 40
 };
 
 // Doubles per FP64 attempt result: gibbs, guard, fug, beta, z_l, z_v, 2 spare,
@@ -94,7 +106,8 @@ __host__ __device__ constexpr int S64Stride() { return 8 + 6 * NM; }
 enum Phase : int {
     pInvalid = -1, pSingle = 0, pTwo = 1, pUnstable = 2, pIndeterminate = 3,
     pPending = 10, pSplit = 11, pReview = 12, pFallback = 13, pSplit64 = 14,
-    pRedo = 15  // warm pass: the warm pair was not accepted, the cell runs the cold pass
+    pRedo = 15,  // warm pass: the warm pair was not accepted, the cell runs the cold pass
+    pCompete = 16  // a polished pair waits on the open attempts' predicted ends
 };
 
 // Passes of the launch sequence: the cold solve of every cell; the warm pass
@@ -123,7 +136,9 @@ struct Workspace {
     signed char* att_class; // [kMaxAttempts * ncell]
     int* att_count;         // [ncell]
     double* cand;           // [7 * NM * ncell]: x, y, lnk, lnphi_l, lnphi_v, common, imposed
-    double* cand_s;         // [8 * ncell]: beta, z_l, z_v, fug, gibbs_change, gibbs_guard, tpd_tol, spare
+    double* cand_s;         // [8 * ncell]: beta, z_l, z_v, fug, gibbs_change, gibbs_guard, tpd_tol, pair guard;
+                            // while FP64 continuations compete with a polished pair (phase pSplit64),
+                            // slots 4 and 6 hold that pair's Gibbs energy (NaN: none) and attempt order
     int* counters_out;      // [cCount * ncell] work counters (FP32 evaluations are in row 1/0/2)
     float* c32;             // [4 * NM * ncell] FP32 cell constants: z, ln z, a_i(T), sqrt(a_i)
     float* ref32;           // [NM * ncell] feed-phase ln phi rounded to FP32
@@ -766,7 +781,13 @@ struct SplitLane {
     float alpha, slope, scale;
     float fug0, ck_fug, rate;  // |r| at the seed, at the last checkpoint; contraction per iteration
     int ck_iter;
+    int limit;  // iteration count at which the lane stops: the reference's 512, or the prediction's cap
 };
+// Iterations the open-attempt prediction runs beyond an attempt's FP32 end
+// point: attempts near a pair converge within a few dozen (host runs of the
+// bench distributions at 4-20 components); one that has not converged by then
+// stays open for the FP64 continuation.
+constexpr int kPredictionIterations = 96;
 
 template <int NM>
 __device__ void split_step_or_finish(SplitLane<NM>& L, float ss_switch) {
@@ -778,7 +799,7 @@ __device__ void split_step_or_finish(SplitLane<NM>& L, float ss_switch) {
         L.ck_fug = L.point.fug;
         L.ck_iter = L.iter;
     }
-    if (L.point.fug <= ss_switch || L.iter >= 512) {
+    if (L.point.fug <= ss_switch || L.iter >= L.limit) {
         L.stage = 2;
         return;
     }
@@ -803,20 +824,61 @@ __device__ void split_step_or_finish(SplitLane<NM>& L, float ss_switch) {
     L.stage = 1;
 }
 
+// Prune decision of an open attempt at its predicted end (open pass of
+// split32_kernel): true when the attempt cannot change the cell's selection,
+// the first attempt of least Gibbs energy among those that converge
+// (pt_split.hpp:459-486) -- its predicted pair is trivial (the reference's
+// attempt would end indistinguishable, pt_split.hpp:351-362), is the polished
+// pair of the cell, or has a Gibbs energy clearly above the polished pair's.
+template <int NM>
+__device__ bool prune_open(const Workspace& ws, const SplitLane<NM>& L) {
+    const int n = L.cell.n;
+    const int64_t c = L.c;
+    float contrast = 0.f, dist = 0.f, big = 0.f;
+    for (int i = 0; i < n; ++i) {
+        if (L.cell.z[i] == 0.f) continue;
+        const float ck = static_cast<float>(ws.cand[idx(2 * NM + i, ws.ncell, c)]);
+        contrast = fmaxf(contrast, fabsf(L.point.lnk[i]));
+        dist = fmaxf(dist, fabsf(L.point.lnk[i] - ck));
+        big = fmaxf(big, fabsf(ck));
+    }
+    if (contrast < 1e-4f || L.point.z_v - L.point.z_l <= 1e-5f * fmaxf(L.point.z_v, L.point.z_l)) return true;
+    if (dist <= 1e-3f * (1.f + big)) return true;
+    const float gc = static_cast<float>(ws.cand_s[idx(4, ws.ncell, c)]);
+    return L.point.gibbs > gc + 1e-4f * (1.f + fabsf(gc));
+}
+
+// FP32 ln K successive substitution over a persistent work queue of attempts.
+// open == 0: every split attempt from its seed, with the reference's Gibbs
+// line search, classified at its end (fp32::SplitClass).
+// open == 1: the attempts the polish left open (class aFailed beside a
+// polished pair), continued from their FP32 end point to predict where they
+// converge.  Where FP32 cannot resolve the reference's Armijo test
+// (predicted decrease below the rounding guard) the step is taken when the
+// Gibbs energy does not rise beyond the guard, without the residual-decrease
+// rule that stopped the first pass.  The prediction only prunes attempts
+// (prune_open); the end point and class of a kept attempt stay as the first
+// pass left them, and the FP64 continuation decides it exactly.
 template <int NM>
 __global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict__ mix_g, Workspace ws,
                                                       const double* __restrict__ p, const double* __restrict__ t,
-                                                      float ss_switch) {
+                                                      float ss_switch, int open) {
     __shared__ Mixture m;
     stage_mixture(mix_g, m);
-    const int total = ws.counters[qAttempts];
+    const int total = ws.counters[open ? qOpenItems : qAttempts];
+    int* const cursor = &ws.counters[open ? qOpenCursor : qAttemptCursor];
     SplitLane<NM> L;
     L.stage = 3;
     L.item = -1;
     bool live = true;
     for (;;) {
         if (live && L.stage >= 2) {
-            if (L.item >= 0 && L.stage == 2) {
+            if (L.item >= 0 && L.stage == 2 && open) {
+                const bool converged = L.iter >= 0 && L.point.fug <= ss_switch;
+                if (converged && prune_open(ws, L))
+                    ws.att_class[idx(L.order, ws.ncell, L.c)] = static_cast<signed char>(fp32::aPruned);
+                atomicAdd(&ws.counters_out[idx(cSplitEvals, ws.ncell, L.c)], L.cell.evals);
+            } else if (L.item >= 0 && L.stage == 2) {
                 int cls = fp32::aFailed;
                 const int n = L.cell.n;
                 float contrast = 0.f;
@@ -835,6 +897,8 @@ __global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict_
                         cls = fp32::aLimit;  // FP32 and FP64 track each other far above the floor
                     else if (L.point.fug <= 1e-3f && static_cast<float>(L.iter) + needed <= 448.f)
                         cls = fp32::aConverged;  // converges well inside the 512-iteration budget
+                    else if (L.point.fug >= fp32::kFarFailure)
+                        cls = fp32::aFailedFar;  // stopped far from any pair
                     // else: unsettled, continued exactly in FP64 with the remaining budget
                     ws.att_rate[idx(L.order, ws.ncell, L.c)] = rate;
                 }
@@ -847,7 +911,7 @@ __global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict_
                 atomicAdd(&ws.counters_out[idx(cSplitEvals, ws.ncell, c)], L.cell.evals);
                 atomicAdd(&ws.counters_out[idx(cSplitIters, ws.ncell, c)], L.iter);
             }
-            L.item = atomicAdd(&ws.counters[qAttemptCursor], 1);
+            L.item = atomicAdd(cursor, 1);
             if (L.item >= total) {
                 live = false;
             } else {
@@ -855,10 +919,11 @@ __global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict_
                 L.c = code >> 5;
                 L.order = code & 31;
                 int active;
-                L.iter = 0;
+                L.iter = open ? ws.att_iter[idx(L.order, ws.ncell, L.c)] : 0;
+                L.limit = open ? min(512, L.iter + kPredictionIterations) : 512;
                 L.stage = 0;
                 L.rate = 0.f;
-                L.ck_iter = 0;
+                L.ck_iter = L.iter;
                 if (!load_cell32(m, ws, L.c, p, t, L.cell, active)) {
                     L.iter = -1;
                     L.stage = 2;
@@ -891,7 +956,7 @@ __global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict_
             const float guard = 64.f * fp32::kEpsF * (L.point.mag + L.next.mag);
             accept = predicted > guard ? L.next.gibbs <= L.point.gibbs - 1e-4f * predicted
                                        : (L.next.gibbs <= L.point.gibbs + guard &&
-                                          L.point.fug - L.next.fug > 1e-4f * (L.alpha / L.scale) * L.point.fug);
+                                          (open || L.point.fug - L.next.fug > 1e-4f * (L.alpha / L.scale) * L.point.fug));
         }
         if (accept) {
             fp32::copy_state(L.point, L.next, n);
@@ -1047,6 +1112,60 @@ __device__ bool polish_split(const Mixture& m, fp64::Cell<NM>& c64, PolishScratc
 // collapsed to the trivial solution or provably end at the iteration limit.
 __device__ __forceinline__ bool unsettled(int cls) { return cls != fp32::aTrivial && cls != fp32::aLimit; }
 
+// Attempts of a cell that FP32 converged elsewhere the polish cannot skip: the
+// reference keeps the first attempt of least Gibbs energy among all that
+// converge (pt_split.hpp:459-486), and an attempt whose FP32 line search
+// stopped near a pair, where FP32 rounding decides its tests (class aFailed),
+// can still converge in the reference's FP64 iteration, to a pair of lower
+// Gibbs energy than the polished one.  An attempt that stopped far from any
+// pair (aFailedFar) stops there in FP64 too.
+__device__ __forceinline__ bool open_attempt(int cls) { return cls == fp32::aFailed; }
+
+// Queues a cell's attempts for the FP64 continuation (split64) and lists the
+// cell for select64: every unsettled attempt when no polished pair was
+// accepted (cand_order < 0), else the open attempts, which then compete with
+// the polished pair of attempt `cand_order` and Gibbs energy `cand_g` already
+// stored in `cand`.  A cell whose items do not fit goes to the plain FP64
+// fallback.
+template <int NM>
+__device__ void queue_attempts64(const Workspace& ws, int64_t c, int na, int cnt, int cand_order, double cand_g) {
+    const int base = atomicAdd(&ws.counters[qS64Items], cnt);
+    if (base + cnt > ws.s64_capacity) {
+        ws.phase[c] = pFallback;
+        atomicAdd(&ws.counters[qFallback], 1);
+        return;
+    }
+    int k = 0;
+    for (int a = 0; a < na; ++a) {
+        const int cls = ws.att_class[idx(a, ws.ncell, c)];
+        if (cand_order < 0 ? unsettled(cls) : open_attempt(cls)) ws.s64_items[base + k++] = (static_cast<int>(c) << 5) | a;
+    }
+    ws.s64_base[c] = base;
+    ws.s64_count[c] = cnt;
+    ws.cand_s[idx(4, ws.ncell, c)] = cand_order >= 0 ? cand_g : __longlong_as_double(0x7ff8000000000000LL);
+    ws.cand_s[idx(6, ws.ncell, c)] = static_cast<double>(cand_order);
+    ws.phase[c] = pSplit64;
+    ws.s64_cells[atomicAdd(&ws.counters[qS64Cells], 1)] = static_cast<int>(c);
+}
+
+// A polished pair of attempt `cand_order` (Gibbs energy `cand_g`, stored in
+// `cand`) beside `open` attempts FP32 left open: the open attempts go to the
+// FP32 prediction (the open pass of split32_kernel) and the cell waits for
+// compete_kernel.  The feed-test cell list is free by now and holds these
+// cells.
+template <int NM>
+__device__ void list_open(const Workspace& ws, int64_t c, int na, int open, int cand_order, double cand_g) {
+    ws.cand_s[idx(4, ws.ncell, c)] = cand_g;
+    ws.cand_s[idx(6, ws.ncell, c)] = static_cast<double>(cand_order);
+    const int base = atomicAdd(&ws.counters[qOpenItems], open);
+    int k = 0;
+    for (int a = 0; a < na; ++a)
+        if (open_attempt(ws.att_class[idx(a, ws.ncell, c)])) ws.attempt_items[base + k++] = (static_cast<int>(c) << 5) | a;
+    ws.phase[c] = pCompete;
+    ws.trial_cells[atomicAdd(&ws.counters[qCompeteCells], 1)] = static_cast<int>(c);
+    atomicAdd(&ws.counters[sCompeting], 1);
+}
+
 template <int NM>
 __device__ bool split_accepted(const fp64::SplitState<NM>& st, int n) {
     double contrast = 0.0;
@@ -1144,6 +1263,7 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
         }
         bool have = false, polish_failed = false;
         double best_g = 0.0;
+        int cand_order = -1;
         for (int k = 0; k < 2 && candidates[k] >= 0; ++k) {
             const int a = candidates[k];
             for (int i = 0; i < n; ++i) s.lnk[i] = ws.att_lnk[idx(a * NM + i, ws.ncell, c)];
@@ -1155,6 +1275,7 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
             if (have && !(s.st.gibbs < best_g)) continue;
             have = true;
             best_g = s.st.gibbs;
+            cand_order = a;
             store_candidate(ws, c, s.st, n);
         }
         atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], c64.counters[cSplitEvals]);
@@ -1176,24 +1297,48 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
                 write_counters<NM>(out, ws, c);
                 continue;
             }
-            const int base = atomicAdd(&ws.counters[qS64Items], cnt);
-            if (base + cnt > ws.s64_capacity) {
-                ws.phase[c] = pFallback;
-                atomicAdd(&ws.counters[qFallback], 1);
-                atomicAdd(&ws.counters[best < 0 ? sFbNoAttempt : (polish_failed ? sFbPolish : sFbRejected)], 1);
-                continue;
-            }
-            int k = 0;
-            for (int a = 0; a < na; ++a)
-                if (unsettled(ws.att_class[idx(a, ws.ncell, c)])) ws.s64_items[base + k++] = (static_cast<int>(c) << 5) | a;
-            ws.s64_base[c] = base;
-            ws.s64_count[c] = cnt;
-            ws.phase[c] = pSplit64;
-            ws.s64_cells[atomicAdd(&ws.counters[qS64Cells], 1)] = static_cast<int>(c);
+            queue_attempts64<NM>(ws, c, na, cnt, -1, 0.0);
             atomicAdd(&ws.counters[best < 0 ? sFbNoAttempt : (polish_failed ? sFbPolish : sFbRejected)], 1);
             continue;
         }
+        int open = 0;
+        for (int a = 0; a < na; ++a) open += open_attempt(ws.att_class[idx(a, ws.ncell, c)]);
+        if (open > 0) {
+            list_open<NM>(ws, c, na, open, cand_order, best_g);
+            continue;
+        }
         begin_review(ws, c, c64, best_g);
+    }
+}
+
+// Cells whose polished pair waited on open attempts: the pair goes to the
+// review when the FP32 prediction pruned every open attempt; otherwise the
+// attempts left open continue exactly in FP64 (split64) and compete with the
+// pair in select64.
+template <int NM>
+__global__ void __launch_bounds__(64) compete_kernel(const Mixture* __restrict__ mix_g, Workspace ws,
+                                                     const double* __restrict__ p, const double* __restrict__ t) {
+    __shared__ Mixture m;
+    stage_mixture(mix_g, m);
+    const int cells = ws.counters[qCompeteCells];
+    for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < cells; slot += gridDim.x * blockDim.x) {
+        const int64_t c = ws.trial_cells[slot];
+        const int na = ws.att_count[c];
+        int open = 0;
+        for (int a = 0; a < na; ++a) open += open_attempt(ws.att_class[idx(a, ws.ncell, c)]);
+        const double cand_g = ws.cand_s[idx(4, ws.ncell, c)];
+        if (open > 0) {
+            queue_attempts64<NM>(ws, c, na, open, static_cast<int>(ws.cand_s[idx(6, ws.ncell, c)]), cand_g);
+            atomicAdd(&ws.counters[sCompeteFp64], 1);
+            continue;
+        }
+        fp64::Cell<NM> c64;
+        if (!load_cell64(m, ws, c, p, t, c64)) {
+            ws.phase[c] = pFallback;
+            atomicAdd(&ws.counters[qFallback], 1);
+            continue;
+        }
+        begin_review(ws, c, c64, cand_g);
     }
 }
 

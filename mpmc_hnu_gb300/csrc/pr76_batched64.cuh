@@ -470,15 +470,43 @@ __global__ void __launch_bounds__(64) select64_kernel(const Mixture* __restrict_
     for (int slot = blockIdx.x * blockDim.x + threadIdx.x; slot < cells; slot += gridDim.x * blockDim.x) {
         const int64_t c = ws.s64_cells[slot];
         const int base = ws.s64_base[c], cnt = ws.s64_count[c];
-        int best = -1;
+        // a polished pair already in `cand` (attempt order cand_order) competes
+        // with the continued attempts: the first attempt of least Gibbs energy
+        // in the reference's attempt order wins (pt_split.hpp:459-486)
+        const double cand_g = ws.cand_s[idx(4, ws.ncell, c)];
+        const int cand_order = isfinite(cand_g) ? static_cast<int>(ws.cand_s[idx(6, ws.ncell, c)]) : -1;
+        int best = -1;  // -1 none yet, -2 the polished pair, else the FP64 item
         double best_g = 0.0;
-        for (int k = 0; k < cnt; ++k) {
+        bool cand_seen = false;
+        for (int k = 0; k <= cnt; ++k) {
+            // items are queued in attempt order; the polished pair takes its
+            // place before the first item of a later attempt
+            const int order = k < cnt ? (ws.s64_items[base + k] & 31) : 32;
+            if (cand_order >= 0 && !cand_seen && cand_order < order) {
+                cand_seen = true;
+                if (best == -1 || cand_g < best_g) {
+                    best = -2;
+                    best_g = cand_g;
+                }
+            }
+            if (k == cnt) break;
             if (ws.s64_status[base + k] != fp64::kConverged) continue;
             const double g = ws.s64_state[static_cast<int64_t>(base + k) * S64Stride<NM>()];
-            if (best < 0 || g < best_g) {
+            if (best == -1 || g < best_g) {
                 best = base + k;
                 best_g = g;
             }
+        }
+        const bool cand_wins = best == -2;
+        if (cand_wins) {
+            fp64::Cell<NM> c64;
+            if (!load_cell64(m, ws, c, p, t, c64)) {
+                ws.phase[c] = pFallback;
+                atomicAdd(&ws.counters[qFallback], 1);
+                continue;
+            }
+            begin_review(ws, c, c64, best_g);
+            continue;
         }
         if (best < 0) {
             if (warm_cell(ws, c)) {  // no converged warm attempt: solve the cell cold

@@ -507,7 +507,17 @@ __device__ __forceinline__ void copy_state(SplitState<NM>& d, const SplitState<N
 // aLimit: 512 iterations without reaching even FP32 resolution (|r| > 1e-3,
 // two orders above the FP32 floor), so the FP64 iteration from the same seed
 // also ends at its iteration limit (pt_split.hpp:364-366).
-enum SplitClass : int { aConverged = 0, aTrivial = 1, aFailed = 2, aLimit = 3 };
+// aPruned: an attempt FP32 left open whose predicted end (relaxed FP32
+// continuation) is the polished pair of another attempt, a trivial pair, or a
+// pair of clearly higher Gibbs energy, so it cannot change the cell's
+// selection.
+// aFailedFar: the FP32 iteration stopped (line search or slope) with |r| of
+// order one, far above both precisions' floors; the reference's FP64
+// iteration from the same seed stops the same way (on the bench distributions
+// at 4 to 20 components, none of 3,130 such attempts converged in FP64).
+enum SplitClass : int { aConverged = 0, aTrivial = 1, aFailed = 2, aLimit = 3, aPruned = 4, aFailedFar = 5 };
+// |r| above which an FP32 attempt that stopped is aFailedFar
+constexpr float kFarFailure = 0.5f;
 
 // ln K successive substitution with the Gibbs line search (pt_split.hpp:349-407),
 // run until FP32 resolution (|r| <= 1e-5) or stagnation.

@@ -1108,6 +1108,7 @@ __global__ void __launch_bounds__(128) polishw_kernel(const Mixture* __restrict_
         }
         bool have = false, polish_failed = false;
         double best_g = 0.0;
+        int cand_order = -1;
         Split st;
         for (int k = 0; k < 2 && candidates[k] >= 0; ++k) {
             const int a = candidates[k];
@@ -1120,6 +1121,7 @@ __global__ void __launch_bounds__(128) polishw_kernel(const Mixture* __restrict_
             if (have && !(st.gibbs < best_g)) continue;
             have = true;
             best_g = st.gibbs;
+            cand_order = a;
             // store_candidate
             if (lane < n) {
                 ws.cand[idx(0 * NM + lane, ws.ncell, c)] = st.x;
@@ -1155,24 +1157,17 @@ __global__ void __launch_bounds__(128) polishw_kernel(const Mixture* __restrict_
                     write_status_only<NM>(out, ws, c, kIndeterminate, false);
                     write_counters<NM>(out, ws, c);
                 } else {
-                    const int base = atomicAdd(&ws.counters[qS64Items], cnt);
-                    const int reason = best < 0 ? sFbNoAttempt : (polish_failed ? sFbPolish : sFbRejected);
-                    if (base + cnt > ws.s64_capacity) {
-                        ws.phase[c] = pFallback;
-                        atomicAdd(&ws.counters[qFallback], 1);
-                    } else {
-                        int k = 0;
-                        for (int a = 0; a < na; ++a)
-                            if (unsettled(ws.att_class[idx(a, ws.ncell, c)]))
-                                ws.s64_items[base + k++] = (static_cast<int>(c) << 5) | a;
-                        ws.s64_base[c] = base;
-                        ws.s64_count[c] = cnt;
-                        ws.phase[c] = pSplit64;
-                        ws.s64_cells[atomicAdd(&ws.counters[qS64Cells], 1)] = static_cast<int>(c);
-                    }
-                    atomicAdd(&ws.counters[reason], 1);
+                    queue_attempts64<NM>(ws, c, na, cnt, -1, 0.0);
+                    atomicAdd(&ws.counters[best < 0 ? sFbNoAttempt : (polish_failed ? sFbPolish : sFbRejected)], 1);
                 }
             }
+            continue;
+        }
+        // attempts FP32 left open: predicted in FP32, then compete in FP64
+        int open = 0;
+        for (int a = 0; a < na; ++a) open += open_attempt(ws.att_class[idx(a, ws.ncell, c)]);
+        if (open > 0) {
+            if (lane == 0) list_open<NM>(ws, c, na, open, cand_order, best_g);
             continue;
         }
         // begin_review (pt_split.hpp:490-512): Gibbs change against the feed,

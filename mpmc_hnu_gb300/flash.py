@@ -148,10 +148,10 @@ BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun
                "fp64_attempts_no_fp32", "fp64_attempts_polish_failed", "fp64_attempts_rejected", "fallback_load",
                "two_candidates", "fp64_trial_items", "fp64_attempt_items", "polished_cells", "select64_cells",
                "slow_trials_skipped", "limit_attempts", "warm_cells", "warm_redo",
-               "warm_redo_no_pair", "warm_redo_unstable"]
+               "warm_redo_no_pair", "warm_redo_unstable", "competing_cells", "competing_cells_fp64"]
 FLAG_STAGE_TIMING = 1
 _QUEUE_STAGES = ["setup", "feed_trials", "feed_classify", "feed_trials64", "decide", "split", "polish",
-                 "split64", "select64", "relist", "review_trials", "review_classify", "review_trials64",
+                 "open32", "compete", "split64", "select64", "relist", "review_trials", "review_classify", "review_trials64",
                  "finish", "fallback", "sensitivity"]
 # the FP64 work-queue form runs on the same stage slots; its FP32 stages
 # (feed_trials, split, review_trials) only queue items or are empty

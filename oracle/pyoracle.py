@@ -39,6 +39,9 @@ class _Out(ctypes.Structure):
 
 
 _built = False
+# where the reference sources lie, if at all (this recipe reads them there;
+# MPMC_REFERENCE_ROOT overrides, as for the tests and golden-vector scripts)
+REFERENCE_ROOT = os.environ.get("MPMC_REFERENCE_ROOT", "/root/reference")
 
 
 def build(force: bool = False) -> None:
@@ -48,8 +51,8 @@ def build(force: bool = False) -> None:
     if _built and not force:
         return
     subprocess.check_call(["make", "-s", "-C", HERE, "all"])
-    if os.path.isdir("/root/reference/modules"):
-        subprocess.check_call(["make", "-s", "-C", HERE, "ref"])
+    if os.path.isdir(os.path.join(REFERENCE_ROOT, "modules")):
+        subprocess.check_call(["make", "-s", "-C", HERE, "ref", f"REFERENCE_ROOT={REFERENCE_ROOT}"])
     _built = True
 
 

@@ -72,7 +72,9 @@ def random_states(n: int, phases: int, ncell: int, seed: int):
         keep = np.ones((n, ncell), bool)
         keep[dep[ph], np.arange(ncell)] = False
         blocks.append(x.T[keep.T].reshape(ncell, n - 1).T)
-    q = np.vstack([p[None], t[None], sat] + blocks)
+    # C order: vstack keeps its inputs' (Fortran) layout, and device copies of
+    # the array must be row-major [q, ncell] like the C ABI's chart layout
+    q = np.ascontiguousarray(np.vstack([p[None], t[None], sat] + blocks))
     return q, dep
 
 

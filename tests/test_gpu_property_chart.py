@@ -65,7 +65,7 @@ def test_chart_device_entry_and_default_pivot(gpu_lib, oracle_lib):
     values_only = g.property_chart(spec, q_last, None, jacobian=False)
     rows, cols = chart_shape(n, phases)
     dev = torch.device("cuda:0")
-    dq = torch.from_numpy(q_last).to(dev)
+    dq = torch.from_numpy(np.ascontiguousarray(q_last)).to(dev).contiguous()
     st = torch.empty(ncell, dtype=torch.int32, device=dev)
     vals = torch.empty((rows, ncell), dtype=torch.float64, device=dev)
     jac = torch.empty((rows, cols, ncell), dtype=torch.float64, device=dev)
