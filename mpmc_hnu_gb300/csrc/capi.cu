@@ -525,14 +525,24 @@ int mpmc_gpu_flash_components(const mpmc_gpu_flash* h) { return h ? h->n : 0; }
 int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* h, int64_t* out, int capacity) {
     if (!h || (h->form != MPMC_FORM_MIXED && h->form != MPMC_FORM_BATCHED) || !h->workspace.ptr) return 0;
     // workspace counter slots (pr76_batched.cuh Slot) in the documented order
-    constexpr int kSlots[] = {8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 20, 22, 23, 24, 25, 27, 28, 29, 30, 31, 32};
+    // negative entries: a 64-bit total held in slots -s and -s + 1
+    constexpr int kSlots[] = {8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 20, 22, 23, 24, 25, 27, 28, 29, 30, 31, 32, 33,
+                              -34, -36, -38, -40, -42, 44, 45};
     constexpr int kCount = static_cast<int>(sizeof(kSlots) / sizeof(kSlots[0]));
-    int vals[40] = {};
+    int vals[48] = {};
     if (cudaSetDevice(h->device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return 0;
     // the counters are the first array of the workspace
     if (cudaMemcpy(vals, h->workspace.ptr, sizeof(vals), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
-    for (int k = 0; k < kCount && k < capacity; ++k)
-        if (out) out[k] = vals[kSlots[k]];
+    for (int k = 0; k < kCount && k < capacity; ++k) {
+        if (!out) continue;
+        if (kSlots[k] >= 0) {
+            out[k] = vals[kSlots[k]];
+        } else {
+            unsigned long long v = 0;
+            std::memcpy(&v, vals - kSlots[k], sizeof(v));
+            out[k] = static_cast<int64_t>(v);
+        }
+    }
     return kCount;
 }
 

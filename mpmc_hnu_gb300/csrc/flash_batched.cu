@@ -47,8 +47,8 @@ size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell, bool fp64
     ws.att_class = reinterpret_cast<signed char*>(take(batched::kMaxAttempts * nc));
     ws.att_count = reinterpret_cast<int*>(take(sizeof(int) * nc));
     ws.att_iter = reinterpret_cast<short*>(take(sizeof(short) * batched::kMaxAttempts * nc));
-    ws.att_lnk64 = fp64_items ? reinterpret_cast<double*>(take(sizeof(double) * batched::kMaxAttempts * NM * nc))
-                              : nullptr;
+    ws.att_lnk64 = reinterpret_cast<double*>(take(sizeof(double) * batched::kMaxAttempts * NM * nc));
+    ws.fp64_items = fp64_items ? 1 : 0;
     ws.att_rate = reinterpret_cast<float*>(take(sizeof(float) * batched::kMaxAttempts * nc));
     ws.cand = reinterpret_cast<double*>(take(sizeof(double) * 7 * NM * nc));
     ws.cand_s = reinterpret_cast<double*>(take(sizeof(double) * 8 * nc));

@@ -94,8 +94,24 @@ enum Slot : int {
     sWarmUnstable = 30,    // ... because the review found a negative TPD
     sCompeting = 31,       // cells whose polished pair waited on attempts FP32 left open
     sCompeteFp64 = 32,     // ... of those, cells with open attempts left for the FP64 continuation
-    qSlots = 40
+    sReplayRisk = 33,      // cells whose polished attempt may stop short in the reference (replay_linear)
+    // 64-bit totals (two slots each) of the FP64 work per stage, for the
+    // algorithmic flop count of each stage: property evaluations ...
+    tE64Setup = 34,        // ... of the feed phase (setup)
+    tE64FeedTrials = 36,   // ... of the FP64 feed-test trial items
+    tE64ReviewTrials = 38, // ... of the FP64 review trial items
+    tE64Polish = 40,       // ... of the Newton polish (first state and chord steps)
+    tE64Split64 = 42,      // ... of the FP64 attempt continuations
+    sPolishJacobians = 44, // closed-form Jacobians built and factorised by the polish
+    sPolishSolves = 45,    // LU solves of the polish's chord steps
+    qSlots = 48
 };
+
+// FP64 attempt items are (cell << 5) | flags | order, order < kMaxAttempts:
+// kFromSeed runs the attempt from its FP64 seed with the whole 512-iteration
+// budget, else it continues from its FP32 end point.
+constexpr int kFromSeed = 16;
+constexpr int kOrderMask = 15;
 
 // Doubles per FP64 attempt result: gibbs, guard, fug, beta, z_l, z_v, 2 spare,
 // then x, y, ln K, ln phi_L, ln phi_V, common log activity.
@@ -149,7 +165,7 @@ struct Workspace {
     signed char* s64_status;// [s64_capacity]
     double* s64_state;      // [s64_capacity * S64Stride] converged attempt states
     short* att_iter;        // [kMaxAttempts * ncell] FP32 SS iterations of the attempt
-    double* att_lnk64;      // [kMaxAttempts * NM * ncell] FP64 seeds (batched FP64 form only, else null)
+    double* att_lnk64;      // [kMaxAttempts * NM * ncell] FP64 seeds of the attempts
     const double* warm_lnk; // [n * ncell] caller's ln K warm starts (NaN = cold), warm pass only
     signed char* warm_cell; // [ncell] 1 = the cell runs from its warm start in the warm pass
     int pass;               // Pass
@@ -159,6 +175,7 @@ struct Workspace {
     int* s64_base;          // [ncell] first FP64 attempt item of the cell
     int* s64_count;         // [ncell]
     int s64_capacity;
+    int fp64_items;         // FP64 work-queue form: every attempt item runs from its FP64 seed
 };
 
 // A cell of the warm pass that runs from its warm start: a rejected pair sends
@@ -168,6 +185,21 @@ __device__ __forceinline__ bool warm_cell(const Workspace& ws, int64_t c) {
 }
 
 __device__ __forceinline__ int64_t idx(int k, int64_t ncell, int64_t c) { return static_cast<int64_t>(k) * ncell + c; }
+
+// Adds each calling lane's `v` to the 64-bit total at counter slot `slot`,
+// one atomic per warp (the lanes of the warp that call it together).
+__device__ __forceinline__ void add_total(const Workspace& ws, int slot, int v) {
+    const unsigned mask = __activemask();
+    const unsigned sum = __reduce_add_sync(mask, static_cast<unsigned>(v));
+    if ((threadIdx.x & 31) == __ffs(mask) - 1)
+        atomicAdd(reinterpret_cast<unsigned long long*>(ws.counters + slot), static_cast<unsigned long long>(sum));
+}
+// 32-bit variant for counts
+__device__ __forceinline__ void add_count(const Workspace& ws, int slot, int v) {
+    const unsigned mask = __activemask();
+    const unsigned sum = __reduce_add_sync(mask, static_cast<unsigned>(v));
+    if ((threadIdx.x & 31) == __ffs(mask) - 1) atomicAdd(ws.counters + slot, static_cast<int>(sum));
+}
 
 // Number of automatic TPD starts for `active` components (pt_stability.hpp:254).
 __device__ __forceinline__ int auto_starts(int active) { return active == 1 ? 1 : active + 2; }
@@ -311,6 +343,7 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
             ph = pSplit;
         }
         ws.phase[c] = ph;
+        add_total(ws, tE64Setup, cell.counters[cInitEvals]);
         if (ws.pass != kPassRedo) {
             for (int k = 0; k < cCount; ++k) ws.counters_out[idx(k, ws.ncell, c)] = 0;
             ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)] = cell.counters[cInitEvals];
@@ -743,10 +776,10 @@ __global__ void __launch_bounds__(64) decide_kernel(const Mixture* __restrict__ 
                     const int item = atomicAdd(&ws.counters[qAttempts], 1);
                     ws.attempt_items[item] = (static_cast<int>(c) << 5) | order;
                     ws.att_class[idx(order, ws.ncell, c)] = fp32::aFailed;  // overwritten by split32
-                    if (ws.att_lnk64) {  // batched FP64 form: the attempt runs from its exact seed
-                        for (int i = 0; i < n; ++i) ws.att_lnk64[idx(order * NM + i, ws.ncell, c)] = s.lk[i];
-                        ws.att_iter[idx(order, ws.ncell, c)] = 0;
-                    }
+                    // the exact seed: every attempt of the FP64 form runs from it, and in
+                    // the mixed form the reference's own run of the attempt when needed
+                    for (int i = 0; i < n; ++i) ws.att_lnk64[idx(order * NM + i, ws.ncell, c)] = s.lk[i];
+                    if (ws.fp64_items) ws.att_iter[idx(order, ws.ncell, c)] = 0;
                 } else {
                     ws.att_class[idx(order, ws.ncell, c)] = fp32::aTrivial;  // unrepresentable seed: not a candidate
                 }
@@ -788,6 +821,10 @@ struct SplitLane {
 // bench distributions at 4-20 components); one that has not converged by then
 // stays open for the FP64 continuation.
 constexpr int kPredictionIterations = 96;
+// Iteration count (FP32 iterations plus the replayed remainder) above which a
+// polished attempt is sent to the exact FP64 continuation instead: the
+// reference stops at 512, and the FP32 count and the replay are estimates.
+constexpr int kReplayLimit = 480;
 
 template <int NM>
 __device__ void split_step_or_finish(SplitLane<NM>& L, float ss_switch) {
@@ -906,8 +943,15 @@ __global__ void __launch_bounds__(128) split32_kernel(const Mixture* __restrict_
                 const int64_t c = L.c;
                 ws.att_class[idx(L.order, ws.ncell, c)] = static_cast<signed char>(cls);
                 if (cls == fp32::aLimit) atomicAdd(&ws.counters[sLimitAttempts], 1);
-                ws.att_gibbs[idx(L.order, ws.ncell, c)] = L.point.gibbs;
-                for (int i = 0; i < n; ++i) ws.att_lnk[idx(L.order * NM + i, ws.ncell, c)] = L.point.lnk[i];
+                if (L.iter >= 0) {
+                    ws.att_gibbs[idx(L.order, ws.ncell, c)] = L.point.gibbs;
+                    for (int i = 0; i < n; ++i) ws.att_lnk[idx(L.order * NM + i, ws.ncell, c)] = L.point.lnk[i];
+                } else {
+                    // no FP32 state of this attempt (its seed or the cell's constants
+                    // did not evaluate): the seed stays, and the FP64 continuation
+                    // runs the attempt from its exact seed
+                    ws.att_gibbs[idx(L.order, ws.ncell, c)] = INFINITY;
+                }
                 atomicAdd(&ws.counters_out[idx(cSplitEvals, ws.ncell, c)], L.cell.evals);
                 atomicAdd(&ws.counters_out[idx(cSplitIters, ws.ncell, c)], L.iter);
             }
@@ -978,6 +1022,7 @@ struct PolishScratch {
     double lnk[NM], e[NM], num[NM], J[NM * NM], d[NM];
     double sl[NM], sv[NM];  // mixing row sums of the two phases
     int piv[NM];
+    int jacobians, solves;  // closed-form Jacobians factorised, chord-step LU solves
 };
 
 // Closed-form full-chart d ln phi_i / d x_j = cs_i s_j + cb_i b_j + ca a_ij of
@@ -1077,22 +1122,106 @@ __device__ bool equilibrium_jacobian(const Mixture& m, fp64::Cell<NM>& c, Polish
     return true;
 }
 
+// The reference's ln K iteration (pt_split.hpp:364-405) replayed on the
+// linearisation r' = r + (alpha / scale) J r around a pair, from the FP64
+// residual r at an attempt's FP32 end point.  Returns the iterations to
+// |r| <= 1e-11 (0 when |I + J| < 1 in the max norm: then every step of every
+// length contracts |r|, so the reference's iteration cannot stall there), or
+// -1 when every halving is rejected, or `budget` when it is reached.
+//  * Where the Gibbs test is resolvable (predicted decrease above the round-off
+//    guard) the step is the reference's Armijo test on the quadratic model of
+//    the Gibbs energy its slope formula implies: grad G = -H r with
+//    H = beta (1 - beta) diag(c) + c c^T / h, c_i = x_i y_i / z_i, so
+//    dG(alpha) = -alpha q / s + alpha^2 p / (2 s^2), q = r^T H r, p = -r^T H J r.
+//  * Below the guard it is the residual-decrease rule, up to 24 halvings.
+// Two outcomes mark an FP32 attempt whose reference run ends elsewhere: a
+// stall (two close slow modes of I + J keep the residual a mix whose max norm
+// rises along the step; the reference ends line_search_failed just short of
+// convergence), and the budget (I + J expands some direction: the FP32
+// iteration stopped near a saddle that the reference's run leaves).
+__device__ inline int replay_linear(int n, const double* J, const double* r0, const double* x, const double* y,
+                                    const double* z, double beta, double guard64, int budget) {
+    // FP32 arithmetic: the decisions compare relative changes of 1e-4 and
+    // more, and FP32 keeps the replay off the FP64 pipe
+    float Jf[kMaxC * kMaxC], r[kMaxC], jr[kMaxC], cw[kMaxC];
+    float h = 0.f, norm = 0.f;
+    for (int i = 0; i < n; ++i) {
+        const bool act = z[i] > 0.0;
+        r[i] = act ? static_cast<float>(r0[i]) : 0.f;
+        cw[i] = act ? static_cast<float>((x[i] / z[i]) * y[i]) : 0.f;
+        if (act) h += static_cast<float>((y[i] - x[i]) * ((y[i] - x[i]) / z[i]));
+        float row = 0.f;
+        for (int j = 0; j < n; ++j) {
+            const bool on = act && z[j] > 0.0;
+            Jf[i * n + j] = on ? static_cast<float>(J[i * n + j]) : 0.f;
+            if (on) row += fabsf((i == j ? 1.f : 0.f) + Jf[i * n + j]);
+        }
+        norm = fmaxf(norm, row);
+    }
+    if (!(h > 0.f)) return -1;
+    if (norm < 1.f - 1e-4f) return 0;
+    const float bb = static_cast<float>(beta * (1.0 - beta));
+    const float guard = static_cast<float>(guard64);
+    for (int it = 0; it < budget; ++it) {
+        float fug = 0.f, first = 0.f, second = 0.f;
+        for (int i = 0; i < n; ++i) {
+            fug = fmaxf(fug, fabsf(r[i]));
+            first = fmaf(cw[i], r[i], first);
+            second = fmaf(cw[i] * r[i], r[i], second);
+        }
+        if (fug <= 1e-11f) return it;
+        const float scale = fmaxf(1.f, fug / 2.f);
+        const float q = bb * second + (first / h) * first;
+        float firstj = 0.f, mixed = 0.f;
+        for (int i = 0; i < n; ++i) {
+            float v = 0.f;
+            for (int j = 0; j < n; ++j) v = fmaf(Jf[i * n + j], r[j], v);
+            jr[i] = v;
+            firstj = fmaf(cw[i], v, firstj);
+            mixed = fmaf(cw[i] * r[i], v, mixed);
+        }
+        const float pq = -(bb * mixed + (first / h) * firstj);
+        float alpha = 1.f;
+        bool accepted = false;
+        for (int bt = 0; bt < 24 && !accepted; ++bt) {
+            if (alpha * q / scale > guard) {
+                accepted = !(pq > 0.f) || alpha * pq <= 2.f * (1.f - 1e-4f) * scale * q;
+            } else {
+                float next = 0.f;
+                for (int i = 0; i < n; ++i) next = fmaxf(next, fabsf(fmaf(alpha / scale, jr[i], r[i])));
+                accepted = next <= 1e-11f || fug - next > 1e-4f * (alpha / scale) * fug;
+            }
+            if (!accepted) alpha *= 0.5f;
+        }
+        if (!accepted) return -1;
+        for (int i = 0; i < n; ++i) r[i] = fmaf(alpha / scale, jr[i], r[i]);
+    }
+    return budget;
+}
+
 // Newton polish of ln K from the FP32 solution: FP64 residual F(ln K) (RR +
 // role phases, pt_split.hpp:300-341) and the exact FP64 Jacobian in closed form
 // taken at the first FP64 state (chord iterations).  On success `s.st` holds the FP64 state
 // at |F| <= 1e-13, or at the point where F stopped decreasing below 1e-11.
+// `replay` receives replay_linear's count from the FP32 end point within
+// `budget` iterations (the reference's 512 less the FP32 iterations), or 0
+// when that point is already converged.
 template <int NM>
-__device__ bool polish_split(const Mixture& m, fp64::Cell<NM>& c64, PolishScratch<NM>& s) {
+__device__ bool polish_split(const Mixture& m, fp64::Cell<NM>& c64, PolishScratch<NM>& s, int budget, int& replay) {
     const int n = c64.n;
     int evals = 0;
+    replay = 0;
     if (fp64::split_evaluate(m, c64, s.lnk, s.st, evals, 1 << 30, s.e, s.num, true) != fp64::kConverged) return false;
     if (s.st.fug <= 1e-13) return true;
     if (!equilibrium_jacobian(m, c64, s)) return false;
+    replay = replay_linear(n, s.J, s.st.res, s.st.x, s.st.y, c64.z, s.st.beta, 2.0 * s.st.guard, budget);
     double norm;
     if (!ad::lu_factor(s.J, s.piv, n, norm)) return false;
+    ++s.jacobians;
     double prev = s.st.fug;
     for (int it = 0; it < 8; ++it) {
         for (int i = 0; i < n; ++i) s.d[i] = -s.st.res[i];
+        ++s.solves;
         if (!ad::lu_solve(s.J, s.piv, n, s.d)) return false;
         for (int i = 0; i < n; ++i) s.lnk[i] = s.st.lnk[i] + s.d[i];
         // RR Newton from the current beta: a chord step moves ln K by |F| or less
@@ -1125,10 +1254,12 @@ __device__ __forceinline__ bool open_attempt(int cls) { return cls == fp32::aFai
 // cell for select64: every unsettled attempt when no polished pair was
 // accepted (cand_order < 0), else the open attempts, which then compete with
 // the polished pair of attempt `cand_order` and Gibbs energy `cand_g` already
-// stored in `cand`.  A cell whose items do not fit goes to the plain FP64
-// fallback.
+// stored in `cand`.  `from_seed`: the attempts run from their FP64 seeds with
+// the full budget (the reference's own runs) instead of from their FP32 end
+// points.  A cell whose items do not fit goes to the plain FP64 fallback.
 template <int NM>
-__device__ void queue_attempts64(const Workspace& ws, int64_t c, int na, int cnt, int cand_order, double cand_g) {
+__device__ void queue_attempts64(const Workspace& ws, int64_t c, int na, int cnt, int cand_order, double cand_g,
+                                 bool from_seed = false) {
     const int base = atomicAdd(&ws.counters[qS64Items], cnt);
     if (base + cnt > ws.s64_capacity) {
         ws.phase[c] = pFallback;
@@ -1138,7 +1269,8 @@ __device__ void queue_attempts64(const Workspace& ws, int64_t c, int na, int cnt
     int k = 0;
     for (int a = 0; a < na; ++a) {
         const int cls = ws.att_class[idx(a, ws.ncell, c)];
-        if (cand_order < 0 ? unsettled(cls) : open_attempt(cls)) ws.s64_items[base + k++] = (static_cast<int>(c) << 5) | a;
+        if (cand_order < 0 ? unsettled(cls) : open_attempt(cls))
+            ws.s64_items[base + k++] = (static_cast<int>(c) << 5) | (from_seed ? kFromSeed : 0) | a;
     }
     ws.s64_base[c] = base;
     ws.s64_count[c] = cnt;
@@ -1228,6 +1360,7 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
         const int64_t c = ws.split_cells[slot];
         fp64::Cell<NM> c64;
         PolishScratch<NM> s;
+        s.jacobians = s.solves = 0;
         if (!load_cell64(m, ws, c, p, t, c64)) {
             ws.phase[c] = pFallback;
             atomicAdd(&ws.counters[qFallback], 1);
@@ -1261,15 +1394,23 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
                 atomicAdd(&ws.counters[sCandidates2], 1);
             }
         }
-        bool have = false, polish_failed = false;
+        bool have = false, polish_failed = false, replay_risk = false;
         double best_g = 0.0;
         int cand_order = -1;
         for (int k = 0; k < 2 && candidates[k] >= 0; ++k) {
             const int a = candidates[k];
             for (int i = 0; i < n; ++i) s.lnk[i] = ws.att_lnk[idx(a * NM + i, ws.ncell, c)];
-            if (!polish_split(m, c64, s)) {
+            const int done = ws.att_iter[idx(a, ws.ncell, c)];
+            int replay = 0;
+            if (!polish_split(m, c64, s, 512 - done, replay)) {
                 polish_failed = true;
                 continue;
+            }
+            // the reference's attempt may stop short of this pair (a stalled line
+            // search, or the iteration limit): the exact FP64 continuation decides
+            if (replay < 0 || done + replay > kReplayLimit) {
+                replay_risk = true;
+                break;
             }
             if (!split_accepted(s.st, n)) continue;
             if (have && !(s.st.gibbs < best_g)) continue;
@@ -1280,6 +1421,17 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
         }
         atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], c64.counters[cSplitEvals]);
         atomicAdd(&ws.counters_out[idx(cRrIters, ws.ncell, c)], c64.counters[cRrIters]);
+        add_total(ws, tE64Polish, c64.counters[cSplitEvals]);
+        add_count(ws, sPolishJacobians, s.jacobians);
+        add_count(ws, sPolishSolves, s.solves);
+        if (replay_risk) {
+            // the reference's own runs of every attempt, from the FP64 seeds
+            int cnt = 0;
+            for (int a = 0; a < na; ++a) cnt += unsettled(ws.att_class[idx(a, ws.ncell, c)]);
+            queue_attempts64<NM>(ws, c, na, cnt, -1, 0.0, true);
+            atomicAdd(&ws.counters[sReplayRisk], 1);
+            continue;
+        }
         if (!have) {
             // FP64 continuation (reference ln K iteration, pt_split.hpp:275-408) of
             // every attempt FP32 left unsettled, from its FP32 end point: split64 items

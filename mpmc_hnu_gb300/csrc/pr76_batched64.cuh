@@ -191,6 +191,7 @@ __global__ void __launch_bounds__(64) trials64_kernel(const Mixture* __restrict_
                     for (int i = 0; i < n; ++i) ws.tw64[idx(L.k * NM + i, ws.ncell, c)] = L.point.w[i];
                 atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)],
                           L.cell.counters[review ? cFinalEvals : cInitEvals]);
+                add_total(ws, review ? tE64ReviewTrials : tE64FeedTrials, L.cell.counters[review ? cFinalEvals : cInitEvals]);
             }
             L.item = atomicAdd(&ws.counters[qT64Cursor], 1);
             if (L.item >= total) live = false;
@@ -339,6 +340,7 @@ __global__ void __launch_bounds__(64) split64_kernel(const Mixture* __restrict__
                     }
                 }
                 atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, L.c)], L.cell.counters[cSplitEvals]);
+                add_total(ws, tE64Split64, L.cell.counters[cSplitEvals]);
             }
             L.item = atomicAdd(&ws.counters[qS64Cursor], 1);
             if (L.item >= total) {
@@ -352,16 +354,20 @@ __global__ void __launch_bounds__(64) split64_kernel(const Mixture* __restrict__
                     L.item = -1;
                 } else {
                     L.c = code >> 5;
-                    L.order = code & 31;
+                    L.order = code & kOrderMask;
+                    const bool from_seed =
+                        ws.fp64_items || (code & kFromSeed) || ws.att_iter[idx(L.order, ws.ncell, L.c)] == 0;
                     L.iter = 0;
                     L.stage = 0;
                     L.evals = 0;
-                    L.done = ws.att_iter[idx(L.order, ws.ncell, L.c)];
+                    L.done = from_seed ? 0 : ws.att_iter[idx(L.order, ws.ncell, L.c)];
                     L.status = fp64::kAttemptPropertyFailure;
                     if (!load_cell64(m, ws, L.c, p, t, L.cell)) {
                         L.stage = 2;
                     } else {
-                        for (int i = 0; i < L.cell.n; ++i) L.lk[i] = ws.att_lnk[idx(L.order * NM + i, ws.ncell, L.c)];
+                        for (int i = 0; i < L.cell.n; ++i)
+                            L.lk[i] = from_seed ? ws.att_lnk64[idx(L.order * NM + i, ws.ncell, L.c)]
+                                                : static_cast<double>(ws.att_lnk[idx(L.order * NM + i, ws.ncell, L.c)]);
                     }
                 }
             }
@@ -481,7 +487,7 @@ __global__ void __launch_bounds__(64) select64_kernel(const Mixture* __restrict_
         for (int k = 0; k <= cnt; ++k) {
             // items are queued in attempt order; the polished pair takes its
             // place before the first item of a later attempt
-            const int order = k < cnt ? (ws.s64_items[base + k] & 31) : 32;
+            const int order = k < cnt ? (ws.s64_items[base + k] & kOrderMask) : kMaxAttempts;
             if (cand_order >= 0 && !cand_seen && cand_order < order) {
                 cand_seen = true;
                 if (best == -1 || cand_g < best_g) {

@@ -65,6 +65,20 @@ __device__ __forceinline__ double wmax(double v) {
     return v;
 }
 template <int S>
+__device__ __forceinline__ float fsum_group(float v) {
+    const unsigned m = seg_mask<S>();
+#pragma unroll
+    for (int o = S / 2; o > 0; o >>= 1) v += __shfl_xor_sync(m, v, o, S);
+    return v;
+}
+template <int S>
+__device__ __forceinline__ float fmax_group(float v) {
+    const unsigned m = seg_mask<S>();
+#pragma unroll
+    for (int o = S / 2; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(m, v, o, S));
+    return v;
+}
+template <int S>
 __device__ __forceinline__ bool wany(bool p) { return __any_sync(seg_mask<S>(), p); }
 template <int S, typename T>
 __device__ __forceinline__ T bcast(T v, int src) { return __shfl_sync(seg_mask<S>(), v, src, S); }
@@ -851,13 +865,68 @@ __device__ double lu_solve_rows(const double (&J)[NM], int n, const int (&piv)[N
     return d;
 }
 
+// batched::replay_linear with the component rows on the group's lanes: lane i
+// holds row i of J, sums and maxima are group reductions.
+template <int NM, int S>
+__device__ int replay_rows(const WCell<NM, S>& c, const double* J, const Split& st, int budget) {
+    float Jf[NM];
+    float row = 0.f;
+#pragma unroll
+    for (int j = 0; j < NM; ++j) {
+        // every lane of the group takes part in the broadcast
+        const bool actj = bcast<S>(c.act ? 1 : 0, j) != 0;
+        const bool on = c.act && j < c.n && actj;
+        Jf[j] = on ? static_cast<float>(J[j]) : 0.f;
+        if (on) row += fabsf((j == c.lane ? 1.f : 0.f) + Jf[j]);
+    }
+    float r = c.act ? static_cast<float>(st.res) : 0.f;
+    const float cw = c.act ? static_cast<float>((st.x / c.z) * st.y) : 0.f;
+    const float h = static_cast<float>(wsum<S>(c.act ? (st.y - st.x) * ((st.y - st.x) / c.z) : 0.0));
+    if (!(h > 0.f)) return -1;
+    if (static_cast<float>(wmax<S>(static_cast<double>(row))) < 1.f - 1e-4f) return 0;
+    const float guard = static_cast<float>(2.0 * st.guard);
+    const float bb = static_cast<float>(st.beta * (1.0 - st.beta));
+    for (int it = 0; it < budget; ++it) {
+        const float fug = fmax_group<S>(fabsf(r));
+        if (fug <= 1e-11f) return it;
+        const float first = fsum_group<S>(cw * r), second = fsum_group<S>((cw * r) * r);
+        const float scale = fmaxf(1.f, fug / 2.f);
+        const float q = bb * second + (first / h) * first;
+        float jr = 0.f;
+#pragma unroll
+        for (int j = 0; j < NM; ++j) {
+            const float rj = bcast<S>(r, j);
+            if (j < c.n) jr = fmaf(Jf[j], rj, jr);
+        }
+        const float firstj = fsum_group<S>(cw * jr), mixed = fsum_group<S>((cw * r) * jr);
+        const float pq = -(bb * mixed + (first / h) * firstj);
+        float alpha = 1.f;
+        bool accepted = false;
+        for (int bt = 0; bt < 24 && !accepted; ++bt) {
+            if (alpha * q / scale > guard) {
+                accepted = !(pq > 0.f) || alpha * pq <= 2.f * (1.f - 1e-4f) * scale * q;
+            } else {
+                const float next = fmax_group<S>(fabsf(fmaf(alpha / scale, jr, r)));
+                accepted = next <= 1e-11f || fug - next > 1e-4f * (alpha / scale) * fug;
+            }
+            if (!accepted) alpha *= 0.5f;
+        }
+        if (!accepted) return -1;
+        r = fmaf(alpha / scale, jr, r);
+    }
+    return budget;
+}
+
 // Newton polish from ln K `lk` (the FP32 solution): FP64 residual (bracketed
 // Newton RR and roots), the closed-form Jacobian at the first FP64 state, at
 // most 8 chord steps while |F| decreases.  True with `st` at |F| <= 1e-13, or
-// where |F| stopped decreasing below 1e-11.
+// where |F| stopped decreasing below 1e-11.  `replay` receives replay_rows's
+// count from the FP32 end point within `budget` iterations (0 when that point
+// is already converged).
 template <int NM, int S>
-__device__ bool polish(WCell<NM, S>& c, double lk, Split& st) {
+__device__ bool polish(WCell<NM, S>& c, double lk, Split& st, int budget, int& replay, int& jacobians, int& solves) {
     int evals = 0;
+    replay = 0;
     if (split_evaluate(c, lk, st, evals, 1 << 30) != fp64::kConverged) return false;
     if (st.fug <= 1e-13) return true;
     PhiCoeffs fl, fv;
@@ -894,10 +963,14 @@ __device__ bool polish(WCell<NM, S>& c, double lk, Split& st) {
         J[j] = j < c.n ? v : 0.0;
     }
     int piv[NM];
-    if (wany<S>(c.comp && !isfinite(J[0])) || !lu_rows<NM, S>(J, c.n, piv)) return false;
+    if (wany<S>(c.comp && !isfinite(J[0]))) return false;
+    replay = replay_rows<NM, S>(c, J, st, budget);
+    if (!lu_rows<NM, S>(J, c.n, piv)) return false;
+    ++jacobians;
     double prev = st.fug;
     Split nx;
     for (int it = 0; it < 8; ++it) {
+        ++solves;
         const double d = lu_solve_rows<NM, S>(J, c.n, piv, c.act ? -st.res : 0.0);
         if (wany<S>(c.comp && !isfinite(d))) return prev <= 1e-11;
         const double next_lk = c.act ? st.lnk + d : 0.0;
@@ -1000,7 +1073,10 @@ __global__ void __launch_bounds__(128) trials64w_kernel(const Mixture* __restric
         if (lane == 0) ws.t64_status[idx(k, ws.ncell, c)] = static_cast<signed char>(status);
         if (!review && status == fp64::kNegativeTpd && lane < m.n)
             ws.tw64[idx(k * NM + lane, ws.ncell, c)] = point.w;
-        if (lane == 0) atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], cell.counters[row]);
+        if (lane == 0) {
+            atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], cell.counters[row]);
+            add_total(ws, review ? tE64ReviewTrials : tE64FeedTrials, cell.counters[row]);
+        }
     }
 }
 
@@ -1020,16 +1096,19 @@ __global__ void __launch_bounds__(128) split64w_kernel(const Mixture* __restrict
         const int code = ws.s64_items[item];
         if (code < 0) continue;
         const int64_t c = code >> 5;
-        const int order = code & 31;
+        const int order = code & kOrderMask;
+        // the FP64 seed with the whole budget, or the FP32 end point with what is left
+        // (an attempt without FP32 progress also starts from its exact seed)
+        const bool from_seed = ws.fp64_items || (code & kFromSeed) || ws.att_iter[idx(order, ws.ncell, c)] == 0;
         WCell<NM, S> cell;
         Split point;
         int evals = 0;
         int status = fp64::kAttemptPropertyFailure;
         if (load_cell(m, ws, c, p, t, cell)) {
             const double lk0 = !cell.comp ? 0.0
-                               : (ws.att_lnk64 ? ws.att_lnk64[idx(order * NM + lane, ws.ncell, c)]
-                                               : static_cast<double>(ws.att_lnk[idx(order * NM + lane, ws.ncell, c)]));
-            status = attempt(cell, lk0, point, evals, ws.att_iter[idx(order, ws.ncell, c)]);
+                               : (from_seed ? ws.att_lnk64[idx(order * NM + lane, ws.ncell, c)]
+                                            : static_cast<double>(ws.att_lnk[idx(order * NM + lane, ws.ncell, c)]));
+            status = attempt(cell, lk0, point, evals, from_seed ? 0 : ws.att_iter[idx(order, ws.ncell, c)]);
         }
         if (lane == 0) ws.s64_status[item] = static_cast<signed char>(status);
         if (status == fp64::kConverged) {
@@ -1051,7 +1130,10 @@ __global__ void __launch_bounds__(128) split64w_kernel(const Mixture* __restrict
                 r[8 + 5 * NM + lane] = point.common;
             }
         }
-        if (lane == 0) atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], cell.counters[cSplitEvals]);
+        if (lane == 0) {
+            atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], cell.counters[cSplitEvals]);
+            add_total(ws, tE64Split64, cell.counters[cSplitEvals]);
+        }
     }
 }
 
@@ -1106,16 +1188,23 @@ __global__ void __launch_bounds__(128) polishw_kernel(const Mixture* __restrict_
                 if (lane == 0) atomicAdd(&ws.counters[sCandidates2], 1);
             }
         }
-        bool have = false, polish_failed = false;
+        bool have = false, polish_failed = false, replay_risk = false;
         double best_g = 0.0;
-        int cand_order = -1;
+        int cand_order = -1, jacobians = 0, solves = 0;
         Split st;
         for (int k = 0; k < 2 && candidates[k] >= 0; ++k) {
             const int a = candidates[k];
             const double lk = cell.comp ? static_cast<double>(ws.att_lnk[idx(a * NM + lane, ws.ncell, c)]) : 0.0;
-            if (!polish(cell, lk, st)) {
+            const int done = ws.att_iter[idx(a, ws.ncell, c)];
+            int replay = 0;
+            if (!polish(cell, lk, st, 512 - done, replay, jacobians, solves)) {
                 polish_failed = true;
                 continue;
+            }
+            // the reference's attempt may stop short of this pair: FP64 decides
+            if (replay < 0 || done + replay > kReplayLimit) {
+                replay_risk = true;
+                break;
             }
             if (!accepted(cell, st)) continue;
             if (have && !(st.gibbs < best_g)) continue;
@@ -1142,6 +1231,18 @@ __global__ void __launch_bounds__(128) polishw_kernel(const Mixture* __restrict_
         if (lane == 0) {
             atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], cell.counters[cSplitEvals]);
             atomicAdd(&ws.counters_out[idx(cRrIters, ws.ncell, c)], cell.counters[cRrIters]);
+            if (replay_risk) atomicAdd(&ws.counters[sReplayRisk], 1);
+            add_total(ws, tE64Polish, cell.counters[cSplitEvals]);
+            add_count(ws, sPolishJacobians, jacobians);
+            add_count(ws, sPolishSolves, solves);
+        }
+        if (replay_risk) {  // the reference's own runs of every attempt, from the FP64 seeds
+            if (lane == 0) {
+                int cnt = 0;
+                for (int a = 0; a < na; ++a) cnt += unsettled(ws.att_class[idx(a, ws.ncell, c)]);
+                queue_attempts64<NM>(ws, c, na, cnt, -1, 0.0, true);
+            }
+            continue;
         }
         if (!have) {
             if (lane == 0) {
