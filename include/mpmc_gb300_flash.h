@@ -54,7 +54,11 @@ typedef enum mpmc_status {
     MPMC_ERR_DOMAIN = 2,           /* reference: std::domain_error (bad mixture data) */
     MPMC_ERR_CUDA = 3,             /* a CUDA runtime call failed */
     MPMC_ERR_UNSUPPORTED = 4,      /* component count or option outside this library */
-    MPMC_ERR_TIMEOUT = 5           /* a bounded device wait gave up */
+    MPMC_ERR_TIMEOUT = 5,          /* a bounded device wait gave up */
+    MPMC_ERR_BUSY = 6,             /* flash server: the concurrency limit is reached (the
+                                      reference adapter's RESOURCE_EXHAUSTED) */
+    MPMC_ERR_DEADLINE = 7          /* flash server: the request's deadline passed before its
+                                      results were published (DEADLINE_EXCEEDED) */
 } mpmc_status;
 
 /* Per-cell phase-set status, mirroring PtSplitStatus
@@ -282,6 +286,37 @@ int mpmc_gpu_flash_solve_device_hinted(mpmc_gpu_flash* handle, int64_t n_cells, 
                                        const mpmc_flash_outputs* out, const mpmc_three_phase_outputs* out3,
                                        void* stream);
 
+/* The general form of solve_pr76_pt_max3's caller inputs
+ * (pr76_three_phase.hpp:328-341): initial_starts, final_starts and one
+ * three-phase start per cell, each with arrays of its own, and the two
+ * options of Pr76PtMax3Options::two_phase a caller sets in the reference's
+ * tests (pt_split.hpp:45-50): initial_stability.automatic_starts and
+ * max_split_attempts.  Both options also govern the fresh two-phase solve
+ * that follows a three-phase phase disappearance (pr76_three_phase.hpp:413-415).
+ * Compositions are laid out as in mpmc_start_hints.  A NULL count array means
+ * no starts of that class.  A start off the feed's support, and a feed test
+ * left with no start at all, make the cell MPMC_FLASH_INVALID_REQUEST (a
+ * domain_error / length_error in the reference). */
+typedef struct mpmc_start_hints_ex {
+    const int32_t* initial_count;           /* [n_cells], 0..3 */
+    const double* initial_composition;      /* [3 * n * n_cells] */
+    const int32_t* final_count;             /* [n_cells], 0..3 */
+    const double* final_composition;        /* [3 * n * n_cells] */
+    const int32_t* three_phase;             /* [n_cells] nonzero: one three-phase start (or NULL) */
+    const double* three_phase_composition;  /* [3 * n * n_cells] */
+    const double* fraction;                 /* [2 * n_cells] phase_fraction_seed of phases 1 and 2 */
+    int32_t initial_automatic_starts;       /* 1: the reference default; 0: the supplied starts only */
+    int32_t max_split_attempts;             /* the reference default is 16; 0 .. 65536 */
+} mpmc_start_hints_ex;
+
+int mpmc_gpu_flash_solve_hinted_ex(mpmc_gpu_flash* handle, int64_t n_cells, const double* p, const double* t,
+                                   const double* z, const mpmc_start_hints_ex* hints, const mpmc_flash_outputs* out,
+                                   const mpmc_three_phase_outputs* out3);
+int mpmc_gpu_flash_solve_device_hinted_ex(mpmc_gpu_flash* handle, int64_t n_cells, const double* p,
+                                          const double* t, const double* z, const mpmc_start_hints_ex* hints,
+                                          const mpmc_flash_outputs* out, const mpmc_three_phase_outputs* out3,
+                                          void* stream);
+
 /* ------------------------------------------------------------------------
  * Selected-phase property chart: the flow module's per-cell property and
  * Jacobian publication on a frozen natural-variable chart,
@@ -385,7 +420,7 @@ int mpmc_gpu_flash_property_chart_device(mpmc_gpu_flash* handle, int64_t n_cells
  * Mixed-precision handles only (MPMC_FORM_MIXED; other forms return
  * MPMC_ERR_UNSUPPORTED).  The work buffers of the solve live in one fixed
  * MPMC_NOALLOC_SCRATCH_BYTES array of device memory per device; a batch whose
- * buffers do not fit (about 4,900 cells at 20 components, 9,700 at 10, more
+ * buffers do not fit (about 2,700 cells at 20 components, 7,300 at 10, more
  * with fewer components) returns MPMC_ERR_INVALID_ARGUMENT with the size in
  * the message.  The first call on a device looks the array's address up
  * (cudaGetSymbolAddress, with that device current), and the first launch of
@@ -419,6 +454,10 @@ int mpmc_gpu_flash_solve_device_noalloc(mpmc_gpu_flash* handle, int64_t n_cells,
  *       lane group with bit 4 (default: per thread up to 12 components)
  *   [6] successive-substitution -> Newton switch: the FP32 |r| (in units of
  *       1e-6) at which the FP32 ln K iteration hands over to the FP64 polish
+ *   [7] cell ranges (1-8) a solve is split into, each a solve of its own on
+ *       its own stream, so that the long last items of one range overlap the
+ *       bulk stages of the others (default 1; every range keeps at least
+ *       65,536 cells; the outputs do not depend on it)
  * 0 selects the default (occupancy-derived residency, lane-group items,
  * switch at 2e-5).  Results do not depend on the shape beyond the rounding of
  * where each iteration stops.  Drops the handle's captured graphs.  No
@@ -453,8 +492,16 @@ int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* handle, float* ms, int capacity
  * cold pass, [18] of those, cells with no converged attempt, [19] of those,
  * cells whose review found a negative TPD, [20] cells whose polished pair
  * waited on attempts that FP32 left open, [21] of those, cells where some open
- * attempt could still change the selection and was continued in FP64.  After
- * a warm-start solve, [0]-[15] count the cold pass and [20]-[21] both passes.
+ * attempt could still change the selection and was continued in FP64, [22]
+ * cells whose polished attempt the linear replay of the reference's line
+ * search showed stalling or near the iteration limit, so every attempt of the
+ * cell was continued in FP64 instead (every entry summed over the solve's
+ * cell ranges); [23]-[27] FP64 property evaluations
+ * of the feed phase (setup), the FP64 feed-test trial items, the FP64 review
+ * trial items, the Newton polish and the FP64 attempt continuations; [28]
+ * closed-form Jacobians the polish factorised and [29] its chord-step solves
+ * (the algorithmic work of each FP64 stage).  After a warm-start solve,
+ * [0]-[15] count the cold pass and [20]-[29] both passes.
  * Writes up to `capacity` values; returns the number available (0 for the
  * plain form).  Diagnostic entry point with no counterpart in the reference. */
 int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* handle, int64_t* out, int capacity);
@@ -486,21 +533,68 @@ int mpmc_gpu_flash_abi_version(void);
  * device memory and creates only as many slots as fit.  Results are per cell
  * and independent of what else is in the batch: a request's outputs are the
  * same alone and in any mix.  Flash fields only (status .. counters); the
- * sensitivity fields of `out` must be NULL.  The reference has no ln K warm
- * start (its hints are TPD start compositions), so none is applied: results
- * equal those of mpmc_gpu_flash_solve. */
+ * sensitivity fields of `out` must be NULL.  Without MPMC_SERVER_WARM_CACHE
+ * results equal those of mpmc_gpu_flash_solve.
+ *
+ * MPMC_SERVER_WARM_CACHE (mixed form): each mixture also keeps, on the device,
+ * the ln K of its recently solved two-phase cells, keyed by the composition
+ * (65,536 entries per mixture, a newer cell overwriting an older one in the
+ * same entry).  A cell of a later request with a cached composition, p within
+ * a factor exp(0.25) and T within 15 K starts from that ln K, as
+ * mpmc_gpu_flash_solve_warm does (one attempt from the start and the
+ * reference's final review; anything else takes the full cold solve).  A
+ * request's statuses then equal the cold solve's and its pairs agree with it
+ * to the polish tolerance, but its raw values depend on what was solved
+ * before.  The reference re-solves every request cold; its solve hints are
+ * TPD start compositions (pt_solve_hints.hpp:26-43). */
+#define MPMC_SERVER_WARM_CACHE 1
+
 typedef struct mpmc_server_options {
     int32_t device;
     int32_t slots;                /* batches in flight; 0 = 4 */
     int64_t max_batch_cells;      /* cells per device batch (and per request); 0 = 65536 */
     int64_t memory_budget_bytes;  /* device memory the server may hold; 0 = 40 GiB */
     int32_t form;                 /* MPMC_FORM_MIXED or MPMC_FORM_PLAIN_FP64 (= 0): set it explicitly */
-    int32_t flags;                /* reserved, 0 */
+    int32_t flags;                /* MPMC_SERVER_WARM_CACHE or 0 */
 } mpmc_server_options;
+
+/* Scheduling and admission policy of a server (mpmc_flash_server_set_policy,
+ * before the first submit; every field 0 = the default in brackets).
+ *  - small_request_cells: requests of at most this many cells are latency
+ *    requests [0: none].  The first `latency_slots` slots [0] serve only them,
+ *    on streams of the highest priority, in batches of at most
+ *    latency_batch_cells cells [max_batch_cells]; the other slots take them
+ *    only when no larger work waits.
+ *  - chunk_cells: a request is solved in tasks of at most this many cells
+ *    [max_batch_cells], so a large request's launches stay short and
+ *    interleave with others; max_request_cells [max_batch_cells] bounds a
+ *    request (at most 4096 chunks).
+ *  - max_in_flight: submitted and not yet completed requests [0: no limit];
+ *    a submit beyond it fails at once with MPMC_ERR_BUSY, as the reference
+ *    adapter refuses a solve beyond max_concurrent_solves
+ *    (pt_grpc_adapter.cpp:547-558, 622-626).
+ *  - max_deadline_us: the largest deadline mpmc_flash_server_submit_deadline
+ *    accepts [0: any], as the adapter's max_solve_deadline
+ *    (pt_grpc_adapter.cpp:377-396). */
+typedef struct mpmc_server_policy {
+    int64_t small_request_cells;
+    int32_t latency_slots;
+    int32_t pad;
+    int64_t latency_batch_cells;
+    int64_t chunk_cells;
+    int64_t max_request_cells;
+    int64_t max_in_flight;
+    int64_t max_deadline_us;
+} mpmc_server_policy;
 
 typedef struct mpmc_flash_server mpmc_flash_server;
 
 int mpmc_flash_server_create(const mpmc_server_options* options, mpmc_flash_server** out);
+
+/* Set the scheduling and admission policy (see mpmc_server_policy); before
+ * the first submit.  No counterpart in the reference beyond the limits cited
+ * there. */
+int mpmc_flash_server_set_policy(mpmc_flash_server* server, const mpmc_server_policy* policy);
 
 /* Register a mixture (validated like mpmc_gpu_flash_create); its id is used
  * by submit.  Up to 64 mixtures per server. */
@@ -513,6 +607,18 @@ int mpmc_flash_server_add_mixture(mpmc_flash_server* server, const mpmc_pr76_mix
 int mpmc_flash_server_submit(mpmc_flash_server* server, int32_t mixture_id, int64_t n_cells, const double* p,
                              const double* t, const double* z, const mpmc_flash_outputs* out, uint64_t* ticket);
 
+/* mpmc_flash_server_submit with a deadline deadline_us > 0 microseconds after
+ * the call, as the reference adapter requires a finite RPC deadline
+ * (pt_grpc_adapter.cpp:377-396): a request whose deadline passes before its
+ * tasks are launched is dropped, and one whose deadline passes before its
+ * results are published gets none; mpmc_flash_server_wait then returns
+ * MPMC_ERR_DEADLINE and the request's outputs are not written (rows of a task
+ * already scattered stay).  A deadline above the policy's max_deadline_us is
+ * MPMC_ERR_INVALID_ARGUMENT. */
+int mpmc_flash_server_submit_deadline(mpmc_flash_server* server, int32_t mixture_id, int64_t n_cells,
+                                      const double* p, const double* t, const double* z,
+                                      const mpmc_flash_outputs* out, int64_t deadline_us, uint64_t* ticket);
+
 /* Wait for a ticket (timeout_us < 0: no limit).  On return 0 the outputs are
  * written and *latency_s (optional) is the time from submit to completion.
  * MPMC_ERR_TIMEOUT if the time ran out; the request stays queued. */
@@ -520,7 +626,9 @@ int mpmc_flash_server_wait(mpmc_flash_server* server, uint64_t ticket, int64_t t
 
 /* Counters: [0] submitted, [1] completed, [2] device batches, [3] cells,
  * [4] slots, [5] device bytes per slot, [6] most requests in one batch,
- * [7] most slots busy at once.  Returns the number written. */
+ * [7] most slots busy at once, [8] submits refused by max_in_flight,
+ * [9] requests whose deadline passed, [10] requests in flight, [11] cells
+ * started from the warm-start cache.  Returns the number written. */
 int mpmc_flash_server_stats(mpmc_flash_server* server, int64_t* out, int capacity);
 
 /* Finish the queued requests, stop the worker and free everything. */

@@ -26,9 +26,10 @@ PROBE_LIB = os.path.join(LIBDIR, "libmpmc_gb300_probe.so")
 CAPACITIES = (4, 8, 12, 16, 20)
 # translation units compiled once per capacity
 PER_CAPACITY = ("flash_plain.cu", "sensitivity.cu", "flash_batched.cu", "flash_max3.cu", "chart.cu")
-# extra nvcc flags per translation unit: the max-3-phase continuation is a
-# rare, latency-irrelevant path whose large kernel takes ptxas minutes at -O3
-EXTRA_FLAGS = {"flash_max3.cu": ["-Xptxas", "-O1"]}
+# extra nvcc flags per translation unit (none: every unit at -O3; the
+# max-3-phase unit keeps its large FP64 routines out of line, which keeps its
+# -O3 build near 20 s)
+EXTRA_FLAGS: dict[str, list[str]] = {}
 # translation units compiled once
 SINGLE = ("capi.cu", "server.cu", "peak_probe.cu")
 

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/mpmc_gb300_flash.h"
@@ -57,6 +58,7 @@ constexpr size_t kMaxGraphs = 4;
 // One captured solve: the cell count and every buffer are baked into it.
 struct GraphEntry {
     int64_t ncell = 0;
+    bool sensitivity = true;  // the sensitivity stage is part of the graph
     const double *p = nullptr, *t = nullptr, *z = nullptr, *warm = nullptr;
     pr76::DeviceOutputs outputs{};
     cudaGraphExec_t exec = nullptr;
@@ -84,9 +86,19 @@ struct mpmc_gpu_flash {
     bool timed_warm = false;  // the last timed solve ran a warm and a cold pass
     DevBuf in_warm;     // host entry: staged ln K warm starts
     DevBuf outs3[5];    // host entry: staged three-phase outputs
-    DevBuf in_hints[4];   // host hinted entry: staged count, compositions, three-phase flags, fractions
+    DevBuf in_hints[7];   // host hinted entry: staged counts, compositions, three-phase flags, fractions
     DevBuf chart_in[2];   // host property-chart entry: staged chart values, dependent components
     DevBuf chart_out[3];  // host property-chart entry: staged status, values, Jacobian
+    // a large work-queue solve runs as cell ranges on these streams (fork/join
+    // by events on the caller's stream), each with its own workspace
+    cudaStream_t range_streams[8] = {};
+    cudaEvent_t fork_event = nullptr;
+    cudaEvent_t join_events[8] = {};
+    int last_ranges = 1;          // ranges of the last work-queue solve and their workspace offsets
+    size_t range_offset[8] = {};
+    cudaStream_t copy_stream = nullptr;  // host entry: copy-out overlapped with the sensitivity stage
+    cudaEvent_t flash_done = nullptr;
+    cudaEvent_t chunk_done[8] = {};
     int32_t shape[8] = {};  // explicit launch shape (mpmc_gpu_flash_set_launch_shape), 0 = default
     bool use_graphs = false;
     std::vector<GraphEntry> graphs;
@@ -223,6 +235,46 @@ pr76::BatchedShape batched_shape(const mpmc_gpu_flash* h, cudaEvent_t* events) {
     return shape;
 }
 
+constexpr int kMaxRanges = 8;
+constexpr int64_t kMinRangeCells = 65536;
+
+// Cell ranges of a work-queue solve: the handle's launch shape [7], else
+// MPMC_RANGES, else 1; each range keeps at least 65,536 cells.  Ranges on
+// separate streams let the long last items of one range overlap the bulk
+// stages of the others.  Measured on a GB300 at 1,048,576 cells (N = 10, 30 %
+// near a boundary, with sensitivities): 1 range 1097 ms, 2 1157 ms, 4 1140
+// ms, 8 1196 ms, every output identical -- the stages already fill the GPU,
+// so one range is the default.
+int solve_ranges(const mpmc_gpu_flash* h, int64_t ncell) {
+    int k = h->shape[7];
+    if (k <= 0)
+        if (const char* v = std::getenv("MPMC_RANGES")) k = std::atoi(v);
+    if (k <= 0) k = 1;
+    k = std::min(std::max(k, 1), kMaxRanges);
+    while (k > 1 && ncell / k < kMinRangeCells) --k;
+    return k;
+}
+
+// Range r of k over ncell cells: [c0, c1).
+void range_of(int64_t ncell, int k, int r, int64_t& c0, int64_t& c1) {
+    const int64_t step = (ncell + k - 1) / k;
+    c0 = std::min<int64_t>(ncell, r * step);
+    c1 = std::min<int64_t>(ncell, c0 + step);
+}
+
+// Workspace bytes of a solve in k ranges (each range's arrays 256-aligned);
+// fills the offsets when `offsets` is given.
+size_t ranged_workspace_bytes(int n, int64_t ncell, bool fp64_items, int k, size_t* offsets = nullptr) {
+    size_t off = 0;
+    for (int r = 0; r < k; ++r) {
+        int64_t c0, c1;
+        range_of(ncell, k, r, c0, c1);
+        if (offsets) offsets[r] = off;
+        off += (pr76::batched_workspace_bytes(n, c1 - c0, fp64_items) + 255) & ~static_cast<size_t>(255);
+    }
+    return off;
+}
+
 // Device scratch of a solve (allocated before any launch, so that a graph
 // capture of the launches sees no allocation).
 int prepare_device(mpmc_gpu_flash* h, int64_t ncell, pr76::DeviceOutputs& d) {
@@ -233,9 +285,19 @@ int prepare_device(mpmc_gpu_flash* h, int64_t ncell, pr76::DeviceOutputs& d) {
     if (h->form == MPMC_FORM_MIXED || h->form == MPMC_FORM_BATCHED) {
         if (ncell >= (int64_t{1} << 24))
             return fail(MPMC_ERR_INVALID_ARGUMENT, "batched forms: at most 16,777,215 cells per call");
-        const cudaError_t e =
-            h->workspace.ensure(pr76::batched_workspace_bytes(h->n, ncell, h->form == MPMC_FORM_BATCHED));
+        const int k = h->stage_timing ? 1 : solve_ranges(h, ncell);
+        cudaError_t e = h->workspace.ensure(ranged_workspace_bytes(h->n, ncell, h->form == MPMC_FORM_BATCHED, k));
         if (e != cudaSuccess) return cuda_fail(e, "batched workspace allocation");
+        if (k > 1 && !h->fork_event) {
+            if ((e = cudaEventCreateWithFlags(&h->fork_event, cudaEventDisableTiming)) != cudaSuccess)
+                return cuda_fail(e, "cudaEventCreate");
+            for (int r = 0; r < kMaxRanges; ++r) {
+                if ((e = cudaStreamCreateWithFlags(&h->range_streams[r], cudaStreamNonBlocking)) != cudaSuccess)
+                    return cuda_fail(e, "range stream");
+                if ((e = cudaEventCreateWithFlags(&h->join_events[r], cudaEventDisableTiming)) != cudaSuccess)
+                    return cuda_fail(e, "cudaEventCreate");
+            }
+        }
     } else if (h->form != MPMC_FORM_PLAIN_FP64) {
         return fail(MPMC_ERR_UNSUPPORTED, "algorithm form not available in this library");
     }
@@ -245,7 +307,8 @@ int prepare_device(mpmc_gpu_flash* h, int64_t ncell, pr76::DeviceOutputs& d) {
 // The launches of one solve on `stream` (no allocation, no synchronisation).
 cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
                            const double* warm, const pr76::DeviceOutputs& d, cudaStream_t stream, bool timing,
-                           const pr76::Max3Outputs* max3 = nullptr, const pr76::Hints* hints = nullptr) {
+                           const pr76::Max3Outputs* max3 = nullptr, const pr76::Hints* hints = nullptr,
+                           bool sensitivity = true) {
     cudaError_t e;
     int next_event = 0;
     auto record = [&]() {
@@ -261,8 +324,39 @@ cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, co
         shape.fp64_items = h->form == MPMC_FORM_BATCHED;
         shape.warm_lnk = warm;
         shape.redo_events = timing ? h->redo_events : nullptr;
-        e = pr76::launch_batched(h->n, h->d_mixture, ncell, p, t, z, d, h->workspace.ptr, h->workspace.bytes, shape,
-                                 stream);
+        const bool fp64_items = h->form == MPMC_FORM_BATCHED;
+        const int k = timing ? 1 : solve_ranges(h, ncell);
+        h->last_ranges = k;
+        ranged_workspace_bytes(h->n, ncell, fp64_items, k, h->range_offset);
+        if (k == 1) {
+            e = pr76::launch_batched(h->n, h->d_mixture, ncell, p, t, z, d, h->workspace.ptr, h->workspace.bytes,
+                                     shape, stream);
+        } else {
+            // each range a solve of its own on its own stream: every pointer at
+            // the range's start, rows at the whole batch's stride
+            e = cudaEventRecord(h->fork_event, stream);
+            for (int r = 0; r < k && e == cudaSuccess; ++r) {
+                int64_t c0, c1;
+                range_of(ncell, k, r, c0, c1);
+                cudaStream_t rs = h->range_streams[r];
+                if ((e = cudaStreamWaitEvent(rs, h->fork_event, 0)) != cudaSuccess) break;
+                pr76::DeviceOutputs dr = d;
+                void** f = reinterpret_cast<void**>(&dr);
+                for (int q = 0; q < kOutputFields; ++q) {
+                    if (!f[q]) continue;
+                    const size_t el = (q == 0 || q == 9 || q == 10) ? 4 : 8;
+                    f[q] = static_cast<char*>(f[q]) + static_cast<size_t>(c0) * el;
+                }
+                pr76::BatchedShape sr = shape;
+                sr.io_stride = ncell;
+                sr.warm_lnk = warm ? warm + c0 : nullptr;
+                const size_t bytes = pr76::batched_workspace_bytes(h->n, c1 - c0, fp64_items);
+                e = pr76::launch_batched(h->n, h->d_mixture, c1 - c0, p + c0, t + c0, z + c0, dr,
+                                         static_cast<char*>(h->workspace.ptr) + h->range_offset[r], bytes, sr, rs);
+                if (e == cudaSuccess) e = cudaEventRecord(h->join_events[r], rs);
+                if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, h->join_events[r], 0);
+            }
+        }
         next_event = timing ? pr76::kBatchedStages + 1 : 0;
     }
     if (e != cudaSuccess) return e;
@@ -270,7 +364,7 @@ cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, co
         e = pr76::launch_max3(h->n, h->d_mixture, ncell, p, t, z, d, *max3, stream, hints ? *hints : pr76::Hints{});
         if (e != cudaSuccess) return e;
     }
-    if (h->want_sensitivity) {
+    if (h->want_sensitivity && sensitivity) {
         e = pr76::launch_sensitivity(h->n, h->d_mixture, ncell, p, t, z, d, stream);
         if (e != cudaSuccess) return e;
     }
@@ -283,14 +377,17 @@ cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, co
 }
 
 bool same_key(const GraphEntry& g, int64_t ncell, const double* p, const double* t, const double* z,
-              const double* warm, const pr76::DeviceOutputs& d) {
-    return g.ncell == ncell && g.p == p && g.t == t && g.z == z && g.warm == warm &&
+              const double* warm, const pr76::DeviceOutputs& d, bool sensitivity) {
+    return g.ncell == ncell && g.sensitivity == sensitivity && g.p == p && g.t == t && g.z == z && g.warm == warm &&
            std::memcmp(&g.outputs, &d, sizeof(pr76::DeviceOutputs)) == 0;
 }
 
+// `sensitivity` false leaves the sensitivity stage to the caller (the
+// host-buffer entry runs it by cell ranges, overlapped with its copies).
 int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
                const double* warm, const pr76::DeviceOutputs& d_in, cudaStream_t stream,
-               const pr76::Max3Outputs* max3 = nullptr, const pr76::Hints* hints = nullptr) {
+               const pr76::Max3Outputs* max3 = nullptr, const pr76::Hints* hints = nullptr,
+               bool sensitivity = true) {
     if (warm && h->form == MPMC_FORM_PLAIN_FP64)
         return fail(MPMC_ERR_UNSUPPORTED,
                     "ln K warm starts need a work-queue form (MPMC_FORM_MIXED or MPMC_FORM_BATCHED); the plain "
@@ -307,13 +404,13 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
             if ((e = cudaEventCreate(&ev)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
     }
     if (!h->use_graphs || h->stage_timing || max3) {
-        e = enqueue_device(h, ncell, p, t, z, warm, d, stream, h->stage_timing, max3, hints);
+        e = enqueue_device(h, ncell, p, t, z, warm, d, stream, h->stage_timing, max3, hints, sensitivity);
         return e == cudaSuccess ? MPMC_OK : cuda_fail(e, "flash kernel launch");
     }
     // CUDA graph of the launch sequence, one per (cells, buffers): captured on
     // the handle's stream at the first call, replayed on `stream` afterwards
     for (GraphEntry& g : h->graphs) {
-        if (!same_key(g, ncell, p, t, z, warm, d)) continue;
+        if (!same_key(g, ncell, p, t, z, warm, d, sensitivity)) continue;
         g.last_use = ++h->graph_clock;
         e = cudaGraphLaunch(g.exec, stream);
         return e == cudaSuccess ? MPMC_OK : cuda_fail(e, "cudaGraphLaunch");
@@ -321,7 +418,7 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
     cudaGraph_t graph = nullptr;
     if ((e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
         return cuda_fail(e, "cudaStreamBeginCapture");
-    const cudaError_t le = enqueue_device(h, ncell, p, t, z, warm, d, h->stream, false);
+    const cudaError_t le = enqueue_device(h, ncell, p, t, z, warm, d, h->stream, false, nullptr, nullptr, sensitivity);
     e = cudaStreamEndCapture(h->stream, &graph);
     if (le != cudaSuccess || e != cudaSuccess) {
         if (graph) cudaGraphDestroy(graph);
@@ -332,6 +429,7 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
     entry.ncell = ncell;
+    entry.sensitivity = sensitivity;
     entry.p = p;
     entry.t = t;
     entry.z = z;
@@ -424,13 +522,14 @@ cudaError_t launch_batched(int n, const Mixture* d_mix, int64_t ncell, const dou
 }
 
 cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
-                               const double* z, const DeviceOutputs& out, cudaStream_t stream) {
+                               const double* z, const DeviceOutputs& out, cudaStream_t stream, int64_t c0,
+                               int64_t c1) {
     switch (capacity_for(n)) {
-    case 4: return launch_sensitivity_nm4(d_mix, ncell, p, t, z, out, stream);
-    case 8: return launch_sensitivity_nm8(d_mix, ncell, p, t, z, out, stream);
-    case 12: return launch_sensitivity_nm12(d_mix, ncell, p, t, z, out, stream);
-    case 16: return launch_sensitivity_nm16(d_mix, ncell, p, t, z, out, stream);
-    case 20: return launch_sensitivity_nm20(d_mix, ncell, p, t, z, out, stream);
+    case 4: return launch_sensitivity_nm4(d_mix, ncell, p, t, z, out, stream, c0, c1);
+    case 8: return launch_sensitivity_nm8(d_mix, ncell, p, t, z, out, stream, c0, c1);
+    case 12: return launch_sensitivity_nm12(d_mix, ncell, p, t, z, out, stream, c0, c1);
+    case 16: return launch_sensitivity_nm16(d_mix, ncell, p, t, z, out, stream, c0, c1);
+    case 20: return launch_sensitivity_nm20(d_mix, ncell, p, t, z, out, stream, c0, c1);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -474,9 +573,46 @@ cudaError_t launch_plain(int n, const Mixture* d_mix, int64_t ncell, const doubl
 }  // namespace pr76
 
 namespace {
+// Caller starts of either hinted entry, in the device's Hints layout (host or
+// device pointers).
+pr76::Hints hints_of(const mpmc_start_hints* h) {
+    pr76::Hints d;
+    d.count = h->count;
+    d.x = h->composition;
+    d.three = h->three_phase;
+    d.fraction = h->fraction;
+    return d;
+}
+pr76::Hints hints_of(const mpmc_start_hints_ex* h) {
+    pr76::Hints d;
+    d.count = h->initial_count;
+    d.x = h->initial_composition;
+    d.final_count = h->final_count;
+    d.final_x = h->final_composition;
+    d.three = h->three_phase;
+    d.three_x = h->three_phase_composition;
+    d.fraction = h->fraction;
+    d.separate = 1;
+    d.initial_automatic_starts = h->initial_automatic_starts != 0;
+    d.max_split_attempts = h->max_split_attempts;
+    return d;
+}
+int check_hints_ex(const mpmc_start_hints_ex* h) {
+    if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "hinted solve: null hints");
+    if ((h->initial_count != nullptr) != (h->initial_composition != nullptr) ||
+        (h->final_count != nullptr) != (h->final_composition != nullptr) ||
+        (h->three_phase != nullptr) != (h->three_phase_composition != nullptr) ||
+        (h->three_phase != nullptr) != (h->fraction != nullptr))
+        return fail(MPMC_ERR_INVALID_ARGUMENT, "hinted solve: each start class needs its count (or flag) and "
+                                               "composition arrays together, the three-phase start its fractions");
+    if (h->max_split_attempts < 0 || h->max_split_attempts > 65536)
+        return fail(MPMC_ERR_INVALID_ARGUMENT, "hinted solve: max_split_attempts must be in [0, 65536]");
+    return MPMC_OK;
+}
+
 int solve_host(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
                const double* ln_k_warm, const mpmc_flash_outputs* out, const mpmc_three_phase_outputs* out3,
-               bool max3, const mpmc_start_hints* hints = nullptr);
+               bool max3, const pr76::Hints* hints = nullptr);
 
 // Validates a property-chart call and fills the kernel's closure constants
 // (the checks of the closure's constructor, pr76_selected_phase_property_closure.hpp:274-319,
@@ -529,18 +665,24 @@ int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* h, int64_t* out, int capacity) {
     constexpr int kSlots[] = {8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 20, 22, 23, 24, 25, 27, 28, 29, 30, 31, 32, 33,
                               -34, -36, -38, -40, -42, 44, 45};
     constexpr int kCount = static_cast<int>(sizeof(kSlots) / sizeof(kSlots[0]));
-    int vals[48] = {};
     if (cudaSetDevice(h->device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return 0;
-    // the counters are the first array of the workspace
-    if (cudaMemcpy(vals, h->workspace.ptr, sizeof(vals), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
-    for (int k = 0; k < kCount && k < capacity; ++k) {
-        if (!out) continue;
-        if (kSlots[k] >= 0) {
-            out[k] = vals[kSlots[k]];
-        } else {
-            unsigned long long v = 0;
-            std::memcpy(&v, vals - kSlots[k], sizeof(v));
-            out[k] = static_cast<int64_t>(v);
+    for (int k = 0; k < kCount && k < capacity; ++k)
+        if (out) out[k] = 0;
+    // the counters are the first array of each range's workspace; sums over ranges
+    for (int r = 0; r < h->last_ranges; ++r) {
+        int vals[48] = {};
+        if (cudaMemcpy(vals, static_cast<char*>(h->workspace.ptr) + h->range_offset[r], sizeof(vals),
+                       cudaMemcpyDeviceToHost) != cudaSuccess)
+            return 0;
+        for (int k = 0; k < kCount && k < capacity; ++k) {
+            if (!out) continue;
+            if (kSlots[k] >= 0) {
+                out[k] += vals[kSlots[k]];
+            } else {
+                unsigned long long v = 0;
+                std::memcpy(&v, vals - kSlots[k], sizeof(v));
+                out[k] += static_cast<int64_t>(v);
+            }
         }
     }
     return kCount;
@@ -622,6 +764,21 @@ int mpmc_gpu_flash_destroy(mpmc_gpu_flash* h) {
     for (auto& ev : h->events)
         if (ev) cudaEventDestroy(ev);
     for (auto& ev : h->redo_events)
+        if (ev) cudaEventDestroy(ev);
+    if (h->copy_stream) {
+        cudaStreamSynchronize(h->copy_stream);
+        cudaStreamDestroy(h->copy_stream);
+    }
+    for (int r = 0; r < kMaxRanges; ++r) {
+        if (h->range_streams[r]) {
+            cudaStreamSynchronize(h->range_streams[r]);
+            cudaStreamDestroy(h->range_streams[r]);
+        }
+        if (h->join_events[r]) cudaEventDestroy(h->join_events[r]);
+    }
+    if (h->fork_event) cudaEventDestroy(h->fork_event);
+    if (h->flash_done) cudaEventDestroy(h->flash_done);
+    for (auto& ev : h->chunk_done)
         if (ev) cudaEventDestroy(ev);
     for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);
     if (h->d_mixture) cudaFree(h->d_mixture);
@@ -737,7 +894,18 @@ int mpmc_gpu_flash_solve_hinted(mpmc_gpu_flash* h, int64_t ncell, const double* 
         (hints->three_phase != nullptr) != (hints->fraction != nullptr))
         return fail(MPMC_ERR_INVALID_ARGUMENT, "hinted solve: count and composition required, three_phase and "
                                                "fraction together");
-    return solve_host(h, ncell, p, t, z, nullptr, out, out3, true, hints);
+    const pr76::Hints hh = hints_of(hints);
+    return solve_host(h, ncell, p, t, z, nullptr, out, out3, true, &hh);
+}
+
+int mpmc_gpu_flash_solve_hinted_ex(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t,
+                                   const double* z, const mpmc_start_hints_ex* hints, const mpmc_flash_outputs* out,
+                                   const mpmc_three_phase_outputs* out3) {
+    if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
+    const int rc = check_hints_ex(hints);
+    if (rc != MPMC_OK) return rc;
+    const pr76::Hints hh = hints_of(hints);
+    return solve_host(h, ncell, p, t, z, nullptr, out, out3, true, &hh);
 }
 
 int mpmc_gpu_flash_solve_device_hinted(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t,
@@ -758,7 +926,28 @@ int mpmc_gpu_flash_solve_device_hinted(mpmc_gpu_flash* h, int64_t ncell, const d
     if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
     pr76::Max3Outputs m3{};
     if (out3) m3 = {out3->max3_status, out3->phase_fraction, out3->composition, out3->ln_phi, out3->z_factor};
-    const pr76::Hints dh{hints->count, hints->composition, hints->three_phase, hints->fraction};
+    const pr76::Hints dh = hints_of(hints);
+    return run_device(h, ncell, p, t, z, nullptr, to_device_outputs(out), static_cast<cudaStream_t>(stream), &m3,
+                      &dh);
+}
+
+int mpmc_gpu_flash_solve_device_hinted_ex(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t,
+                                          const double* z, const mpmc_start_hints_ex* hints,
+                                          const mpmc_flash_outputs* out, const mpmc_three_phase_outputs* out3,
+                                          void* stream) {
+    if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
+    if (ncell < 0) return fail(MPMC_ERR_INVALID_ARGUMENT, "negative cell count");
+    const int rc = check_hints_ex(hints);
+    if (rc != MPMC_OK) return rc;
+    if (ncell == 0) return MPMC_OK;
+    if (!p || !t || !z) return fail(MPMC_ERR_INVALID_ARGUMENT, "p, t and z must not be null");
+    if (!out || !out->status || !out->ln_k)
+        return fail(MPMC_ERR_INVALID_ARGUMENT, "hinted solve: the status and ln_k outputs are required");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaSetDevice");
+    pr76::Max3Outputs m3{};
+    if (out3) m3 = {out3->max3_status, out3->phase_fraction, out3->composition, out3->ln_phi, out3->z_factor};
+    const pr76::Hints dh = hints_of(hints);
     return run_device(h, ncell, p, t, z, nullptr, to_device_outputs(out), static_cast<cudaStream_t>(stream), &m3,
                       &dh);
 }
@@ -834,7 +1023,7 @@ namespace {
 // requested outputs back, synchronise.
 int solve_host(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
                const double* ln_k_warm, const mpmc_flash_outputs* out, const mpmc_three_phase_outputs* out3,
-               bool max3, const mpmc_start_hints* hints) {
+               bool max3, const pr76::Hints* hints) {
     if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
     if (max3 && (!out || !out->status || !out->ln_k))
         return fail(MPMC_ERR_INVALID_ARGUMENT, "max-3-phase solve: the status and ln_k outputs are required");
@@ -895,27 +1084,87 @@ int solve_host(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
         m3 = {static_cast<int32_t*>(dev3[0]), static_cast<double*>(dev3[1]), static_cast<double*>(dev3[2]),
               static_cast<double*>(dev3[3]), static_cast<double*>(dev3[4])};
     }
-    // caller start hints: staged like the inputs
+    // caller start hints: every array present staged like the inputs
     pr76::Hints dh{};
     if (hints) {
-        const size_t bytes[4] = {nc * sizeof(int32_t), 3 * n * nc * sizeof(double),
-                                 hints->three_phase ? nc * sizeof(int32_t) : 0,
-                                 hints->three_phase ? 2 * nc * sizeof(double) : 0};
-        const void* src[4] = {hints->count, hints->composition, hints->three_phase, hints->fraction};
-        for (int k = 0; k < 4; ++k) {
-            if (!bytes[k]) continue;
-            if ((e = h->in_hints[k].ensure(bytes[k])) != cudaSuccess) return cuda_fail(e, "hint staging allocation");
-            if ((e = cudaMemcpyAsync(h->in_hints[k].ptr, src[k], bytes[k], cudaMemcpyHostToDevice, s)) != cudaSuccess)
-                return cuda_fail(e, "hint copy");
-        }
-        dh = {static_cast<const int32_t*>(h->in_hints[0].ptr), static_cast<const double*>(h->in_hints[1].ptr),
-              hints->three_phase ? static_cast<const int32_t*>(h->in_hints[2].ptr) : nullptr,
-              hints->three_phase ? static_cast<const double*>(h->in_hints[3].ptr) : nullptr};
+        dh = *hints;
+        int slot = 0;
+        auto stage = [&](auto*& field, size_t bytes) -> cudaError_t {
+            DevBuf& b = h->in_hints[slot++];
+            if (!field) return cudaSuccess;
+            cudaError_t err = b.ensure(bytes);
+            if (err == cudaSuccess) err = cudaMemcpyAsync(b.ptr, field, bytes, cudaMemcpyHostToDevice, s);
+            if (err == cudaSuccess) field = static_cast<std::remove_reference_t<decltype(field)>>(b.ptr);
+            return err;
+        };
+        const size_t counts = nc * sizeof(int32_t), comps = 3 * n * nc * sizeof(double);
+        if ((e = stage(dh.count, counts)) != cudaSuccess || (e = stage(dh.x, comps)) != cudaSuccess ||
+            (e = stage(dh.final_count, counts)) != cudaSuccess || (e = stage(dh.final_x, comps)) != cudaSuccess ||
+            (e = stage(dh.three, counts)) != cudaSuccess || (e = stage(dh.three_x, comps)) != cudaSuccess ||
+            (e = stage(dh.fraction, 2 * nc * sizeof(double))) != cudaSuccess)
+            return cuda_fail(e, "hint staging");
     }
-    const int rc = run_device(h, ncell, static_cast<const double*>(h->in_p.ptr),
-                              static_cast<const double*>(h->in_t.ptr), static_cast<const double*>(h->in_z.ptr),
-                              d_warm, to_device_outputs(&dev_out), s, max3 ? &m3 : nullptr, hints ? &dh : nullptr);
+    // With sensitivities requested, the copy-out overlaps the sensitivity
+    // stage: it runs by cell ranges on `s` while a second stream copies the
+    // flash fields, then each finished range's derivative rows.
+    bool overlap = h->want_sensitivity && !max3 && !hints && !h->stage_timing;
+    bool any_sens = false;
+    for (int k = 10; k < kOutputFields; ++k) any_sens = any_sens || *field_ptr(&host_out, k) != nullptr;
+    overlap = overlap && any_sens;
+    const double* dp_ = static_cast<const double*>(h->in_p.ptr);
+    const double* dt_ = static_cast<const double*>(h->in_t.ptr);
+    const double* dz_ = static_cast<const double*>(h->in_z.ptr);
+    const int rc = run_device(h, ncell, dp_, dt_, dz_, d_warm, to_device_outputs(&dev_out), s, max3 ? &m3 : nullptr,
+                              hints ? &dh : nullptr, !overlap);
     if (rc != MPMC_OK) return rc;
+    if (overlap) {
+        constexpr int kChunks = 8;
+        if (!h->copy_stream) {
+            if ((e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking)) != cudaSuccess)
+                return cuda_fail(e, "copy stream");
+            if ((e = cudaEventCreateWithFlags(&h->flash_done, cudaEventDisableTiming)) != cudaSuccess)
+                return cuda_fail(e, "cudaEventCreate");
+            for (auto& ev : h->chunk_done)
+                if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess)
+                    return cuda_fail(e, "cudaEventCreate");
+        }
+        cudaStream_t cs = h->copy_stream;
+        pr76::DeviceOutputs d = to_device_outputs(&dev_out);
+        const int irc = with_sensitivity_inputs(h, ncell, d);  // the scratch run_device routed them to
+        if (irc != MPMC_OK) return irc;
+        if ((e = cudaEventRecord(h->flash_done, s)) != cudaSuccess || (e = cudaStreamWaitEvent(cs, h->flash_done, 0)) !=
+                                                                          cudaSuccess)
+            return cuda_fail(e, "copy stream ordering");
+        for (int k = 0; k < 10; ++k) {
+            void* hp = *field_ptr(&host_out, k);
+            if (!hp) continue;
+            if ((e = cudaMemcpyAsync(hp, h->outs[k].ptr, per_cell[k] * elem[k] * nc, cudaMemcpyDeviceToHost, cs)) !=
+                cudaSuccess)
+                return cuda_fail(e, "output copy");
+        }
+        const int64_t step = (ncell + kChunks - 1) / kChunks;
+        for (int c = 0; c < kChunks; ++c) {
+            const int64_t c0 = c * step, c1 = std::min<int64_t>(ncell, c0 + step);
+            if (c0 >= c1) break;
+            e = pr76::launch_sensitivity(h->n, h->d_mixture, ncell, dp_, dt_, dz_, d, s, c0, c1);
+            if (e != cudaSuccess) return cuda_fail(e, "sensitivity kernel launch");
+            if ((e = cudaEventRecord(h->chunk_done[c], s)) != cudaSuccess ||
+                (e = cudaStreamWaitEvent(cs, h->chunk_done[c], 0)) != cudaSuccess)
+                return cuda_fail(e, "copy stream ordering");
+            for (int k = 10; k < kOutputFields; ++k) {
+                char* hp = static_cast<char*>(*field_ptr(&host_out, k));
+                if (!hp) continue;
+                const size_t el = elem[k], pitch = nc * el;
+                const char* dv = static_cast<const char*>(h->outs[k].ptr);
+                if ((e = cudaMemcpy2DAsync(hp + c0 * el, pitch, dv + c0 * el, pitch, static_cast<size_t>(c1 - c0) * el,
+                                           per_cell[k], cudaMemcpyDeviceToHost, cs)) != cudaSuccess)
+                    return cuda_fail(e, "output copy");
+            }
+        }
+        if ((e = cudaStreamSynchronize(cs)) != cudaSuccess || (e = cudaStreamSynchronize(s)) != cudaSuccess)
+            return cuda_fail(e, "flash execution");
+        return MPMC_OK;
+    }
     for (int k = 0; k < kOutputFields; ++k) {
         void* hp = *field_ptr(&host_out, k);
         if (!hp) continue;

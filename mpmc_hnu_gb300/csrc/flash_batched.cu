@@ -99,6 +99,7 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     const bool fp64_items = shape.fp64_items != 0;
     if (carve(ws, nullptr, n, ncell, fp64_items) > scratch_bytes || scratch == nullptr) return cudaErrorInvalidValue;
     carve(ws, static_cast<char*>(scratch), n, ncell, fp64_items);
+    ws.io_stride = shape.io_stride > 0 ? shape.io_stride : ncell;
     int device = 0, sms = 0;
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);

@@ -1,6 +1,7 @@
 // Max-3-phase continuation kernel (pr76_max3.cuh).  A rare path (only cells
-// whose two-phase answer is phase_set_unstable do work), so its translation
-// unit is compiled with light ptxas optimisation to keep the build short.
+// whose two-phase answer is phase_set_unstable do work); its large FP64
+// routines stay out of line (MPMC_FP64_CALL), which keeps the unit's build
+// short.
 #define MPMC_FP64_CALL __noinline__
 #include "launch.h"
 #include "pr76_hints.cuh"
@@ -57,8 +58,8 @@ __global__ void __launch_bounds__(64) max3_kernel(const Mixture* __restrict__ mi
             CellHints<NM> hs;
             load_hints<NM>(hints, feed, n, ncell, cell, hs);
             if (temp_setup(m, c))
-                r = max3_cell(m, c, feed, lnk, s, hs.count > 0 ? hs.ptr : nullptr, hs.count,
-                              hs.has_three ? hs.three : nullptr);
+                r = max3_cell(m, c, feed, lnk, s, hs.fcount > 0 ? hs.fptr : nullptr, hs.fcount,
+                              hs.has_three ? hs.three : nullptr, hs.options);
             else
                 r.status = -1;
             m3 = r.status;

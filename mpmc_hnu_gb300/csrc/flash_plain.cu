@@ -48,8 +48,9 @@ __device__ void plain_cell(const Mixture& m, int64_t ncell, int64_t cell, const 
     // (solve_pt_vle's initial_starts and final_starts, pt_split.hpp:415-419)
     CellHints<NM> hs;
     const bool hints_ok = load_hints<NM>(hints, feed, c.n, ncell, cell, hs);
-    const double* const* extra = hs.count > 0 ? hs.ptr : nullptr;
-    const int status = hints_ok ? solve_cell(m, c, feed, w, r, extra, hs.count, extra, hs.count) : kInvalid;
+    const int status = hints_ok ? solve_cell(m, c, feed, w, r, hs.count > 0 ? hs.ptr : nullptr, hs.count,
+                                             hs.fcount > 0 ? hs.fptr : nullptr, hs.fcount, hs.options)
+                                : kInvalid;
     const int n = c.n;
     const double nan = __longlong_as_double(0x7ff8000000000000LL);
     auto put = [&](double* a, int k, double v) {

@@ -66,6 +66,8 @@ struct BatchedShape {
     // the cell cold); null = cold solve of every cell
     const double* warm_lnk;
     cudaEvent_t* redo_events;  // optional: the events of the cold pass after a warm pass
+    int64_t io_stride;         // stride of z, the warm starts and the outputs (0 = ncell): a solve of one
+                               // cell range of a larger batch, with every pointer at the range's start
 };
 constexpr int kBatchedStages = 17;
 
@@ -83,11 +85,23 @@ cudaError_t launch_batched(int n, const Mixture* d_mix, int64_t ncell, const dou
 // three compositions are also a three-phase start whose phase-1 and phase-2
 // fractions are fraction[k * ncell + c].  Device pointers; count == null
 // means no hints.
+// Caller starts of solve_pr76_pt_max3 / solve_pt_vle, cell-fastest:
+// composition k of cell c, component i at (k * n + i) * ncell + c.  With
+// `separate` 0 (the continuation's hints) the `count` compositions are the
+// initial and the final starts and, when three of them, the three-phase start;
+// with `separate` 1 the final starts and the three-phase start have arrays of
+// their own.
 struct Hints {
-    const int32_t* count;
-    const double* x;
-    const int32_t* three;
-    const double* fraction;
+    const int32_t* count = nullptr;  // initial starts (0..3 per cell)
+    const double* x = nullptr;
+    const int32_t* three = nullptr;  // nonzero: a three-phase start
+    const double* fraction = nullptr;  // its phase_fraction_seed [2 * ncell]
+    const int32_t* final_count = nullptr;
+    const double* final_x = nullptr;
+    const double* three_x = nullptr;
+    int separate = 0;
+    int initial_automatic_starts = 1;  // options.two_phase.initial_stability.automatic_starts
+    int max_split_attempts = 16;       // options.two_phase.max_split_attempts
 };
 
 // Three-phase outputs of the max-3-phase continuation (layout a[k * ncell + c];
@@ -140,17 +154,20 @@ cudaError_t launch_plain(int n, const Mixture* d_mix, int64_t ncell, const doubl
                          const double* z, const DeviceOutputs& out, cudaStream_t stream,
                          const Hints& hints = Hints{});
 
-// Implicit sensitivity of accepted two-phase cells (sensitivity.cu); reads the
-// flash fields of `out` (status, beta, x, y, lnk, z_l, z_v), which must be set.
+// Implicit sensitivity of accepted two-phase cells (sensitivity.cu) among the
+// cells [c0, c1) of the batch (c1 < 0: to the end); reads the flash fields of
+// `out` (status, beta, x, y, lnk, z_l, z_v), which must be set.
 cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
-                               const double* z, const DeviceOutputs& out, cudaStream_t stream);
+                               const double* z, const DeviceOutputs& out, cudaStream_t stream, int64_t c0 = 0,
+                               int64_t c1 = -1);
 
 #define MPMC_DECLARE_PLAIN(NM)                                                                         \
     cudaError_t launch_plain_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t, \
                                     const double* z, const DeviceOutputs& out, cudaStream_t stream,       \
                                     const Hints& hints);                                                  \
     cudaError_t launch_sensitivity_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t, \
-                                          const double* z, const DeviceOutputs& out, cudaStream_t stream); \
+                                          const double* z, const DeviceOutputs& out, cudaStream_t stream,      \
+                                          int64_t c0, int64_t c1);                                             \
     cudaError_t launch_max3_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t,      \
                                    const double* z, const DeviceOutputs& out, const Max3Outputs& out3,           \
                                    cudaStream_t stream, const Hints& hints);                                      \

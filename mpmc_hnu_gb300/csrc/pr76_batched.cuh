@@ -176,6 +176,8 @@ struct Workspace {
     int* s64_count;         // [ncell]
     int s64_capacity;
     int fp64_items;         // FP64 work-queue form: every attempt item runs from its FP64 seed
+    int64_t io_stride;      // stride of the caller's z and output rows (the whole batch when this
+                            // solve is one cell range of it; the pointers start at the range)
 };
 
 // A cell of the warm pass that runs from its warm start: a rejected pair sends
@@ -258,7 +260,7 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
         cell.t = t[c];
         for (int k = 0; k < cCount; ++k) cell.counters[k] = 0;
         double feed[NM];
-        for (int i = 0; i < cell.n; ++i) feed[i] = z[idx(i, ws.ncell, c)];
+        for (int i = 0; i < cell.n; ++i) feed[i] = z[idx(i, ws.io_stride, c)];
         int ph = pPending;
         if (!isfinite(cell.p) || cell.p <= 0.0 || !isfinite(cell.t) || cell.t <= 0.0 ||
             !fp64::normalise_feed(cell, feed) || !fp64::temp_setup(m, cell)) {
@@ -275,7 +277,7 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
             double contrast = 0.0;
             for (int i = 0; i < cell.n; ++i) {
                 if (cell.z[i] == 0.0) continue;
-                const double v = ws.warm_lnk[idx(i, ws.ncell, c)];
+                const double v = ws.warm_lnk[idx(i, ws.io_stride, c)];
                 warm = warm && isfinite(v) && fabs(v) < 700.0;
                 contrast = fmax(contrast, fabs(v));
             }
@@ -318,9 +320,9 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
                 const double sign = k == 0 ? 1.0 : -1.0;
                 double largest = -INFINITY, sum = 0.0;
                 for (int i = 0; i < cell.n; ++i)
-                    if (cell.z[i] > 0.0) largest = fmax(largest, cell.lz[i] + sign * ws.warm_lnk[idx(i, ws.ncell, c)]);
+                    if (cell.z[i] > 0.0) largest = fmax(largest, cell.lz[i] + sign * ws.warm_lnk[idx(i, ws.io_stride, c)]);
                 for (int i = 0; i < cell.n; ++i)
-                    if (cell.z[i] > 0.0) sum += exp(cell.lz[i] + sign * ws.warm_lnk[idx(i, ws.ncell, c)] - largest);
+                    if (cell.z[i] > 0.0) sum += exp(cell.lz[i] + sign * ws.warm_lnk[idx(i, ws.io_stride, c)] - largest);
                 ls[k] = largest + log(sum);
             }
             double shift = 0.0;
@@ -331,7 +333,7 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
                 else if (ls[1] < margin) shift = ls[1] - margin;
             }
             for (int i = 0; i < cell.n; ++i) {
-                const double v = cell.z[i] > 0.0 ? ws.warm_lnk[idx(i, ws.ncell, c)] + shift : 0.0;
+                const double v = cell.z[i] > 0.0 ? ws.warm_lnk[idx(i, ws.io_stride, c)] + shift : 0.0;
                 ws.att_lnk[idx(i, ws.ncell, c)] = static_cast<float>(v);
                 if (ws.att_lnk64) ws.att_lnk64[idx(i, ws.ncell, c)] = v;
             }
@@ -357,7 +359,7 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
             if (out.status) out.status[c] = ph == pInvalid ? static_cast<int>(kInvalid) : static_cast<int>(kIndeterminate);
             if (out.beta) out.beta[c] = nan;
             for (int i = 0; i < cell.n; ++i) {
-                const int64_t k = idx(i, ws.ncell, c);
+                const int64_t k = idx(i, ws.io_stride, c);
                 if (out.x) out.x[k] = nan;
                 if (out.y) out.y[k] = nan;
                 if (out.lnk) out.lnk[k] = nan;
@@ -367,7 +369,7 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
             if (out.z_l) out.z_l[c] = nan;
             if (out.z_v) out.z_v[c] = nan;
             if (out.counters)
-                for (int k = 0; k < cCount; ++k) out.counters[idx(k, ws.ncell, c)] = cell.counters[k];
+                for (int k = 0; k < cCount; ++k) out.counters[idx(k, ws.io_stride, c)] = cell.counters[k];
         }
         if (ph == pPending) {
             const int slot = atomicAdd(&ws.counters[qTrialCells], 1);
@@ -659,12 +661,12 @@ __device__ void write_single(const DeviceOutputs& out, const Workspace& ws, int6
     if (out.status) out.status[c] = kSinglePhase;
     if (out.beta) out.beta[c] = nan;
     for (int i = 0; i < n; ++i) {
-        const int64_t k = idx(i, ws.ncell, c);
-        if (out.x) out.x[k] = ws.z[k];
-        if (out.y) out.y[k] = nan;
-        if (out.lnk) out.lnk[k] = nan;
-        if (out.lnphi_l) out.lnphi_l[k] = ws.ref_lnphi[k];
-        if (out.lnphi_v) out.lnphi_v[k] = nan;
+        const int64_t k = idx(i, ws.ncell, c), o = idx(i, ws.io_stride, c);
+        if (out.x) out.x[o] = ws.z[k];
+        if (out.y) out.y[o] = nan;
+        if (out.lnk) out.lnk[o] = nan;
+        if (out.lnphi_l) out.lnphi_l[o] = ws.ref_lnphi[k];
+        if (out.lnphi_v) out.lnphi_v[o] = nan;
     }
     if (out.z_l) out.z_l[c] = ws.ref_z[c];
     if (out.z_v) out.z_v[c] = nan;
@@ -678,7 +680,7 @@ __device__ void write_status_only(const DeviceOutputs& out, const Workspace& ws,
     if (out.status) out.status[c] = status;
     if (out.beta) out.beta[c] = with_pair ? ws.cand_s[idx(0, ws.ncell, c)] : nan;
     for (int i = 0; i < n; ++i) {
-        const int64_t k = idx(i, ws.ncell, c);
+        const int64_t k = idx(i, ws.io_stride, c);
         if (out.x) out.x[k] = with_pair ? ws.cand[idx(0 * NM + i, ws.ncell, c)] : nan;
         if (out.y) out.y[k] = with_pair ? ws.cand[idx(1 * NM + i, ws.ncell, c)] : nan;
         if (out.lnk) out.lnk[k] = with_pair ? ws.cand[idx(2 * NM + i, ws.ncell, c)] : nan;
@@ -692,7 +694,7 @@ __device__ void write_status_only(const DeviceOutputs& out, const Workspace& ws,
 template <int NM>
 __device__ void write_counters(const DeviceOutputs& out, const Workspace& ws, int64_t c) {
     if (!out.counters) return;
-    for (int k = 0; k < cCount; ++k) out.counters[idx(k, ws.ncell, c)] = ws.counters_out[idx(k, ws.ncell, c)];
+    for (int k = 0; k < cCount; ++k) out.counters[idx(k, ws.io_stride, c)] = ws.counters_out[idx(k, ws.ncell, c)];
 }
 
 // ---------------------------------------------------------------------------
@@ -1593,7 +1595,7 @@ __global__ void __launch_bounds__(64) fallback_kernel(const Mixture* __restrict_
         cell.t = t[c];
         for (int k = 0; k < cCount; ++k) cell.counters[k] = 0;
         double feed[NM];
-        for (int i = 0; i < cell.n; ++i) feed[i] = z[idx(i, ws.ncell, c)];
+        for (int i = 0; i < cell.n; ++i) feed[i] = z[idx(i, ws.io_stride, c)];
         Scratch<NM> w;
         CellResult<NM> r;
         const int status = solve_cell(m, cell, feed, w, r);
@@ -1605,7 +1607,7 @@ __global__ void __launch_bounds__(64) fallback_kernel(const Mixture* __restrict_
         const SplitState<NM>& b = w.best;
         if (out.beta) out.beta[c] = pair ? b.beta : nan;
         for (int i = 0; i < n; ++i) {
-            const int64_t k = idx(i, ws.ncell, c);
+            const int64_t k = idx(i, ws.io_stride, c);
             const bool single = status == kSinglePhase;
             if (out.x) out.x[k] = pair ? b.x[i] : (single ? cell.z[i] : nan);
             if (out.y) out.y[k] = pair ? b.y[i] : nan;
@@ -1617,7 +1619,7 @@ __global__ void __launch_bounds__(64) fallback_kernel(const Mixture* __restrict_
         if (out.z_v) out.z_v[c] = pair ? b.z_v : nan;
         if (out.counters)
             for (int k = 0; k < cCount; ++k)
-                out.counters[idx(k, ws.ncell, c)] = ws.counters_out[idx(k, ws.ncell, c)] + cell.counters[k];
+                out.counters[idx(k, ws.io_stride, c)] = ws.counters_out[idx(k, ws.ncell, c)] + cell.counters[k];
     }
 }
 

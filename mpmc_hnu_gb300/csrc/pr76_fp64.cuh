@@ -973,23 +973,52 @@ __device__ bool normalise_feed(Cell<NM>& c, const double* feed) {
     return true;
 }
 
+// The two PtSplitOptions fields a caller may change (pt_split.hpp:45-50):
+// initial_stability.automatic_starts and max_split_attempts.
+struct SolveOptions {
+    bool initial_automatic_starts = true;
+    int max_split_attempts = 16;
+};
+
+// A caller start must be a composition with the raw feed's support (a
+// domain_error in the reference: pt_stability.hpp:263-272, pt_split.hpp:436-443).
+template <int NM>
+__device__ bool start_on_support(const double* feed, int n, const double* s) {
+    double ssum;
+    if (!check_composition(s, n, ssum)) return false;
+    for (int i = 0; i < n; ++i)
+        if ((feed[i] > 0.0) != (s[i] > 0.0)) return false;
+    return true;
+}
+
 // `init_extra` (n_init of them) join the automatic feed-test starts and
 // `final_extra` (n_final, at most 3) precede the pair's x and y in the review,
 // as solve_pt_vle's initial_starts / final_starts (pt_split.hpp:415-419, 512).
+// Every caller start is checked before the first property call, final starts
+// first (pt_split.hpp:436-443, pt_stability.hpp:254-272).
 template <int NM>
 __device__ MPMC_FP64_CALL int solve_cell(const Mixture& m, Cell<NM>& c, const double* feed_in, Scratch<NM>& w,
                           CellResult<NM>& out, const double* const* init_extra = nullptr, int n_init = 0,
-                          const double* const* final_extra = nullptr, int n_final = 0) {
+                          const double* const* final_extra = nullptr, int n_final = 0,
+                          const SolveOptions& opt = SolveOptions{}) {
     const int n = c.n;
     out.has_pair = false;
     if (!isfinite(c.p) || c.p <= 0.0 || !isfinite(c.t) || c.t <= 0.0) return kInvalid;
     if (!normalise_feed(c, feed_in)) return kInvalid;
+    for (int k = 0; k < n_final && k < 3; ++k)
+        if (!start_on_support<NM>(feed_in, n, final_extra[k])) return kInvalid;
+    int active = 0;
+    for (int i = 0; i < n; ++i) active += feed_in[i] > 0.0;
+    const int n_auto = active == 1 ? 1 : active + 2;
+    // the feed test's automatic starts, off on the caller's request; a test
+    // with no start at all is a length_error in the reference
+    const int n_auto_init = opt.initial_automatic_starts ? n_auto : 0;
+    if (n_auto_init + n_init == 0) return kInvalid;
+    for (int k = 0; k < n_init; ++k)
+        if (!start_on_support<NM>(feed_in, n, init_extra[k])) return kInvalid;
     for (int i = 0; i < n; ++i)
         if (feed_in[i] > 0.0 && c.z[i] == 0.0) return kIndeterminate;
     if (!temp_setup(m, c)) return kInvalid;
-    int active = 0;
-    for (int i = 0; i < n; ++i) active += c.z[i] > 0.0;
-    const int n_auto = active == 1 ? 1 : active + 2;
     // ---- initial stability: reference phase at the feed
     int evals = 1;
     bool smooth_ref;
@@ -1002,10 +1031,8 @@ __device__ MPMC_FP64_CALL int solve_cell(const Mixture& m, Cell<NM>& c, const do
     bool negative_found = false, all_stationary = true;
     int attempts = 0, split_evals = 0;
     bool limit = false;
-    for (int k = 0; k < n_init; ++k)
-        if (!start_matches_feed(c, init_extra[k])) return kInvalid;
-    for (int k = 0; k < n_auto + n_init; ++k) {
-        make_start(c, k, active, init_extra, n_auto, w.point.w);
+    for (int k = 0; k < n_auto_init + n_init; ++k) {
+        make_start(c, k, active, init_extra, n_auto_init, w.point.w);
         const int ts = run_trial(m, c, out.ref_lnphi, so, w.point, w.next, w.direction, w.lnphi, evals);
         if (ts < 0) return kInvalid;
         all_stationary = all_stationary && ts == kStationary;
@@ -1014,7 +1041,7 @@ __device__ MPMC_FP64_CALL int solve_cell(const Mixture& m, Cell<NM>& c, const do
         // split attempts of this witness, pt_split.hpp:459-486
         if (limit) continue;
         for (int role = 0; role < 2; ++role) {
-            if (attempts >= 16 || split_evals >= 20000) {
+            if (attempts >= opt.max_split_attempts || split_evals >= 20000) {
                 limit = true;
                 break;
             }
@@ -1067,10 +1094,7 @@ __device__ MPMC_FP64_CALL int solve_cell(const Mixture& m, Cell<NM>& c, const do
     int fevals = 0;
     const double* review_extra[5];
     int n_review = 0;
-    for (int k = 0; k < n_final && k < 3; ++k) {
-        if (!start_matches_feed(c, final_extra[k])) return kInvalid;
-        review_extra[n_review++] = final_extra[k];
-    }
+    for (int k = 0; k < n_final && k < 3; ++k) review_extra[n_review++] = final_extra[k];
     review_extra[n_review++] = cand.x;
     review_extra[n_review++] = cand.y;
     for (int k = 0; k < n_auto + n_review; ++k) {

@@ -12,9 +12,26 @@ struct CellHints {
     double x[3][NM];
     const double* ptr[3];
     int count;
+    double fx[3][NM];
+    const double* fptr[3];
+    int fcount;
     bool has_three;
     double three[3 * NM + 2];  // the three compositions, then the fractions of phases 1 and 2
+    SolveOptions options;
 };
+
+template <int NM>
+__device__ int load_set(const int32_t* count, const double* x, int n, int64_t ncell, int64_t cell,
+                        double (&dst)[3][NM], const double* (&ptr)[3]) {
+    if (count == nullptr || x == nullptr) return 0;
+    int k = count[cell];
+    k = k < 0 ? 0 : (k > 3 ? 3 : k);
+    for (int q = 0; q < k; ++q) {
+        for (int i = 0; i < n; ++i) dst[q][i] = x[(static_cast<int64_t>(q) * n + i) * ncell + cell];
+        ptr[q] = dst[q];
+    }
+    return k;
+}
 
 // Loads cell `cell`'s hints.  False when its three-phase start fails the
 // reference's start check (pr76_three_phase.hpp:211-244: fractions inside
@@ -22,25 +39,28 @@ struct CellHints {
 template <int NM>
 __device__ bool load_hints(const Hints& h, const double* feed, int n, int64_t ncell, int64_t cell,
                            CellHints<NM>& out) {
-    out.count = 0;
     out.has_three = false;
-    if (h.count == nullptr || h.x == nullptr) return true;
-    int k = h.count[cell];
-    k = k < 0 ? 0 : (k > 3 ? 3 : k);
-    for (int q = 0; q < k; ++q) {
-        for (int i = 0; i < n; ++i) out.x[q][i] = h.x[(static_cast<int64_t>(q) * n + i) * ncell + cell];
-        out.ptr[q] = out.x[q];
+    out.options.initial_automatic_starts = h.initial_automatic_starts != 0;
+    out.options.max_split_attempts = h.max_split_attempts;
+    out.count = load_set<NM>(h.count, h.x, n, ncell, cell, out.x, out.ptr);
+    if (h.separate) {
+        out.fcount = load_set<NM>(h.final_count, h.final_x, n, ncell, cell, out.fx, out.fptr);
+    } else {
+        out.fcount = out.count;
+        for (int q = 0; q < out.count; ++q) out.fptr[q] = out.ptr[q];
     }
-    out.count = k;
-    if (h.three == nullptr || h.fraction == nullptr || h.three[cell] == 0 || k != 3) return true;
+    const double* tx = h.separate ? h.three_x : h.x;
+    if (h.three == nullptr || h.fraction == nullptr || tx == nullptr || h.three[cell] == 0 ||
+        (!h.separate && out.count != 3))
+        return true;
     const double f1 = h.fraction[cell], f2 = h.fraction[ncell + cell];
     if (!rr3_feasible(f1, f2)) return false;
     for (int q = 0; q < 3; ++q) {
+        for (int i = 0; i < n; ++i) out.three[q * n + i] = tx[(static_cast<int64_t>(q) * n + i) * ncell + cell];
         double sum;
-        if (!check_composition(out.x[q], n, sum)) return false;
+        if (!check_composition(out.three + q * n, n, sum)) return false;
         for (int i = 0; i < n; ++i)
-            if ((feed[i] > 0.0) != (out.x[q][i] > 0.0)) return false;
-        for (int i = 0; i < n; ++i) out.three[q * n + i] = out.x[q][i];
+            if ((feed[i] > 0.0) != (out.three[q * n + i] > 0.0)) return false;
     }
     out.three[3 * n] = f1;
     out.three[3 * n + 1] = f2;

@@ -401,11 +401,13 @@ __device__ MPMC_FP64_CALL int three_review(const Mixture& m, Cell<NM>& c, Max3Sc
 // the extra final-review starts the base solve ran with, ahead of the pair,
 // and `three_hint` (3 n compositions, then the fractions of phases 1 and 2)
 // is a three-phase start whose attempts run first, one per combination of
-// root sides (:457-486), with their own quota of 16.
+// root sides (:457-486), with their own quota of 16.  `opt` are the caller's
+// two-phase options, which the fresh two-phase neighbour of a phase
+// disappearance runs with (:413-415).
 template <int NM>
 __device__ Max3Result max3_cell(const Mixture& m, Cell<NM>& c, const double* feed, const double* lnk,
                                 Max3Scratch<NM>& s, const double* const* hints = nullptr, int n_hints = 0,
-                                const double* three_hint = nullptr) {
+                                const double* three_hint = nullptr, const SolveOptions& opt = SolveOptions{}) {
     const int n = c.n;
     Max3Result r{kM3Indeterminate, false, false};
     c.newton = false;  // the reference's bisection roots and RR
@@ -470,7 +472,8 @@ __device__ Max3Result max3_cell(const Mixture& m, Cell<NM>& c, const double* fee
                     keep[1][i] = starts[1][i];
                 }
                 const double* kst[2] = {keep[0], keep[1]};
-                const int nst = solve_cell(m, c, nfeed, s.w, nb, kst, 2, kst, 2);
+                // with the caller's two-phase options (pr76_three_phase.hpp:413-415)
+                const int nst = solve_cell(m, c, nfeed, s.w, nb, kst, 2, kst, 2, opt);
                 c.newton = false;
                 if (nst == kTwoPhase) {
                     r.status = kM3Two;

@@ -39,20 +39,21 @@ __device__ void nan_fill(int n, int64_t ncell, int64_t cell, const DeviceOutputs
 // cells without an accepted pair, and stops at its next two-phase cell; then
 // the warp differentiates those cells together.  A quarter of the cells are
 // two-phase at the bench distribution, so a plain grid-stride loop would keep
-// three lanes of four idle through the FP64 work.
+// three lanes of four idle through the FP64 work.  Cells [c0, c1) of the
+// ncell-cell batch.
 template <int NM>
 __global__ void __launch_bounds__(64) sensitivity_kernel(const Mixture* __restrict__ mix_g, int64_t ncell,
-                                                         const double* __restrict__ p,
+                                                         int64_t c0, int64_t c1, const double* __restrict__ p,
                                                          const double* __restrict__ t,
                                                          const double* __restrict__ z, DeviceOutputs out) {
     __shared__ Mixture m;
     stage_mixture(mix_g, m);
     const int n = m.n;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    int64_t next = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t next = c0 + static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     for (;;) {
         int64_t cell = -1;
-        while (next < ncell) {
+        while (next < c1) {
             const int64_t c = next;
             next += stride;
             if (out.status[c] == kTwoPhase) {
@@ -94,16 +95,18 @@ __global__ void __launch_bounds__(64) sensitivity_kernel(const Mixture* __restri
 
 cudaError_t MPMC_CAT(launch_sensitivity_nm, MPMC_NM)(const Mixture* d_mix, int64_t ncell, const double* p,
                                                        const double* t, const double* z, const DeviceOutputs& out,
-                                                       cudaStream_t stream) {
-    if (ncell <= 0) return cudaSuccess;
+                                                       cudaStream_t stream, int64_t c0, int64_t c1) {
+    if (c1 < 0) c1 = ncell;
+    if (c1 <= c0) return cudaSuccess;
     int device = 0, sms = 0;
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const int block = 64;  // a multiple of the warp: every lane reaches the warp vote
     int64_t grid = static_cast<int64_t>(sms) * 4;
-    const int64_t needed = (ncell + block - 1) / block;
+    const int64_t needed = (c1 - c0 + block - 1) / block;
     if (grid > needed) grid = needed;
-    sensitivity_kernel<MPMC_NM><<<static_cast<unsigned>(grid), block, 0, stream>>>(d_mix, ncell, p, t, z, out);
+    sensitivity_kernel<MPMC_NM><<<static_cast<unsigned>(grid), block, 0, stream>>>(d_mix, ncell, c0, c1, p, t, z,
+                                                                                   out);
     return cudaGetLastError();
 }
 

@@ -81,6 +81,14 @@ class _StartHints(ctypes.Structure):
                 ("fraction", ctypes.c_void_p)]
 
 
+class _StartHintsEx(ctypes.Structure):
+    _fields_ = [("initial_count", ctypes.c_void_p), ("initial_composition", ctypes.c_void_p),
+                ("final_count", ctypes.c_void_p), ("final_composition", ctypes.c_void_p),
+                ("three_phase", ctypes.c_void_p), ("three_phase_composition", ctypes.c_void_p),
+                ("fraction", ctypes.c_void_p), ("initial_automatic_starts", ctypes.c_int32),
+                ("max_split_attempts", ctypes.c_int32)]
+
+
 # selected-phase property chart (mpmc_property_chart_spec / _outputs)
 class _ChartSpec(ctypes.Structure):
     _fields_ = [("phase_count", ctypes.c_int32), ("root_index", ctypes.c_int32 * 3),
@@ -133,6 +141,17 @@ class _ServerOptions(ctypes.Structure):
                 ("memory_budget_bytes", ctypes.c_int64), ("form", ctypes.c_int32), ("flags", ctypes.c_int32)]
 
 
+class _ServerPolicy(ctypes.Structure):
+    _fields_ = [("small_request_cells", ctypes.c_int64), ("latency_slots", ctypes.c_int32), ("pad", ctypes.c_int32),
+                ("latency_batch_cells", ctypes.c_int64), ("chunk_cells", ctypes.c_int64),
+                ("max_request_cells", ctypes.c_int64), ("max_in_flight", ctypes.c_int64),
+                ("max_deadline_us", ctypes.c_int64)]
+
+
+SERVER_WARM_CACHE = 1
+ERR_TIMEOUT, ERR_BUSY, ERR_DEADLINE = 5, 6, 7
+
+
 EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu_flash_solve",
                     "mpmc_gpu_flash_solve_device", "mpmc_gpu_flash_components", "mpmc_gpu_flash_last_error",
                     "mpmc_gpu_flash_abi_version", "mpmc_gpu_flash_stage_timings", "mpmc_gpu_flash_batch_stats",
@@ -141,14 +160,18 @@ EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu
                     "mpmc_flash_server_destroy", "mpmc_gpu_flash_set_launch_shape", "mpmc_gpu_flash_solve_warm",
                     "mpmc_gpu_flash_solve_device_warm", "mpmc_gpu_flash_solve_max3", "mpmc_gpu_flash_solve_device_max3",
                     "mpmc_gpu_flash_property_chart", "mpmc_gpu_flash_property_chart_device",
-                    "mpmc_gpu_flash_solve_hinted", "mpmc_gpu_flash_solve_device_hinted"]
+                    "mpmc_gpu_flash_solve_hinted", "mpmc_gpu_flash_solve_device_hinted",
+                    "mpmc_flash_server_set_policy", "mpmc_flash_server_submit_deadline",
+                    "mpmc_gpu_flash_solve_hinted_ex", "mpmc_gpu_flash_solve_device_hinted_ex"]
 FLAG_CUDA_GRAPH = 2
 NOALLOC_SCRATCH_BYTES = 48 << 20
 BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun", "fallback_nonsmooth",
                "fp64_attempts_no_fp32", "fp64_attempts_polish_failed", "fp64_attempts_rejected", "fallback_load",
                "two_candidates", "fp64_trial_items", "fp64_attempt_items", "polished_cells", "select64_cells",
                "slow_trials_skipped", "limit_attempts", "warm_cells", "warm_redo",
-               "warm_redo_no_pair", "warm_redo_unstable", "competing_cells", "competing_cells_fp64"]
+               "warm_redo_no_pair", "warm_redo_unstable", "competing_cells", "competing_cells_fp64", "replay_risk_cells",
+               "fp64_evals_setup", "fp64_evals_feed_trials", "fp64_evals_review_trials", "fp64_evals_polish",
+               "fp64_evals_split64", "polish_jacobians", "polish_solves"]
 FLAG_STAGE_TIMING = 1
 _QUEUE_STAGES = ["setup", "feed_trials", "feed_classify", "feed_trials64", "decide", "split", "polish",
                  "open32", "compete", "split64", "select64", "relist", "review_trials", "review_classify", "review_trials64",
@@ -202,6 +225,9 @@ def library() -> ctypes.CDLL:
             [ctypes.c_void_p] * 3 + [ctypes.POINTER(_Outputs), ctypes.POINTER(ctypes.c_uint64)]
         lib.mpmc_flash_server_wait.argtypes = [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int64,
                                                ctypes.POINTER(ctypes.c_double)]
+        lib.mpmc_flash_server_set_policy.argtypes = [ctypes.c_void_p, ctypes.POINTER(_ServerPolicy)]
+        lib.mpmc_flash_server_submit_deadline.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64] + \
+            [ctypes.c_void_p] * 3 + [ctypes.POINTER(_Outputs), ctypes.c_int64, ctypes.POINTER(ctypes.c_uint64)]
         lib.mpmc_flash_server_stats.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         lib.mpmc_flash_server_destroy.argtypes = [ctypes.c_void_p]
         lib.mpmc_gpu_flash_set_launch_shape.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
@@ -347,6 +373,57 @@ class GpuFlash:
         return ({f: (v[0] if rows[f] == 1 else v) for f, v in out.items()},
                 {f: (v[0] if v.shape[0] == 1 else v) for f, v in out3.items()})
 
+    def solve_hinted_ex(self, p, t, z, hints: dict, fields: list[str] | None = None):
+        """`solve_max3` with the general caller inputs of solve_pr76_pt_max3
+        (mpmc_gpu_flash_solve_hinted_ex).  `hints` holds initial_count [ncell]
+        and initial_composition [3 n, ncell] (initial starts), final_count /
+        final_composition (final starts), three_phase [ncell] /
+        three_phase_composition [3 n, ncell] / fraction [2, ncell] (one
+        three-phase start), initial_automatic_starts and max_split_attempts;
+        a missing start class is no starts of that class.  Returns (flash
+        outputs, three-phase outputs)."""
+        p = np.ascontiguousarray(p, dtype=np.float64)
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        z = np.ascontiguousarray(z, dtype=np.float64)
+        if z.shape != (self.n, p.shape[0]) or t.shape != p.shape:
+            raise ValueError("expected p[ncell], t[ncell], z[n, ncell]")
+        ncell = p.shape[0]
+        keep = {}
+
+        def arr(name, dtype, shape):
+            v = hints.get(name)
+            if v is None:
+                return None
+            a = np.ascontiguousarray(v, dtype=dtype)
+            if a.shape != shape:
+                raise ValueError(f"expected {name} of shape {shape}")
+            keep[name] = a
+            return a.ctypes.data
+
+        h = _StartHintsEx(arr("initial_count", np.int32, (ncell,)),
+                          arr("initial_composition", np.float64, (3 * self.n, ncell)),
+                          arr("final_count", np.int32, (ncell,)),
+                          arr("final_composition", np.float64, (3 * self.n, ncell)),
+                          arr("three_phase", np.int32, (ncell,)),
+                          arr("three_phase_composition", np.float64, (3 * self.n, ncell)),
+                          arr("fraction", np.float64, (2, ncell)),
+                          int(bool(hints.get("initial_automatic_starts", True))),
+                          int(hints.get("max_split_attempts", 16)))
+        fields = fields or self.fields()
+        for need in ("status", "ln_k"):
+            if need not in fields:
+                fields = fields + [need]
+        rows = output_rows(self.n)
+        dtypes = {f: d for f, d, _ in OUTPUT_FIELDS}
+        out = {f: np.empty((rows[f], ncell), dtypes[f]) for f in fields}
+        out3 = {f: np.empty((r(self.n), ncell), d) for f, d, r in THREE_PHASE_FIELDS}
+        s = _Outputs(**{f: out[f].ctypes.data for f in fields})
+        s3 = _ThreePhaseOutputs(**{f: v.ctypes.data for f, v in out3.items()})
+        _check(library().mpmc_gpu_flash_solve_hinted_ex(self._h, ncell, p.ctypes.data, t.ctypes.data, z.ctypes.data,
+                                                        ctypes.byref(h), ctypes.byref(s), ctypes.byref(s3)))
+        return ({f: (v[0] if rows[f] == 1 else v) for f, v in out.items()},
+                {f: (v[0] if v.shape[0] == 1 else v) for f, v in out3.items()})
+
     def property_chart(self, spec: PropertyChartSpec, q, dependent=None, jacobian: bool = True) -> dict:
         """Selected-phase property chart of every cell (mpmc_gpu_flash_property_chart):
         q [(P n + 1), ncell] natural variables, dependent [P, ncell] pivot
@@ -393,8 +470,8 @@ class GpuFlash:
 
     def batch_stats(self) -> dict[str, int]:
         """Work statistics of the last mixed-form solve."""
-        out = np.zeros(32, np.int64)
-        k = library().mpmc_gpu_flash_batch_stats(self._h, out.ctypes.data, 32)
+        out = np.zeros(64, np.int64)
+        k = library().mpmc_gpu_flash_batch_stats(self._h, out.ctypes.data, 64)
         return {BATCH_STATS[i]: int(out[i]) for i in range(min(k, len(BATCH_STATS)))}
 
     def stage_timings(self) -> dict[str, float]:
@@ -427,7 +504,10 @@ class GpuFlash:
 
 
 SERVER_STATS = ["submitted", "completed", "batches", "cells", "slots", "slot_bytes", "most_requests_in_batch",
-                "most_slots_busy"]
+                "most_slots_busy", "refused_busy", "expired", "in_flight", "warm_cells"]
+# mpmc_server_policy fields, in order
+SERVER_POLICY = ["small_request_cells", "latency_slots", "latency_batch_cells", "chunk_cells", "max_request_cells",
+                 "max_in_flight", "max_deadline_us"]
 
 
 class FlashServer:
@@ -437,11 +517,19 @@ class FlashServer:
     the output arrays it allocates are kept alive here until `wait()`."""
 
     def __init__(self, device: int = 0, slots: int = 4, max_batch_cells: int = 65536,
-                 memory_budget_bytes: int = 40 << 30, form: str = "mixed"):
-        o = _ServerOptions(device, slots, max_batch_cells, memory_budget_bytes, FORMS[form], 0)
+                 memory_budget_bytes: int = 40 << 30, form: str = "mixed", warm_cache: bool = False,
+                 policy: dict | None = None):
+        o = _ServerOptions(device, slots, max_batch_cells, memory_budget_bytes, FORMS[form],
+                           SERVER_WARM_CACHE if warm_cache else 0)
         h = ctypes.c_void_p()
         _check(library().mpmc_flash_server_create(ctypes.byref(o), ctypes.byref(h)))
         self._h = h
+        if policy:
+            unknown = set(policy) - set(SERVER_POLICY)
+            if unknown:
+                raise ValueError(f"unknown policy fields {sorted(unknown)}")
+            pol = _ServerPolicy(**{k: int(policy.get(k, 0)) for k in SERVER_POLICY})
+            _check(library().mpmc_flash_server_set_policy(self._h, ctypes.byref(pol)))
         self._n = {}
         self._keep = {}
         self._mix_keep = []
@@ -456,7 +544,8 @@ class FlashServer:
         self._n[mid.value] = int(mixture.n)
         return mid.value
 
-    def submit(self, mixture_id: int, p, t, z, fields: list[str] | None = None) -> int:
+    def submit(self, mixture_id: int, p, t, z, fields: list[str] | None = None,
+               deadline_s: float | None = None) -> int:
         n = self._n[mixture_id]
         p = np.ascontiguousarray(p, dtype=np.float64)
         t = np.ascontiguousarray(t, dtype=np.float64)
@@ -467,8 +556,16 @@ class FlashServer:
         out = {f: np.empty((rows[f], ncell), dtypes[f]) for f in (fields or FLASH_FIELDS)}
         s = _Outputs(**{f: v.ctypes.data for f, v in out.items()})
         ticket = ctypes.c_uint64()
-        _check(library().mpmc_flash_server_submit(self._h, mixture_id, ncell, p.ctypes.data, t.ctypes.data,
-                                                  z.ctypes.data, ctypes.byref(s), ctypes.byref(ticket)))
+        if deadline_s is None:
+            _check(library().mpmc_flash_server_submit(self._h, mixture_id, ncell, p.ctypes.data, t.ctypes.data,
+                                                      z.ctypes.data, ctypes.byref(s), ctypes.byref(ticket)))
+        else:
+            us = int(round(deadline_s * 1e6))
+            if deadline_s > 0:
+                us = max(us, 1)
+            _check(library().mpmc_flash_server_submit_deadline(self._h, mixture_id, ncell, p.ctypes.data,
+                                                               t.ctypes.data, z.ctypes.data, ctypes.byref(s), us,
+                                                               ctypes.byref(ticket)))
         self._keep[ticket.value] = (p, t, z, out)
         return ticket.value
 
@@ -476,13 +573,16 @@ class FlashServer:
         """Outputs of the request and its submit-to-completion latency (s)."""
         lat = ctypes.c_double()
         tmo = -1 if timeout_s is None else int(timeout_s * 1e6)
-        _check(library().mpmc_flash_server_wait(self._h, ticket, tmo, ctypes.byref(lat)))
-        _, _, _, out = self._keep.pop(ticket)
+        rc = library().mpmc_flash_server_wait(self._h, ticket, tmo, ctypes.byref(lat))
+        # the ticket is spent unless the wait timed out (the request stays queued)
+        kept = self._keep.pop(ticket, None) if rc != ERR_TIMEOUT else None
+        _check(rc)
+        out = kept[3]
         return {f: (v[0] if v.shape[0] == 1 else v) for f, v in out.items()}, lat.value
 
     def stats(self) -> dict[str, int]:
-        out = np.zeros(8, np.int64)
-        k = library().mpmc_flash_server_stats(self._h, out.ctypes.data, 8)
+        out = np.zeros(len(SERVER_STATS), np.int64)
+        k = library().mpmc_flash_server_stats(self._h, out.ctypes.data, len(SERVER_STATS))
         return {SERVER_STATS[i]: int(out[i]) for i in range(k)}
 
     def close(self) -> None:

@@ -72,7 +72,14 @@ def make_mixture(n: int, seed: int) -> Mixture:
 
 def make_cells(n: int, ncell: int, seed: int, offset: int = 0):
     """(p [Pa], T [K], z [n, ncell]) for cells offset .. offset+ncell-1."""
-    c = np.arange(offset, offset + ncell, dtype=np.uint64)
+    return make_cells_at(n, np.arange(offset, offset + ncell, dtype=np.uint64), seed)
+
+
+def make_cells_at(n: int, index, seed: int):
+    """(p [Pa], T [K], z [n, len(index)]) for the cells at counter positions
+    `index` (make_cells draws a contiguous range of them)."""
+    c = np.asarray(index, dtype=np.uint64)
+    ncell = c.size
     e = np.empty((n, ncell))
     for i in range(n):
         u = uniform(seed, S_Z, c * np.uint64(n) + np.uint64(i))

@@ -494,6 +494,7 @@ struct StabilityOptions {  // :44-56
     int max_iterations = 512;
     int max_backtracks = 32;
     long long max_evaluations = 100000;
+    bool automatic_starts = true;  // :55, feed, uniform and 0.1 z + 0.9 e_i starts
 };
 enum TrialStatus {
     kNegativeTpd, kStationary, kIterationLimit, kEvaluationLimit, kLineSearchFailed,
@@ -596,6 +597,8 @@ inline bool stability_test(const Model& m, Work& wk, double p, double t, const s
     if (!check_composition(feed_in.data(), n, input_sum)) return false;
     int active = 0;
     for (double v : feed_in) active += v > 0;
+    // :254-262: no start at all is a length_error in the reference
+    if ((o.automatic_starts ? (active == 1 ? 1 : active + 2) : 0) + extra.size() == 0) return false;
     for (const auto& s : extra) {  // :263-272, a domain_error in the reference
         double ssum;
         if (static_cast<int>(s.size()) != n || !check_composition(s.data(), n, ssum)) return false;
@@ -614,8 +617,8 @@ inline bool stability_test(const Model& m, Work& wk, double p, double t, const s
         tr.initial = std::move(s);
         res.trials.push_back(std::move(tr));
     };
-    add_start(res.feed);  // :294-310
-    if (active > 1) {
+    if (o.automatic_starts) add_start(res.feed);  // :294-310
+    if (o.automatic_starts && active > 1) {
         std::vector<double> uniform(n, 0.0);
         for (int i = 0; i < n; ++i)
             if (res.feed[i] > 0) uniform[i] = 1.0 / static_cast<double>(active);
@@ -1085,12 +1088,20 @@ struct FlashResult {
     long long split_evaluations = 0;
 };
 
+// The two PtSplitOptions fields a caller changes here (pt_split.hpp:45-50):
+// initial_stability.automatic_starts and max_split_attempts.
+struct VleOptions {
+    bool initial_automatic_starts = true;
+    int max_split_attempts = 16;
+};
+
 // pt_split.hpp:415-525 with its optional extra starts: `initial_starts` join
 // the automatic feed-test starts, `final_starts` precede the pair's x and y in
 // the review.
 inline FlashResult solve_vle(const Model& m, Work& wk, double p, double t, const std::vector<double>& feed,
                              const std::vector<std::vector<double>>& initial_starts = {},
-                             const std::vector<std::vector<double>>& final_starts = {}) {
+                             const std::vector<std::vector<double>>& final_starts = {},
+                             const VleOptions& vo = {}) {
     FlashResult res;
     const int n = m.n;
     double sum;
@@ -1099,7 +1110,21 @@ inline FlashResult solve_vle(const Model& m, Work& wk, double p, double t, const
         res.status = kInvalid;
         return res;
     }
+    // the final starts are checked before any property call (:436-443)
+    for (const auto& w : final_starts) {
+        double wsum;
+        if (static_cast<int>(w.size()) != n || !check_composition(w.data(), n, wsum)) {
+            res.status = kInvalid;
+            return res;
+        }
+        for (int i = 0; i < n; ++i)
+            if ((feed[i] > 0) != (w[i] > 0)) {
+                res.status = kInvalid;
+                return res;
+            }
+    }
     StabilityOptions so;
+    so.automatic_starts = vo.initial_automatic_starts;
     SplitOptions sp;
     if (!stability_test(m, wk, p, t, feed, so, initial_starts, {}, res.initial)) {
         res.status = kInvalid;
@@ -1120,7 +1145,7 @@ inline FlashResult solve_vle(const Model& m, Work& wk, double p, double t, const
         const Trial& wit = res.initial.trials[k];
         if (wit.status != kNegativeTpd || !wit.has_point || !stability_negative(wit.point, so)) continue;
         for (bool as_vapor : {true, false}) {
-            if (res.attempts >= 16 || res.split_evaluations >= sp.max_evaluations) {
+            if (res.attempts >= vo.max_split_attempts || res.split_evaluations >= sp.max_evaluations) {
                 limit = true;
                 break;
             }
@@ -1153,7 +1178,7 @@ inline FlashResult solve_vle(const Model& m, Work& wk, double p, double t, const
     }
     const double gibbs_change = cand.gibbs - feed_g;
     const double gibbs_guard = cand.guard + 256 * kEps * magnitude;
-    StabilityOptions fo = so;
+    StabilityOptions fo;  // final_stability: the defaults, automatic starts on
     fo.tpd_tolerance += 0.5 * cand.fug_norm;
     if (!std::isfinite(gibbs_change) || !std::isfinite(gibbs_guard) || !std::isfinite(fo.tpd_tolerance)) {
         res.status = kIndeterminate;
@@ -1593,7 +1618,7 @@ struct ThreeStart {
 inline Max3Result solve_max3(const Model& m, Work& wk, double p, double t, const std::vector<double>& feed,
                              const std::vector<std::vector<double>>& initial_starts = {},
                              const std::vector<std::vector<double>>& final_starts = {},
-                             const std::vector<ThreeStart>& three_starts = {}) {
+                             const std::vector<ThreeStart>& three_starts = {}, const VleOptions& vo = {}) {
     Max3Result r;
     // pr76_pt_max3_check_starts, :211-244: a bad start is a domain_error
     for (const ThreeStart& st : three_starts) {
@@ -1614,7 +1639,7 @@ inline Max3Result solve_max3(const Model& m, Work& wk, double p, double t, const
                 }
         }
     }
-    r.base = solve_vle(m, wk, p, t, feed, initial_starts, final_starts);
+    r.base = solve_vle(m, wk, p, t, feed, initial_starts, final_starts, vo);
     switch (r.base.status) {
     case kInvalid: r.status = -1; return r;
     case kSinglePhase: r.status = kM3Single; return r;
@@ -1649,7 +1674,8 @@ inline Max3Result solve_max3(const Model& m, Work& wk, double p, double t, const
             for (int k = 0; k < 3; ++k)
                 if (k != eq.disappearing) starts.push_back(eq.point.x[k]);
             if (starts.size() == 2) {
-                FlashResult nb = solve_vle(m, wk, p, t, nfeed, starts, starts);
+                // options.two_phase again (pr76_three_phase.hpp:413-415)
+                FlashResult nb = solve_vle(m, wk, p, t, nfeed, starts, starts, vo);
                 if (nb.status == kTwoPhase) {
                     r.neighbor = nb;
                     r.has_neighbor = true;
@@ -2626,9 +2652,36 @@ int oracle_property_chart_batch(int n, const double* tc, const double* pc, const
     return 0;
 }
 
-int oracle_max3_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+// Caller starts and options of solve_pr76_pt_max3 (pr76_three_phase.hpp:328-341;
+// the split options of pt_split.hpp:45-50).  Compositions are cell-fastest:
+// composition k of cell c, component i at (k * n + i) * ncell + c.
+struct StartHints {
+    const int32_t* initial_count;      // [ncell], 0..3 initial_starts (NULL: none)
+    const double* initial_x;           // [3 n ncell]
+    const int32_t* final_count;        // [ncell], 0..3 final_starts (NULL: none)
+    const double* final_x;             // [3 n ncell]
+    const int32_t* three_phase;        // [ncell], nonzero: one three-phase start (NULL: none)
+    const double* three_x;             // [3 n ncell]
+    const double* fraction;            // [2 ncell]: phase_fraction_seed of phases 1 and 2
+    int32_t initial_automatic_starts;  // options.two_phase.initial_stability.automatic_starts
+    int32_t max_split_attempts;        // options.two_phase.max_split_attempts
+};
+
+static void hint_set(const int32_t* count, const double* x, int n, int64_t ncell, int64_t c,
+                     std::vector<std::vector<double>>& out) {
+    out.clear();
+    if (!count || !x) return;
+    const int k = std::min(3, std::max(0, static_cast<int>(count[c])));
+    for (int q = 0; q < k; ++q) {
+        std::vector<double> w(n);
+        for (int i = 0; i < n; ++i) w[i] = x[(static_cast<int64_t>(q) * n + i) * ncell + c];
+        out.push_back(std::move(w));
+    }
+}
+
+static int max3_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
                       int64_t ncell, const double* p, const double* t, const double* z, int threads,
-                      const Max3Outputs* o) {
+                      const Max3Outputs* o, const StartHints* h) {
     if (n < 1 || n > 256 || ncell < 0 || !tc || !pc || !omega || !kij || !p || !t || !z || !o) return -1;
     const oracle::Model m = oracle::make_model(n, tc, pc, omega, kij);
     auto run = [&](int64_t lo, int64_t hi) {
@@ -2636,7 +2689,29 @@ int oracle_max3_batch(int n, const double* tc, const double* pc, const double* o
         Work wk;
         wk.init(n);
         std::vector<double> feed(n);
+        std::vector<std::vector<double>> init, fin;
+        std::vector<ThreeStart> three;
+        VleOptions vo;
+        if (h) {
+            vo.initial_automatic_starts = h->initial_automatic_starts != 0;
+            vo.max_split_attempts = h->max_split_attempts;
+        }
         for (int64_t c = lo; c < hi; ++c) {
+            three.clear();
+            if (h) {
+                hint_set(h->initial_count, h->initial_x, n, ncell, c, init);
+                hint_set(h->final_count, h->final_x, n, ncell, c, fin);
+                if (h->three_phase && h->three_x && h->fraction && h->three_phase[c]) {
+                    ThreeStart st;
+                    for (int q = 0; q < 3; ++q) {
+                        st.x[q].resize(n);
+                        for (int i = 0; i < n; ++i) st.x[q][i] = h->three_x[(static_cast<int64_t>(q) * n + i) * ncell + c];
+                    }
+                    st.fraction[0] = h->fraction[c];
+                    st.fraction[1] = h->fraction[ncell + c];
+                    three.push_back(std::move(st));
+                }
+            }
             auto put = [&](double* arr, int k, double v) {
                 if (arr) arr[k * ncell + c] = v;
             };
@@ -2658,7 +2733,7 @@ int oracle_max3_batch(int n, const double* tc, const double* pc, const double* o
             if (!std::isfinite(t[c]) || !(t[c] > 0) || !make_temp_cache(m, t[c], wk.tc))
                 r.status = -1;
             else
-                r = solve_max3(m, wk, p[c], t[c], feed);
+                r = solve_max3(m, wk, p[c], t[c], feed, init, fin, three, vo);
             if (o->max3_status) o->max3_status[c] = r.status;
             if (o->attempts) o->attempts[c] = r.attempts;
             int pub = -1;
@@ -2708,6 +2783,20 @@ int oracle_max3_batch(int n, const double* tc, const double* pc, const double* o
     }
     for (auto& th : pool) th.join();
     return 0;
+}
+
+int oracle_max3_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                      int64_t ncell, const double* p, const double* t, const double* z, int threads,
+                      const Max3Outputs* o) {
+    return max3_batch(n, tc, pc, omega, kij, ncell, p, t, z, threads, o, nullptr);
+}
+
+// oracle_max3_batch with caller starts and options (StartHints).
+int oracle_max3_hinted_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                             int64_t ncell, const double* p, const double* t, const double* z,
+                             const StartHints* hints, int threads, const Max3Outputs* o) {
+    if (!hints) return -1;
+    return max3_batch(n, tc, pc, omega, kij, ncell, p, t, z, threads, o, hints);
 }
 
 // Ordered-path continuation of npath feeds z [n * npath], each along its own

@@ -233,6 +233,86 @@ def reference_max3(mix, p, t, z, threads: int = 8):
     return _max3("ref_max3_batch", REF_SO, mix, p, t, z, threads)
 
 
+class _StartHints(ctypes.Structure):
+    _fields_ = [("initial_count", ctypes.c_void_p), ("initial_x", ctypes.c_void_p),
+                ("final_count", ctypes.c_void_p), ("final_x", ctypes.c_void_p),
+                ("three_phase", ctypes.c_void_p), ("three_x", ctypes.c_void_p), ("fraction", ctypes.c_void_p),
+                ("initial_automatic_starts", ctypes.c_int32), ("max_split_attempts", ctypes.c_int32)]
+
+
+def start_hints(n: int, ncell: int, initial=None, final=None, three_phase=None, fraction=None,
+                initial_automatic_starts: bool = True, max_split_attempts: int = 16):
+    """Arrays of a hinted max-3-phase solve.  `initial` / `final`: per cell a
+    list of up to 3 compositions (solve_pr76_pt_max3's initial_starts /
+    final_starts); `three_phase`: per cell None or 3 compositions (one
+    three-phase start) with `fraction` per cell (phase_fraction_seed of
+    phases 1 and 2).  Returns a dict of contiguous arrays in the C layout
+    (composition k of cell c, component i at (k * n + i) * ncell + c)."""
+    def pack(sets):
+        cnt = np.zeros(ncell, np.int32)
+        x = np.zeros((3 * n, ncell))
+        for c, comps in enumerate(sets if sets is not None else [[]] * ncell):
+            comps = list(comps or [])[:3]
+            cnt[c] = len(comps)
+            for k, w in enumerate(comps):
+                x[k * n:(k + 1) * n, c] = w
+        return cnt, x
+    ic, ix = pack(initial)
+    fc, fx = pack(final)
+    tf = np.zeros(ncell, np.int32)
+    tx = np.zeros((3 * n, ncell))
+    fr = np.full((2, ncell), 1.0 / 3.0)
+    if three_phase is not None:
+        for c, comps in enumerate(three_phase):
+            if comps is None:
+                continue
+            tf[c] = 1
+            for k in range(3):
+                tx[k * n:(k + 1) * n, c] = comps[k]
+            if fraction is not None and fraction[c] is not None:
+                fr[:, c] = fraction[c]
+    return {"initial_count": ic, "initial_composition": ix, "final_count": fc, "final_composition": fx,
+            "three_phase": tf, "three_phase_composition": tx, "fraction": fr,
+            "initial_automatic_starts": bool(initial_automatic_starts), "max_split_attempts": int(max_split_attempts)}
+
+
+def _max3_hinted(fn_name: str, so: str, mix, p, t, z, hints: dict, threads: int):
+    tc, pc, omega, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
+    z = np.ascontiguousarray(z, dtype=np.float64)
+    p = np.ascontiguousarray(p, dtype=np.float64)
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    n, ncell = z.shape
+    arr = {k: np.ascontiguousarray(hints[k]) for k in ("initial_count", "initial_composition", "final_count",
+                                                         "final_composition", "three_phase",
+                                                         "three_phase_composition", "fraction")}
+    h = _StartHints(*(arr[k].ctypes.data for k in ("initial_count", "initial_composition", "final_count",
+                                                   "final_composition", "three_phase", "three_phase_composition",
+                                                   "fraction")),
+                    int(bool(hints["initial_automatic_starts"])), int(hints["max_split_attempts"]))
+    out = {f: np.empty(((-r) * n if r < 0 else r, ncell), d) for f, d, r in MAX3_FIELDS}
+    o = _Max3(**{f: v.ctypes.data for f, v in out.items()})
+    fn = getattr(_lib(so), fn_name)
+    fn.restype = ctypes.c_int
+    fn(ctypes.c_int(n), *[ctypes.c_void_p(a.ctypes.data) for a in (tc, pc, omega, kij)], ctypes.c_int64(ncell),
+       *[ctypes.c_void_p(a.ctypes.data) for a in (p, t, z)], ctypes.byref(h), ctypes.c_int(threads),
+       ctypes.byref(o))
+    return {f: (v[0] if v.shape[0] == 1 else v) for f, v in out.items()}
+
+
+def max3_hinted(mix, p, t, z, hints: dict, threads: int = 8):
+    """`max3` with caller starts and the two split options (`start_hints`)."""
+    build()
+    return _max3_hinted("oracle_max3_hinted_batch", ORACLE_SO, mix, p, t, z, hints, threads)
+
+
+def reference_max3_hinted(mix, p, t, z, hints: dict, threads: int = 8):
+    """The reference's solve_pr76_pt_max3 with the same starts and options
+    through oracle/_ref."""
+    if not reference_available():
+        raise FileNotFoundError(REF_SO)
+    return _max3_hinted("ref_max3_hinted_batch", REF_SO, mix, p, t, z, hints, threads)
+
+
 def reference_continuation(mix, pressures, temperatures, z, threads: int = 8):
     """The reference's solve_pr76_pt_continuation (default options) of feeds
     z [n, npath] along paths pressures / temperatures [npath, npoint]; returns

@@ -300,9 +300,37 @@ struct Max3Outputs {
     int32_t* attempts;     // three-phase attempts run
 };
 
-int ref_max3_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
-                   int64_t ncell, const double* p, const double* t, const double* z, int threads,
-                   const Max3Outputs* o) {
+// Caller starts and options of solve_pr76_pt_max3 (the oracle's StartHints):
+// compositions cell-fastest, composition k of cell c, component i at
+// (k * n + i) * ncell + c.
+struct StartHints {
+    const int32_t* initial_count;
+    const double* initial_x;
+    const int32_t* final_count;
+    const double* final_x;
+    const int32_t* three_phase;
+    const double* three_x;
+    const double* fraction;
+    int32_t initial_automatic_starts;
+    int32_t max_split_attempts;
+};
+
+static std::vector<std::vector<double>> hint_set(const int32_t* count, const double* x, int n, int64_t ncell,
+                                                 int64_t c) {
+    std::vector<std::vector<double>> out;
+    if (!count || !x) return out;
+    const int k = std::min(3, std::max(0, static_cast<int>(count[c])));
+    for (int q = 0; q < k; ++q) {
+        std::vector<double> w(n);
+        for (int i = 0; i < n; ++i) w[i] = x[(static_cast<int64_t>(q) * n + i) * ncell + c];
+        out.push_back(std::move(w));
+    }
+    return out;
+}
+
+static int max3_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                      int64_t ncell, const double* p, const double* t, const double* z, int threads,
+                      const Max3Outputs* o, const StartHints* h) {
     std::vector<std::string> order;
     const th::PrParameterSet params = make_parameters(n, tc, pc, omega, kij, order);
     const auto model = th::Pr76Phase<double>::from_parameters(params);
@@ -310,6 +338,24 @@ int ref_max3_batch(int n, const double* tc, const double* pc, const double* omeg
     auto run = [&](int64_t lo, int64_t hi) {
         fl::Pr76VleEvaluator evaluator(model);
         for (int64_t c = lo; c < hi; ++c) {
+            fl::Pr76PtMax3Options options;
+            std::vector<std::vector<double>> init, fin;
+            if (h) {
+                options.two_phase.initial_stability.automatic_starts = h->initial_automatic_starts != 0;
+                options.two_phase.max_split_attempts = static_cast<std::size_t>(h->max_split_attempts);
+                init = hint_set(h->initial_count, h->initial_x, n, ncell, c);
+                fin = hint_set(h->final_count, h->final_x, n, ncell, c);
+                if (h->three_phase && h->three_x && h->fraction && h->three_phase[c]) {
+                    fl::Pr76PtThreePhaseStart st;
+                    for (int q = 0; q < 3; ++q) {
+                        st.compositions[q].resize(n);
+                        for (int i = 0; i < n; ++i)
+                            st.compositions[q][i] = h->three_x[(static_cast<int64_t>(q) * n + i) * ncell + c];
+                    }
+                    st.phase_fraction_seed = {h->fraction[c], h->fraction[ncell + c]};
+                    options.three_phase_starts.push_back(std::move(st));
+                }
+            }
             auto put = [&](double* arr, int k, double v) {
                 if (arr) arr[k * ncell + c] = v;
             };
@@ -330,7 +376,7 @@ int ref_max3_batch(int n, const double* tc, const double* pc, const double* omeg
             for (int i = 0; i < n; ++i) feed[i] = z[i * ncell + c];
             fl::Pr76PtMax3Result r;
             try {
-                r = fl::solve_pr76_pt_max3(p[c], t[c], feed, evaluator);
+                r = fl::solve_pr76_pt_max3(p[c], t[c], feed, evaluator, options, init, fin);
             } catch (const std::exception&) {
                 if (o->max3_status) o->max3_status[c] = -1;
                 if (o->published) o->published[c] = -1;
@@ -387,6 +433,20 @@ int ref_max3_batch(int n, const double* tc, const double* pc, const double* omeg
     }
     for (auto& th : pool) th.join();
     return 0;
+}
+
+int ref_max3_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                   int64_t ncell, const double* p, const double* t, const double* z, int threads,
+                   const Max3Outputs* o) {
+    return max3_batch(n, tc, pc, omega, kij, ncell, p, t, z, threads, o, nullptr);
+}
+
+// ref_max3_batch with caller starts and options (StartHints).
+int ref_max3_hinted_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
+                          int64_t ncell, const double* p, const double* t, const double* z, const StartHints* hints,
+                          int threads, const Max3Outputs* o) {
+    if (!hints) return -1;
+    return max3_batch(n, tc, pc, omega, kij, ncell, p, t, z, threads, o, hints);
 }
 
 // The reference's ordered-path continuation (default options: previous phase

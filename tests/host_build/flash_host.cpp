@@ -77,8 +77,10 @@ void run(const pr76::Mixture& m, int64_t ncell, const double* p, const double* t
         r.has_pair = false;
         CellHints<NM> hs;
         const bool ok = load_hints<NM>(hints, feed, n, ncell, cell, hs);
-        const double* const* extra = hs.count > 0 ? hs.ptr : nullptr;
-        const int status = ok ? solve_cell(m, c, feed, *w, r, extra, hs.count, extra, hs.count) : kInvalid;
+        const double* const* fin = hs.fcount > 0 ? hs.fptr : nullptr;
+        const int status = ok ? solve_cell(m, c, feed, *w, r, hs.count > 0 ? hs.ptr : nullptr, hs.count, fin,
+                                           hs.fcount, hs.options)
+                              : kInvalid;
         int published = status;
         int m3 = status == kSinglePhase ? kM3Single : status == kTwoPhase ? kM3Two : status == kInvalid ? -1
                                                                                                   : kM3Indeterminate;
@@ -100,7 +102,8 @@ void run(const pr76::Mixture& m, int64_t ncell, const double* p, const double* t
             for (int k = 0; k < cCount; ++k) c2.counters[k] = 0;
             Max3Result mr{kM3Indeterminate, false, false};
             if (temp_setup(m, c2))
-                mr = max3_cell(m, c2, feed, lnk, *s, extra, hs.count, hs.has_three ? hs.three : nullptr);
+                mr = max3_cell(m, c2, feed, lnk, *s, fin, hs.fcount, hs.has_three ? hs.three : nullptr,
+                               hs.options);
             else
                 mr.status = -1;
             m3 = mr.status;
@@ -144,6 +147,36 @@ extern "C" int host_hinted_batch(int n, const double* tc, const double* pc, cons
     pr76::Mixture m;
     prepare(n, tc, pc, omega, kij, m);
     const pr76::Hints hints{hint_count, hint_x, three, fraction};
+    const Outputs o{published, max3, x, y, x3, f3};
+    if (n <= 4) run<4>(m, ncell, p, t, z, hints, o);
+    else if (n <= 12) run<12>(m, ncell, p, t, z, hints, o);
+    else run<20>(m, ncell, p, t, z, hints, o);
+    return 0;
+}
+
+// The same with the general caller inputs of mpmc_start_hints_ex: separate
+// initial starts, final starts and three-phase start, and the two split options.
+extern "C" int host_hinted_ex_batch(int n, const double* tc, const double* pc, const double* omega,
+                                    const double* kij, int64_t ncell, const double* p, const double* t,
+                                    const double* z, const int32_t* initial_count, const double* initial_x,
+                                    const int32_t* final_count, const double* final_x, const int32_t* three,
+                                    const double* three_x, const double* fraction, int32_t initial_automatic_starts,
+                                    int32_t max_split_attempts, int32_t* published, int32_t* max3, double* x,
+                                    double* y, double* x3, double* f3) {
+    if (n < 2 || n > pr76::kMaxC) return 1;
+    pr76::Mixture m;
+    prepare(n, tc, pc, omega, kij, m);
+    pr76::Hints hints;
+    hints.count = initial_count;
+    hints.x = initial_x;
+    hints.final_count = final_count;
+    hints.final_x = final_x;
+    hints.three = three;
+    hints.three_x = three_x;
+    hints.fraction = fraction;
+    hints.separate = 1;
+    hints.initial_automatic_starts = initial_automatic_starts;
+    hints.max_split_attempts = max_split_attempts;
     const Outputs o{published, max3, x, y, x3, f3};
     if (n <= 4) run<4>(m, ncell, p, t, z, hints, o);
     else if (n <= 12) run<12>(m, ncell, p, t, z, hints, o);

@@ -6,18 +6,23 @@ Parity bar, per cell:
    indeterminate / invalid).
 2. Two-phase cells converge to the SAME equilibrium: the GPU's and the
    oracle's ln K, each Newton-polished by the oracle to |F| ~ 1e-15, agree
-   within POLISHED_TOL relative (ln K floor LNK_FLOOR, beta floor
-   BETA_FLOOR) -- typically ~1e-12.
+   within POLISHED_TOL relative (ln K floor LNK_FLOOR) -- typically ~1e-12.
+   The polished beta, x and y agree within POLISHED_TOL relative (beta floor
+   BETA_FLOOR) plus that ln K tolerance carried through the Rachford-Rice
+   solution (`rr_band`): near a critical point d beta / d ln K grows large,
+   and two ln K that agree to 2e-11 give betas 1.5e-10 apart.
 3. The raw (unpolished) ln K agree within
        FLASH_TOL * max(|ln K|, LNK_FLOOR) + 4 * 1e-11 * ||(dF/dlnK)^-1||_inf,
    i.e. 1e-10 relative plus the band that the reference's own stopping rule
    |F|_inf <= 1e-11 (pt_split.hpp:31, :351) leaves around the exact root for
    two independent runs.  The reference compiled with and without FMA
    contraction differs from itself by the same amount.
-4. Raw beta, x, y, ln phi and Z: max <= RAW_MAX (ln phi relative to
-   max(|ln phi|, 1)); the p99 is reported.  Both
-   stopping points lie in the same band, so raw p99 differences of ~5e-10
-   appear between two builds of the reference itself.
+4. Raw beta, x and y within the same band carried through the
+   Rachford-Rice solution: |x_gpu - x_ref|_i <= sum_j |dx_i / d ln K_j| b_j
+   + FLASH_TOL |x_i| with b_j the ln K band of 3. (likewise y and beta), the
+   derivatives taken by differences of the Rachford-Rice solution at the
+   oracle's ln K (`rr_band`).  Raw ln phi and Z: max <= RAW_MAX (ln phi
+   relative to max(|ln phi|, 1)); the p99 is reported.
 
 Sensitivities are compared at the same accepted state (the oracle
 differentiates the GPU's state): see `sensitivity_report`.
@@ -67,6 +72,50 @@ def _rows(a):
     return a[None] if a.ndim == 1 else a
 
 
+def rr_solution(z, lnk):
+    """Rachford-Rice solution (beta, x, y) of each cell (columns) at ln K, by
+    bisection on the feasible interval of beta (test arithmetic, FP64)."""
+    k = np.exp(lnk)
+    lo = np.full(z.shape[1], -1e300)
+    hi = np.full(z.shape[1], 1e300)
+    km = k - 1.0
+    with np.errstate(divide="ignore"):
+        # 1 + beta (K - 1) > 0 for every component present
+        lo = np.max(np.where((km > 0) & (z > 0), -1.0 / np.where(km > 0, km, 1.0), -np.inf), axis=0)
+        hi = np.min(np.where((km < 0) & (z > 0), -1.0 / np.where(km < 0, km, -1.0), np.inf), axis=0)
+    a, b = lo + 1e-15 * np.maximum(1, np.abs(lo)), hi - 1e-15 * np.maximum(1, np.abs(hi))
+    for _ in range(200):
+        m = 0.5 * (a + b)
+        f = np.sum(z * km / (1.0 + m * km), axis=0)
+        a = np.where(f > 0, m, a)
+        b = np.where(f > 0, b, m)
+    beta = 0.5 * (a + b)
+    x = z / (1.0 + beta * km)
+    y = k * x
+    return beta, x / x.sum(axis=0), y / y.sum(axis=0)
+
+
+def rr_band(z, lnk, band):
+    """First-order bounds on beta, x and y from ln K errors up to `band`
+    (per component and cell): sum_j |d(.)/d ln K_j| band_j, by central
+    differences of the Rachford-Rice solution."""
+    n = lnk.shape[0]
+    bb = np.zeros(lnk.shape[1])
+    bx = np.zeros_like(lnk)
+    by = np.zeros_like(lnk)
+    for j in range(n):
+        h = 1e-6 * np.maximum(1.0, np.abs(lnk[j]))
+        up, dn = lnk.copy(), lnk.copy()
+        up[j] += h
+        dn[j] -= h
+        b1, x1, y1 = rr_solution(z, up)
+        b0, x0, y0 = rr_solution(z, dn)
+        bb += np.abs((b1 - b0) / (2 * h)) * band[j]
+        bx += np.abs((x1 - x0) / (2 * h)) * band[j]
+        by += np.abs((y1 - y0) / (2 * h)) * band[j]
+    return bb, bx, by
+
+
 def flash_report(gpu: dict, ref: dict, mix=None, p=None, t=None, z=None):
     """Status agreement and per-field errors; with (mix, p, t, z) also the
     polished comparison and the conditioning-aware ln K bound."""
@@ -103,22 +152,46 @@ def flash_report(gpu: dict, ref: dict, mix=None, p=None, t=None, z=None):
             "x": float(rel_err(pg["x"][:, ok], pr["x"][:, ok], 1e-300).max()) if ok.any() else 0.0,
             "y": float(rel_err(pg["y"][:, ok], pr["y"][:, ok], 1e-300).max()) if ok.any() else 0.0,
         }
+        if ok.any():
+            zp = np.asarray(z, dtype=np.float64)[:, ok]
+            zp = zp / zp.sum(axis=0)
+            lk = pr["ln_k"][:, ok]
+            pb, px, py = rr_band(zp, lk, POLISHED_TOL * np.maximum(np.abs(lk), LNK_FLOOR))
+            floors = {"beta": BETA_FLOOR, "x": 1e-300, "y": 1e-300}
+            band = {"beta": pb, "x": px, "y": py}
+            out["polished_band_ratio_max"] = {
+                k: float((np.abs(pg[k][..., ok] - pr[k][..., ok]) /
+                          (band[k] + POLISHED_TOL * np.maximum(np.abs(pr[k][..., ok]), floors[k]))).max())
+                for k in ("beta", "x", "y")}
         a, b = _rows(gpu["ln_k"]), _rows(ref["ln_k"])
         bound = FLASH_TOL * np.maximum(np.abs(b), LNK_FLOOR) + 4 * STOP_TOL * np.nan_to_num(pr["ainv"], nan=0.0)
         ratio = np.abs(a - b) / bound
         out["lnk_bound_ratio_max"] = float(ratio[:, ok].max()) if ok.any() else 0.0
+        if ok.any():
+            # beta, x and y: the same band through the Rachford-Rice solution
+            zz = np.asarray(z, dtype=np.float64)[:, ok]
+            zz = zz / zz.sum(axis=0)
+            bb, bx, by = rr_band(zz, b[:, ok], bound[:, ok])
+            ratios = {}
+            for g, r, bd in (("vapor_fraction", "beta", bb), ("liquid", "x", bx), ("vapor", "y", by)):
+                ga, ra = _rows(gpu[g])[:, ok], _rows(ref[r])[:, ok]
+                ratios[r] = float((np.abs(ga - ra) / (bd + FLASH_TOL * np.abs(ra) + 1e-300)).max())
+            out["rr_bound_ratio_max"] = ratios
     return out
 
 
-def assert_flash_parity(rep: dict) -> None:
-    assert rep["n_mismatch"] == 0, rep
-    for g in FLASH_MAP:
+def assert_flash_parity(rep: dict, allowed: int = 0) -> None:
+    assert rep["n_mismatch"] <= allowed, rep
+    for g in ("ln_phi_liquid", "ln_phi_vapor", "z_liquid", "z_vapor"):
         assert rep["max"][g] <= RAW_MAX, (g, rep)
     if "polished_max" in rep:
         assert rep["polish_failed"] == 0, rep
-        for k, v in rep["polished_max"].items():
-            assert v <= POLISHED_TOL, (k, rep)
+        assert rep["polished_max"]["ln_k"] <= POLISHED_TOL, rep
+        for k, v in rep.get("polished_band_ratio_max", {}).items():
+            assert v <= 1.0, (k, rep)
         assert rep["lnk_bound_ratio_max"] <= 1.0, rep
+        for k, v in rep.get("rr_bound_ratio_max", {}).items():
+            assert v <= 1.0, (k, rep)
 
 
 def sensitivity_report(gpu: dict, ref: dict, rcond=None):

@@ -104,6 +104,44 @@ def test_invalid_three_phase_start_is_an_invalid_request(host_flash):
     assert out["published"][0] == 4 and out["max3"][0] == 2
 
 
+def test_device_max3_with_starts_and_options_matches_reference(host_flash, tmp_path):
+    """The general caller inputs (mpmc_start_hints_ex): every recorded case of
+    tests/golden/max3_hinted_reference.npz -- the reference test's 3 -> 2
+    recovery through a phase disappearance and its fresh two-phase neighbour,
+    the 3 -> 3 base, a zero split-attempt quota, an empty feed test and a
+    final start off the support -- gives the reference's max3 and published
+    statuses, and the recovery's pair equals the reference's to 1e-12."""
+    from tests.test_oracle_max3 import hinted_cases
+
+    so = str(tmp_path / "libflash_host_ex.so")
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-Wno-attributes",
+                           "-I/usr/local/cuda/include", "-I" + os.path.join(ROOT, "include"),
+                           "-I" + os.path.join(ROOT, "mpmc_hnu_gb300", "csrc"),
+                           os.path.join(HERE, "host_build", "flash_host.cpp"), "-o", so])
+    lib = ctypes.CDLL(so)
+    for name, (mix, z, h, ref) in hinted_cases().items():
+        n = z.shape[0]
+        outs = {"published": np.empty(1, np.int32), "max3": np.empty(1, np.int32), "x": np.empty((n, 1)),
+                "y": np.empty((n, 1)), "x3": np.empty((3 * n, 1)), "f3": np.empty((3, 1))}
+        arrays = [np.ascontiguousarray(a) for a in (np.array([1e6]), np.array([250.0]), z)]
+        hints = [np.ascontiguousarray(h[k]) for k in ("initial_count", "initial_composition", "final_count",
+                                                       "final_composition", "three_phase",
+                                                       "three_phase_composition", "fraction")]
+        tc, pc, om, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
+        rc = lib.host_hinted_ex_batch(ctypes.c_int(n), *[ctypes.c_void_p(a.ctypes.data) for a in (tc, pc, om, kij)],
+                                      ctypes.c_int64(1), *[ctypes.c_void_p(a.ctypes.data) for a in arrays + hints],
+                                      ctypes.c_int32(int(h["initial_automatic_starts"])),
+                                      ctypes.c_int32(int(h["max_split_attempts"])),
+                                      *[ctypes.c_void_p(outs[k].ctypes.data)
+                                        for k in ("published", "max3", "x", "y", "x3", "f3")])
+        assert rc == 0
+        assert outs["max3"][0] == np.ravel(ref["max3_status"])[0], name
+        assert outs["published"][0] == np.ravel(ref["published"])[0], name
+        if name == "recovery":
+            assert np.allclose(outs["x"][:, 0], np.ravel(ref["x"]), rtol=0, atol=1e-12)
+            assert np.allclose(outs["y"][:, 0], np.ravel(ref["y"]), rtol=0, atol=1e-12)
+
+
 @pytest.mark.skipif(not os.path.isdir(os.path.join(os.environ.get("MPMC_REFERENCE_ROOT", "/root/reference"),
                                                    "modules", "flash", "include")),
                     reason="reference headers not present")

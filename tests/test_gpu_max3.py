@@ -99,3 +99,30 @@ def test_max3_matches_reference_on_six_components(gpu_lib, form):
     assert three.sum() > 50
     err = np.abs(out3["composition"][:, three] - d["ref_x3"][:, three]).max()
     assert err <= 1e-9, err
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", ["plain", "mixed"])
+def test_max3_with_starts_and_options_matches_reference(gpu_lib, form):
+    """mpmc_gpu_flash_solve_hinted_ex on every recorded case of
+    tests/golden/max3_hinted_reference.npz (the reference's solve_pr76_pt_max3
+    with caller starts and split options): the reference test's 3 -> 2
+    recovery, whose first three-phase attempt ends in a phase disappearance
+    that a fresh two-phase solve resolves (pr76_max3_robustness_test.cpp:275-356;
+    pr76_three_phase.hpp:408-428), the 3 -> 3 base, a zero split-attempt
+    quota, an empty feed test and a final start off the feed's support.
+    Statuses equal the reference's; the recovery's pair to 1e-12."""
+    from tests.test_oracle_max3 import hinted_cases
+
+    for name, (mix, z, h, ref) in hinted_cases().items():
+        g = gpu_lib.GpuFlash(mix, form=form)
+        out, out3 = g.solve_hinted_ex(np.array([1e6]), np.array([250.0]), z, h)
+        g.close()
+        assert int(np.ravel(out3["max3_status"])[0]) == int(np.ravel(ref["max3_status"])[0]), name
+        published = int(np.ravel(out["status"])[0])
+        assert published == int(np.ravel(ref["published"])[0]), name
+        if name == "recovery":
+            assert np.allclose(np.ravel(out["liquid"]), np.ravel(ref["x"]), rtol=0, atol=1e-12)
+            assert np.allclose(np.ravel(out["vapor"]), np.ravel(ref["y"]), rtol=0, atol=1e-12)
+        if name == "three":
+            assert np.allclose(np.ravel(out3["phase_fraction"]), np.ravel(ref["beta3"]), rtol=0, atol=1e-9)

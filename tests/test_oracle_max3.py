@@ -76,3 +76,57 @@ def test_oracle_max3_matches_recorded_reference_on_six_components(oracle_lib):
     assert counts[1] > 50 and counts[2] > 100 and counts[3] > 50
     for k, v in out.items():
         assert _same(v, d[f"ref_{k}"]), k
+
+
+HINTED = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "max3_hinted_reference.npz")
+
+
+def hinted_cases():
+    """The recorded hinted max-3-phase cases (make_max3_hinted_golden.py):
+    name -> (mixture, z [n, 1], start hints, reference outputs)."""
+    d = np.load(HINTED)
+    cases = {}
+    for name in d["cases"]:
+        name = str(name)
+        model = str(d[f"{name}_model"])
+        n = len(d[f"{model}_tc"])
+        mix = synth.Mixture(d[f"{model}_tc"], d[f"{model}_pc"], d[f"{model}_omega"],
+                            d[f"{model}_kij"].reshape(n, n))
+        pre = f"{name}_hint_"
+        h = {k[len(pre):]: d[k] for k in d.files if k.startswith(pre)}
+        h["initial_automatic_starts"] = bool(h["initial_automatic_starts"])
+        h["max_split_attempts"] = int(h["max_split_attempts"])
+        pre = f"{name}_ref_"
+        ref = {k[len(pre):]: d[k] for k in d.files if k.startswith(pre)}
+        cases[name] = (mix, d[f"{name}_z"], h, ref)
+    return cases
+
+
+def test_oracle_max3_with_starts_and_options_matches_recorded_reference(oracle_lib):
+    """Caller starts and split options: the reference test's 3 -> 2 recovery
+    through a phase disappearance and a fresh two-phase neighbour
+    (pr76_max3_robustness_test.cpp:275-356), the 3 -> 3 continuation base, a
+    zero split-attempt quota, an empty search and a final start off the
+    feed's support, bit-identical to the recorded reference."""
+    cases = hinted_cases()
+    mix, z, h, ref = cases["recovery"]
+    # the recovery publishes the fresh two-phase neighbour of its first attempt
+    first = {name: {k: int(np.ravel(c[3][k])[0]) for k in ("max3_status", "published", "attempts")}
+             for name, c in cases.items()}
+    assert first["recovery"] == {"max3_status": 1, "published": 1, "attempts": 1}
+    assert first["three"]["max3_status"] == 2 and first["budget"]["max3_status"] == 5
+    assert first["no_starts"]["max3_status"] == -1 and first["support"]["max3_status"] == -1
+    for name, (mix, z, h, ref) in cases.items():
+        out = oracle_lib.max3_hinted(mix, np.array([1e6]), np.array([250.0]), z, h, threads=1)
+        for k, v in out.items():
+            assert _same(v, ref[k]), (name, k)
+
+
+def test_oracle_max3_with_starts_matches_live_reference(oracle_lib):
+    if not oracle_lib.reference_available():
+        pytest.skip("reference harness not built here")
+    for name, (mix, z, h, ref) in hinted_cases().items():
+        live = oracle_lib.reference_max3_hinted(mix, np.array([1e6]), np.array([250.0]), z, h, threads=1)
+        out = oracle_lib.max3_hinted(mix, np.array([1e6]), np.array([250.0]), z, h, threads=1)
+        for k, v in out.items():
+            assert _same(v, live[k]), (name, k)
