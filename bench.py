@@ -417,12 +417,14 @@ def wilson_ln_k(mix, p, t):
 
 
 def kernels_per_solve(form: str, sens: bool) -> int:
-    """Kernels one device-resident solve launches (flash_batched.cu's pass:
-    setup, feed trials32 / classify / trials64, decide, split32, polish,
-    open32, compete, split64, select64, relist, review trials32 / classify /
-    trials64, finish, fallback; the plain form one kernel), plus the
-    sensitivity kernel."""
-    return (1 if form == "plain" else 17) + (1 if sens else 0)
+    """Kernels one cold device-resident solve launches: 17 per pass of
+    flash_batched.cu (setup, feed trials / classify / trials64, decide,
+    split32, polish, open32, compete, split64, select64, relist, review
+    trials / classify / trials64, finish, fallback); the mixed form runs the
+    main pass and the exact pass, the FP64 work-queue form one pass, the plain
+    form one kernel; plus the sensitivity kernel."""
+    per = {"plain": 1, "batched": 17, "mixed": 34}[form]
+    return per + (1 if sens else 0)
 
 
 def _timed(fn, stream, torch):
@@ -695,15 +697,17 @@ SERVING_MIXTURES = [(3, 501), (3, 502), (6, 503), (6, 504), (10, 505), (10, 506)
 
 def serving_pool(synth, count: int, seed: int = 77):
     """Seeded requests: mixture among 8 (N in {3, 6, 10, 20}), cells per request
-    floor(exp(U ln 65536)), cells from the base distributions; half re-query
-    the previous request's mixture with p * exp(N(0, 0.02)), T + N(0, 1 K)."""
+    floor(exp(U ln 65536)), cells from the base distributions.  Half re-query
+    an earlier fresh request (drawn uniformly): its mixture and cells (drawn
+    with replacement) at p * exp(N(0, 0.02)), T + N(0, 1 K).  A re-query
+    perturbs a fresh request's states, never another re-query's, so repeated
+    re-queries do not random-walk the states into one small (p, T) region."""
     rng = np.random.default_rng(seed)
-    pool = []
+    pool, fresh = [], []
     for k in range(count):
         ncell = max(1, int(np.exp(rng.uniform(0.0, np.log(65536.0)))))
-        if pool and rng.uniform() < 0.5:
-            j, p0, t0, z0 = pool[-1]
-            n = SERVING_MIXTURES[j][0]
+        if fresh and rng.uniform() < 0.5:
+            j, p0, t0, z0 = pool[fresh[int(rng.integers(0, len(fresh)))]]
             src = rng.integers(0, p0.shape[0], ncell)
             p = p0[src] * np.exp(rng.normal(0.0, 0.02, ncell))
             t = t0[src] + rng.normal(0.0, 1.0, ncell)
@@ -712,6 +716,7 @@ def serving_pool(synth, count: int, seed: int = 77):
             j = int(rng.integers(0, len(SERVING_MIXTURES)))
             n = SERVING_MIXTURES[j][0]
             p, t, z = synth.make_cells(n, ncell, 9000 + k)
+            fresh.append(k)
         pool.append((j, np.ascontiguousarray(p), np.ascontiguousarray(t), z))
     return pool
 

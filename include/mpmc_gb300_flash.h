@@ -422,7 +422,10 @@ int mpmc_gpu_flash_property_chart_device(mpmc_gpu_flash* handle, int64_t n_cells
  * MPMC_NOALLOC_SCRATCH_BYTES array of device memory per device; a batch whose
  * buffers do not fit (about 2,700 cells at 20 components, 7,300 at 10, more
  * with fewer components) returns MPMC_ERR_INVALID_ARGUMENT with the size in
- * the message.  The first call on a device looks the array's address up
+ * the message.  The queue of FP64 attempt continuations takes the rest of the
+ * array, up to one entry per attempt (16 per cell): in a batch of hard cells
+ * whose queue still overflows, the cells that do not fit run the plain FP64
+ * fallback -- the same answers, slower.  The first call on a device looks the array's address up
  * (cudaGetSymbolAddress, with that device current), and the first launch of
  * each of its kernels in the process lets the CUDA driver size the context's
  * local-memory (stack) reservation for that kernel -- the implicit-sensitivity
@@ -451,13 +454,23 @@ int mpmc_gpu_flash_solve_device_noalloc(mpmc_gpu_flash* handle, int64_t n_cells,
  *   [4] per-cell kernel blocks per SM   [5] item form: bit 0 feed trials, bit 1
  *       review trials, bit 2 attempts run one item per thread instead of one
  *       per lane group; the polish runs one cell per thread with bit 3, one per
- *       lane group with bit 4 (default: per thread up to 12 components)
+ *       lane group with bit 4 (default: per thread up to 12 components);
+ *       FP64 trial items run 32 / S to a warp (S = the component capacity
+ *       rounded to a power of two), or one per warp with bit 5; FP64
+ *       attempt items one per warp with bit 6, 32 / S to a warp with bit 7
+ *       (default: packed up to 8 components)
  *   [6] successive-substitution -> Newton switch: the FP32 |r| (in units of
  *       1e-6) at which the FP32 ln K iteration hands over to the FP64 polish
  *   [7] cell ranges (1-8) a solve is split into, each a solve of its own on
  *       its own stream, so that the long last items of one range overlap the
  *       bulk stages of the others (default 1; every range keeps at least
  *       65,536 cells; the outputs do not depend on it)
+ *   [8] FP32 trial screen: a stability trial whose FP32 descent projects
+ *       more FP64 iterations than this (1-512) is re-run exactly in FP64
+ *       instead of being decided from its FP32 end point
+ *   [9] an undecided trial or unsettled split attempt whose FP32 run took at
+ *       least this many iterations (1-512) runs from its start in FP64
+ *       instead of continuing from its FP32 end point
  * 0 selects the default (occupancy-derived residency, lane-group items,
  * switch at 2e-5).  Results do not depend on the shape beyond the rounding of
  * where each iteration stops.  Drops the handle's captured graphs.  No
@@ -500,8 +513,13 @@ int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* handle, float* ms, int capacity
  * of the feed phase (setup), the FP64 feed-test trial items, the FP64 review
  * trial items, the Newton polish and the FP64 attempt continuations; [28]
  * closed-form Jacobians the polish factorised and [29] its chord-step solves
- * (the algorithmic work of each FP64 stage).  After a warm-start solve,
- * [0]-[15] count the cold pass and [20]-[29] both passes.
+ * (the algorithmic work of each FP64 stage); [30] cells the plain FP64
+ * fallback solved (a nonsmooth feed phase, unusable constants, or FP64
+ * attempt items beyond the queue's capacity); [31] cells the exact pass
+ * solved again with every trial and attempt in FP64 (no FP32 attempt
+ * converged, or the replay put the polished attempt at risk).  After a
+ * warm-start solve, [0]-[15] and [30] count the last pass and [20]-[29] and
+ * [31] every pass.
  * Writes up to `capacity` values; returns the number available (0 for the
  * plain form).  Diagnostic entry point with no counterpart in the reference. */
 int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* handle, int64_t* out, int capacity);

@@ -82,8 +82,10 @@ struct mpmc_gpu_flash {
     bool stage_timing = false;
     cudaEvent_t events[24] = {};
     cudaEvent_t redo_events[24] = {};  // the cold pass after a warm pass
+    cudaEvent_t exact_events[24] = {};  // the exact pass of the mixed form
     int n_events = 0;   // events recorded by the last solve (stages + 1)
     bool timed_warm = false;  // the last timed solve ran a warm and a cold pass
+    bool timed_exact = false; // the last timed solve ran the exact pass
     DevBuf in_warm;     // host entry: staged ln K warm starts
     DevBuf outs3[5];    // host entry: staged three-phase outputs
     DevBuf in_hints[7];   // host hinted entry: staged counts, compositions, three-phase flags, fractions
@@ -99,7 +101,7 @@ struct mpmc_gpu_flash {
     cudaStream_t copy_stream = nullptr;  // host entry: copy-out overlapped with the sensitivity stage
     cudaEvent_t flash_done = nullptr;
     cudaEvent_t chunk_done[8] = {};
-    int32_t shape[8] = {};  // explicit launch shape (mpmc_gpu_flash_set_launch_shape), 0 = default
+    int32_t shape[10] = {};  // explicit launch shape (mpmc_gpu_flash_set_launch_shape), 0 = default
     bool use_graphs = false;
     std::vector<GraphEntry> graphs;
     uint64_t graph_clock = 0;
@@ -232,6 +234,8 @@ pr76::BatchedShape batched_shape(const mpmc_gpu_flash* h, cudaEvent_t* events) {
     for (int k = 0; k < 6; ++k)
         if (h->shape[k] > 0) *fields[k] = h->shape[k];
     if (h->shape[6] > 0) shape.ss_switch = 1e-6f * static_cast<float>(h->shape[6]);
+    if (h->shape[8] > 0) shape.slow_projection = static_cast<float>(h->shape[8]);
+    if (h->shape[9] > 0) shape.continue_limit = h->shape[9];
     return shape;
 }
 
@@ -324,6 +328,7 @@ cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, co
         shape.fp64_items = h->form == MPMC_FORM_BATCHED;
         shape.warm_lnk = warm;
         shape.redo_events = timing ? h->redo_events : nullptr;
+        shape.exact_events = timing ? h->exact_events : nullptr;
         const bool fp64_items = h->form == MPMC_FORM_BATCHED;
         const int k = timing ? 1 : solve_ranges(h, ncell);
         h->last_ranges = k;
@@ -371,7 +376,8 @@ cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, co
     record();  // end of the sensitivity stage (zero length without sensitivities)
     if (timing) {
         h->n_events = next_event;
-        h->timed_warm = warm != nullptr;
+        h->timed_warm = warm != nullptr && (h->form == MPMC_FORM_MIXED || h->form == MPMC_FORM_BATCHED);
+        h->timed_exact = h->form == MPMC_FORM_MIXED && !hints;
     }
     return cudaSuccess;
 }
@@ -401,6 +407,8 @@ int run_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
         for (auto& ev : h->events)
             if ((e = cudaEventCreate(&ev)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
         for (auto& ev : h->redo_events)
+            if ((e = cudaEventCreate(&ev)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
+        for (auto& ev : h->exact_events)
             if ((e = cudaEventCreate(&ev)) != cudaSuccess) return cuda_fail(e, "cudaEventCreate");
     }
     if (!h->use_graphs || h->stage_timing || max3) {
@@ -497,13 +505,13 @@ int capacity_for(int n) {
     return 0;
 }
 
-size_t batched_workspace_bytes(int n, int64_t ncell, bool fp64_items) {
+size_t batched_workspace_bytes(int n, int64_t ncell, bool fp64_items, int s64_per_cell) {
     switch (capacity_for(n)) {
-    case 4: return batched_workspace_bytes_nm4(n, ncell, fp64_items);
-    case 8: return batched_workspace_bytes_nm8(n, ncell, fp64_items);
-    case 12: return batched_workspace_bytes_nm12(n, ncell, fp64_items);
-    case 16: return batched_workspace_bytes_nm16(n, ncell, fp64_items);
-    case 20: return batched_workspace_bytes_nm20(n, ncell, fp64_items);
+    case 4: return batched_workspace_bytes_nm4(n, ncell, fp64_items, s64_per_cell);
+    case 8: return batched_workspace_bytes_nm8(n, ncell, fp64_items, s64_per_cell);
+    case 12: return batched_workspace_bytes_nm12(n, ncell, fp64_items, s64_per_cell);
+    case 16: return batched_workspace_bytes_nm16(n, ncell, fp64_items, s64_per_cell);
+    case 20: return batched_workspace_bytes_nm20(n, ncell, fp64_items, s64_per_cell);
     default: return 0;
     }
 }
@@ -663,7 +671,7 @@ int mpmc_gpu_flash_batch_stats(mpmc_gpu_flash* h, int64_t* out, int capacity) {
     // workspace counter slots (pr76_batched.cuh Slot) in the documented order
     // negative entries: a 64-bit total held in slots -s and -s + 1
     constexpr int kSlots[] = {8, 9, 10, 11, 12, 13, 14, 15, 16, 17, 18, 20, 22, 23, 24, 25, 27, 28, 29, 30, 31, 32, 33,
-                              -34, -36, -38, -40, -42, 44, 45};
+                              -34, -36, -38, -40, -42, 44, 45, 4, 46};
     constexpr int kCount = static_cast<int>(sizeof(kSlots) / sizeof(kSlots[0]));
     if (cudaSetDevice(h->device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return 0;
     for (int k = 0; k < kCount && k < capacity; ++k)
@@ -696,13 +704,23 @@ int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* h, float* ms, int capacity) {
         float v = 0.f;
         cudaEventElapsedTime(&v, h->events[k], h->events[k + 1]);
         // after a warm pass, each stage's time is that of both passes
-        if (h->timed_warm && k < pr76::kBatchedStages) {
+        // each stage's time is that of every pass the solve ran (first, then
+        // the cold pass after a warm pass, then the exact pass)
+        if (k < pr76::kBatchedStages) {
             float r = 0.f;
-            cudaEventElapsedTime(&r, h->redo_events[k], h->redo_events[k + 1]);
-            v += r;
-        } else if (h->timed_warm && k == pr76::kBatchedStages) {
-            // the sensitivity stage follows the cold pass
-            cudaEventElapsedTime(&v, h->redo_events[pr76::kBatchedStages], h->events[k + 1]);
+            if (h->timed_warm) {
+                cudaEventElapsedTime(&r, h->redo_events[k], h->redo_events[k + 1]);
+                v += r;
+            }
+            if (h->timed_exact) {
+                cudaEventElapsedTime(&r, h->exact_events[k], h->exact_events[k + 1]);
+                v += r;
+            }
+        } else if (k == pr76::kBatchedStages && (h->timed_warm || h->timed_exact)) {
+            // the sensitivity stage follows the last pass
+            cudaEventElapsedTime(&v, h->timed_exact ? h->exact_events[pr76::kBatchedStages]
+                                                    : h->redo_events[pr76::kBatchedStages],
+                                 h->events[k + 1]);
         }
         if (ms) ms[k] = v;
     }
@@ -765,6 +783,8 @@ int mpmc_gpu_flash_destroy(mpmc_gpu_flash* h) {
         if (ev) cudaEventDestroy(ev);
     for (auto& ev : h->redo_events)
         if (ev) cudaEventDestroy(ev);
+    for (auto& ev : h->exact_events)
+        if (ev) cudaEventDestroy(ev);
     if (h->copy_stream) {
         cudaStreamSynchronize(h->copy_stream);
         cudaStreamDestroy(h->copy_stream);
@@ -822,12 +842,12 @@ int mpmc_gpu_flash_solve_device_warm(mpmc_gpu_flash* h, int64_t ncell, const dou
 
 int mpmc_gpu_flash_set_launch_shape(mpmc_gpu_flash* h, const int32_t* values, int count) {
     if (!h) return fail(MPMC_ERR_INVALID_ARGUMENT, "null handle");
-    if (count < 0 || count > 8 || (count > 0 && !values))
-        return fail(MPMC_ERR_INVALID_ARGUMENT, "launch shape: 0 to 8 values");
+    if (count < 0 || count > 10 || (count > 0 && !values))
+        return fail(MPMC_ERR_INVALID_ARGUMENT, "launch shape: 0 to 10 values");
     for (int k = 0; k < count; ++k)
-        if (values[k] < 0 || values[k] > (k == 6 ? 1000000 : 64))
+        if (values[k] < 0 || values[k] > (k == 6 ? 1000000 : (k == 5 ? 255 : (k >= 8 ? 512 : 64))))
             return fail(MPMC_ERR_INVALID_ARGUMENT, "launch shape value out of range");
-    for (int k = 0; k < 8; ++k) h->shape[k] = k < count ? values[k] : 0;
+    for (int k = 0; k < 10; ++k) h->shape[k] = k < count ? values[k] : 0;
     cudaSetDevice(h->device);
     for (auto& g : h->graphs) cudaGraphExecDestroy(g.exec);  // captured with the old shape
     h->graphs.clear();
@@ -844,7 +864,8 @@ int mpmc_gpu_flash_solve_device_noalloc(mpmc_gpu_flash* h, int64_t ncell, const 
     if (!p || !t || !z) return fail(MPMC_ERR_INVALID_ARGUMENT, "p, t and z must not be null");
     if (ncell >= (int64_t{1} << 24))
         return fail(MPMC_ERR_INVALID_ARGUMENT, "mixed form: at most 16,777,215 cells per call");
-    const size_t need = pr76::batched_workspace_bytes(h->n, ncell);
+    // the least scratch that runs: one FP64 attempt item per cell
+    const size_t need = pr76::batched_workspace_bytes(h->n, ncell, false, 1);
     if (need > MPMC_NOALLOC_SCRATCH_BYTES)
         return fail(MPMC_ERR_INVALID_ARGUMENT,
                     "no-allocation entry point: " + std::to_string(ncell) + " cells of " + std::to_string(h->n) +

@@ -22,7 +22,7 @@ size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
 
 // Carves the workspace arrays out of one scratch allocation; with base ==
 // nullptr only computes the size.
-size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell, bool fp64_items) {
+size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell, bool fp64_items, int s64_per_cell) {
     const size_t nc = static_cast<size_t>(ncell);
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -58,9 +58,12 @@ size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell, bool fp64
     ws.t64_items = reinterpret_cast<int*>(take(sizeof(int) * (NM + 4) * nc));
     ws.t64_status = reinterpret_cast<signed char*>(take((NM + 4) * nc));
     ws.tw64 = reinterpret_cast<double*>(take(sizeof(double) * (NM + 4) * NM * nc));
-    // FP64 attempt items: the unsettled attempts of the mixed form (capacity
-    // ncell, at least 16384); every attempt of every cell in the FP64 form
-    ws.s64_capacity = static_cast<int>(fp64_items ? batched::kMaxAttempts * nc : (nc < 4096 ? 4 * 4096 : nc));
+    // FP64 attempt items: every attempt of every cell in the FP64 form; the
+    // unsettled attempts of the mixed form, s64_per_cell per cell (at least
+    // 16384 items).  A cell whose items do not fit runs the plain fallback.
+    const size_t per = static_cast<size_t>(s64_per_cell < 1 ? 1 : s64_per_cell);
+    ws.s64_capacity = static_cast<int>(fp64_items ? batched::kMaxAttempts * nc
+                                                  : (per * nc < 4 * 4096 ? 4 * 4096 : per * nc));
     const size_t cap = static_cast<size_t>(ws.s64_capacity);
     ws.s64_items = reinterpret_cast<int*>(take(sizeof(int) * cap));
     ws.s64_status = reinterpret_cast<signed char*>(take(cap));
@@ -83,9 +86,9 @@ int resident_blocks(K kernel, int block) {
 }  // namespace batched_host_nm<NM>
 using namespace MPMC_CAT(batched_host_nm, MPMC_NM);
 
-size_t MPMC_CAT(batched_workspace_bytes_nm, MPMC_NM)(int n, int64_t ncell, bool fp64_items) {
+size_t MPMC_CAT(batched_workspace_bytes_nm, MPMC_NM)(int n, int64_t ncell, bool fp64_items, int s64_per_cell) {
     batched::Workspace ws;
-    return carve(ws, nullptr, n, ncell, fp64_items);
+    return carve(ws, nullptr, n, ncell, fp64_items, s64_per_cell);
 }
 
 cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, int64_t ncell, const double* p,
@@ -97,9 +100,15 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     if (ncell >= (int64_t{1} << 24)) return cudaErrorInvalidValue;  // work-item encodings hold 24-bit cells
     Workspace ws;
     const bool fp64_items = shape.fp64_items != 0;
-    if (carve(ws, nullptr, n, ncell, fp64_items) > scratch_bytes || scratch == nullptr) return cudaErrorInvalidValue;
-    carve(ws, static_cast<char*>(scratch), n, ncell, fp64_items);
+    // the largest FP64 attempt-item capacity the scratch holds
+    int per = kS64PerCell;
+    while (per > 1 && carve(ws, nullptr, n, ncell, fp64_items, per) > scratch_bytes) per /= 2;
+    if (carve(ws, nullptr, n, ncell, fp64_items, per) > scratch_bytes || scratch == nullptr)
+        return cudaErrorInvalidValue;
+    carve(ws, static_cast<char*>(scratch), n, ncell, fp64_items, per);
     ws.io_stride = shape.io_stride > 0 ? shape.io_stride : ncell;
+    ws.slow_projection = shape.slow_projection > 0.f ? shape.slow_projection : kSlowProjection;
+    ws.continue_limit = shape.continue_limit > 0 ? shape.continue_limit : kContinueLimit;
     int device = 0, sms = 0;
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -117,11 +126,19 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     const int split_res = shape.split_blocks_per_sm > 0 ? shape.split_blocks_per_sm
                                                         : resident_blocks(split32_kernel<NM>, qblock);
     const int t64_res = shape.t64_blocks_per_sm > 0 ? shape.t64_blocks_per_sm : 2;
+    // FP64 trial and attempt items: 32 / kSeg per warp (kSeg the component
+    // capacity rounded to a power of two), or one per warp.  Measured on a
+    // GB300: packed trial items gain at every size (N = 4: 1.88 s -> 0.85 s of
+    // feed trials on 1M cells; N = 10 bench: 147 -> 138 ms); packed attempt
+    // items gain where many short items share a warp (N = 4: 3.30 -> 2.26 s)
+    // and lose where a few long ones set the stage's tail (N = 10: 176 -> 198 ms).
+    const bool packed_trials = (shape.item_form & 32) == 0;
+    const bool packed_attempts = (shape.item_form & 64) ? false : ((shape.item_form & 128) ? true : NM <= 8);
     const int s64_res = shape.s64_blocks_per_sm > 0 ? shape.s64_blocks_per_sm : 2;
     // one pass of the launch sequence over the cells `ws.pass` selects
-    auto run_pass = [&](cudaEvent_t* events) -> cudaError_t {
+    auto run_pass = [&](cudaEvent_t* events, bool f64) -> cudaError_t {
         // the warm pass's statistics stay for the cold pass after it
-        const int clear = ws.pass == kPassRedo ? qPassSlots : qSlots;
+        const int clear = ws.pass >= kPassRedo ? qPassSlots : qSlots;
         cudaError_t e = cudaMemsetAsync(ws.counters, 0, sizeof(int) * clear, stream);
         if (e != cudaSuccess) return e;
         e = cudaMemsetAsync(ws.s64_items, 0xff, sizeof(int) * static_cast<size_t>(ws.s64_capacity), stream);
@@ -136,14 +153,15 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
         mark();
         // The FP64 form queues every trial and attempt as an exact FP64 item (the
         // FP32 screening stages become empty), on the same stage slots.
-        if (fp64_items) rerun_all_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(ws, 0);
+        if (f64) rerun_all_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(ws, 0);
         else trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 0);
         mark();
         classify_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, 0);
         mark();
         // one warp per trial item: items of slow descents dominate, so latency
         // matters more than packing several items into a warp (measured)
-        if ((shape.item_form & 1) && !fp64_items) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+        if ((shape.item_form & 1) && !f64) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+        else if (packed_trials) w64::trials64w_kernel<NM, w64::kSeg<NM>><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
         else w64::trials64w_kernel<NM, 32><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
         mark();
         decide_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
@@ -151,7 +169,7 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
         // FP32 successive substitution hands over to the FP64 Newton polish at
         // |r| <= ss_switch (default 2e-5, a few times the FP32 rounding floor)
         const float ss_switch = shape.ss_switch > 0.f ? shape.ss_switch : 2e-5f;
-        if (!fp64_items) split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t, ss_switch, 0);
+        if (!f64) split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t, ss_switch, 0);
         mark();
         // polish: one cell per thread up to 12 components (its per-cell arrays
         // still fit the cache), one cell per lane group above
@@ -161,11 +179,12 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
         mark();
         // attempts FP32 left open beside a polished pair: their FP32 prediction,
         // then the pair's review or the FP64 continuation of what stays open
-        if (!fp64_items) split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t, ss_switch, 1);
+        if (!f64) split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t, ss_switch, 1);
         mark();
         compete_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t);
         mark();
-        if ((shape.item_form & 4) && !fp64_items) split64_kernel<NM><<<sms * s64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+        if ((shape.item_form & 4) && !f64) split64_kernel<NM><<<sms * s64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+        else if (packed_attempts) w64::split64w_kernel<NM, w64::kSeg<NM>><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t);
         else w64::split64w_kernel<NM, 32><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t);
         mark();
         select64_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
@@ -173,12 +192,13 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
         relist_kernel<NM><<<1, 1024, 0, stream>>>(ws);
         cudaMemsetAsync(ws.counters + qT64Items, 0, 2 * sizeof(int), stream);
         mark();
-        if (fp64_items) rerun_all_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(ws, 1);
+        if (f64) rerun_all_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(ws, 1);
         else trials32_kernel<NM><<<sms * trial_res, qblock, 0, stream>>>(d_mix, ws, p, t, 1);
         mark();
         classify_kernel<NM><<<cell_grid(ncell), 128, 0, stream>>>(d_mix, ws, 1);
         mark();
-        if ((shape.item_form & 2) && !fp64_items) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+        if ((shape.item_form & 2) && !f64) trials64_kernel<NM><<<sms * t64_res, 64, 0, stream>>>(d_mix, ws, p, t);
+        else if (packed_trials) w64::trials64w_kernel<NM, w64::kSeg<NM>><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
         else w64::trials64w_kernel<NM, 32><<<sms * t64_res, 128, 0, stream>>>(d_mix, ws, p, t);
         mark();
         finish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
@@ -189,13 +209,25 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     };
     ws.warm_lnk = shape.warm_lnk;
     ws.pass = shape.warm_lnk ? kPassWarm : kPassCold;
-    cudaError_t e = run_pass(shape.events);
-    if (e != cudaSuccess || !shape.warm_lnk) return e;
-    // the warm cells whose pair was not accepted: the full cold solve (a
-    // nearly empty pass when the warm starts are good)
-    ws.pass = kPassRedo;
-    e = run_pass(shape.redo_events);
+    cudaError_t e = run_pass(shape.events, fp64_items);
     if (e != cudaSuccess) return e;
+    if (shape.warm_lnk) {
+        // the warm cells whose pair was not accepted: the full cold solve (a
+        // nearly empty pass when the warm starts are good)
+        ws.pass = kPassRedo;
+        e = run_pass(shape.redo_events, fp64_items);
+        if (e != cudaSuccess) return e;
+    }
+    if (!fp64_items) {
+        // the cells FP32 could not screen (mark_exact): the whole solve again
+        // with every trial and attempt an exact FP64 item, as the FP64
+        // work-queue form runs it (a nearly empty pass on most batches)
+        ws.pass = kPassExact;
+        ws.fp64_items = 1;
+        e = run_pass(shape.exact_events, true);
+        ws.fp64_items = 0;
+        if (e != cudaSuccess) return e;
+    }
     return cudaGetLastError();
 }
 

@@ -66,14 +66,26 @@ struct BatchedShape {
     // the cell cold); null = cold solve of every cell
     const double* warm_lnk;
     cudaEvent_t* redo_events;  // optional: the events of the cold pass after a warm pass
+    cudaEvent_t* exact_events; // optional: the events of the exact pass (mixed form)
+    float slow_projection;     // projected FP64 iterations above which an FP32 trial is re-run exactly
+                               // in FP64 (0 = the default)
+    int continue_limit;        // FP32 iterations from which an undecided trial or unsettled attempt
+                               // runs from its start in FP64 (0 = the default)
     int64_t io_stride;         // stride of z, the warm starts and the outputs (0 = ncell): a solve of one
                                // cell range of a larger batch, with every pointer at the range's start
 };
 constexpr int kBatchedStages = 17;
 
+// FP64 attempt-item capacity of the mixed form per cell: every attempt of
+// every cell (kMaxAttempts), so that no cell of a hard batch -- near-critical
+// cells whose 16 attempts all stay unsettled in FP32 -- overflows to the
+// one-thread-per-cell fallback.  A smaller scratch (the no-allocation entry)
+// takes the largest of 16, 8, 4, 2, 1 per cell that fits.
+constexpr int kS64PerCell = 16;
+
 // Batched mixed-precision flash (flash_batched.cu): scratch bytes needed for
 // ncell cells, and the launch sequence using that scratch.
-size_t batched_workspace_bytes(int n, int64_t ncell, bool fp64_items = false);
+size_t batched_workspace_bytes(int n, int64_t ncell, bool fp64_items = false, int s64_per_cell = kS64PerCell);
 cudaError_t launch_batched(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
                            const double* z, const DeviceOutputs& out, void* scratch, size_t scratch_bytes,
                            const BatchedShape& shape, cudaStream_t stream);
@@ -174,7 +186,7 @@ cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const
     cudaError_t launch_chart_nm##NM(const Mixture* d_mix, const ChartParams& params, int64_t ncell,           \
                                     const double* q, const int32_t* dep, const ChartOutputs& out,               \
                                     cudaStream_t stream);                                                        \
-    size_t batched_workspace_bytes_nm##NM(int n, int64_t ncell, bool fp64_items);                             \
+    size_t batched_workspace_bytes_nm##NM(int n, int64_t ncell, bool fp64_items, int s64_per_cell);           \
     cudaError_t launch_batched_nm##NM(const Mixture* d_mix, int n, int64_t ncell, const double* p,            \
                                       const double* t, const double* z, const DeviceOutputs& out, void* scratch, \
                                       size_t scratch_bytes, const BatchedShape& shape, cudaStream_t stream);

@@ -56,6 +56,9 @@ constexpr int kSlowFlag = 8;
 #define MPMC_SLOW_PROJECTION 448.f
 #endif
 constexpr float kSlowProjection = MPMC_SLOW_PROJECTION;
+// FP32 iterations from which an undecided trial or an unsettled attempt is run
+// from its start in FP64 rather than continued from its FP32 end point.
+constexpr int kContinueLimit = 512;
 
 // Queue/counter slots in Workspace::counters.
 enum Slot : int {
@@ -104,6 +107,7 @@ enum Slot : int {
     tE64Split64 = 42,      // ... of the FP64 attempt continuations
     sPolishJacobians = 44, // closed-form Jacobians built and factorised by the polish
     sPolishSolves = 45,    // LU solves of the polish's chord steps
+    sExactCells = 46,      // cells solved again by the exact pass (every trial and attempt in FP64)
     qSlots = 48
 };
 
@@ -123,7 +127,8 @@ enum Phase : int {
     pInvalid = -1, pSingle = 0, pTwo = 1, pUnstable = 2, pIndeterminate = 3,
     pPending = 10, pSplit = 11, pReview = 12, pFallback = 13, pSplit64 = 14,
     pRedo = 15,  // warm pass: the warm pair was not accepted, the cell runs the cold pass
-    pCompete = 16  // a polished pair waits on the open attempts' predicted ends
+    pCompete = 16,  // a polished pair waits on the open attempts' predicted ends
+    pExact = 17     // FP32 could not screen the cell: the exact pass solves it again in FP64
 };
 
 // Passes of the launch sequence: the cold solve of every cell; the warm pass
@@ -131,7 +136,7 @@ enum Phase : int {
 // the common-tangent review, no feed test, while the other cells take the
 // cold path in the same pass); the cold solve of the warm cells whose pair was
 // not accepted.
-enum Pass : int { kPassCold = 0, kPassWarm = 1, kPassRedo = 2 };
+enum Pass : int { kPassCold = 0, kPassWarm = 1, kPassRedo = 2, kPassExact = 3 };
 
 // Device workspace for one batch (all arrays entry-major, cell fastest).
 struct Workspace {
@@ -176,6 +181,9 @@ struct Workspace {
     int* s64_count;         // [ncell]
     int s64_capacity;
     int fp64_items;         // FP64 work-queue form: every attempt item runs from its FP64 seed
+    float slow_projection;  // projected FP64 iterations above which a trial is re-run exactly
+    int continue_limit;     // FP32 iterations from which an undecided trial or unsettled attempt
+                            // runs from its start in FP64 instead of from its FP32 end point
     int64_t io_stride;      // stride of the caller's z and output rows (the whole batch when this
                             // solve is one cell range of it; the pointers start at the range)
 };
@@ -252,7 +260,9 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
     stage_mixture(mix_g, m);
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; c < ws.ncell; c += stride) {
-        if (ws.pass == kPassRedo && ws.phase[c] != pRedo) continue;  // settled by the warm pass
+        // the later passes take only the cells their pass was left
+        if (ws.pass == kPassRedo && ws.phase[c] != pRedo) continue;
+        if (ws.pass == kPassExact && ws.phase[c] != pExact) continue;
         fp64::Cell<NM> cell;
         cell.n = m.n;
         cell.newton = true;
@@ -283,7 +293,7 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
             }
             warm = warm && contrast > 0.0;  // else: the cold path in this pass
         }
-        if (ws.pass != kPassRedo) ws.warm_cell[c] = warm ? 1 : 0;
+        if (ws.pass < kPassRedo) ws.warm_cell[c] = warm ? 1 : 0;
         if (warm) atomicAdd(&ws.counters[sWarmCells], 1);
         if (ph == pPending) {
             double lp[NM], zref = 0.0;
@@ -346,12 +356,12 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
         }
         ws.phase[c] = ph;
         add_total(ws, tE64Setup, cell.counters[cInitEvals]);
-        if (ws.pass != kPassRedo) {
+        if (ws.pass < kPassRedo) {
             for (int k = 0; k < cCount; ++k) ws.counters_out[idx(k, ws.ncell, c)] = 0;
             ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)] = cell.counters[cInitEvals];
             if (ph == pSplit) ws.counters_out[idx(cAttempts, ws.ncell, c)] = 1;
         } else {
-            // the warm attempt's work stays counted
+            // the earlier pass's work stays counted
             ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)] += cell.counters[cInitEvals];
         }
         if (ph == pInvalid || ph == pIndeterminate) {
@@ -546,7 +556,7 @@ __device__ float projected_fp64_iterations(const TrialLane<NM>& L) {
 }
 
 template <int NM>
-__device__ int trial_classify(const TrialLane<NM>& L) {
+__device__ int trial_classify(const TrialLane<NM>& L, float slow_projection) {
     const fp32::ScreenOptions so = fp32::screen_options();
     const int n = L.cell.n;
     const float margin = so.decide * L.point.mag;
@@ -557,7 +567,7 @@ __device__ int trial_classify(const TrialLane<NM>& L) {
     // (the projection is only a screen: near the FP32 noise floor the measured
     // contraction understates the FP64 rate, so no trial is declared
     // "iteration_limit" from it without the FP64 run)
-    const int slow = (L.iter >= 400 || projected_fp64_iterations(L) > kSlowProjection) ? kSlowFlag : 0;
+    const int slow = (L.iter >= 400 || projected_fp64_iterations(L) > slow_projection) ? kSlowFlag : 0;
     if (L.point.stat > 10.f * so.stat_tol) return fp32::tMarginal | slow;
     for (int r = 0; r < L.nrefs; ++r) {
         float dist = 0.f;
@@ -584,7 +594,7 @@ __global__ void __launch_bounds__(128) trials32_kernel(const Mixture* __restrict
     for (;;) {
         if (live && L.stage >= 2) {
             if (L.item >= 0 && L.stage == 2) {
-                const int cls = L.result >= 0 ? L.result : trial_classify(L);
+                const int cls = L.result >= 0 ? L.result : trial_classify(L, ws.slow_projection);
                 const int64_t c = L.c;
                 ws.tclass[idx(L.k, ws.ncell, c)] = static_cast<signed char>(cls);
                 ws.titer[idx(L.k, ws.ncell, c)] = static_cast<short>(L.iter);
@@ -1252,6 +1262,21 @@ __device__ __forceinline__ bool unsettled(int cls) { return cls != fp32::aTrivia
 // pair (aFailedFar) stops there in FP64 too.
 __device__ __forceinline__ bool open_attempt(int cls) { return cls == fp32::aFailed; }
 
+// A cell FP32 cannot screen -- no FP32 attempt converged, or the replay of the
+// reference's line search puts the polished attempt at risk -- is solved again
+// by the exact pass, every trial and attempt an FP64 item along the
+// reference's own path from its start.  On such cells (hard near-critical
+// states, N = 20 at 10-12 MPa and 365-375 K) FP32 descents stop early and the
+// FP64 runs continued from there end differently from the reference's runs
+// from the start.  Warm cells go to the cold pass instead.  Returns whether the
+// cell was marked.
+__device__ __forceinline__ bool mark_exact(const Workspace& ws, int64_t c) {
+    if (ws.fp64_items || (ws.pass == kPassWarm && ws.warm_cell[c] != 0)) return false;
+    ws.phase[c] = pExact;
+    atomicAdd(&ws.counters[sExactCells], 1);
+    return true;
+}
+
 // Queues a cell's attempts for the FP64 continuation (split64) and lists the
 // cell for select64: every unsettled attempt when no polished pair was
 // accepted (cand_order < 0), else the open attempts, which then compete with
@@ -1427,11 +1452,12 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
         add_count(ws, sPolishJacobians, s.jacobians);
         add_count(ws, sPolishSolves, s.solves);
         if (replay_risk) {
-            // the reference's own runs of every attempt, from the FP64 seeds
+            atomicAdd(&ws.counters[sReplayRisk], 1);
+            if (mark_exact(ws, c)) continue;
+            // (a warm cell) the reference's own runs of every attempt, from the FP64 seeds
             int cnt = 0;
             for (int a = 0; a < na; ++a) cnt += unsettled(ws.att_class[idx(a, ws.ncell, c)]);
             queue_attempts64<NM>(ws, c, na, cnt, -1, 0.0, true);
-            atomicAdd(&ws.counters[sReplayRisk], 1);
             continue;
         }
         if (!have) {
@@ -1451,8 +1477,9 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
                 write_counters<NM>(out, ws, c);
                 continue;
             }
-            queue_attempts64<NM>(ws, c, na, cnt, -1, 0.0);
             atomicAdd(&ws.counters[best < 0 ? sFbNoAttempt : (polish_failed ? sFbPolish : sFbRejected)], 1);
+            if (best < 0 && mark_exact(ws, c)) continue;
+            queue_attempts64<NM>(ws, c, na, cnt, -1, 0.0);
             continue;
         }
         int open = 0;

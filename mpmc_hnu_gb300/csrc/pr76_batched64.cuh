@@ -355,8 +355,9 @@ __global__ void __launch_bounds__(64) split64_kernel(const Mixture* __restrict__
                 } else {
                     L.c = code >> 5;
                     L.order = code & kOrderMask;
+                    const int done = ws.att_iter[idx(L.order, ws.ncell, L.c)];
                     const bool from_seed =
-                        ws.fp64_items || (code & kFromSeed) || ws.att_iter[idx(L.order, ws.ncell, L.c)] == 0;
+                        ws.fp64_items || (code & kFromSeed) || done == 0 || done >= ws.continue_limit;
                     L.iter = 0;
                     L.stage = 0;
                     L.evals = 0;
@@ -439,6 +440,9 @@ __global__ void __launch_bounds__(128) classify_kernel(const Mixture* __restrict
             const int cls = raw & (kSlowFlag - 1);
             const bool slow = (raw & kSlowFlag) != 0;
             bool rerun = cls == fp32::tRerun;
+            // a long FP32 descent is not continued: its FP64 count from the
+            // FP32 end point need not be the reference's from the start
+            if (cls == fp32::tMarginal && ws.titer[idx(k, ws.ncell, c)] >= ws.continue_limit) rerun = true;
             if (slow) {
                 // Another trial of this test is already negative, so the test is
                 // "unstable" whatever this one does; its FP32 end point has a

@@ -1043,32 +1043,39 @@ __global__ void __launch_bounds__(128) trials64w_kernel(const Mixture* __restric
                 ref = cell.comp ? ws.ref_lnphi[idx(lane, ws.ncell, c)] : 0.0;
                 tol = 1e-10;
             }
-            double w = 0.0;
             const bool rerun = mode == mFeedRerun || mode == mReviewRerun;
-            if (rerun) {
-                // trial starts (pt_stability.hpp:294-310, extra starts :263-272)
+            // the trial's start (pt_stability.hpp:294-310, extra starts :263-272)
+            double w0 = 0.0;
+            {
                 const int n_auto = auto_starts(active);
                 if (k >= n_auto) {
-                    w = (k - n_auto == 0) ? ex0 : ex1;
+                    w0 = (k - n_auto == 0) ? ex0 : ex1;
                 } else if (k == 0) {
-                    w = cell.z;
+                    w0 = cell.z;
                 } else if (k == 1) {
-                    w = cell.act ? 1.0 / static_cast<double>(active) : 0.0;
+                    w0 = cell.act ? 1.0 / static_cast<double>(active) : 0.0;
                 } else {
                     const unsigned mask = seg_ballot<S>(cell.act);
                     const int rank = __popc(mask & ((1u << lane) - 1u));
-                    w = cell.z * 0.1 + ((cell.act && rank == k - 2) ? 0.9 : 0.0);
+                    w0 = cell.z * 0.1 + ((cell.act && rank == k - 2) ? 0.9 : 0.0);
                 }
-                if (!cell.comp) w = 0.0;
-                w /= wsum<S>(w);
-            } else {
+                if (!cell.comp) w0 = 0.0;
+                w0 /= wsum<S>(w0);
+                if (!cell.comp) w0 = 0.0;
+            }
+            double w = w0;
+            if (!rerun) {
                 w = cell.act ? static_cast<double>(ws.tw[idx(k * NM + lane, ws.ncell, c)]) : 0.0;
                 w /= wsum<S>(w);
+                if (!cell.comp) w = 0.0;
             }
-            if (!cell.comp) w = 0.0;
-            if (!ok) status = fp64::kPropertyFailure;
-            else if (wany<S>(cell.act && w == 0.0)) status = fp64::kUnrepresentableComposition;
-            else status = trial(cell, w, ref, tol, row, point, rerun ? 0 : ws.titer[idx(k, ws.ncell, c)]);
+            if (!ok) {
+                status = fp64::kPropertyFailure;
+            } else if (wany<S>(cell.act && w == 0.0)) {
+                status = fp64::kUnrepresentableComposition;
+            } else {
+                status = trial(cell, w, ref, tol, row, point, rerun ? 0 : ws.titer[idx(k, ws.ncell, c)]);
+            }
         }
         if (lane == 0) ws.t64_status[idx(k, ws.ncell, c)] = static_cast<signed char>(status);
         if (!review && status == fp64::kNegativeTpd && lane < m.n)
@@ -1099,7 +1106,10 @@ __global__ void __launch_bounds__(128) split64w_kernel(const Mixture* __restrict
         const int order = code & kOrderMask;
         // the FP64 seed with the whole budget, or the FP32 end point with what is left
         // (an attempt without FP32 progress also starts from its exact seed)
-        const bool from_seed = ws.fp64_items || (code & kFromSeed) || ws.att_iter[idx(order, ws.ncell, c)] == 0;
+        // (and one whose FP32 run was long: its FP64 count from the FP32 end
+        // point need not be the reference's from the seed)
+        const int done = ws.att_iter[idx(order, ws.ncell, c)];
+        const bool from_seed = ws.fp64_items || (code & kFromSeed) || done == 0 || done >= ws.continue_limit;
         WCell<NM, S> cell;
         Split point;
         int evals = 0;
@@ -1108,7 +1118,7 @@ __global__ void __launch_bounds__(128) split64w_kernel(const Mixture* __restrict
             const double lk0 = !cell.comp ? 0.0
                                : (from_seed ? ws.att_lnk64[idx(order * NM + lane, ws.ncell, c)]
                                             : static_cast<double>(ws.att_lnk[idx(order * NM + lane, ws.ncell, c)]));
-            status = attempt(cell, lk0, point, evals, from_seed ? 0 : ws.att_iter[idx(order, ws.ncell, c)]);
+            status = attempt(cell, lk0, point, evals, from_seed ? 0 : done);
         }
         if (lane == 0) ws.s64_status[item] = static_cast<signed char>(status);
         if (status == fp64::kConverged) {
@@ -1236,8 +1246,8 @@ __global__ void __launch_bounds__(128) polishw_kernel(const Mixture* __restrict_
             add_count(ws, sPolishJacobians, jacobians);
             add_count(ws, sPolishSolves, solves);
         }
-        if (replay_risk) {  // the reference's own runs of every attempt, from the FP64 seeds
-            if (lane == 0) {
+        if (replay_risk) {  // the exact pass, or (a warm cell) every attempt from its FP64 seed
+            if (lane == 0 && !mark_exact(ws, c)) {
                 int cnt = 0;
                 for (int a = 0; a < na; ++a) cnt += unsettled(ws.att_class[idx(a, ws.ncell, c)]);
                 queue_attempts64<NM>(ws, c, na, cnt, -1, 0.0, true);
@@ -1258,8 +1268,8 @@ __global__ void __launch_bounds__(128) polishw_kernel(const Mixture* __restrict_
                     write_status_only<NM>(out, ws, c, kIndeterminate, false);
                     write_counters<NM>(out, ws, c);
                 } else {
-                    queue_attempts64<NM>(ws, c, na, cnt, -1, 0.0);
                     atomicAdd(&ws.counters[best < 0 ? sFbNoAttempt : (polish_failed ? sFbPolish : sFbRejected)], 1);
+                    if (!(best < 0 && mark_exact(ws, c))) queue_attempts64<NM>(ws, c, na, cnt, -1, 0.0);
                 }
             }
             continue;

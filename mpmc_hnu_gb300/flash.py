@@ -171,7 +171,7 @@ BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun
                "slow_trials_skipped", "limit_attempts", "warm_cells", "warm_redo",
                "warm_redo_no_pair", "warm_redo_unstable", "competing_cells", "competing_cells_fp64", "replay_risk_cells",
                "fp64_evals_setup", "fp64_evals_feed_trials", "fp64_evals_review_trials", "fp64_evals_polish",
-               "fp64_evals_split64", "polish_jacobians", "polish_solves"]
+               "fp64_evals_split64", "polish_jacobians", "polish_solves", "fallback_cells", "exact_cells"]
 FLAG_STAGE_TIMING = 1
 _QUEUE_STAGES = ["setup", "feed_trials", "feed_classify", "feed_trials64", "decide", "split", "polish",
                  "open32", "compete", "split64", "select64", "relist", "review_trials", "review_classify", "review_trials64",

@@ -63,11 +63,14 @@ def test_launch_shapes_keep_the_results(gpu_lib, oracle_lib):
     g = gpu_lib.GpuFlash(mix, form="mixed")
     # residency and item forms (the SS -> Newton switch moves rounding of the
     # FP32 stopping point and is guarded by the autotuner instead)
-    for shape in ([0] * 7, [2, 2, 1, 4, 8, 8], [4, 4, 4, 1, 4, 0], [0, 0, 0, 0, 0, 15]):
+    for shape in ([0] * 7, [2, 2, 1, 4, 8, 8], [4, 4, 4, 1, 4, 0], [0, 0, 0, 0, 0, 15], [0, 0, 0, 0, 0, 32 + 128],
+                  [0, 0, 0, 0, 0, 64, 0, 2], [0] * 8 + [128, 64]):
         g.set_launch_shape(shape)
         out = g.solve(p, t, z)
         rep = parity.flash_report(out, ref, mix, p, t, z)
         parity.assert_flash_parity(rep)
     with pytest.raises(gpu_lib.FlashError):
-        g.set_launch_shape([0, 0, 0, 0, 0, 0, 0, 0, 0])
+        g.set_launch_shape([0] * 11)
+    with pytest.raises(gpu_lib.FlashError):
+        g.set_launch_shape([0] * 8 + [513])
     g.close()
