@@ -420,10 +420,11 @@ def kernels_per_solve(form: str, sens: bool) -> int:
     """Kernels one cold device-resident solve launches: 17 per pass of
     flash_batched.cu (setup, feed trials / classify / trials64, decide,
     split32, polish, open32, compete, split64, select64, relist, review
-    trials / classify / trials64, finish, fallback); the mixed form runs the
-    main pass and the exact pass, the FP64 work-queue form one pass, the plain
-    form one kernel; plus the sensitivity kernel."""
-    per = {"plain": 1, "batched": 17, "mixed": 34}[form]
+    trials / classify / trials64, finish, fallback); the mixed form runs its
+    pass and the exact sub-solve (gather, the FP64 form's 17, scatter), the
+    FP64 work-queue form one pass, the plain form one kernel; plus the
+    sensitivity kernel."""
+    per = {"plain": 1, "batched": 17, "mixed": 36}[form]
     return per + (1 if sens else 0)
 
 

@@ -515,10 +515,10 @@ int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* handle, float* ms, int capacity
  * closed-form Jacobians the polish factorised and [29] its chord-step solves
  * (the algorithmic work of each FP64 stage); [30] cells the plain FP64
  * fallback solved (a nonsmooth feed phase, unusable constants, or FP64
- * attempt items beyond the queue's capacity); [31] cells the exact pass
+ * attempt items beyond the queue's capacity); [31] cells the exact sub-solve
  * solved again with every trial and attempt in FP64 (no FP32 attempt
- * converged, or the replay put the polished attempt at risk).  After a
- * warm-start solve, [0]-[15] and [30] count the last pass and [20]-[29] and
+ * converged, or the replay put the polished attempt at risk; the
+ * sub-solve's own work is not in [0]-[29]).  After a warm-start solve, [0]-[15] and [30] count the last pass and [20]-[29] and
  * [31] every pass.
  * Writes up to `capacity` values; returns the number available (0 for the
  * plain form).  Diagnostic entry point with no counterpart in the reference. */

@@ -82,10 +82,10 @@ struct mpmc_gpu_flash {
     bool stage_timing = false;
     cudaEvent_t events[24] = {};
     cudaEvent_t redo_events[24] = {};  // the cold pass after a warm pass
-    cudaEvent_t exact_events[24] = {};  // the exact pass of the mixed form
+    cudaEvent_t exact_events[24] = {};  // the exact sub-solve of the mixed form
     int n_events = 0;   // events recorded by the last solve (stages + 1)
     bool timed_warm = false;  // the last timed solve ran a warm and a cold pass
-    bool timed_exact = false; // the last timed solve ran the exact pass
+    bool timed_exact = false; // the last timed solve ran the exact sub-solve
     DevBuf in_warm;     // host entry: staged ln K warm starts
     DevBuf outs3[5];    // host entry: staged three-phase outputs
     DevBuf in_hints[7];   // host hinted entry: staged counts, compositions, three-phase flags, fractions
@@ -95,6 +95,9 @@ struct mpmc_gpu_flash {
     // by events on the caller's stream), each with its own workspace
     cudaStream_t range_streams[8] = {};
     cudaEvent_t fork_event = nullptr;
+    // the mixed form's exact sub-solve overlaps the main pass on this stream
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t side_fork = nullptr, side_join = nullptr;
     cudaEvent_t join_events[8] = {};
     int last_ranges = 1;          // ranges of the last work-queue solve and their workspace offsets
     size_t range_offset[8] = {};
@@ -292,6 +295,13 @@ int prepare_device(mpmc_gpu_flash* h, int64_t ncell, pr76::DeviceOutputs& d) {
         const int k = h->stage_timing ? 1 : solve_ranges(h, ncell);
         cudaError_t e = h->workspace.ensure(ranged_workspace_bytes(h->n, ncell, h->form == MPMC_FORM_BATCHED, k));
         if (e != cudaSuccess) return cuda_fail(e, "batched workspace allocation");
+        if (h->form == MPMC_FORM_MIXED && !h->side_stream) {
+            if ((e = cudaStreamCreateWithFlags(&h->side_stream, cudaStreamNonBlocking)) != cudaSuccess)
+                return cuda_fail(e, "side stream");
+            if ((e = cudaEventCreateWithFlags(&h->side_fork, cudaEventDisableTiming)) != cudaSuccess ||
+                (e = cudaEventCreateWithFlags(&h->side_join, cudaEventDisableTiming)) != cudaSuccess)
+                return cuda_fail(e, "cudaEventCreate");
+        }
         if (k > 1 && !h->fork_event) {
             if ((e = cudaEventCreateWithFlags(&h->fork_event, cudaEventDisableTiming)) != cudaSuccess)
                 return cuda_fail(e, "cudaEventCreate");
@@ -334,6 +344,13 @@ cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, co
         h->last_ranges = k;
         ranged_workspace_bytes(h->n, ncell, fp64_items, k, h->range_offset);
         if (k == 1) {
+            // the exact sub-solve on the side stream, except when the stages
+            // are timed (then it runs after the main pass, with its own events)
+            if (!timing && h->side_stream) {
+                shape.side_stream = h->side_stream;
+                shape.side_fork = h->side_fork;
+                shape.side_join = h->side_join;
+            }
             e = pr76::launch_batched(h->n, h->d_mixture, ncell, p, t, z, d, h->workspace.ptr, h->workspace.bytes,
                                      shape, stream);
         } else {
@@ -705,7 +722,7 @@ int mpmc_gpu_flash_stage_timings(mpmc_gpu_flash* h, float* ms, int capacity) {
         cudaEventElapsedTime(&v, h->events[k], h->events[k + 1]);
         // after a warm pass, each stage's time is that of both passes
         // each stage's time is that of every pass the solve ran (first, then
-        // the cold pass after a warm pass, then the exact pass)
+        // the cold pass after a warm pass, then the exact sub-solve)
         if (k < pr76::kBatchedStages) {
             float r = 0.f;
             if (h->timed_warm) {
@@ -797,6 +814,12 @@ int mpmc_gpu_flash_destroy(mpmc_gpu_flash* h) {
         if (h->join_events[r]) cudaEventDestroy(h->join_events[r]);
     }
     if (h->fork_event) cudaEventDestroy(h->fork_event);
+    if (h->side_stream) {
+        cudaStreamSynchronize(h->side_stream);
+        cudaStreamDestroy(h->side_stream);
+    }
+    if (h->side_fork) cudaEventDestroy(h->side_fork);
+    if (h->side_join) cudaEventDestroy(h->side_join);
     if (h->flash_done) cudaEventDestroy(h->flash_done);
     for (auto& ev : h->chunk_done)
         if (ev) cudaEventDestroy(ev);

@@ -22,7 +22,28 @@ size_t align256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
 
 // Carves the workspace arrays out of one scratch allocation; with base ==
 // nullptr only computes the size.
-size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell, bool fp64_items, int s64_per_cell) {
+// The exact sub-solve of the mixed form (cells FP32 could not screen, solved
+// again with every trial and attempt in FP64): its packed inputs and outputs
+// and the FP64 form's workspace for `cap` cells, carved after the main
+// workspace.
+struct ExactRegion {
+    double *p = nullptr, *t = nullptr, *z = nullptr;
+    DeviceOutputs out{};
+    char* scratch = nullptr;
+    size_t scratch_bytes = 0;
+};
+
+size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell, bool fp64_items, int s64_per_cell,
+             int exact_cap = 0, ExactRegion* exact = nullptr);
+
+// Cells the exact sub-solve holds for a batch of ncell: all of a small batch,
+// an eighth of a large one (at least 65,536).
+int exact_capacity(int64_t ncell) {
+    return static_cast<int>(ncell <= 65536 ? ncell : std::max<int64_t>(65536, ncell / 8));
+}
+
+size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell, bool fp64_items, int s64_per_cell,
+             int exact_cap, ExactRegion* exact) {
     const size_t nc = static_cast<size_t>(ncell);
     size_t off = 0;
     auto take = [&](size_t bytes) {
@@ -73,6 +94,29 @@ size_t carve(batched::Workspace& ws, char* base, int n, int64_t ncell, bool fp64
     ws.s64_cells = reinterpret_cast<int*>(take(sizeof(int) * nc));
     ws.s64_base = reinterpret_cast<int*>(take(sizeof(int) * nc));
     ws.s64_count = reinterpret_cast<int*>(take(sizeof(int) * nc));
+    ws.exact_capacity = fp64_items ? 0 : exact_cap;
+    ws.exact_list = reinterpret_cast<int*>(take(sizeof(int) * static_cast<size_t>(ws.exact_capacity)));
+    if (ws.exact_capacity > 0) {
+        const size_t cap = static_cast<size_t>(ws.exact_capacity);
+        ExactRegion r;
+        r.p = reinterpret_cast<double*>(take(sizeof(double) * cap));
+        r.t = reinterpret_cast<double*>(take(sizeof(double) * cap));
+        r.z = reinterpret_cast<double*>(take(sizeof(double) * NM * cap));
+        r.out.status = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * cap));
+        r.out.beta = reinterpret_cast<double*>(take(sizeof(double) * cap));
+        r.out.x = reinterpret_cast<double*>(take(sizeof(double) * NM * cap));
+        r.out.y = reinterpret_cast<double*>(take(sizeof(double) * NM * cap));
+        r.out.lnk = reinterpret_cast<double*>(take(sizeof(double) * NM * cap));
+        r.out.lnphi_l = reinterpret_cast<double*>(take(sizeof(double) * NM * cap));
+        r.out.lnphi_v = reinterpret_cast<double*>(take(sizeof(double) * NM * cap));
+        r.out.z_l = reinterpret_cast<double*>(take(sizeof(double) * cap));
+        r.out.z_v = reinterpret_cast<double*>(take(sizeof(double) * cap));
+        r.out.counters = reinterpret_cast<int32_t*>(take(sizeof(int32_t) * cCount * cap));
+        batched::Workspace sub;
+        r.scratch_bytes = carve(sub, nullptr, n, ws.exact_capacity, true, kS64PerCell);
+        r.scratch = take(r.scratch_bytes);
+        if (exact) *exact = r;
+    }
     return off;
 }
 
@@ -88,7 +132,10 @@ using namespace MPMC_CAT(batched_host_nm, MPMC_NM);
 
 size_t MPMC_CAT(batched_workspace_bytes_nm, MPMC_NM)(int n, int64_t ncell, bool fp64_items, int s64_per_cell) {
     batched::Workspace ws;
-    return carve(ws, nullptr, n, ncell, fp64_items, s64_per_cell);
+    // s64_per_cell below the full capacity: the least scratch that runs, with
+    // no exact sub-solve (its cells take the plain fallback)
+    return carve(ws, nullptr, n, ncell, fp64_items, s64_per_cell,
+                 s64_per_cell >= kS64PerCell ? exact_capacity(ncell) : 0);
 }
 
 cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, int64_t ncell, const double* p,
@@ -100,12 +147,14 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     if (ncell >= (int64_t{1} << 24)) return cudaErrorInvalidValue;  // work-item encodings hold 24-bit cells
     Workspace ws;
     const bool fp64_items = shape.fp64_items != 0;
-    // the largest FP64 attempt-item capacity the scratch holds
-    int per = kS64PerCell;
-    while (per > 1 && carve(ws, nullptr, n, ncell, fp64_items, per) > scratch_bytes) per /= 2;
-    if (carve(ws, nullptr, n, ncell, fp64_items, per) > scratch_bytes || scratch == nullptr)
+    // the largest FP64 attempt-item capacity and exact sub-solve the scratch holds
+    int per = kS64PerCell, ecap = fp64_items ? 0 : exact_capacity(ncell);
+    while (ecap > 0 && carve(ws, nullptr, n, ncell, fp64_items, per, ecap) > scratch_bytes) ecap /= 2;
+    while (per > 1 && carve(ws, nullptr, n, ncell, fp64_items, per, ecap) > scratch_bytes) per /= 2;
+    if (carve(ws, nullptr, n, ncell, fp64_items, per, ecap) > scratch_bytes || scratch == nullptr)
         return cudaErrorInvalidValue;
-    carve(ws, static_cast<char*>(scratch), n, ncell, fp64_items, per);
+    ExactRegion exact;
+    carve(ws, static_cast<char*>(scratch), n, ncell, fp64_items, per, ecap, &exact);
     ws.io_stride = shape.io_stride > 0 ? shape.io_stride : ncell;
     ws.slow_projection = shape.slow_projection > 0.f ? shape.slow_projection : kSlowProjection;
     ws.continue_limit = shape.continue_limit > 0 ? shape.continue_limit : kContinueLimit;
@@ -136,7 +185,37 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     const bool packed_attempts = (shape.item_form & 64) ? false : ((shape.item_form & 128) ? true : NM <= 8);
     const int s64_res = shape.s64_blocks_per_sm > 0 ? shape.s64_blocks_per_sm : 2;
     // one pass of the launch sequence over the cells `ws.pass` selects
-    auto run_pass = [&](cudaEvent_t* events, bool f64) -> cudaError_t {
+    // The exact sub-solve: the marked cells gathered, solved by the FP64
+    // work-queue form on their own workspace, written back.  On a side stream
+    // it overlaps the main pass's stages after the polish.
+    const bool side = shape.side_stream != nullptr && shape.side_fork != nullptr && shape.side_join != nullptr;
+    auto launch_exact = [&]() -> cudaError_t {
+        const int cap = ws.exact_capacity;
+        if (cap <= 0) return cudaSuccess;
+        cudaStream_t es = side ? shape.side_stream : stream;
+        cudaError_t err;
+        if (side) {
+            if ((err = cudaEventRecord(shape.side_fork, stream)) != cudaSuccess) return err;
+            if ((err = cudaStreamWaitEvent(es, shape.side_fork, 0)) != cudaSuccess) return err;
+        }
+        const unsigned g = static_cast<unsigned>(std::min<int64_t>((cap + 127) / 128, sms * 8));
+        gather_exact_kernel<NM><<<g, 128, 0, es>>>(ws, p, t, z, n, cap, exact.p, exact.t, exact.z);
+        BatchedShape sub = shape;
+        sub.fp64_items = 1;
+        sub.warm_lnk = nullptr;
+        sub.io_stride = 0;
+        sub.events = shape.exact_events;
+        sub.redo_events = nullptr;
+        sub.exact_events = nullptr;
+        sub.side_stream = nullptr;
+        err = MPMC_CAT(launch_batched_nm, MPMC_NM)(d_mix, n, cap, exact.p, exact.t, exact.z, exact.out, exact.scratch,
+                                                   exact.scratch_bytes, sub, es);
+        if (err != cudaSuccess) return err;
+        scatter_exact_kernel<NM><<<g, 128, 0, es>>>(ws, n, cap, exact.out, out);
+        if (side && (err = cudaEventRecord(shape.side_join, es)) != cudaSuccess) return err;
+        return cudaGetLastError();
+    };
+    auto run_pass = [&](cudaEvent_t* events, bool f64, bool fork_exact) -> cudaError_t {
         // the warm pass's statistics stay for the cold pass after it
         const int clear = ws.pass >= kPassRedo ? qPassSlots : qSlots;
         cudaError_t e = cudaMemsetAsync(ws.counters, 0, sizeof(int) * clear, stream);
@@ -177,6 +256,12 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
         if (lane_polish) polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
         else w64::polishw_kernel<NM, w64::kSeg<NM>><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t, out);
         mark();
+        // every cell the exact sub-solve takes is marked by now (in this
+        // pass's polish, or an earlier pass's)
+        if (fork_exact && side) {
+            const cudaError_t err = launch_exact();
+            if (err != cudaSuccess) return err;
+        }
         // attempts FP32 left open beside a polished pair: their FP32 prediction,
         // then the pair's review or the FP64 continuation of what stays open
         if (!f64) split32_kernel<NM><<<sms * split_res, qblock, 0, stream>>>(d_mix, ws, p, t, ss_switch, 1);
@@ -209,23 +294,21 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
     };
     ws.warm_lnk = shape.warm_lnk;
     ws.pass = shape.warm_lnk ? kPassWarm : kPassCold;
-    cudaError_t e = run_pass(shape.events, fp64_items);
+    cudaError_t e = run_pass(shape.events, fp64_items, !shape.warm_lnk);
     if (e != cudaSuccess) return e;
     if (shape.warm_lnk) {
         // the warm cells whose pair was not accepted: the full cold solve (a
         // nearly empty pass when the warm starts are good)
         ws.pass = kPassRedo;
-        e = run_pass(shape.redo_events, fp64_items);
+        e = run_pass(shape.redo_events, fp64_items, true);
         if (e != cudaSuccess) return e;
     }
     if (!fp64_items) {
-        // the cells FP32 could not screen (mark_exact): the whole solve again
-        // with every trial and attempt an exact FP64 item, as the FP64
-        // work-queue form runs it (a nearly empty pass on most batches)
-        ws.pass = kPassExact;
-        ws.fp64_items = 1;
-        e = run_pass(shape.exact_events, true);
-        ws.fp64_items = 0;
+        // the cells FP32 could not screen (mark_exact): without a side stream
+        // the sub-solve runs here, after the main passes; with one, the main
+        // stream waits for it (a nearly empty sub-solve on most batches)
+        if (!side) e = launch_exact();
+        else e = cudaStreamWaitEvent(stream, shape.side_join, 0);
         if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();

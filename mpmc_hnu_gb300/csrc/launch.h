@@ -66,7 +66,11 @@ struct BatchedShape {
     // the cell cold); null = cold solve of every cell
     const double* warm_lnk;
     cudaEvent_t* redo_events;  // optional: the events of the cold pass after a warm pass
-    cudaEvent_t* exact_events; // optional: the events of the exact pass (mixed form)
+    cudaEvent_t* exact_events; // optional: the stage events of the exact sub-solve (mixed form)
+    // optional: a second stream and two events on which the exact sub-solve
+    // overlaps the main pass (null: it runs on the solve's stream after it)
+    cudaStream_t side_stream;
+    cudaEvent_t side_fork, side_join;
     float slow_projection;     // projected FP64 iterations above which an FP32 trial is re-run exactly
                                // in FP64 (0 = the default)
     int continue_limit;        // FP32 iterations from which an undecided trial or unsettled attempt

@@ -107,7 +107,7 @@ enum Slot : int {
     tE64Split64 = 42,      // ... of the FP64 attempt continuations
     sPolishJacobians = 44, // closed-form Jacobians built and factorised by the polish
     sPolishSolves = 45,    // LU solves of the polish's chord steps
-    sExactCells = 46,      // cells solved again by the exact pass (every trial and attempt in FP64)
+    sExactCells = 46,      // cells marked for the exact sub-solve (every trial and attempt in FP64)
     qSlots = 48
 };
 
@@ -128,7 +128,7 @@ enum Phase : int {
     pPending = 10, pSplit = 11, pReview = 12, pFallback = 13, pSplit64 = 14,
     pRedo = 15,  // warm pass: the warm pair was not accepted, the cell runs the cold pass
     pCompete = 16,  // a polished pair waits on the open attempts' predicted ends
-    pExact = 17     // FP32 could not screen the cell: the exact pass solves it again in FP64
+    pExact = 17     // FP32 could not screen the cell: the exact sub-solve solves it again in FP64
 };
 
 // Passes of the launch sequence: the cold solve of every cell; the warm pass
@@ -184,6 +184,8 @@ struct Workspace {
     float slow_projection;  // projected FP64 iterations above which a trial is re-run exactly
     int continue_limit;     // FP32 iterations from which an undecided trial or unsettled attempt
                             // runs from its start in FP64 instead of from its FP32 end point
+    int* exact_list;        // [exact_capacity] cells for the exact sub-solve, in marking order
+    int exact_capacity;     // cells the exact sub-solve holds (beyond it: the plain fallback)
     int64_t io_stride;      // stride of the caller's z and output rows (the whole batch when this
                             // solve is one cell range of it; the pointers start at the range)
 };
@@ -1264,7 +1266,7 @@ __device__ __forceinline__ bool open_attempt(int cls) { return cls == fp32::aFai
 
 // A cell FP32 cannot screen -- no FP32 attempt converged, or the replay of the
 // reference's line search puts the polished attempt at risk -- is solved again
-// by the exact pass, every trial and attempt an FP64 item along the
+// by the exact sub-solve, every trial and attempt an FP64 item along the
 // reference's own path from its start.  On such cells (hard near-critical
 // states, N = 20 at 10-12 MPa and 365-375 K) FP32 descents stop early and the
 // FP64 runs continued from there end differently from the reference's runs
@@ -1272,9 +1274,60 @@ __device__ __forceinline__ bool open_attempt(int cls) { return cls == fp32::aFai
 // cell was marked.
 __device__ __forceinline__ bool mark_exact(const Workspace& ws, int64_t c) {
     if (ws.fp64_items || (ws.pass == kPassWarm && ws.warm_cell[c] != 0)) return false;
-    ws.phase[c] = pExact;
-    atomicAdd(&ws.counters[sExactCells], 1);
+    const int slot = atomicAdd(&ws.counters[sExactCells], 1);
+    if (slot < ws.exact_capacity) {
+        ws.exact_list[slot] = static_cast<int>(c);
+        ws.phase[c] = pExact;
+    } else {
+        // beyond the sub-solve's capacity: the plain FP64 solver, the same rules
+        ws.phase[c] = pFallback;
+        atomicAdd(&ws.counters[qFallback], 1);
+    }
     return true;
+}
+
+// The exact sub-solve's inputs: the marked cells packed into `cap` slots
+// (cell-fastest, stride cap); unused slots get an invalid pressure, which the
+// sub-solve's setup turns into an invalid request at no cost.
+template <int NM>
+__global__ void gather_exact_kernel(Workspace ws, const double* __restrict__ p, const double* __restrict__ t,
+                                    const double* __restrict__ z, int n, int cap, double* sp, double* st,
+                                    double* sz) {
+    const int count = min(ws.counters[sExactCells], cap);
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < cap; k += gridDim.x * blockDim.x) {
+        const bool live = k < count;
+        const int64_t c = live ? ws.exact_list[k] : 0;
+        sp[k] = live ? p[c] : nan;
+        st[k] = live ? t[c] : 300.0;
+        for (int i = 0; i < n; ++i) sz[static_cast<int64_t>(i) * cap + k] = live ? z[idx(i, ws.io_stride, c)] : 1.0 / n;
+    }
+}
+
+// The exact sub-solve's answers written back at the marked cells' places.
+template <int NM>
+__global__ void scatter_exact_kernel(Workspace ws, int n, int cap, DeviceOutputs sub, DeviceOutputs out) {
+    const int count = min(ws.counters[sExactCells], cap);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += gridDim.x * blockDim.x) {
+        const int64_t c = ws.exact_list[k];
+        auto row = [&](const double* from, double* to, int rows) {
+            if (!to) return;
+            for (int i = 0; i < rows; ++i) to[idx(i, ws.io_stride, c)] = from[static_cast<int64_t>(i) * cap + k];
+        };
+        if (out.status) out.status[c] = sub.status[k];
+        row(sub.beta, out.beta, 1);
+        row(sub.x, out.x, n);
+        row(sub.y, out.y, n);
+        row(sub.lnk, out.lnk, n);
+        row(sub.lnphi_l, out.lnphi_l, n);
+        row(sub.lnphi_v, out.lnphi_v, n);
+        row(sub.z_l, out.z_l, 1);
+        row(sub.z_v, out.z_v, 1);
+        if (out.counters)
+            for (int r = 0; r < cCount; ++r)
+                out.counters[idx(r, ws.io_stride, c)] = sub.counters[static_cast<int64_t>(r) * cap + k];
+        ws.phase[c] = sub.status[k];
+    }
 }
 
 // Queues a cell's attempts for the FP64 continuation (split64) and lists the

@@ -1246,7 +1246,7 @@ __global__ void __launch_bounds__(128) polishw_kernel(const Mixture* __restrict_
             add_count(ws, sPolishJacobians, jacobians);
             add_count(ws, sPolishSolves, solves);
         }
-        if (replay_risk) {  // the exact pass, or (a warm cell) every attempt from its FP64 seed
+        if (replay_risk) {  // the exact sub-solve, or (a warm cell) every attempt from its FP64 seed
             if (lane == 0 && !mark_exact(ws, c)) {
                 int cnt = 0;
                 for (int a = 0; a < na; ++a) cnt += unsettled(ws.att_class[idx(a, ws.ncell, c)]);
