@@ -417,14 +417,15 @@ def wilson_ln_k(mix, p, t):
 
 
 def kernels_per_solve(form: str, sens: bool) -> int:
-    """Kernels one cold device-resident solve launches: 17 per pass of
-    flash_batched.cu (setup, feed trials / classify / trials64, decide,
-    split32, polish, open32, compete, split64, select64, relist, review
-    trials / classify / trials64, finish, fallback); the mixed form runs its
-    pass and the exact sub-solve (gather, the FP64 form's 17, scatter), the
-    FP64 work-queue form one pass, the plain form one kernel; plus the
-    sensitivity kernel."""
-    per = {"plain": 1, "batched": 17, "mixed": 36}[form]
+    """Kernels one cold device-resident solve launches (counted in the ncu
+    launch list of one solve): the mixed form's pass has 17 (setup, feed
+    trials32 / classify / trials64, decide, split32, polish, open32, compete,
+    split64, select64, relist, review trials32 / classify / trials64, finish,
+    fallback); the FP64 work-queue form's 15 (no FP32 ln K iterations, its
+    trials queued by rerun_all); the mixed form adds the exact sub-solve
+    (gather, the FP64 form's 15, scatter); the plain form is one kernel; plus
+    the sensitivity kernel."""
+    per = {"plain": 1, "batched": 15, "mixed": 34}[form]
     return per + (1 if sens else 0)
 
 

@@ -136,7 +136,7 @@ enum Phase : int {
 // the common-tangent review, no feed test, while the other cells take the
 // cold path in the same pass); the cold solve of the warm cells whose pair was
 // not accepted.
-enum Pass : int { kPassCold = 0, kPassWarm = 1, kPassRedo = 2, kPassExact = 3 };
+enum Pass : int { kPassCold = 0, kPassWarm = 1, kPassRedo = 2 };
 
 // Device workspace for one batch (all arrays entry-major, cell fastest).
 struct Workspace {
@@ -262,9 +262,7 @@ __global__ void __launch_bounds__(128) setup_kernel(const Mixture* __restrict__ 
     stage_mixture(mix_g, m);
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t c = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; c < ws.ncell; c += stride) {
-        // the later passes take only the cells their pass was left
-        if (ws.pass == kPassRedo && ws.phase[c] != pRedo) continue;
-        if (ws.pass == kPassExact && ws.phase[c] != pExact) continue;
+        if (ws.pass == kPassRedo && ws.phase[c] != pRedo) continue;  // settled by the warm pass
         fp64::Cell<NM> cell;
         cell.n = m.n;
         cell.newton = true;
