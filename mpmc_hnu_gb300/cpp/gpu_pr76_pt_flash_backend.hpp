@@ -20,8 +20,13 @@
 // (phase_set_transition_flash_adapter.hpp:130-248); an indeterminate result
 // from an unresolved two-phase or three-phase search carries none, since the
 // C ABI does not return the attempts behind it.  Caller starts are carried in
-// the form the C ABI takes (GpuPr76BackendStarts, below); not carried: the
-// phase metadata.
+// the form the C ABI takes (GpuPr76BackendStarts, below): the continuation's
+// form (the same compositions as initial, final and three-phase starts) or
+// the general one, which gpu_starts_from() fills from the reference's own
+// Pr76PtFlashBackendOptions (initial_starts, final_starts, one three-phase
+// start, split.initial_stability.automatic_starts, split.max_split_attempts;
+// every other field at its default, as the device code implements it); not
+// carried: the phase metadata.
 //
 // Errors follow the reference's classes: an invalid request (feed size,
 // non-finite or non-positive p and T, a feed outside the simplex) throws
@@ -70,9 +75,47 @@ struct GpuPr76Mixture {
 // three compositions with that phase_fraction_seed (Pr76PtThreePhaseStart,
 // pr76_three_phase.hpp:114-117).  Every request of the backend gets them.
 struct GpuPr76BackendStarts {
+    // the continuation's form: these compositions are the initial and the
+    // final starts and, with a fraction seed, the three-phase start
     std::vector<std::vector<double>> stability_starts;
     std::optional<std::array<double, 2>> three_phase_fraction_seed;
+    // the general form (mpmc_gpu_flash_solve_hinted_ex), used when `general`
+    bool general = false;
+    std::vector<std::vector<double>> initial_starts, final_starts;
+    std::optional<std::array<std::vector<double>, 3>> three_phase_start;
+    std::array<double, 2> three_phase_seed{1.0 / 3.0, 1.0 / 3.0};
+    bool initial_automatic_starts = true;
+    int max_split_attempts = 16;
 };
+
+#if __has_include(<mpmc/flash/pr76_pt_flash_backend.hpp>)
+}  // namespace mpmc::flash
+#include <mpmc/flash/pr76_pt_flash_backend.hpp>
+namespace mpmc::flash {
+
+// The caller inputs of a Pr76PtFlashBackendOptions (pr76_pt_flash_backend.hpp:
+// 26-40) in the binding's general form.  The device code takes at most three
+// initial and three final starts and one three-phase start per cell, and the
+// two split options; more starts throw std::invalid_argument.
+inline GpuPr76BackendStarts gpu_starts_from(const Pr76PtFlashBackendOptions& o) {
+    if (o.initial_starts.size() > 3 || o.final_starts.size() > 3 || o.three_phase_starts.size() > 1)
+        throw std::invalid_argument("GPU PR76 backend: at most three initial and three final starts and one "
+                                    "three-phase start");
+    if (o.split.max_split_attempts > 65536)
+        throw std::invalid_argument("GPU PR76 backend: max_split_attempts above 65536");
+    GpuPr76BackendStarts s;
+    s.general = true;
+    s.initial_starts = o.initial_starts;
+    s.final_starts = o.final_starts;
+    if (!o.three_phase_starts.empty()) {
+        s.three_phase_start = o.three_phase_starts.front().compositions;
+        s.three_phase_seed = o.three_phase_starts.front().phase_fraction_seed;
+    }
+    s.initial_automatic_starts = o.split.initial_stability.automatic_starts;
+    s.max_split_attempts = static_cast<int>(o.split.max_split_attempts);
+    return s;
+}
+#endif
 
 class GpuPr76PtFlashBackend final : public PtFlashBackend {
 public:
@@ -83,8 +126,17 @@ public:
             (starts_.three_phase_fraction_seed && starts_.stability_starts.size() != 3))
             throw std::invalid_argument("GPU PR76 backend: at most three stability starts, exactly three with a "
                                         "three-phase start");
-        for (const auto& st : starts_.stability_starts)
+        if (starts_.general && (starts_.initial_starts.size() > 3 || starts_.final_starts.size() > 3 ||
+                                starts_.max_split_attempts < 0))
+            throw std::invalid_argument("GPU PR76 backend: at most three initial and three final starts");
+        auto sized = [&](const std::vector<double>& st) {
             if (st.size() != n_) throw std::invalid_argument("GPU PR76 backend: start size does not match the mixture");
+        };
+        for (const auto& st : starts_.stability_starts) sized(st);
+        for (const auto& st : starts_.initial_starts) sized(st);
+        for (const auto& st : starts_.final_starts) sized(st);
+        if (starts_.three_phase_start)
+            for (const auto& st : *starts_.three_phase_start) sized(st);
         if (n_ == 0 || mixture.critical_temperature_k.size() != n_ || mixture.critical_pressure_pa.size() != n_ ||
             mixture.acentric_factor.size() != n_ || mixture.kij.size() != n_ * n_)
             throw std::invalid_argument("GPU PR76 backend: mixture arrays do not match the component list");
@@ -171,7 +223,34 @@ public:
         std::vector<int32_t> max3(cells);
         std::vector<double> frac3(3 * cells), comp3(3 * n_ * cells), phi3(3 * n_ * cells), z3(3 * cells);
         mpmc_three_phase_outputs out3{max3.data(), frac3.data(), comp3.data(), phi3.data(), z3.data()};
-        if (cells > 0 && starts_.stability_starts.empty()) {
+        if (cells > 0 && starts_.general) {
+            // the general caller inputs, the same for every request
+            auto set = [&](const std::vector<std::vector<double>>& starts, std::vector<int32_t>& count,
+                           std::vector<double>& comp) {
+                count.assign(cells, static_cast<int32_t>(starts.size()));
+                comp.assign(3 * n_ * cells, 0.0);
+                for (std::size_t c = 0; c < cells; ++c)
+                    for (std::size_t q = 0; q < starts.size(); ++q)
+                        for (std::size_t i = 0; i < n_; ++i) comp[(q * n_ + i) * cells + c] = starts[q][i];
+            };
+            std::vector<int32_t> icount, fcount, three(cells, starts_.three_phase_start ? 1 : 0);
+            std::vector<double> icomp, fcomp, tcomp(3 * n_ * cells, 0.0), frac(2 * cells, 0.0);
+            set(starts_.initial_starts, icount, icomp);
+            set(starts_.final_starts, fcount, fcomp);
+            for (std::size_t c = 0; c < cells; ++c) {
+                frac[c] = starts_.three_phase_seed[0];
+                frac[cells + c] = starts_.three_phase_seed[1];
+                if (starts_.three_phase_start)
+                    for (std::size_t q = 0; q < 3; ++q)
+                        for (std::size_t i = 0; i < n_; ++i)
+                            tcomp[(q * n_ + i) * cells + c] = (*starts_.three_phase_start)[q][i];
+            }
+            const mpmc_start_hints_ex hints{icount.data(), icomp.data(), fcount.data(), fcomp.data(), three.data(),
+                                            tcomp.data(),  frac.data(),  starts_.initial_automatic_starts ? 1 : 0,
+                                            starts_.max_split_attempts};
+            check(mpmc_gpu_flash_solve_hinted_ex(handle_, static_cast<int64_t>(cells), p.data(), t.data(), z.data(),
+                                                 &hints, &out, &out3));
+        } else if (cells > 0 && starts_.stability_starts.empty()) {
             check(mpmc_gpu_flash_solve_max3(handle_, static_cast<int64_t>(cells), p.data(), t.data(), z.data(), &out,
                                             &out3));
         } else if (cells > 0) {

@@ -46,6 +46,11 @@ int mpmc_gpu_flash_solve_max3(mpmc_gpu_flash*, int64_t, const double*, const dou
                               const mpmc_flash_outputs*, const mpmc_three_phase_outputs*) {
     return MPMC_ERR_UNSUPPORTED;  // not used: this scenario has caller starts
 }
+int mpmc_gpu_flash_solve_hinted_ex(mpmc_gpu_flash*, int64_t, const double*, const double*, const double*,
+                                   const mpmc_start_hints_ex*, const mpmc_flash_outputs*,
+                                   const mpmc_three_phase_outputs*) {
+    return MPMC_ERR_UNSUPPORTED;  // not used: this scenario has the continuation's starts
+}
 int mpmc_gpu_flash_solve_hinted(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* t, const double* z,
                                 const mpmc_start_hints* hints, const mpmc_flash_outputs* out,
                                 const mpmc_three_phase_outputs* out3) {

@@ -208,3 +208,58 @@ def test_seeded_backend_binding_matches_reference(tmp_path):
     assert ref_status == got_status == "0" and ref_phases == got_phases == "3"
     assert float(worst) <= 1e-12
     assert ref_23 == got_23 == "1"
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "modules", "flash", "include")),
+                    reason="reference headers not present")
+@pytest.mark.skipif(shutil.which("g++") is None, reason="no g++")
+def test_backend_binding_takes_the_reference_options(tmp_path):
+    """GpuPr76PtFlashBackend built from the reference's own
+    Pr76PtFlashBackendOptions (gpu_starts_from) over the host build of the
+    device code, beside the reference's Pr76PtFlashBackend with the same
+    options, on the recorded hinted cases (tests/golden/max3_hinted_reference.npz):
+    the 3 -> 2 recovery through a phase disappearance (initial starts without
+    the automatic ones, 2 split attempts, separate final and three-phase
+    starts) and the zero split-attempt quota.  Same status, same phase count,
+    compositions within 1e-12."""
+    import numpy as np
+
+    from tests.test_oracle_max3 import hinted_cases
+
+    exe = str(tmp_path / "options_backend")
+    cmd = ["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-Wno-attributes", "-I/usr/local/cuda/include",
+           "-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(ROOT, "mpmc_hnu_gb300", "csrc"),
+           "-I" + os.path.join(ROOT, "mpmc_hnu_gb300", "cpp")]
+    cmd += ["-I" + os.path.join(REFERENCE, "modules", m, "include") for m in ("ad", "thermodynamics", "flash",
+                                                                               "physics", "flow", "mesh")]
+    subprocess.check_call(cmd + [os.path.join(ROOT, "tests", "host_build", "options_backend.cpp"),
+                                 os.path.join(ROOT, "tests", "host_build", "flash_host.cpp"), "-o", exe,
+                                 "-lpthread"])
+    cases = hinted_cases()
+    for name in ("recovery", "budget", "three"):
+        mix, z, h, ref = cases[name]
+        n = z.shape[0]
+
+        def comps(count_key, comp_key):
+            k = int(np.ravel(h[count_key])[0])
+            return [np.asarray(h[comp_key])[q * n:(q + 1) * n, 0] for q in range(k)]
+
+        vals = [n, *mix.tc, *mix.pc, *mix.omega, *np.asarray(mix.kij).ravel(), 1e6, 250.0, *z[:, 0]]
+        for key in (("initial_count", "initial_composition"), ("final_count", "final_composition")):
+            sts = comps(*key)
+            vals += [len(sts)] + [v for w in sts for v in w]
+        three = int(np.ravel(h["three_phase"])[0])
+        vals.append(three)
+        if three:
+            vals += list(np.asarray(h["three_phase_composition"])[:, 0]) + list(np.asarray(h["fraction"])[:, 0])
+        vals += [1.0 if h["initial_automatic_starts"] else 0.0, float(h["max_split_attempts"])]
+        inp = tmp_path / f"{name}.bin"
+        inp.write_bytes(np.asarray(vals, dtype=np.float64).tobytes())
+        out = subprocess.run([exe, str(inp)], capture_output=True, text=True, check=True).stdout.split()
+        ref_status, got_status, ref_phases, got_phases, worst = out
+        assert ref_status == got_status, (name, out)
+        assert ref_phases == got_phases, (name, out)
+        if int(ref_phases) > 0:
+            assert float(worst) <= 1e-12, (name, out)
+        if name == "recovery":
+            assert ref_phases == "2"
