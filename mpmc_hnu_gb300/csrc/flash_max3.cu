@@ -8,23 +8,30 @@
 
 namespace pr76 {
 
-// Max-3-phase continuation: one thread per cell over the whole batch; a cell
-// whose two-phase status is phase_set_unstable runs fp64::max3_cell, every
-// other cell only gets its max3 status (pr76_three_phase.hpp:336-358).
+constexpr int kMax3Block = 64;  // two cells (warps) per block
+
+// Max-3-phase continuation: one warp per cell over the whole batch; a cell
+// whose two-phase status is phase_set_unstable runs fp64::max3_cell on all 32
+// lanes (each lane with its own copy of the same state, so the lanes agree at
+// every step; the attempts' line searches spread their trials over the
+// lanes), every other cell only gets its max3 status
+// (pr76_three_phase.hpp:336-358).  Lane 0 writes the outputs.
 template <int NM>
-__global__ void __launch_bounds__(64) max3_kernel(const Mixture* __restrict__ mix_g, int64_t ncell,
-                                                  const double* __restrict__ p, const double* __restrict__ t,
-                                                  const double* __restrict__ z, DeviceOutputs out,
-                                                  Max3Outputs out3, Hints hints) {
+__global__ void __launch_bounds__(kMax3Block) max3_kernel(const Mixture* __restrict__ mix_g, int64_t ncell,
+                                                          const double* __restrict__ p, const double* __restrict__ t,
+                                                          const double* __restrict__ z, DeviceOutputs out,
+                                                          Max3Outputs out3, Hints hints) {
     __shared__ Mixture m;
     stage_mixture(mix_g, m);
     using namespace fp64;
     const int n = m.n;
     const double nan = __longlong_as_double(0x7ff8000000000000LL);
-    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    for (int64_t cell = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; cell < ncell; cell += stride) {
+    const bool writer = (threadIdx.x & 31u) == 0;
+    const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x / 32);
+    for (int64_t cell = static_cast<int64_t>(blockIdx.x) * (blockDim.x / 32) + threadIdx.x / 32; cell < ncell;
+         cell += warps) {
         auto put = [&](double* a, int k, double v) {
-            if (a) a[static_cast<int64_t>(k) * ncell + cell] = v;
+            if (a && writer) a[static_cast<int64_t>(k) * ncell + cell] = v;
         };
         for (int q = 0; q < 3; ++q) {
             put(out3.fraction, q, nan);
@@ -35,6 +42,8 @@ __global__ void __launch_bounds__(64) max3_kernel(const Mixture* __restrict__ mi
             }
         }
         const int status = out.status[cell];
+        __syncwarp();  // every lane has read the cell's status before lane 0 may rewrite it
+                       // (the status is the same on all lanes: the branch below is uniform)
         int m3 = status == kSinglePhase ? kM3Single
                  : status == kTwoPhase  ? kM3Two
                  : status == kInvalid   ? -1
@@ -59,10 +68,11 @@ __global__ void __launch_bounds__(64) max3_kernel(const Mixture* __restrict__ mi
             load_hints<NM>(hints, feed, n, ncell, cell, hs);
             if (temp_setup(m, c))
                 r = max3_cell(m, c, feed, lnk, s, hs.fcount > 0 ? hs.fptr : nullptr, hs.fcount,
-                              hs.has_three ? hs.three : nullptr, hs.options);
+                              hs.has_three ? hs.three : nullptr, hs.options, true);
             else
                 r.status = -1;
             m3 = r.status;
+            __syncwarp();  // every lane has read the cell's ln K before lane 0 may rewrite it
             // publication, pt_phase_set.hpp:91-150
             int published = kIndeterminate;
             bool clear_pair = true;
@@ -97,7 +107,7 @@ __global__ void __launch_bounds__(64) max3_kernel(const Mixture* __restrict__ mi
             } else if (m3 < 0) {
                 published = kInvalid;
             }
-            out.status[cell] = published;
+            if (writer) out.status[cell] = published;
             if (clear_pair) {
                 put(out.beta, 0, nan);
                 for (int i = 0; i < n; ++i) {
@@ -111,7 +121,7 @@ __global__ void __launch_bounds__(64) max3_kernel(const Mixture* __restrict__ mi
                 put(out.z_v, 0, nan);
             }
         }
-        if (out3.max3_status) out3.max3_status[cell] = m3;
+        if (out3.max3_status && writer) out3.max3_status[cell] = m3;
     }
 }
 
@@ -129,12 +139,12 @@ cudaError_t MPMC_CAT(launch_max3_nm, MPMC_NM)(const Mixture* d_mix, int64_t ncel
     int device = 0, sms = 0;
     cudaGetDevice(&device);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    const int block = 64;
-    int64_t grid = static_cast<int64_t>(sms) * 2;
-    const int64_t needed = (ncell + block - 1) / block;
+    // one warp per cell, up to four blocks per SM at once
+    int64_t grid = static_cast<int64_t>(sms) * 4;
+    const int64_t needed = (ncell + kMax3Block / 32 - 1) / (kMax3Block / 32);
     if (grid > needed) grid = needed;
-    max3_kernel<MPMC_NM><<<static_cast<unsigned>(grid), block, 0, stream>>>(d_mix, ncell, p, t, z, out, out3,
-                                                                             hints);
+    max3_kernel<MPMC_NM><<<static_cast<unsigned>(grid), kMax3Block, 0, stream>>>(d_mix, ncell, p, t, z, out,
+                                                                                  out3, hints);
     return cudaGetLastError();
 }
 

@@ -1,5 +1,5 @@
 // Max-3-phase continuation of a phase_set_unstable two-phase answer, in FP64,
-// one cell per thread (the reference's PR76 backend path for such cells).
+// one cell per warp (the reference's PR76 backend path for such cells).
 //
 //   orchestration        modules/flash/include/mpmc/flash/pr76_three_phase.hpp:328-561
 //                        (backend defaults, pr76_pt_flash_backend.hpp:190-206:
@@ -15,7 +15,9 @@
 // review is re-run to recover its negative witnesses, and each witness seeds
 // three-phase attempts in the reference's order.  Cells reach this path
 // rarely (none of the 1M cells of the default bench workload), so the code
-// favours a direct restatement over speed.
+// is a direct restatement; its one concession to latency is the warp form of
+// the attempts' line search (iterate_three), whose answers are the
+// sequential ones.
 #pragma once
 
 #include "pr76_fp64.cuh"
@@ -30,6 +32,10 @@ enum ThreeStatus : int {
     kTPhaseDisappearance, kTIndistinguishable, kTPropertyFailure, kTIterationLimit, kTEvaluationLimit,
     kTLineSearchFailed
 };
+
+// An attempt's evaluation budget (pt_three_phase.hpp:459-565): at most 30000
+// phase property evaluations, checked before each one.
+constexpr int kThreeEvals = 30000;
 
 template <int NM>
 struct ThreeState {  // pt_three_phase.hpp:68-84
@@ -187,7 +193,7 @@ __device__ MPMC_FP64_CALL int three_state(const Mixture& m, Cell<NM>& c, const d
     const int b = solve_rr3(c, lk1, lk2, seed, st, scratch);
     if (b != kTConverged) return b;
     for (int k = 0; k < 3; ++k) {
-        if (evals >= 30000) return kTEvaluationLimit;
+        if (evals >= kThreeEvals) return kTEvaluationLimit;
         ++evals;
         int branch;
         if (role_provider(m, c, st.x[k], upper[k], st.lnphi[k], st.zf[k], branch) != kOk) return kTPropertyFailure;
@@ -243,11 +249,84 @@ struct ThreeScratch {
     double lk1[NM], lk2[NM], nk1[NM], nk2[NM], rr[3][NM];
 };
 
+// Backtracking trial `bt` of the line search (alpha = 0.5^bt, exact) into
+// s.next with its own evaluation count `used` (0-3; the shared budget is
+// applied by line_walk).  Returns the state's status and sets `ok` when the
+// trial passes the progress and Gibbs tests (pt_three_phase.hpp:600-650).
+template <int NM>
+__device__ __forceinline__ int line_trial(const Mixture& m, Cell<NM>& c, const bool upper[3], ThreeScratch<NM>& s,
+                                          double scale, int bt, int& used, bool& ok) {
+    const int n = c.n;
+    const ThreeState<NM>& pt = s.point;
+    const double alpha = ldexp(1.0, -bt);
+    for (int i = 0; i < n; ++i) {
+        s.nk1[i] = pt.lk1[i] + (alpha / scale) * pt.r1[i];
+        s.nk2[i] = pt.lk2[i] + (alpha / scale) * pt.r2[i];
+    }
+    const double seed[2] = {pt.fraction[1], pt.fraction[2]};
+    used = 0;
+    ok = false;
+    const int st = three_state(m, c, s.nk1, s.nk2, seed, upper, s.next, s.rr, used);
+    if (st != kTConverged) return st;  // rejected evaluation
+    const double required = 1e-4 * (alpha / scale) * pt.cp_norm;
+    const bool progress = s.next.cp_norm <= 1e-11 || pt.cp_norm - s.next.cp_norm > required;
+    const bool gibbs_ok = s.next.gibbs <= pt.gibbs + pt.guard + s.next.guard;
+    ok = progress && gibbs_ok;
+    return st;
+}
+
+enum LineWalk : int { kWalkNext = 0, kWalkAccept, kWalkLimit };
+
+// The in-order line search's bookkeeping for one trial that used `used`
+// evaluations: the reference checks the budget before each evaluation, so the
+// trial runs out of it when its last evaluation would start at the limit.
+__device__ __forceinline__ int line_walk(int& evals, int used, int st, bool ok) {
+    if (used > 0 && evals + used - 1 >= kThreeEvals) return kWalkLimit;
+    evals += used;
+    return st == kTConverged && ok ? kWalkAccept : kWalkNext;
+}
+
+#ifdef __CUDA_ARCH__
+// Every lane of the warp takes lane `src`'s state (the fields copy_three copies).
+template <int NM>
+__device__ __forceinline__ void shfl_three(ThreeState<NM>& d, const ThreeState<NM>& s, int n, int src) {
+    constexpr unsigned kAll = 0xffffffffu;
+    for (int k = 0; k < 3; ++k) {
+        d.fraction[k] = __shfl_sync(kAll, s.fraction[k], src);
+        d.zf[k] = __shfl_sync(kAll, s.zf[k], src);
+        for (int i = 0; i < n; ++i) {
+            d.x[k][i] = __shfl_sync(kAll, s.x[k][i], src);
+            d.lnphi[k][i] = __shfl_sync(kAll, s.lnphi[k][i], src);
+        }
+    }
+    for (int i = 0; i < n; ++i) {
+        d.lk1[i] = __shfl_sync(kAll, s.lk1[i], src);
+        d.lk2[i] = __shfl_sync(kAll, s.lk2[i], src);
+        d.r1[i] = __shfl_sync(kAll, s.r1[i], src);
+        d.r2[i] = __shfl_sync(kAll, s.r2[i], src);
+        d.common[i] = __shfl_sync(kAll, s.common[i], src);
+    }
+    d.cp_norm = __shfl_sync(kAll, s.cp_norm, src);
+    d.gibbs = __shfl_sync(kAll, s.gibbs, src);
+    d.guard = __shfl_sync(kAll, s.guard, src);
+    d.rr_residual = __shfl_sync(kAll, s.rr_residual, src);
+    d.mass_abs = __shfl_sync(kAll, s.mass_abs, src);
+    d.mass_rel = __shfl_sync(kAll, s.mass_rel, src);
+}
+#endif
+
 // iterate_pt_three_phase, :399-676, on the cell's current (normalised) feed.
 // `point` holds the last state; `disappearing` the phase that left.
+//
+// warp = true (device only): the 32 lanes of the warp run the same cell with
+// the same state, and the line search's 32 backtracking trials run at once,
+// trial bt on lane bt.  The in-order walk over their outcomes then picks the
+// trial (and spends the evaluations) the reference's sequential loop would,
+// and every lane takes that trial's state.  The answer is the sequential one;
+// an iteration that backtracks k times costs one trial's latency, not k.
 template <int NM>
 __device__ MPMC_FP64_CALL int iterate_three(const Mixture& m, Cell<NM>& c, const double frac0[2], const bool upper[3],
-                             ThreeScratch<NM>& s, int& disappearing) {
+                             ThreeScratch<NM>& s, int& disappearing, bool warp = false) {
     const int n = c.n;
     int evals = 0;
     {
@@ -271,27 +350,38 @@ __device__ MPMC_FP64_CALL int iterate_three(const Mixture& m, Cell<NM>& c, const
         }
         if (iterations >= 512) return kTIterationLimit;
         const double scale = fmax(1.0, pt.cp_norm / 2.0);
-        bool accepted = false;
-        double alpha = 1.0;
-        for (int bt = 0; bt < 32; ++bt, alpha *= 0.5) {
-            for (int i = 0; i < n; ++i) {
-                s.nk1[i] = pt.lk1[i] + (alpha / scale) * pt.r1[i];
-                s.nk2[i] = pt.lk2[i] + (alpha / scale) * pt.r2[i];
+        int walk = kWalkNext;
+#ifdef __CUDA_ARCH__
+        // The lanes agree at every step, so they normally arrive here converged.
+        // When the 32 are not all converged here, each lane searches in order on
+        // its own below (the same answer, with no exchange between lanes).
+        constexpr unsigned kAll = 0xffffffffu;
+        if (warp && __activemask() == kAll) {
+            int used;
+            bool ok;
+            const int st = line_trial(m, c, upper, s, scale, static_cast<int>(threadIdx.x & 31u), used, ok);
+            int winner = 0;
+            for (int bt = 0; bt < 32 && walk == kWalkNext; ++bt) {
+                walk = line_walk(evals, __shfl_sync(kAll, used, bt), __shfl_sync(kAll, st, bt),
+                                 __shfl_sync(kAll, static_cast<int>(ok), bt) != 0);
+                winner = bt;
             }
-            const double seed[2] = {pt.fraction[1], pt.fraction[2]};
-            const int st = three_state(m, c, s.nk1, s.nk2, seed, upper, s.next, s.rr, evals);
-            if (st == kTEvaluationLimit) return st;
-            if (st != kTConverged) continue;  // rejected evaluation
-            const double required = 1e-4 * (alpha / scale) * pt.cp_norm;
-            const bool progress = s.next.cp_norm <= 1e-11 || pt.cp_norm - s.next.cp_norm > required;
-            const bool gibbs_ok = s.next.gibbs <= pt.gibbs + pt.guard + s.next.guard;
-            if (progress && gibbs_ok) {
-                copy_three(s.point, s.next, n);
-                accepted = true;
-                break;
-            }
+            if (walk == kWalkLimit) return kTEvaluationLimit;
+            if (walk != kWalkAccept) return kTLineSearchFailed;
+            shfl_three(s.point, s.next, n, winner);
+            ++iterations;
+            continue;
         }
-        if (!accepted) return kTLineSearchFailed;
+#endif
+        for (int bt = 0; bt < 32 && walk == kWalkNext; ++bt) {
+            int used;
+            bool ok;
+            const int st = line_trial(m, c, upper, s, scale, bt, used, ok);
+            walk = line_walk(evals, used, st, ok);
+        }
+        if (walk == kWalkLimit) return kTEvaluationLimit;
+        if (walk != kWalkAccept) return kTLineSearchFailed;
+        copy_three(s.point, s.next, n);
         ++iterations;
     }
 }
@@ -403,11 +493,14 @@ __device__ MPMC_FP64_CALL int three_review(const Mixture& m, Cell<NM>& c, Max3Sc
 // is a three-phase start whose attempts run first, one per combination of
 // root sides (:457-486), with their own quota of 16.  `opt` are the caller's
 // two-phase options, which the fresh two-phase neighbour of a phase
-// disappearance runs with (:413-415).
+// disappearance runs with (:413-415).  `warp`: the whole warp runs this cell
+// (every lane with its own copy of the same state), and the attempts' line
+// searches run their backtracking trials on the lanes (iterate_three).
 template <int NM>
 __device__ Max3Result max3_cell(const Mixture& m, Cell<NM>& c, const double* feed, const double* lnk,
                                 Max3Scratch<NM>& s, const double* const* hints = nullptr, int n_hints = 0,
-                                const double* three_hint = nullptr, const SolveOptions& opt = SolveOptions{}) {
+                                const double* three_hint = nullptr, const SolveOptions& opt = SolveOptions{},
+                                bool warp = false) {
     const int n = c.n;
     Max3Result r{kM3Indeterminate, false, false};
     c.newton = false;  // the reference's bisection roots and RR
@@ -453,7 +546,7 @@ __device__ Max3Result max3_cell(const Mixture& m, Cell<NM>& c, const double* fee
             return true;
         }
         int disappearing = -1;
-        const int st = iterate_three(m, c, fr, upper, s.t, disappearing);
+        const int st = iterate_three(m, c, fr, upper, s.t, disappearing, warp);
         if (st == kTPhaseDisappearance) {
             saw_boundary = true;
             const double* starts[2];
