@@ -246,7 +246,8 @@ int mpmc_gpu_flash_solve_device_warm(mpmc_gpu_flash* handle, int64_t n_cells, co
  * Cells that are not phase_set_unstable keep their two-phase answer, and
  * out3->max3_status records every cell's outcome.  out->status and
  * out->ln_k are required.  The continuation runs in FP64 with the
- * reference's arithmetic, one cell per thread, for every form.  These calls
+ * reference's arithmetic, one cell per warp (the line-search trials of its
+ * three-phase attempts on the lanes), for every form.  These calls
  * do not use CUDA graphs, and the sensitivities of a handle created with
  * want_sensitivity are taken after the continuation. */
 int mpmc_gpu_flash_solve_max3(mpmc_gpu_flash* handle, int64_t n_cells, const double* p, const double* t,
