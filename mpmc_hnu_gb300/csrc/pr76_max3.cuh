@@ -286,7 +286,14 @@ __device__ __forceinline__ int line_walk(int& evals, int used, int st, bool ok) 
     return st == kTConverged && ok ? kWalkAccept : kWalkNext;
 }
 
-#ifdef __CUDA_ARCH__
+// The warp form of the line search builds for the device, and for the host
+// under a warp emulation that provides __shfl_sync, __activemask and a
+// per-lane threadIdx (a test build that runs the 32 lanes as threads).
+#if defined(__CUDA_ARCH__) || defined(MPMC_WARP_EMULATION)
+#define MPMC_MAX3_WARP 1
+#endif
+
+#ifdef MPMC_MAX3_WARP
 // Every lane of the warp takes lane `src`'s state (the fields copy_three copies).
 template <int NM>
 __device__ __forceinline__ void shfl_three(ThreeState<NM>& d, const ThreeState<NM>& s, int n, int src) {
@@ -351,7 +358,7 @@ __device__ MPMC_FP64_CALL int iterate_three(const Mixture& m, Cell<NM>& c, const
         if (iterations >= 512) return kTIterationLimit;
         const double scale = fmax(1.0, pt.cp_norm / 2.0);
         int walk = kWalkNext;
-#ifdef __CUDA_ARCH__
+#ifdef MPMC_MAX3_WARP
         // The lanes agree at every step, so they normally arrive here converged.
         // When the 32 are not all converged here, each lane searches in order on
         // its own below (the same answer, with no exchange between lanes).

@@ -9,19 +9,30 @@
 // the continuation with the same hints and the three-phase start, and the
 // publication of pt_phase_set.hpp:91-150.  The tests check it against the
 // reference's recorded max3 statuses and hint-seeded continuation.
+//
+// Built with -DMPMC_WARP_EMULATION, the continuation runs as the max3 kernel
+// runs it: on the 32 lanes of an emulated warp (warp_emu.h), each lane with
+// its own copy of the cell, the line-search trials spread over the lanes.
+// Every lane must end with the same answer, and a cell whose lanes diverge or
+// disagree gets max3 status -99.
 #include <cuda_runtime.h>
 
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 
 using std::isfinite;
+#ifdef MPMC_WARP_EMULATION
+#include "warp_emu.h"
+#else
 struct HostDim3 {
     unsigned x, y, z;
 };
 static HostDim3 threadIdx{0, 0, 0}, blockDim{1, 1, 1};
 static inline void __syncthreads() {}
+#endif
 
 #include "launch.h"
 #include "pr76_hints.cuh"
@@ -49,6 +60,60 @@ struct Outputs {
     double* x3;          // [3 * n * ncell] the three-phase set
     double* f3;          // [3 * ncell]
 };
+
+#ifdef MPMC_WARP_EMULATION
+// The max3 kernel's per-cell work on an emulated warp: every lane runs
+// max3_cell in warp mode on its own copy of the cell.  True when the lanes
+// stayed together and agree bit for bit on everything the kernel publishes;
+// lane 0's scratch and result are then returned in s and r.
+template <int NM>
+bool max3_on_warp(const pr76::Mixture& m, const pr76::fp64::Cell<NM>& c0, const double* feed, const double* lnk,
+                  const pr76::fp64::CellHints<NM>& hs, const double* const* fin, pr76::fp64::Max3Scratch<NM>& s,
+                  pr76::fp64::Max3Result& r) {
+    using namespace pr76::fp64;
+    const int n = c0.n;
+    std::unique_ptr<Max3Scratch<NM>[]> lane_s(new Max3Scratch<NM>[warp_emu::kLanes]());
+    Max3Result lane_r[warp_emu::kLanes];
+    const bool together = warp_emu::run([&](int lane) {
+        Cell<NM> c = c0;
+        Max3Result res{kM3Indeterminate, false, false};
+        if (temp_setup(m, c))
+            res = max3_cell(m, c, feed, lnk, lane_s[lane], fin, hs.fcount, hs.has_three ? hs.three : nullptr,
+                            hs.options, true);
+        else
+            res.status = -1;
+        lane_r[lane] = res;
+    });
+    if (!together) {
+        std::fprintf(stderr, "warp emulation: the lanes diverged\n");
+        return false;
+    }
+    auto same = [](double a, double b) { return std::memcmp(&a, &b, sizeof(double)) == 0; };
+    for (int lane = 1; lane < warp_emu::kLanes; ++lane) {
+        const Max3Result& a = lane_r[0];
+        const Max3Result& b = lane_r[lane];
+        bool agree = a.status == b.status && a.has_pair == b.has_pair && a.has_three == b.has_three;
+        const ThreeState<NM>& p0 = lane_s[0].t.point;
+        const ThreeState<NM>& p1 = lane_s[lane].t.point;
+        const SplitState<NM>& w0 = lane_s[0].w.best;
+        const SplitState<NM>& w1 = lane_s[lane].w.best;
+        for (int q = 0; q < 3 && agree; ++q) {
+            agree = same(p0.fraction[q], p1.fraction[q]) && same(p0.zf[q], p1.zf[q]);
+            for (int i = 0; i < n && agree; ++i)
+                agree = same(p0.x[q][i], p1.x[q][i]) && same(p0.lnphi[q][i], p1.lnphi[q][i]);
+        }
+        if (agree && a.has_pair)
+            for (int i = 0; i < n && agree; ++i) agree = same(w0.x[i], w1.x[i]) && same(w0.y[i], w1.y[i]);
+        if (!agree) {
+            std::fprintf(stderr, "warp emulation: lane %d disagrees with lane 0\n", lane);
+            return false;
+        }
+    }
+    s = lane_s[0];
+    r = lane_r[0];
+    return true;
+}
+#endif
 
 template <int NM>
 void run(const pr76::Mixture& m, int64_t ncell, const double* p, const double* t, const double* z,
@@ -101,11 +166,15 @@ void run(const pr76::Mixture& m, int64_t ncell, const double* p, const double* t
             c2.t = t[cell];
             for (int k = 0; k < cCount; ++k) c2.counters[k] = 0;
             Max3Result mr{kM3Indeterminate, false, false};
+#ifdef MPMC_WARP_EMULATION
+            if (!max3_on_warp(m, c2, feed, lnk, hs, fin, *s, mr)) mr.status = -99;
+#else
             if (temp_setup(m, c2))
                 mr = max3_cell(m, c2, feed, lnk, *s, fin, hs.fcount, hs.has_three ? hs.three : nullptr,
                                hs.options);
             else
                 mr.status = -1;
+#endif
             m3 = mr.status;
             published = kIndeterminate;
             bool clear = true;
