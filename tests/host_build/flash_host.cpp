@@ -74,7 +74,7 @@ bool max3_on_warp(const pr76::Mixture& m, const pr76::fp64::Cell<NM>& c0, const 
     const int n = c0.n;
     std::unique_ptr<Max3Scratch<NM>[]> lane_s(new Max3Scratch<NM>[warp_emu::kLanes]());
     Max3Result lane_r[warp_emu::kLanes];
-    const bool together = warp_emu::run([&](int lane) {
+    const bool together = warp_emu::run(warp_emu::kLanes, [&](int lane) {
         Cell<NM> c = c0;
         Max3Result res{kM3Indeterminate, false, false};
         if (temp_setup(m, c))
