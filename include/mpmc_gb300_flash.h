@@ -120,6 +120,12 @@ typedef struct mpmc_pr76_mixture {
 /* Option flags (mpmc_flash_options.flags). */
 #define MPMC_FLAG_STAGE_TIMING 1 /* record CUDA events around every device stage */
 #define MPMC_FLAG_CUDA_GRAPH 2   /* replay solves as CUDA graphs (see mpmc_gpu_flash_solve_device) */
+/* Take the sensitivities with the lane-group kernel (component i of a cell on
+ * lane i of a group of lanes; rows of the Jacobians and of dF/d ln K in the
+ * group's shared memory) instead of one thread per cell.  Same outputs and
+ * statuses, to rounding.  Opt-in: checked on the CPU under a warp emulation,
+ * not yet timed on a GPU. */
+#define MPMC_FLAG_SENSITIVITY_LANES 4
 
 typedef struct mpmc_flash_options {
     int32_t form;              /* MPMC_FORM_* */

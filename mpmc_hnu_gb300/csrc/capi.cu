@@ -106,6 +106,7 @@ struct mpmc_gpu_flash {
     cudaEvent_t chunk_done[1] = {};
     int32_t shape[10] = {};  // explicit launch shape (mpmc_gpu_flash_set_launch_shape), 0 = default
     bool use_graphs = false;
+    bool sens_lanes = false;  // the lane-group sensitivity kernel (MPMC_FLAG_SENSITIVITY_LANES)
     std::vector<GraphEntry> graphs;
     uint64_t graph_clock = 0;
 };
@@ -387,7 +388,7 @@ cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, co
         if (e != cudaSuccess) return e;
     }
     if (h->want_sensitivity && sensitivity) {
-        e = pr76::launch_sensitivity(h->n, h->d_mixture, ncell, p, t, z, d, stream);
+        e = pr76::launch_sensitivity(h->n, h->d_mixture, ncell, p, t, z, d, stream, 0, -1, h->sens_lanes);
         if (e != cudaSuccess) return e;
     }
     record();  // end of the sensitivity stage (zero length without sensitivities)
@@ -548,7 +549,15 @@ cudaError_t launch_batched(int n, const Mixture* d_mix, int64_t ncell, const dou
 
 cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
                                const double* z, const DeviceOutputs& out, cudaStream_t stream, int64_t c0,
-                               int64_t c1) {
+                               int64_t c1, bool lanes) {
+    if (lanes) switch (capacity_for(n)) {
+        case 4: return launch_sensitivity_lanes_nm4(d_mix, ncell, p, t, z, out, stream, c0, c1);
+        case 8: return launch_sensitivity_lanes_nm8(d_mix, ncell, p, t, z, out, stream, c0, c1);
+        case 12: return launch_sensitivity_lanes_nm12(d_mix, ncell, p, t, z, out, stream, c0, c1);
+        case 16: return launch_sensitivity_lanes_nm16(d_mix, ncell, p, t, z, out, stream, c0, c1);
+        case 20: return launch_sensitivity_lanes_nm20(d_mix, ncell, p, t, z, out, stream, c0, c1);
+        default: return cudaErrorInvalidValue;
+        }
     switch (capacity_for(n)) {
     case 4: return launch_sensitivity_nm4(d_mix, ncell, p, t, z, out, stream, c0, c1);
     case 8: return launch_sensitivity_nm8(d_mix, ncell, p, t, z, out, stream, c0, c1);
@@ -768,6 +777,7 @@ int mpmc_gpu_flash_create(const mpmc_pr76_mixture* mixture, const mpmc_flash_opt
     h->want_sensitivity = opt.want_sensitivity;
     h->stage_timing = (opt.flags & MPMC_FLAG_STAGE_TIMING) != 0;
     h->use_graphs = (opt.flags & MPMC_FLAG_CUDA_GRAPH) != 0;
+    h->sens_lanes = (opt.flags & MPMC_FLAG_SENSITIVITY_LANES) != 0;
     h->host_mixture = m;
     e = cudaMalloc(&h->d_mixture, sizeof(pr76::Mixture));
     if (e == cudaSuccess) e = cudaMemcpy(h->d_mixture, &m, sizeof(pr76::Mixture), cudaMemcpyHostToDevice);
@@ -909,7 +919,7 @@ int mpmc_gpu_flash_solve_device_noalloc(mpmc_gpu_flash* h, int64_t ncell, const 
     e = pr76::launch_batched(h->n, h->d_mixture, ncell, p, t, z, d, scratch, MPMC_NOALLOC_SCRATCH_BYTES, shape, s);
     if (e != cudaSuccess) return cuda_fail(e, "flash kernel launch");
     if (h->want_sensitivity) {
-        e = pr76::launch_sensitivity(h->n, h->d_mixture, ncell, p, t, z, d, s);
+        e = pr76::launch_sensitivity(h->n, h->d_mixture, ncell, p, t, z, d, s, 0, -1, h->sens_lanes);
         if (e != cudaSuccess) return cuda_fail(e, "sensitivity kernel launch");
     }
     return MPMC_OK;
@@ -1188,7 +1198,7 @@ int solve_host(mpmc_gpu_flash* h, int64_t ncell, const double* p, const double* 
         // the sensitivities in one launch, then every derivative field in one
         // contiguous copy: measured on a GB300 (1M cells, N = 10), 80 ms less
         // per call than eight cell ranges each copied as 2D row segments
-        e = pr76::launch_sensitivity(h->n, h->d_mixture, ncell, dp_, dt_, dz_, d, s);
+        e = pr76::launch_sensitivity(h->n, h->d_mixture, ncell, dp_, dt_, dz_, d, s, 0, -1, h->sens_lanes);
         if (e != cudaSuccess) return cuda_fail(e, "sensitivity kernel launch");
         if ((e = cudaEventRecord(h->chunk_done[0], s)) != cudaSuccess ||
             (e = cudaStreamWaitEvent(cs, h->chunk_done[0], 0)) != cudaSuccess)

@@ -173,9 +173,10 @@ cudaError_t launch_plain(int n, const Mixture* d_mix, int64_t ncell, const doubl
 // Implicit sensitivity of accepted two-phase cells (sensitivity.cu) among the
 // cells [c0, c1) of the batch (c1 < 0: to the end); reads the flash fields of
 // `out` (status, beta, x, y, lnk, z_l, z_v), which must be set.
+// lanes: the lane-group form (pr76_sensw.cuh) instead of one thread per cell.
 cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
                                const double* z, const DeviceOutputs& out, cudaStream_t stream, int64_t c0 = 0,
-                               int64_t c1 = -1);
+                               int64_t c1 = -1, bool lanes = false);
 
 #define MPMC_DECLARE_PLAIN(NM)                                                                         \
     cudaError_t launch_plain_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t, \
@@ -184,6 +185,9 @@ cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const
     cudaError_t launch_sensitivity_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t, \
                                           const double* z, const DeviceOutputs& out, cudaStream_t stream,      \
                                           int64_t c0, int64_t c1);                                             \
+    cudaError_t launch_sensitivity_lanes_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p,          \
+                                                const double* t, const double* z, const DeviceOutputs& out,      \
+                                                cudaStream_t stream, int64_t c0, int64_t c1);                    \
     cudaError_t launch_max3_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t,      \
                                    const double* z, const DeviceOutputs& out, const Max3Outputs& out3,           \
                                    cudaStream_t stream, const Hints& hints);                                      \

@@ -3,6 +3,7 @@
 // component capacity (-DMPMC_NM).
 #include "launch.h"
 #include "pr76_ad.cuh"
+#include "pr76_sensw.cuh"
 
 #ifndef MPMC_NM
 #error "compile with -DMPMC_NM=<capacity>"
@@ -90,6 +91,63 @@ __global__ void __launch_bounds__(64) sensitivity_kernel(const Mixture* __restri
     }
 }
 
+// The lane-group form (pr76_sensw.cuh): one group of S lanes per cell, cells
+// [c0, c1) in a grid-stride loop over the groups; cells without an accepted
+// pair are NaN-filled by the group's lanes together.
+constexpr int kSensLanesBlock = 64;
+
+template <int NM>
+__device__ void nan_fill_group(int n, int64_t ncell, int64_t cell, const DeviceOutputs& out, int lane, int lanes) {
+    const double nan = __longlong_as_double(0x7ff8000000000000LL);
+    const int q = n + 1;
+    auto put = [&](double* a, int k) {
+        if (a) a[static_cast<int64_t>(k) * ncell + cell] = nan;
+    };
+    for (int k = lane; k < n * q; k += lanes) {
+        put(out.dlnk, k);
+        put(out.dx, k);
+        put(out.dy, k);
+    }
+    for (int k = lane; k < q; k += lanes) {
+        put(out.dbeta, k);
+        put(out.dzl, k);
+        put(out.dzv, k);
+        put(out.drhol, k);
+        put(out.drhov, k);
+    }
+    for (int k = lane; k < (n + 1) * (n + 2); k += lanes) {
+        put(out.jl, k);
+        put(out.jv, k);
+    }
+}
+
+template <int NM>
+__global__ void __launch_bounds__(kSensLanesBlock) sensitivity_lanes_kernel(const Mixture* __restrict__ mix_g,
+                                                                            int64_t ncell, int64_t c0, int64_t c1,
+                                                                            const double* __restrict__ p,
+                                                                            const double* __restrict__ t,
+                                                                            const double* __restrict__ z,
+                                                                            DeviceOutputs out) {
+    constexpr int S = w64::kSeg<NM>;
+    constexpr int kGroups = kSensLanesBlock / S;
+    __shared__ Mixture m;
+    __shared__ sensw::GroupScratch<NM> scratch[kGroups];
+    stage_mixture(mix_g, m);
+    const int group = threadIdx.x / S;
+    const int lane = w64::seg_lane<S>();
+    sensw::GroupScratch<NM>& sh = scratch[group];
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * kGroups;
+    for (int64_t cell = c0 + static_cast<int64_t>(blockIdx.x) * kGroups + group; cell < c1; cell += stride) {
+        int st = ad::sNotAccepted;
+        if (out.status[cell] == kTwoPhase) st = sensw::cell<NM, S>(m, sh, ncell, cell, p, t, z, out);
+        // the group's partial writes of a failed cell come before its NaN fill
+        sensw::group_sync<S>();
+        if (st != ad::sSuccess) nan_fill_group<NM>(m.n, ncell, cell, out, lane, S);
+        if (out.sens_status && lane == 0) out.sens_status[cell] = st;
+        sensw::group_sync<S>();  // the scratch is free for the next cell
+    }
+}
+
 #define MPMC_CAT2(a, b) a##b
 #define MPMC_CAT(a, b) MPMC_CAT2(a, b)
 
@@ -107,6 +165,24 @@ cudaError_t MPMC_CAT(launch_sensitivity_nm, MPMC_NM)(const Mixture* d_mix, int64
     if (grid > needed) grid = needed;
     sensitivity_kernel<MPMC_NM><<<static_cast<unsigned>(grid), block, 0, stream>>>(d_mix, ncell, c0, c1, p, t, z,
                                                                                    out);
+    return cudaGetLastError();
+}
+
+cudaError_t MPMC_CAT(launch_sensitivity_lanes_nm, MPMC_NM)(const Mixture* d_mix, int64_t ncell, const double* p,
+                                                             const double* t, const double* z,
+                                                             const DeviceOutputs& out, cudaStream_t stream,
+                                                             int64_t c0, int64_t c1) {
+    if (c1 < 0) c1 = ncell;
+    if (c1 <= c0) return cudaSuccess;
+    int device = 0, sms = 0;
+    cudaGetDevice(&device);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    constexpr int groups = kSensLanesBlock / w64::kSeg<MPMC_NM>;
+    int64_t grid = static_cast<int64_t>(sms) * 8;
+    const int64_t needed = (c1 - c0 + groups - 1) / groups;
+    if (grid > needed) grid = needed;
+    sensitivity_lanes_kernel<MPMC_NM><<<static_cast<unsigned>(grid), kSensLanesBlock, 0, stream>>>(
+        d_mix, ncell, c0, c1, p, t, z, out);
     return cudaGetLastError();
 }
 
