@@ -874,6 +874,8 @@ def main() -> None:
     ap.add_argument("--cells", type=int, default=1 << 20)
     ap.add_argument("--near-fraction", type=float, default=0.3)
     ap.add_argument("--no-ad", action="store_true")
+    ap.add_argument("--sensitivity-lanes", action="store_true",
+                    help="take the sensitivities with the opt-in lane-group kernel (MPMC_FLAG_SENSITIVITY_LANES)")
     ap.add_argument("--plain-sample", type=int, default=65536)
     ap.add_argument("--batched-sample", type=int, default=131072)
     ap.add_argument("--warm-fraction", type=float, default=0.75,
@@ -911,6 +913,8 @@ def main() -> None:
                             f"{int(args.near_fraction * 100)}% within 2% of the phase-boundary pressure",
                 "cells_per_gpu": args.cells, "components": args.n, "sensitivity": sens,
                 "l2_flush": "inputs+outputs larger than L2", "parallelism": f"replicas{world}"}
+    if args.sensitivity_lanes:
+        workload["sensitivity_kernel"] = "lane groups (MPMC_FLAG_SENSITIVITY_LANES)"
 
     if args.impl == "reference":
         # the reference's CPU flash (C++ restatement; the reference sources are
@@ -965,7 +969,8 @@ def main() -> None:
     n, ncell = args.n, args.cells
     # the timed handle replays its launch sequence as a CUDA graph (same cells
     # and buffers every step)
-    g = flash.GpuFlash(mix, args.form, sensitivity=sens, device=device, graphs=True)
+    lanes = bool(args.sensitivity_lanes)
+    g = flash.GpuFlash(mix, args.form, sensitivity=sens, device=device, graphs=True, sensitivity_lanes=lanes)
     tuning = None
     if args.form == "mixed" and args.launch_shape:
         tuning = {"shape": [int(v) for v in args.launch_shape.split(",")]}
@@ -1039,7 +1044,8 @@ def main() -> None:
     del houts, hp, ht, hz
 
     # per-stage device times and work totals (separate instrumented call) for the roofline
-    gt = flash.GpuFlash(mix, args.form, sensitivity=sens, device=device, stage_timing=True)
+    gt = flash.GpuFlash(mix, args.form, sensitivity=sens, device=device, stage_timing=True,
+                        sensitivity_lanes=lanes)
     if tuning is not None:
         gt.set_launch_shape(tuning["shape"])
     gt.solve_device(ncell, dp.data_ptr(), dt.data_ptr(), dz.data_ptr(), ptrs, stream.cuda_stream)
