@@ -39,8 +39,9 @@ class _Out(ctypes.Structure):
 
 
 _built = False
-# where the reference sources lie, if at all (this recipe reads them there;
-# MPMC_REFERENCE_ROOT overrides, as for the tests and golden-vector scripts)
+# Where the reference sources lie, if at all: MPMC_REFERENCE_ROOT, else the
+# checkout this recipe was written against.  The tests and the golden-vector
+# scripts take it from here; oracle/Makefile has the same default.
 REFERENCE_ROOT = os.environ.get("MPMC_REFERENCE_ROOT", "/root/reference")
 
 

@@ -39,7 +39,7 @@ sys.path.insert(0, ROOT)
 from mpmc_hnu_gb300 import synth  # noqa: E402
 from oracle import pyoracle  # noqa: E402
 
-REF = os.environ.get("MPMC_REFERENCE_ROOT", "/root/reference")
+REF = pyoracle.REFERENCE_ROOT
 SPLIT = os.path.join(REF, "tests", "flash", "pt_split")
 CLOSURE = os.path.join(REF, "tests", "physics", "thermodynamic_closure")
 

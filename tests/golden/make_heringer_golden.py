@@ -31,7 +31,7 @@ sys.path.insert(0, ROOT)
 from mpmc_hnu_gb300 import synth  # noqa: E402
 from oracle import pyoracle  # noqa: E402
 
-REFERENCE = os.environ.get("MPMC_REFERENCE_ROOT", "/root/reference")
+REFERENCE = pyoracle.REFERENCE_ROOT
 FIXTURE = os.path.join(REFERENCE, "tests", "flash", "pr76_three_phase", "heringer_2026_sour_gas_fixture.hpp")
 
 DUMP = r"""

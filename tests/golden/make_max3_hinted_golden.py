@@ -46,7 +46,7 @@ sys.path.insert(0, ROOT)
 from mpmc_hnu_gb300 import synth  # noqa: E402
 from oracle import pyoracle  # noqa: E402
 
-REFERENCE = os.environ.get("MPMC_REFERENCE_ROOT", "/root/reference")
+REFERENCE = pyoracle.REFERENCE_ROOT
 TEST = os.path.join(REFERENCE, "tests", "flash", "pr76_three_phase", "pr76_max3_robustness_test.cpp")
 
 DUMP = r"""

@@ -15,8 +15,10 @@ import subprocess
 
 import pytest
 
+from oracle import pyoracle
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REFERENCE = os.environ.get("MPMC_REFERENCE_ROOT", "/root/reference")
+REFERENCE = pyoracle.REFERENCE_ROOT
 MODULES = ("ad", "thermodynamics", "flash", "physics", "flow", "mesh")
 
 SOURCE = r"""

@@ -25,6 +25,7 @@ import numpy as np
 import pytest
 
 from mpmc_hnu_gb300 import continuation, synth
+from oracle import pyoracle
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
@@ -142,7 +143,7 @@ def test_device_max3_with_starts_and_options_matches_reference(host_flash, tmp_p
             assert np.allclose(outs["y"][:, 0], np.ravel(ref["y"]), rtol=0, atol=1e-12)
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(os.environ.get("MPMC_REFERENCE_ROOT", "/root/reference"),
+@pytest.mark.skipif(not os.path.isdir(os.path.join(pyoracle.REFERENCE_ROOT,
                                                    "modules", "flash", "include")),
                     reason="reference headers not present")
 def test_cpp_continuation_binding_matches_reference(tmp_path):
@@ -150,7 +151,7 @@ def test_cpp_continuation_binding_matches_reference(tmp_path):
     the device code (its three C-ABI calls provided by
     tests/host_build/continuation_binding.cpp): every recorded point's max3
     status and every path's brackets as the reference's continuation has them."""
-    ref_root = os.environ.get("MPMC_REFERENCE_ROOT", "/root/reference")
+    ref_root = pyoracle.REFERENCE_ROOT
     d = np.load(os.path.join(HERE, "golden", "continuation_reference.npz"))
     exe = str(tmp_path / "continuation_binding")
     cmd = ["g++", "-std=c++20", "-O2", "-ffp-contract=off", "-Wno-attributes", "-I/usr/local/cuda/include",
