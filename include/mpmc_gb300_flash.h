@@ -126,6 +126,13 @@ typedef struct mpmc_pr76_mixture {
  * statuses, to rounding.  Opt-in: checked on the CPU under a warp emulation,
  * not yet timed on a GPU. */
 #define MPMC_FLAG_SENSITIVITY_LANES 4
+/* The max-3-phase continuation (mpmc_gpu_flash_solve_max3, _hinted) solves
+ * the cubic and the Rachford-Rice equations by bracketed Newton with the
+ * reference's stopping width, as the flash's FP64 items do, instead of the
+ * reference's bisection: fewer FP64 instructions per phase evaluation, the
+ * same status on every recorded cell (checked on the CPU), phase sets equal
+ * to rounding.  Opt-in: not yet timed on a GPU. */
+#define MPMC_FLAG_MAX3_NEWTON_ROOTS 8
 
 typedef struct mpmc_flash_options {
     int32_t form;              /* MPMC_FORM_* */

@@ -107,6 +107,7 @@ struct mpmc_gpu_flash {
     int32_t shape[10] = {};  // explicit launch shape (mpmc_gpu_flash_set_launch_shape), 0 = default
     bool use_graphs = false;
     bool sens_lanes = false;  // the lane-group sensitivity kernel (MPMC_FLAG_SENSITIVITY_LANES)
+    bool max3_newton = false;  // Newton roots in the max-3-phase continuation (MPMC_FLAG_MAX3_NEWTON_ROOTS)
     std::vector<GraphEntry> graphs;
     uint64_t graph_clock = 0;
 };
@@ -384,7 +385,8 @@ cudaError_t enqueue_device(mpmc_gpu_flash* h, int64_t ncell, const double* p, co
     }
     if (e != cudaSuccess) return e;
     if (max3) {  // before the sensitivities: a fresh two-phase neighbor is differentiated too
-        e = pr76::launch_max3(h->n, h->d_mixture, ncell, p, t, z, d, *max3, stream, hints ? *hints : pr76::Hints{});
+        e = pr76::launch_max3(h->n, h->d_mixture, ncell, p, t, z, d, *max3, stream, hints ? *hints : pr76::Hints{},
+                              h->max3_newton);
         if (e != cudaSuccess) return e;
     }
     if (h->want_sensitivity && sensitivity) {
@@ -570,13 +572,13 @@ cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const
 
 cudaError_t launch_max3(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
                         const double* z, const DeviceOutputs& out, const Max3Outputs& out3, cudaStream_t stream,
-                        const Hints& hints) {
+                        const Hints& hints, bool newton_roots) {
     switch (capacity_for(n)) {
-    case 4: return launch_max3_nm4(d_mix, ncell, p, t, z, out, out3, stream, hints);
-    case 8: return launch_max3_nm8(d_mix, ncell, p, t, z, out, out3, stream, hints);
-    case 12: return launch_max3_nm12(d_mix, ncell, p, t, z, out, out3, stream, hints);
-    case 16: return launch_max3_nm16(d_mix, ncell, p, t, z, out, out3, stream, hints);
-    case 20: return launch_max3_nm20(d_mix, ncell, p, t, z, out, out3, stream, hints);
+    case 4: return launch_max3_nm4(d_mix, ncell, p, t, z, out, out3, stream, hints, newton_roots);
+    case 8: return launch_max3_nm8(d_mix, ncell, p, t, z, out, out3, stream, hints, newton_roots);
+    case 12: return launch_max3_nm12(d_mix, ncell, p, t, z, out, out3, stream, hints, newton_roots);
+    case 16: return launch_max3_nm16(d_mix, ncell, p, t, z, out, out3, stream, hints, newton_roots);
+    case 20: return launch_max3_nm20(d_mix, ncell, p, t, z, out, out3, stream, hints, newton_roots);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -778,6 +780,7 @@ int mpmc_gpu_flash_create(const mpmc_pr76_mixture* mixture, const mpmc_flash_opt
     h->stage_timing = (opt.flags & MPMC_FLAG_STAGE_TIMING) != 0;
     h->use_graphs = (opt.flags & MPMC_FLAG_CUDA_GRAPH) != 0;
     h->sens_lanes = (opt.flags & MPMC_FLAG_SENSITIVITY_LANES) != 0;
+    h->max3_newton = (opt.flags & MPMC_FLAG_MAX3_NEWTON_ROOTS) != 0;
     h->host_mixture = m;
     e = cudaMalloc(&h->d_mixture, sizeof(pr76::Mixture));
     if (e == cudaSuccess) e = cudaMemcpy(h->d_mixture, &m, sizeof(pr76::Mixture), cudaMemcpyHostToDevice);

@@ -20,7 +20,7 @@ template <int NM>
 __global__ void __launch_bounds__(kMax3Block) max3_kernel(const Mixture* __restrict__ mix_g, int64_t ncell,
                                                           const double* __restrict__ p, const double* __restrict__ t,
                                                           const double* __restrict__ z, DeviceOutputs out,
-                                                          Max3Outputs out3, Hints hints) {
+                                                          Max3Outputs out3, Hints hints, bool newton_roots) {
     __shared__ Mixture m;
     stage_mixture(mix_g, m);
     using namespace fp64;
@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(kMax3Block) max3_kernel(const Mixture* __restr
             load_hints<NM>(hints, feed, n, ncell, cell, hs);
             if (temp_setup(m, c))
                 r = max3_cell(m, c, feed, lnk, s, hs.fcount > 0 ? hs.fptr : nullptr, hs.fcount,
-                              hs.has_three ? hs.three : nullptr, hs.options, true);
+                              hs.has_three ? hs.three : nullptr, hs.options, true, newton_roots);
             else
                 r.status = -1;
             m3 = r.status;
@@ -133,7 +133,8 @@ __global__ void __launch_bounds__(kMax3Block) max3_kernel(const Mixture* __restr
 
 cudaError_t MPMC_CAT(launch_max3_nm, MPMC_NM)(const Mixture* d_mix, int64_t ncell, const double* p,
                                                 const double* t, const double* z, const DeviceOutputs& out,
-                                                const Max3Outputs& out3, cudaStream_t stream, const Hints& hints) {
+                                                const Max3Outputs& out3, cudaStream_t stream, const Hints& hints,
+                                                bool newton_roots) {
     if (ncell <= 0) return cudaSuccess;
     if (!out.status || !out.lnk) return cudaErrorInvalidValue;
     int device = 0, sms = 0;
@@ -144,7 +145,7 @@ cudaError_t MPMC_CAT(launch_max3_nm, MPMC_NM)(const Mixture* d_mix, int64_t ncel
     const int64_t needed = (ncell + kMax3Block / 32 - 1) / (kMax3Block / 32);
     if (grid > needed) grid = needed;
     max3_kernel<MPMC_NM><<<static_cast<unsigned>(grid), kMax3Block, 0, stream>>>(d_mix, ncell, p, t, z, out,
-                                                                                  out3, hints);
+                                                                                  out3, hints, newton_roots);
     return cudaGetLastError();
 }
 

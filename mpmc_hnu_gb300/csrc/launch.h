@@ -131,13 +131,14 @@ struct Max3Outputs {
     double* z;             // [3] compressibility factors
 };
 
-// Max-3-phase continuation (flash_plain.cu) of the cells whose flash status in
+// Max-3-phase continuation (flash_max3.cu) of the cells whose flash status in
 // `out` is phase_set_unstable; every cell gets its max3_status.  Reads and
 // rewrites the two-phase fields of `out` (status, pair) as the reference's
-// publication does.
+// publication does.  newton_roots: bracketed-Newton roots and Rachford-Rice
+// in the continuation instead of the reference's bisection.
 cudaError_t launch_max3(int n, const Mixture* d_mix, int64_t ncell, const double* p, const double* t,
                         const double* z, const DeviceOutputs& out, const Max3Outputs& out3, cudaStream_t stream,
-                        const Hints& hints = Hints{});
+                        const Hints& hints = Hints{}, bool newton_roots = false);
 
 // Closure constants of a selected-phase property chart call (pr76_chart.cuh),
 // passed to the kernel by value.
@@ -190,7 +191,7 @@ cudaError_t launch_sensitivity(int n, const Mixture* d_mix, int64_t ncell, const
                                                 cudaStream_t stream, int64_t c0, int64_t c1);                    \
     cudaError_t launch_max3_nm##NM(const Mixture* d_mix, int64_t ncell, const double* p, const double* t,      \
                                    const double* z, const DeviceOutputs& out, const Max3Outputs& out3,           \
-                                   cudaStream_t stream, const Hints& hints);                                      \
+                                   cudaStream_t stream, const Hints& hints, bool newton_roots);                   \
     cudaError_t launch_chart_nm##NM(const Mixture* d_mix, const ChartParams& params, int64_t ncell,           \
                                     const double* q, const int32_t* dep, const ChartOutputs& out,               \
                                     cudaStream_t stream);                                                        \

@@ -503,14 +503,18 @@ __device__ MPMC_FP64_CALL int three_review(const Mixture& m, Cell<NM>& c, Max3Sc
 // disappearance runs with (:413-415).  `warp`: the whole warp runs this cell
 // (every lane with its own copy of the same state), and the attempts' line
 // searches run their backtracking trials on the lanes (iterate_three).
+// `newton_roots`: the cubic and the Rachford-Rice equation by bracketed Newton
+// with the reference's stopping width, as the flash's FP64 items solve them,
+// instead of the reference's bisection (fewer FP64 instructions per phase
+// evaluation; the statuses of every recorded cell are unchanged).
 template <int NM>
 __device__ Max3Result max3_cell(const Mixture& m, Cell<NM>& c, const double* feed, const double* lnk,
                                 Max3Scratch<NM>& s, const double* const* hints = nullptr, int n_hints = 0,
                                 const double* three_hint = nullptr, const SolveOptions& opt = SolveOptions{},
-                                bool warp = false) {
+                                bool warp = false, bool newton_roots = false) {
     const int n = c.n;
     Max3Result r{kM3Indeterminate, false, false};
-    c.newton = false;  // the reference's bisection roots and RR
+    c.newton = newton_roots;  // false: the reference's bisection roots and RR
     if (!normalise_feed(c, feed)) {
         r.status = -1;
         return r;
@@ -574,7 +578,7 @@ __device__ Max3Result max3_cell(const Mixture& m, Cell<NM>& c, const double* fee
                 const double* kst[2] = {keep[0], keep[1]};
                 // with the caller's two-phase options (pr76_three_phase.hpp:413-415)
                 const int nst = solve_cell(m, c, nfeed, s.w, nb, kst, 2, kst, 2, opt);
-                c.newton = false;
+                c.newton = newton_roots;
                 if (nst == kTwoPhase) {
                     r.status = kM3Two;
                     r.has_pair = true;  // s.w.best

@@ -165,6 +165,7 @@ EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu
                     "mpmc_gpu_flash_solve_hinted_ex", "mpmc_gpu_flash_solve_device_hinted_ex"]
 FLAG_CUDA_GRAPH = 2
 FLAG_SENSITIVITY_LANES = 4  # the lane-group sensitivity kernel (opt-in)
+FLAG_MAX3_NEWTON_ROOTS = 8  # Newton roots in the max-3-phase continuation (opt-in)
 NOALLOC_SCRATCH_BYTES = 48 << 20
 BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun", "fallback_nonsmooth",
                "fp64_attempts_no_fp32", "fp64_attempts_polish_failed", "fp64_attempts_rejected", "fallback_load",
@@ -258,7 +259,8 @@ class GpuFlash:
     """One mixture on one GPU; batches of cells per call."""
 
     def __init__(self, mixture, form: str | int = "plain", sensitivity: bool = False, device: int = 0,
-                 stage_timing: bool = False, graphs: bool = False, sensitivity_lanes: bool = False):
+                 stage_timing: bool = False, graphs: bool = False, sensitivity_lanes: bool = False,
+                 max3_newton_roots: bool = False):
         self.mixture = mixture
         self.n = int(mixture.n)
         self.form = FORMS[form] if isinstance(form, str) else int(form)
@@ -267,7 +269,8 @@ class GpuFlash:
                       (mixture.tc, mixture.pc, mixture.omega, np.asarray(mixture.kij).reshape(-1))]
         m = _Mixture(self.n, *(a.ctypes.data for a in self._keep))
         flags = ((FLAG_STAGE_TIMING if stage_timing else 0) | (FLAG_CUDA_GRAPH if graphs else 0)
-                 | (FLAG_SENSITIVITY_LANES if sensitivity_lanes else 0))
+                 | (FLAG_SENSITIVITY_LANES if sensitivity_lanes else 0)
+                 | (FLAG_MAX3_NEWTON_ROOTS if max3_newton_roots else 0))
         o = _Options(self.form, int(self.sensitivity), device, flags)
         h = ctypes.c_void_p()
         _check(library().mpmc_gpu_flash_create(ctypes.byref(m), ctypes.byref(o), ctypes.byref(h)))

@@ -39,6 +39,10 @@ static inline void __syncthreads() {}
 
 namespace {
 
+// The continuation's root solver: false, the reference's bisection; true,
+// bracketed Newton (MPMC_FLAG_MAX3_NEWTON_ROOTS).  Set by host_set_max3_newton.
+bool g_max3_newton = false;
+
 void prepare(int n, const double* tc, const double* pc, const double* omega, const double* kij, pr76::Mixture& m) {
     std::memset(&m, 0, sizeof(m));
     m.n = n;
@@ -79,7 +83,7 @@ bool max3_on_warp(const pr76::Mixture& m, const pr76::fp64::Cell<NM>& c0, const 
         Max3Result res{kM3Indeterminate, false, false};
         if (temp_setup(m, c))
             res = max3_cell(m, c, feed, lnk, lane_s[lane], fin, hs.fcount, hs.has_three ? hs.three : nullptr,
-                            hs.options, true);
+                            hs.options, true, g_max3_newton);
         else
             res.status = -1;
         lane_r[lane] = res;
@@ -171,7 +175,7 @@ void run(const pr76::Mixture& m, int64_t ncell, const double* p, const double* t
 #else
             if (temp_setup(m, c2))
                 mr = max3_cell(m, c2, feed, lnk, *s, fin, hs.fcount, hs.has_three ? hs.three : nullptr,
-                               hs.options);
+                               hs.options, false, g_max3_newton);
             else
                 mr.status = -1;
 #endif
@@ -206,6 +210,8 @@ void run(const pr76::Mixture& m, int64_t ncell, const double* p, const double* t
 }
 
 }  // namespace
+
+extern "C" void host_set_max3_newton(int on) { g_max3_newton = on != 0; }
 
 extern "C" int host_hinted_batch(int n, const double* tc, const double* pc, const double* omega, const double* kij,
                                  int64_t ncell, const double* p, const double* t, const double* z,

@@ -64,6 +64,7 @@ def host_flash(tmp_path_factory):
 
         return step
 
+    make_step.lib = lib
     return make_step
 
 
@@ -189,3 +190,38 @@ def test_device_max3_on_six_components_matches_reference(host_flash):
     out = host_flash(mix)(d["p"], d["t"], z, *_no_hints(6, z.shape[1]))
     assert np.array_equal(out["max3"], d["ref_max3_status"])
     assert np.array_equal(out["published"], d["ref_published"])
+
+
+def test_newton_roots_keep_every_recorded_status(host_flash):
+    """MPMC_FLAG_MAX3_NEWTON_ROOTS: the continuation with bracketed-Newton
+    roots and Rachford-Rice (the flash's FP64 items' solvers, the reference's
+    stopping width) instead of bisection reproduces every recorded max3 and
+    published status -- the three-phase fixture's 1,649 cells, the
+    six-component fixture's 429 and the hint-seeded scan's 960 points -- and
+    its three-phase sets equal the bisection ones to 1e-9."""
+    lib = host_flash.lib
+    d = np.load(os.path.join(HERE, "golden", "max3_reference.npz"))
+    mix3 = synth.three_phase_fixture_mixture()
+    z3 = np.ascontiguousarray(d["z"])
+    bisection = host_flash(mix3)(d["p"], d["t"], z3, *_no_hints(3, z3.shape[1]))
+    lib.host_set_max3_newton(1)
+    try:
+        out = host_flash(mix3)(d["p"], d["t"], z3, *_no_hints(3, z3.shape[1]))
+        assert np.array_equal(out["max3"], d["ref_max3_status"])
+        assert np.array_equal(out["published"], d["ref_published"])
+        three = out["max3"] == 2
+        assert three.sum() > 600
+        assert np.abs(out["x3"][:, three] - bisection["x3"][:, three]).max() <= 1e-9
+        assert np.abs(out["f3"][:, three] - bisection["f3"][:, three]).max() <= 1e-9
+        h = np.load(os.path.join(HERE, "golden", "max3_heringer_reference.npz"))
+        mix6 = synth.Mixture(h["tc"], h["pc"], h["omega"], h["kij"])
+        z6 = np.ascontiguousarray(h["z"])
+        out6 = host_flash(mix6)(h["p"], h["t"], z6, *_no_hints(6, z6.shape[1]))
+        assert np.array_equal(out6["max3"], h["ref_max3_status"])
+        assert np.array_equal(out6["published"], h["ref_published"])
+        c = np.load(os.path.join(HERE, "golden", "continuation_reference.npz"))
+        res = continuation.scan_with_hints(host_flash(mix3), c["z"], c["p"], c["t"])
+        assert np.array_equal(res["max3_status"], c["ref_max3_status"])
+        assert np.array_equal(res["status"], c["ref_published"])
+    finally:
+        lib.host_set_max3_newton(0)

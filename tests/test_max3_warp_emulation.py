@@ -95,3 +95,20 @@ def test_warp_form_equals_sequential_on_recorded_cells(libs):
     assert np.array_equal(b["max3"], d["ref_max3_status"])
     assert np.array_equal(b["published"], d["ref_published"])
     _assert_bitwise_equal(a, b)
+
+
+def test_warp_form_with_newton_roots_equals_sequential(libs):
+    """The same with bracketed-Newton roots (MPMC_FLAG_MAX3_NEWTON_ROOTS)."""
+    seq, warp = libs
+    mix = synth.three_phase_fixture_mixture()
+    p, t, z = synth.make_three_phase_cells(32, seed=5, anchor_fraction=0.5)
+    for lib in libs:
+        lib.host_set_max3_newton(1)
+    try:
+        a, b = _solve(seq, mix, p, t, z), _solve(warp, mix, p, t, z)
+    finally:
+        for lib in libs:
+            lib.host_set_max3_newton(0)
+    assert not (b["max3"] == -99).any(), "lanes diverged or disagreed"
+    assert (a["max3"] == 2).sum() == 14
+    _assert_bitwise_equal(a, b)
