@@ -66,8 +66,8 @@ def f_jacobian(n: int) -> float:
 
 
 def stage_flops(n: int, stats: dict, counters_sum: dict, sens_cells: int) -> dict:
-    """Algorithmic flops of each stage of one mixed-form solve (SURVEY.md
-    8(d) conventions): property evaluations x f_eval, the polish's Rachford-
+    """Algorithmic flops of each stage of one mixed-form solve (the flop
+    conventions of f_eval and f_ad): property evaluations x f_eval, the polish's Rachford-
     Rice iterations x 6 n, Jacobians x f_jacobian and chord solves x 2 n^2,
     the sensitivities x f_ad.  FP32 evaluations come from the per-cell work
     counters, FP64 ones from the per-stage totals."""
