@@ -1,0 +1,136 @@
+"""The batched flash pipeline -- the headline mixed-precision form and the FP64
+work-queue form, every kernel of flash_batched.cu -- run on the CPU under the
+host launch emulation, against the oracle.
+
+tests/host_build/emulate_launches.py rewrites the kernel launches of
+flash_batched.cu into calls of tests/host_build/cuda_emu.h, which runs each
+launch's blocks as host threads with the warp intrinsics as rendezvous of the
+named lanes; tests/host_build/batched_host.cpp calls the unchanged
+orchestration (launch_batched_nm) on host memory.  So the device code of the
+pipeline -- FP32 screening, FP64 lane-group items, the polish, the queues, the
+exact sub-solve -- is checked here without a GPU, at small sizes and with the
+host compiler's arithmetic:
+
+1. the mixed form's statuses equal the oracle's on every cell, and its
+   outputs meet the GPU parity bar of tests/test_gpu_parity.py
+   (parity.assert_flash_parity: polished ln K within 1e-10, raw values in the
+   reference's stopping band), at N = 3, 6, 10 and 20 and on near-critical
+   cells;
+2. the same for the FP64 work-queue form;
+3. from ln K warm starts (a second solve started at the first one's ln K,
+   perturbed), the statuses are the cold ones;
+4. no emulated lane ever waits at an intrinsic that another lane of its mask
+   does not reach.
+"""
+
+import concurrent.futures as cf
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from mpmc_hnu_gb300 import synth
+from tests import parity
+from tests.host_build import emulate_launches
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(ROOT, "mpmc_hnu_gb300", "csrc")
+CAPACITIES = (4, 8, 12, 20)
+
+
+@pytest.fixture(scope="module")
+def pipeline(tmp_path_factory):
+    cxx = shutil.which("g++")
+    cuda_inc = "/usr/local/cuda/include"
+    if not cxx or not os.path.exists(os.path.join(cuda_inc, "cuda_runtime.h")):
+        pytest.skip("host compiler or CUDA headers missing")
+    tmp = tmp_path_factory.mktemp("batched_emu")
+    source = str(tmp / "flash_batched_emulated.cpp")
+    emulate_launches.rewrite(os.path.join(CSRC, "flash_batched.cu"), source)
+
+    def build(nm):
+        so = str(tmp / f"libbatched_emu_nm{nm}.so")
+        subprocess.check_call([cxx, "-std=c++20", "-O2", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",
+                               "-Wno-attributes", "-Wno-unknown-pragmas", f"-DMPMC_NM={nm}",
+                               f'-DMPMC_BATCHED_SOURCE="{source}"', "-I" + cuda_inc,
+                               "-I" + os.path.join(ROOT, "include"), "-I" + CSRC,
+                               "-I" + os.path.join(HERE, "host_build"),
+                               os.path.join(HERE, "host_build", "batched_host.cpp"), "-o", so])
+        return nm, ctypes.CDLL(so)
+
+    with cf.ThreadPoolExecutor(max_workers=len(CAPACITIES)) as ex:
+        return dict(ex.map(build, CAPACITIES))
+
+
+def _capacity(n):
+    return next(c for c in CAPACITIES if n <= c)
+
+
+def solve(libs, mix, p, t, z, fp64=False, warm=None):
+    n = mix.n
+    lib = libs[_capacity(n)]
+    tc, pc, om, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
+    z = np.ascontiguousarray(z, dtype=np.float64)
+    nc = z.shape[1]
+    o = {"status": np.full(nc, -7, np.int32), "vapor_fraction": np.empty(nc), "liquid": np.empty((n, nc)),
+         "vapor": np.empty((n, nc)), "ln_k": np.empty((n, nc)), "ln_phi_liquid": np.empty((n, nc)),
+         "ln_phi_vapor": np.empty((n, nc)), "z_liquid": np.empty(nc), "z_vapor": np.empty(nc),
+         "counters": np.zeros((8, nc), np.int32)}
+    ins = [np.ascontiguousarray(a, dtype=np.float64) for a in (p, t)] + [z]
+    w = np.ascontiguousarray(warm, dtype=np.float64) if warm is not None else None
+    rc = lib.host_batched_solve(ctypes.c_int(n), *[ctypes.c_void_p(a.ctypes.data) for a in (tc, pc, om, kij)],
+                                ctypes.c_int64(nc), *[ctypes.c_void_p(a.ctypes.data) for a in ins],
+                                ctypes.c_void_p(w.ctypes.data if w is not None else None), ctypes.c_int(int(fp64)),
+                                *[ctypes.c_void_p(o[k].ctypes.data) for k in
+                                  ("status", "vapor_fraction", "liquid", "vapor", "ln_k", "ln_phi_liquid",
+                                   "ln_phi_vapor", "z_liquid", "z_vapor", "counters")])
+    assert rc != -1, "emulated lanes diverged at an intrinsic"
+    assert rc == 0, f"orchestration error {rc}"
+    return o
+
+
+@pytest.mark.parametrize("n,ncell,seed", [(3, 512, 5), (6, 256, 1), (10, 256, 2), (20, 64, 4)])
+def test_mixed_form_matches_the_oracle(pipeline, oracle_lib, n, ncell, seed):
+    mix = synth.make_mixture(n, seed)
+    p, t, z = synth.make_cells(n, ncell, seed)
+    out = solve(pipeline, mix, p, t, z)
+    ref = oracle_lib.flash(mix, p, t, z, threads=8)
+    rep = parity.flash_report(out, ref, mix, p, t, z)
+    parity.assert_flash_parity(rep)
+    assert rep["two_phase"] > 0
+
+
+@pytest.mark.parametrize("n,ncell,seed", [(10, 128, 12), (20, 48, 13)])
+def test_mixed_form_near_critical(pipeline, oracle_lib, n, ncell, seed):
+    mix = synth.make_mixture(n, seed)
+    p, t, z = synth.make_near_critical_cells(mix, ncell, seed, fraction=0.5)
+    out = solve(pipeline, mix, p, t, z)
+    ref = oracle_lib.flash(mix, p, t, z, threads=8)
+    parity.assert_flash_parity(parity.flash_report(out, ref, mix, p, t, z))
+
+
+@pytest.mark.parametrize("n,ncell,seed", [(3, 256, 5), (4, 64, 6)])
+def test_fp64_form_matches_the_oracle(pipeline, oracle_lib, n, ncell, seed):
+    mix = synth.make_mixture(n, seed)
+    p, t, z = synth.make_cells(n, ncell, seed)
+    out = solve(pipeline, mix, p, t, z, fp64=True)
+    ref = oracle_lib.flash(mix, p, t, z, threads=8)
+    parity.assert_flash_parity(parity.flash_report(out, ref, mix, p, t, z))
+
+
+def test_warm_starts_keep_the_cold_statuses(pipeline, oracle_lib):
+    n, ncell, seed = 6, 256, 3
+    mix = synth.make_mixture(n, seed)
+    p, t, z = synth.make_cells(n, ncell, seed)
+    cold = solve(pipeline, mix, p, t, z)
+    rng = np.random.default_rng(seed)
+    warm = cold["ln_k"] + 0.1 * rng.standard_normal(cold["ln_k"].shape)
+    warm[:, cold["status"] != 1] = np.nan
+    out = solve(pipeline, mix, p, t, z, warm=warm)
+    ref = oracle_lib.flash(mix, p, t, z, threads=8)
+    assert np.array_equal(out["status"], ref["status"])
+    assert np.array_equal(out["status"], cold["status"])
