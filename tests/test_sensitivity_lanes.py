@@ -174,3 +174,64 @@ def test_failure_statuses_agree(host):
         seen.update(a["sens_status"].tolist())
     # the phase-boundary, ill-conditioned and arithmetic statuses are all reached
     assert seen[2] > 0 and seen[5] > 0 and seen[6] > 0, seen
+
+
+@pytest.fixture(scope="module")
+def kernels(tmp_path_factory):
+    """sensitivity.cu itself under the host launch emulation (cuda_emu.h):
+    both kernels with their launch shapes, grid-stride loops and fills."""
+    cxx = shutil.which("g++")
+    cuda_inc = "/usr/local/cuda/include"
+    if not cxx or not os.path.exists(os.path.join(cuda_inc, "cuda_runtime.h")):
+        pytest.skip("host compiler or CUDA headers missing")
+    from tests.host_build import emulate_launches
+    tmp = tmp_path_factory.mktemp("sens_kernels")
+    source = str(tmp / "sensitivity_emulated.cpp")
+    emulate_launches.rewrite(os.path.join(ROOT, "mpmc_hnu_gb300", "csrc", "sensitivity.cu"), source)
+    libs = {}
+    for nm in (4, 12, 20):
+        so = str(tmp / f"libsens_kernels_nm{nm}.so")
+        subprocess.check_call([cxx, "-std=c++20", "-O2", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",
+                               "-Wno-attributes", "-Wno-unknown-pragmas", f"-DMPMC_NM={nm}",
+                               f'-DMPMC_SENS_SOURCE="{source}"', "-I" + cuda_inc,
+                               "-I" + os.path.join(ROOT, "include"),
+                               "-I" + os.path.join(ROOT, "mpmc_hnu_gb300", "csrc"),
+                               "-I" + os.path.join(HERE, "host_build"),
+                               os.path.join(HERE, "host_build", "sens_kernels_host.cpp"), "-o", so])
+        libs[nm] = ctypes.CDLL(so)
+    return libs
+
+
+def run_kernel(libs, mix, p, t, z, lanes):
+    n = mix.n
+    lib = libs[4 if n <= 4 else (12 if n <= 12 else 20)]
+    tc, pc, om, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
+    z = np.ascontiguousarray(z, dtype=np.float64)
+    nc = z.shape[1]
+    o = _outputs(n, nc)
+    for k, v in o.items():
+        v.fill(-5 if v.dtype == np.int32 else 7.0)  # a value no kernel writes
+    ins = [np.ascontiguousarray(a, dtype=np.float64) for a in (p, t)] + [z]
+    rc = lib.host_sensitivity_kernel(ctypes.c_int(n), *[ctypes.c_void_p(a.ctypes.data) for a in (tc, pc, om, kij)],
+                                     ctypes.c_int64(nc), *[ctypes.c_void_p(a.ctypes.data) for a in ins],
+                                     ctypes.c_int(int(lanes)), *[ctypes.c_void_p(o[k].ctypes.data) for k in KEYS])
+    assert rc != -1, "emulated lanes diverged"
+    assert rc == 0
+    return o
+
+
+@pytest.mark.parametrize("n,ncell,seed", [(3, 200, 5), (9, 150, 7), (12, 100, 3), (20, 40, 4)])
+def test_lane_kernel_equals_per_thread_kernel(kernels, n, ncell, seed):
+    """The kernels as launched: every cell gets a status and every output a
+    value (NaN where the status is not success), the same in both."""
+    mix = synth.make_mixture(n, seed)
+    p, t, z = synth.make_cells(n, ncell, seed)
+    a, b = run_kernel(kernels, mix, p, t, z, False), run_kernel(kernels, mix, p, t, z, True)
+    assert np.array_equal(a["sens_status"], b["sens_status"])
+    ok = a["sens_status"] == 0
+    assert 0 < ok.sum() < ncell
+    for k in DERIVS + ("jac_liquid", "jac_vapor"):
+        assert not (a[k] == 7.0).any() and not (b[k] == 7.0).any(), k
+        assert np.array_equal(np.isnan(a[k]), np.isnan(b[k])), k
+        assert np.isnan(b[k][:, ~ok]).all(), k
+    assert _normwise(a, b, ok) <= 1e-13
