@@ -32,6 +32,9 @@ using std::isfinite;
 #undef __shared__
 #define __shared__ static  // one block runs at a time
 #define __launch_bounds__(...)
+#ifndef __noinline__
+#define __noinline__ __attribute__((noinline))
+#endif
 
 // the integer min / max device code calls unqualified
 template <class T>
