@@ -254,7 +254,9 @@ inline T atomicAdd(T* p, T v) {
 }
 
 // ---- runtime calls of the orchestration ----------------------------------
-// (defined once: the test harness that includes this header is one translation unit)
+// (defined once: the test harness that includes this header is one translation
+// unit; it links with -Bsymbolic, so that a CUDA runtime already loaded into
+// the process cannot take these calls over)
 extern "C" {
 cudaError_t cudaGetLastError(void) { return cudaSuccess; }
 cudaError_t cudaMemsetAsync(void* p, int v, size_t n, cudaStream_t) {

@@ -55,7 +55,7 @@ def pipeline(tmp_path_factory):
     def build(nm):
         so = str(tmp / f"libbatched_emu_nm{nm}.so")
         subprocess.check_call([cxx, "-std=c++20", "-O2", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",
-                               "-Wno-attributes", "-Wno-unknown-pragmas", f"-DMPMC_NM={nm}",
+                               "-Wno-attributes", "-Wno-unknown-pragmas", "-Wl,-Bsymbolic", f"-DMPMC_NM={nm}",
                                f'-DMPMC_BATCHED_SOURCE="{source}"', "-I" + cuda_inc,
                                "-I" + os.path.join(ROOT, "include"), "-I" + CSRC,
                                "-I" + os.path.join(HERE, "host_build"),

@@ -41,7 +41,7 @@ def kernels(tmp_path_factory):
     for nm in (4, 8, 12):
         so = str(tmp / f"libkernels_nm{nm}.so")
         subprocess.check_call([cxx, "-std=c++20", "-O2", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",
-                               "-Wno-attributes", "-Wno-unknown-pragmas", f"-DMPMC_NM={nm}",
+                               "-Wno-attributes", "-Wno-unknown-pragmas", "-Wl,-Bsymbolic", f"-DMPMC_NM={nm}",
                                f'-DMPMC_PLAIN_SOURCE="{plain}"', f'-DMPMC_MAX3_SOURCE="{max3}"', "-I" + cuda_inc,
                                "-I" + os.path.join(ROOT, "include"), "-I" + CSRC,
                                "-I" + os.path.join(HERE, "host_build"),

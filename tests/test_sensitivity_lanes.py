@@ -192,7 +192,7 @@ def kernels(tmp_path_factory):
     for nm in (4, 12, 20):
         so = str(tmp / f"libsens_kernels_nm{nm}.so")
         subprocess.check_call([cxx, "-std=c++20", "-O2", "-fPIC", "-shared", "-pthread", "-ffp-contract=off",
-                               "-Wno-attributes", "-Wno-unknown-pragmas", f"-DMPMC_NM={nm}",
+                               "-Wno-attributes", "-Wno-unknown-pragmas", "-Wl,-Bsymbolic", f"-DMPMC_NM={nm}",
                                f'-DMPMC_SENS_SOURCE="{source}"', "-I" + cuda_inc,
                                "-I" + os.path.join(ROOT, "include"),
                                "-I" + os.path.join(ROOT, "mpmc_hnu_gb300", "csrc"),
