@@ -1426,6 +1426,97 @@ __device__ void store_candidate(const Workspace& ws, int64_t c, const fp64::Spli
     ws.cand_s[idx(7, ws.ncell, c)] = st.guard;
 }
 
+// The polish candidates of cell c (its na attempts): the minimum-Gibbs
+// FP32-converged attempt, and the second one where FP32 cannot separate the
+// two Gibbs energies at different compositions (FP64 arbitrates); -1 for none.
+// Returns the first.
+template <int NM>
+__device__ __forceinline__ int polish_candidates(const Workspace& ws, int64_t c, int n, int na, int candidates[2]) {
+    // rank converged attempts by FP32 Gibbs energy (ties in FP32 resolved in FP64)
+    int best = -1, second = -1;
+    for (int a = 0; a < na; ++a) {
+        if (ws.att_class[idx(a, ws.ncell, c)] != fp32::aConverged) continue;
+        const float g = ws.att_gibbs[idx(a, ws.ncell, c)];
+        if (best < 0 || g < ws.att_gibbs[idx(best, ws.ncell, c)]) {
+            second = best;
+            best = a;
+        } else if (second < 0 || g < ws.att_gibbs[idx(second, ws.ncell, c)]) {
+            second = a;
+        }
+    }
+    // a second converged attempt at a different composition with a Gibbs
+    // energy FP32 cannot separate from the best: let FP64 arbitrate
+    candidates[0] = best;
+    candidates[1] = -1;
+    if (best >= 0 && second >= 0) {
+        const float gb = ws.att_gibbs[idx(best, ws.ncell, c)], gs = ws.att_gibbs[idx(second, ws.ncell, c)];
+        float dist = 0.f;
+        for (int i = 0; i < n; ++i)
+            dist = fmaxf(dist, fabsf(ws.att_lnk[idx(best * NM + i, ws.ncell, c)] -
+                                     ws.att_lnk[idx(second * NM + i, ws.ncell, c)]));
+        if (gs - gb <= 1e-4f * (1.f + fabsf(gb)) && dist > 1e-2f) {
+            candidates[1] = second;
+            atomicAdd(&ws.counters[sCandidates2], 1);
+        }
+    }
+    return best;
+}
+
+// A cell after its candidates' polishes: the work counters; then, on a replay
+// risk, the exact sub-solve (or the FP64 runs of every attempt for a warm
+// cell); without an accepted pair, the FP64 continuations of the unsettled
+// attempts or the cell's status; with one, the competition of the attempts
+// FP32 left open, or the review.
+template <int NM>
+__device__ __forceinline__ void polish_cell_next(const Workspace& ws, const DeviceOutputs& out, int64_t c,
+                                                 fp64::Cell<NM>& c64, int na, int best, bool have, bool polish_failed,
+                                                 bool replay_risk, double best_g, int cand_order, int jacobians,
+                                                 int solves) {
+    atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], c64.counters[cSplitEvals]);
+    atomicAdd(&ws.counters_out[idx(cRrIters, ws.ncell, c)], c64.counters[cRrIters]);
+    add_total(ws, tE64Polish, c64.counters[cSplitEvals]);
+    add_count(ws, sPolishJacobians, jacobians);
+    add_count(ws, sPolishSolves, solves);
+    if (replay_risk) {
+        atomicAdd(&ws.counters[sReplayRisk], 1);
+        if (mark_exact(ws, c)) return;
+        // (a warm cell) the reference's own runs of every attempt, from the FP64 seeds
+        int cnt = 0;
+        for (int a = 0; a < na; ++a) cnt += unsettled(ws.att_class[idx(a, ws.ncell, c)]);
+        queue_attempts64<NM>(ws, c, na, cnt, -1, 0.0, true);
+        return;
+    }
+    if (!have) {
+        // FP64 continuation (reference ln K iteration, pt_split.hpp:275-408) of
+        // every attempt FP32 left unsettled, from its FP32 end point: split64 items
+        int cnt = 0;
+        for (int a = 0; a < na; ++a) cnt += unsettled(ws.att_class[idx(a, ws.ncell, c)]);
+        if (cnt == 0) {
+            if (warm_cell(ws, c)) {  // the warm attempt collapsed: solve the cell cold
+                ws.phase[c] = pRedo;
+                atomicAdd(&ws.counters[sWarmRedo], 1);
+                atomicAdd(&ws.counters[sWarmNoPair], 1);
+                return;
+            }
+            ws.phase[c] = pIndeterminate;  // every attempt collapsed to the trivial solution
+            write_status_only<NM>(out, ws, c, kIndeterminate, false);
+            write_counters<NM>(out, ws, c);
+            return;
+        }
+        atomicAdd(&ws.counters[best < 0 ? sFbNoAttempt : (polish_failed ? sFbPolish : sFbRejected)], 1);
+        if (best < 0 && mark_exact(ws, c)) return;
+        queue_attempts64<NM>(ws, c, na, cnt, -1, 0.0);
+        return;
+    }
+    int open = 0;
+    for (int a = 0; a < na; ++a) open += open_attempt(ws.att_class[idx(a, ws.ncell, c)]);
+    if (open > 0) {
+        list_open<NM>(ws, c, na, open, cand_order, best_g);
+        return;
+    }
+    begin_review(ws, c, c64, best_g);
+}
+
 template <int NM>
 __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ mix_g, Workspace ws,
                                                     const double* __restrict__ p, const double* __restrict__ t,
@@ -1445,33 +1536,9 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
             atomicAdd(&ws.counters[sFbLoad], 1);
             continue;
         }
-        // rank converged attempts by FP32 Gibbs energy (ties in FP32 resolved in FP64 below)
         const int na = ws.att_count[c];
-        int best = -1, second = -1;
-        for (int a = 0; a < na; ++a) {
-            if (ws.att_class[idx(a, ws.ncell, c)] != fp32::aConverged) continue;
-            const float g = ws.att_gibbs[idx(a, ws.ncell, c)];
-            if (best < 0 || g < ws.att_gibbs[idx(best, ws.ncell, c)]) {
-                second = best;
-                best = a;
-            } else if (second < 0 || g < ws.att_gibbs[idx(second, ws.ncell, c)]) {
-                second = a;
-            }
-        }
-        // a second converged attempt at a different composition with a Gibbs
-        // energy FP32 cannot separate from the best: let FP64 arbitrate
-        int candidates[2] = {best, -1};
-        if (best >= 0 && second >= 0) {
-            const float gb = ws.att_gibbs[idx(best, ws.ncell, c)], gs = ws.att_gibbs[idx(second, ws.ncell, c)];
-            float dist = 0.f;
-            for (int i = 0; i < n; ++i)
-                dist = fmaxf(dist, fabsf(ws.att_lnk[idx(best * NM + i, ws.ncell, c)] -
-                                         ws.att_lnk[idx(second * NM + i, ws.ncell, c)]));
-            if (gs - gb <= 1e-4f * (1.f + fabsf(gb)) && dist > 1e-2f) {
-                candidates[1] = second;
-                atomicAdd(&ws.counters[sCandidates2], 1);
-            }
-        }
+        int candidates[2];
+        const int best = polish_candidates<NM>(ws, c, n, na, candidates);
         bool have = false, polish_failed = false, replay_risk = false;
         double best_g = 0.0;
         int cand_order = -1;
@@ -1497,49 +1564,8 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
             cand_order = a;
             store_candidate(ws, c, s.st, n);
         }
-        atomicAdd(&ws.counters_out[idx(kFp64EvalRow, ws.ncell, c)], c64.counters[cSplitEvals]);
-        atomicAdd(&ws.counters_out[idx(cRrIters, ws.ncell, c)], c64.counters[cRrIters]);
-        add_total(ws, tE64Polish, c64.counters[cSplitEvals]);
-        add_count(ws, sPolishJacobians, s.jacobians);
-        add_count(ws, sPolishSolves, s.solves);
-        if (replay_risk) {
-            atomicAdd(&ws.counters[sReplayRisk], 1);
-            if (mark_exact(ws, c)) continue;
-            // (a warm cell) the reference's own runs of every attempt, from the FP64 seeds
-            int cnt = 0;
-            for (int a = 0; a < na; ++a) cnt += unsettled(ws.att_class[idx(a, ws.ncell, c)]);
-            queue_attempts64<NM>(ws, c, na, cnt, -1, 0.0, true);
-            continue;
-        }
-        if (!have) {
-            // FP64 continuation (reference ln K iteration, pt_split.hpp:275-408) of
-            // every attempt FP32 left unsettled, from its FP32 end point: split64 items
-            int cnt = 0;
-            for (int a = 0; a < na; ++a) cnt += unsettled(ws.att_class[idx(a, ws.ncell, c)]);
-            if (cnt == 0) {
-                if (warm_cell(ws, c)) {  // the warm attempt collapsed: solve the cell cold
-                    ws.phase[c] = pRedo;
-                    atomicAdd(&ws.counters[sWarmRedo], 1);
-                    atomicAdd(&ws.counters[sWarmNoPair], 1);
-                    continue;
-                }
-                ws.phase[c] = pIndeterminate;  // every attempt collapsed to the trivial solution
-                write_status_only<NM>(out, ws, c, kIndeterminate, false);
-                write_counters<NM>(out, ws, c);
-                continue;
-            }
-            atomicAdd(&ws.counters[best < 0 ? sFbNoAttempt : (polish_failed ? sFbPolish : sFbRejected)], 1);
-            if (best < 0 && mark_exact(ws, c)) continue;
-            queue_attempts64<NM>(ws, c, na, cnt, -1, 0.0);
-            continue;
-        }
-        int open = 0;
-        for (int a = 0; a < na; ++a) open += open_attempt(ws.att_class[idx(a, ws.ncell, c)]);
-        if (open > 0) {
-            list_open<NM>(ws, c, na, open, cand_order, best_g);
-            continue;
-        }
-        begin_review(ws, c, c64, best_g);
+        polish_cell_next<NM>(ws, out, c, c64, na, best, have, polish_failed, replay_risk, best_g, cand_order,
+                             s.jacobians, s.solves);
     }
 }
 
