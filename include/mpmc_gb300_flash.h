@@ -133,6 +133,13 @@ typedef struct mpmc_pr76_mixture {
  * same status on every recorded cell (checked on the CPU), phase sets equal
  * to rounding.  Opt-in: not yet timed on a GPU. */
 #define MPMC_FLAG_MAX3_NEWTON_ROOTS 8
+/* The mixed form's per-thread FP64 polish as a state machine that makes one
+ * property evaluation per loop iteration for every thread, whatever step of
+ * its cell's polish that is, so that a warp's lanes evaluate together.  The
+ * same arithmetic per cell as the default polish: the outputs are the same
+ * (checked on the CPU under a launch emulation).  Opt-in: not yet timed on
+ * a GPU. */
+#define MPMC_FLAG_POLISH_STREAM 16
 
 typedef struct mpmc_flash_options {
     int32_t form;              /* MPMC_FORM_* */

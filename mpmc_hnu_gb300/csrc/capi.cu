@@ -108,6 +108,7 @@ struct mpmc_gpu_flash {
     bool use_graphs = false;
     bool sens_lanes = false;  // the lane-group sensitivity kernel (MPMC_FLAG_SENSITIVITY_LANES)
     bool max3_newton = false;  // Newton roots in the max-3-phase continuation (MPMC_FLAG_MAX3_NEWTON_ROOTS)
+    bool polish_stream = false;  // the state-machine polish (MPMC_FLAG_POLISH_STREAM)
     std::vector<GraphEntry> graphs;
     uint64_t graph_clock = 0;
 };
@@ -241,6 +242,7 @@ pr76::BatchedShape batched_shape(const mpmc_gpu_flash* h, cudaEvent_t* events) {
     if (h->shape[6] > 0) shape.ss_switch = 1e-6f * static_cast<float>(h->shape[6]);
     if (h->shape[8] > 0) shape.slow_projection = static_cast<float>(h->shape[8]);
     if (h->shape[9] > 0) shape.continue_limit = h->shape[9];
+    shape.polish_stream = h->polish_stream ? 1 : 0;
     return shape;
 }
 
@@ -781,6 +783,7 @@ int mpmc_gpu_flash_create(const mpmc_pr76_mixture* mixture, const mpmc_flash_opt
     h->use_graphs = (opt.flags & MPMC_FLAG_CUDA_GRAPH) != 0;
     h->sens_lanes = (opt.flags & MPMC_FLAG_SENSITIVITY_LANES) != 0;
     h->max3_newton = (opt.flags & MPMC_FLAG_MAX3_NEWTON_ROOTS) != 0;
+    h->polish_stream = (opt.flags & MPMC_FLAG_POLISH_STREAM) != 0;
     h->host_mixture = m;
     e = cudaMalloc(&h->d_mixture, sizeof(pr76::Mixture));
     if (e == cudaSuccess) e = cudaMemcpy(h->d_mixture, &m, sizeof(pr76::Mixture), cudaMemcpyHostToDevice);

@@ -253,7 +253,9 @@ cudaError_t MPMC_CAT(launch_batched_nm, MPMC_NM)(const Mixture* d_mix, int n, in
         // polish: one cell per thread up to 12 components (its per-cell arrays
         // still fit the cache), one cell per lane group above
         const bool lane_polish = (shape.item_form & 8) ? true : ((shape.item_form & 16) ? false : NM <= 12);
-        if (lane_polish) polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+        if (lane_polish && shape.polish_stream)
+            polish_stream_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
+        else if (lane_polish) polish_kernel<NM><<<cell_grid(ncell), cell_block, 0, stream>>>(d_mix, ws, p, t, out);
         else w64::polishw_kernel<NM, w64::kSeg<NM>><<<sms * s64_res, 128, 0, stream>>>(d_mix, ws, p, t, out);
         mark();
         // every cell the exact sub-solve takes is marked by now (in this

@@ -77,6 +77,8 @@ struct BatchedShape {
                                // runs from its start in FP64 (0 = the default)
     int64_t io_stride;         // stride of z, the warm starts and the outputs (0 = ncell): a solve of one
                                // cell range of a larger batch, with every pointer at the range's start
+    int polish_stream;         // nonzero: the per-thread polish as one evaluation per loop iteration
+                               // (polish_stream_kernel) instead of cell by cell (polish_kernel)
 };
 constexpr int kBatchedStages = 17;
 

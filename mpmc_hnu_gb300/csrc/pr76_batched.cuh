@@ -1569,6 +1569,160 @@ __global__ void __launch_bounds__(64) polish_kernel(const Mixture* __restrict__ 
     }
 }
 
+// The per-thread polish as a state machine (opt-in, BatchedShape::polish_stream):
+// the work of polish_kernel, cell by cell down the thread's grid-stride
+// sequence and with the same arithmetic, but every loop iteration makes one
+// FP64 property evaluation (split_evaluate, one call site) for every thread
+// that has a cell, whatever step of its polish that cell is at -- a
+// candidate's first FP64 state or one of its chord steps.  In polish_kernel a
+// warp's lanes reach their evaluations at different points of the cell loop
+// (one building a Jacobian, one in its fifth chord step, one starting its next
+// cell) and run them one after another; here they evaluate together, and
+// only the Jacobians, their factorisation and the per-cell bookkeeping
+// diverge.
+template <int NM>
+__global__ void __launch_bounds__(64) polish_stream_kernel(const Mixture* __restrict__ mix_g, Workspace ws,
+                                                           const double* __restrict__ p, const double* __restrict__ t,
+                                                           DeviceOutputs out) {
+    __shared__ Mixture m;
+    stage_mixture(mix_g, m);
+    const int cells = ws.counters[qSplitCells];
+    const int n = m.n;
+    const int stride = gridDim.x * blockDim.x;
+    int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    enum Step : int { kFetch, kFirst, kChord, kDone };
+    int step = kFetch;
+    // the cell
+    int64_t c = -1;
+    fp64::Cell<NM> c64;
+    PolishScratch<NM> s;
+    int na = 0, best = -1, k = 0, cand_order = -1;
+    int candidates[2] = {-1, -1};
+    bool have = false, polish_failed = false, replay_risk = false;
+    double best_g = 0.0;
+    // the candidate being polished (polish_split's state)
+    int done = 0, replay = 0, chord = 0, evals = 0;
+    double prev = 0.0;
+    auto start_candidate = [&]() {
+        const int a = candidates[k];
+        for (int i = 0; i < n; ++i) s.lnk[i] = ws.att_lnk[idx(a * NM + i, ws.ncell, c)];
+        done = ws.att_iter[idx(a, ws.ncell, c)];
+        replay = 0;
+        evals = 0;
+        step = kFirst;
+    };
+    // the candidate loop of polish_kernel after polish_split returned `ok`
+    auto end_candidate = [&](bool ok) {
+        const int a = candidates[k];
+        bool stop = false;
+        if (!ok) {
+            polish_failed = true;
+        } else if (replay < 0 || done + replay > kReplayLimit) {
+            replay_risk = true;
+            stop = true;
+        } else if (split_accepted(s.st, n) && (!have || s.st.gibbs < best_g)) {
+            have = true;
+            best_g = s.st.gibbs;
+            cand_order = a;
+            store_candidate(ws, c, s.st, n);
+        }
+        ++k;
+        if (!stop && k < 2 && candidates[k] >= 0) {
+            start_candidate();
+            return;
+        }
+        polish_cell_next<NM>(ws, out, c, c64, na, best, have, polish_failed, replay_risk, best_g, cand_order,
+                             s.jacobians, s.solves);
+        step = kFetch;
+    };
+    // the next chord step's ln K: J d = -F at the current state (false: the solve failed)
+    auto chord_target = [&]() -> bool {
+        for (int i = 0; i < n; ++i) s.d[i] = -s.st.res[i];
+        ++s.solves;
+        if (!ad::lu_solve(s.J, s.piv, n, s.d)) return false;
+        for (int i = 0; i < n; ++i) s.lnk[i] = s.st.lnk[i] + s.d[i];
+        return true;
+    };
+    for (;;) {
+        while (step == kFetch) {
+            if (slot >= cells) {
+                step = kDone;
+                break;
+            }
+            c = ws.split_cells[slot];
+            slot += stride;
+            s.jacobians = s.solves = 0;
+            if (!load_cell64(m, ws, c, p, t, c64)) {
+                ws.phase[c] = pFallback;
+                atomicAdd(&ws.counters[qFallback], 1);
+                atomicAdd(&ws.counters[sFbLoad], 1);
+                continue;
+            }
+            na = ws.att_count[c];
+            best = polish_candidates<NM>(ws, c, n, na, candidates);
+            have = polish_failed = replay_risk = false;
+            best_g = 0.0;
+            cand_order = -1;
+            k = 0;
+            if (candidates[0] < 0) {
+                polish_cell_next<NM>(ws, out, c, c64, na, best, have, polish_failed, replay_risk, best_g,
+                                     cand_order, s.jacobians, s.solves);
+                continue;
+            }
+            start_candidate();
+        }
+        if (step == kDone) break;
+        // this iteration's evaluation: a candidate's first FP64 state, or a chord step
+        const bool first = step == kFirst;
+        const int r = fp64::split_evaluate(m, c64, s.lnk, first ? s.st : s.nx, evals, 1 << 30, s.e, s.num, true,
+                                           first ? 0.5 : s.st.beta, first ? nullptr : &s.st);
+        if (first) {
+            if (r != fp64::kConverged) {
+                end_candidate(false);
+                continue;
+            }
+            if (s.st.fug <= 1e-13) {
+                end_candidate(true);
+                continue;
+            }
+            if (!equilibrium_jacobian(m, c64, s)) {
+                end_candidate(false);
+                continue;
+            }
+            replay = replay_linear(n, s.J, s.st.res, s.st.x, s.st.y, c64.z, s.st.beta, 2.0 * s.st.guard, 512 - done);
+            double norm;
+            if (!ad::lu_factor(s.J, s.piv, n, norm)) {
+                end_candidate(false);
+                continue;
+            }
+            ++s.jacobians;
+            prev = s.st.fug;
+            chord = 0;
+            if (!chord_target()) {
+                end_candidate(false);
+                continue;
+            }
+            step = kChord;
+            continue;
+        }
+        if (r != fp64::kConverged || !(s.nx.fug < prev)) {
+            end_candidate(prev <= 1e-11);
+            continue;
+        }
+        fp64::copy_state(s.st, s.nx, n);
+        prev = s.st.fug;
+        if (prev <= 1e-13) {
+            end_candidate(true);
+            continue;
+        }
+        if (++chord >= 8) {
+            end_candidate(prev <= 1e-11);
+            continue;
+        }
+        if (!chord_target()) end_candidate(false);
+    }
+}
+
 // Cells whose polished pair waited on open attempts: the pair goes to the
 // review when the FP32 prediction pruned every open attempt; otherwise the
 // attempts left open continue exactly in FP64 (split64) and compete with the

@@ -166,6 +166,7 @@ EXPORTED_SYMBOLS = ["mpmc_gpu_flash_create", "mpmc_gpu_flash_destroy", "mpmc_gpu
 FLAG_CUDA_GRAPH = 2
 FLAG_SENSITIVITY_LANES = 4  # the lane-group sensitivity kernel (opt-in)
 FLAG_MAX3_NEWTON_ROOTS = 8  # Newton roots in the max-3-phase continuation (opt-in)
+FLAG_POLISH_STREAM = 16  # the state-machine FP64 polish (opt-in)
 NOALLOC_SCRATCH_BYTES = 48 << 20
 BATCH_STATS = ["feed_continued", "feed_rerun", "review_continued", "review_rerun", "fallback_nonsmooth",
                "fp64_attempts_no_fp32", "fp64_attempts_polish_failed", "fp64_attempts_rejected", "fallback_load",
@@ -260,7 +261,7 @@ class GpuFlash:
 
     def __init__(self, mixture, form: str | int = "plain", sensitivity: bool = False, device: int = 0,
                  stage_timing: bool = False, graphs: bool = False, sensitivity_lanes: bool = False,
-                 max3_newton_roots: bool = False):
+                 max3_newton_roots: bool = False, polish_stream: bool = False):
         self.mixture = mixture
         self.n = int(mixture.n)
         self.form = FORMS[form] if isinstance(form, str) else int(form)
@@ -270,7 +271,8 @@ class GpuFlash:
         m = _Mixture(self.n, *(a.ctypes.data for a in self._keep))
         flags = ((FLAG_STAGE_TIMING if stage_timing else 0) | (FLAG_CUDA_GRAPH if graphs else 0)
                  | (FLAG_SENSITIVITY_LANES if sensitivity_lanes else 0)
-                 | (FLAG_MAX3_NEWTON_ROOTS if max3_newton_roots else 0))
+                 | (FLAG_MAX3_NEWTON_ROOTS if max3_newton_roots else 0)
+                 | (FLAG_POLISH_STREAM if polish_stream else 0))
         o = _Options(self.form, int(self.sensitivity), device, flags)
         h = ctypes.c_void_p()
         _check(library().mpmc_gpu_flash_create(ctypes.byref(m), ctypes.byref(o), ctypes.byref(h)))

@@ -34,12 +34,12 @@ void prepare(int n, const double* tc, const double* pc, const double* omega, con
 // work-queue form (1), from ln K warm starts [n ncell] when warm_lnk is not
 // null (a non-finite entry makes its cell cold), as
 // mpmc_gpu_flash_solve_device_warm runs it; outputs as mpmc_flash_outputs'
-// flash fields.  Returns
+// flash fields; polish_stream selects the state-machine polish.  Returns
 // 0, a CUDA error code of the orchestration, or -1 when the emulated lanes
 // diverged at an intrinsic.
 extern "C" int host_batched_solve(int n, const double* tc, const double* pc, const double* omega, const double* kij,
                                   int64_t ncell, const double* p, const double* t, const double* z,
-                                  const double* warm_lnk, int fp64_items,
+                                  const double* warm_lnk, int fp64_items, int polish_stream,
                                   int32_t* status, double* beta, double* x, double* y, double* lnk, double* lnphi_l,
                                   double* lnphi_v, double* z_l, double* z_v, int32_t* counters) {
     pr76::Mixture m;
@@ -58,6 +58,7 @@ extern "C" int host_batched_solve(int n, const double* tc, const double* pc, con
     pr76::BatchedShape shape{};
     shape.fp64_items = fp64_items;
     shape.warm_lnk = warm_lnk;
+    shape.polish_stream = polish_stream;
     const size_t bytes = MPMC_CAT(pr76::batched_workspace_bytes_nm, MPMC_NM)(n, ncell, fp64_items != 0,
                                                                             pr76::kS64PerCell);
     std::vector<unsigned char> scratch(bytes + 256);

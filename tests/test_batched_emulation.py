@@ -19,7 +19,9 @@ host compiler's arithmetic:
 2. the same for the FP64 work-queue form;
 3. from ln K warm starts (a second solve started at the first one's ln K,
    perturbed), the statuses are the cold ones;
-4. no emulated lane ever waits at an intrinsic that another lane of its mask
+4. the opt-in state-machine polish (MPMC_FLAG_POLISH_STREAM) gives the
+   default polish's outputs bit for bit;
+5. no emulated lane ever waits at an intrinsic that another lane of its mask
    does not reach.
 """
 
@@ -70,7 +72,7 @@ def _capacity(n):
     return next(c for c in CAPACITIES if n <= c)
 
 
-def solve(libs, mix, p, t, z, fp64=False, warm=None):
+def solve(libs, mix, p, t, z, fp64=False, warm=None, polish_stream=False):
     n = mix.n
     lib = libs[_capacity(n)]
     tc, pc, om, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
@@ -85,6 +87,7 @@ def solve(libs, mix, p, t, z, fp64=False, warm=None):
     rc = lib.host_batched_solve(ctypes.c_int(n), *[ctypes.c_void_p(a.ctypes.data) for a in (tc, pc, om, kij)],
                                 ctypes.c_int64(nc), *[ctypes.c_void_p(a.ctypes.data) for a in ins],
                                 ctypes.c_void_p(w.ctypes.data if w is not None else None), ctypes.c_int(int(fp64)),
+                                ctypes.c_int(int(polish_stream)),
                                 *[ctypes.c_void_p(o[k].ctypes.data) for k in
                                   ("status", "vapor_fraction", "liquid", "vapor", "ln_k", "ln_phi_liquid",
                                    "ln_phi_vapor", "z_liquid", "z_vapor", "counters")])
@@ -134,3 +137,18 @@ def test_warm_starts_keep_the_cold_statuses(pipeline, oracle_lib):
     ref = oracle_lib.flash(mix, p, t, z, threads=8)
     assert np.array_equal(out["status"], ref["status"])
     assert np.array_equal(out["status"], cold["status"])
+
+
+@pytest.mark.parametrize("n,ncell,seed", [(3, 512, 5), (6, 256, 1), (10, 256, 2), (20, 64, 4)])
+def test_state_machine_polish_equals_the_default(pipeline, oracle_lib, n, ncell, seed):
+    """MPMC_FLAG_POLISH_STREAM: the state-machine polish makes the same
+    evaluations per cell as the default polish, so every output is the same
+    bit for bit (at N = 20 both run the lane-group polish)."""
+    mix = synth.make_mixture(n, seed)
+    p, t, z = synth.make_cells(n, ncell, seed)
+    a = solve(pipeline, mix, p, t, z)
+    b = solve(pipeline, mix, p, t, z, polish_stream=True)
+    for k in a:
+        assert a[k].tobytes() == b[k].tobytes(), k
+    ref = oracle_lib.flash(mix, p, t, z, threads=8)
+    parity.assert_flash_parity(parity.flash_report(b, ref, mix, p, t, z))
