@@ -876,6 +876,8 @@ def main() -> None:
     ap.add_argument("--no-ad", action="store_true")
     ap.add_argument("--sensitivity-lanes", action="store_true",
                     help="take the sensitivities with the opt-in lane-group kernel (MPMC_FLAG_SENSITIVITY_LANES)")
+    ap.add_argument("--polish-stream", action="store_true",
+                    help="run the opt-in state-machine FP64 polish (MPMC_FLAG_POLISH_STREAM)")
     ap.add_argument("--plain-sample", type=int, default=65536)
     ap.add_argument("--batched-sample", type=int, default=131072)
     ap.add_argument("--warm-fraction", type=float, default=0.75,
@@ -915,6 +917,8 @@ def main() -> None:
                 "l2_flush": "inputs+outputs larger than L2", "parallelism": f"replicas{world}"}
     if args.sensitivity_lanes:
         workload["sensitivity_kernel"] = "lane groups (MPMC_FLAG_SENSITIVITY_LANES)"
+    if args.polish_stream:
+        workload["polish_kernel"] = "state machine (MPMC_FLAG_POLISH_STREAM)"
 
     if args.impl == "reference":
         # the reference's CPU flash (C++ restatement; the reference sources are
@@ -969,8 +973,9 @@ def main() -> None:
     n, ncell = args.n, args.cells
     # the timed handle replays its launch sequence as a CUDA graph (same cells
     # and buffers every step)
-    lanes = bool(args.sensitivity_lanes)
-    g = flash.GpuFlash(mix, args.form, sensitivity=sens, device=device, graphs=True, sensitivity_lanes=lanes)
+    lanes, pstream = bool(args.sensitivity_lanes), bool(args.polish_stream)
+    g = flash.GpuFlash(mix, args.form, sensitivity=sens, device=device, graphs=True, sensitivity_lanes=lanes,
+                       polish_stream=pstream)
     tuning = None
     if args.form == "mixed" and args.launch_shape:
         tuning = {"shape": [int(v) for v in args.launch_shape.split(",")]}
@@ -1045,7 +1050,7 @@ def main() -> None:
 
     # per-stage device times and work totals (separate instrumented call) for the roofline
     gt = flash.GpuFlash(mix, args.form, sensitivity=sens, device=device, stage_timing=True,
-                        sensitivity_lanes=lanes)
+                        sensitivity_lanes=lanes, polish_stream=pstream)
     if tuning is not None:
         gt.set_launch_shape(tuning["shape"])
     gt.solve_device(ncell, dp.data_ptr(), dt.data_ptr(), dz.data_ptr(), ptrs, stream.cuda_stream)

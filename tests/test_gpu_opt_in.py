@@ -1,4 +1,4 @@
-"""GPU checks of the two opt-in paths, run with MPMC_TEST_OPT_IN=1:
+"""GPU checks of the opt-in paths, run with MPMC_TEST_OPT_IN=1:
 
 * MPMC_FLAG_SENSITIVITY_LANES, the lane-group sensitivity kernel
   (pr76_sensw.cuh): the same statuses and flash fields as the per-thread
@@ -6,12 +6,14 @@
   tests/test_gpu_sensitivity.py;
 * MPMC_FLAG_MAX3_NEWTON_ROOTS, bracketed-Newton roots in the max-3-phase
   continuation: the recorded statuses of tests/test_gpu_max3.py, and
-  three-phase sets within 1e-9 of the recorded ones.
+  three-phase sets within 1e-9 of the recorded ones;
+* MPMC_FLAG_POLISH_STREAM, the state-machine FP64 polish: the default
+  polish's statuses and the oracle's parity bar.
 
-Both paths are checked on the CPU (tests/test_sensitivity_lanes.py,
-tests/test_continuation_hints.py, tests/test_max3_warp_emulation.py); these
-tests are their first GPU runs, kept out of the default suite until a GPU
-has run them.
+All three are checked on the CPU (tests/test_sensitivity_lanes.py,
+tests/test_continuation_hints.py, tests/test_max3_warp_emulation.py,
+tests/test_batched_emulation.py); these tests are their first GPU runs, kept
+out of the default suite until a GPU has run them.
 """
 
 import os
@@ -80,3 +82,20 @@ def test_max3_newton_roots_keep_the_recorded_statuses(gpu_lib, form):
     assert three.sum() > 100
     for f_gpu, f_ref in (("phase_fraction", "ref_beta3"), ("composition", "ref_x3"), ("z_factor", "ref_z3")):
         assert np.abs(out3[f_gpu][:, three] - d[f_ref][:, three]).max() <= 1e-9, f_gpu
+
+
+@pytest.mark.parametrize("n,ncell,seed", [(3, 2048, 5), (6, 2048, 1), (10, 2048, 2)])
+def test_state_machine_polish_matches_the_default_and_the_oracle(gpu_lib, oracle_lib, n, ncell, seed):
+    """MPMC_FLAG_POLISH_STREAM: the same statuses as the default polish, and
+    the parity bar of tests/test_gpu_parity.py against the oracle."""
+    from tests import parity
+    mix = synth.make_mixture(n, seed)
+    p, t, z = synth.make_cells(n, ncell, seed)
+    outs = []
+    for stream in (False, True):
+        g = gpu_lib.GpuFlash(mix, form="mixed", polish_stream=stream)
+        outs.append(g.solve(p, t, z))
+        g.close()
+    assert np.array_equal(outs[0]["status"], outs[1]["status"])
+    ref = oracle_lib.flash(mix, p, t, z, threads=8)
+    parity.assert_flash_parity(parity.flash_report(outs[1], ref, mix, p, t, z))
