@@ -34,14 +34,16 @@ void prepare(int n, const double* tc, const double* pc, const double* omega, con
 // work-queue form (1), from ln K warm starts [n ncell] when warm_lnk is not
 // null (a non-finite entry makes its cell cold), as
 // mpmc_gpu_flash_solve_device_warm runs it; outputs as mpmc_flash_outputs'
-// flash fields; polish_stream selects the state-machine polish.  Returns
+// flash fields; polish_stream selects the state-machine polish; stats
+// (optional) receives the batch's counter slots (batched::Slot).  Returns
 // 0, a CUDA error code of the orchestration, or -1 when the emulated lanes
 // diverged at an intrinsic.
 extern "C" int host_batched_solve(int n, const double* tc, const double* pc, const double* omega, const double* kij,
                                   int64_t ncell, const double* p, const double* t, const double* z,
                                   const double* warm_lnk, int fp64_items, int polish_stream,
                                   int32_t* status, double* beta, double* x, double* y, double* lnk, double* lnphi_l,
-                                  double* lnphi_v, double* z_l, double* z_v, int32_t* counters) {
+                                  double* lnphi_v, double* z_l, double* z_v, int32_t* counters,
+                                  int32_t* stats) {
     pr76::Mixture m;
     prepare(n, tc, pc, omega, kij, m);
     pr76::DeviceOutputs out{};
@@ -67,5 +69,7 @@ extern "C" int host_batched_solve(int n, const double* tc, const double* pc, con
     const cudaError_t e = MPMC_CAT(pr76::launch_batched_nm, MPMC_NM)(&m, n, ncell, p, t, z, out, base, bytes, shape,
                                                                       nullptr);
     if (cuda_emu::g_failed.load()) return -1;
+    // the batch's queue and statistics slots (the workspace starts with them)
+    if (stats) std::memcpy(stats, base, sizeof(int32_t) * pr76::batched::qSlots);
     return static_cast<int>(e);
 }

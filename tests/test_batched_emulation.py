@@ -72,7 +72,10 @@ def _capacity(n):
     return next(c for c in CAPACITIES if n <= c)
 
 
-def solve(libs, mix, p, t, z, fp64=False, warm=None, polish_stream=False):
+STATS = 48  # batched::qSlots
+
+
+def solve(libs, mix, p, t, z, fp64=False, warm=None, polish_stream=False, stats=None):
     n = mix.n
     lib = libs[_capacity(n)]
     tc, pc, om, kij = (np.ascontiguousarray(a, dtype=np.float64) for a in mix.as_tuple())
@@ -90,7 +93,8 @@ def solve(libs, mix, p, t, z, fp64=False, warm=None, polish_stream=False):
                                 ctypes.c_int(int(polish_stream)),
                                 *[ctypes.c_void_p(o[k].ctypes.data) for k in
                                   ("status", "vapor_fraction", "liquid", "vapor", "ln_k", "ln_phi_liquid",
-                                   "ln_phi_vapor", "z_liquid", "z_vapor", "counters")])
+                                   "ln_phi_vapor", "z_liquid", "z_vapor", "counters")],
+                                ctypes.c_void_p(stats.ctypes.data if stats is not None else None))
     assert rc != -1, "emulated lanes diverged at an intrinsic"
     assert rc == 0, f"orchestration error {rc}"
     return o
@@ -152,3 +156,22 @@ def test_state_machine_polish_equals_the_default(pipeline, oracle_lib, n, ncell,
         assert a[k].tobytes() == b[k].tobytes(), k
     ref = oracle_lib.flash(mix, p, t, z, threads=8)
     parity.assert_flash_parity(parity.flash_report(b, ref, mix, p, t, z))
+
+
+def test_exact_sub_solve_matches_the_oracle(pipeline, oracle_lib):
+    """Hard cells (N = 10 at 10-12 MPa and 365-375 K) on which FP32 cannot
+    screen one cell: it is marked for the exact sub-solve (the FP64
+    work-queue form on that cell alone, gathered and scattered back), and
+    every status and value still meets the parity bar."""
+    n, seed, ncell = 10, 7, 128
+    rng = np.random.default_rng(1000 + seed)
+    mix = synth.make_mixture(n, seed)
+    p = rng.uniform(10e6, 12e6, ncell)
+    t = rng.uniform(365.0, 375.0, ncell)
+    z = rng.exponential(size=(n, ncell))
+    z /= z.sum(axis=0)
+    stats = np.zeros(STATS, np.int32)
+    out = solve(pipeline, mix, p, t, z, stats=stats)
+    assert stats[46] >= 1  # batched::sExactCells
+    ref = oracle_lib.flash(mix, p, t, z, threads=8)
+    parity.assert_flash_parity(parity.flash_report(out, ref, mix, p, t, z))
