@@ -175,3 +175,39 @@ def test_exact_sub_solve_matches_the_oracle(pipeline, oracle_lib):
     assert stats[46] >= 1  # batched::sExactCells
     ref = oracle_lib.flash(mix, p, t, z, threads=8)
     parity.assert_flash_parity(parity.flash_report(out, ref, mix, p, t, z))
+
+
+def _near_boundary_cells(oracle_lib, mix, ncell, seed):
+    """Cells placed within 2 % of a pressure where the oracle's phase count
+    changes (bisection in ln p on [0.5, 40] MPa), as the bench places 30 % of
+    its cells; cells with no change in range are dropped."""
+    n = mix.n
+    p, t, z = synth.make_cells(n, 4 * ncell, seed)
+    lo, hi = np.full(p.shape, np.log(0.5e6)), np.full(p.shape, np.log(40e6))
+    s_lo = oracle_lib.flash(mix, np.exp(lo), t, z, threads=8)["status"]
+    s_hi = oracle_lib.flash(mix, np.exp(hi), t, z, threads=8)["status"]
+    keep = s_lo != s_hi
+    lo, hi, t, z, s_lo = lo[keep], hi[keep], t[keep], z[:, keep], s_lo[keep]
+    for _ in range(30):
+        mid = 0.5 * (lo + hi)
+        s_mid = oracle_lib.flash(mix, np.exp(mid), t, z, threads=8)["status"]
+        same = s_mid == s_lo
+        lo = np.where(same, mid, lo)
+        hi = np.where(same, hi, mid)
+    rng = np.random.default_rng(seed)
+    pb = np.exp(0.5 * (lo + hi)) * (1.0 + rng.uniform(-0.02, 0.02, lo.shape))
+    return pb[:ncell], t[:ncell], np.ascontiguousarray(z[:, :ncell])
+
+
+@pytest.mark.parametrize("n,ncell,seed", [(4, 256, 21), (10, 128, 22)])
+def test_mixed_form_near_the_phase_boundary(pipeline, oracle_lib, n, ncell, seed):
+    """The bench's hard regime: every cell within 2 % of its own phase-count
+    change pressure."""
+    mix = synth.make_mixture(n, seed)
+    p, t, z = _near_boundary_cells(oracle_lib, mix, ncell, seed)
+    assert p.size >= ncell // 2
+    out = solve(pipeline, mix, p, t, z)
+    ref = oracle_lib.flash(mix, p, t, z, threads=8)
+    rep = parity.flash_report(out, ref, mix, p, t, z)
+    parity.assert_flash_parity(rep)
+    assert rep["two_phase"] > 0
